@@ -1,0 +1,103 @@
+"""Build libark_gb300.so (and the ark_run driver) for sm_103a with nvcc, in-tree.
+
+    python ark-cpp-mpi_gb300/ark_build.py            # build if sources changed
+    python ark-cpp-mpi_gb300/ark_build.py --force    # rebuild
+
+Translation units are compiled in parallel:
+  ark_fp64.cu  FP64 kernels, --fmad=false (bit parity with the reference's FP64 rounding)
+  ark_fp32.cu  FP32 kernels, FMA contraction on
+  ark_api.cu   C ABI, context, CUDA-graph step
+  ark_host.cpp host-only helpers (seeded channel init)
+Outputs go to ark-cpp-mpi_gb300/lib/ (git-ignored).
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "lib")
+OBJ = os.path.join(OUT, "obj")
+LIB = os.path.join(OUT, "libark_gb300.so")
+RUN = os.path.join(OUT, "ark_run")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.isfile(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _digest(extra=()):
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(SRC)) + [os.path.join("..", "..", "include", "ark_gpu.h")]:
+        p = os.path.join(SRC, name)
+        if os.path.isfile(p):
+            h.update(name.encode())
+            with open(p, "rb") as f:
+                h.update(f.read())
+    with open(__file__, "rb") as f:
+        h.update(f.read())
+    for e in extra:
+        h.update(str(e).encode())
+    return h.hexdigest()
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OBJ, exist_ok=True)
+    stamp = os.path.join(OUT, ".stamp")
+    dig = _digest()
+    if not force and os.path.isfile(LIB) and os.path.isfile(RUN) and os.path.isfile(stamp):
+        with open(stamp) as f:
+            if f.read().strip() == dig:
+                return LIB
+    nv = nvcc()
+    common = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+    jobs = [
+        [nv] + common + ["--fmad=false", "-c", os.path.join(SRC, "ark_fp64.cu"), "-o", os.path.join(OBJ, "ark_fp64.o")],
+        [nv] + common + ["--fmad=true", "-c", os.path.join(SRC, "ark_fp32.cu"), "-o", os.path.join(OBJ, "ark_fp32.o")],
+        [nv] + common + ["-c", os.path.join(SRC, "ark_api.cu"), "-o", os.path.join(OBJ, "ark_api.o")],
+        ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-c",
+         os.path.join(SRC, "ark_host.cpp"), "-o", os.path.join(OBJ, "ark_host.o")],
+        ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-c",
+         os.path.join(SRC, "ark_run.cpp"), "-o", os.path.join(OBJ, "ark_run.o")],
+    ]
+    procs = []
+    for cmd in jobs:
+        if verbose:
+            print(" ".join(cmd))
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    failed = []
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            failed.append((cmd, out.decode(errors="replace")))
+        elif verbose and out:
+            print(out.decode(errors="replace"))
+    if failed:
+        msg = "\n".join(" ".join(c) + "\n" + o for c, o in failed)
+        raise RuntimeError("build failed:\n" + msg)
+    objs = [os.path.join(OBJ, n) for n in ("ark_fp64.o", "ark_fp32.o", "ark_api.o", "ark_host.o")]
+    subprocess.run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static"], check=True)
+    subprocess.run(["g++", "-o", RUN, os.path.join(OBJ, "ark_run.o"), "-L", OUT, "-lark_gb300",
+                    "-Wl,-rpath,$ORIGIN"], check=True)
+    with open(stamp, "w") as f:
+        f.write(dig)
+    return LIB
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("-v", "--verbose", action="store_true")
+    a = ap.parse_args()
+    print(build(force=a.force, verbose=a.verbose))
+    sys.exit(0)

@@ -1,0 +1,307 @@
+"""ctypes binding of libark_gb300.so (include/ark_gpu.h) for Python callers and tests.
+
+This is a thin mirror of the C ABI: every method is one C call and raises ArkError on a
+non-zero status.  There is no CPU fallback: if the shared library is missing, loading
+raises.  Host arrays are numpy float64 arrays in the reference's Arr3d layout
+(C-order shape (C3+2, C2+2, C1+2) for cells, (C3+3, C2+3, C1+3) for faces).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libark_gb300.so")
+
+FP64, FP32 = 0, 1
+
+CELL_FIELDS = ("roCon", "u1Con", "u2Con", "u3Con", "ronCon", "u1nCon", "u2nCon", "u3nCon", "condition")
+FACE_FIELDS = ("p1", "ro1", "u11", "u21", "u31", "p2", "ro2", "u12", "u22", "u32",
+               "p3", "ro3", "u13", "u23", "u33")
+STATE_FIELDS = CELL_FIELDS + FACE_FIELDS
+
+# Every symbol include/ark_gpu.h declares.
+EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "ark_cell_count",
+           "ark_face_count", "ark_upload", "ark_download", "ark_get_array", "ark_put_array",
+           "ark_time_step_size", "ark_phase1", "ark_stress_tensor", "ark_use_forces", "ark_phase2",
+           "ark_boundary_fill", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
+           "ark_get_scalars", "ark_set_scalars", "ark_conservation_sums", "ark_channel_init",
+           "ark_kernel_times", "ark_kernel_name", "ark_alloc_host_state", "ark_free_host_state")
+
+
+class ArkError(RuntimeError):
+    def __init__(self, fn, status, text):
+        super().__init__(f"{fn} -> {status}: {text}")
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("n1_cells", ctypes.c_int), ("n2_cells", ctypes.c_int), ("n3_cells", ctypes.c_int),
+                ("lx", ctypes.c_double), ("ly", ctypes.c_double), ("lz", ctypes.c_double),
+                ("vis", ctypes.c_double), ("sound", ctypes.c_double), ("ro0", ctypes.c_double),
+                ("cfl", ctypes.c_double), ("periodic_x", ctypes.c_int), ("periodic_z", ctypes.c_int),
+                ("precision", ctypes.c_int), ("forcing", ctypes.c_int), ("u_target", ctypes.c_double),
+                ("keep_stress", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+class HostState(ctypes.Structure):
+    _fields_ = [(n, _DP) for n in STATE_FIELDS]
+
+
+class Scalars(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("time", ctypes.c_double), ("nstep", ctypes.c_longlong),
+                ("bulk_velocity", ctypes.c_double), ("bulk_force", ctypes.c_double)]
+
+
+class Sums(ctypes.Structure):
+    _fields_ = [("mass", ctypes.c_double), ("momentum1", ctypes.c_double), ("momentum2", ctypes.c_double),
+                ("momentum3", ctypes.c_double), ("kinetic", ctypes.c_double), ("cells", ctypes.c_longlong)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libark_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} missing: run ark-cpp-mpi_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)
+        L.ark_create.restype = vp
+        L.ark_create.argtypes = [ctypes.POINTER(Params), ip]
+        L.ark_destroy.argtypes = [vp]
+        L.ark_last_error.restype = ctypes.c_char_p
+        L.ark_status_string.restype = ctypes.c_char_p
+        L.ark_status_string.argtypes = [ctypes.c_int]
+        L.ark_cell_count.restype = ctypes.c_size_t
+        L.ark_cell_count.argtypes = [ctypes.POINTER(Params)]
+        L.ark_face_count.restype = ctypes.c_size_t
+        L.ark_face_count.argtypes = [ctypes.POINTER(Params)]
+        L.ark_upload.argtypes = [vp, ctypes.POINTER(HostState)]
+        L.ark_download.argtypes = [vp, ctypes.POINTER(HostState)]
+        L.ark_get_array.argtypes = [vp, ctypes.c_char_p, _DP]
+        L.ark_put_array.argtypes = [vp, ctypes.c_char_p, _DP]
+        for fn in ("ark_time_step_size", "ark_phase1", "ark_stress_tensor", "ark_use_forces", "ark_phase2",
+                   "ark_sync"):
+            getattr(L, fn).argtypes = [vp]
+        L.ark_boundary_fill.argtypes = [vp, ctypes.c_int]
+        L.ark_set_dt.argtypes = [vp, ctypes.c_double]
+        L.ark_step.argtypes = [vp, ctypes.c_int]
+        L.ark_time_steps.argtypes = [vp, ctypes.c_int, _DP]
+        L.ark_get_scalars.argtypes = [vp, ctypes.POINTER(Scalars)]
+        L.ark_set_scalars.argtypes = [vp, ctypes.POINTER(Scalars)]
+        L.ark_conservation_sums.argtypes = [vp, ctypes.POINTER(Sums)]
+        L.ark_channel_init.argtypes = [ctypes.POINTER(Params), ctypes.c_uint64, ctypes.c_double,
+                                       ctypes.POINTER(HostState)]
+        L.ark_kernel_times.argtypes = [vp, ctypes.c_int, _DP, ctypes.c_int, ip]
+        L.ark_kernel_name.restype = ctypes.c_char_p
+        L.ark_kernel_name.argtypes = [ctypes.c_int]
+        L.ark_alloc_host_state.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(HostState)]
+        L.ark_free_host_state.argtypes = [ctypes.POINTER(HostState)]
+        _lib = L
+    return _lib
+
+
+def make_params(C1, C2, C3, re_b=2800.0, sound=10.0, rho0=1.0, cfl=0.2, lx=2 * math.pi, ly=2.0,
+                lz=math.pi, ub=1.0, precision=FP64, forcing=True, keep_stress=False, device=0, vis=None):
+    p = Params()
+    p.n1_cells, p.n2_cells, p.n3_cells = C1, C2, C3
+    p.lx, p.ly, p.lz = lx, ly, lz
+    p.vis = (1.0 / re_b) if vis is None else vis
+    p.sound, p.ro0, p.cfl = sound, rho0, cfl
+    p.periodic_x = p.periodic_z = 1
+    p.precision = precision
+    p.forcing = int(bool(forcing))
+    p.u_target = ub
+    p.keep_stress = int(bool(keep_stress))
+    p.device = device
+    return p
+
+
+def shapes(p: Params):
+    return (p.n3_cells + 2, p.n2_cells + 2, p.n1_cells + 2), (p.n3_cells + 3, p.n2_cells + 3, p.n1_cells + 3)
+
+
+def empty_state(p: Params, alloc=np.empty) -> dict:
+    cs, fs = shapes(p)
+    st = {n: alloc(cs) for n in CELL_FIELDS}
+    st.update({n: alloc(fs) for n in FACE_FIELDS})
+    return st
+
+
+def host_struct(st: dict) -> HostState:
+    h = HostState()
+    for n in STATE_FIELDS:
+        a = st.get(n)
+        if a is not None:
+            assert a.dtype == np.float64 and a.flags.c_contiguous, n
+            setattr(h, n, a.ctypes.data_as(_DP))
+    return h
+
+
+def _check(fn, rc):
+    if rc != 0:
+        raise ArkError(fn, rc, lib().ark_last_error().decode(errors="replace"))
+
+
+def channel_init(p: Params, seed=12345, amp=0.1) -> dict:
+    st = empty_state(p)
+    _check("ark_channel_init", lib().ark_channel_init(ctypes.byref(p), seed, amp, ctypes.byref(host_struct(st))))
+    return st
+
+
+class PinnedState:
+    """A host state whose arrays live in page-locked memory (ark_alloc_host_state)."""
+
+    def __init__(self, p: Params):
+        self.h = HostState()
+        _check("ark_alloc_host_state", lib().ark_alloc_host_state(ctypes.byref(p), ctypes.byref(self.h)))
+        cs, fs = shapes(p)
+        self.arrays = {}
+        for n in STATE_FIELDS:
+            shape = cs if n in CELL_FIELDS else fs
+            ptr = getattr(self.h, n)
+            self.arrays[n] = np.ctypeslib.as_array(ptr, shape=shape)
+
+    def fill(self, st: dict):
+        for n, a in st.items():
+            self.arrays[n][...] = a
+
+    def struct(self, with_condition=True) -> HostState:
+        h = HostState()
+        for n in STATE_FIELDS:
+            if n == "condition" and not with_condition:
+                continue
+            setattr(h, n, getattr(self.h, n))
+        return h
+
+    def nbytes(self, with_condition=True):
+        return sum(a.nbytes for n, a in self.arrays.items() if with_condition or n != "condition")
+
+    def close(self):
+        if getattr(self, "h", None) is not None:
+            self.arrays = {}
+            lib().ark_free_host_state(ctypes.byref(self.h))
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Context:
+    """One ark_ctx (one CUDA stream on one device)."""
+
+    def __init__(self, p: Params):
+        self.p = p
+        rc = ctypes.c_int(0)
+        self.h = lib().ark_create(ctypes.byref(p), ctypes.byref(rc))
+        if not self.h:
+            _check("ark_create", rc.value or 2)
+        self.cshape, self.fshape = shapes(p)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ark_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _call(self, fn, *args):
+        _check(fn, getattr(lib(), fn)(self.h, *args))
+
+    def upload(self, st: dict):
+        self._call("ark_upload", ctypes.byref(host_struct(st)))
+
+    def download(self, names=STATE_FIELDS) -> dict:
+        st = {}
+        for n in names:
+            st[n] = np.empty(self.cshape if n in CELL_FIELDS else self.fshape)
+        self._call("ark_download", ctypes.byref(host_struct(st)))
+        return st
+
+    def download_into(self, st: dict):
+        self._call("ark_download", ctypes.byref(host_struct(st)))
+
+    def get(self, name, face=None):
+        if face is None:
+            face = not (name in CELL_FIELDS or name in ("f1", "f2", "f3"))
+        out = np.empty(self.fshape if face else self.cshape)
+        self._call("ark_get_array", name.encode(), out.ctypes.data_as(_DP))
+        return out
+
+    def put(self, name, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self._call("ark_put_array", name.encode(), a.ctypes.data_as(_DP))
+
+    def time_step_size(self):
+        self._call("ark_time_step_size")
+
+    def phase1(self):
+        self._call("ark_phase1")
+
+    def stress_tensor(self):
+        self._call("ark_stress_tensor")
+
+    def use_forces(self):
+        self._call("ark_use_forces")
+
+    def phase2(self):
+        self._call("ark_phase2")
+
+    def boundary_fill(self, axis):
+        self._call("ark_boundary_fill", int(axis))
+
+    def set_dt(self, dt):
+        self._call("ark_set_dt", float(dt))
+
+    def step(self, n=1):
+        self._call("ark_step", int(n))
+
+    def sync(self):
+        self._call("ark_sync")
+
+    def time_steps(self, n):
+        ms = ctypes.c_double(0.0)
+        self._call("ark_time_steps", int(n), ctypes.byref(ms))
+        return ms.value
+
+    def kernel_times(self, nsteps):
+        """Mean device ms of each launch of the fused step: list of (name, ms)."""
+        ms = (ctypes.c_double * 32)()
+        cnt = ctypes.c_int(0)
+        self._call("ark_kernel_times", int(nsteps), ms, 32, ctypes.byref(cnt))
+        return [(lib().ark_kernel_name(q).decode(), ms[q]) for q in range(cnt.value)]
+
+    def upload_struct(self, h: HostState):
+        self._call("ark_upload", ctypes.byref(h))
+
+    def download_struct(self, h: HostState):
+        self._call("ark_download", ctypes.byref(h))
+
+    def scalars(self) -> Scalars:
+        s = Scalars()
+        self._call("ark_get_scalars", ctypes.byref(s))
+        return s
+
+    def set_scalars(self, s: Scalars):
+        self._call("ark_set_scalars", ctypes.byref(s))
+
+    def sums(self) -> Sums:
+        s = Sums()
+        self._call("ark_conservation_sums", ctypes.byref(s))
+        return s

@@ -1,0 +1,731 @@
+// C ABI of the GB300 CABARET step (include/ark_gpu.h): context, state transfer, the
+// reference's step pieces and the fused, graph-captured time step.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ark_gpu.h"
+#include "ark_state.h"
+
+using namespace ark;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string &msg) {
+    g_last_error = msg;
+    return status;
+}
+
+#define ARK_CUDA(call)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(e_ == cudaErrorMemoryAllocation ? ARK_ERR_NOMEM : ARK_ERR_CUDA,           \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+    } while (0)
+
+// Field names of the host state, in struct order, and whether each is a face array.
+struct FieldRef {
+    const char *name;
+    double *ark_host_state::*member;
+    int face;
+};
+const FieldRef kFields[] = {
+    {"roCon", &ark_host_state::roCon, 0},   {"u1Con", &ark_host_state::u1Con, 0},
+    {"u2Con", &ark_host_state::u2Con, 0},   {"u3Con", &ark_host_state::u3Con, 0},
+    {"ronCon", &ark_host_state::ronCon, 0}, {"u1nCon", &ark_host_state::u1nCon, 0},
+    {"u2nCon", &ark_host_state::u2nCon, 0}, {"u3nCon", &ark_host_state::u3nCon, 0},
+    {"condition", &ark_host_state::condition, 0},
+    {"p1", &ark_host_state::p1, 1},  {"ro1", &ark_host_state::ro1, 1}, {"u11", &ark_host_state::u11, 1},
+    {"u21", &ark_host_state::u21, 1}, {"u31", &ark_host_state::u31, 1},
+    {"p2", &ark_host_state::p2, 1},  {"ro2", &ark_host_state::ro2, 1}, {"u12", &ark_host_state::u12, 1},
+    {"u22", &ark_host_state::u22, 1}, {"u32", &ark_host_state::u32, 1},
+    {"p3", &ark_host_state::p3, 1},  {"ro3", &ark_host_state::ro3, 1}, {"u13", &ark_host_state::u13, 1},
+    {"u23", &ark_host_state::u23, 1}, {"u33", &ark_host_state::u33, 1},
+};
+
+Geom make_geom(const ark_params &p) {
+    Geom g;
+    g.C1 = p.n1_cells;
+    g.C2 = p.n2_cells;
+    g.C3 = p.n3_cells;
+    g.cs1 = g.C1 + 2;
+    g.cs2 = (int64_t)(g.C1 + 2) * (g.C2 + 2);
+    g.fs1 = g.C1 + 3;
+    g.fs2 = (int64_t)(g.C1 + 3) * (g.C2 + 3);
+    return g;
+}
+
+// Run constants, evaluated exactly as the reference evaluates them: grid steps as
+// InitializeData forms them (main.cpp:284-290, domain [0,lx] x [-ly/2,ly/2] x [0,lz]),
+// areas and volume as Phase1 (main.cpp:456-462), dt numerators as TimeStepSize.
+Consts make_consts(const ark_params &p) {
+    Consts k;
+    k.dx[0] = (p.lx - 0.) / (double)p.n1_cells;
+    k.dx[1] = (0.5 * p.ly - -0.5 * p.ly) / (double)p.n2_cells;
+    k.dx[2] = (p.lz - 0.) / (double)p.n3_cells;
+    for (int d = 0; d < 3; ++d) {
+        k.rdx[d] = 1.0 / k.dx[d];
+        k.cfl_dx[d] = p.cfl * k.dx[d];
+    }
+    k.ds[0] = k.dx[1] * k.dx[2];
+    k.ds[1] = k.dx[0] * k.dx[2];
+    k.ds[2] = k.dx[0] * k.dx[1];
+    k.dvc = k.dx[0] * k.dx[1] * k.dx[2];
+    k.vis = p.vis;
+    k.two_vis = 2 * p.vis;
+    k.sound = p.sound;
+    k.ro0 = p.ro0;
+    k.c2 = p.sound * p.sound;
+    k.rc2 = 1.0 / k.c2;
+    k.roc = p.ro0 * p.sound;
+    k.rroc = 1.0 / k.roc;
+    if (p.vis > 1e-16) {
+        const double dtv1 = p.cfl * k.dx[0] * k.dx[0] / (2. * p.vis);
+        const double dtv2 = p.cfl * k.dx[1] * k.dx[1] / (2. * p.vis);
+        const double dtv3 = p.cfl * k.dx[2] * k.dx[2] / (2. * p.vis);
+        double m = dtv1 > dtv2 ? dtv2 : dtv1;
+        k.dtv = m > dtv3 ? dtv3 : m;
+    } else {
+        k.dtv = 1e16;
+    }
+    k.u_target = p.u_target;
+    k.forcing = p.forcing;
+    return k;
+}
+
+// The launches of one fused step, in order (ark_kernel_times reports them in this order).
+const char *const kStepKernels[] = {"reduce_start", "finalize_dt", "wrap_con",    "phase1_stress_forces",
+                                    "wrap_phase2",  "sweep_x1",    "sweep_x2",    "sweep_x3",
+                                    "phase1_forces"};
+constexpr int kNumStepKernels = 9;
+
+// Precision-independent engine interface.
+struct Engine {
+    virtual ~Engine() {}
+    virtual int alloc() = 0;
+    virtual int upload_field(int which, int face, const double *host) = 0;
+    virtual int download_field(int which, int face, double *host) = 0;
+    virtual void *field_ptr(const char *name, int *face) = 0;
+    virtual void time_step_size(int con, int advance) = 0;
+    virtual void phase1(int src, int dst, int mode) = 0;
+    virtual void stress(int con, int bulk) = 0;
+    virtual void use_forces(int ncon) = 0;
+    virtual void phase2(int con) = 0;
+    virtual void step(int con, cudaEvent_t *ev) = 0;
+    virtual void boundary_fill(int ncon, int axis, int periodic) = 0;
+    virtual void sums(int ncon) = 0;
+    virtual DevScalars *scalars() = 0;
+    virtual uint8_t *flags() = 0;
+};
+
+} // namespace
+
+struct ark_ctx {
+    ark_params P;
+    Geom g;
+    Consts k;
+    cudaStream_t st = nullptr;
+    std::unique_ptr<Engine> eng;
+    std::vector<double> cond_host;
+    int con = 0; // the level index holding "Con"
+    bool uploaded = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double *stage = nullptr; // device double staging for FP32 contexts
+};
+
+namespace {
+
+template <class T> struct EngineT : Engine {
+    ark_ctx *ctx;
+    DevState<T> S;
+    std::vector<void *> allocs;
+
+    explicit EngineT(ark_ctx *c) : ctx(c) { std::memset(&S, 0, sizeof(S)); }
+    ~EngineT() override {
+        for (void *p : allocs) cudaFree(p);
+    }
+
+    template <class U> int get(U **out, size_t n) {
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(U));
+        if (e != cudaSuccess) return fail(ARK_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(p);
+        cudaMemset(p, 0, n * sizeof(U));
+        *out = (U *)p;
+        return ARK_OK;
+    }
+
+    int alloc() override {
+        S.g = ctx->g;
+        S.k = ctx->k;
+        const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
+        int rc = 0;
+        for (int l = 0; l < 2; ++l) {
+            rc |= get(&S.lv[l].ro, nc);
+            rc |= get(&S.lv[l].u1, nc);
+            rc |= get(&S.lv[l].u2, nc);
+            rc |= get(&S.lv[l].u3, nc);
+        }
+        for (int m = 0; m < 3; ++m) rc |= get(&S.f[m], nc);
+        for (int d = 0; d < 3; ++d) {
+            rc |= get(&S.fc[d].p, nf);
+            rc |= get(&S.fc[d].ro, nf);
+            for (int m = 0; m < 3; ++m) rc |= get(&S.fc[d].u[m], nf);
+            for (int m = 0; m < 3; ++m) {
+                if (ctx->P.keep_stress) rc |= get(&S.sig[d][m], nf);
+                else S.sig[d][m] = nullptr;
+            }
+        }
+        rc |= get(&S.flags, nc);
+        rc |= get(&S.sc, 1);
+        if (rc) return ARK_ERR_NOMEM;
+        return ARK_OK;
+    }
+
+    // which: index into kFields (0..23), levels resolved through ctx->con
+    T *dev_of(int which) {
+        const int con = ctx->con, ncon = con ^ 1;
+        switch (which) {
+        case 0: return S.lv[con].ro;
+        case 1: return S.lv[con].u1;
+        case 2: return S.lv[con].u2;
+        case 3: return S.lv[con].u3;
+        case 4: return S.lv[ncon].ro;
+        case 5: return S.lv[ncon].u1;
+        case 6: return S.lv[ncon].u2;
+        case 7: return S.lv[ncon].u3;
+        default: break;
+        }
+        if (which >= 9 && which < 24) {
+            const int d = (which - 9) / 5, v = (which - 9) % 5;
+            FaceSet<T> &F = S.fc[d];
+            return v == 0 ? F.p : v == 1 ? F.ro : F.u[v - 2];
+        }
+        return nullptr;
+    }
+
+    int copy_in(T *dev, const double *host, size_t n) {
+        if (sizeof(T) == sizeof(double)) {
+            ARK_CUDA(cudaMemcpy(dev, host, n * sizeof(double), cudaMemcpyHostToDevice));
+        } else {
+            ARK_CUDA(cudaMemcpy(ctx->stage, host, n * sizeof(double), cudaMemcpyHostToDevice));
+            convert_from_double<T>(dev, ctx->stage, (int64_t)n, ctx->st);
+            ARK_CUDA(cudaStreamSynchronize(ctx->st));
+        }
+        return ARK_OK;
+    }
+
+    int copy_out(double *host, const T *dev, size_t n) {
+        if (sizeof(T) == sizeof(double)) {
+            ARK_CUDA(cudaMemcpy(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost));
+        } else {
+            convert_to_double<T>(ctx->stage, dev, (int64_t)n, ctx->st);
+            ARK_CUDA(cudaStreamSynchronize(ctx->st));
+            ARK_CUDA(cudaMemcpy(host, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+        return ARK_OK;
+    }
+
+    int upload_field(int which, int face, const double *host) override {
+        const size_t n = face ? (size_t)S.g.nface() : (size_t)S.g.ncell();
+        return copy_in(dev_of(which), host, n);
+    }
+    int download_field(int which, int face, double *host) override {
+        const size_t n = face ? (size_t)S.g.nface() : (size_t)S.g.ncell();
+        return copy_out(host, dev_of(which), n);
+    }
+
+    void *field_ptr(const char *name, int *face) override {
+        for (int w = 0; w < 24; ++w)
+            if (w != 8 && std::strcmp(name, kFields[w].name) == 0) {
+                *face = kFields[w].face;
+                return dev_of(w);
+            }
+        if (name[0] == 'f' && name[1] >= '1' && name[1] <= '3' && name[2] == 0) {
+            *face = 0;
+            return S.f[name[1] - '1'];
+        }
+        if (std::strncmp(name, "sigm", 4) == 0 && name[4] >= '1' && name[4] <= '3' && name[5] >= '1' &&
+            name[5] <= '3' && name[6] == 0) {
+            *face = 1;
+            return S.sig[name[5] - '1'][name[4] - '1'];
+        }
+        return nullptr;
+    }
+
+    void time_step_size(int con, int advance) override {
+        Launch<T>::reduce_start(S, con, ctx->k.forcing, ctx->st);
+        Launch<T>::finalize_dt(S, advance, ctx->st);
+    }
+    void phase1(int src, int dst, int mode) override { Launch<T>::phase1(S, src, dst, mode, ctx->st); }
+    void stress(int con, int bulk) override {
+        T *u[3] = {S.lv[con].u1, S.lv[con].u2, S.lv[con].u3};
+        Launch<T>::wrap_cells(S, u, 3, ctx->st);
+        if (S.sig[0][0]) {
+            for (int d = 0; d < 3; ++d)
+                for (int m = 0; m < 3; ++m)
+                    cudaMemsetAsync(S.sig[d][m], 0, sizeof(T) * (size_t)S.g.nface(), ctx->st);
+        }
+        Launch<T>::stress(S, con, bulk, ctx->st);
+    }
+    void use_forces(int ncon) override { Launch<T>::use_forces(S, ncon, ctx->st); }
+    void phase2(int con) override {
+        Launch<T>::wrap_phase2(S, con, ctx->st);
+        for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, con, ax, ctx->st);
+    }
+    // One full step of main.cpp:82-91 with "Con" = level x at entry and exit.  With ev
+    // given, an event is recorded after each of the kStepKernels launches.
+    void step(int x, cudaEvent_t *ev) override {
+        const int y = x ^ 1;
+        cudaStream_t st = ctx->st;
+        auto mark = [&](int q) {
+            if (ev) cudaEventRecord(ev[q], st);
+        };
+        Launch<T>::reduce_start(S, x, ctx->k.forcing, st);
+        mark(0);
+        Launch<T>::finalize_dt(S, 1, st);
+        mark(1);
+        T *cells[4] = {S.lv[y].u1, S.lv[y].u2, S.lv[y].u3, S.lv[y].ro};
+        Launch<T>::wrap_cells(S, cells, 4, st);
+        mark(2);
+        Launch<T>::phase1(S, y, x, P1_STRESS | P1_FORCES | (ctx->k.forcing ? P1_BULK : 0), st);
+        mark(3);
+        Launch<T>::wrap_phase2(S, y, st);
+        mark(4);
+        for (int ax = 0; ax < 3; ++ax) {
+            Launch<T>::sweep(S, y, ax, st);
+            mark(5 + ax);
+        }
+        Launch<T>::phase1(S, x, y, P1_FORCES, st);
+        mark(8);
+    }
+    void boundary_fill(int ncon, int axis, int periodic) override {
+        Launch<T>::boundary_fill(S, ncon, axis, periodic, ctx->st);
+    }
+    void sums(int ncon) override { Launch<T>::sums(S, ncon, ctx->st); }
+    DevScalars *scalars() override { return S.sc; }
+    uint8_t *flags() override { return S.flags; }
+};
+
+int check_params(const ark_params *p) {
+    if (!p) return fail(ARK_ERR_PARAM, "params is NULL");
+    if (p->n1_cells < 2 || p->n2_cells < 1 || p->n3_cells < 2)
+        return fail(ARK_ERR_PARAM, "need at least 2 x 1 x 2 cells");
+    const double cells = (double)p->n1_cells * p->n2_cells * p->n3_cells;
+    if (cells > 2.0e9) return fail(ARK_ERR_PARAM, "grid too large");
+    if (!(p->lx > 0) || !(p->ly > 0) || !(p->lz > 0)) return fail(ARK_ERR_PARAM, "domain extents must be > 0");
+    if (!(p->sound > 0) || !(p->ro0 > 0) || !(p->cfl > 0) || !(p->vis >= 0))
+        return fail(ARK_ERR_PARAM, "sound, ro0, cfl must be > 0 and vis >= 0");
+    if (p->precision != ARK_FP64 && p->precision != ARK_FP32) return fail(ARK_ERR_PARAM, "unknown precision");
+    if (!p->periodic_x || !p->periodic_z)
+        return fail(ARK_ERR_UNSUPPORTED, "bounded x or z (inflow/outflow, zero-gradient edges) is not implemented");
+    return ARK_OK;
+}
+
+int check_ctx(ark_ctx *ctx, bool need_state) {
+    if (!ctx) return fail(ARK_ERR_PARAM, "context is NULL");
+    if (need_state && !ctx->uploaded) return fail(ARK_ERR_STATE, "no state uploaded");
+    return ARK_OK;
+}
+
+int launch_status(ark_ctx *ctx) {
+    (void)ctx;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ARK_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return ARK_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *ark_last_error(void) { return g_last_error.c_str(); }
+
+const char *ark_status_string(int s) {
+    switch (s) {
+    case ARK_OK: return "ok";
+    case ARK_ERR_PARAM: return "bad parameter";
+    case ARK_ERR_CUDA: return "CUDA error";
+    case ARK_ERR_NONFINITE: return "non-finite value in the velocity field";
+    case ARK_ERR_STATE: return "call out of order";
+    case ARK_ERR_NOMEM: return "device allocation failed";
+    case ARK_ERR_UNSUPPORTED: return "unsupported configuration";
+    default: return "unknown status";
+    }
+}
+
+size_t ark_cell_count(const ark_params *p) {
+    return p ? (size_t)(p->n1_cells + 2) * (p->n2_cells + 2) * (p->n3_cells + 2) : 0;
+}
+size_t ark_face_count(const ark_params *p) {
+    return p ? (size_t)(p->n1_cells + 3) * (p->n2_cells + 3) * (p->n3_cells + 3) : 0;
+}
+
+ark_ctx *ark_create(const ark_params *params, int *status) {
+    int dummy;
+    if (!status) status = &dummy;
+    *status = check_params(params);
+    if (*status) return nullptr;
+    if (cudaSetDevice(params->device) != cudaSuccess) {
+        *status = fail(ARK_ERR_CUDA, "cudaSetDevice failed (no usable GPU?)");
+        return nullptr;
+    }
+    std::unique_ptr<ark_ctx> ctx(new ark_ctx());
+    ctx->P = *params;
+    ctx->g = make_geom(*params);
+    ctx->k = make_consts(*params);
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+        *status = fail(ARK_ERR_CUDA, "cudaStreamCreate failed");
+        return nullptr;
+    }
+    if (params->precision == ARK_FP64) ctx->eng.reset(new EngineT<double>(ctx.get()));
+    else ctx->eng.reset(new EngineT<float>(ctx.get()));
+    *status = ctx->eng->alloc();
+    if (*status) return nullptr;
+    if (params->precision == ARK_FP32) {
+        if (cudaMalloc(&ctx->stage, sizeof(double) * (size_t)ctx->g.nface()) != cudaSuccess) {
+            *status = fail(ARK_ERR_NOMEM, "staging allocation failed");
+            return nullptr;
+        }
+    }
+    cudaEventCreate(&ctx->ev0);
+    cudaEventCreate(&ctx->ev1);
+    *status = ARK_OK;
+    return ctx.release();
+}
+
+int ark_destroy(ark_ctx *ctx) {
+    if (!ctx) return ARK_OK;
+    cudaStreamSynchronize(ctx->st);
+    for (int q = 0; q < 2; ++q)
+        if (ctx->graph[q]) cudaGraphExecDestroy(ctx->graph[q]);
+    ctx->eng.reset();
+    if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return ARK_OK;
+}
+
+int ark_upload(ark_ctx *ctx, const ark_host_state *h) {
+    if (int rc = check_ctx(ctx, false)) return rc;
+    if (!h) return fail(ARK_ERR_PARAM, "host state is NULL");
+    for (const FieldRef &f : kFields)
+        if (!(h->*f.member) && !(f.member == &ark_host_state::condition && ctx->uploaded))
+            return fail(ARK_ERR_PARAM, std::string("host array ") + f.name + " is NULL");
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ctx->con = 0;
+    for (int w = 0; w < 24; ++w) {
+        if (w == 8) continue;
+        if (int rc = ctx->eng->upload_field(w, kFields[w].face, h->*kFields[w].member)) return rc;
+    }
+    if (!h->condition) return ARK_OK; // keep the condition (and the scalars) of the last upload
+    // condition: kept on the host for download, turned into flag bits on the device
+    const size_t nc = (size_t)ctx->g.ncell();
+    ctx->cond_host.assign(h->condition, h->condition + nc);
+    std::vector<uint8_t> fl(nc);
+    long long nfluid = 0;
+    for (size_t c = 0; c < nc; ++c) {
+        const double v = h->condition[c];
+        fl[c] = (uint8_t)((v < 0.5 ? FL_LT : 0) | (v > 0.5 ? FL_GT : 0) | (v == 0 ? FL_EQ0 : 0));
+    }
+    const Geom &g = ctx->g;
+    for (int k = 1; k <= g.C3; ++k)
+        for (int j = 1; j <= g.C2; ++j)
+            for (int i = 1; i <= g.C1; ++i)
+                if (fl[(size_t)g.cell(i, j, k)] & FL_EQ0) ++nfluid;
+    ARK_CUDA(cudaMemcpy(ctx->eng->flags(), fl.data(), nc, cudaMemcpyHostToDevice));
+    DevScalars sc;
+    std::memset(&sc, 0, sizeof(sc));
+    sc.nfluid = nfluid;
+    ARK_CUDA(cudaMemcpy(ctx->eng->scalars(), &sc, sizeof(sc), cudaMemcpyHostToDevice));
+    ctx->uploaded = true;
+    return ARK_OK;
+}
+
+int ark_download(ark_ctx *ctx, ark_host_state *h) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!h) return fail(ARK_ERR_PARAM, "host state is NULL");
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    for (int w = 0; w < 24; ++w) {
+        double *dst = h->*kFields[w].member;
+        if (!dst) continue;
+        if (w == 8) {
+            std::memcpy(dst, ctx->cond_host.data(), sizeof(double) * ctx->cond_host.size());
+            continue;
+        }
+        if (int rc = ctx->eng->download_field(w, kFields[w].face, dst)) return rc;
+    }
+    return ARK_OK;
+}
+
+int ark_get_array(ark_ctx *ctx, const char *name, double *host) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!name || !host) return fail(ARK_ERR_PARAM, "NULL name or buffer");
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    if (std::strcmp(name, "condition") == 0) {
+        std::memcpy(host, ctx->cond_host.data(), sizeof(double) * ctx->cond_host.size());
+        return ARK_OK;
+    }
+    for (int w = 0; w < 24; ++w)
+        if (w != 8 && std::strcmp(name, kFields[w].name) == 0) return ctx->eng->download_field(w, kFields[w].face, host);
+    int face = 0;
+    void *p = ctx->eng->field_ptr(name, &face);
+    if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
+    const size_t n = face ? (size_t)ctx->g.nface() : (size_t)ctx->g.ncell();
+    if (ctx->P.precision == ARK_FP64) {
+        ARK_CUDA(cudaMemcpy(host, p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        convert_to_double<float>(ctx->stage, (const float *)p, (int64_t)n, ctx->st);
+        ARK_CUDA(cudaStreamSynchronize(ctx->st));
+        ARK_CUDA(cudaMemcpy(host, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return ARK_OK;
+}
+
+int ark_put_array(ark_ctx *ctx, const char *name, const double *host) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!name || !host) return fail(ARK_ERR_PARAM, "NULL name or buffer");
+    if (std::strcmp(name, "condition") == 0) return fail(ARK_ERR_PARAM, "condition is set by ark_upload");
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    for (int w = 0; w < 24; ++w)
+        if (w != 8 && std::strcmp(name, kFields[w].name) == 0) return ctx->eng->upload_field(w, kFields[w].face, host);
+    int face = 0;
+    void *p = ctx->eng->field_ptr(name, &face);
+    if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
+    const size_t n = face ? (size_t)ctx->g.nface() : (size_t)ctx->g.ncell();
+    if (ctx->P.precision == ARK_FP64) {
+        ARK_CUDA(cudaMemcpy(p, host, n * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        ARK_CUDA(cudaMemcpy(ctx->stage, host, n * sizeof(double), cudaMemcpyHostToDevice));
+        convert_from_double<float>((float *)p, ctx->stage, (int64_t)n, ctx->st);
+        ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    }
+    return ARK_OK;
+}
+
+int ark_time_step_size(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->eng->time_step_size(ctx->con, 0);
+    return launch_status(ctx);
+}
+
+int ark_phase1(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    // "Con" <- "nCon" is a relabelling: the old nCon level is read as Con and the new
+    // nCon values are written over the old Con level.
+    const int src = ctx->con ^ 1, dst = ctx->con;
+    ctx->eng->phase1(src, dst, P1_PLAIN);
+    ctx->con = src;
+    return launch_status(ctx);
+}
+
+int ark_stress_tensor(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->eng->stress(ctx->con, ctx->k.forcing);
+    return launch_status(ctx);
+}
+
+int ark_use_forces(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->eng->use_forces(ctx->con ^ 1);
+    return launch_status(ctx);
+}
+
+int ark_phase2(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->eng->phase2(ctx->con);
+    return launch_status(ctx);
+}
+
+int ark_boundary_fill(ark_ctx *ctx, int axis) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (axis < 1 || axis > 3) return fail(ARK_ERR_PARAM, "axis must be 1, 2 or 3");
+    const int periodic = axis == 2 ? 0 : axis == 3 ? ctx->P.periodic_z : 0;
+    ctx->eng->boundary_fill(ctx->con ^ 1, axis, periodic);
+    return launch_status(ctx);
+}
+
+int ark_set_dt(ark_ctx *ctx, double dt) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ARK_CUDA(cudaMemcpy(&ctx->eng->scalars()->dt, &dt, sizeof(double), cudaMemcpyHostToDevice));
+    return ARK_OK;
+}
+
+// Captures the fused step for the current role of the two cell levels (once per role).
+static int ensure_graph(ark_ctx *ctx) {
+    const int x = ctx->con;
+    if (!ctx->graph[x]) {
+        cudaGraph_t graph = nullptr;
+        ARK_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+        ctx->eng->step(x, nullptr);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(ctx->st, &graph);
+        if (le != cudaSuccess || ce != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(ARK_ERR_CUDA, std::string("step capture: ") +
+                                          cudaGetErrorString(le != cudaSuccess ? le : ce));
+        }
+        cudaError_t ie = cudaGraphInstantiate(&ctx->graph[x], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            ctx->graph[x] = nullptr;
+            return fail(ARK_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        }
+    }
+    return ARK_OK;
+}
+
+int ark_step(ark_ctx *ctx, int nsteps) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (nsteps < 0) return fail(ARK_ERR_PARAM, "nsteps < 0");
+    if (nsteps == 0) return ARK_OK;
+    if (int rc = ensure_graph(ctx)) return rc;
+    for (int s = 0; s < nsteps; ++s) ARK_CUDA(cudaGraphLaunch(ctx->graph[ctx->con], ctx->st));
+    return ARK_OK;
+}
+
+int ark_sync(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, false)) return rc;
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    int status = 0;
+    ARK_CUDA(cudaMemcpy(&status, &ctx->eng->scalars()->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status & STATUS_NONFINITE) return fail(ARK_ERR_NONFINITE, "non-finite velocity detected on the device");
+    return ARK_OK;
+}
+
+int ark_time_steps(ark_ctx *ctx, int nsteps, double *ms) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!ms) return fail(ARK_ERR_PARAM, "ms is NULL");
+    if (int rc = ensure_graph(ctx)) return rc; // built outside the timed region
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ARK_CUDA(cudaEventRecord(ctx->ev0, ctx->st));
+    if (int rc = ark_step(ctx, nsteps)) return rc;
+    ARK_CUDA(cudaEventRecord(ctx->ev1, ctx->st));
+    ARK_CUDA(cudaEventSynchronize(ctx->ev1));
+    float f = 0.f;
+    ARK_CUDA(cudaEventElapsedTime(&f, ctx->ev0, ctx->ev1));
+    *ms = (double)f;
+    return ark_sync(ctx);
+}
+
+int ark_kernel_times(ark_ctx *ctx, int nsteps, double *ms, int cap, int *count) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!ms || !count || nsteps < 1) return fail(ARK_ERR_PARAM, "bad arguments");
+    *count = kNumStepKernels;
+    std::vector<cudaEvent_t> ev(kNumStepKernels + 1);
+    for (auto &e : ev) ARK_CUDA(cudaEventCreate(&e));
+    std::vector<double> acc(kNumStepKernels, 0.0);
+    int rc = ARK_OK;
+    for (int s = 0; s < nsteps && rc == ARK_OK; ++s) {
+        cudaEventRecord(ev[0], ctx->st);
+        ctx->eng->step(ctx->con, ev.data() + 1);
+        if ((rc = launch_status(ctx))) break;
+        if (cudaEventSynchronize(ev[kNumStepKernels]) != cudaSuccess) {
+            rc = fail(ARK_ERR_CUDA, "event synchronize failed");
+            break;
+        }
+        for (int q = 0; q < kNumStepKernels; ++q) {
+            float f = 0.f;
+            cudaEventElapsedTime(&f, ev[q], ev[q + 1]);
+            acc[q] += f;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int q = 0; q < kNumStepKernels && q < cap; ++q) ms[q] = acc[q] / nsteps;
+    if (rc) return rc;
+    return ark_sync(ctx);
+}
+
+const char *ark_kernel_name(int index) {
+    return index >= 0 && index < kNumStepKernels ? kStepKernels[index] : nullptr;
+}
+
+int ark_alloc_host_state(const ark_params *p, ark_host_state *out) {
+    if (!p || !out) return fail(ARK_ERR_PARAM, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    const size_t nc = ark_cell_count(p), nf = ark_face_count(p);
+    for (const FieldRef &f : kFields) {
+        void *ptr = nullptr;
+        const size_t bytes = sizeof(double) * (f.face ? nf : nc);
+        cudaError_t e = cudaHostAlloc(&ptr, bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            ark_free_host_state(out);
+            return fail(ARK_ERR_NOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+        }
+        std::memset(ptr, 0, bytes);
+        out->*f.member = (double *)ptr;
+    }
+    return ARK_OK;
+}
+
+int ark_free_host_state(ark_host_state *h) {
+    if (!h) return ARK_OK;
+    for (const FieldRef &f : kFields) {
+        if (h->*f.member) cudaFreeHost(h->*f.member);
+        h->*f.member = nullptr;
+    }
+    return ARK_OK;
+}
+
+int ark_get_scalars(ark_ctx *ctx, ark_scalars *out) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!out) return fail(ARK_ERR_PARAM, "out is NULL");
+    DevScalars sc;
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ARK_CUDA(cudaMemcpy(&sc, ctx->eng->scalars(), sizeof(sc), cudaMemcpyDeviceToHost));
+    out->dt = sc.dt;
+    out->time = sc.time;
+    out->nstep = sc.nstep;
+    out->bulk_velocity = sc.ub;
+    out->bulk_force = sc.G;
+    return ARK_OK;
+}
+
+int ark_set_scalars(ark_ctx *ctx, const ark_scalars *in) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!in) return fail(ARK_ERR_PARAM, "in is NULL");
+    DevScalars sc;
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ARK_CUDA(cudaMemcpy(&sc, ctx->eng->scalars(), sizeof(sc), cudaMemcpyDeviceToHost));
+    sc.dt = in->dt;
+    sc.time = in->time;
+    sc.nstep = in->nstep;
+    sc.ub = in->bulk_velocity;
+    sc.G = in->bulk_force;
+    ARK_CUDA(cudaMemcpy(ctx->eng->scalars(), &sc, sizeof(sc), cudaMemcpyHostToDevice));
+    return ARK_OK;
+}
+
+int ark_conservation_sums(ark_ctx *ctx, ark_sums *out) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!out) return fail(ARK_ERR_PARAM, "out is NULL");
+    DevScalars *dsc = ctx->eng->scalars();
+    ARK_CUDA(cudaMemsetAsync(&dsc->sums[0], 0, sizeof(long long) * 6, ctx->st));
+    ctx->eng->sums(ctx->con ^ 1);
+    if (int rc = launch_status(ctx)) return rc;
+    long long v[6];
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ARK_CUDA(cudaMemcpy(v, &dsc->sums[0], sizeof(v), cudaMemcpyDeviceToHost));
+    const double q = 1.0 / 4294967296.0;
+    out->mass = (double)v[0] * q;
+    out->momentum1 = (double)v[1] * q;
+    out->momentum2 = (double)v[2] * q;
+    out->momentum3 = (double)v[3] * q;
+    out->kinetic = (double)v[4] * q;
+    out->cells = v[5];
+    return ARK_OK;
+}
+
+} // extern "C"

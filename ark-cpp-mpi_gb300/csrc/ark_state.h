@@ -1,0 +1,104 @@
+// Device-side data model of the CABARET step (shared by host launch code and kernels).
+//
+// Layout in HBM: every field is its own array in the reference's Arr3d index space
+// (source/Arr3d.cpp:19-21, i fastest), so the host<->device transfer of a reference array
+// is one contiguous copy:
+//   cells  (C1+2)(C2+2)(C3+2)   interior 1..C, one ghost layer (main.cpp:198-224)
+//   faces  (C1+3)(C2+3)(C3+3)   faces normal to d: 1..C_d+1 along d, halo 0 and C_d+2
+// Two cell levels hold "Con" and "nCon"; the step swaps their roles instead of copying
+// (Phase1's nCon -> Con copy, main.cpp:419-432, becomes a relabelling).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ark {
+
+struct Geom {
+    int C1, C2, C3;
+    int64_t cs1, cs2; // cell strides of j and k
+    int64_t fs1, fs2; // face strides of j and k
+    __host__ __device__ __forceinline__ int64_t cell(int i, int j, int k) const {
+        return (int64_t)k * cs2 + (int64_t)j * cs1 + i;
+    }
+    __host__ __device__ __forceinline__ int64_t face(int i, int j, int k) const {
+        return (int64_t)k * fs2 + (int64_t)j * fs1 + i;
+    }
+    __host__ __device__ int64_t ncell() const { return cs2 * (C3 + 2); }
+    __host__ __device__ int64_t nface() const { return fs2 * (C3 + 3); }
+};
+
+// Sticky device status bits.
+enum : int { STATUS_NONFINITE = 1 };
+
+// Cell-flag bits: the reference tests the double `condition` three ways.
+enum : uint8_t {
+    FL_LT = 1, // condition < 0.5   (fluid in Phase1, stress and Phase2 branches)
+    FL_GT = 2, // condition > 0.5   (solid in stress and Phase2 branches)
+    FL_EQ0 = 4 // condition == 0    (StressTensor force and UseForces, main.cpp:999,1035)
+};
+
+template <class T> struct Level { T *ro, *u1, *u2, *u3; };
+
+// Faces normal to one axis: pressure, density, velocity components u[0..2].
+template <class T> struct FaceSet { T *p, *ro, *u[3]; };
+
+// Constants of a run, computed once on the host in double (the FP32 path rounds them).
+struct Consts {
+    double dx[3], rdx[3];  // grid steps and their correctly rounded reciprocals
+    double ds[3], dvc;     // face areas dx2*dx3, dx1*dx3, dx1*dx2 and cell volume dx1*dx2*dx3
+    double vis, two_vis;   // VIS and 2*VIS
+    double sound, ro0;
+    double c2, rc2;        // sound*sound and its reciprocal
+    double roc, rroc;      // ro0_g*sound and its reciprocal
+    double cfl_dx[3];      // CFL*dx_d (TimeStepSize's numerators)
+    double dtv;            // viscous dt limit of TimeStepSize (cell independent)
+    double u_target;
+    int forcing;
+};
+
+// Scalars and reduction accumulators living on the device, so a whole step (and a
+// CUDA graph of it) never waits for the host.
+struct DevScalars {
+    double dt, time, ub, G;
+    long long nstep;
+    unsigned long long umax[3]; // max |u_d| of the "Con" level, as IEEE bit patterns
+    long long usum;             // sum of u1 over fluid cells, 2^-32 fixed point
+    long long nfluid;           // fluid cells (condition == 0), set at upload
+    int status;                 // sticky error bits (ARK_ERR_NONFINITE)
+    int pad;
+    long long sums[5];          // conservation sums (fixed point), see ark_sums
+    long long sum_cells;
+};
+
+template <class T> struct DevState {
+    Geom g;
+    Consts k;
+    Level<T> lv[2];
+    T *f[3];
+    FaceSet<T> fc[3];
+    T *sig[3][3]; // sig[d][m]: component m on faces normal to d (nullptr unless kept)
+    uint8_t *flags;
+    DevScalars *sc;
+};
+
+// Launch entry points (defined per precision in ark_fp64.cu / ark_fp32.cu).
+enum Phase1Mode { P1_PLAIN = 0, P1_STRESS = 1, P1_FORCES = 2, P1_BULK = 4 };
+
+template <class T> struct Launch {
+    static void reduce_start(const DevState<T> &S, int con, int with_sum, cudaStream_t st);
+    static void finalize_dt(const DevState<T> &S, int advance_time, cudaStream_t st);
+    static void wrap_cells(const DevState<T> &S, T *const *arrs, int n, cudaStream_t st);
+    static void wrap_phase2(const DevState<T> &S, int con, cudaStream_t st);
+    static void phase1(const DevState<T> &S, int src, int dst, int mode, cudaStream_t st);
+    static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
+    static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
+    static void sweep(const DevState<T> &S, int con, int axis, cudaStream_t st);
+    static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
+    static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
+};
+
+// double <-> T copies for FP32 contexts (host arrays are always double)
+template <class T> void convert_from_double(T *dst, const double *src, int64_t n, cudaStream_t st);
+template <class T> void convert_to_double(double *dst, const T *src, int64_t n, cudaStream_t st);
+
+} // namespace ark

@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Throughput of the CABARET channel time step on GB300 (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the FP64 channel at 256x128x128 cells, Re_b 5600, c = 10, CFL 0.2, bulk forcing,
+seeded perturbations (the reference-parity configuration).  One "step" is one full time
+step (main.cpp:82-91).  Metric: Mcell-steps/s = cells * steps / seconds.  The FP32 path at
+512x256x256 is measured beside it (key "fp32").  Synthetic data: the seeded channel state
+is the benchmark input (the reference has no dataset).
+
+--impl reference times the reference's CPU step on the host cores instead: the compiled
+reference (oracle/_ref) where it exists, else its C restatement (oracle/), with all threads.
+
+Under torchrun (N > 1) every rank advances its own independent channel (replicas; the
+path has no exchange on one GPU per rank), timed between barriers; value = all ranks'
+cell-steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ark-cpp-mpi_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s on 1 GB300, FP32 vs plain FP64 at stated error; % HBM roofline"
+UNIT = "Mcell-steps/s"
+
+# Algorithmic (compulsory) values moved per cell by each launch of the fused step: every
+# input element read once, every output element written once (faces counted once per cell:
+# each face is shared by two cells).  Flags are 1 byte per cell.
+ALGO_VALUES = {
+    "reduce_start": (4, 1),          # Con u1..u3, nCon u1; flags
+    "finalize_dt": (0, 0),
+    "wrap_con": (0, 0),
+    "phase1_stress_forces": (26, 1),  # Con 4 + faces 15 -> nCon 4 + f 3
+    "wrap_phase2": (0, 0),
+    "sweep_x1": (17, 1),              # Con 4 + nCon 4 + faces 4 -> faces 5
+    "sweep_x2": (17, 1),
+    "sweep_x3": (17, 1),
+    "phase1_forces": (26, 1),         # Con 4 + faces 15 + f 3 -> nCon 4
+}
+# Persistent state per cell: cell rho,u1,u2,u3 + 3 face sets x {p,u1,u2,u3}; read and
+# written once per step (the step's algorithmic bytes).
+STEP_VALUES = 2 * 16
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_cell():
+    """DRAM bytes per cell of each kernel from the committed ncu summary (or {})."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_cell.txt")
+    out = {}
+    if os.path.isfile(path):
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 3 and not line.startswith("#"):
+                    out[(parts[0], parts[1])] = float(parts[2])
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", f"ark_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "-i", str(self.device),
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.isfile(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.path) as f:
+            for line in f:
+                v = [x.strip() for x in line.split(",")]
+                if len(v) < 9:
+                    continue
+                try:
+                    sm.append(float(v[1]))
+                    smax.append(float(v[2]))
+                except ValueError:
+                    continue
+                for nm, flag in zip(names, v[5:9]):
+                    if flag.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def channel_params(arkgpu, C, re_b, precision):
+    return arkgpu.make_params(*C, re_b=re_b, sound=10.0, rho0=1.0, cfl=0.2, precision=precision)
+
+
+def gpu_leg(arkgpu, C, re_b, precision, steps, warmup, device, seed, kernel_steps=10):
+    """Device-timed throughput, per-launch times and the roofline of the dominant kernel."""
+    p = channel_params(arkgpu, C, re_b, precision)
+    p.device = device
+    st = arkgpu.channel_init(p, seed=seed, amp=0.1)
+    cells = C[0] * C[1] * C[2]
+    with arkgpu.Context(p) as ctx:
+        ctx.upload(st)
+        del st
+        ctx.step(warmup)
+        ctx.sync()
+        with ClockSampler(device) as clk:
+            ms = ctx.time_steps(steps)
+        clocks = clk.summary()
+        ktimes = ctx.kernel_times(kernel_steps)
+        sc = ctx.scalars()
+    return {"cells": cells, "ms": ms, "clocks": clocks, "ktimes": ktimes, "dt": sc.dt, "ub": sc.bulk_velocity}
+
+
+def roofline(kt, cells, word, peak, peak_kind, traffic_tab, prec_name):
+    name, ms = max(kt, key=lambda x: x[1])
+    vals, flag_b = ALGO_VALUES.get(name, (0, 0))
+    algo = cells * (vals * word + flag_b)
+    achieved = algo / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    tpc = traffic_tab.get((prec_name, name))
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+            "traffic": (round(tpc * cells) if tpc is not None else None),
+            "algorithmic_bytes": algo, "launch_ms": round(ms, 4)}
+
+
+def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
+    """Through the C ABI with host buffers: every step uploads the full state from pinned
+    memory, runs one step and downloads the full state."""
+    p = channel_params(arkgpu, C, re_b, precision)
+    p.device = device
+    st = arkgpu.channel_init(p, seed=seed, amp=0.1)
+    hs = arkgpu.PinnedState(p)
+    hs.fill(st)
+    del st
+    cells = C[0] * C[1] * C[2]
+    with arkgpu.Context(p) as ctx:
+        ctx.upload_struct(hs.struct(True))
+        ctx.step(1)
+        ctx.sync()
+        h_up = hs.struct(False)
+        h_dn = hs.struct(False)
+        ctx.upload_struct(h_up)
+        ctx.step(1)
+        ctx.download_struct(h_dn)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.upload_struct(h_up)
+            ctx.step(1)
+            ctx.download_struct(h_dn)
+        secs = time.perf_counter() - t0
+        ctx.sync()
+    nbytes = hs.nbytes(False)
+    hs.close()
+    return {"value": round(cells * steps / secs / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes, "steps": steps}
+
+
+def cpu_leg(C, re_b, budget_s=12.0, max_steps=400, threads=None):
+    """The oracle's C restatement of the reference step on the host cores."""
+    import oracle
+
+    oracle.build(port=True, ref=False)
+    threads = threads or os.cpu_count() or 1
+    p = oracle.channel_params(*C, re_b=re_b, seed=7)
+    o = oracle.Port(p, threads=threads)
+    o.load(oracle.channel_state(p))
+    o.run(1)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while n < max_steps and time.perf_counter() - t0 < budget_s:
+        o.run(1)
+        n += 1
+    secs = time.perf_counter() - t0
+    cells = C[0] * C[1] * C[2]
+    return {"value": round(cells * n / secs / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} full steps of the {C[0]}x{C[1]}x{C[2]} FP64 channel, {threads} OpenMP threads "
+                      f"({secs:.1f} s)"}
+
+
+def reference_arm(args, world, rank, dist):
+    """--impl reference: the reference's CPU step (C restatement) timed on the host cores."""
+    if rank != 0:
+        return 0
+    import oracle
+
+    oracle.build(port=True, ref=False)
+    threads = os.cpu_count() or 1
+    C = tuple(args.grid)
+    p = oracle.channel_params(*C, re_b=args.re, seed=7)
+    o = oracle.Port(p, threads=threads)
+    o.load(oracle.channel_state(p))
+    o.run(args.warmup)
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    secs = time.perf_counter() - t0
+    cells = C[0] * C[1] * C[2]
+    v = cells * args.steps / secs / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded channel state)",
+            "config": {"workload": f"channel {C[0]}x{C[1]}x{C[2]} FP64 Re_b={args.re:g}, bulk forcing",
+                       "grid": list(C), "precision": "fp64", "parallelism": "host threads"},
+            "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full steps of the {C[0]}x{C[1]}x{C[2]} channel, "
+                                       f"{threads} OpenMP threads"},
+            "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--grid", type=int, nargs=3, default=(256, 128, 128))
+    ap.add_argument("--re", type=float, default=5600.0)
+    ap.add_argument("--fp32-grid", type=int, nargs=3, default=(512, 256, 256))
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=30)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        rc = reference_arm(args, world, rank, dist)
+        if dist is not None:
+            dist.destroy_process_group()
+        return rc
+
+    import arkgpu
+
+    arkgpu.lib()
+    device = local
+    C = tuple(args.grid)
+    peak, peak_kind = measured_peaks()
+    traffic = ncu_traffic_per_cell()
+
+    barrier(dist)
+    g = gpu_leg(arkgpu, C, args.re, arkgpu.FP64, args.steps, args.warmup, device, seed=1000 + rank)
+    barrier(dist)
+    ms = max_over_ranks(dist, g["ms"])
+    total_cells = g["cells"] * world
+    value = total_cells * args.steps / (ms * 1e-3) / 1e6
+    launches_per_step = len(g["ktimes"])
+
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded channel state)",
+            "config": {"workload": f"channel {C[0]}x{C[1]}x{C[2]} FP64 Re_b={args.re:g}, c=10, CFL 0.2, bulk forcing",
+                       "grid": list(C), "precision": "fp64", "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": f"inputs larger than L2: {g['cells'] * 8 * 41 / 1e9:.2f} GB of state streamed per step"},
+            "clocks": g["clocks"],
+            "gpu_launches": launches_per_step * args.steps}
+    line["roofline"] = roofline(g["ktimes"], g["cells"], 8, peak, peak_kind, traffic, "fp64")
+    step_s = ms * 1e-3 / args.steps
+    line["step_roofline"] = {"bytes_per_cell": STEP_VALUES * 8,
+                             "achieved": round(g["cells"] * STEP_VALUES * 8 / step_s / 1e9, 1),
+                             "peak": peak, "unit": "GB/s",
+                             "frac": round(g["cells"] * STEP_VALUES * 8 / step_s / 1e9 / peak, 4)}
+    line["kernels_ms"] = {k: round(v, 4) for k, v in g["ktimes"]}
+
+    if rank == 0 and not args.no_fp32:
+        C32 = tuple(args.fp32_grid)
+        f = gpu_leg(arkgpu, C32, args.re, arkgpu.FP32, max(20, args.steps // 3), args.warmup, device, seed=77)
+        f_steps = max(20, args.steps // 3)
+        fv = f["cells"] * f_steps / (f["ms"] * 1e-3) / 1e6
+        f_step_s = f["ms"] * 1e-3 / f_steps
+        line["fp32"] = {"value": round(fv, 3), "unit": UNIT, "grid": list(C32), "steps": f_steps,
+                        "ms_per_step": round(f["ms"] / f_steps, 4), "dtype": "f32 (f64 reductions)",
+                        "roofline": roofline(f["ktimes"], f["cells"], 4, peak, peak_kind, traffic, "fp32"),
+                        "step_roofline": {"bytes_per_cell": STEP_VALUES * 4,
+                                          "achieved": round(f["cells"] * STEP_VALUES * 4 / f_step_s / 1e9, 1),
+                                          "peak": peak, "unit": "GB/s",
+                                          "frac": round(f["cells"] * STEP_VALUES * 4 / f_step_s / 1e9 / peak, 4)},
+                        "kernels_ms": {k: round(v, 4) for k, v in f["ktimes"]}, "clocks": f["clocks"]}
+        line["gpu_launches"] += launches_per_step * f_steps
+
+    if rank == 0:
+        line["e2e"] = e2e_leg(arkgpu, C, args.re, arkgpu.FP64, args.e2e_steps, device, seed=5)
+        if world == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_leg(C, args.re)
+        print(json.dumps(line), flush=True)
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

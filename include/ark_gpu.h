@@ -1,0 +1,201 @@
+/*
+ * ark_gpu.h -- C ABI of the GB300 CABARET time step (libark_gb300.so).
+ *
+ * The reference (ark-cpp-mpi) has no plugin or FFI layer: its solver is a set of
+ * `void f(void)` functions working on global Arr3d arrays (source/main.cpp:12-21,
+ * headers/bulk.h:51-108, headers/stress.h:21-23, headers/forces.h:15) and driven by the
+ * loop in main.cpp:80-104.  This header is the drop-in for that loop: the same step
+ * pieces under the same names, operating on a context instead of globals, plus a fused
+ * `ark_step` that runs main.cpp:82-91 on the device.
+ *
+ * Host arrays use the reference's Arr3d layout (source/Arr3d.cpp:19-21):
+ * element (i,j,k) at [k*N1*N2 + j*N1 + i], i fastest.  With C1 x C2 x C3 cells
+ * (reference node counts n = C + 1, main.cpp:147-151):
+ *   cell arrays  : N = (C1+2, C2+2, C3+2)  -- Arr3d(n1+1, n2+1, n3+1), main.cpp:198-224
+ *   face arrays  : N = (C1+3, C2+3, C3+3)  -- Arr3d(n1+2, n2+2, n3+2), main.cpp:226-251
+ * Interior cells are 1..C; faces normal to axis d are 1..C_d+1 along d.
+ *
+ * Every call returns an int status (ARK_OK == 0).  Nothing exits the process or traps the
+ * GPU.  One context belongs to one host thread and one CUDA stream; the library keeps no
+ * global state.  Host arrays stay owned by the caller; the context owns all device memory.
+ */
+#ifndef ARK_GPU_H
+#define ARK_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum ark_status {
+    ARK_OK = 0,
+    ARK_ERR_PARAM = 1,       /* bad argument or unsupported configuration                 */
+    ARK_ERR_CUDA = 2,        /* a CUDA call failed; ark_last_error() has the text         */
+    ARK_ERR_NONFINITE = 3,   /* a NaN or Inf reached the velocity field                    */
+    ARK_ERR_STATE = 4,       /* call out of order (e.g. a step before ark_upload)          */
+    ARK_ERR_NOMEM = 5,       /* device allocation failed                                   */
+    ARK_ERR_UNSUPPORTED = 6  /* a valid request this build does not implement              */
+};
+
+enum ark_precision {
+    ARK_FP64 = 0, /* parity path: FP64 storage and arithmetic, bit-for-bit with the reference */
+    ARK_FP32 = 1  /* FP32 storage and arithmetic; dt, flow-rate and conservation sums in FP64 */
+};
+
+/* Scalar parameters.  Names follow headers/constants.h:20-22 and headers/bulk.h:18-35. */
+typedef struct ark_params {
+    int n1_cells, n2_cells, n3_cells; /* C1, C2, C3 (the reference's n?_g - 1)                 */
+    double lx, ly, lz;                /* domain extents: dx_d = L_d / C_d (main.cpp:284-290)    */
+    double vis;                       /* VIS, kinematic viscosity                               */
+    double sound;                     /* sound speed                                            */
+    double ro0;                       /* ro0_g, unperturbed density                             */
+    double cfl;                       /* CFL number                                             */
+    int periodic_x;                   /* 1: periodic x.  0 (bounded, inflow/outflow): rejected  */
+    int periodic_z;                   /* 1: periodic z.  0 (bounded, zero-gradient): rejected   */
+    int precision;                    /* enum ark_precision                                     */
+    int forcing;                      /* 1: constant-flow-rate bulk forcing                     */
+    double u_target;                  /* bulk velocity the forcing holds                        */
+    int keep_stress;                  /* 1: ark_stress_tensor also fills the sigm?? arrays      */
+    int device;                       /* CUDA device ordinal                                    */
+} ark_params;
+
+/* Host state in Arr3d layout.  Names are the reference globals.  In ark_download any
+ * pointer may be NULL (that array is skipped); ark_upload needs all of them. */
+typedef struct ark_host_state {
+    double *roCon, *u1Con, *u2Con, *u3Con;     /* cells, level "Con"  (main.cpp:199-204)   */
+    double *ronCon, *u1nCon, *u2nCon, *u3nCon; /* cells, level "nCon" (main.cpp:206-211)   */
+    double *condition;                         /* cells, 1 solid / 0 fluid (main.cpp:219)  */
+    double *p1, *ro1, *u11, *u21, *u31;        /* faces normal to x1 (main.cpp:227-232)    */
+    double *p2, *ro2, *u12, *u22, *u32;        /* faces normal to x2 (main.cpp:235-240)    */
+    double *p3, *ro3, *u13, *u23, *u33;        /* faces normal to x3 (main.cpp:243-248)    */
+} ark_host_state;
+
+/* Scalars of the time loop: dt and TIME (headers/constants.h:20), nStep (headers/bulk.h:18),
+ * and the bulk-forcing state of the last step. */
+typedef struct ark_scalars {
+    double dt;
+    double time;
+    long long nstep;
+    double bulk_velocity; /* mean u1 over fluid cells, taken at the start of the step */
+    double bulk_force;    /* G = (u_target - bulk_velocity) / dt                       */
+} ark_scalars;
+
+/* Conservation sums over interior fluid cells of the "nCon" level.  Each term is summed in
+ * exact 2^-32 fixed point, so the result does not depend on the launch configuration. */
+typedef struct ark_sums {
+    double mass;      /* sum of ro                            */
+    double momentum1; /* sum of ro * u1                       */
+    double momentum2; /* sum of ro * u2                       */
+    double momentum3; /* sum of ro * u3                       */
+    double kinetic;   /* sum of (u1^2 + u2^2 + u3^2) / 2 (the WriteEnergy sum, main.cpp:2851-2860) */
+    long long cells;  /* fluid cells summed                   */
+} ark_sums;
+
+typedef struct ark_ctx ark_ctx;
+
+/* ---- lifetime ------------------------------------------------------------------------ */
+
+/* Allocates every device array (replaces Input()'s allocation block, main.cpp:198-277).
+ * Returns NULL and sets *status on failure. */
+ark_ctx *ark_create(const ark_params *params, int *status);
+
+/* Frees the context (replaces FreeMemory(), main.cpp:2893-2961). */
+int ark_destroy(ark_ctx *ctx);
+
+/* Text of the last error on this thread. */
+const char *ark_last_error(void);
+const char *ark_status_string(int status);
+
+/* Number of doubles in a host cell array / face array for these parameters. */
+size_t ark_cell_count(const ark_params *params);
+size_t ark_face_count(const ark_params *params);
+
+/* ---- state transfer --------------------------------------------------------------------- */
+
+/* Copies a complete host state to the device (synchronous).  After the first upload,
+ * host->condition may be NULL: the previous condition, dt, TIME and nStep are kept, so a
+ * caller that keeps the state on the host can round-trip it every step. */
+int ark_upload(ark_ctx *ctx, const ark_host_state *host);
+
+/* Copies the device state back into every non-NULL host array (synchronous). */
+int ark_download(ark_ctx *ctx, ark_host_state *host);
+
+/* Reads or writes one named array ("f1".."f3", "sigm11".."sigm33", or any ark_host_state
+ * member name) in Arr3d layout.  Synchronous. */
+int ark_get_array(ark_ctx *ctx, const char *name, double *host);
+int ark_put_array(ark_ctx *ctx, const char *name, const double *host);
+
+/* ---- the reference's step pieces (same names, same semantics) -------------------------- */
+
+/* TimeStepSize (main.cpp:374-415): dt from the "Con" velocities.  When forcing is on it also
+ * takes the bulk velocity of the "nCon" level and sets G for the next ark_stress_tensor. */
+int ark_time_step_size(ark_ctx *ctx);
+
+/* Phase1 (main.cpp:417-575): "Con" <- "nCon", then the conservative half step. */
+int ark_phase1(ark_ctx *ctx);
+
+/* StressTensor (main.cpp:577-1024): ghost fill of u?Con, viscous stress, force f1..f3
+ * (plus the bulk force when forcing is on). */
+int ark_stress_tensor(ark_ctx *ctx);
+
+/* UseForces (main.cpp:1026-1045). */
+int ark_use_forces(ark_ctx *ctx);
+
+/* Phase2 (main.cpp:1047-2495): ghost fill, then the x1, x2 and x3 characteristic sweeps. */
+int ark_phase2(ark_ctx *ctx);
+
+/* BoundaryConditions::alongX1/2/3 (source/BoundaryConditions.cpp:22-83) applied to the "nCon"
+ * cell level on the device: axis 1 zero-gradient copy; axes 2 and 3 periodic copy when
+ * that axis is periodic, else no-slip (u = 0, ro zero-gradient). */
+int ark_boundary_fill(ark_ctx *ctx, int axis);
+
+/* Sets / reads dt (used by the step pieces above). */
+int ark_set_dt(ark_ctx *ctx, double dt);
+
+/* ---- the fused time loop ----------------------------------------------------------------- */
+
+/* nsteps iterations of main.cpp:82-91 (TimeStepSize, Phase1, StressTensor, UseForces, Phase2,
+ * Phase1, UseForces, with nStep and TIME advanced as there), asynchronous on the context's
+ * stream.  The step is captured once into a CUDA graph and replayed. */
+int ark_step(ark_ctx *ctx, int nsteps);
+
+/* Blocks until the context's stream is idle and reports a deferred device error
+ * (ARK_ERR_NONFINITE when a NaN/Inf was seen in the velocity field). */
+int ark_sync(ark_ctx *ctx);
+
+/* Runs nsteps like ark_step and returns the device time between CUDA events recorded on
+ * the context's stream around them (milliseconds). */
+int ark_time_steps(ark_ctx *ctx, int nsteps, double *ms);
+
+/* Runs nsteps un-graphed fused steps with a CUDA event after every launch and writes the
+ * mean device time of each launch (ms) into ms[0..cap-1], in step order; *count receives the
+ * number of launches per step.  ark_kernel_name(i) names launch i. */
+int ark_kernel_times(ark_ctx *ctx, int nsteps, double *ms, int cap, int *count);
+const char *ark_kernel_name(int index);
+
+int ark_get_scalars(ark_ctx *ctx, ark_scalars *out);
+int ark_set_scalars(ark_ctx *ctx, const ark_scalars *in);
+int ark_conservation_sums(ark_ctx *ctx, ark_sums *out);
+
+/* ---- host-side helpers (no GPU needed) ----------------------------------------------------- */
+
+/* Seeded channel-flow initial state (a project definition, not part of the reference):
+ * interior cell (i,j,k), visited k-major / i fastest, draws three splitmix64 uniforms
+ * r1,r2,r3 in [0,1) and sets u1 = 1.5*u_target*(1 - y*y) + amp*(2*r1 - 1),
+ * u2 = amp*(2*r2 - 1), u3 = amp*(2*r3 - 1), ro = ro0, with y = -ly/2 + (j - 0.5)*dy.
+ * Ghost cells are periodic copies in x and z; y ghost rows are solid (condition = 1).
+ * Faces hold the mean of their two cells (0 on the y walls), p = 0, face ro = ro0.
+ * "Con" starts equal to "nCon".  Fills every array of *out (caller-allocated). */
+int ark_channel_init(const ark_params *params, uint64_t seed, double amp, ark_host_state *out);
+
+/* Allocates every array of a host state in page-locked memory (zero-filled), sized for
+ * params; ark_free_host_state releases them.  Either works without ark_create. */
+int ark_alloc_host_state(const ark_params *params, ark_host_state *out);
+int ark_free_host_state(ark_host_state *host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

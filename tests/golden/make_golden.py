@@ -1,0 +1,131 @@
+"""Generate the golden fixtures from the REFERENCE ITSELF (compiled in place).
+
+    make -C oracle ref         # builds oracle/_ref/libark_ref.so from the reference sources
+    python tests/golden/make_golden.py
+
+The reference (ark-cpp-mpi) ships no tests, fixtures or known-answer vectors, so these
+fixtures are outputs of its own source/main.cpp solver functions (TimeStepSize, Phase1,
+StressTensor, UseForces, Phase2), driven by oracle/ref_harness.cpp on seeded channel
+states.  They pin the C restatement (oracle/ark_oracle.c) on any machine, including the
+GPU machine where the reference sources are absent.
+
+Files:
+  small_run.npz      12x8x6 cells, 20 full steps with bulk forcing: interior arrays
+  small_bounded.npz  14x6x6 cells, 10 steps, bounded x (inflow/outflow) and z edges
+  phases.npz         10x6x8 cells: one call of each step piece on a perturbed state
+  digests.json       sha256 of every interior array after longer runs (64x32x32 x 100
+                     steps at Re_b 2800, 33x17x9 x 50 steps), plus dt, TIME, U_b
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+CHECK = ["roCon", "u1Con", "u2Con", "u3Con", "ronCon", "u1nCon", "u2nCon", "u3nCon"] + list(oracle.FACE_NAMES)
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def interior_dump(m) -> dict:
+    return {n: oracle.interior(n, m.get(n)) for n in CHECK}
+
+
+def perturbed_state(p, seed):
+    """A channel state whose faces and pressure are also perturbed, so every branch of the
+    face update and the limiter is exercised by single calls."""
+    st = oracle.channel_state(p)
+    draws = [0]
+
+    def noise(shape):  # splitmix64 uniforms in [-1, 1), a fresh stream per array
+        draws[0] += 1
+        n = int(np.prod(shape))
+        return (2.0 * oracle.uniform01(seed * 1000 + draws[0], n) - 1.0).reshape(shape)
+
+    for d in (1, 2, 3):
+        for v in ("u1", "u2", "u3"):
+            n = f"{v}{d}"
+            st[n] = st[n] + 0.05 * noise(st[n].shape)
+        st[f"p{d}"] = 0.2 * noise(st[f"p{d}"].shape)
+    for lvl in ("", "n"):
+        st[f"ro{lvl}Con"] = st[f"ro{lvl}Con"] + 0.002 * noise(st[f"ro{lvl}Con"].shape)
+    st["u1Con"] = st["u1nCon"] + 0.01 * noise(st["u1nCon"].shape)
+    return st
+
+
+def main():
+    assert oracle.Reference.available(), "build oracle/_ref first: make -C oracle ref"
+    out = {}
+
+    # 1. short forced run, full interior arrays
+    p = oracle.channel_params(12, 8, 6, seed=7)
+    ref = oracle.Reference(p)
+    ref.load(oracle.channel_state(p))
+    ref.run(20)
+    d = interior_dump(ref)
+    np.savez_compressed(os.path.join(HERE, "small_run.npz"), params=json.dumps(p), steps=20,
+                        dt=ref.dt, time=ref.time, ub=ref.last_ub, G=ref.last_g, **d)
+
+    # 2. bounded x (inflow R=1 / outflow Q=5/6, main.cpp:1731-1745) and bounded z
+    p2 = oracle.channel_params(14, 6, 6, seed=11)
+    ref = oracle.Reference(p2, periodic_x=False, periodic_z=False)
+    ref.load(oracle.channel_state(p2))
+    ref.run(10)
+    d = interior_dump(ref)
+    np.savez_compressed(os.path.join(HERE, "small_bounded.npz"), params=json.dumps(p2), steps=10,
+                        dt=ref.dt, time=ref.time, **d)
+
+    # 3. single calls of each step piece (forcing off: pieces exactly as the reference has them)
+    p3 = oracle.channel_params(10, 6, 8, seed=3)
+    st = perturbed_state(p3, 5)
+    ph = {}
+    ref = oracle.Reference(p3, forcing=False)
+    ref.load(st)
+    ref.time_step_size()
+    ph["dt"] = ref.dt
+    ref.phase1()
+    for n in ("roCon", "u1Con", "u2Con", "u3Con", "ronCon", "u1nCon", "u2nCon", "u3nCon"):
+        ph[f"phase1/{n}"] = oracle.interior(n, ref.get(n))
+    ref.stress_tensor()
+    for n in ("f1", "f2", "f3"):
+        ph[f"stress/{n}"] = oracle.interior(n, ref.get(n))
+    for m in "123":
+        for dd in "123":
+            ph[f"stress/sigm{m}{dd}"] = ref.get(f"sigm{m}{dd}")
+    ref.use_forces()
+    for n in ("u1nCon", "u2nCon", "u3nCon"):
+        ph[f"forces/{n}"] = oracle.interior(n, ref.get(n))
+    ref.phase2()
+    for n in oracle.FACE_NAMES:
+        ph[f"phase2/{n}"] = oracle.interior(n, ref.get(n))
+    np.savez_compressed(os.path.join(HERE, "phases.npz"), params=json.dumps(p3), state_seed=5, **ph)
+
+    # 4. digests of longer runs
+    dig = {}
+    for (C, steps, re_b, seed) in (((64, 32, 32), 100, 2800.0, 12345), ((33, 17, 9), 50, 2800.0, 99)):
+        pp = oracle.channel_params(*C, re_b=re_b, seed=seed)
+        ref = oracle.Reference(pp)
+        ref.load(oracle.channel_state(pp))
+        ref.run(steps)
+        key = f"{C[0]}x{C[1]}x{C[2]}_{steps}"
+        dig[key] = {"params": pp, "steps": steps, "dt": ref.dt, "time": ref.time, "ub": ref.last_ub,
+                    "sha256": {n: digest(oracle.interior(n, ref.get(n))) for n in CHECK},
+                    "l2": {n: float(np.linalg.norm(oracle.interior(n, ref.get(n)))) for n in CHECK}}
+    with open(os.path.join(HERE, "digests.json"), "w") as f:
+        json.dump(dig, f, indent=1, sort_keys=True)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

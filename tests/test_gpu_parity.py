@@ -1,0 +1,220 @@
+"""GPU parity: the CUDA step against the oracle, through the C ABI.
+
+FP64 bar: bit-for-bit (which implies the stated 1e-12 relative L2 per field).  Fixtures in
+tests/golden come from the reference itself; larger cases compare with the C restatement
+(pinned to the reference by tests/test_oracle.py) or use size-independent properties.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CELLS = ["roCon", "u1Con", "u2Con", "u3Con", "ronCon", "u1nCon", "u2nCon", "u3nCon"]
+FACES = ["p1", "ro1", "u11", "u21", "u31", "p2", "ro2", "u12", "u22", "u32", "p3", "ro3", "u13", "u23", "u33"]
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint64), np.ascontiguousarray(b).view(np.uint64))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def rel_l2(a, b):
+    n = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (n if n > 0 else 1.0)
+
+
+def params_from(ark, p, **kw):
+    return ark.make_params(p["C1"], p["C2"], p["C3"], re_b=1.0 / p["nu"], sound=p["sound"], rho0=p["rho0"],
+                           cfl=p["cfl"], lx=p["lx"], ly=p["ly"], lz=p["lz"], ub=p["ub"], **kw)
+
+
+def test_step_pieces_match_reference_bitwise(ark, port):
+    """Each of ark_time_step_size / ark_phase1 / ark_stress_tensor / ark_use_forces /
+    ark_phase2, called once in the reference's order, against the reference's own output."""
+    from make_golden import perturbed_state
+
+    g = np.load(os.path.join(GOLD, "phases.npz"))
+    p = json.loads(str(g["params"]))
+    with ark.Context(params_from(ark, p, forcing=False, keep_stress=True)) as ctx:
+        ctx.upload(perturbed_state(p, int(g["state_seed"])))
+        ctx.time_step_size()
+        assert ctx.scalars().dt == float(g["dt"])
+        ctx.phase1()
+        st = ctx.download(CELLS)
+        for n in CELLS:
+            assert bits_equal(port.interior(n, st[n]), g[f"phase1/{n}"]), n
+        ctx.stress_tensor()
+        for n in ("f1", "f2", "f3"):
+            assert bits_equal(port.interior(n, ctx.get(n, face=False)), g[f"stress/{n}"]), n
+        for m in "123":
+            for d in "123":
+                assert bits_equal(ctx.get(f"sigm{m}{d}", face=True), g[f"stress/sigm{m}{d}"]), (m, d)
+        ctx.use_forces()
+        st = ctx.download(["u1nCon", "u2nCon", "u3nCon"])
+        for n in ("u1nCon", "u2nCon", "u3nCon"):
+            assert bits_equal(port.interior(n, st[n]), g[f"forces/{n}"]), n
+        ctx.phase2()
+        st = ctx.download(FACES)
+        for n in FACES:
+            assert bits_equal(port.interior(n, st[n]), g[f"phase2/{n}"]), n
+
+
+def test_fused_step_matches_reference_small(ark, port):
+    g = np.load(os.path.join(GOLD, "small_run.npz"))
+    p = json.loads(str(g["params"]))
+    with ark.Context(params_from(ark, p)) as ctx:
+        ctx.upload(port.channel_state(p))
+        ctx.step(int(g["steps"]))
+        ctx.sync()
+        sc = ctx.scalars()
+        assert sc.dt == float(g["dt"]) and sc.time == float(g["time"]) and sc.nstep == int(g["steps"])
+        assert sc.bulk_velocity == float(g["ub"]) and sc.bulk_force == float(g["G"])
+        st = ctx.download(CELLS + FACES)
+        for n in CELLS + FACES:
+            assert bits_equal(port.interior(n, st[n]), g[n]), n
+
+
+@pytest.mark.parametrize("key", ["33x17x9_50", "64x32x32_100"])
+def test_fused_step_matches_reference_digests(ark, port, key):
+    """BASELINE's parity case (64x32x32, Re_b 2800, 100 steps) and an odd-sized grid: every
+    interior array bit-identical to the reference (sha256), so rel. L2 = 0 <= 1e-12."""
+    with open(os.path.join(GOLD, "digests.json")) as f:
+        d = json.load(f)[key]
+    p = d["params"]
+    with ark.Context(params_from(ark, p)) as ctx:
+        ctx.upload(port.channel_state(p))
+        ctx.step(d["steps"])
+        ctx.sync()
+        sc = ctx.scalars()
+        assert sc.dt == d["dt"] and sc.time == d["time"] and sc.bulk_velocity == d["ub"]
+        st = ctx.download(CELLS + FACES)
+        for n in CELLS + FACES:
+            a = port.interior(n, st[n])
+            assert sha(a) == d["sha256"][n], (n, np.linalg.norm(a), d["l2"][n])
+
+
+def test_per_phase_api_equals_fused_step(ark, port):
+    """The reference-order calls (main.cpp:82-91) through the C ABI give the same bits as the
+    fused graph step."""
+    p = port.channel_params(20, 10, 12, seed=8)
+    st0 = port.channel_state(p)
+    with ark.Context(params_from(ark, p)) as a:
+        a.upload(st0)
+        a.step(5)
+        fused = a.download(CELLS + FACES)
+    with ark.Context(params_from(ark, p)) as b:
+        b.upload(st0)
+        for _ in range(5):
+            b.time_step_size()
+            b.phase1()
+            b.stress_tensor()
+            b.use_forces()
+            b.phase2()
+            b.phase1()
+            b.use_forces()
+        phased = b.download(CELLS + FACES)
+    for n in CELLS + FACES:
+        assert bits_equal(port.interior(n, fused[n]), port.interior(n, phased[n])), n
+
+
+@pytest.mark.parametrize("C,steps", [((128, 64, 64), 6), ((256, 128, 128), 2)])
+def test_fused_step_matches_oracle_large(ark, port, C, steps):
+    """Full-size grids (256x128x128 is BASELINE's GPU parity grid) against the C restatement
+    for a few steps, bit for bit."""
+    p = port.channel_params(*C, re_b=5600.0, seed=2024)
+    st0 = port.channel_state(p)
+    o = port.Port(p)
+    o.load(st0)
+    o.run(steps)
+    with ark.Context(params_from(ark, p)) as ctx:
+        ctx.upload(st0)
+        ctx.step(steps)
+        ctx.sync()
+        st = ctx.download(CELLS + FACES)
+    assert ctx is not None
+    for n in CELLS + FACES:
+        a, b = port.interior(n, st[n]), port.interior(n, o.get(n))
+        assert bits_equal(a, b), (n, rel_l2(a, b))
+
+
+def test_long_run_properties(ark, port):
+    """Size-independent properties over many steps at 256x128x128: finite state, mass
+    conserved to round-off, bulk velocity held by the forcing, periodic faces identical."""
+    p = port.channel_params(256, 128, 128, re_b=5600.0, seed=5)
+    with ark.Context(params_from(ark, p)) as ctx:
+        ctx.upload(port.channel_state(p))
+        m0 = ctx.sums().mass
+        ctx.step(200)
+        ctx.sync()
+        s = ctx.sums()
+        assert abs(s.mass - m0) / m0 < 1e-9
+        sc = ctx.scalars()
+        assert sc.nstep == 200 and abs(sc.bulk_velocity - 1.0) < 1e-3
+        u11 = ctx.get("u11")
+        assert bits_equal(u11[1:-2, 1:-2, 1], u11[1:-2, 1:-2, 257])
+        u33 = ctx.get("u33")
+        assert bits_equal(u33[1, 1:-2, 1:-2], u33[129, 1:-2, 1:-2])
+        assert np.isfinite(ctx.get("u1nCon", face=False)).all()
+
+
+def test_nonfinite_is_reported(ark, port):
+    """A NaN placed in the uploaded state (host-side fault injection) is reported by
+    ark_sync as ARK_ERR_NONFINITE; the context stays usable."""
+    p = port.channel_params(16, 8, 8, seed=1)
+    st = port.channel_state(p)
+    st["u1nCon"][4, 4, 4] = np.nan
+    st["u1Con"][4, 4, 4] = np.nan
+    with ark.Context(params_from(ark, p)) as ctx:
+        ctx.upload(st)
+        ctx.step(2)
+        with pytest.raises(ark.ArkError) as e:
+            ctx.sync()
+        assert e.value.status == 3
+        ctx.upload(port.channel_state(p))
+        ctx.step(1)
+
+
+def test_boundary_fill_semantics(ark, port):
+    """ark_boundary_fill mirrors BoundaryConditions::alongX1/2/3 on the nCon level:
+    x zero-gradient, y no-slip (u = 0, ro zero-gradient), z periodic copy."""
+    p = port.channel_params(8, 6, 5, seed=3)
+    st = port.channel_state(p)
+    with ark.Context(params_from(ark, p)) as ctx:
+        ctx.upload(st)
+        for ax in (1, 2, 3):
+            ctx.boundary_fill(ax)
+        out = ctx.download(["u1nCon", "ronCon"])
+    u, r = out["u1nCon"], out["ronCon"]
+    assert bits_equal(u[1:-1, 1:-1, 0], u[1:-1, 1:-1, 1]) and bits_equal(u[1:-1, 1:-1, 9], u[1:-1, 1:-1, 8])
+    assert (u[1:-1, 0, 1:-1] == 0).all() and (u[1:-1, 7, 1:-1] == 0).all()
+    assert bits_equal(r[1:-1, 0, 1:-1], r[1:-1, 1, 1:-1])
+    assert bits_equal(u[0, 1:-1, 1:-1], u[5, 1:-1, 1:-1]) and bits_equal(u[6, 1:-1, 1:-1], u[1, 1:-1, 1:-1])
+
+
+def test_fp32_path_error_vs_fp64(ark, port):
+    """FP32 storage/arithmetic (FP64 reductions): field error vs the FP64 GPU path, and the
+    mean u(y) profile error, after 100 steps of the 64x32x32 channel."""
+    p = port.channel_params(64, 32, 32, seed=12345)
+    st0 = port.channel_state(p)
+    res = {}
+    for prec in (ark.FP64, ark.FP32):
+        with ark.Context(params_from(ark, p, precision=prec)) as ctx:
+            ctx.upload(st0)
+            ctx.step(100)
+            ctx.sync()
+            res[prec] = ctx.download(["ronCon", "u1nCon", "u2nCon", "u3nCon"])
+    for n in ("ronCon", "u1nCon", "u2nCon", "u3nCon"):
+        a, b = port.interior(n, res[ark.FP32][n]), port.interior(n, res[ark.FP64][n])
+        tol = 1e-7 if n == "ronCon" else 1e-3
+        assert rel_l2(a, b) < tol, (n, rel_l2(a, b))
+    prof32 = port.interior("u1nCon", res[ark.FP32]["u1nCon"]).mean(axis=(0, 2))
+    prof64 = port.interior("u1nCon", res[ark.FP64]["u1nCon"]).mean(axis=(0, 2))
+    assert np.abs(prof32 - prof64).max() < 1e-3

@@ -1,0 +1,157 @@
+"""The oracle (C restatement of the reference step) against the reference's own outputs.
+
+The golden fixtures under tests/golden were produced by the reference's source/main.cpp
+compiled in place (tests/golden/make_golden.py); the live comparison runs only where the
+reference sources exist.  Everything here is CPU-only.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CELLS = ["roCon", "u1Con", "u2Con", "u3Con", "ronCon", "u1nCon", "u2nCon", "u3nCon"]
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint64), np.ascontiguousarray(b).view(np.uint64))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_port_matches_golden_small_run(port):
+    g = np.load(os.path.join(GOLD, "small_run.npz"))
+    p = json.loads(str(g["params"]))
+    o = port.Port(p)
+    o.load(port.channel_state(p))
+    o.run(int(g["steps"]))
+    assert o.dt == float(g["dt"]) and o.time == float(g["time"]) and o.last_ub == float(g["ub"])
+    for n in CELLS + list(port.FACE_NAMES):
+        assert bits_equal(port.interior(n, o.get(n)), g[n]), n
+
+
+def test_port_matches_golden_bounded_edges(port):
+    """Bounded x (inflow/outflow invariants, main.cpp:1731-1745) and zero-gradient z."""
+    g = np.load(os.path.join(GOLD, "small_bounded.npz"))
+    p = json.loads(str(g["params"]))
+    o = port.Port(p, periodic_x=False, periodic_z=False)
+    o.load(port.channel_state(p))
+    o.run(int(g["steps"]))
+    assert o.dt == float(g["dt"])
+    for n in CELLS + list(port.FACE_NAMES):
+        assert bits_equal(port.interior(n, o.get(n)), g[n]), n
+
+
+def test_port_matches_golden_step_pieces(port):
+    from make_golden import perturbed_state
+
+    g = np.load(os.path.join(GOLD, "phases.npz"))
+    p = json.loads(str(g["params"]))
+    o = port.Port(p, forcing=False)
+    o.load(perturbed_state(p, int(g["state_seed"])))
+    o.time_step_size()
+    assert o.dt == float(g["dt"])
+    o.phase1()
+    for n in CELLS:
+        assert bits_equal(port.interior(n, o.get(n)), g[f"phase1/{n}"]), n
+    o.stress_tensor()
+    for n in ("f1", "f2", "f3"):
+        assert bits_equal(port.interior(n, o.get(n)), g[f"stress/{n}"]), n
+    for m in "123":
+        for d in "123":
+            assert bits_equal(o.get(f"sigm{m}{d}"), g[f"stress/sigm{m}{d}"]), (m, d)
+    o.use_forces()
+    for n in ("u1nCon", "u2nCon", "u3nCon"):
+        assert bits_equal(port.interior(n, o.get(n)), g[f"forces/{n}"]), n
+    o.phase2()
+    for n in port.FACE_NAMES:
+        assert bits_equal(port.interior(n, o.get(n)), g[f"phase2/{n}"]), n
+
+
+@pytest.mark.parametrize("key", ["33x17x9_50", "64x32x32_100"])
+def test_port_matches_golden_digests(port, key):
+    with open(os.path.join(GOLD, "digests.json")) as f:
+        d = json.load(f)[key]
+    p = d["params"]
+    o = port.Port(p)
+    o.load(port.channel_state(p))
+    o.run(d["steps"])
+    assert o.dt == d["dt"] and o.time == d["time"] and o.last_ub == d["ub"]
+    for n, h in d["sha256"].items():
+        assert sha(port.interior(n, o.get(n))) == h, n
+
+
+def test_port_thread_count_invariance(port):
+    """Only order-independent reductions: 1 thread and many threads agree bit for bit."""
+    p = port.channel_params(20, 12, 10, seed=4)
+    st = port.channel_state(p)
+    a = port.Port(p, threads=1)
+    a.load(st)
+    a.run(6)
+    ra = {n: a.get(n) for n in CELLS}
+    b = port.Port(p, threads=4)
+    b.load(st)
+    b.run(6)
+    for n in CELLS:
+        assert bits_equal(port.interior(n, b.get(n)), port.interior(n, ra[n])), n
+    port.Port.lib().aor_set_threads(os.cpu_count() or 1)
+
+
+def test_port_conserves_mass(port):
+    p = port.channel_params(24, 16, 8, seed=9)
+    o = port.Port(p)
+    o.load(port.channel_state(p))
+    m0 = port.interior("ronCon", o.get("ronCon")).sum()
+    o.run(30)
+    m1 = port.interior("ronCon", o.get("ronCon")).sum()
+    assert abs(m1 - m0) / m0 < 1e-13
+
+
+def test_port_periodic_faces_consistent(port):
+    """With periodic x and z, face 1 and face C+1 carry identical values."""
+    p = port.channel_params(16, 8, 12, seed=2)
+    o = port.Port(p)
+    o.load(port.channel_state(p))
+    o.run(10)
+    u11 = o.get("u11")
+    assert bits_equal(u11[1:-2, 1:-2, 1], u11[1:-2, 1:-2, p["C1"] + 1])
+    u13 = o.get("u13")
+    assert bits_equal(u13[1, 1:-2, 1:-2], u13[p["C3"] + 1, 1:-2, 1:-2])
+
+
+def test_port_matches_live_reference(port):
+    """Where the reference sources exist, the compiled reference and the port agree on a
+    fresh configuration (odd sizes, forcing on)."""
+    port.build(port=False)
+    if not port.Reference.available():
+        pytest.skip("reference sources not present on this machine")
+    p = port.channel_params(13, 7, 5, re_b=1500.0, seed=31, amp=0.13)
+    st = port.channel_state(p)
+    r = port.Reference(p)
+    r.load(st)
+    r.run(12)
+    o = port.Port(p)
+    o.load(st)
+    o.run(12)
+    assert r.dt == o.dt
+    for n in CELLS + list(port.FACE_NAMES):
+        assert bits_equal(port.interior(n, r.get(n)), port.interior(n, o.get(n))), n
+
+
+def test_channel_init_matches_library(port, ark):
+    """The numpy channel init (oracle side) and ark_channel_init (library side) agree."""
+    p = ark.make_params(9, 6, 5)
+    st = ark.channel_init(p, seed=77, amp=0.12)
+    ref = port.channel_state(port.channel_params(9, 6, 5, seed=77, amp=0.12))
+    for n in ark.STATE_FIELDS:
+        assert bits_equal(st[n], ref[n]), n
+
+
+def test_splitmix64_known_values(port):
+    # splitmix64 seeded with 0: published first outputs of the generator
+    v = port.splitmix64(0, 3)
+    assert [int(x) for x in v] == [0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4, 0x06C45D188009454F]
