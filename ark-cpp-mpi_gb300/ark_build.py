@@ -7,6 +7,7 @@ Translation units are compiled in parallel:
   ark_fp64.cu  FP64 kernels, --fmad=false (bit parity with the reference's FP64 rounding)
   ark_fp32.cu  FP32 kernels, FMA contraction on
   ark_api.cu   C ABI, context, CUDA-graph step
+  ark_noalloc.cu  conservation sums over caller-owned device arrays, static scratch (--fmad=false)
   ark_host.cpp host-only helpers (seeded channel init)
 Outputs go to ark-cpp-mpi_gb300/lib/ (git-ignored).
 """
@@ -65,6 +66,8 @@ def build(force=False, verbose=False):
         [nv] + common + ["--fmad=false", "-c", os.path.join(SRC, "ark_fp64.cu"), "-o", os.path.join(OBJ, "ark_fp64.o")],
         [nv] + common + ["--fmad=true", "-c", os.path.join(SRC, "ark_fp32.cu"), "-o", os.path.join(OBJ, "ark_fp32.o")],
         [nv] + common + ["-c", os.path.join(SRC, "ark_api.cu"), "-o", os.path.join(OBJ, "ark_api.o")],
+        [nv] + common + ["--fmad=false", "-c", os.path.join(SRC, "ark_noalloc.cu"), "-o",
+                         os.path.join(OBJ, "ark_noalloc.o")],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-c",
          os.path.join(SRC, "ark_host.cpp"), "-o", os.path.join(OBJ, "ark_host.o")],
         ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-c",
@@ -85,7 +88,7 @@ def build(force=False, verbose=False):
     if failed:
         msg = "\n".join(" ".join(c) + "\n" + o for c, o in failed)
         raise RuntimeError("build failed:\n" + msg)
-    objs = [os.path.join(OBJ, n) for n in ("ark_fp64.o", "ark_fp32.o", "ark_api.o", "ark_host.o")]
+    objs = [os.path.join(OBJ, n) for n in ("ark_fp64.o", "ark_fp32.o", "ark_api.o", "ark_noalloc.o", "ark_host.o")]
     subprocess.run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static"], check=True)
     subprocess.run(["g++", "-o", RUN, os.path.join(OBJ, "ark_run.o"), "-L", OUT, "-lark_gb300",
                     "-Wl,-rpath,$ORIGIN"], check=True)

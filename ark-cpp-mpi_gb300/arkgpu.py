@@ -29,7 +29,8 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_time_step_size", "ark_phase1", "ark_stress_tensor", "ark_use_forces", "ark_phase2",
            "ark_boundary_fill", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
            "ark_get_scalars", "ark_set_scalars", "ark_conservation_sums", "ark_channel_init",
-           "ark_kernel_times", "ark_kernel_name", "ark_alloc_host_state", "ark_free_host_state")
+           "ark_kernel_times", "ark_kernel_name", "ark_alloc_host_state", "ark_free_host_state",
+           "ark_conservation_sums_noalloc")
 
 
 class ArkError(RuntimeError):
@@ -106,6 +107,8 @@ def lib():
         L.ark_kernel_name.argtypes = [ctypes.c_int]
         L.ark_alloc_host_state.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(HostState)]
         L.ark_free_host_state.argtypes = [ctypes.POINTER(HostState)]
+        L.ark_conservation_sums_noalloc.argtypes = [ctypes.POINTER(Params)] + [ctypes.c_void_p] * 5 + [
+            ctypes.POINTER(Sums)]
         _lib = L
     return _lib
 

@@ -190,6 +190,21 @@ int ark_conservation_sums(ark_ctx *ctx, ark_sums *out);
  * "Con" starts equal to "nCon".  Fills every array of *out (caller-allocated). */
 int ark_channel_init(const ark_params *params, uint64_t seed, double amp, ark_host_state *out);
 
+/* Conservation sums (the same fixed-point sums as ark_conservation_sums) of FP64 DEVICE
+ * arrays that the caller owns, in Arr3d cell layout: ro, u1, u2, u3 and condition, each
+ * (C1+2)(C2+2)(C3+2) doubles, cells with condition == 0 summed.  No counterpart in the
+ * reference.  It allocates nothing, for callers that cannot allocate device memory at this
+ * point (their memory is held by a full grid or by another framework's pool, and a
+ * cudaMalloc/cudaFree would synchronize the device or fail); it needs no ark_ctx.
+ * Limit: at most 67,108,864 interior cells (larger grids return ARK_ERR_PARAM).  Scratch is
+ * one static 66,048-byte device array per GPU, kept until exit and shared by all calls:
+ * calls that overlap on the GPU race.  Runs on the current device's legacy default stream
+ * and waits for the result.  The first call on a device looks up the scratch address, so
+ * make it before any stream capture. */
+int ark_conservation_sums_noalloc(const ark_params *params, const double *ro, const double *u1,
+                                  const double *u2, const double *u3, const double *condition,
+                                  ark_sums *out);
+
 /* Allocates every array of a host state in page-locked memory (zero-filled), sized for
  * params; ark_free_host_state releases them.  Either works without ark_create. */
 int ark_alloc_host_state(const ark_params *params, ark_host_state *out);
