@@ -102,10 +102,9 @@ Consts make_consts(const ark_params &p) {
 }
 
 // The launches of one fused step, in order (ark_kernel_times reports them in this order).
-const char *const kStepKernels[] = {"reduce_start", "finalize_dt", "wrap_con",    "phase1_stress_forces",
-                                    "wrap_phase2",  "sweep_x1",    "sweep_x2",    "sweep_x3",
-                                    "phase1_forces"};
-constexpr int kNumStepKernels = 9;
+const char *const kStepKernels[] = {"finalize_dt", "wrap_con", "phase1_stress_forces", "wrap_phase2",
+                                    "sweep_x1",    "sweep_x2", "sweep_x3",             "phase1_forces"};
+constexpr int kNumStepKernels = 8;
 
 // Precision-independent engine interface.
 struct Engine {
@@ -114,12 +113,15 @@ struct Engine {
     virtual int upload_field(int which, int face, const double *host) = 0;
     virtual int download_field(int which, int face, double *host) = 0;
     virtual void *field_ptr(const char *name, int *face) = 0;
+    virtual int download_raw(void *p, size_t n, double *host) = 0;
+    virtual int upload_raw(void *p, size_t n, const double *host) = 0;
     virtual void time_step_size(int con, int advance) = 0;
-    virtual void phase1(int src, int dst, int mode) = 0;
+    virtual void reduce(int con) = 0;
+    virtual void phase1(int src, int dst, int fcur, int mode) = 0;
     virtual void stress(int con, int bulk) = 0;
     virtual void use_forces(int ncon) = 0;
-    virtual void phase2(int con) = 0;
-    virtual void step(int con, cudaEvent_t *ev) = 0;
+    virtual void phase2(int con, int fcur) = 0;
+    virtual void step(int con, int fcur, cudaEvent_t *ev) = 0;
     virtual void boundary_fill(int ncon, int axis, int periodic) = 0;
     virtual void sums(int ncon) = 0;
     virtual DevScalars *scalars() = 0;
@@ -135,9 +137,11 @@ struct ark_ctx {
     cudaStream_t st = nullptr;
     std::unique_ptr<Engine> eng;
     std::vector<double> cond_host;
-    int con = 0; // the level index holding "Con"
+    int con = 0;  // the cell level holding "Con"
+    int fcur = 0; // the current face generation
     bool uploaded = false;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool parts_valid = false; // the dt / bulk-flow partials describe the current state
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [con][fcur]
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double *stage = nullptr; // device double staging for FP32 contexts
 };
@@ -176,17 +180,23 @@ template <class T> struct EngineT : Engine {
             rc |= get(&S.lv[l].u3, nc);
         }
         for (int m = 0; m < 3; ++m) rc |= get(&S.f[m], nc);
-        for (int d = 0; d < 3; ++d) {
-            rc |= get(&S.fc[d].p, nf);
-            rc |= get(&S.fc[d].ro, nf);
-            for (int m = 0; m < 3; ++m) rc |= get(&S.fc[d].u[m], nf);
+        for (int gen = 0; gen < 2; ++gen)
+            for (int d = 0; d < 3; ++d) {
+                FaceSet<T> &F = S.fc[gen][d];
+                rc |= get(&F.p, nf);
+                if (Storage<T>::deviation) F.ro = nullptr; // derived from p
+                else rc |= get(&F.ro, nf);
+                for (int m = 0; m < 3; ++m) rc |= get(&F.u[m], nf);
+            }
+        for (int d = 0; d < 3; ++d)
             for (int m = 0; m < 3; ++m) {
                 if (ctx->P.keep_stress) rc |= get(&S.sig[d][m], nf);
                 else S.sig[d][m] = nullptr;
             }
-        }
         rc |= get(&S.flags, nc);
         rc |= get(&S.sc, 1);
+        rc |= get(&S.part_max, 3 * (size_t)tile_count(S.g));
+        rc |= get(&S.part_sum, (size_t)tile_count(S.g));
         if (rc) return ARK_ERR_NOMEM;
         return ARK_OK;
     }
@@ -207,42 +217,61 @@ template <class T> struct EngineT : Engine {
         }
         if (which >= 9 && which < 24) {
             const int d = (which - 9) / 5, v = (which - 9) % 5;
-            FaceSet<T> &F = S.fc[d];
+            FaceSet<T> &F = S.fc[ctx->fcur][d];
             return v == 0 ? F.p : v == 1 ? F.ro : F.u[v - 2];
         }
         return nullptr;
     }
 
-    int copy_in(T *dev, const double *host, size_t n) {
+    // FP64: plain copies.  FP32: through the double staging buffer, density fields shifted
+    // by ro0 (the device holds rho - ro0).
+    int copy_in(T *dev, const double *host, size_t n, double offset) {
         if (sizeof(T) == sizeof(double)) {
             ARK_CUDA(cudaMemcpy(dev, host, n * sizeof(double), cudaMemcpyHostToDevice));
         } else {
             ARK_CUDA(cudaMemcpy(ctx->stage, host, n * sizeof(double), cudaMemcpyHostToDevice));
-            convert_from_double<T>(dev, ctx->stage, (int64_t)n, ctx->st);
+            convert_from_double<T>(dev, ctx->stage, (int64_t)n, offset, ctx->st);
             ARK_CUDA(cudaStreamSynchronize(ctx->st));
         }
         return ARK_OK;
     }
 
-    int copy_out(double *host, const T *dev, size_t n) {
+    int copy_out(double *host, const T *dev, size_t n, double offset) {
         if (sizeof(T) == sizeof(double)) {
             ARK_CUDA(cudaMemcpy(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost));
         } else {
-            convert_to_double<T>(ctx->stage, dev, (int64_t)n, ctx->st);
+            convert_to_double<T>(ctx->stage, dev, (int64_t)n, offset, ctx->st);
             ARK_CUDA(cudaStreamSynchronize(ctx->st));
             ARK_CUDA(cudaMemcpy(host, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost));
         }
         return ARK_OK;
     }
 
+    static bool is_cell_density(int which) { return which == 0 || which == 4; }
+    static bool is_face_density(int which) { return which >= 9 && which < 24 && (which - 9) % 5 == 1; }
+
     int upload_field(int which, int face, const double *host) override {
         const size_t n = face ? (size_t)S.g.nface() : (size_t)S.g.ncell();
-        return copy_in(dev_of(which), host, n);
+        if (Storage<T>::deviation && is_face_density(which)) return ARK_OK; // derived from p
+        const double off = (Storage<T>::deviation && is_cell_density(which)) ? ctx->P.ro0 : 0.0;
+        return copy_in(dev_of(which), host, n, off);
     }
     int download_field(int which, int face, double *host) override {
         const size_t n = face ? (size_t)S.g.nface() : (size_t)S.g.ncell();
-        return copy_out(host, dev_of(which), n);
+        if (Storage<T>::deviation && is_face_density(which)) {
+            const int d = (which - 9) / 5;
+            face_density_to_double<T>(ctx->stage, S.fc[ctx->fcur][d].p, (int64_t)n, ctx->k.ro0, ctx->k.rc2, ctx->st);
+            ARK_CUDA(cudaStreamSynchronize(ctx->st));
+            ARK_CUDA(cudaMemcpy(host, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost));
+            return ARK_OK;
+        }
+        const double off = (Storage<T>::deviation && is_cell_density(which)) ? ctx->P.ro0 : 0.0;
+        return copy_out(host, dev_of(which), n, off);
     }
+    int download_raw(void *p, size_t n, double *host) override {
+        return copy_out(host, (const T *)p, n, 0.0);
+    }
+    int upload_raw(void *p, size_t n, const double *host) override { return copy_in((T *)p, host, n, 0.0); }
 
     void *field_ptr(const char *name, int *face) override {
         for (int w = 0; w < 24; ++w)
@@ -263,10 +292,13 @@ template <class T> struct EngineT : Engine {
     }
 
     void time_step_size(int con, int advance) override {
-        Launch<T>::reduce_start(S, con, ctx->k.forcing, ctx->st);
+        Launch<T>::reduce_start(S, con, ctx->st);
         Launch<T>::finalize_dt(S, advance, ctx->st);
     }
-    void phase1(int src, int dst, int mode) override { Launch<T>::phase1(S, src, dst, mode, ctx->st); }
+    void reduce(int con) override { Launch<T>::reduce_start(S, con, ctx->st); }
+    void phase1(int src, int dst, int fcur, int mode) override {
+        Launch<T>::phase1(S, src, dst, fcur, mode, ctx->st);
+    }
     void stress(int con, int bulk) override {
         T *u[3] = {S.lv[con].u1, S.lv[con].u2, S.lv[con].u3};
         Launch<T>::wrap_cells(S, u, 3, ctx->st);
@@ -278,35 +310,34 @@ template <class T> struct EngineT : Engine {
         Launch<T>::stress(S, con, bulk, ctx->st);
     }
     void use_forces(int ncon) override { Launch<T>::use_forces(S, ncon, ctx->st); }
-    void phase2(int con) override {
-        Launch<T>::wrap_phase2(S, con, ctx->st);
-        for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, con, ax, ctx->st);
+    void phase2(int con, int fcur) override {
+        Launch<T>::wrap_phase2(S, con, fcur, ctx->st);
+        for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, con, fcur, ax, ctx->st);
     }
-    // One full step of main.cpp:82-91 with "Con" = level x at entry and exit.  With ev
-    // given, an event is recorded after each of the kStepKernels launches.
-    void step(int x, cudaEvent_t *ev) override {
+    // One full step of main.cpp:82-91 with "Con" = level x at entry and exit, reading the
+    // dt / bulk-flow partials of the current state and leaving those of the next one.  With
+    // ev given, an event is recorded after each of the kStepKernels launches.
+    void step(int x, int fcur, cudaEvent_t *ev) override {
         const int y = x ^ 1;
         cudaStream_t st = ctx->st;
         auto mark = [&](int q) {
             if (ev) cudaEventRecord(ev[q], st);
         };
-        Launch<T>::reduce_start(S, x, ctx->k.forcing, st);
-        mark(0);
         Launch<T>::finalize_dt(S, 1, st);
-        mark(1);
+        mark(0);
         T *cells[4] = {S.lv[y].u1, S.lv[y].u2, S.lv[y].u3, S.lv[y].ro};
         Launch<T>::wrap_cells(S, cells, 4, st);
+        mark(1);
+        Launch<T>::phase1(S, y, x, fcur, P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0), st);
         mark(2);
-        Launch<T>::phase1(S, y, x, P1_STRESS | P1_FORCES | (ctx->k.forcing ? P1_BULK : 0), st);
+        Launch<T>::wrap_phase2(S, y, fcur, st);
         mark(3);
-        Launch<T>::wrap_phase2(S, y, st);
-        mark(4);
         for (int ax = 0; ax < 3; ++ax) {
-            Launch<T>::sweep(S, y, ax, st);
-            mark(5 + ax);
+            Launch<T>::sweep(S, y, fcur, ax, st);
+            mark(4 + ax);
         }
-        Launch<T>::phase1(S, x, y, P1_FORCES, st);
-        mark(8);
+        Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, st);
+        mark(7);
     }
     void boundary_fill(int ncon, int axis, int periodic) override {
         Launch<T>::boundary_fill(S, ncon, axis, periodic, ctx->st);
@@ -320,8 +351,8 @@ int check_params(const ark_params *p) {
     if (!p) return fail(ARK_ERR_PARAM, "params is NULL");
     if (p->n1_cells < 2 || p->n2_cells < 1 || p->n3_cells < 2)
         return fail(ARK_ERR_PARAM, "need at least 2 x 1 x 2 cells");
-    const double cells = (double)p->n1_cells * p->n2_cells * p->n3_cells;
-    if (cells > 2.0e9) return fail(ARK_ERR_PARAM, "grid too large");
+    const double faces = (double)(p->n1_cells + 3) * (p->n2_cells + 3) * (p->n3_cells + 3);
+    if (faces >= 2147483647.0) return fail(ARK_ERR_PARAM, "grid too large: arrays are indexed with 32 bits");
     if (!(p->lx > 0) || !(p->ly > 0) || !(p->lz > 0)) return fail(ARK_ERR_PARAM, "domain extents must be > 0");
     if (!(p->sound > 0) || !(p->ro0 > 0) || !(p->cfl > 0) || !(p->vis >= 0))
         return fail(ARK_ERR_PARAM, "sound, ro0, cfl must be > 0 and vis >= 0");
@@ -406,8 +437,9 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
 int ark_destroy(ark_ctx *ctx) {
     if (!ctx) return ARK_OK;
     cudaStreamSynchronize(ctx->st);
-    for (int q = 0; q < 2; ++q)
-        if (ctx->graph[q]) cudaGraphExecDestroy(ctx->graph[q]);
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            if (ctx->graph[a][b]) cudaGraphExecDestroy(ctx->graph[a][b]);
     ctx->eng.reset();
     if (ctx->stage) cudaFree(ctx->stage);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -425,6 +457,8 @@ int ark_upload(ark_ctx *ctx, const ark_host_state *h) {
             return fail(ARK_ERR_PARAM, std::string("host array ") + f.name + " is NULL");
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
     ctx->con = 0;
+    ctx->fcur = 0;
+    ctx->parts_valid = false;
     for (int w = 0; w < 24; ++w) {
         if (w == 8) continue;
         if (int rc = ctx->eng->upload_field(w, kFields[w].face, h->*kFields[w].member)) return rc;
@@ -483,18 +517,12 @@ int ark_get_array(ark_ctx *ctx, const char *name, double *host) {
     void *p = ctx->eng->field_ptr(name, &face);
     if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
     const size_t n = face ? (size_t)ctx->g.nface() : (size_t)ctx->g.ncell();
-    if (ctx->P.precision == ARK_FP64) {
-        ARK_CUDA(cudaMemcpy(host, p, n * sizeof(double), cudaMemcpyDeviceToHost));
-    } else {
-        convert_to_double<float>(ctx->stage, (const float *)p, (int64_t)n, ctx->st);
-        ARK_CUDA(cudaStreamSynchronize(ctx->st));
-        ARK_CUDA(cudaMemcpy(host, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost));
-    }
-    return ARK_OK;
+    return ctx->eng->download_raw(p, n, host);
 }
 
 int ark_put_array(ark_ctx *ctx, const char *name, const double *host) {
     if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->parts_valid = false;
     if (!name || !host) return fail(ARK_ERR_PARAM, "NULL name or buffer");
     if (std::strcmp(name, "condition") == 0) return fail(ARK_ERR_PARAM, "condition is set by ark_upload");
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
@@ -504,14 +532,7 @@ int ark_put_array(ark_ctx *ctx, const char *name, const double *host) {
     void *p = ctx->eng->field_ptr(name, &face);
     if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
     const size_t n = face ? (size_t)ctx->g.nface() : (size_t)ctx->g.ncell();
-    if (ctx->P.precision == ARK_FP64) {
-        ARK_CUDA(cudaMemcpy(p, host, n * sizeof(double), cudaMemcpyHostToDevice));
-    } else {
-        ARK_CUDA(cudaMemcpy(ctx->stage, host, n * sizeof(double), cudaMemcpyHostToDevice));
-        convert_from_double<float>((float *)p, ctx->stage, (int64_t)n, ctx->st);
-        ARK_CUDA(cudaStreamSynchronize(ctx->st));
-    }
-    return ARK_OK;
+    return ctx->eng->upload_raw(p, n, host);
 }
 
 int ark_time_step_size(ark_ctx *ctx) {
@@ -522,34 +543,40 @@ int ark_time_step_size(ark_ctx *ctx) {
 
 int ark_phase1(ark_ctx *ctx) {
     if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->parts_valid = false;
     // "Con" <- "nCon" is a relabelling: the old nCon level is read as Con and the new
     // nCon values are written over the old Con level.
     const int src = ctx->con ^ 1, dst = ctx->con;
-    ctx->eng->phase1(src, dst, P1_PLAIN);
+    ctx->eng->phase1(src, dst, ctx->fcur, P1_PLAIN);
     ctx->con = src;
     return launch_status(ctx);
 }
 
 int ark_stress_tensor(ark_ctx *ctx) {
     if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->parts_valid = false;
     ctx->eng->stress(ctx->con, ctx->k.forcing);
     return launch_status(ctx);
 }
 
 int ark_use_forces(ark_ctx *ctx) {
     if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->parts_valid = false;
     ctx->eng->use_forces(ctx->con ^ 1);
     return launch_status(ctx);
 }
 
 int ark_phase2(ark_ctx *ctx) {
     if (int rc = check_ctx(ctx, true)) return rc;
-    ctx->eng->phase2(ctx->con);
+    ctx->parts_valid = false;
+    ctx->eng->phase2(ctx->con, ctx->fcur);
+    ctx->fcur ^= 1; // the sweeps wrote the other face generation
     return launch_status(ctx);
 }
 
 int ark_boundary_fill(ark_ctx *ctx, int axis) {
     if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->parts_valid = false;
     if (axis < 1 || axis > 3) return fail(ARK_ERR_PARAM, "axis must be 1, 2 or 3");
     const int periodic = axis == 2 ? 0 : axis == 3 ? ctx->P.periodic_z : 0;
     ctx->eng->boundary_fill(ctx->con ^ 1, axis, periodic);
@@ -565,11 +592,11 @@ int ark_set_dt(ark_ctx *ctx, double dt) {
 
 // Captures the fused step for the current role of the two cell levels (once per role).
 static int ensure_graph(ark_ctx *ctx) {
-    const int x = ctx->con;
-    if (!ctx->graph[x]) {
+    const int x = ctx->con, fc = ctx->fcur;
+    if (!ctx->graph[x][fc]) {
         cudaGraph_t graph = nullptr;
         ARK_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-        ctx->eng->step(x, nullptr);
+        ctx->eng->step(x, fc, nullptr);
         cudaError_t le = cudaGetLastError();
         cudaError_t ce = cudaStreamEndCapture(ctx->st, &graph);
         if (le != cudaSuccess || ce != cudaSuccess) {
@@ -577,10 +604,10 @@ static int ensure_graph(ark_ctx *ctx) {
             return fail(ARK_ERR_CUDA, std::string("step capture: ") +
                                           cudaGetErrorString(le != cudaSuccess ? le : ce));
         }
-        cudaError_t ie = cudaGraphInstantiate(&ctx->graph[x], graph, 0);
+        cudaError_t ie = cudaGraphInstantiate(&ctx->graph[x][fc], graph, 0);
         cudaGraphDestroy(graph);
         if (ie != cudaSuccess) {
-            ctx->graph[x] = nullptr;
+            ctx->graph[x][fc] = nullptr;
             return fail(ARK_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
         }
     }
@@ -591,8 +618,16 @@ int ark_step(ark_ctx *ctx, int nsteps) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (nsteps < 0) return fail(ARK_ERR_PARAM, "nsteps < 0");
     if (nsteps == 0) return ARK_OK;
-    if (int rc = ensure_graph(ctx)) return rc;
-    for (int s = 0; s < nsteps; ++s) ARK_CUDA(cudaGraphLaunch(ctx->graph[ctx->con], ctx->st));
+    if (!ctx->parts_valid) {
+        ctx->eng->reduce(ctx->con);
+        ctx->parts_valid = true;
+    }
+    // each step flips the face generation; the graph of each parity is captured once
+    for (int s = 0; s < nsteps; ++s) {
+        if (int rc = ensure_graph(ctx)) return rc;
+        ARK_CUDA(cudaGraphLaunch(ctx->graph[ctx->con][ctx->fcur], ctx->st));
+        ctx->fcur ^= 1;
+    }
     return ARK_OK;
 }
 
@@ -608,7 +643,12 @@ int ark_sync(ark_ctx *ctx) {
 int ark_time_steps(ark_ctx *ctx, int nsteps, double *ms) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (!ms) return fail(ARK_ERR_PARAM, "ms is NULL");
-    if (int rc = ensure_graph(ctx)) return rc; // built outside the timed region
+    // both face-generation graphs are built outside the timed region
+    if (int rc = ensure_graph(ctx)) return rc;
+    ctx->fcur ^= 1;
+    int rc2 = ensure_graph(ctx);
+    ctx->fcur ^= 1;
+    if (rc2) return rc2;
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
     ARK_CUDA(cudaEventRecord(ctx->ev0, ctx->st));
     if (int rc = ark_step(ctx, nsteps)) return rc;
@@ -628,9 +668,14 @@ int ark_kernel_times(ark_ctx *ctx, int nsteps, double *ms, int cap, int *count) 
     for (auto &e : ev) ARK_CUDA(cudaEventCreate(&e));
     std::vector<double> acc(kNumStepKernels, 0.0);
     int rc = ARK_OK;
+    if (!ctx->parts_valid) {
+        ctx->eng->reduce(ctx->con);
+        ctx->parts_valid = true;
+    }
     for (int s = 0; s < nsteps && rc == ARK_OK; ++s) {
         cudaEventRecord(ev[0], ctx->st);
-        ctx->eng->step(ctx->con, ev.data() + 1);
+        ctx->eng->step(ctx->con, ctx->fcur, ev.data() + 1);
+        ctx->fcur ^= 1;
         if ((rc = launch_status(ctx))) break;
         if (cudaEventSynchronize(ev[kNumStepKernels]) != cudaSuccess) {
             rc = fail(ARK_ERR_CUDA, "event synchronize failed");

@@ -1,9 +1,10 @@
 // CUDA kernels of the CABARET step, templated on the storage/arithmetic type T.
 //
 // ark_fp64.cu instantiates T = double in a translation unit compiled with --fmad=false:
-// every expression below keeps the reference's operand order (source/main.cpp), so the
+// every FP64 expression below keeps the reference's operand order (source/main.cpp), so the
 // FP64 path rounds exactly like the reference built with -ffp-contract=off.
-// ark_fp32.cu instantiates T = float with FMA contraction allowed.
+// ark_fp32.cu instantiates T = float (also without FMA contraction) with the density stored as
+// the deviation rho - ro0 and face density derived from face pressure (Storage<T>).
 //
 // Kernels and the reference code they restate:
 //   k_reduce_start / k_finalize_dt   TimeStepSize (main.cpp:374-415) + bulk-flow sum
@@ -12,8 +13,10 @@
 //   k_phase1<MODE>                   Phase1 (main.cpp:417-575), optionally fused with
 //                                    StressTensor's force (main.cpp:856-1023) and
 //                                    UseForces (main.cpp:1026-1045)
-//   k_stress_faces                   StressTensor's face stresses (main.cpp:856-982)
+//   k_stress_faces / k_stress_force  StressTensor alone (main.cpp:856-1023)
+//   k_use_forces                     UseForces alone
 //   k_sweep_x, k_sweep_col<AX>       Phase2 sweeps (main.cpp:1726-2011, 2023-2255, 2261-2494)
+//   k_boundary_fill                  BoundaryConditions (source/BoundaryConditions.cpp:22-83)
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -55,14 +58,16 @@ __device__ __forceinline__ float divv(float a, float b) { return __fdiv_rn(a, b)
 
 // Run constants rounded to T.
 template <class T> struct K {
-    T dx[3], rdx[3], ds[3], dvc, vis, two_vis, sound, ro0, c2, rc2, roc, rroc;
+    T dx[3], rdx[3], ds[3], dvc, rdvc, vis, two_vis, sound, ro0, c2, rc2, roc, rroc;
     __device__ __forceinline__ explicit K(const Consts &k) {
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
             dx[d] = (T)k.dx[d];
             rdx[d] = (T)k.rdx[d];
             ds[d] = (T)k.ds[d];
         }
         dvc = (T)k.dvc;
+        rdvc = (T)(1.0 / k.dvc);
         vis = (T)k.vis;
         two_vis = (T)k.two_vis;
         sound = (T)k.sound;
@@ -105,51 +110,140 @@ __device__ __forceinline__ long long warp_sum_i64(long long v) {
     return v;
 }
 
-// Max |u_d| over interior cells of level `con` (dt is monotone in it: min over cells of
-// CFL*dx/(c + |u|) is CFL*dx/(c + max|u|) exactly, since IEEE + and / are monotone), and
-// the fixed-point sum of u1 over fluid cells of level `ncon`.  Integer max and sum are
-// order independent, so any grid gives the same bits.
+// Fixed-point image of an FP32 value for the FP32 path's bulk-flow sum: round(v * 2^16) in a
+// 32-bit integer (|v| < 2^15), NaN -> 0.  Integer sums are order independent, and nothing
+// here uses the FP64 pipe (1/64 of the FP32 rate on this part).
+__device__ __forceinline__ long long fixed16(float v) {
+    if (v != v) v = 0.f;
+    v = fminf(fmaxf(v, -32767.f), 32767.f);
+    return (long long)__float2int_rn(v * 65536.f);
+}
+__device__ __forceinline__ long long fixed_sum_term(double v) { return fixed32(v); }
+__device__ __forceinline__ long long fixed_sum_term(float v) { return fixed16(v); }
+template <class T> struct FixedScale { static constexpr double inv = 1.0 / 4294967296.0; };
+template <> struct FixedScale<float> { static constexpr double inv = 1.0 / 65536.0; };
+
+// |v| as an order-preserving integer: FP64 bit pattern, or FP32 bit pattern (widened to an
+// FP64 bit pattern once per tile, see tile_store).
+__device__ __forceinline__ unsigned long long abs_key(double v) { return abs_bits(v); }
+__device__ __forceinline__ unsigned long long abs_key(float v) { return (unsigned long long)__float_as_uint(fabsf(v)); }
+__device__ __forceinline__ unsigned long long key_to_double_bits(unsigned long long m, double) { return m; }
+__device__ __forceinline__ unsigned long long key_to_double_bits(unsigned long long m, float) {
+    return (unsigned long long)__double_as_longlong((double)__uint_as_float((unsigned)m));
+}
+
+__device__ __forceinline__ int tile_index() {
+    return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+}
+
+// Block-wide combination of the per-thread partials into this tile's slots.  Every thread of
+// the block must call it.
 template <class T>
-__global__ void __launch_bounds__(256) k_reduce_start(DevState<T> S, int con, int with_sum) {
+__device__ __forceinline__ void tile_store(const DevState<T> &S, bool do_max, bool do_sum, unsigned long long m0,
+                                           unsigned long long m1, unsigned long long m2, long long s) {
+    __shared__ unsigned long long smax[3][kTileX * kTileY / 32];
+    __shared__ long long ssum[kTileX * kTileY / 32];
+    m0 = warp_max_u64(m0);
+    m1 = warp_max_u64(m1);
+    m2 = warp_max_u64(m2);
+    s = warp_sum_i64(s);
+    const int t = threadIdx.y * blockDim.x + threadIdx.x, w = t >> 5;
+    if ((t & 31) == 0) {
+        smax[0][w] = m0;
+        smax[1][w] = m1;
+        smax[2][w] = m2;
+        ssum[w] = s;
+    }
+    __syncthreads();
+    const int tile = tile_index();
+    if (t < 3 && do_max) {
+        unsigned long long m = 0;
+        for (int v = 0; v < kTileX * kTileY / 32; ++v) m = smax[t][v] > m ? smax[t][v] : m;
+        S.part_max[3 * tile + t] = key_to_double_bits(m, T());
+    } else if (t == 3 && do_sum) {
+        long long z = 0;
+        for (int v = 0; v < kTileX * kTileY / 32; ++v) z += ssum[v];
+        S.part_sum[tile] = z;
+    }
+}
+
+// Standalone partials of the step start (used after an upload or the reference-order calls;
+// the fused step takes the same partials inside its Phase1 kernels): max |u_d| of level
+// `con` and the fixed-point sum of u1 over fluid cells of level `con^1`, tile by tile.
+// dt is monotone in max |u|: min over cells of CFL*dx/(c + |u|) is CFL*dx/(c + max|u|)
+// exactly, since IEEE + and / are monotone.  Max and integer sums are order independent.
+template <class T> __global__ void __launch_bounds__(kTileX *kTileY) k_reduce_start(DevState<T> S, int con) {
     const Geom g = S.g;
-    const Level<T> Lc = S.lv[con], Ln = S.lv[con ^ 1];
-    const int64_t n = (int64_t)g.C1 * g.C2 * g.C3;
+    const int i = blockIdx.x * kTileX + threadIdx.x + 1;
+    const int j = blockIdx.y * kTileY + threadIdx.y + 1;
+    const int k0 = blockIdx.z * kTileK + 1;
+    const int k1 = k0 + kTileK - 1 < g.C3 ? k0 + kTileK - 1 : g.C3;
+    const T *__restrict__ cu1 = S.lv[con].u1;
+    const T *__restrict__ cu2 = S.lv[con].u2;
+    const T *__restrict__ cu3 = S.lv[con].u3;
+    const T *__restrict__ nu1 = S.lv[con ^ 1].u1;
+    const uint8_t *__restrict__ fl = S.flags;
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long s = 0;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.C1) + 1;
-        const int64_t r = t / g.C1;
-        const int j = (int)(r % g.C2) + 1;
-        const int k = (int)(r / g.C2) + 1;
-        const int64_t c = g.cell(i, j, k);
-        unsigned long long b0 = abs_bits(Lc.u1[c]), b1 = abs_bits(Lc.u2[c]), b2 = abs_bits(Lc.u3[c]);
-        m0 = b0 > m0 ? b0 : m0;
-        m1 = b1 > m1 ? b1 : m1;
-        m2 = b2 > m2 ? b2 : m2;
-        if (with_sum && (S.flags[c] & FL_EQ0)) s += fixed32((double)Ln.u1[c]);
+    if (i <= g.C1 && j <= g.C2) {
+        const int cs2 = (int)g.cs2;
+        int c = g.ci(i, j, k0);
+#pragma unroll 4
+        for (int k = k0; k <= k1; ++k, c += cs2) {
+            const unsigned long long b0 = abs_key(cu1[c]), b1 = abs_key(cu2[c]), b2 = abs_key(cu3[c]);
+            m0 = b0 > m0 ? b0 : m0;
+            m1 = b1 > m1 ? b1 : m1;
+            m2 = b2 > m2 ? b2 : m2;
+            if (fl[c] & FL_EQ0) s += fixed_sum_term(nu1[c]);
+        }
+    }
+    tile_store(S, true, true, m0, m1, m2, s);
+}
+
+// One block: combine the tile partials, form dt as TimeStepSize does, then the bulk force.
+template <class T> __global__ void __launch_bounds__(1024) k_finalize_dt(DevState<T> S, int advance_time, int ntiles) {
+    __shared__ unsigned long long smax[3][32];
+    __shared__ long long ssum[32];
+    unsigned long long m0 = 0, m1 = 0, m2 = 0;
+    long long s = 0;
+    for (int q = threadIdx.x; q < ntiles; q += blockDim.x) {
+        const unsigned long long a = S.part_max[3 * q], b = S.part_max[3 * q + 1], c = S.part_max[3 * q + 2];
+        m0 = a > m0 ? a : m0;
+        m1 = b > m1 ? b : m1;
+        m2 = c > m2 ? c : m2;
+        s += S.part_sum[q];
     }
     m0 = warp_max_u64(m0);
     m1 = warp_max_u64(m1);
     m2 = warp_max_u64(m2);
     s = warp_sum_i64(s);
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        atomicMax(&S.sc->umax[0], m0);
-        atomicMax(&S.sc->umax[1], m1);
-        atomicMax(&S.sc->umax[2], m2);
-        if (with_sum && s != 0) atomicAdd((unsigned long long *)&S.sc->usum, (unsigned long long)s);
+        smax[0][w] = m0;
+        smax[1][w] = m1;
+        smax[2][w] = m2;
+        ssum[w] = s;
     }
-}
-
-// One thread: dt as TimeStepSize forms it, then the bulk force, then reset the accumulators.
-template <class T> __global__ void k_finalize_dt(DevState<T> S, int advance_time) {
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const int nw = (blockDim.x + 31) / 32;
+    for (int v = 1; v < nw; ++v) {
+        m0 = smax[0][v] > m0 ? smax[0][v] : m0;
+        m1 = smax[1][v] > m1 ? smax[1][v] : m1;
+        m2 = smax[2][v] > m2 ? smax[2][v] : m2;
+    }
+    m0 = smax[0][0] > m0 ? smax[0][0] : m0;
+    m1 = smax[1][0] > m1 ? smax[1][0] : m1;
+    m2 = smax[2][0] > m2 ? smax[2][0] : m2;
+    s = 0;
+    for (int v = 0; v < nw; ++v) s += ssum[v];
     DevScalars *sc = S.sc;
     const Consts &k = S.k;
     const unsigned long long inf_bits = 0x7FF0000000000000ull;
-    if (sc->umax[0] >= inf_bits || sc->umax[1] >= inf_bits || sc->umax[2] >= inf_bits) sc->status |= STATUS_NONFINITE;
-    const double M0 = __longlong_as_double((long long)sc->umax[0]);
-    const double M1 = __longlong_as_double((long long)sc->umax[1]);
-    const double M2 = __longlong_as_double((long long)sc->umax[2]);
+    if (m0 >= inf_bits || m1 >= inf_bits || m2 >= inf_bits) sc->status |= STATUS_NONFINITE;
+    const double M0 = __longlong_as_double((long long)m0);
+    const double M1 = __longlong_as_double((long long)m1);
+    const double M2 = __longlong_as_double((long long)m2);
     const double dtu1 = k.cfl_dx[0] / (k.sound + M0);
     const double dtu2 = k.cfl_dx[1] / (k.sound + M1);
     const double dtu3 = k.cfl_dx[2] / (k.sound + M2);
@@ -157,8 +251,7 @@ template <class T> __global__ void k_finalize_dt(DevState<T> S, int advance_time
     const double dt = min3d(1e8, dtu, k.dtv);
     sc->dt = dt;
     if (k.forcing) {
-        const double ub =
-            sc->nfluid > 0 ? ((double)sc->usum * (1.0 / 4294967296.0)) / (double)sc->nfluid : 0.0;
+        const double ub = sc->nfluid > 0 ? ((double)s * FixedScale<T>::inv) / (double)sc->nfluid : 0.0;
         sc->ub = ub;
         sc->G = (k.u_target - ub) / dt;
     }
@@ -167,8 +260,6 @@ template <class T> __global__ void k_finalize_dt(DevState<T> S, int advance_time
         sc->time += 0.5 * dt;
         sc->time += 0.5 * dt;
     }
-    sc->umax[0] = sc->umax[1] = sc->umax[2] = 0;
-    sc->usum = 0;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -218,7 +309,8 @@ template <class T> __global__ void k_wrap(Geom g, WrapJob J) {
 }
 
 // BoundaryConditions::alongX1/2/3 (source/BoundaryConditions.cpp:22-83) on one cell level,
-// without the temperature.  axis 1: zero-gradient; axes 2, 3: periodic copy or no-slip.
+// without the temperature.  axis 1: zero-gradient; axes 2, 3: periodic copy or no-slip
+// (u = 0, density zero-gradient).  Copies are the same for rho and for rho - ro0.
 template <class T> __global__ void k_boundary_fill(Geom g, Level<T> L, int axis, int periodic) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     T *a[4] = {L.u1, L.u2, L.u3, L.ro};
@@ -252,6 +344,8 @@ template <class T> __global__ void k_boundary_fill(Geom g, Level<T> L, int axis,
     }
 }
 
+constexpr int kCellBX = 64, kCellBY = 2; // block shape of the one-cell-per-thread kernels
+
 // ---------------------------------------------------------------------------------------
 // viscous stress on one face (main.cpp:856-982), component by component
 // ---------------------------------------------------------------------------------------
@@ -264,49 +358,82 @@ __device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const 
     return (T)0;
 }
 
-// ---------------------------------------------------------------------------------------
-// Phase1 (+ stress force, bulk force, UseForces)
-// ---------------------------------------------------------------------------------------
-
-// src: the level read as "Con" (the previous "nCon"); dst: the level written as "nCon".
-template <class T, int MODE>
-__global__ void __launch_bounds__(128) k_phase1(DevState<T> S, int src, int dst) {
-    const Geom g = S.g;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > g.C1 || j > g.C2) return;
-    const K<T> kk(S.k);
-    const T dt = (T)S.sc->dt;
-    const Level<T> Ls = S.lv[src], Ld = S.lv[dst];
-    const int64_t c = g.cell(i, j, k);
-    const uint8_t fl = S.flags[c];
-    const T ro_c = Ls.ro[c];
-    const T uc[3] = {Ls.u1[c], Ls.u2[c], Ls.u3[c]};
-    T ro_cn, ucn[3];
-    if (fl & FL_LT) {
-        const int64_t fw = g.face(i, j, k);
-        const int64_t fh[3] = {fw + 1, fw + g.fs1, fw + g.fs2};
-        T rl[3], rh[3], pl[3], ph[3], ul[3][3], uh[3][3];
+// The stress force of one cell (main.cpp:995-1023): f_m = sum_d (sigma_md(+) - sigma_md(-))
+// * ds_d * ro_c.  fln/un: flags and velocities of the six neighbours in the order
+// (i-1, i+1, j-1, j+1, k-1, k+1).  FP64 evaluates every face stress exactly as the reference
+// does; FP32 uses the equivalent coefficient form sigma = a_c u_c - a_w u_w per face.
+template <class T>
+__device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6][3], uint8_t fl, const T uc[3],
+                                             T ro_c, const K<T> &kk, T f[3]) {
+    if (!Storage<T>::deviation) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            T sw[3], se[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                sw[d] = sigma(fln[2 * d], fl, un[2 * d][m], uc[m], kk, d);
+                se[d] = sigma(fl, fln[2 * d + 1], uc[m], un[2 * d + 1][m], kk, d);
+            }
+            f[m] = ((se[0] - sw[0]) * kk.ds[0] + (se[1] - sw[1]) * kk.ds[1] + (se[2] - sw[2]) * kk.ds[2]) * ro_c;
+        }
+    } else {
+        T aw[6], ac[6]; // per face: coefficient on the cell behind (w) and ahead (c)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const FaceSet<T> F = S.fc[d];
-            rl[d] = F.ro[fw];
-            rh[d] = F.ro[fh[d]];
-            pl[d] = F.p[fw];
-            ph[d] = F.p[fh[d]];
+            const T v = kk.vis * kk.rdx[d];
 #pragma unroll
-            for (int m = 0; m < 3; ++m) {
-                ul[d][m] = F.u[m][fw];
-                uh[d][m] = F.u[m][fh[d]];
+            for (int side = 0; side < 2; ++side) {
+                const uint8_t fw = side ? fl : fln[2 * d], fc = side ? fln[2 * d + 1] : fl;
+                const bool wl = fw & FL_LT, wg = fw & FL_GT, cl = fc & FL_LT, cg = fc & FL_GT;
+                const int q = 2 * d + side;
+                aw[q] = (wl && cl) ? v : (wl && cg) ? (T)2 * v : (T)0;
+                ac[q] = (wl && cl) ? v : (wg && cl) ? (T)2 * v : (T)0;
             }
         }
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            T acc = (T)0;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const T sw = ac[2 * d] * uc[m] - aw[2 * d] * un[2 * d][m];
+                const T se = ac[2 * d + 1] * un[2 * d + 1][m] - aw[2 * d + 1] * uc[m];
+                acc += (se - sw) * kk.ds[d];
+            }
+            f[m] = acc * ro_c;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Phase1 (+ stress force, bulk force, UseForces, dt / bulk-flow partials)
+// ---------------------------------------------------------------------------------------
+
+// One face's values: pressure, density, velocity components.
+template <class T> struct FaceVal { T p, ro, u[3]; };
+
+template <class T>
+__device__ __forceinline__ FaceVal<T> load_face(const FaceSet<T> &F, int f, const K<T> &kk) {
+    FaceVal<T> v;
+    v.p = __ldg(F.p + f);
+    v.ro = Storage<T>::deviation ? kk.ro0 + v.p * kk.rc2 : __ldg(F.ro + f);
+    v.u[0] = __ldg(F.u[0] + f);
+    v.u[1] = __ldg(F.u[1] + f);
+    v.u[2] = __ldg(F.u[2] + f);
+    return v;
+}
+
+// The conservative half step of one fluid cell (main.cpp:530-551) from its six faces
+// lo[d] (west/south/bottom) and hi[d] (east/north/top).  ro_c: density (FP64) or deviation.
+template <class T>
+__device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<T> hi[3], T ro_c, const T uc[3],
+                                          T dt, const K<T> &kk, T &ro_cn, T ucn[3]) {
+    if (!Storage<T>::deviation) {
         // new density (main.cpp:530-533)
-        ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((rh[0] * uh[0][0] - rl[0] * ul[0][0]) * kk.ds[0] +
-                                                    (rh[1] * uh[1][1] - rl[1] * ul[1][1]) * kk.ds[1] +
-                                                    (rh[2] * uh[2][2] - rl[2] * ul[2][2]) * kk.ds[2]),
-                     kk.dvc, (T)(1.0 / S.k.dvc));
-        // momentum (main.cpp:536-551): flux of u_m through faces normal to d is
+        ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
+                                                    (hi[1].ro * hi[1].u[1] - lo[1].ro * lo[1].u[1]) * kk.ds[1] +
+                                                    (hi[2].ro * hi[2].u[2] - lo[2].ro * lo[2].u[2]) * kk.ds[2]),
+                     kk.dvc, kk.rdvc);
+        // momentum (main.cpp:536-551): the flux of u_m through faces normal to d is
         // (ro*u_m)*u_d, plus p when m == d
         const T den = ro_cn * kk.dvc;
 #pragma unroll
@@ -315,66 +442,184 @@ __global__ void __launch_bounds__(128) k_phase1(DevState<T> S, int src, int dst)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (m == d)
-                    fx[d] = (rh[d] * uh[d][m] * uh[d][d] + ph[d]) - (rl[d] * ul[d][m] * ul[d][d] + pl[d]);
+                    fx[d] = (hi[d].ro * hi[d].u[m] * hi[d].u[d] + hi[d].p) - (lo[d].ro * lo[d].u[m] * lo[d].u[d] + lo[d].p);
                 else
-                    fx[d] = rh[d] * uh[d][m] * uh[d][d] - rl[d] * ul[d][m] * ul[d][d];
+                    fx[d] = hi[d].ro * hi[d].u[m] * hi[d].u[d] - lo[d].ro * lo[d].u[m] * lo[d].u[d];
             }
             ucn[m] = divv(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx[0] * kk.ds[0] + fx[1] * kk.ds[1] + fx[2] * kk.ds[2]),
                           den);
         }
     } else {
-        ucn[0] = ucn[1] = ucn[2] = (T)0;
-        ro_cn = kk.ro0;
-    }
-
-    if (MODE & (P1_STRESS | P1_FORCES)) {
-        T f[3];
-        if (MODE & P1_STRESS) {
-            // StressTensor force of this cell (main.cpp:995-1023) from the six face stresses
-            if (fl & FL_EQ0) {
-                const int64_t nb[6] = {c - 1, c + 1, c - g.cs1, c + g.cs1, c - g.cs2, c + g.cs2};
-                uint8_t fln[6];
-                T un[6][3];
+        // the same balance with the volume divided out and the density as a deviation:
+        // ro'_new = ro'_c - (dt/2/dvc) sum_d (rho u_d)|_faces ds_d
+        const T h = (T)0.5 * dt * kk.rdvc;
+        ro_cn = ro_c - h * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
+                            (hi[1].ro * hi[1].u[1] - lo[1].ro * lo[1].u[1]) * kk.ds[1] +
+                            (hi[2].ro * hi[2].u[2] - lo[2].ro * lo[2].u[2]) * kk.ds[2]);
+        const T rden = (T)1 / (kk.ro0 + ro_cn);
+        const T ro_cf = kk.ro0 + ro_c;
 #pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    fln[q] = S.flags[nb[q]];
-                    un[q][0] = Ls.u1[nb[q]];
-                    un[q][1] = Ls.u2[nb[q]];
-                    un[q][2] = Ls.u3[nb[q]];
-                }
+        for (int m = 0; m < 3; ++m) {
+            T fx[3];
 #pragma unroll
-                for (int m = 0; m < 3; ++m) {
-                    T sw[3], se[3];
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        sw[d] = sigma(fln[2 * d], fl, un[2 * d][m], uc[m], kk, d);
-                        se[d] = sigma(fl, fln[2 * d + 1], uc[m], un[2 * d + 1][m], kk, d);
-                    }
-                    f[m] = ((se[0] - sw[0]) * kk.ds[0] + (se[1] - sw[1]) * kk.ds[1] + (se[2] - sw[2]) * kk.ds[2]) * ro_c;
-                }
-                if (MODE & P1_BULK) f[0] = f[0] + (ro_c * kk.dvc) * (T)S.sc->G;
-            } else {
-                f[0] = f[1] = f[2] = (T)0;
+            for (int d = 0; d < 3; ++d) {
+                fx[d] = hi[d].ro * hi[d].u[m] * hi[d].u[d] - lo[d].ro * lo[d].u[m] * lo[d].u[d];
+                if (m == d) fx[d] += hi[d].p - lo[d].p;
             }
-            S.f[0][c] = f[0];
-            S.f[1][c] = f[1];
-            S.f[2][c] = f[2];
-        } else {
-            f[0] = S.f[0][c];
-            f[1] = S.f[1][c];
-            f[2] = S.f[2][c];
-        }
-        if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
-            // UseForces (main.cpp:1035-1041)
-            const T den = kk.dvc * ro_cn;
-#pragma unroll
-            for (int m = 0; m < 3; ++m) ucn[m] = divv(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den);
+            ucn[m] = (ro_cf * uc[m] - h * (fx[0] * kk.ds[0] + fx[1] * kk.ds[1] + fx[2] * kk.ds[2])) * rden;
         }
     }
-    Ld.ro[c] = ro_cn;
-    Ld.u1[c] = ucn[0];
-    Ld.u2[c] = ucn[1];
-    Ld.u3[c] = ucn[2];
+}
+
+// Phase1 over one tile (kTileX x kTileY cells, kTileK planes), marching up in k: the face
+// below a cell is the face above the previous one, and the stress's lower neighbour is the
+// previous centre, so both stay in registers.  src: the level read as "Con" (the previous
+// "nCon"); dst: the level written as "nCon"; faces of generation fcur.  MODE adds the
+// stress force (+ bulk force) of the src level, UseForces, and the partials of the next
+// step's dt (max |u| of dst) or bulk flow (sum of u1 of dst).
+template <class T, int MODE>
+__global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int src, int dst, int fcur) {
+    constexpr bool DEV = Storage<T>::deviation;
+    constexpr bool STRESS = MODE & P1_STRESS;
+    const Geom g = S.g;
+    const int i = blockIdx.x * kTileX + threadIdx.x + 1;
+    const int j = blockIdx.y * kTileY + threadIdx.y + 1;
+    const int k0 = blockIdx.z * kTileK + 1;
+    const int k1 = k0 + kTileK - 1 < g.C3 ? k0 + kTileK - 1 : g.C3;
+    unsigned long long m0 = 0, m1 = 0, m2 = 0;
+    long long rsum = 0;
+    if (i <= g.C1 && j <= g.C2) {
+        const K<T> kk(S.k);
+        const T dt = (T)S.sc->dt;
+        const T *__restrict__ sro = S.lv[src].ro;
+        const T *__restrict__ su1 = S.lv[src].u1;
+        const T *__restrict__ su2 = S.lv[src].u2;
+        const T *__restrict__ su3 = S.lv[src].u3;
+        T *__restrict__ dro = S.lv[dst].ro;
+        T *__restrict__ du1 = S.lv[dst].u1;
+        T *__restrict__ du2 = S.lv[dst].u2;
+        T *__restrict__ du3 = S.lv[dst].u3;
+        const uint8_t *__restrict__ flags = S.flags;
+        const int cs1 = (int)g.cs1, cs2 = (int)g.cs2, fs1 = (int)g.fs1, fs2 = (int)g.fs2;
+        const T G = (MODE & P1_BULK) ? (T)S.sc->G : (T)0;
+        int c = g.ci(i, j, k0), fw = g.fi(i, j, k0);
+        FaceVal<T> bot = load_face(S.fc[fcur][2], fw, kk);
+        // stress state carried up the column: the cell below and the current cell
+        uint8_t fdn = 0, fcen = 0;
+        T udn[3] = {(T)0, (T)0, (T)0}, ucen[3] = {(T)0, (T)0, (T)0}, rocen = (T)0;
+        if (STRESS) {
+            fdn = flags[c - cs2];
+            udn[0] = su1[c - cs2];
+            udn[1] = su2[c - cs2];
+            udn[2] = su3[c - cs2];
+            fcen = flags[c];
+            ucen[0] = su1[c];
+            ucen[1] = su2[c];
+            ucen[2] = su3[c];
+            rocen = sro[c];
+        }
+        for (int k = k0; k <= k1; ++k, c += cs2, fw += fs2) {
+            uint8_t fl;
+            T ro_c, uc[3];
+            if (STRESS) {
+                fl = fcen;
+                ro_c = rocen;
+                uc[0] = ucen[0];
+                uc[1] = ucen[1];
+                uc[2] = ucen[2];
+            } else {
+                fl = flags[c];
+                ro_c = sro[c];
+                uc[0] = su1[c];
+                uc[1] = su2[c];
+                uc[2] = su3[c];
+            }
+            const FaceVal<T> top = load_face(S.fc[fcur][2], fw + fs2, kk);
+            T ro_cn, ucn[3];
+            if (fl & FL_LT) {
+                FaceVal<T> lo[3], hi[3];
+                lo[0] = load_face(S.fc[fcur][0], fw, kk);
+                hi[0] = load_face(S.fc[fcur][0], fw + 1, kk);
+                lo[1] = load_face(S.fc[fcur][1], fw, kk);
+                hi[1] = load_face(S.fc[fcur][1], fw + fs1, kk);
+                lo[2] = bot;
+                hi[2] = top;
+                half_step(lo, hi, ro_c, uc, dt, kk, ro_cn, ucn);
+            } else {
+                ucn[0] = ucn[1] = ucn[2] = (T)0;
+                ro_cn = DEV ? (T)0 : kk.ro0;
+            }
+            T f[3] = {(T)0, (T)0, (T)0};
+            if (STRESS) {
+                // the cell above: next iteration's centre
+                const uint8_t fup = flags[c + cs2];
+                const T uup[3] = {su1[c + cs2], su2[c + cs2], su3[c + cs2]};
+                if (fl & FL_EQ0) {
+                    const int nb[4] = {c - 1, c + 1, c - cs1, c + cs1};
+                    uint8_t fln[6];
+                    T un[6][3];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        fln[q] = flags[nb[q]];
+                        un[q][0] = su1[nb[q]];
+                        un[q][1] = su2[nb[q]];
+                        un[q][2] = su3[nb[q]];
+                    }
+                    fln[4] = fdn;
+                    fln[5] = fup;
+#pragma unroll
+                    for (int m = 0; m < 3; ++m) {
+                        un[4][m] = udn[m];
+                        un[5][m] = uup[m];
+                    }
+                    const T ro_cf = DEV ? kk.ro0 + ro_c : ro_c;
+                    stress_force(fln, un, fl, uc, ro_cf, kk, f);
+                    if (MODE & P1_BULK) f[0] = f[0] + (ro_cf * kk.dvc) * G;
+                }
+                S.f[0][c] = f[0];
+                S.f[1][c] = f[1];
+                S.f[2][c] = f[2];
+                fdn = fl;
+                udn[0] = uc[0];
+                udn[1] = uc[1];
+                udn[2] = uc[2];
+                fcen = fup;
+                ucen[0] = uup[0];
+                ucen[1] = uup[1];
+                ucen[2] = uup[2];
+                if (k < k1) rocen = sro[c + cs2];
+            } else if (MODE & P1_FORCES) {
+                f[0] = __ldg(S.f[0] + c);
+                f[1] = __ldg(S.f[1] + c);
+                f[2] = __ldg(S.f[2] + c);
+            }
+            if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
+                // UseForces (main.cpp:1035-1041)
+                if (!DEV) {
+                    const T den = kk.dvc * ro_cn;
+#pragma unroll
+                    for (int m = 0; m < 3; ++m) ucn[m] = divv(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den);
+                } else {
+                    const T g2 = (T)0.5 * dt * kk.rdvc / (kk.ro0 + ro_cn);
+#pragma unroll
+                    for (int m = 0; m < 3; ++m) ucn[m] += g2 * f[m];
+                }
+            }
+            dro[c] = ro_cn;
+            du1[c] = ucn[0];
+            du2[c] = ucn[1];
+            du3[c] = ucn[2];
+            if (MODE & P1_RMAX) {
+                const unsigned long long b0 = abs_key(ucn[0]), b1 = abs_key(ucn[1]), b2 = abs_key(ucn[2]);
+                m0 = b0 > m0 ? b0 : m0;
+                m1 = b1 > m1 ? b1 : m1;
+                m2 = b2 > m2 ? b2 : m2;
+            }
+            if ((MODE & P1_RSUM) && (fl & FL_EQ0)) rsum += fixed_sum_term(ucn[0]);
+            bot = top;
+        }
+    }
+    if (MODE & (P1_RMAX | P1_RSUM)) tile_store(S, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
 }
 
 // StressTensor's face stresses into the sigm arrays (kept only on request), faces normal
@@ -392,13 +637,50 @@ template <class T> __global__ void k_stress_faces(DevState<T> S, int con, int d)
     const int64_t cw = c - (d == 0 ? 1 : d == 1 ? g.cs1 : g.cs2);
     const uint8_t fc = S.flags[c], fw = S.flags[cw];
     const int64_t fi = g.face(i, j, k);
-    S.sig[d][0][fi] = sigma(fw, fc, L.u1[cw], L.u1[c], kk, d);
-    S.sig[d][1][fi] = sigma(fw, fc, L.u2[cw], L.u2[c], kk, d);
-    S.sig[d][2][fi] = sigma(fw, fc, L.u3[cw], L.u3[c], kk, d);
+    T *s0 = d == 0 ? S.sig[0][0] : d == 1 ? S.sig[1][0] : S.sig[2][0];
+    T *s1 = d == 0 ? S.sig[0][1] : d == 1 ? S.sig[1][1] : S.sig[2][1];
+    T *s2 = d == 0 ? S.sig[0][2] : d == 1 ? S.sig[1][2] : S.sig[2][2];
+    s0[fi] = sigma(fw, fc, L.u1[cw], L.u1[c], kk, d);
+    s1[fi] = sigma(fw, fc, L.u2[cw], L.u2[c], kk, d);
+    s2[fi] = sigma(fw, fc, L.u3[cw], L.u3[c], kk, d);
+}
+
+// StressTensor's force alone (the same device code the fused Phase1 uses).
+template <class T> __global__ void k_stress_force(DevState<T> S, int con, int bulk) {
+    constexpr bool DEV = Storage<T>::deviation;
+    const Geom g = S.g;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.C1 || j > g.C2) return;
+    const K<T> kk(S.k);
+    const Level<T> L = S.lv[con];
+    const int64_t c = g.cell(i, j, k);
+    const uint8_t fl = S.flags[c];
+    T f[3] = {(T)0, (T)0, (T)0};
+    if (fl & FL_EQ0) {
+        const T ro_c = DEV ? kk.ro0 + L.ro[c] : L.ro[c];
+        const T uc[3] = {L.u1[c], L.u2[c], L.u3[c]};
+        const int64_t nb[6] = {c - 1, c + 1, c - g.cs1, c + g.cs1, c - g.cs2, c + g.cs2};
+        uint8_t fln[6];
+        T un[6][3];
+        for (int q = 0; q < 6; ++q) {
+            fln[q] = S.flags[nb[q]];
+            un[q][0] = L.u1[nb[q]];
+            un[q][1] = L.u2[nb[q]];
+            un[q][2] = L.u3[nb[q]];
+        }
+        stress_force(fln, un, fl, uc, ro_c, kk, f);
+        if (bulk) f[0] = f[0] + (ro_c * kk.dvc) * (T)S.sc->G;
+    }
+    S.f[0][c] = f[0];
+    S.f[1][c] = f[1];
+    S.f[2][c] = f[2];
 }
 
 // UseForces alone (main.cpp:1026-1045) on level ncon.
 template <class T> __global__ void k_use_forces(DevState<T> S, int ncon) {
+    constexpr bool DEV = Storage<T>::deviation;
     const Geom g = S.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -409,11 +691,18 @@ template <class T> __global__ void k_use_forces(DevState<T> S, int ncon) {
     const K<T> kk(S.k);
     const T dt = (T)S.sc->dt;
     const Level<T> L = S.lv[ncon];
-    const T ro_cn = L.ro[c];
-    const T den = kk.dvc * ro_cn;
-    L.u1[c] = divv(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den);
-    L.u2[c] = divv(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den);
-    L.u3[c] = divv(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den);
+    if (!DEV) {
+        const T ro_cn = L.ro[c];
+        const T den = kk.dvc * ro_cn;
+        L.u1[c] = divv(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den);
+        L.u2[c] = divv(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den);
+        L.u3[c] = divv(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den);
+    } else {
+        const T g2 = (T)0.5 * dt * kk.rdvc / (kk.ro0 + L.ro[c]);
+        L.u1[c] += g2 * S.f[0][c];
+        L.u2[c] += g2 * S.f[1][c];
+        L.u3[c] += g2 * S.f[2][c];
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -429,15 +718,17 @@ template <class T> struct SweepK {
 };
 
 // One cell of a sweep (main.cpp:1756-1873 for x1; the x2 and x3 sweeps are the same with
-// the axes permuted).  n: the velocity component normal to the sweep, a/b: tangential.
-// Q_USES_R selects the x1/x3 form of the Q-limiter source, 2*(r_cn - r_c)/dt
-// (main.cpp:1804, 2321); the x2 sweep uses 2*(q_cn - q_c)/dt (main.cpp:2083).
+// the axes permuted).  u1: the velocity component normal to the sweep, u2/u3: tangential.
+// ro_cn/ro_c: density (FP64) or density deviation (FP32).  Q_USES_R selects the x1/x3 form
+// of the Q-limiter source, 2*(r_cn - r_c)/dt (main.cpp:1804, 2321); the x2 sweep uses
+// 2*(q_cn - q_c)/dt (main.cpp:2083).
 template <class T, bool Q_USES_R>
 __device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T u2_f, T u2_b, T u2_cn,
                                               T u2_c, T u3_f, T u3_b, T u3_cn, T u3_c, T ro_cn, T ro_c,
                                               T p_f, T p_b, const SweepK<T> &q) {
-    const T p_cn = q.c2 * (ro_cn - q.ro0);
-    const T p_c = q.c2 * (ro_c - q.ro0);
+    constexpr bool DEV = Storage<T>::deviation;
+    const T p_cn = DEV ? q.c2 * ro_cn : q.c2 * (ro_cn - q.ro0);
+    const T p_c = DEV ? q.c2 * ro_c : q.c2 * (ro_c - q.ro0);
     const T pf = divk(p_f, q.roc, q.rroc), pb = divk(p_b, q.roc, q.rroc);
     const T pcn = divk(p_cn, q.roc, q.rroc), pc = divk(p_c, q.roc, q.rroc);
 
@@ -488,27 +779,39 @@ __device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T
     return e;
 }
 
+// Half-step cell values a face update may need in its rarer branches (loaded on demand).
+template <class T> struct NCell {
+    const T *__restrict__ nN;
+    const T *__restrict__ nA;
+    const T *__restrict__ nB;
+    const T *__restrict__ ro;
+};
+
+// The new face generation of one sweep direction.
+template <class T> struct FaceOut {
+    T *__restrict__ p;
+    T *__restrict__ ro;
+    T *__restrict__ n;
+    T *__restrict__ a;
+    T *__restrict__ b;
+};
+
 // Face update (main.cpp:1920-2008).  prev = the cell behind the face (index f-1), cur = the
-// cell ahead (index f).  cb/cf index those cells, fc the face; n/a/b the component indices
-// of the sweep.  uA_old/uB_old: the face's previous tangential velocities.  WALL_A_FROM_N:
-// the x2 sweep takes the tangential u1 from u2nCon in its wall branches (main.cpp:2219,
-// 2238).
+// cell ahead (index f); cb/cf index those cells, fc the face; flb/flf their flags and
+// ucb/ucf their half-step normal velocities.  uA_old/uB_old: the face's previous tangential
+// velocities.  WALL_A_FROM_N: the x2 sweep takes the tangential u1 from u2nCon in its wall
+// branches (main.cpp:2219, 2238).
 template <class T, bool WALL_A_FROM_N>
-__device__ __forceinline__ void face_update(const DevState<T> &S, const Level<T> &Ln, const FaceSet<T> &F,
-                                            int n, int a, int b, int64_t cb, int64_t cf, int64_t fc,
-                                            const Ext<T> &prev, const Ext<T> &cur, T uA_old, T uB_old,
-                                            const SweepK<T> &q) {
-    const T *nN = n == 0 ? Ln.u1 : n == 1 ? Ln.u2 : Ln.u3;
-    const T *nA = a == 0 ? Ln.u1 : Ln.u2;
-    const T *nB = b == 1 ? Ln.u2 : Ln.u3;
-    const uint8_t flb = S.flags[cb], flf = S.flags[cf];
+__device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> &W, int cb, int cf, int fc,
+                                            uint8_t flb, uint8_t flf, T ucb, T ucf, const Ext<T> &prev,
+                                            const Ext<T> &cur, T uA_old, T uB_old, const SweepK<T> &q) {
+    constexpr bool DEV = Storage<T>::deviation;
     T un, pn, ro_n, ua, ub;
     if ((flb & FL_LT) && (flf & FL_LT)) {
         const T rn = prev.rf, qn = cur.qb;
         un = (rn + qn) / (T)2;
         pn = (rn - qn) * q.sound * q.ro0 / (T)2;
         ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
-        const T ucf = nN[cf], ucb = nN[cb];
         if (ucf >= (T)0 && ucb >= (T)0) {
             ua = prev.af;
             ub = prev.bf;
@@ -524,36 +827,36 @@ __device__ __forceinline__ void face_update(const DevState<T> &S, const Level<T>
                 ub = cur.bb;
             }
         } else {
-            ua = nA[cf] + nA[cb] - uA_old;
-            ub = nB[cf] + nB[cb] - uB_old;
+            ua = N.nA[cf] + N.nA[cb] - uA_old;
+            ub = N.nB[cf] + N.nB[cb] - uB_old;
         }
     } else {
         un = (T)0;
         if ((flb & FL_GT) && (flf & FL_LT)) {
-            if (nN[cf] <= (T)0) {
+            if (ucf <= (T)0) {
                 const T qn = cur.qb;
                 pn = -qn * q.sound * q.ro0;
                 ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
                 ua = cur.ab;
                 ub = cur.bb;
             } else {
-                ro_n = Ln.ro[cf];
-                pn = (ro_n - q.ro0) * q.c2;
-                ua = WALL_A_FROM_N ? nN[cf] : nA[cf];
-                ub = nB[cf];
+                ro_n = N.ro[cf];
+                pn = DEV ? ro_n * q.c2 : (ro_n - q.ro0) * q.c2;
+                ua = WALL_A_FROM_N ? ucf : N.nA[cf];
+                ub = N.nB[cf];
             }
         } else if ((flb & FL_LT) && (flf & FL_GT)) {
-            if (nN[cb] >= (T)0) {
+            if (ucb >= (T)0) {
                 const T rn = prev.rf;
                 pn = rn * q.sound * q.ro0;
                 ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
                 ua = prev.af;
                 ub = prev.bf;
             } else {
-                ro_n = Ln.ro[cb];
-                pn = (ro_n - q.ro0) * q.c2;
-                ua = WALL_A_FROM_N ? nN[cb] : nA[cb];
-                ub = nB[cb];
+                ro_n = N.ro[cb];
+                pn = DEV ? ro_n * q.c2 : (ro_n - q.ro0) * q.c2;
+                ua = WALL_A_FROM_N ? ucb : N.nA[cb];
+                ub = N.nB[cb];
             }
         } else {
             pn = (T)0;
@@ -562,11 +865,11 @@ __device__ __forceinline__ void face_update(const DevState<T> &S, const Level<T>
             ub = (T)0;
         }
     }
-    F.p[fc] = pn;
-    F.u[n][fc] = un;
-    F.ro[fc] = ro_n;
-    F.u[a][fc] = ua;
-    F.u[b][fc] = ub;
+    W.p[fc] = pn;
+    W.n[fc] = un;
+    if (!DEV) W.ro[fc] = ro_n;
+    W.a[fc] = ua;
+    W.b[fc] = ub;
 }
 
 template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d) {
@@ -585,86 +888,179 @@ template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevSt
     return q;
 }
 
+// Everything one cell of a sweep reads: its forward face (s+1), the half-step ("n") and
+// old ("c") values of the cell, and its flags.  The backward face is the previous cell's
+// forward face.
+template <class T> struct SweepIn {
+    T uN_f, uA_f, uB_f, p_f, nN, cN, nA, cA, nB, cB, nR, cR;
+    uint8_t fl;
+};
+
+// The pointers of one sweep: old faces F*, cell levels c* ("Con") and n* ("nCon").
+template <class T> struct SweepSrc {
+    const T *__restrict__ FN;
+    const T *__restrict__ FA;
+    const T *__restrict__ FB;
+    const T *__restrict__ FP;
+    const T *__restrict__ cN;
+    const T *__restrict__ nN;
+    const T *__restrict__ cA;
+    const T *__restrict__ nA;
+    const T *__restrict__ cB;
+    const T *__restrict__ nB;
+    const T *__restrict__ cR;
+    const T *__restrict__ nR;
+    const uint8_t *__restrict__ fl;
+};
+
+template <class T>
+__device__ __forceinline__ SweepSrc<T> sweep_src(const DevState<T> &S, int con, int fcur, int ax) {
+    const Level<T> Lc = S.lv[con], Ln = S.lv[con ^ 1];
+    const FaceSet<T> F = S.fc[fcur][ax];
+    const int a = ax == 0 ? 1 : 0, b = ax == 2 ? 1 : 2;
+    const T *cu[3] = {Lc.u1, Lc.u2, Lc.u3}, *nu[3] = {Ln.u1, Ln.u2, Ln.u3};
+    SweepSrc<T> r = {F.u[ax], F.u[a], F.u[b], F.p, cu[ax], nu[ax], cu[a], nu[a], cu[b], nu[b], Lc.ro, Ln.ro, S.flags};
+    return r;
+}
+
+template <class T> __device__ __forceinline__ FaceOut<T> sweep_out(const DevState<T> &S, int fcur, int ax) {
+    const FaceSet<T> W = S.fc[fcur ^ 1][ax];
+    const int a = ax == 0 ? 1 : 0, b = ax == 2 ? 1 : 2;
+    FaceOut<T> o = {W.p, W.ro, W.u[ax], W.u[a], W.u[b]};
+    return o;
+}
+
+template <class T>
+__device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, SweepIn<T> &x) {
+    x.uN_f = R.FN[ff];
+    x.uA_f = R.FA[ff];
+    x.uB_f = R.FB[ff];
+    x.p_f = R.FP[ff];
+    x.nN = R.nN[c];
+    x.cN = R.cN[c];
+    x.nA = R.nA[c];
+    x.cA = R.cA[c];
+    x.nB = R.nB[c];
+    x.cB = R.cB[c];
+    x.nR = R.nR[c];
+    x.cR = R.cR[c];
+    x.fl = R.fl[c];
+}
+
 // x1 sweep: one warp per (j,k) line, lanes on consecutive cells (coalesced), marching along
-// i in chunks of 32.  A face needs the forward values of the cell behind it: a shuffle
-// from the neighbouring lane, or the carry from the previous chunk's last lane.  Each
-// warp owns all faces of its line, so the faces are updated in place.
-template <class T> __global__ void __launch_bounds__(128) k_sweep_x(DevState<T> S, int con) {
+// i in chunks of 32 with the next chunk's loads issued before the current chunk is
+// computed.  A face needs the forward values of the cell behind it: a shuffle from the
+// neighbouring lane, or the carry from the previous chunk's last lane.  Old faces come from
+// generation fcur, new faces go to fcur^1.
+template <class T> __global__ void __launch_bounds__(128) k_sweep_x(DevState<T> S, int con, int fcur) {
     const Geom g = S.g;
     const int lane = threadIdx.x & 31;
     const int line = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     if (line >= g.C2 * g.C3) return;
     const int j = line % g.C2 + 1, k = line / g.C2 + 1;
-    const Level<T> Lc = S.lv[con], Ln = S.lv[con ^ 1];
-    const FaceSet<T> F = S.fc[0];
+    const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
+    const FaceOut<T> W = sweep_out(S, fcur, 0);
+    const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
     const SweepK<T> q = sweep_consts(S, 0);
-    const int64_t c0 = g.cell(0, j, k), f0 = g.face(0, j, k);
+    const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k);
     const int nd = g.C1 + 1;
     Ext<T> carry = {};
+    T carry_u = 0;
+    uint8_t carry_fl = 0;
+    SweepIn<T> cur = {}, nxt = {};
+    T uN_b = 0, uA_b = 0, uB_b = 0, p_b = 0, nuN_b = 0, nuA_b = 0, nuB_b = 0, np_b = 0;
+    if (lane <= nd) {
+        sweep_load(R, c0 + lane, f0 + lane + 1, cur);
+        uN_b = R.FN[f0 + lane];
+        uA_b = R.FA[f0 + lane];
+        uB_b = R.FB[f0 + lane];
+        p_b = R.FP[f0 + lane];
+    }
     for (int s0 = 0; s0 <= nd; s0 += 32) {
         const int s = s0 + lane;
         const bool act = s <= nd;
-        Ext<T> e = {};
-        T uA_old = 0, uB_old = 0;
-        if (act) {
-            const int64_t c = c0 + s, fb = f0 + s, ff = fb + 1;
-            uA_old = F.u[1][fb];
-            uB_old = F.u[2][fb];
-            e = extrapolate<T, true>(F.u[0][ff], F.u[0][fb], Ln.u1[c], Lc.u1[c], F.u[1][ff], uA_old, Ln.u2[c],
-                                     Lc.u2[c], F.u[2][ff], uB_old, Ln.u3[c], Lc.u3[c], Ln.ro[c], Lc.ro[c],
-                                     F.p[ff], F.p[fb], q);
+        const int sn = s + 32;
+        if (sn <= nd) {
+            sweep_load(R, c0 + sn, f0 + sn + 1, nxt);
+            nuN_b = R.FN[f0 + sn];
+            nuA_b = R.FA[f0 + sn];
+            nuB_b = R.FB[f0 + sn];
+            np_b = R.FP[f0 + sn];
         }
+        Ext<T> e = {};
+        if (act)
+            e = extrapolate<T, true>(cur.uN_f, uN_b, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA, cur.uB_f, uB_b,
+                                     cur.nB, cur.cB, cur.nR, cur.cR, cur.p_f, p_b, q);
         Ext<T> prev;
         prev.rf = __shfl_up_sync(0xffffffffu, e.rf, 1);
         prev.af = __shfl_up_sync(0xffffffffu, e.af, 1);
         prev.bf = __shfl_up_sync(0xffffffffu, e.bf, 1);
+        T ucb = __shfl_up_sync(0xffffffffu, cur.nN, 1);
+        uint8_t flb = (uint8_t)__shfl_up_sync(0xffffffffu, (int)cur.fl, 1);
         if (lane == 0) {
             prev.rf = carry.rf;
             prev.af = carry.af;
             prev.bf = carry.bf;
+            ucb = carry_u;
+            flb = carry_fl;
         }
         carry.rf = __shfl_sync(0xffffffffu, e.rf, 31);
         carry.af = __shfl_sync(0xffffffffu, e.af, 31);
         carry.bf = __shfl_sync(0xffffffffu, e.bf, 31);
-        __syncwarp();
+        carry_u = __shfl_sync(0xffffffffu, cur.nN, 31);
+        carry_fl = (uint8_t)__shfl_sync(0xffffffffu, (int)cur.fl, 31);
         if (act && s >= 1)
-            face_update<T, false>(S, Ln, F, 0, 1, 2, c0 + s - 1, c0 + s, f0 + s, prev, e, uA_old, uB_old, q);
-        __syncwarp();
+            face_update<T, false>(N, W, c0 + s - 1, c0 + s, f0 + s, flb, cur.fl, ucb, cur.nN, prev, e, uA_b, uB_b, q);
+        cur = nxt;
+        uN_b = nuN_b;
+        uA_b = nuA_b;
+        uB_b = nuB_b;
+        p_b = np_b;
     }
 }
 
-// x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per line, threads on consecutive i
-// (coalesced), marching along the sweep axis; the face behind the current cell is carried
-// in registers, so every face is read once and updated in place.
-template <class T, int AX> __global__ void __launch_bounds__(128) k_sweep_col(DevState<T> S, int con) {
+// x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,
+// threads on consecutive i (coalesced), marching along the sweep axis with the next cell's
+// loads issued before the current cell is computed.  A segment of faces s0+1..s1 needs
+// cells s0..s1 (cell s0 is the one overlap with the previous segment); the face behind
+// the current cell is carried in registers.  Old faces come from generation fcur, new
+// faces go to fcur^1, so segments are independent.
+template <class T, int AX>
+__global__ void __launch_bounds__(128) k_sweep_col(DevState<T> S, int con, int fcur, int seg) {
     const Geom g = S.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int o = blockIdx.y + 1;
-    if (i > g.C1) return;
-    const Level<T> Lc = S.lv[con], Ln = S.lv[con ^ 1];
-    const FaceSet<T> F = S.fc[AX];
-    const SweepK<T> q = sweep_consts(S, AX);
-    constexpr int A = 0, B = (AX == 1) ? 2 : 1;
-    const int64_t cst = AX == 1 ? g.cs1 : g.cs2, fst = AX == 1 ? g.fs1 : g.fs2;
-    const int64_t c0 = AX == 1 ? g.cell(i, 0, o) : g.cell(i, o, 0);
-    const int64_t f0 = AX == 1 ? g.face(i, 0, o) : g.face(i, o, 0);
     const int nd = (AX == 1 ? g.C2 : g.C3) + 1;
-    const T *cN = AX == 1 ? Lc.u2 : Lc.u3, *nN = AX == 1 ? Ln.u2 : Ln.u3;
-    const T *cA = Lc.u1, *nA = Ln.u1;
-    const T *cB = B == 2 ? Lc.u3 : Lc.u2, *nB = B == 2 ? Ln.u3 : Ln.u2;
-    T uN_b = F.u[AX][f0], uA_b = F.u[A][f0], uB_b = F.u[B][f0], p_b = F.p[f0];
+    const int s0 = blockIdx.z * seg;
+    if (i > g.C1 || s0 >= nd) return;
+    const int s1 = s0 + seg < nd ? s0 + seg : nd;
+    const SweepSrc<T> R = sweep_src(S, con, fcur, AX);
+    const FaceOut<T> W = sweep_out(S, fcur, AX);
+    const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
+    const SweepK<T> q = sweep_consts(S, AX);
+    const int cst = AX == 1 ? (int)g.cs1 : (int)g.cs2, fst = AX == 1 ? (int)g.fs1 : (int)g.fs2;
+    int c = (AX == 1 ? g.ci(i, 0, o) : g.ci(i, o, 0)) + s0 * cst;
+    int fb = (AX == 1 ? g.fi(i, 0, o) : g.fi(i, o, 0)) + s0 * fst;
+    T uN_b = R.FN[fb], uA_b = R.FA[fb], uB_b = R.FB[fb], p_b = R.FP[fb];
+    SweepIn<T> cur, nxt = {};
+    sweep_load(R, c, fb + fst, cur);
     Ext<T> prev = {};
-    for (int s = 0; s <= nd; ++s) {
-        const int64_t c = c0 + s * cst, ff = f0 + (s + 1) * fst;
-        const T uN_f = F.u[AX][ff], uA_f = F.u[A][ff], uB_f = F.u[B][ff], p_f = F.p[ff];
-        const Ext<T> e = extrapolate<T, AX == 2>(uN_f, uN_b, nN[c], cN[c], uA_f, uA_b, nA[c], cA[c], uB_f, uB_b,
-                                                 nB[c], cB[c], Ln.ro[c], Lc.ro[c], p_f, p_b, q);
-        if (s >= 1) face_update<T, AX == 1>(S, Ln, F, AX, A, B, c - cst, c, f0 + s * fst, prev, e, uA_b, uB_b, q);
+    T uprev = 0;
+    uint8_t flprev = 0;
+    for (int s = s0; s <= s1; ++s, c += cst, fb += fst) {
+        if (s < s1) sweep_load(R, c + cst, fb + 2 * fst, nxt);
+        const Ext<T> e = extrapolate<T, AX == 2>(cur.uN_f, uN_b, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA,
+                                                 cur.uB_f, uB_b, cur.nB, cur.cB, cur.nR, cur.cR, cur.p_f, p_b, q);
+        if (s > s0)
+            face_update<T, AX == 1>(N, W, c - cst, c, fb, flprev, cur.fl, uprev, cur.nN, prev, e, uA_b, uB_b, q);
         prev = e;
-        uN_b = uN_f;
-        uA_b = uA_f;
-        uB_b = uB_f;
-        p_b = p_f;
+        uprev = cur.nN;
+        flprev = cur.fl;
+        uN_b = cur.uN_f;
+        uA_b = cur.uA_f;
+        uB_b = cur.uB_f;
+        p_b = cur.p_f;
+        cur = nxt;
     }
 }
 
@@ -672,32 +1068,38 @@ template <class T, int AX> __global__ void __launch_bounds__(128) k_sweep_col(De
 // conservation sums of one level (fixed point: identical for any grid)
 // ---------------------------------------------------------------------------------------
 
-template <class T> __global__ void __launch_bounds__(256) k_sums(DevState<T> S, int ncon) {
+template <class T> __global__ void __launch_bounds__(kTileX *kTileY) k_sums(DevState<T> S, int ncon) {
+    constexpr bool DEV = Storage<T>::deviation;
+    __shared__ long long red[6][kTileX * kTileY / 32];
     const Geom g = S.g;
     const Level<T> L = S.lv[ncon];
-    const int64_t n = (int64_t)g.C1 * g.C2 * g.C3;
-    long long a[5] = {0, 0, 0, 0, 0}, cnt = 0;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.C1) + 1;
-        const int64_t r = t / g.C1;
-        const int j = (int)(r % g.C2) + 1;
-        const int k = (int)(r / g.C2) + 1;
-        const int64_t c = g.cell(i, j, k);
-        if (!(S.flags[c] & FL_EQ0)) continue;
-        const double ro = L.ro[c], u1 = L.u1[c], u2 = L.u2[c], u3 = L.u3[c];
-        a[0] += fixed32(ro);
-        a[1] += fixed32(ro * u1);
-        a[2] += fixed32(ro * u2);
-        a[3] += fixed32(ro * u3);
-        a[4] += fixed32((u1 * u1 + u2 * u2 + u3 * u3) / 2);
-        cnt += 1;
+    const int i = blockIdx.x * kTileX + threadIdx.x + 1;
+    const int j = blockIdx.y * kTileY + threadIdx.y + 1;
+    long long a[6] = {0, 0, 0, 0, 0, 0};
+    if (i <= g.C1 && j <= g.C2) {
+        int64_t c = g.cell(i, j, 1);
+        for (int k = 1; k <= g.C3; ++k, c += g.cs2) {
+            if (!(S.flags[c] & FL_EQ0)) continue;
+            const double ro = DEV ? S.k.ro0 + (double)L.ro[c] : (double)L.ro[c];
+            const double u1 = L.u1[c], u2 = L.u2[c], u3 = L.u3[c];
+            a[0] += fixed32(ro);
+            a[1] += fixed32(ro * u1);
+            a[2] += fixed32(ro * u2);
+            a[3] += fixed32(ro * u3);
+            a[4] += fixed32((u1 * u1 + u2 * u2 + u3 * u3) / 2);
+            a[5] += 1;
+        }
     }
-    for (int q = 0; q < 5; ++q) a[q] = warp_sum_i64(a[q]);
-    cnt = warp_sum_i64(cnt);
-    if ((threadIdx.x & 31) == 0) {
-        for (int q = 0; q < 5; ++q) atomicAdd((unsigned long long *)&S.sc->sums[q], (unsigned long long)a[q]);
-        atomicAdd((unsigned long long *)&S.sc->sum_cells, (unsigned long long)cnt);
+    for (int q = 0; q < 6; ++q) a[q] = warp_sum_i64(a[q]);
+    const int t = threadIdx.y * kTileX + threadIdx.x, w = t >> 5;
+    if ((t & 31) == 0)
+        for (int q = 0; q < 6; ++q) red[q][w] = a[q];
+    __syncthreads();
+    if (t < 6) {
+        long long z = 0;
+        for (int v = 0; v < kTileX * kTileY / 32; ++v) z += red[t][v];
+        if (z != 0)
+            atomicAdd((unsigned long long *)(t < 5 ? &S.sc->sums[t] : &S.sc->sum_cells), (unsigned long long)z);
     }
 }
 
@@ -712,19 +1114,18 @@ inline int grid_for(int64_t n, int block, int cap) {
     return (int)b;
 }
 
-template <class T> inline void cell_grid(const Geom &g, dim3 &grid, dim3 &block) {
-    block = dim3(g.C1 >= 64 ? 64 : 32, 2, 1);
-    grid = dim3((g.C1 + block.x - 1) / block.x, (g.C2 + block.y - 1) / block.y, g.C3);
+inline dim3 cell_grid(const Geom &g) {
+    return dim3((g.C1 + kCellBX - 1) / kCellBX, (g.C2 + kCellBY - 1) / kCellBY, g.C3);
 }
 
-template <class T>
-void Launch<T>::reduce_start(const DevState<T> &S, int con, int with_sum, cudaStream_t st) {
-    const int64_t n = (int64_t)S.g.C1 * S.g.C2 * S.g.C3;
-    k_reduce_start<T><<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(S, con, with_sum);
+inline dim3 tile_grid(const Geom &g) { return dim3(tiles_x(g), tiles_y(g), tiles_k(g)); }
+
+template <class T> void Launch<T>::reduce_start(const DevState<T> &S, int con, cudaStream_t st) {
+    k_reduce_start<T><<<tile_grid(S.g), dim3(kTileX, kTileY), 0, st>>>(S, con);
 }
 
 template <class T> void Launch<T>::finalize_dt(const DevState<T> &S, int advance_time, cudaStream_t st) {
-    k_finalize_dt<T><<<1, 1, 0, st>>>(S, advance_time);
+    k_finalize_dt<T><<<1, 1024, 0, st>>>(S, advance_time, tile_count(S.g));
 }
 
 template <class T> void Launch<T>::wrap_cells(const DevState<T> &S, T *const *arrs, int n, cudaStream_t st) {
@@ -741,7 +1142,7 @@ template <class T> void Launch<T>::wrap_cells(const DevState<T> &S, T *const *ar
 
 // The halo exchange before Phase2 (main.cpp:1049-1631): cells u?nCon, ronCon and roCon in x
 // and z; faces normal to x1 wrapped in x, faces normal to x3 wrapped in z.
-template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, cudaStream_t st) {
+template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st) {
     WrapJob J = {};
     const Level<T> Ln = S.lv[con ^ 1], Lc = S.lv[con];
     T *cells[5] = {Ln.u1, Ln.u2, Ln.u3, Ln.ro, Lc.ro};
@@ -751,14 +1152,17 @@ template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, cu
         J.face[n] = 0;
         J.axis_mask[n++] = 3;
     }
-    T *fx[5] = {S.fc[0].p, S.fc[0].ro, S.fc[0].u[0], S.fc[0].u[1], S.fc[0].u[2]};
-    T *fz[5] = {S.fc[2].p, S.fc[2].ro, S.fc[2].u[0], S.fc[2].u[1], S.fc[2].u[2]};
+    const FaceSet<T> &X = S.fc[fcur][0], &Z = S.fc[fcur][2];
+    T *fx[5] = {X.p, X.u[0], X.u[1], X.u[2], X.ro};
+    T *fz[5] = {Z.p, Z.u[0], Z.u[1], Z.u[2], Z.ro};
     for (int q = 0; q < 5; ++q) {
+        if (!fx[q]) continue;
         J.a[n] = fx[q];
         J.face[n] = 1;
         J.axis_mask[n++] = 1;
     }
     for (int q = 0; q < 5; ++q) {
+        if (!fz[q]) continue;
         J.a[n] = fz[q];
         J.face[n] = 1;
         J.axis_mask[n++] = 2;
@@ -768,67 +1172,28 @@ template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, cu
     k_wrap<T><<<grid_for(tot, 256, 1 << 30), 256, 0, st>>>(S.g, J);
 }
 
-template <class T> void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int mode, cudaStream_t st) {
-    dim3 grid, block;
-    cell_grid<T>(S.g, grid, block);
+template <class T>
+void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, cudaStream_t st) {
+    const dim3 grid = tile_grid(S.g), block(kTileX, kTileY);
     switch (mode) {
-    case P1_PLAIN: k_phase1<T, P1_PLAIN><<<grid, block, 0, st>>>(S, src, dst); break;
-    case P1_STRESS | P1_FORCES: k_phase1<T, P1_STRESS | P1_FORCES><<<grid, block, 0, st>>>(S, src, dst); break;
-    case P1_STRESS | P1_FORCES | P1_BULK:
-        k_phase1<T, P1_STRESS | P1_FORCES | P1_BULK><<<grid, block, 0, st>>>(S, src, dst);
+    case P1_PLAIN: k_phase1<T, P1_PLAIN><<<grid, block, 0, st>>>(S, src, dst, fcur); break;
+    case P1_STRESS | P1_FORCES | P1_RMAX:
+        k_phase1<T, P1_STRESS | P1_FORCES | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur);
         break;
-    case P1_FORCES: k_phase1<T, P1_FORCES><<<grid, block, 0, st>>>(S, src, dst); break;
+    case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
+        k_phase1<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur);
+        break;
+    case P1_FORCES | P1_RSUM: k_phase1<T, P1_FORCES | P1_RSUM><<<grid, block, 0, st>>>(S, src, dst, fcur); break;
     default: break;
     }
 }
 
-// StressTensor alone: the force (the same device code as the fused Phase1 computes it,
-// with nothing else written) and, on request, the face stresses.
-template <class T> __global__ void k_stress_force(DevState<T> S, int con, int bulk) {
-    const Geom g = S.g;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > g.C1 || j > g.C2) return;
-    const K<T> kk(S.k);
-    const Level<T> L = S.lv[con];
-    const int64_t c = g.cell(i, j, k);
-    const uint8_t fl = S.flags[c];
-    T f[3] = {(T)0, (T)0, (T)0};
-    if (fl & FL_EQ0) {
-        const T ro_c = L.ro[c];
-        const T uc[3] = {L.u1[c], L.u2[c], L.u3[c]};
-        const int64_t nb[6] = {c - 1, c + 1, c - g.cs1, c + g.cs1, c - g.cs2, c + g.cs2};
-        uint8_t fln[6];
-        T un[6][3];
-        for (int q = 0; q < 6; ++q) {
-            fln[q] = S.flags[nb[q]];
-            un[q][0] = L.u1[nb[q]];
-            un[q][1] = L.u2[nb[q]];
-            un[q][2] = L.u3[nb[q]];
-        }
-        for (int m = 0; m < 3; ++m) {
-            T sw[3], se[3];
-            for (int d = 0; d < 3; ++d) {
-                sw[d] = sigma(fln[2 * d], fl, un[2 * d][m], uc[m], kk, d);
-                se[d] = sigma(fl, fln[2 * d + 1], uc[m], un[2 * d + 1][m], kk, d);
-            }
-            f[m] = ((se[0] - sw[0]) * kk.ds[0] + (se[1] - sw[1]) * kk.ds[1] + (se[2] - sw[2]) * kk.ds[2]) * ro_c;
-        }
-        if (bulk) f[0] = f[0] + (ro_c * kk.dvc) * (T)S.sc->G;
-    }
-    S.f[0][c] = f[0];
-    S.f[1][c] = f[1];
-    S.f[2][c] = f[2];
-}
-
 template <class T> void Launch<T>::stress(const DevState<T> &S, int con, int bulk, cudaStream_t st) {
-    dim3 grid, block;
-    cell_grid<T>(S.g, grid, block);
-    k_stress_force<T><<<grid, block, 0, st>>>(S, con, bulk);
+    const dim3 block(kCellBX, kCellBY);
+    k_stress_force<T><<<cell_grid(S.g), block, 0, st>>>(S, con, bulk);
     if (S.sig[0][0]) {
         for (int d = 0; d < 3; ++d) {
-            dim3 gd((S.g.C1 + (d == 0) + block.x - 1) / block.x, (S.g.C2 + (d == 1) + block.y - 1) / block.y,
+            dim3 gd((S.g.C1 + (d == 0) + kCellBX - 1) / kCellBX, (S.g.C2 + (d == 1) + kCellBY - 1) / kCellBY,
                     S.g.C3 + (d == 2));
             k_stress_faces<T><<<gd, block, 0, st>>>(S, con, d);
         }
@@ -836,19 +1201,28 @@ template <class T> void Launch<T>::stress(const DevState<T> &S, int con, int bul
 }
 
 template <class T> void Launch<T>::use_forces(const DevState<T> &S, int ncon, cudaStream_t st) {
-    dim3 grid, block;
-    cell_grid<T>(S.g, grid, block);
-    k_use_forces<T><<<grid, block, 0, st>>>(S, ncon);
+    k_use_forces<T><<<cell_grid(S.g), dim3(kCellBX, kCellBY), 0, st>>>(S, ncon);
 }
 
-template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int axis, cudaStream_t st) {
+// Segments of at most 32 faces, balanced so no thread gets a short tail.
+inline int sweep_segment(int nd, int *nseg) {
+    const int n = (nd + 31) / 32;
+    *nseg = n;
+    return (nd + n - 1) / n;
+}
+
+template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st) {
     if (axis == 0) {
         const int lines_x = S.g.C2 * S.g.C3;
-        k_sweep_x<T><<<(lines_x + 3) / 4, 128, 0, st>>>(S, con);
+        k_sweep_x<T><<<(lines_x + 3) / 4, 128, 0, st>>>(S, con, fcur);
     } else if (axis == 1) {
-        k_sweep_col<T, 1><<<dim3((S.g.C1 + 127) / 128, S.g.C3), 128, 0, st>>>(S, con);
+        int nseg;
+        const int seg = sweep_segment(S.g.C2 + 1, &nseg);
+        k_sweep_col<T, 1><<<dim3((S.g.C1 + 127) / 128, S.g.C3, nseg), 128, 0, st>>>(S, con, fcur, seg);
     } else {
-        k_sweep_col<T, 2><<<dim3((S.g.C1 + 127) / 128, S.g.C2), 128, 0, st>>>(S, con);
+        int nseg;
+        const int seg = sweep_segment(S.g.C3 + 1, &nseg);
+        k_sweep_col<T, 2><<<dim3((S.g.C1 + 127) / 128, S.g.C2, nseg), 128, 0, st>>>(S, con, fcur, seg);
     }
 }
 
@@ -860,29 +1234,36 @@ void Launch<T>::boundary_fill(const DevState<T> &S, int ncon, int axis, int peri
 }
 
 template <class T> void Launch<T>::sums(const DevState<T> &S, int ncon, cudaStream_t st) {
-    const int64_t n = (int64_t)S.g.C1 * S.g.C2 * S.g.C3;
-    k_sums<T><<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(S, ncon);
+    dim3 grid(tiles_x(S.g), tiles_y(S.g));
+    k_sums<T><<<grid, dim3(kTileX, kTileY), 0, st>>>(S, ncon);
 }
-
-} // namespace ark
-
-namespace ark {
 
 // Precision conversion for FP32 contexts (host arrays are always double).
-template <class T> __global__ void k_from_double(T *dst, const double *src, int64_t n) {
+template <class T> __global__ void k_from_double(T *dst, const double *src, int64_t n, double offset) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-        dst[t] = (T)src[t];
+        dst[t] = (T)(src[t] - offset);
 }
-template <class T> __global__ void k_to_double(double *dst, const T *src, int64_t n) {
+template <class T> __global__ void k_to_double(double *dst, const T *src, int64_t n, double offset) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-        dst[t] = (double)src[t];
+        dst[t] = (double)src[t] + offset;
+}
+template <class T>
+__global__ void k_face_density(double *dst, const T *p, int64_t n, double ro0, double rc2) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        dst[t] = ro0 + (double)p[t] * rc2;
 }
 
-template <class T> void convert_from_double(T *dst, const double *src, int64_t n, cudaStream_t st) {
-    k_from_double<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, n);
+template <class T>
+void convert_from_double(T *dst, const double *src, int64_t n, double offset, cudaStream_t st) {
+    k_from_double<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, n, offset);
 }
-template <class T> void convert_to_double(double *dst, const T *src, int64_t n, cudaStream_t st) {
-    k_to_double<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, n);
+template <class T>
+void convert_to_double(double *dst, const T *src, int64_t n, double offset, cudaStream_t st) {
+    k_to_double<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, n, offset);
+}
+template <class T>
+void face_density_to_double(double *dst, const T *p, int64_t n, double ro0, double rc2, cudaStream_t st) {
+    k_face_density<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, p, n, ro0, rc2);
 }
 
 } // namespace ark

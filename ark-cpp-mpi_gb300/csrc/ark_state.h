@@ -23,9 +23,25 @@ struct Geom {
     __host__ __device__ __forceinline__ int64_t face(int i, int j, int k) const {
         return (int64_t)k * fs2 + (int64_t)j * fs1 + i;
     }
+    // 32-bit forms for the hot kernels (ark_create keeps every array below 2^31 elements)
+    __host__ __device__ __forceinline__ int ci(int i, int j, int k) const {
+        return (k * (int)cs1 * (C2 + 2)) + j * (int)cs1 + i;
+    }
+    __host__ __device__ __forceinline__ int fi(int i, int j, int k) const {
+        return (k * (int)fs1 * (C2 + 3)) + j * (int)fs1 + i;
+    }
     __host__ __device__ int64_t ncell() const { return cs2 * (C3 + 2); }
     __host__ __device__ int64_t nface() const { return fs2 * (C3 + 3); }
 };
+
+// Tiling of the per-cell kernels: a block covers kTileX x kTileY cells of a k-column chunk
+// of kTileK planes and marches through it in k.  The reductions that TimeStepSize and the
+// bulk forcing need are taken per block into partial slots (one per block).
+constexpr int kTileX = 64, kTileY = 2, kTileK = 16;
+__host__ __device__ inline int tiles_x(const Geom &g) { return (g.C1 + kTileX - 1) / kTileX; }
+__host__ __device__ inline int tiles_y(const Geom &g) { return (g.C2 + kTileY - 1) / kTileY; }
+__host__ __device__ inline int tiles_k(const Geom &g) { return (g.C3 + kTileK - 1) / kTileK; }
+__host__ __device__ inline int tile_count(const Geom &g) { return tiles_x(g) * tiles_y(g) * tiles_k(g); }
 
 // Sticky device status bits.
 enum : int { STATUS_NONFINITE = 1 };
@@ -61,44 +77,60 @@ struct Consts {
 struct DevScalars {
     double dt, time, ub, G;
     long long nstep;
-    unsigned long long umax[3]; // max |u_d| of the "Con" level, as IEEE bit patterns
-    long long usum;             // sum of u1 over fluid cells, 2^-32 fixed point
-    long long nfluid;           // fluid cells (condition == 0), set at upload
-    int status;                 // sticky error bits (ARK_ERR_NONFINITE)
+    long long nfluid;  // fluid cells (condition == 0), set at upload
+    int status;        // sticky error bits (STATUS_NONFINITE)
     int pad;
-    long long sums[5];          // conservation sums (fixed point), see ark_sums
+    long long sums[5]; // conservation sums (fixed point), see ark_sums
     long long sum_cells;
 };
 
 template <class T> struct DevState {
     Geom g;
     Consts k;
-    Level<T> lv[2];
+    Level<T> lv[2];  // the two cell levels; which one is "Con" is passed to each kernel
     T *f[3];
-    FaceSet<T> fc[3];
-    T *sig[3][3]; // sig[d][m]: component m on faces normal to d (nullptr unless kept)
+    FaceSet<T> fc[2][3]; // two face generations: Phase2 reads fc[cur] and writes fc[cur^1]
+    T *sig[3][3];        // sig[d][m]: component m on faces normal to d (nullptr unless kept)
     uint8_t *flags;
     DevScalars *sc;
+    // per-tile partials: max |u_d| of the "Con" level as IEEE double bit patterns (3 per
+    // tile) and the fixed-point sum of u1 over fluid cells of the "nCon" level (1 per tile)
+    unsigned long long *part_max;
+    long long *part_sum;
 };
 
+// FP32 contexts store the density deviation rho - ro0 in the cell levels and derive face
+// density from face pressure (ro0 + p / c^2); FP64 contexts store rho itself, as the
+// reference does, so its arithmetic is mirrored operation by operation.
+template <class T> struct Storage { static constexpr bool deviation = false; };
+template <> struct Storage<float> { static constexpr bool deviation = true; };
+
 // Launch entry points (defined per precision in ark_fp64.cu / ark_fp32.cu).
-enum Phase1Mode { P1_PLAIN = 0, P1_STRESS = 1, P1_FORCES = 2, P1_BULK = 4 };
+// P1_RMAX / P1_RSUM: also take the dt partials (max |u| of the level written) or the bulk-flow
+// partials (sum of u1 of the level written) for the next step.
+enum Phase1Mode { P1_PLAIN = 0, P1_STRESS = 1, P1_FORCES = 2, P1_BULK = 4, P1_RMAX = 8, P1_RSUM = 16 };
 
 template <class T> struct Launch {
-    static void reduce_start(const DevState<T> &S, int con, int with_sum, cudaStream_t st);
+    static void reduce_start(const DevState<T> &S, int con, cudaStream_t st);
     static void finalize_dt(const DevState<T> &S, int advance_time, cudaStream_t st);
     static void wrap_cells(const DevState<T> &S, T *const *arrs, int n, cudaStream_t st);
-    static void wrap_phase2(const DevState<T> &S, int con, cudaStream_t st);
-    static void phase1(const DevState<T> &S, int src, int dst, int mode, cudaStream_t st);
+    static void wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st);
+    static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, cudaStream_t st);
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
-    static void sweep(const DevState<T> &S, int con, int axis, cudaStream_t st);
+    static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st);
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
 };
 
-// double <-> T copies for FP32 contexts (host arrays are always double)
-template <class T> void convert_from_double(T *dst, const double *src, int64_t n, cudaStream_t st);
-template <class T> void convert_to_double(double *dst, const T *src, int64_t n, cudaStream_t st);
+// double <-> T copies for FP32 contexts (host arrays are always double):
+// dst = (T)(src - offset) and dst = (double)src + offset.
+template <class T>
+void convert_from_double(T *dst, const double *src, int64_t n, double offset, cudaStream_t st);
+template <class T>
+void convert_to_double(double *dst, const T *src, int64_t n, double offset, cudaStream_t st);
+// face density of an FP32 context: dst = ro0 + (double)p * rc2
+template <class T>
+void face_density_to_double(double *dst, const T *p, int64_t n, double ro0, double rc2, cudaStream_t st);
 
 } // namespace ark
