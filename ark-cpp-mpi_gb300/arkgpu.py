@@ -30,7 +30,7 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_boundary_fill", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
            "ark_get_scalars", "ark_set_scalars", "ark_conservation_sums", "ark_channel_init",
            "ark_kernel_times", "ark_kernel_name", "ark_alloc_host_state", "ark_free_host_state",
-           "ark_conservation_sums_noalloc")
+           "ark_conservation_sums_noalloc", "ark_mean_profile", "ark_selftest_division")
 
 
 class ArkError(RuntimeError):
@@ -107,6 +107,8 @@ def lib():
         L.ark_kernel_name.argtypes = [ctypes.c_int]
         L.ark_alloc_host_state.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(HostState)]
         L.ark_free_host_state.argtypes = [ctypes.POINTER(HostState)]
+        L.ark_mean_profile.argtypes = [vp, _DP, _DP]
+        L.ark_selftest_division.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_longlong)]
         L.ark_conservation_sums_noalloc.argtypes = [ctypes.POINTER(Params)] + [ctypes.c_void_p] * 5 + [
             ctypes.POINTER(Sums)]
         _lib = L
@@ -303,6 +305,13 @@ class Context:
 
     def set_scalars(self, s: Scalars):
         self._call("ark_set_scalars", ctypes.byref(s))
+
+    def mean_profile(self):
+        """(mean u1 per y plane, (wall shear at y = -ly/2, at y = +ly/2))."""
+        prof = np.empty(self.p.n2_cells)
+        ws = np.empty(2)
+        self._call("ark_mean_profile", prof.ctypes.data_as(_DP), ws.ctypes.data_as(_DP))
+        return prof, ws
 
     def sums(self) -> Sums:
         s = Sums()

@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -63,6 +64,25 @@ Geom make_geom(const ark_params &p) {
     return g;
 }
 
+template <class T> void fill_kt(const Consts &k, KT<T> &t) {
+    for (int d = 0; d < 3; ++d) {
+        t.dx[d] = (T)k.dx[d];
+        t.rdx[d] = (T)k.rdx[d];
+        t.vrdx[d] = (T)(k.vis * k.rdx[d]);
+        t.ds[d] = (T)k.ds[d];
+    }
+    t.dvc = (T)k.dvc;
+    t.rdvc = (T)(1.0 / k.dvc);
+    t.vis = (T)k.vis;
+    t.two_vis = (T)k.two_vis;
+    t.sound = (T)k.sound;
+    t.ro0 = (T)k.ro0;
+    t.c2 = (T)k.c2;
+    t.rc2 = (T)k.rc2;
+    t.roc = (T)k.roc;
+    t.rroc = (T)k.rroc;
+}
+
 // Run constants, evaluated exactly as the reference evaluates them: grid steps as
 // InitializeData forms them (main.cpp:284-290, domain [0,lx] x [-ly/2,ly/2] x [0,lz]),
 // areas and volume as Phase1 (main.cpp:456-462), dt numerators as TimeStepSize.
@@ -98,6 +118,8 @@ Consts make_consts(const ark_params &p) {
     }
     k.u_target = p.u_target;
     k.forcing = p.forcing;
+    fill_kt(k, k.kd);
+    fill_kt(k, k.kf);
     return k;
 }
 
@@ -124,6 +146,7 @@ struct Engine {
     virtual void step(int con, int fcur, cudaEvent_t *ev) = 0;
     virtual void boundary_fill(int ncon, int axis, int periodic) = 0;
     virtual void sums(int ncon) = 0;
+    virtual void mean_profile(int ncon, long long *acc) = 0;
     virtual DevScalars *scalars() = 0;
     virtual uint8_t *flags() = 0;
 };
@@ -141,6 +164,7 @@ struct ark_ctx {
     int fcur = 0; // the current face generation
     bool uploaded = false;
     bool parts_valid = false; // the dt / bulk-flow partials describe the current state
+    int march[2] = {1, 0};    // Phase1 kernel shape of the two Phase1 launches of a step
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [con][fcur]
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double *stage = nullptr; // device double staging for FP32 contexts
@@ -195,8 +219,8 @@ template <class T> struct EngineT : Engine {
             }
         rc |= get(&S.flags, nc);
         rc |= get(&S.sc, 1);
-        rc |= get(&S.part_max, 3 * (size_t)tile_count(S.g));
-        rc |= get(&S.part_sum, (size_t)tile_count(S.g));
+        rc |= get(&S.part_max, 3 * (size_t)kBuckets);
+        rc |= get(&S.part_sum, (size_t)kBuckets);
         if (rc) return ARK_ERR_NOMEM;
         return ARK_OK;
     }
@@ -291,13 +315,21 @@ template <class T> struct EngineT : Engine {
         return nullptr;
     }
 
+    void clear_parts() {
+        cudaMemsetAsync(S.part_max, 0, sizeof(unsigned long long) * 3 * kBuckets, ctx->st);
+        cudaMemsetAsync(S.part_sum, 0, sizeof(long long) * kBuckets, ctx->st);
+    }
     void time_step_size(int con, int advance) override {
+        clear_parts();
         Launch<T>::reduce_start(S, con, ctx->st);
         Launch<T>::finalize_dt(S, advance, ctx->st);
     }
-    void reduce(int con) override { Launch<T>::reduce_start(S, con, ctx->st); }
+    void reduce(int con) override {
+        clear_parts();
+        Launch<T>::reduce_start(S, con, ctx->st);
+    }
     void phase1(int src, int dst, int fcur, int mode) override {
-        Launch<T>::phase1(S, src, dst, fcur, mode, ctx->st);
+        Launch<T>::phase1(S, src, dst, fcur, mode, ctx->march[0], ctx->st);
     }
     void stress(int con, int bulk) override {
         T *u[3] = {S.lv[con].u1, S.lv[con].u2, S.lv[con].u3};
@@ -328,7 +360,8 @@ template <class T> struct EngineT : Engine {
         T *cells[4] = {S.lv[y].u1, S.lv[y].u2, S.lv[y].u3, S.lv[y].ro};
         Launch<T>::wrap_cells(S, cells, 4, st);
         mark(1);
-        Launch<T>::phase1(S, y, x, fcur, P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0), st);
+        Launch<T>::phase1(S, y, x, fcur, P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0),
+                          ctx->march[0], st);
         mark(2);
         Launch<T>::wrap_phase2(S, y, fcur, st);
         mark(3);
@@ -336,21 +369,21 @@ template <class T> struct EngineT : Engine {
             Launch<T>::sweep(S, y, fcur, ax, st);
             mark(4 + ax);
         }
-        Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, st);
+        Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
         mark(7);
     }
     void boundary_fill(int ncon, int axis, int periodic) override {
         Launch<T>::boundary_fill(S, ncon, axis, periodic, ctx->st);
     }
     void sums(int ncon) override { Launch<T>::sums(S, ncon, ctx->st); }
+    void mean_profile(int ncon, long long *acc) override { Launch<T>::mean_profile(S, ncon, acc, ctx->st); }
     DevScalars *scalars() override { return S.sc; }
     uint8_t *flags() override { return S.flags; }
 };
 
 int check_params(const ark_params *p) {
     if (!p) return fail(ARK_ERR_PARAM, "params is NULL");
-    if (p->n1_cells < 2 || p->n2_cells < 1 || p->n3_cells < 2)
-        return fail(ARK_ERR_PARAM, "need at least 2 x 1 x 2 cells");
+    if (p->n1_cells < 1 || p->n2_cells < 1 || p->n3_cells < 1) return fail(ARK_ERR_PARAM, "need at least one cell per axis");
     const double faces = (double)(p->n1_cells + 3) * (p->n2_cells + 3) * (p->n3_cells + 3);
     if (faces >= 2147483647.0) return fail(ARK_ERR_PARAM, "grid too large: arrays are indexed with 32 bits");
     if (!(p->lx > 0) || !(p->ly > 0) || !(p->lz > 0)) return fail(ARK_ERR_PARAM, "domain extents must be > 0");
@@ -360,6 +393,14 @@ int check_params(const ark_params *p) {
     if (!p->periodic_x || !p->periodic_z)
         return fail(ARK_ERR_UNSUPPORTED, "bounded x or z (inflow/outflow, zero-gradient edges) is not implemented");
     return ARK_OK;
+}
+
+// dt and the copies the kernels read (1/dt, and both rounded to FP32)
+void set_dt_fields(DevScalars &sc, double dt) {
+    sc.dt = dt;
+    sc.rdt = 1.0 / dt;
+    sc.dtf = (float)dt;
+    sc.rdtf = (float)(1.0 / dt);
 }
 
 int check_ctx(ark_ctx *ctx, bool need_state) {
@@ -427,6 +468,15 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
             *status = fail(ARK_ERR_NOMEM, "staging allocation failed");
             return nullptr;
         }
+    }
+    // Phase1 kernel shapes measured fastest on GB300: FP32 marches the stress Phase1 in k
+    // (1.05 vs 1.27 ms at 512x256x256) and runs the second Phase1 one cell per thread (0.78 vs
+    // 0.93 ms); FP64 is ALU-bound and prefers one cell per thread for both (2.88 vs 2.98 ms).
+    ctx->march[0] = params->precision == ARK_FP32 ? 1 : 0;
+    ctx->march[1] = 0;
+    if (const char *e = std::getenv("ARK_PHASE1_MARCH")) { // "ab": a for Phase1 with stress, b without
+        if (e[0] == '0' || e[0] == '1') ctx->march[0] = e[0] - '0';
+        if (e[0] && (e[1] == '0' || e[1] == '1')) ctx->march[1] = e[1] - '0';
     }
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
@@ -585,8 +635,11 @@ int ark_boundary_fill(ark_ctx *ctx, int axis) {
 
 int ark_set_dt(ark_ctx *ctx, double dt) {
     if (int rc = check_ctx(ctx, true)) return rc;
+    DevScalars sc;
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
-    ARK_CUDA(cudaMemcpy(&ctx->eng->scalars()->dt, &dt, sizeof(double), cudaMemcpyHostToDevice));
+    ARK_CUDA(cudaMemcpy(&sc, ctx->eng->scalars(), sizeof(sc), cudaMemcpyDeviceToHost));
+    set_dt_fields(sc, dt);
+    ARK_CUDA(cudaMemcpy(ctx->eng->scalars(), &sc, sizeof(sc), cudaMemcpyHostToDevice));
     return ARK_OK;
 }
 
@@ -744,11 +797,12 @@ int ark_set_scalars(ark_ctx *ctx, const ark_scalars *in) {
     DevScalars sc;
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
     ARK_CUDA(cudaMemcpy(&sc, ctx->eng->scalars(), sizeof(sc), cudaMemcpyDeviceToHost));
-    sc.dt = in->dt;
+    set_dt_fields(sc, in->dt);
     sc.time = in->time;
     sc.nstep = in->nstep;
     sc.ub = in->bulk_velocity;
     sc.G = in->bulk_force;
+    sc.Gf = (float)in->bulk_force;
     ARK_CUDA(cudaMemcpy(ctx->eng->scalars(), &sc, sizeof(sc), cudaMemcpyHostToDevice));
     return ARK_OK;
 }
@@ -770,6 +824,45 @@ int ark_conservation_sums(ark_ctx *ctx, ark_sums *out) {
     out->momentum3 = (double)v[3] * q;
     out->kinetic = (double)v[4] * q;
     out->cells = v[5];
+    return ARK_OK;
+}
+
+int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches) {
+    if (!mismatches || n < 0) return fail(ARK_ERR_PARAM, "bad arguments");
+    unsigned long long *bad = nullptr;
+    ARK_CUDA(cudaMalloc(&bad, sizeof(unsigned long long)));
+    cudaMemset(bad, 0, sizeof(unsigned long long));
+    selftest_division(n, seed, bad, 0);
+    cudaError_t e = cudaGetLastError();
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    if (e != cudaSuccess) return fail(ARK_ERR_CUDA, std::string("selftest: ") + cudaGetErrorString(e));
+    *mismatches = (long long)h;
+    return ARK_OK;
+}
+
+int ark_mean_profile(ark_ctx *ctx, double *mean_u1, double *wall_shear) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!mean_u1) return fail(ARK_ERR_PARAM, "mean_u1 is NULL");
+    const int n = ctx->g.C2;
+    long long *acc = nullptr;
+    ARK_CUDA(cudaMallocAsync((void **)&acc, sizeof(long long) * 2 * n, ctx->st));
+    ctx->eng->mean_profile(ctx->con ^ 1, acc);
+    int rc = launch_status(ctx);
+    std::vector<long long> h(2 * (size_t)n);
+    if (!rc && cudaMemcpyAsync(h.data(), acc, sizeof(long long) * 2 * n, cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess)
+        rc = fail(ARK_ERR_CUDA, "profile copy failed");
+    cudaFreeAsync(acc, ctx->st);
+    if (!rc) ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    if (rc) return rc;
+    for (int j = 0; j < n; ++j)
+        mean_u1[j] = h[2 * j + 1] > 0 ? ((double)h[2 * j] * (1.0 / 4294967296.0)) / (double)h[2 * j + 1] : 0.0;
+    if (wall_shear) {
+        // one-sided wall form of StressTensor (main.cpp:924-927): 2*VIS*u_c/dx2 at both walls
+        wall_shear[0] = 2 * ctx->P.vis * mean_u1[0] / ctx->k.dx[1];
+        wall_shear[1] = 2 * ctx->P.vis * mean_u1[n - 1] / ctx->k.dx[1];
+    }
     return ARK_OK;
 }
 

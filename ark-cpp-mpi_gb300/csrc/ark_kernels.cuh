@@ -41,12 +41,32 @@ template <class T> __device__ __forceinline__ T max3d(T x1, T x2, T x3) {
     return x1;
 }
 
-// Division by a run constant b whose reciprocal rb is known.  FP64: the IEEE quotient
-// (the parity bar).  FP32: multiplication by the reciprocal.
-__device__ __forceinline__ double divk(double a, double b, double rb) {
-    (void)rb;
-    return a / b;
+// True when a double is +0 or -0 (integer test: keeps the FP64 pipe free).
+__device__ __forceinline__ bool is_zero(double r) { return (__double_as_longlong(r) << 1) == 0; }
+
+// a / b correctly rounded, given rb = RN(1/b) (the IEEE reciprocal).  Markstein's theorem
+// (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990): if rb is within half an ulp of 1/b and q is
+// within one ulp of a/b, then with the exact residual r = a - b*q (one FMA),
+// RN(q + r*rb) = RN(a/b).  q = RN(a*rb) may be up to 1.5 ulp off, so one correction makes
+// it faithful and a second one makes it correctly rounded: 1 multiply + 4 FMA.  A zero
+// residual means q is already exact, and is kept as is so the sign of a zero quotient is
+// the IEEE one.  The FP64 parity tests check every quotient of the step against the
+// reference bit for bit, and ark_selftest_division compares with the hardware division.
+__device__ __forceinline__ double div_rn(double a, double b, double rb) {
+    double q = a * rb;
+    double r = __fma_rn(-q, b, a);
+    if (!is_zero(r)) {
+        q = __fma_rn(r, rb, q);
+        r = __fma_rn(-q, b, a);
+        if (!is_zero(r)) q = __fma_rn(r, rb, q);
+    }
+    return q;
 }
+
+// Division by a run constant b whose reciprocal rb is known.  FP64: the correctly rounded
+// quotient (the parity bar).  FP32: multiplication by the reciprocal.
+__device__ __forceinline__ double divk(double a, double b, double rb) { return div_rn(a, b, rb); }
 __device__ __forceinline__ float divk(float a, float b, float rb) {
     (void)b;
     return a * rb;
@@ -56,28 +76,18 @@ __device__ __forceinline__ float divk(float a, float b, float rb) {
 __device__ __forceinline__ double divv(double a, double b) { return a / b; }
 __device__ __forceinline__ float divv(float a, float b) { return __fdiv_rn(a, b); }
 
-// Run constants rounded to T.
-template <class T> struct K {
-    T dx[3], rdx[3], ds[3], dvc, rdvc, vis, two_vis, sound, ro0, c2, rc2, roc, rroc;
-    __device__ __forceinline__ explicit K(const Consts &k) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            dx[d] = (T)k.dx[d];
-            rdx[d] = (T)k.rdx[d];
-            ds[d] = (T)k.ds[d];
-        }
-        dvc = (T)k.dvc;
-        rdvc = (T)(1.0 / k.dvc);
-        vis = (T)k.vis;
-        two_vis = (T)k.two_vis;
-        sound = (T)k.sound;
-        ro0 = (T)k.ro0;
-        c2 = (T)k.c2;
-        rc2 = (T)k.rc2;
-        roc = (T)k.roc;
-        rroc = (T)k.rroc;
-    }
-};
+// Reciprocal of a cell-dependent value for divr below: IEEE 1/b (FP64), or 1/b (FP32).
+__device__ __forceinline__ double recip(double b) { return __drcp_rn(b); }
+__device__ __forceinline__ float recip(float b) { return __frcp_rn(b); }
+// a / b with rb = recip(b): correctly rounded in FP64, a*rb in FP32.
+__device__ __forceinline__ double divr(double a, double b, double rb) { return div_rn(a, b, rb); }
+__device__ __forceinline__ float divr(float a, float b, float rb) {
+    (void)b;
+    return a * rb;
+}
+
+// Run constants rounded to T (filled on the host).
+template <class T> using K = KT<T>;
 
 // ---------------------------------------------------------------------------------------
 // TimeStepSize + bulk flow rate
@@ -136,7 +146,7 @@ __device__ __forceinline__ int tile_index() {
     return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
 }
 
-// Block-wide combination of the per-thread partials into this tile's slots.  Every thread of
+// Block-wide combination of the per-thread partials into the block's slot.  Every thread of
 // the block must call it.
 template <class T>
 __device__ __forceinline__ void tile_store(const DevState<T> &S, bool do_max, bool do_sum, unsigned long long m0,
@@ -155,21 +165,22 @@ __device__ __forceinline__ void tile_store(const DevState<T> &S, bool do_max, bo
         ssum[w] = s;
     }
     __syncthreads();
-    const int tile = tile_index();
+    const int slot = tile_index() % kBuckets;
     if (t < 3 && do_max) {
         unsigned long long m = 0;
         for (int v = 0; v < kTileX * kTileY / 32; ++v) m = smax[t][v] > m ? smax[t][v] : m;
-        S.part_max[3 * tile + t] = key_to_double_bits(m, T());
+        if (m) atomicMax(&S.part_max[3 * slot + t], key_to_double_bits(m, T()));
     } else if (t == 3 && do_sum) {
         long long z = 0;
         for (int v = 0; v < kTileX * kTileY / 32; ++v) z += ssum[v];
-        S.part_sum[tile] = z;
+        if (z) atomicAdd((unsigned long long *)&S.part_sum[slot], (unsigned long long)z);
     }
 }
 
 // Standalone partials of the step start (used after an upload or the reference-order calls;
 // the fused step takes the same partials inside its Phase1 kernels): max |u_d| of level
-// `con` and the fixed-point sum of u1 over fluid cells of level `con^1`, tile by tile.
+// `con` and the fixed-point sum of u1 over fluid cells of level `con^1`.  The slots must be
+// clear.
 // dt is monotone in max |u|: min over cells of CFL*dx/(c + |u|) is CFL*dx/(c + max|u|)
 // exactly, since IEEE + and / are monotone.  Max and integer sums are order independent.
 template <class T> __global__ void __launch_bounds__(kTileX *kTileY) k_reduce_start(DevState<T> S, int con) {
@@ -200,18 +211,21 @@ template <class T> __global__ void __launch_bounds__(kTileX *kTileY) k_reduce_st
     tile_store(S, true, true, m0, m1, m2, s);
 }
 
-// One block: combine the tile partials, form dt as TimeStepSize does, then the bulk force.
-template <class T> __global__ void __launch_bounds__(1024) k_finalize_dt(DevState<T> S, int advance_time, int ntiles) {
+// One block: combine (and clear) the partial slots, form dt as TimeStepSize does, then the
+// bulk force.
+template <class T> __global__ void __launch_bounds__(1024) k_finalize_dt(DevState<T> S, int advance_time) {
     __shared__ unsigned long long smax[3][32];
     __shared__ long long ssum[32];
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long s = 0;
-    for (int q = threadIdx.x; q < ntiles; q += blockDim.x) {
+    for (int q = threadIdx.x; q < kBuckets; q += blockDim.x) {
         const unsigned long long a = S.part_max[3 * q], b = S.part_max[3 * q + 1], c = S.part_max[3 * q + 2];
         m0 = a > m0 ? a : m0;
         m1 = b > m1 ? b : m1;
         m2 = c > m2 ? c : m2;
         s += S.part_sum[q];
+        S.part_max[3 * q] = S.part_max[3 * q + 1] = S.part_max[3 * q + 2] = 0;
+        S.part_sum[q] = 0;
     }
     m0 = warp_max_u64(m0);
     m1 = warp_max_u64(m1);
@@ -250,10 +264,14 @@ template <class T> __global__ void __launch_bounds__(1024) k_finalize_dt(DevStat
     const double dtu = min3d(dtu1, dtu2, dtu3);
     const double dt = min3d(1e8, dtu, k.dtv);
     sc->dt = dt;
+    sc->rdt = 1.0 / dt;
+    sc->dtf = (float)dt;
+    sc->rdtf = (float)(1.0 / dt);
     if (k.forcing) {
         const double ub = sc->nfluid > 0 ? ((double)s * FixedScale<T>::inv) / (double)sc->nfluid : 0.0;
         sc->ub = ub;
         sc->G = (k.u_target - ub) / dt;
+        sc->Gf = (float)sc->G;
     }
     if (advance_time) {
         sc->nstep += 1;
@@ -380,7 +398,7 @@ __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6]
         T aw[6], ac[6]; // per face: coefficient on the cell behind (w) and ahead (c)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const T v = kk.vis * kk.rdx[d];
+            const T v = kk.vrdx[d];
 #pragma unroll
             for (int side = 0; side < 2; ++side) {
                 const uint8_t fw = side ? fl : fln[2 * d], fc = side ? fln[2 * d + 1] : fl;
@@ -426,7 +444,7 @@ __device__ __forceinline__ FaceVal<T> load_face(const FaceSet<T> &F, int f, cons
 // lo[d] (west/south/bottom) and hi[d] (east/north/top).  ro_c: density (FP64) or deviation.
 template <class T>
 __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<T> hi[3], T ro_c, const T uc[3],
-                                          T dt, const K<T> &kk, T &ro_cn, T ucn[3]) {
+                                          T dt, const K<T> &kk, T &ro_cn, T ucn[3], T &rden_out) {
     if (!Storage<T>::deviation) {
         // new density (main.cpp:530-533)
         ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
@@ -435,7 +453,11 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
                      kk.dvc, kk.rdvc);
         // momentum (main.cpp:536-551): the flux of u_m through faces normal to d is
         // (ro*u_m)*u_d, plus p when m == d
+        // one reciprocal serves the three momentum quotients (and UseForces, whose divisor
+        // dvc*ro_cn is the same product)
         const T den = ro_cn * kk.dvc;
+        const T rden = recip(den);
+        rden_out = rden;
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
             T fx[3];
@@ -446,8 +468,8 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
                 else
                     fx[d] = hi[d].ro * hi[d].u[m] * hi[d].u[d] - lo[d].ro * lo[d].u[m] * lo[d].u[d];
             }
-            ucn[m] = divv(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx[0] * kk.ds[0] + fx[1] * kk.ds[1] + fx[2] * kk.ds[2]),
-                          den);
+            ucn[m] = divr(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx[0] * kk.ds[0] + fx[1] * kk.ds[1] + fx[2] * kk.ds[2]),
+                          den, rden);
         }
     } else {
         // the same balance with the volume divided out and the density as a deviation:
@@ -457,6 +479,7 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
                             (hi[1].ro * hi[1].u[1] - lo[1].ro * lo[1].u[1]) * kk.ds[1] +
                             (hi[2].ro * hi[2].u[2] - lo[2].ro * lo[2].u[2]) * kk.ds[2]);
         const T rden = (T)1 / (kk.ro0 + ro_cn);
+        rden_out = rden;
         const T ro_cf = kk.ro0 + ro_c;
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
@@ -489,8 +512,8 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int sr
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long rsum = 0;
     if (i <= g.C1 && j <= g.C2) {
-        const K<T> kk(S.k);
-        const T dt = (T)S.sc->dt;
+        const K<T> &kk = kconst<T>(S.k);
+        const T dt = sc_dt<T>(S.sc);
         const T *__restrict__ sro = S.lv[src].ro;
         const T *__restrict__ su1 = S.lv[src].u1;
         const T *__restrict__ su2 = S.lv[src].u2;
@@ -501,7 +524,7 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int sr
         T *__restrict__ du3 = S.lv[dst].u3;
         const uint8_t *__restrict__ flags = S.flags;
         const int cs1 = (int)g.cs1, cs2 = (int)g.cs2, fs1 = (int)g.fs1, fs2 = (int)g.fs2;
-        const T G = (MODE & P1_BULK) ? (T)S.sc->G : (T)0;
+        const T G = (MODE & P1_BULK) ? sc_G<T>(S.sc) : (T)0;
         int c = g.ci(i, j, k0), fw = g.fi(i, j, k0);
         FaceVal<T> bot = load_face(S.fc[fcur][2], fw, kk);
         // stress state carried up the column: the cell below and the current cell
@@ -535,7 +558,7 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int sr
                 uc[2] = su3[c];
             }
             const FaceVal<T> top = load_face(S.fc[fcur][2], fw + fs2, kk);
-            T ro_cn, ucn[3];
+            T ro_cn, ucn[3], rden = (T)0;
             if (fl & FL_LT) {
                 FaceVal<T> lo[3], hi[3];
                 lo[0] = load_face(S.fc[fcur][0], fw, kk);
@@ -544,7 +567,7 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int sr
                 hi[1] = load_face(S.fc[fcur][1], fw + fs1, kk);
                 lo[2] = bot;
                 hi[2] = top;
-                half_step(lo, hi, ro_c, uc, dt, kk, ro_cn, ucn);
+                half_step(lo, hi, ro_c, uc, dt, kk, ro_cn, ucn, rden);
             } else {
                 ucn[0] = ucn[1] = ucn[2] = (T)0;
                 ro_cn = DEV ? (T)0 : kk.ro0;
@@ -594,13 +617,14 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int sr
                 f[2] = __ldg(S.f[2] + c);
             }
             if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
-                // UseForces (main.cpp:1035-1041)
+                // UseForces (main.cpp:1035-1041); a fluid cell always went through half_step,
+                // so rden is 1/(dvc*ro_cn) (FP64) or 1/(ro0 + ro'_cn) (FP32)
                 if (!DEV) {
                     const T den = kk.dvc * ro_cn;
 #pragma unroll
-                    for (int m = 0; m < 3; ++m) ucn[m] = divv(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den);
+                    for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
                 } else {
-                    const T g2 = (T)0.5 * dt * kk.rdvc / (kk.ro0 + ro_cn);
+                    const T g2 = (T)0.5 * dt * kk.rdvc * rden;
 #pragma unroll
                     for (int m = 0; m < 3; ++m) ucn[m] += g2 * f[m];
                 }
@@ -622,6 +646,95 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int sr
     if (MODE & (P1_RMAX | P1_RSUM)) tile_store(S, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
 }
 
+// Phase1 with one cell per thread (grid z over all planes): fewer registers than the marching
+// kernel, so more warps in flight.  Same arithmetic and outputs as k_phase1.
+template <class T, int MODE>
+__global__ void __launch_bounds__(kTileX *kTileY) k_phase1_cell(DevState<T> S, int src, int dst, int fcur) {
+    constexpr bool DEV = Storage<T>::deviation;
+    const Geom g = S.g;
+    const int i = blockIdx.x * kTileX + threadIdx.x + 1;
+    const int j = blockIdx.y * kTileY + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    unsigned long long m0 = 0, m1 = 0, m2 = 0;
+    long long rsum = 0;
+    if (i <= g.C1 && j <= g.C2) {
+        const K<T> &kk = kconst<T>(S.k);
+        const T dt = sc_dt<T>(S.sc);
+        const T *__restrict__ sro = S.lv[src].ro;
+        const T *__restrict__ su1 = S.lv[src].u1;
+        const T *__restrict__ su2 = S.lv[src].u2;
+        const T *__restrict__ su3 = S.lv[src].u3;
+        const uint8_t *__restrict__ flags = S.flags;
+        const int cs1 = (int)g.cs1, cs2 = (int)g.cs2, fs1 = (int)g.fs1, fs2 = (int)g.fs2;
+        const int c = g.ci(i, j, k), fw = g.fi(i, j, k);
+        const uint8_t fl = flags[c];
+        const T ro_c = sro[c];
+        const T uc[3] = {su1[c], su2[c], su3[c]};
+        T ro_cn, ucn[3], rden = (T)0;
+        if (fl & FL_LT) {
+            FaceVal<T> lo[3], hi[3];
+            lo[0] = load_face(S.fc[fcur][0], fw, kk);
+            hi[0] = load_face(S.fc[fcur][0], fw + 1, kk);
+            lo[1] = load_face(S.fc[fcur][1], fw, kk);
+            hi[1] = load_face(S.fc[fcur][1], fw + fs1, kk);
+            lo[2] = load_face(S.fc[fcur][2], fw, kk);
+            hi[2] = load_face(S.fc[fcur][2], fw + fs2, kk);
+            half_step(lo, hi, ro_c, uc, dt, kk, ro_cn, ucn, rden);
+        } else {
+            ucn[0] = ucn[1] = ucn[2] = (T)0;
+            ro_cn = DEV ? (T)0 : kk.ro0;
+        }
+        T f[3] = {(T)0, (T)0, (T)0};
+        if (MODE & P1_STRESS) {
+            if (fl & FL_EQ0) {
+                const int nb[6] = {c - 1, c + 1, c - cs1, c + cs1, c - cs2, c + cs2};
+                uint8_t fln[6];
+                T un[6][3];
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    fln[q] = flags[nb[q]];
+                    un[q][0] = su1[nb[q]];
+                    un[q][1] = su2[nb[q]];
+                    un[q][2] = su3[nb[q]];
+                }
+                const T ro_cf = DEV ? kk.ro0 + ro_c : ro_c;
+                stress_force(fln, un, fl, uc, ro_cf, kk, f);
+                if (MODE & P1_BULK) f[0] = f[0] + (ro_cf * kk.dvc) * sc_G<T>(S.sc);
+            }
+            S.f[0][c] = f[0];
+            S.f[1][c] = f[1];
+            S.f[2][c] = f[2];
+        } else if (MODE & P1_FORCES) {
+            f[0] = __ldg(S.f[0] + c);
+            f[1] = __ldg(S.f[1] + c);
+            f[2] = __ldg(S.f[2] + c);
+        }
+        if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
+            // UseForces (main.cpp:1035-1041), with the reciprocal half_step formed
+            if (!DEV) {
+                const T den = kk.dvc * ro_cn;
+#pragma unroll
+                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
+            } else {
+                const T g2 = (T)0.5 * dt * kk.rdvc * rden;
+#pragma unroll
+                for (int m = 0; m < 3; ++m) ucn[m] += g2 * f[m];
+            }
+        }
+        S.lv[dst].ro[c] = ro_cn;
+        S.lv[dst].u1[c] = ucn[0];
+        S.lv[dst].u2[c] = ucn[1];
+        S.lv[dst].u3[c] = ucn[2];
+        if (MODE & P1_RMAX) {
+            m0 = abs_key(ucn[0]);
+            m1 = abs_key(ucn[1]);
+            m2 = abs_key(ucn[2]);
+        }
+        if ((MODE & P1_RSUM) && (fl & FL_EQ0)) rsum = fixed_sum_term(ucn[0]);
+    }
+    if (MODE & (P1_RMAX | P1_RSUM)) tile_store(S, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+}
+
 // StressTensor's face stresses into the sigm arrays (kept only on request), faces normal
 // to d with index 1..C_d+1 along d (main.cpp:856-982).
 template <class T> __global__ void k_stress_faces(DevState<T> S, int con, int d) {
@@ -631,7 +744,7 @@ template <class T> __global__ void k_stress_faces(DevState<T> S, int con, int d)
     const int k = blockIdx.z + 1;
     const int hi0 = g.C1 + (d == 0), hi1 = g.C2 + (d == 1), hi2 = g.C3 + (d == 2);
     if (i > hi0 || j > hi1 || k > hi2) return;
-    const K<T> kk(S.k);
+    const K<T> &kk = kconst<T>(S.k);
     const Level<T> L = S.lv[con];
     const int64_t c = g.cell(i, j, k);
     const int64_t cw = c - (d == 0 ? 1 : d == 1 ? g.cs1 : g.cs2);
@@ -653,7 +766,7 @@ template <class T> __global__ void k_stress_force(DevState<T> S, int con, int bu
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.C1 || j > g.C2) return;
-    const K<T> kk(S.k);
+    const K<T> &kk = kconst<T>(S.k);
     const Level<T> L = S.lv[con];
     const int64_t c = g.cell(i, j, k);
     const uint8_t fl = S.flags[c];
@@ -671,7 +784,7 @@ template <class T> __global__ void k_stress_force(DevState<T> S, int con, int bu
             un[q][2] = L.u3[nb[q]];
         }
         stress_force(fln, un, fl, uc, ro_c, kk, f);
-        if (bulk) f[0] = f[0] + (ro_c * kk.dvc) * (T)S.sc->G;
+        if (bulk) f[0] = f[0] + (ro_c * kk.dvc) * sc_G<T>(S.sc);
     }
     S.f[0][c] = f[0];
     S.f[1][c] = f[1];
@@ -688,17 +801,18 @@ template <class T> __global__ void k_use_forces(DevState<T> S, int ncon) {
     if (i > g.C1 || j > g.C2) return;
     const int64_t c = g.cell(i, j, k);
     if (!(S.flags[c] & FL_EQ0)) return;
-    const K<T> kk(S.k);
-    const T dt = (T)S.sc->dt;
+    const K<T> &kk = kconst<T>(S.k);
+    const T dt = sc_dt<T>(S.sc);
     const Level<T> L = S.lv[ncon];
     if (!DEV) {
         const T ro_cn = L.ro[c];
         const T den = kk.dvc * ro_cn;
-        L.u1[c] = divv(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den);
-        L.u2[c] = divv(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den);
-        L.u3[c] = divv(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den);
+        const T rden = recip(den);
+        L.u1[c] = divr(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den, rden);
+        L.u2[c] = divr(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den, rden);
+        L.u3[c] = divr(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den, rden);
     } else {
-        const T g2 = (T)0.5 * dt * kk.rdvc / (kk.ro0 + L.ro[c]);
+        const T g2 = (T)0.5 * dt * kk.rdvc * recip(kk.ro0 + L.ro[c]);
         L.u1[c] += g2 * S.f[0][c];
         L.u2[c] += g2 * S.f[1][c];
         L.u3[c] += g2 * S.f[2][c];
@@ -873,18 +987,18 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
 }
 
 template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d) {
+    const KT<T> &k = kconst<T>(S.k);
     SweepK<T> q;
-    const double dt = S.sc->dt;
-    q.sound = (T)S.k.sound;
-    q.ro0 = (T)S.k.ro0;
-    q.c2 = (T)S.k.c2;
-    q.rc2 = (T)S.k.rc2;
-    q.roc = (T)S.k.roc;
-    q.rroc = (T)S.k.rroc;
-    q.dt = (T)dt;
-    q.rdt = (T)(1.0 / dt);
-    q.dx = (T)S.k.dx[d];
-    q.rdx = (T)S.k.rdx[d];
+    q.sound = k.sound;
+    q.ro0 = k.ro0;
+    q.c2 = k.c2;
+    q.rc2 = k.rc2;
+    q.roc = k.roc;
+    q.rroc = k.rroc;
+    q.dt = sc_dt<T>(S.sc);
+    q.rdt = sc_rdt<T>(S.sc);
+    q.dx = k.dx[d];
+    q.rdx = k.rdx[d];
     return q;
 }
 
@@ -1103,6 +1217,42 @@ template <class T> __global__ void __launch_bounds__(kTileX *kTileY) k_sums(DevS
     }
 }
 
+// Mean of u1 over the fluid cells of each y plane (one block per plane), summed in exact
+// 2^-32 fixed point: acc[2*(j-1)] = sum, acc[2*(j-1)+1] = cells.  The plane mean profile
+// U(y) and, from its first and last entries, the wall shear 2*VIS*U/dx2 in the one-sided
+// wall form of StressTensor (main.cpp:924-927).
+template <class T> __global__ void __launch_bounds__(256) k_mean_profile(DevState<T> S, int ncon, long long *acc) {
+    __shared__ long long red[2][8];
+    const Geom g = S.g;
+    const int j = blockIdx.x + 1;
+    const T *__restrict__ u1 = S.lv[ncon].u1;
+    long long s = 0, n = 0;
+    const int plane = g.C1 * g.C3;
+    for (int t = threadIdx.x; t < plane; t += blockDim.x) {
+        const int i = t % g.C1 + 1, k = t / g.C1 + 1;
+        const int64_t c = g.cell(i, j, k);
+        if (!(S.flags[c] & FL_EQ0)) continue;
+        s += fixed32((double)u1[c]);
+        n += 1;
+    }
+    s = warp_sum_i64(s);
+    n = warp_sum_i64(n);
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = s;
+        red[1][threadIdx.x >> 5] = n;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long a = 0, b = 0;
+        for (int w = 0; w < 8; ++w) {
+            a += red[0][w];
+            b += red[1][w];
+        }
+        acc[2 * (j - 1)] = a;
+        acc[2 * (j - 1) + 1] = b;
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------
@@ -1125,7 +1275,7 @@ template <class T> void Launch<T>::reduce_start(const DevState<T> &S, int con, c
 }
 
 template <class T> void Launch<T>::finalize_dt(const DevState<T> &S, int advance_time, cudaStream_t st) {
-    k_finalize_dt<T><<<1, 1024, 0, st>>>(S, advance_time, tile_count(S.g));
+    k_finalize_dt<T><<<1, 1024, 0, st>>>(S, advance_time);
 }
 
 template <class T> void Launch<T>::wrap_cells(const DevState<T> &S, T *const *arrs, int n, cudaStream_t st) {
@@ -1172,20 +1322,39 @@ template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, in
     k_wrap<T><<<grid_for(tot, 256, 1 << 30), 256, 0, st>>>(S.g, J);
 }
 
-template <class T>
-void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, cudaStream_t st) {
-    const dim3 grid = tile_grid(S.g), block(kTileX, kTileY);
+template <class T, template <class, int> class KERNEL>
+void launch_phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, dim3 grid, cudaStream_t st) {
+    const dim3 block(kTileX, kTileY);
     switch (mode) {
-    case P1_PLAIN: k_phase1<T, P1_PLAIN><<<grid, block, 0, st>>>(S, src, dst, fcur); break;
+    case P1_PLAIN: KERNEL<T, P1_PLAIN>::launch(grid, block, st, S, src, dst, fcur); break;
     case P1_STRESS | P1_FORCES | P1_RMAX:
-        k_phase1<T, P1_STRESS | P1_FORCES | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur);
+        KERNEL<T, P1_STRESS | P1_FORCES | P1_RMAX>::launch(grid, block, st, S, src, dst, fcur);
         break;
     case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
-        k_phase1<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur);
+        KERNEL<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>::launch(grid, block, st, S, src, dst, fcur);
         break;
-    case P1_FORCES | P1_RSUM: k_phase1<T, P1_FORCES | P1_RSUM><<<grid, block, 0, st>>>(S, src, dst, fcur); break;
+    case P1_FORCES | P1_RSUM: KERNEL<T, P1_FORCES | P1_RSUM>::launch(grid, block, st, S, src, dst, fcur); break;
     default: break;
     }
+}
+template <class T, int MODE> struct MarchK {
+    static void launch(dim3 g, dim3 b, cudaStream_t st, const DevState<T> &S, int src, int dst, int fcur) {
+        k_phase1<T, MODE><<<g, b, 0, st>>>(S, src, dst, fcur);
+    }
+};
+template <class T, int MODE> struct CellK {
+    static void launch(dim3 g, dim3 b, cudaStream_t st, const DevState<T> &S, int src, int dst, int fcur) {
+        k_phase1_cell<T, MODE><<<g, b, 0, st>>>(S, src, dst, fcur);
+    }
+};
+
+// march = 1: k_phase1 (a block marches kTileK planes); 0: k_phase1_cell (one plane per block)
+template <class T>
+void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st) {
+    if (march)
+        launch_phase1<T, MarchK>(S, src, dst, fcur, mode, tile_grid(S.g), st);
+    else
+        launch_phase1<T, CellK>(S, src, dst, fcur, mode, dim3(tiles_x(S.g), tiles_y(S.g), S.g.C3), st);
 }
 
 template <class T> void Launch<T>::stress(const DevState<T> &S, int con, int bulk, cudaStream_t st) {
@@ -1231,6 +1400,10 @@ void Launch<T>::boundary_fill(const DevState<T> &S, int ncon, int axis, int peri
     const int64_t n = axis == 1 ? (int64_t)S.g.C2 * S.g.C3 : axis == 2 ? (int64_t)S.g.C1 * S.g.C3
                                                                        : (int64_t)S.g.C1 * S.g.C2;
     k_boundary_fill<T><<<grid_for(n, 256, 1 << 30), 256, 0, st>>>(S.g, S.lv[ncon], axis, periodic);
+}
+
+template <class T> void Launch<T>::mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st) {
+    k_mean_profile<T><<<S.g.C2, 256, 0, st>>>(S, ncon, acc);
 }
 
 template <class T> void Launch<T>::sums(const DevState<T> &S, int ncon, cudaStream_t st) {

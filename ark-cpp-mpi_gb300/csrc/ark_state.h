@@ -43,6 +43,11 @@ __host__ __device__ inline int tiles_y(const Geom &g) { return (g.C2 + kTileY - 
 __host__ __device__ inline int tiles_k(const Geom &g) { return (g.C3 + kTileK - 1) / kTileK; }
 __host__ __device__ inline int tile_count(const Geom &g) { return tiles_x(g) * tiles_y(g) * tiles_k(g); }
 
+// Blocks fold their partials into kBuckets slots with atomics (block b -> slot b % kBuckets);
+// k_finalize_dt reads the slots and clears them.  Max and integer sums are order
+// independent, so the result does not depend on the launch configuration.
+constexpr int kBuckets = 256;
+
 // Sticky device status bits.
 enum : int { STATUS_NONFINITE = 1 };
 
@@ -58,7 +63,16 @@ template <class T> struct Level { T *ro, *u1, *u2, *u3; };
 // Faces normal to one axis: pressure, density, velocity components u[0..2].
 template <class T> struct FaceSet { T *p, *ro, *u[3]; };
 
-// Constants of a run, computed once on the host in double (the FP32 path rounds them).
+// Constants of a run rounded to one precision, computed on the host (kernels never convert
+// or divide to get them: FP64 instructions run at 1/64 of the FP32 rate on this part).
+template <class T> struct KT {
+    T dx[3], rdx[3];  // grid steps and their reciprocals
+    T vrdx[3];        // VIS / dx_d (FP32 stress coefficients)
+    T ds[3], dvc, rdvc;
+    T vis, two_vis, sound, ro0, c2, rc2, roc, rroc;
+};
+
+// Constants of a run, computed once on the host in double, plus their per-precision copies.
 struct Consts {
     double dx[3], rdx[3];  // grid steps and their correctly rounded reciprocals
     double ds[3], dvc;     // face areas dx2*dx3, dx1*dx3, dx1*dx2 and cell volume dx1*dx2*dx3
@@ -70,7 +84,13 @@ struct Consts {
     double dtv;            // viscous dt limit of TimeStepSize (cell independent)
     double u_target;
     int forcing;
+    KT<double> kd;
+    KT<float> kf;
 };
+
+template <class T> __host__ __device__ inline const KT<T> &kconst(const Consts &k);
+template <> __host__ __device__ inline const KT<double> &kconst<double>(const Consts &k) { return k.kd; }
+template <> __host__ __device__ inline const KT<float> &kconst<float>(const Consts &k) { return k.kf; }
 
 // Scalars and reduction accumulators living on the device, so a whole step (and a
 // CUDA graph of it) never waits for the host.
@@ -82,7 +102,19 @@ struct DevScalars {
     int pad;
     long long sums[5]; // conservation sums (fixed point), see ark_sums
     long long sum_cells;
+    double rdt;        // 1/dt
+    float dtf, rdtf, Gf, padf; // dt, 1/dt and G rounded to FP32 for the FP32 kernels
 };
+
+template <class T> __device__ __forceinline__ T sc_dt(const DevScalars *s);
+template <> __device__ __forceinline__ double sc_dt<double>(const DevScalars *s) { return s->dt; }
+template <> __device__ __forceinline__ float sc_dt<float>(const DevScalars *s) { return s->dtf; }
+template <class T> __device__ __forceinline__ T sc_rdt(const DevScalars *s);
+template <> __device__ __forceinline__ double sc_rdt<double>(const DevScalars *s) { return s->rdt; }
+template <> __device__ __forceinline__ float sc_rdt<float>(const DevScalars *s) { return s->rdtf; }
+template <class T> __device__ __forceinline__ T sc_G(const DevScalars *s);
+template <> __device__ __forceinline__ double sc_G<double>(const DevScalars *s) { return s->G; }
+template <> __device__ __forceinline__ float sc_G<float>(const DevScalars *s) { return s->Gf; }
 
 template <class T> struct DevState {
     Geom g;
@@ -93,8 +125,8 @@ template <class T> struct DevState {
     T *sig[3][3];        // sig[d][m]: component m on faces normal to d (nullptr unless kept)
     uint8_t *flags;
     DevScalars *sc;
-    // per-tile partials: max |u_d| of the "Con" level as IEEE double bit patterns (3 per
-    // tile) and the fixed-point sum of u1 over fluid cells of the "nCon" level (1 per tile)
+    // partial-slot buckets: max |u_d| of the "Con" level as IEEE double bit patterns (3 per
+    // slot) and the fixed-point sum of u1 over fluid cells of the "nCon" level (1 per slot)
     unsigned long long *part_max;
     long long *part_sum;
 };
@@ -115,13 +147,17 @@ template <class T> struct Launch {
     static void finalize_dt(const DevState<T> &S, int advance_time, cudaStream_t st);
     static void wrap_cells(const DevState<T> &S, T *const *arrs, int n, cudaStream_t st);
     static void wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st);
-    static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, cudaStream_t st);
+    static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st);
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
     static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st);
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
+    static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);
 };
+
+// div_rn against the hardware division on n random operand pairs (mismatches added to *bad)
+void selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st);
 
 // double <-> T copies for FP32 contexts (host arrays are always double):
 // dst = (T)(src - offset) and dst = (double)src + offset.

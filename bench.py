@@ -38,7 +38,6 @@ UNIT = "Mcell-steps/s"
 # input element read once, every output element written once (faces counted once per cell:
 # each face is shared by two cells).  Flags are 1 byte per cell.
 ALGO_VALUES = {
-    "reduce_start": (4, 1),          # Con u1..u3, nCon u1; flags
     "finalize_dt": (0, 0),
     "wrap_con": (0, 0),
     "phase1_stress_forces": (26, 1),  # Con 4 + faces 15 -> nCon 4 + f 3
@@ -48,6 +47,10 @@ ALGO_VALUES = {
     "sweep_x3": (17, 1),
     "phase1_forces": (26, 1),         # Con 4 + faces 15 + f 3 -> nCon 4
 }
+# FP32 stores no face density (it is ro0 + p/c^2): three values fewer per Phase1 and one
+# fewer per sweep.
+ALGO_VALUES_FP32 = dict(ALGO_VALUES, phase1_stress_forces=(23, 1), phase1_forces=(23, 1), sweep_x1=(16, 1),
+                        sweep_x2=(16, 1), sweep_x3=(16, 1))
 # Persistent state per cell: cell rho,u1,u2,u3 + 3 face sets x {p,u1,u2,u3}; read and
 # written once per step (the step's algorithmic bytes).
 STEP_VALUES = 2 * 16
@@ -187,7 +190,7 @@ def gpu_leg(arkgpu, C, re_b, precision, steps, warmup, device, seed, kernel_step
 
 def roofline(kt, cells, word, peak, peak_kind, traffic_tab, prec_name):
     name, ms = max(kt, key=lambda x: x[1])
-    vals, flag_b = ALGO_VALUES.get(name, (0, 0))
+    vals, flag_b = (ALGO_VALUES_FP32 if word == 4 else ALGO_VALUES).get(name, (0, 0))
     algo = cells * (vals * word + flag_b)
     achieved = algo / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
     tpc = traffic_tab.get((prec_name, name))
@@ -198,8 +201,10 @@ def roofline(kt, cells, word, peak, peak_kind, traffic_tab, prec_name):
 
 
 def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
-    """Through the C ABI with host buffers: every step uploads the full state from pinned
-    memory, runs one step and downloads the full state."""
+    """Through the C ABI with host buffers, as a program replacing the reference's main loop
+    uses it: upload the whole state from pinned host memory, then every step run ark_step and
+    read the step's scalars back (dt, TIME, bulk velocity: a synchronous device->host read),
+    then download the whole state.  All of it is inside the timed region."""
     p = channel_params(arkgpu, C, re_b, precision)
     p.device = device
     st = arkgpu.channel_init(p, seed=seed, amp=0.1)
@@ -208,25 +213,40 @@ def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
     del st
     cells = C[0] * C[1] * C[2]
     with arkgpu.Context(p) as ctx:
-        ctx.upload_struct(hs.struct(True))
-        ctx.step(1)
-        ctx.sync()
-        h_up = hs.struct(False)
-        h_dn = hs.struct(False)
-        ctx.upload_struct(h_up)
-        ctx.step(1)
-        ctx.download_struct(h_dn)
+        ctx.upload_struct(hs.struct(True))  # warm-up: graphs, first transfers
+        ctx.step(2)
+        ctx.scalars()
+        ctx.download_struct(hs.struct(False))
         t0 = time.perf_counter()
+        ctx.upload_struct(hs.struct(True))
         for _ in range(steps):
-            ctx.upload_struct(h_up)
             ctx.step(1)
-            ctx.download_struct(h_dn)
+            ctx.scalars()
+        ctx.download_struct(hs.struct(False))
         secs = time.perf_counter() - t0
         ctx.sync()
-    nbytes = hs.nbytes(False)
+        # per-step full-state round trip (the state kept on the host between steps)
+        h = hs.struct(False)
+        ctx.upload_struct(h)
+        ctx.step(1)
+        ctx.download_struct(h)
+        n_rt = max(3, steps // 10)
+        t1 = time.perf_counter()
+        for _ in range(n_rt):
+            ctx.upload_struct(h)
+            ctx.step(1)
+            ctx.download_struct(h)
+        rt_secs = time.perf_counter() - t1
+    up = hs.nbytes(True)
+    down = hs.nbytes(False)
+    scal = 5 * 8  # the ark_scalars read every step
     hs.close()
-    return {"value": round(cells * steps / secs / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
-            "d2h_bytes_per_step": nbytes, "steps": steps}
+    return {"value": round(cells * steps / secs / 1e6, 3), "unit": UNIT,
+            "h2d_bytes_per_step": round(up / steps), "d2h_bytes_per_step": round(down / steps) + scal,
+            "steps": steps,
+            "note": "one job: state upload, steps each with a synchronous scalar read-back, state download",
+            "state_roundtrip_every_step": {"value": round(cells * n_rt / rt_secs / 1e6, 3), "unit": UNIT,
+                                           "h2d_bytes_per_step": down, "d2h_bytes_per_step": down, "steps": n_rt}}
 
 
 def cpu_leg(C, re_b, budget_s=12.0, max_steps=400, threads=None):
@@ -293,7 +313,7 @@ def main():
     ap.add_argument("--fp32-grid", type=int, nargs=3, default=(512, 256, 256))
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=30)
+    ap.add_argument("--e2e-steps", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

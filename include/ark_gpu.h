@@ -179,6 +179,18 @@ int ark_get_scalars(ark_ctx *ctx, ark_scalars *out);
 int ark_set_scalars(ark_ctx *ctx, const ark_scalars *in);
 int ark_conservation_sums(ark_ctx *ctx, ark_sums *out);
 
+/* Mean u1 over the fluid cells of each y plane of the "nCon" level (mean_u1[j-1], j = 1..C2,
+ * summed in exact fixed point) and, when wall_shear is not NULL, the wall shear stress at
+ * y = -ly/2 and y = +ly/2 in StressTensor's one-sided wall form 2*VIS*u_c/dx2
+ * (main.cpp:924-927).  Synchronous. */
+int ark_mean_profile(ark_ctx *ctx, double *mean_u1, double *wall_shear);
+
+/* Self-check of the correctly rounded division by a run constant that the FP64 kernels use
+ * (q = a*RN(1/b) plus two Markstein corrections) against the GPU's IEEE division, on n
+ * random operand pairs and on small exact cases; *mismatches receives the count (0 expected).
+ * Runs on the current device. */
+int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches);
+
 /* ---- host-side helpers (no GPU needed) ----------------------------------------------------- */
 
 /* Seeded channel-flow initial state (a project definition, not part of the reference):

@@ -39,7 +39,7 @@ def test_counts(ark):
 
 
 @pytest.mark.parametrize("field,value,status", [
-    ("n1_cells", 0, 1), ("n3_cells", 1, 1), ("sound", 0.0, 1), ("cfl", -1.0, 1), ("vis", -1.0, 1),
+    ("n1_cells", 0, 1), ("n3_cells", 0, 1), ("n2_cells", -3, 1), ("sound", 0.0, 1), ("cfl", -1.0, 1), ("vis", -1.0, 1),
     ("ly", 0.0, 1), ("precision", 7, 1), ("periodic_x", 0, 6), ("periodic_z", 0, 6)])
 def test_create_rejects_bad_params(ark, field, value, status):
     p = ark.make_params(8, 6, 4)

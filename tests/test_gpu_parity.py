@@ -254,3 +254,47 @@ def test_fp32_per_phase_equals_fused(ark, port):
             outs.append(c.download(CELLS + FACES))
     for n in CELLS + FACES:
         assert bits_equal(port.interior(n, outs[0][n]), port.interior(n, outs[1][n])), n
+
+
+def test_phase1_kernel_shapes_agree(ark, port, monkeypatch):
+    """The marching and the one-cell-per-thread Phase1 kernels (ARK_PHASE1_MARCH) produce the
+    same bits in both precisions."""
+    p = port.channel_params(40, 20, 36, seed=21)
+    st0 = port.channel_state(p)
+    for prec in (ark.FP64, ark.FP32):
+        outs = []
+        for m in ("00", "11", "10"):
+            monkeypatch.setenv("ARK_PHASE1_MARCH", m)
+            with ark.Context(params_from(ark, p, precision=prec)) as c:
+                c.upload(st0)
+                c.step(4)
+                c.sync()
+                outs.append(c.download(CELLS + FACES))
+        for o in outs[1:]:
+            for n in CELLS + FACES:
+                assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), (prec, n)
+
+
+def test_mean_profile_and_wall_shear(ark, port):
+    """ark_mean_profile against numpy on the downloaded field; wall shear in the one-sided
+    wall form 2*VIS*U/dy."""
+    p = port.channel_params(32, 16, 12, seed=6)
+    with ark.Context(params_from(ark, p)) as ctx:
+        ctx.upload(port.channel_state(p))
+        ctx.step(5)
+        prof, ws = ctx.mean_profile()
+        u = port.interior("u1nCon", ctx.download(["u1nCon"])["u1nCon"])
+    want = u.mean(axis=(0, 2))
+    np.testing.assert_allclose(prof, want, rtol=0, atol=1e-9)
+    dy = p["ly"] / p["C2"]
+    np.testing.assert_allclose(ws, [2 * p["nu"] * prof[0] / dy, 2 * p["nu"] * prof[-1] / dy], rtol=1e-14)
+
+
+def test_constant_division_is_correctly_rounded(ark):
+    """The FP64 kernels divide by run constants as a*RN(1/b) with two Markstein corrections;
+    on 2^26 random operand pairs it agrees with the GPU's IEEE division bit for bit."""
+    import ctypes
+
+    bad = ctypes.c_longlong(-1)
+    assert ark.lib().ark_selftest_division(1 << 26, 2024, ctypes.byref(bad)) == 0
+    assert bad.value == 0
