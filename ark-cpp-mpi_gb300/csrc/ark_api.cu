@@ -118,6 +118,8 @@ Consts make_consts(const ark_params &p) {
     }
     k.u_target = p.u_target;
     k.forcing = p.forcing;
+    k.periodic_x = p.periodic_x != 0;
+    k.periodic_z = p.periodic_z != 0;
     fill_kt(k, k.kd);
     fill_kt(k, k.kf);
     return k;
@@ -332,8 +334,7 @@ template <class T> struct EngineT : Engine {
         Launch<T>::phase1(S, src, dst, fcur, mode, ctx->march[0], ctx->st);
     }
     void stress(int con, int bulk) override {
-        T *u[3] = {S.lv[con].u1, S.lv[con].u2, S.lv[con].u3};
-        Launch<T>::wrap_cells(S, u, 3, ctx->st);
+        Launch<T>::wrap_con(S, con, 0, ctx->st);
         if (S.sig[0][0]) {
             for (int d = 0; d < 3; ++d)
                 for (int m = 0; m < 3; ++m)
@@ -357,8 +358,7 @@ template <class T> struct EngineT : Engine {
         };
         Launch<T>::finalize_dt(S, 1, st);
         mark(0);
-        T *cells[4] = {S.lv[y].u1, S.lv[y].u2, S.lv[y].u3, S.lv[y].ro};
-        Launch<T>::wrap_cells(S, cells, 4, st);
+        Launch<T>::wrap_con(S, y, 1, st);
         mark(1);
         Launch<T>::phase1(S, y, x, fcur, P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0),
                           ctx->march[0], st);
@@ -390,8 +390,6 @@ int check_params(const ark_params *p) {
     if (!(p->sound > 0) || !(p->ro0 > 0) || !(p->cfl > 0) || !(p->vis >= 0))
         return fail(ARK_ERR_PARAM, "sound, ro0, cfl must be > 0 and vis >= 0");
     if (p->precision != ARK_FP64 && p->precision != ARK_FP32) return fail(ARK_ERR_PARAM, "unknown precision");
-    if (!p->periodic_x || !p->periodic_z)
-        return fail(ARK_ERR_UNSUPPORTED, "bounded x or z (inflow/outflow, zero-gradient edges) is not implemented");
     return ARK_OK;
 }
 

@@ -284,43 +284,51 @@ template <class T> __global__ void __launch_bounds__(1024) k_finalize_dt(DevStat
 // ghost fill (periodic x and z)
 // ---------------------------------------------------------------------------------------
 
+enum : uint8_t { GH_NONE = 0, GH_WRAP = 1, GH_COPY = 2 };
+
 struct WrapJob {
     void *a[16];
     uint8_t face[16];
-    uint8_t axis_mask[16]; // bit 0: wrap in x, bit 1: wrap in z
+    uint8_t mode[16][2]; // per array, for x and for z: GH_NONE, GH_WRAP or GH_COPY
     int n;
 };
 
-// The halo exchange of one rank with itself: ghost 0 <- cell C, ghost C+1 <- cell 1
-// (faces: halo 0 <- face C, halo C+2 <- face 2), over the interior of the other axes.
+// The halo exchange of one rank with itself, per axis and array:
+//   GH_WRAP (periodic axis): ghost 0 <- cell C, ghost C+1 <- cell 1; faces: halo 0 <- face C,
+//           halo C+2 <- face 2 (main.cpp:603-801, 1049-1631 with self-neighbours);
+//   GH_COPY (bounded axis): zero-gradient ghost 0 <- cell 1, ghost C+1 <- cell C; faces:
+//           halo 0 <- face 1, halo C+2 <- face C+1 (main.cpp:803-845, 1633-1698);
+// over the interior of the other two axes.
 template <class T> __global__ void k_wrap(Geom g, WrapJob J) {
     const int64_t nx = (int64_t)g.C2 * g.C3, nz = (int64_t)g.C1 * g.C2;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < nx) {
         const int j = (int)(t % g.C2) + 1, k = (int)(t / g.C2) + 1;
         for (int q = 0; q < J.n; ++q) {
-            if (!(J.axis_mask[q] & 1)) continue;
+            const uint8_t m = J.mode[q][0];
+            if (m == GH_NONE) continue;
             T *a = (T *)J.a[q];
             if (J.face[q]) {
-                a[g.face(0, j, k)] = a[g.face(g.C1, j, k)];
-                a[g.face(g.C1 + 2, j, k)] = a[g.face(2, j, k)];
+                a[g.face(0, j, k)] = a[g.face(m == GH_WRAP ? g.C1 : 1, j, k)];
+                a[g.face(g.C1 + 2, j, k)] = a[g.face(m == GH_WRAP ? 2 : g.C1 + 1, j, k)];
             } else {
-                a[g.cell(0, j, k)] = a[g.cell(g.C1, j, k)];
-                a[g.cell(g.C1 + 1, j, k)] = a[g.cell(1, j, k)];
+                a[g.cell(0, j, k)] = a[g.cell(m == GH_WRAP ? g.C1 : 1, j, k)];
+                a[g.cell(g.C1 + 1, j, k)] = a[g.cell(m == GH_WRAP ? 1 : g.C1, j, k)];
             }
         }
     } else if (t < nx + nz) {
         const int64_t u = t - nx;
         const int i = (int)(u % g.C1) + 1, j = (int)(u / g.C1) + 1;
         for (int q = 0; q < J.n; ++q) {
-            if (!(J.axis_mask[q] & 2)) continue;
+            const uint8_t m = J.mode[q][1];
+            if (m == GH_NONE) continue;
             T *a = (T *)J.a[q];
             if (J.face[q]) {
-                a[g.face(i, j, 0)] = a[g.face(i, j, g.C3)];
-                a[g.face(i, j, g.C3 + 2)] = a[g.face(i, j, 2)];
+                a[g.face(i, j, 0)] = a[g.face(i, j, m == GH_WRAP ? g.C3 : 1)];
+                a[g.face(i, j, g.C3 + 2)] = a[g.face(i, j, m == GH_WRAP ? 2 : g.C3 + 1)];
             } else {
-                a[g.cell(i, j, 0)] = a[g.cell(i, j, g.C3)];
-                a[g.cell(i, j, g.C3 + 1)] = a[g.cell(i, j, 1)];
+                a[g.cell(i, j, 0)] = a[g.cell(i, j, m == GH_WRAP ? g.C3 : 1)];
+                a[g.cell(i, j, g.C3 + 1)] = a[g.cell(i, j, m == GH_WRAP ? 1 : g.C3)];
             }
         }
     }
@@ -1078,6 +1086,7 @@ template <class T> __global__ void __launch_bounds__(128) k_sweep_x(DevState<T> 
     const SweepK<T> q = sweep_consts(S, 0);
     const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k);
     const int nd = g.C1 + 1;
+    const bool bounded = !S.k.periodic_x;
     Ext<T> carry = {};
     T carry_u = 0;
     uint8_t carry_fl = 0;
@@ -1105,6 +1114,21 @@ template <class T> __global__ void __launch_bounds__(128) k_sweep_x(DevState<T> 
         if (act)
             e = extrapolate<T, true>(cur.uN_f, uN_b, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA, cur.uB_f, uB_b,
                                      cur.nB, cur.cB, cur.nR, cur.cR, cur.p_f, p_b, q);
+        if (bounded) {
+            // a bounded x axis sweeps cells 1..C1 only; the edge faces take the reference's
+            // inflow invariant R = 1 (0 behind a solid first cell) and outflow Q = 5/6 with
+            // zero tangential velocity (main.cpp:1731-1745)
+            if (s == 0) {
+                e.rf = (R.fl[c0 + 1] & FL_LT) ? (T)1 : (T)0;
+                e.af = (T)0;
+                e.bf = (T)0;
+            }
+            if (s == nd) {
+                e.qb = (T)(5. / 6.);
+                e.ab = (T)0;
+                e.bb = (T)0;
+            }
+        }
         Ext<T> prev;
         prev.rf = __shfl_up_sync(0xffffffffu, e.rf, 1);
         prev.af = __shfl_up_sync(0xffffffffu, e.af, 1);
@@ -1278,48 +1302,55 @@ template <class T> void Launch<T>::finalize_dt(const DevState<T> &S, int advance
     k_finalize_dt<T><<<1, 1024, 0, st>>>(S, advance_time);
 }
 
-template <class T> void Launch<T>::wrap_cells(const DevState<T> &S, T *const *arrs, int n, cudaStream_t st) {
-    WrapJob J = {};
-    J.n = n;
-    for (int q = 0; q < n; ++q) {
-        J.a[q] = arrs[q];
-        J.face[q] = 0;
-        J.axis_mask[q] = 3;
-    }
+inline void wrap_add(WrapJob &J, void *a, int face, uint8_t mx, uint8_t mz) {
+    if (!a || (mx == GH_NONE && mz == GH_NONE)) return;
+    J.a[J.n] = a;
+    J.face[J.n] = (uint8_t)face;
+    J.mode[J.n][0] = mx;
+    J.mode[J.n][1] = mz;
+    ++J.n;
+}
+
+template <class T> inline void wrap_launch(const DevState<T> &S, const WrapJob &J, cudaStream_t st) {
+    if (J.n == 0) return;
     const int64_t tot = (int64_t)S.g.C2 * S.g.C3 + (int64_t)S.g.C1 * S.g.C2;
     k_wrap<T><<<grid_for(tot, 256, 1 << 30), 256, 0, st>>>(S.g, J);
 }
 
-// The halo exchange before Phase2 (main.cpp:1049-1631): cells u?nCon, ronCon and roCon in x
-// and z; faces normal to x1 wrapped in x, faces normal to x3 wrapped in z.
+// StressTensor's exchange of u1Con, u2Con, u3Con (main.cpp:603-845): periodic axes wrap,
+// bounded x and z take the zero-gradient copy.  with_ro also fills roCon's ghosts as Phase2's
+// exchange does (main.cpp:1049-1698: wrapped on periodic axes, copied on a bounded z, left
+// alone on a bounded x), for the fused step, which reads that level before Phase2.
+template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st) {
+    const uint8_t ux = S.k.periodic_x ? GH_WRAP : GH_COPY, uz = S.k.periodic_z ? GH_WRAP : GH_COPY;
+    WrapJob J = {};
+    const Level<T> L = S.lv[con];
+    wrap_add(J, L.u1, 0, ux, uz);
+    wrap_add(J, L.u2, 0, ux, uz);
+    wrap_add(J, L.u3, 0, ux, uz);
+    if (with_ro) wrap_add(J, L.ro, 0, S.k.periodic_x ? GH_WRAP : GH_NONE, uz);
+    wrap_launch(S, J, st);
+}
+
+// The halo exchange before Phase2 (main.cpp:1049-1698): u?nCon and ronCon wrap or copy on
+// both axes; roCon wraps, or is copied on a bounded z only; faces normal to x1 wrap in x (a
+// bounded x sweep never reads their halo); faces normal to x3 wrap or copy in z.
 template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st) {
+    const bool px = S.k.periodic_x, pz = S.k.periodic_z;
+    const uint8_t cx = px ? GH_WRAP : GH_COPY, cz = pz ? GH_WRAP : GH_COPY;
     WrapJob J = {};
     const Level<T> Ln = S.lv[con ^ 1], Lc = S.lv[con];
-    T *cells[5] = {Ln.u1, Ln.u2, Ln.u3, Ln.ro, Lc.ro};
-    int n = 0;
-    for (int q = 0; q < 5; ++q) {
-        J.a[n] = cells[q];
-        J.face[n] = 0;
-        J.axis_mask[n++] = 3;
-    }
+    wrap_add(J, Ln.u1, 0, cx, cz);
+    wrap_add(J, Ln.u2, 0, cx, cz);
+    wrap_add(J, Ln.u3, 0, cx, cz);
+    wrap_add(J, Ln.ro, 0, cx, cz);
+    wrap_add(J, Lc.ro, 0, px ? GH_WRAP : GH_NONE, cz);
     const FaceSet<T> &X = S.fc[fcur][0], &Z = S.fc[fcur][2];
     T *fx[5] = {X.p, X.u[0], X.u[1], X.u[2], X.ro};
     T *fz[5] = {Z.p, Z.u[0], Z.u[1], Z.u[2], Z.ro};
-    for (int q = 0; q < 5; ++q) {
-        if (!fx[q]) continue;
-        J.a[n] = fx[q];
-        J.face[n] = 1;
-        J.axis_mask[n++] = 1;
-    }
-    for (int q = 0; q < 5; ++q) {
-        if (!fz[q]) continue;
-        J.a[n] = fz[q];
-        J.face[n] = 1;
-        J.axis_mask[n++] = 2;
-    }
-    J.n = n;
-    const int64_t tot = (int64_t)S.g.C2 * S.g.C3 + (int64_t)S.g.C1 * S.g.C2;
-    k_wrap<T><<<grid_for(tot, 256, 1 << 30), 256, 0, st>>>(S.g, J);
+    for (int q = 0; q < 5; ++q) wrap_add(J, fx[q], 1, px ? GH_WRAP : GH_NONE, GH_NONE);
+    for (int q = 0; q < 5; ++q) wrap_add(J, fz[q], 1, GH_NONE, cz);
+    wrap_launch(S, J, st);
 }
 
 template <class T, template <class, int> class KERNEL>

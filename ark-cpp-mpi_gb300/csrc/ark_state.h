@@ -84,6 +84,7 @@ struct Consts {
     double dtv;            // viscous dt limit of TimeStepSize (cell independent)
     double u_target;
     int forcing;
+    int periodic_x, periodic_z; // 0: the reference's bounded edges (see k_wrap, k_sweep_x)
     KT<double> kd;
     KT<float> kf;
 };
@@ -145,7 +146,7 @@ enum Phase1Mode { P1_PLAIN = 0, P1_STRESS = 1, P1_FORCES = 2, P1_BULK = 4, P1_RM
 template <class T> struct Launch {
     static void reduce_start(const DevState<T> &S, int con, cudaStream_t st);
     static void finalize_dt(const DevState<T> &S, int advance_time, cudaStream_t st);
-    static void wrap_cells(const DevState<T> &S, T *const *arrs, int n, cudaStream_t st);
+    static void wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st);
     static void wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st);
     static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st);
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);

@@ -52,8 +52,9 @@ typedef struct ark_params {
     double sound;                     /* sound speed                                            */
     double ro0;                       /* ro0_g, unperturbed density                             */
     double cfl;                       /* CFL number                                             */
-    int periodic_x;                   /* 1: periodic x.  0 (bounded, inflow/outflow): rejected  */
-    int periodic_z;                   /* 1: periodic z.  0 (bounded, zero-gradient): rejected   */
+    int periodic_x;                   /* 1: periodic x.  0: bounded, zero-gradient ghosts and the
+                                         inflow R = 1 / outflow Q = 5/6 invariants (main.cpp:1731-1745) */
+    int periodic_z;                   /* 1: periodic z.  0: bounded, zero-gradient ghosts        */
     int precision;                    /* enum ark_precision                                     */
     int forcing;                      /* 1: constant-flow-rate bulk forcing                     */
     double u_target;                  /* bulk velocity the forcing holds                        */

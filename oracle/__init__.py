@@ -304,6 +304,25 @@ class Reference:
         for nm in ("t1", "t2", "t3"):
             self.put(nm, np.full(self.fshape, temp0))
 
+    @classmethod
+    def stock(cls):
+        """The reference's own stock case, set up by its Input() and InitializeData()
+        (200x60x1 backward-facing step, bounded in every direction, no forcing).  Returns the
+        Reference and the matching parameter dict."""
+        L = cls.lib()
+        L.ref_teardown()
+        assert L.ref_stock_setup() == 0
+        cells = (ctypes.c_int * 3)()
+        vals = (ctypes.c_double * 10)()
+        L.ref_stock_params(cells, vals)
+        p = dict(C1=cells[0], C2=cells[1], C3=cells[2], nu=vals[3], sound=vals[4], rho0=vals[5], cfl=vals[6],
+                 lx=vals[7], ly=vals[8], lz=vals[9], ub=1.0, amp=0.0, seed=0)
+        self = cls.__new__(cls)
+        self.p = p
+        self.cshape = (p["C3"] + 2, p["C2"] + 2, p["C1"] + 2)
+        self.fshape = (p["C3"] + 3, p["C2"] + 3, p["C1"] + 3)
+        return self, p
+
     def put(self, name, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
         n = self.lib().ref_array_len(name.encode())

@@ -53,7 +53,9 @@ extern int left, right, up, down, top, bottom, nproc, rank, px, py, pz, coordX, 
 extern int coords[3], dims[3];
 extern MPI_Comm newComm;
 
-/* ---- the reference's solver functions (main.cpp:14-21) ---- */
+/* ---- the reference's solver functions (main.cpp:12-21) ---- */
+void Input();
+void InitializeData();
 void TimeStepSize();
 void Phase1();
 void Phase2();
@@ -207,6 +209,41 @@ int ref_teardown() {
     delete[] rBuf; delete[] qBuf; delete[] tfBuf; delete[] tbBuf;
     delete[] u2fBuf; delete[] u2bBuf; delete[] u3fBuf; delete[] u3bBuf;
     g_ready = false;
+    return 0;
+}
+
+/* The reference's own stock case: Input() (main.cpp:118-278: 200x60x1 cells, backward-facing
+ * step, VIS 1e-3, c 10, CFL 0.2) and InitializeData() (main.cpp:280-372), on one rank with
+ * every neighbour MPI_PROC_NULL and coords 0 (bounded x, y and z).  The arrays Input()
+ * allocates are zero-filled before InitializeData() (the reference leaves them
+ * uninitialised), and the "Con" level starts equal to "nCon" (TimeStepSize reads it before
+ * any Phase1 has written it). */
+int ref_stock_setup() {
+    if (g_ready) return 1;
+    dims[0] = dims[1] = dims[2] = 1;
+    coords[0] = coords[1] = coords[2] = 0;
+    nproc = 1; rank = 0; newComm = 0;
+    left = right = down = up = bottom = top = MPI_PROC_NULL;
+    Input();
+    g_ready = true;
+    for (const Named &a : kArrays) std::memset((*a.arr)->ref(), 0, sizeof(double) * count_of(&a));
+    InitializeData();
+    const size_t nc = (size_t)(n1 + 1) * (n2 + 1) * (n3 + 1);
+    std::memcpy(roCon->ref(), ronCon->ref(), sizeof(double) * nc);
+    std::memcpy(u1Con->ref(), u1nCon->ref(), sizeof(double) * nc);
+    std::memcpy(u2Con->ref(), u2nCon->ref(), sizeof(double) * nc);
+    std::memcpy(u3Con->ref(), u3nCon->ref(), sizeof(double) * nc);
+    std::memcpy(tCon->ref(), tnCon->ref(), sizeof(double) * nc);
+    g_forcing = 0;
+    return 0;
+}
+
+/* Grid and parameters after ref_stock_setup: cells C1..C3, then dx1..dx3, VIS, sound, ro0_g, CFL. */
+int ref_stock_params(int *cells, double *vals) {
+    if (!g_ready) return 1;
+    cells[0] = n1 - 1; cells[1] = n2 - 1; cells[2] = n3 - 1;
+    vals[0] = dx1; vals[1] = dx2; vals[2] = dx3; vals[3] = VIS; vals[4] = sound; vals[5] = ro0_g; vals[6] = CFL;
+    vals[7] = x1_e - x1_w; vals[8] = x2_n - x2_s; vals[9] = x3_t - x3_b;
     return 0;
 }
 

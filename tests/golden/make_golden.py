@@ -15,6 +15,9 @@ Files:
   phases.npz         10x6x8 cells: one call of each step piece on a perturbed state
   digests.json       sha256 of every interior array after longer runs (64x32x32 x 100
                      steps at Re_b 2800, 33x17x9 x 50 steps), plus dt, TIME, U_b
+  stock_case.npz     the reference's own case, set up by its Input() and InitializeData()
+                     (200x60x1 backward-facing step): the initial state and the interior
+                     arrays after 40 steps
 """
 from __future__ import annotations
 
@@ -111,7 +114,15 @@ def main():
         ph[f"phase2/{n}"] = oracle.interior(n, ref.get(n))
     np.savez_compressed(os.path.join(HERE, "phases.npz"), params=json.dumps(p3), state_seed=5, **ph)
 
-    # 4. digests of longer runs
+    # 4. the reference's own stock case (its Input() and InitializeData())
+    ref, ps = oracle.Reference.stock()
+    init = {n: ref.get(n) for n in oracle.STATE_NAMES}
+    ref.run(40)
+    d = interior_dump(ref)
+    np.savez_compressed(os.path.join(HERE, "stock_case.npz"), params=json.dumps(ps), steps=40, dt=ref.dt,
+                        time=ref.time, **{f"init/{n}": a for n, a in init.items()}, **d)
+
+    # 5. digests of longer runs
     dig = {}
     for (C, steps, re_b, seed) in (((64, 32, 32), 100, 2800.0, 12345), ((33, 17, 9), 50, 2800.0, 99)):
         pp = oracle.channel_params(*C, re_b=re_b, seed=seed)

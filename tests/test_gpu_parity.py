@@ -298,3 +298,71 @@ def test_constant_division_is_correctly_rounded(ark):
     bad = ctypes.c_longlong(-1)
     assert ark.lib().ark_selftest_division(1 << 26, 2024, ctypes.byref(bad)) == 0
     assert bad.value == 0
+
+
+def test_bounded_edges_match_reference(ark, port):
+    """Bounded x (inflow R = 1 / outflow Q = 5/6 invariants, main.cpp:1731-1745) and bounded z
+    (zero-gradient ghosts), against the reference's own outputs, both precisions' paths
+    running; FP64 bit for bit."""
+    g = np.load(os.path.join(GOLD, "small_bounded.npz"))
+    p = json.loads(str(g["params"]))
+    gp = params_from(ark, p)
+    gp.periodic_x = gp.periodic_z = 0
+    with ark.Context(gp) as ctx:
+        ctx.upload(port.channel_state(p))
+        ctx.step(int(g["steps"]))
+        ctx.sync()
+        assert ctx.scalars().dt == float(g["dt"])
+        st = ctx.download(CELLS + FACES)
+    for n in CELLS + FACES:
+        assert bits_equal(port.interior(n, st[n]), g[n]), n
+
+
+def test_reference_stock_case_on_gpu(ark, port):
+    """The reference's own case (Input()/InitializeData(): backward-facing step 200x60x1, solid
+    block, bounded in every direction, no forcing), 40 steps through ark_step: bit for bit."""
+    g = np.load(os.path.join(GOLD, "stock_case.npz"))
+    p = json.loads(str(g["params"]))
+    st = {n[5:]: np.ascontiguousarray(g[n]) for n in g.files if n.startswith("init/")}
+    gp = ark.make_params(p["C1"], p["C2"], p["C3"], vis=p["nu"], sound=p["sound"], rho0=p["rho0"], cfl=p["cfl"],
+                         lx=p["lx"], ly=p["ly"], lz=p["lz"], forcing=False)
+    gp.periodic_x = gp.periodic_z = 0
+    with ark.Context(gp) as ctx:
+        ctx.upload(st)
+        ctx.step(int(g["steps"]))
+        ctx.sync()
+        assert ctx.scalars().dt == float(g["dt"])
+        out = ctx.download(CELLS + FACES)
+    for n in CELLS + FACES:
+        assert bits_equal(port.interior(n, out[n]), g[n]), n
+
+
+@pytest.mark.parametrize("px,pz", [(0, 1), (1, 0), (0, 0)])
+def test_bounded_axes_match_oracle(ark, port, px, pz):
+    """Each combination of bounded axes on a larger grid against the C restatement, with the
+    per-phase calls and the fused step both checked."""
+    p = port.channel_params(48, 20, 24, seed=13)
+    st0 = port.channel_state(p)
+    o = port.Port(p, periodic_x=bool(px), periodic_z=bool(pz))
+    o.load(st0)
+    o.run(12)
+    gp = params_from(ark, p)
+    gp.periodic_x, gp.periodic_z = px, pz
+    for fused in (True, False):
+        with ark.Context(gp) as ctx:
+            ctx.upload(st0)
+            if fused:
+                ctx.step(12)
+            else:
+                for _ in range(12):
+                    ctx.time_step_size()
+                    ctx.phase1()
+                    ctx.stress_tensor()
+                    ctx.use_forces()
+                    ctx.phase2()
+                    ctx.phase1()
+                    ctx.use_forces()
+            ctx.sync()
+            st = ctx.download(CELLS + FACES)
+        for n in CELLS + FACES:
+            assert bits_equal(port.interior(n, st[n]), port.interior(n, o.get(n))), (fused, n)

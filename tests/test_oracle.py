@@ -155,3 +155,17 @@ def test_splitmix64_known_values(port):
     # splitmix64 seeded with 0: published first outputs of the generator
     v = port.splitmix64(0, 3)
     assert [int(x) for x in v] == [0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4, 0x06C45D188009454F]
+
+
+def test_port_matches_reference_stock_case(port):
+    """The reference's own case (its Input() and InitializeData(): 200x60x1 backward-facing
+    step, bounded in x and z, solid block x <= 5, y <= 1), 40 steps, bit for bit."""
+    g = np.load(os.path.join(GOLD, "stock_case.npz"))
+    p = json.loads(str(g["params"]))
+    st = {n[5:]: g[n] for n in g.files if n.startswith("init/")}
+    o = port.Port(p, periodic_x=False, periodic_z=False, forcing=False)
+    o.load(st)
+    o.run(int(g["steps"]))
+    assert o.dt == float(g["dt"])
+    for n in CELLS + list(port.FACE_NAMES):
+        assert bits_equal(port.interior(n, o.get(n)), g[n]), n
