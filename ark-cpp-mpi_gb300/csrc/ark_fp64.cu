@@ -6,35 +6,36 @@ namespace ark {
 template struct Launch<double>;
 
 // Self-check of div_rn against the hardware IEEE division: n operand pairs from splitmix64
-// (numerators and divisors with random signs, mantissas and exponents in [-40, 40]);
-// divisors are reused 8 times so the reciprocal is a "run constant" like dx or dt.
+// (random signs and mantissas; numerator exponents over the whole range, subnormals and
+// zeros included, divisor exponents in [-120, 120]); divisors are reused 8 times so the
+// reciprocal is a "run constant" like dx or dt.  Also the small exact cases the step meets.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
 }
-__device__ __forceinline__ double rnd_double(unsigned long long z) {
+__device__ __forceinline__ double rnd_double(unsigned long long z, int emin, int emax) {
     const unsigned long long mant = z & 0x000FFFFFFFFFFFFFull;
-    const long long e = (long long)((z >> 52) % 81) - 40 + 1023;
+    const long long e = (long long)((z >> 52) % (unsigned long long)(emax - emin + 1)) + emin + 1023;
     const unsigned long long sign = (z >> 63) << 63;
+    if (e <= 0) return __longlong_as_double((long long)(sign | (mant >> (1 - e)))); // subnormal / zero
     return __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | mant));
 }
 __global__ void k_selftest_division(long long n, unsigned long long seed, unsigned long long *bad) {
     unsigned long long local = 0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const double a = rnd_double(mix64(seed + 2 * (unsigned long long)t));
-        const double b = rnd_double(mix64(seed + 2 * (unsigned long long)(t / 8) + 1));
+        const unsigned long long za = mix64(seed + 2 * (unsigned long long)t);
+        const double a = (t & 3) == 0 ? rnd_double(za, -1075, 1000) : rnd_double(za, -60, 60);
+        const double b = rnd_double(mix64(seed + 2 * (unsigned long long)(t / 8) + 1), -120, 120);
         const double rb = 1.0 / b;
         const double want = a / b, got = div_rn(a, b, rb);
         if (__double_as_longlong(want) != __double_as_longlong(got)) ++local;
-        // the small-integer and exact cases the step meets (2*(x - y), p with ro0 = 1, c = 10)
         const double a2 = (double)(long long)(t % 2001 - 1000) * 0.5, b2 = 10.0;
         if (__double_as_longlong(a2 / b2) != __double_as_longlong(div_rn(a2, b2, 1.0 / b2))) ++local;
     }
     if (local) atomicAdd(bad, local);
 }
-
 
 void selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st) {
     k_selftest_division<<<152 * 4, 256, 0, st>>>(n, seed, bad);

@@ -41,27 +41,27 @@ template <class T> __device__ __forceinline__ T max3d(T x1, T x2, T x3) {
     return x1;
 }
 
-// True when a double is +0 or -0 (integer test: keeps the FP64 pipe free).
-__device__ __forceinline__ bool is_zero(double r) { return (__double_as_longlong(r) << 1) == 0; }
-
 // a / b correctly rounded, given rb = RN(1/b) (the IEEE reciprocal).  Markstein's theorem
 // (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
 // processor", IBM J. Res. Dev. 34(1), 1990): if rb is within half an ulp of 1/b and q is
 // within one ulp of a/b, then with the exact residual r = a - b*q (one FMA),
-// RN(q + r*rb) = RN(a/b).  q = RN(a*rb) may be up to 1.5 ulp off, so one correction makes
-// it faithful and a second one makes it correctly rounded: 1 multiply + 4 FMA.  A zero
-// residual means q is already exact, and is kept as is so the sign of a zero quotient is
-// the IEEE one.  The FP64 parity tests check every quotient of the step against the
-// reference bit for bit, and ark_selftest_division compares with the hardware division.
+// RN(q + r*rb) = RN(a/b), provided nothing underflows or overflows.  q = RN(a*rb) may be up
+// to 1.5 ulp off, so one correction makes it faithful and a second one makes it correctly
+// rounded: 1 multiply + 4 FMA.  Operands outside 2^-895 <= |a| < 2^897 and
+// 2^-100 <= |b| < 2^101 (where the residual could leave the normal range), zeros included,
+// take the IEEE division instead; the exponent test is integer work.  The FP64 parity tests
+// check every quotient of the step against the reference bit for bit, and
+// ark_selftest_division compares with the hardware division, tiny and subnormal operands
+// included.
 __device__ __forceinline__ double div_rn(double a, double b, double rb) {
+    const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7FFu;
+    const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7FFu;
+    if (ea - 128u > 1792u || eb - 923u > 200u) return a / b;
     double q = a * rb;
     double r = __fma_rn(-q, b, a);
-    if (!is_zero(r)) {
-        q = __fma_rn(r, rb, q);
-        r = __fma_rn(-q, b, a);
-        if (!is_zero(r)) q = __fma_rn(r, rb, q);
-    }
-    return q;
+    q = __fma_rn(r, rb, q);
+    r = __fma_rn(-q, b, a);
+    return __fma_rn(r, rb, q);
 }
 
 // Division by a run constant b whose reciprocal rb is known.  FP64: the correctly rounded
