@@ -30,7 +30,11 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_boundary_fill", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
            "ark_get_scalars", "ark_set_scalars", "ark_conservation_sums", "ark_channel_init",
            "ark_kernel_times", "ark_kernel_name", "ark_alloc_host_state", "ark_free_host_state",
-           "ark_conservation_sums_noalloc", "ark_mean_profile", "ark_selftest_division")
+           "ark_conservation_sums_noalloc", "ark_mean_profile", "ark_selftest_division",
+           "ark_ensemble_create", "ark_ensemble_destroy", "ark_ensemble_last_error", "ark_ensemble_size",
+           "ark_ensemble_upload", "ark_ensemble_download", "ark_ensemble_step", "ark_ensemble_sync",
+           "ark_ensemble_time_steps", "ark_ensemble_get_scalars", "ark_ensemble_mean_profile",
+           "ark_ensemble_autotune", "ark_ensemble_set_shape", "ark_ensemble_kernel_times")
 
 
 class ArkError(RuntimeError):
@@ -108,6 +112,21 @@ def lib():
         L.ark_alloc_host_state.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(HostState)]
         L.ark_free_host_state.argtypes = [ctypes.POINTER(HostState)]
         L.ark_mean_profile.argtypes = [vp, _DP, _DP]
+        L.ark_ensemble_create.restype = vp
+        L.ark_ensemble_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
+        L.ark_ensemble_last_error.restype = ctypes.c_char_p
+        for fn in ("ark_ensemble_destroy", "ark_ensemble_sync"):
+            getattr(L, fn).argtypes = [vp]
+        L.ark_ensemble_size.argtypes = [vp]
+        L.ark_ensemble_upload.argtypes = [vp, ctypes.c_int, ctypes.POINTER(HostState)]
+        L.ark_ensemble_download.argtypes = [vp, ctypes.c_int, ctypes.POINTER(HostState)]
+        L.ark_ensemble_step.argtypes = [vp, ctypes.c_int]
+        L.ark_ensemble_time_steps.argtypes = [vp, ctypes.c_int, _DP]
+        L.ark_ensemble_kernel_times.argtypes = [vp, ctypes.c_int, _DP, ctypes.c_int, ip]
+        L.ark_ensemble_get_scalars.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Scalars)]
+        L.ark_ensemble_mean_profile.argtypes = [vp, ctypes.c_int, _DP, _DP]
+        L.ark_ensemble_autotune.argtypes = [vp, ctypes.c_int, ip]
+        L.ark_ensemble_set_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.ark_selftest_division.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_longlong)]
         L.ark_conservation_sums_noalloc.argtypes = [ctypes.POINTER(Params)] + [ctypes.c_void_p] * 5 + [
             ctypes.POINTER(Sums)]
@@ -317,3 +336,81 @@ class Context:
         s = Sums()
         self._call("ark_conservation_sums", ctypes.byref(s))
         return s
+
+
+class Ensemble:
+    """An ark_ensemble: independent FP32 channels advanced together, one launch per phase."""
+
+    def __init__(self, params: list):
+        L = lib()
+        self.params = list(params)
+        arr = (Params * len(params))(*params)
+        rc = ctypes.c_int(0)
+        self.h = L.ark_ensemble_create(arr, len(params), ctypes.byref(rc))
+        if not self.h:
+            raise ArkError("ark_ensemble_create", rc.value or 2, L.ark_ensemble_last_error().decode())
+
+    def _call(self, fn, *args):
+        rc = getattr(lib(), fn)(self.h, *args)
+        if rc != 0:
+            raise ArkError(fn, rc, lib().ark_ensemble_last_error().decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ark_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, member, st: dict):
+        self._call("ark_ensemble_upload", int(member), ctypes.byref(host_struct(st)))
+
+    def download(self, member, names=STATE_FIELDS) -> dict:
+        cs, fs = shapes(self.params[member])
+        st = {n: np.empty(cs if n in CELL_FIELDS else fs) for n in names}
+        self._call("ark_ensemble_download", int(member), ctypes.byref(host_struct(st)))
+        return st
+
+    def step(self, n=1):
+        self._call("ark_ensemble_step", int(n))
+
+    def sync(self):
+        self._call("ark_ensemble_sync")
+
+    def time_steps(self, n):
+        ms = ctypes.c_double(0.0)
+        self._call("ark_ensemble_time_steps", int(n), ctypes.byref(ms))
+        return ms.value
+
+    def kernel_times(self, nsteps):
+        """Mean device ms of each launch of the ensemble step: list of (name, ms)."""
+        ms = (ctypes.c_double * 32)()
+        cnt = ctypes.c_int(0)
+        self._call("ark_ensemble_kernel_times", int(nsteps), ms, 32, ctypes.byref(cnt))
+        return [(lib().ark_kernel_name(q).decode(), ms[q]) for q in range(cnt.value)]
+
+    def scalars(self, member) -> Scalars:
+        s = Scalars()
+        self._call("ark_ensemble_get_scalars", int(member), ctypes.byref(s))
+        return s
+
+    def mean_profile(self, member):
+        prof = np.empty(self.params[member].n2_cells)
+        ws = np.empty(2)
+        self._call("ark_ensemble_mean_profile", int(member), prof.ctypes.data_as(_DP), ws.ctypes.data_as(_DP))
+        return prof, ws
+
+    def autotune(self, steps_per_candidate=3):
+        c = (ctypes.c_int * 4)()
+        self._call("ark_ensemble_autotune", int(steps_per_candidate), c)
+        return {"march_phase1_stress": c[0], "march_phase1": c[1], "segment": c[2], "us_per_step": c[3]}
+
+    def set_shape(self, march_a, march_b, segment):
+        self._call("ark_ensemble_set_shape", int(march_a), int(march_b), int(segment))

@@ -155,6 +155,11 @@ struct Engine {
 
 } // namespace
 
+namespace ark {
+// Run constants of a parameter set (shared with the ensemble code).
+Consts make_run_consts(const ark_params &p) { return make_consts(p); }
+} // namespace ark
+
 struct ark_ctx {
     ark_params P;
     Geom g;

@@ -1,0 +1,734 @@
+// Ensembles: many independent channels of different sizes and parameters advanced together,
+// one launch per phase of the step for all members, the whole step captured in one CUDA graph.
+//
+// Each batched kernel is persistent: a grid sized to what the GPU holds at once walks a work
+// list that concatenates every member's blocks ("tiles").  A block finds its member by
+// binary search over the list's start offsets and then runs exactly the device code the
+// single-grid kernels run (the *_body functions of ark_kernels.cuh), so each member's
+// result is bit-identical to running it alone in its own ark_ctx.  Members are FP32
+// contexts (density stored as rho - ro0; FP64 reductions), as the FP32 path is the
+// throughput path.
+//
+// Kernel shapes (Phase1 marching or one cell per thread, for each of the two Phase1s; the
+// face-segment length of the x2/x3 sweeps) change which thread computes what but not the
+// results; ark_ensemble_autotune times every combination on the live state and keeps the
+// fastest.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ark_gpu.h"
+#include "ark_kernels.cuh"
+
+using namespace ark;
+
+namespace ark {
+Consts make_run_consts(const ark_params &p); // ark_api.cu
+}
+
+namespace {
+
+thread_local std::string g_ens_error;
+
+int efail(int st, const std::string &m) {
+    g_ens_error = m;
+    return st;
+}
+
+#define ENS_CUDA(call)                                                                               \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return efail(e_ == cudaErrorMemoryAllocation ? ARK_ERR_NOMEM : ARK_ERR_CUDA,             \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+    } while (0)
+
+// A work list: info[q] = {first block of member q, blocks in x, blocks in y, unused};
+// extra[q] a per-member integer (the sweep segment length).
+struct WorkList {
+    const int4 *info;
+    const int *extra;
+    int n;
+    int total;
+};
+
+__device__ __forceinline__ int find_member(const WorkList &W, int b) {
+    int lo = 0, hi = W.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (W.info[mid].x <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ BIx decode(const WorkList &W, int q, int b) {
+    const int4 f = W.info[q];
+    const int local = b - f.x;
+    BIx bx;
+    bx.gx = f.y;
+    bx.gy = f.z;
+    bx.x = local % f.y;
+    const int r = local / f.y;
+    bx.y = r % f.z;
+    bx.z = r / f.z;
+    return bx;
+}
+
+using DS = DevState<float>;
+
+__global__ void __launch_bounds__(1024) kb_finalize(const DS *__restrict__ inst, int advance) {
+    finalize_dt_body<float>(inst[blockIdx.x], advance);
+}
+
+__global__ void __launch_bounds__(kTileX *kTileY) kb_reduce(const DS *__restrict__ inst, WorkList W, int con) {
+    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+        const int q = find_member(W, b);
+        reduce_start_body<float>(inst[q], con, decode(W, q, b));
+        __syncthreads();
+    }
+}
+
+// jobs[q]: member q's ghost-fill job; threads of a block cover 128 plane points
+__global__ void __launch_bounds__(128) kb_wrap(const DS *__restrict__ inst, const WrapJob *__restrict__ jobs, WorkList W) {
+    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+        const int q = find_member(W, b);
+        const BIx bx = decode(W, q, b);
+        wrap_body<float>(inst[q].g, jobs[q], (int64_t)bx.x * 128 + threadIdx.x);
+    }
+}
+
+template <int MODE, bool MARCH>
+__global__ void __launch_bounds__(kTileX *kTileY) kb_phase1(const DS *__restrict__ inst, WorkList W, int src, int dst, int fcur) {
+    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+        const int q = find_member(W, b);
+        const BIx bx = decode(W, q, b);
+        if (MARCH) phase1_march_body<float, MODE>(inst[q], src, dst, fcur, bx);
+        else phase1_cell_body<float, MODE>(inst[q], src, dst, fcur, bx);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(128) kb_sweep_x(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
+    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+        const int q = find_member(W, b);
+        sweep_x_body<float>(inst[q], con, fcur, decode(W, q, b));
+    }
+}
+
+template <int AX>
+__global__ void __launch_bounds__(128) kb_sweep_col(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
+    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+        const int q = find_member(W, b);
+        sweep_col_body<float, AX>(inst[q], con, fcur, W.extra[q], decode(W, q, b));
+    }
+}
+
+// Kinds of work list.
+enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_COUNT };
+
+// The candidate kernel shapes the autotuner chooses between.
+struct Shape {
+    int march_a, march_b; // Phase1 with stress / second Phase1: 1 marching, 0 one cell per thread
+    int seg;              // target faces per thread segment in the x2/x3 sweeps
+};
+
+} // namespace
+
+struct ark_ensemble {
+    int n = 0;
+    std::vector<ark_params> P;
+    std::vector<Consts> K;
+    std::vector<DS> S; // host copies of the members' device states
+    std::vector<void *> allocs;
+    std::vector<std::vector<double>> cond_host;
+    DS *d_inst = nullptr;
+    cudaStream_t st = nullptr;
+    double *stage = nullptr; // double staging buffer (largest member)
+    // work lists: device arrays, rebuilt when the shape changes
+    int4 *d_info[WL_COUNT] = {};
+    int *d_extra[WL_COUNT] = {};
+    int total[WL_COUNT] = {};
+    WrapJob *d_jobs = nullptr; // [6][n]: wrap_con for level 0/1, wrap_phase2 for (con, fcur)
+    int persist = 1;           // persistent blocks per launch (all SMs x resident blocks)
+    Shape shape = {1, 0, 32};
+    int con = 0, fcur = 0;
+    bool parts_valid = false;
+    bool uploaded_all = false;
+    std::vector<char> uploaded;
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+template <class U> int ens_alloc(ark_ensemble *E, U **out, size_t n) {
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(U));
+    if (e != cudaSuccess) return efail(ARK_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    E->allocs.push_back(p);
+    cudaMemset(p, 0, n * sizeof(U));
+    *out = (U *)p;
+    return ARK_OK;
+}
+
+Geom geom_of(const ark_params &p) {
+    Geom g;
+    g.C1 = p.n1_cells;
+    g.C2 = p.n2_cells;
+    g.C3 = p.n3_cells;
+    g.cs1 = g.C1 + 2;
+    g.cs2 = (int64_t)(g.C1 + 2) * (g.C2 + 2);
+    g.fs1 = g.C1 + 3;
+    g.fs2 = (int64_t)(g.C1 + 3) * (g.C2 + 3);
+    return g;
+}
+
+int alloc_member(ark_ensemble *E, DS &S) {
+    const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
+    int rc = 0;
+    for (int l = 0; l < 2; ++l) {
+        rc |= ens_alloc(E, &S.lv[l].ro, nc);
+        rc |= ens_alloc(E, &S.lv[l].u1, nc);
+        rc |= ens_alloc(E, &S.lv[l].u2, nc);
+        rc |= ens_alloc(E, &S.lv[l].u3, nc);
+    }
+    for (int m = 0; m < 3; ++m) rc |= ens_alloc(E, &S.f[m], nc);
+    for (int gen = 0; gen < 2; ++gen)
+        for (int d = 0; d < 3; ++d) {
+            FaceSet<float> &F = S.fc[gen][d];
+            rc |= ens_alloc(E, &F.p, nf);
+            F.ro = nullptr; // FP32 derives face density from p
+            for (int m = 0; m < 3; ++m) rc |= ens_alloc(E, &F.u[m], nf);
+        }
+    for (int d = 0; d < 3; ++d)
+        for (int m = 0; m < 3; ++m) S.sig[d][m] = nullptr;
+    rc |= ens_alloc(E, &S.flags, nc);
+    rc |= ens_alloc(E, &S.sc, 1);
+    rc |= ens_alloc(E, &S.part_max, 3 * (size_t)kBuckets);
+    rc |= ens_alloc(E, &S.part_sum, (size_t)kBuckets);
+    return rc ? ARK_ERR_NOMEM : ARK_OK;
+}
+
+int segment_for(int nd, int target) {
+    const int ns = (nd + target - 1) / target;
+    return (nd + ns - 1) / ns;
+}
+
+// Builds the work lists for the current shape.
+int build_lists(ark_ensemble *E) {
+    for (int kind = 0; kind < WL_COUNT; ++kind) {
+        std::vector<int4> info(E->n);
+        std::vector<int> extra(E->n, 0);
+        int start = 0;
+        for (int q = 0; q < E->n; ++q) {
+            const Geom &g = E->S[q].g;
+            int gx = 1, gy = 1, gz = 1;
+            switch (kind) {
+            case WL_TILES: gx = tiles_x(g), gy = tiles_y(g), gz = tiles_k(g); break;
+            case WL_CELLS: gx = tiles_x(g), gy = tiles_y(g), gz = g.C3; break;
+            case WL_SWEEPX: gx = (g.C2 * g.C3 + 3) / 4; break;
+            case WL_COL1: {
+                const int seg = segment_for(g.C2 + 1, E->shape.seg);
+                extra[q] = seg;
+                gx = (g.C1 + 127) / 128, gy = g.C3, gz = (g.C2 + 1 + seg - 1) / seg;
+                break;
+            }
+            case WL_COL2: {
+                const int seg = segment_for(g.C3 + 1, E->shape.seg);
+                extra[q] = seg;
+                gx = (g.C1 + 127) / 128, gy = g.C2, gz = (g.C3 + 1 + seg - 1) / seg;
+                break;
+            }
+            case WL_WRAP: {
+                const int64_t tot = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
+                gx = (int)((tot + 127) / 128);
+                break;
+            }
+            }
+            info[q] = make_int4(start, gx, gy, gz);
+            start += gx * gy * gz;
+        }
+        E->total[kind] = start;
+        if (!E->d_info[kind]) {
+            if (int rc = ens_alloc(E, &E->d_info[kind], (size_t)E->n)) return rc;
+            if (int rc = ens_alloc(E, &E->d_extra[kind], (size_t)E->n)) return rc;
+        }
+        ENS_CUDA(cudaMemcpy(E->d_info[kind], info.data(), sizeof(int4) * E->n, cudaMemcpyHostToDevice));
+        ENS_CUDA(cudaMemcpy(E->d_extra[kind], extra.data(), sizeof(int) * E->n, cudaMemcpyHostToDevice));
+    }
+    return ARK_OK;
+}
+
+// Ghost-fill jobs of every member for both level roles and face generations (the same
+// arrays and modes as Launch<float>::wrap_con / wrap_phase2).
+int build_jobs(ark_ensemble *E) {
+    std::vector<WrapJob> jobs(6 * (size_t)E->n);
+    for (int q = 0; q < E->n; ++q) {
+        const DS &S = E->S[q];
+        const bool px = S.k.periodic_x, pz = S.k.periodic_z;
+        const uint8_t cx = px ? GH_WRAP : GH_COPY, cz = pz ? GH_WRAP : GH_COPY;
+        for (int lv = 0; lv < 2; ++lv) {
+            WrapJob J = {};
+            const Level<float> L = S.lv[lv];
+            wrap_add(J, L.u1, 0, cx, cz);
+            wrap_add(J, L.u2, 0, cx, cz);
+            wrap_add(J, L.u3, 0, cx, cz);
+            wrap_add(J, L.ro, 0, px ? GH_WRAP : GH_NONE, cz);
+            jobs[(size_t)lv * E->n + q] = J;
+        }
+        for (int con = 0; con < 2; ++con)
+            for (int fc = 0; fc < 2; ++fc) {
+                WrapJob J = {};
+                const Level<float> Ln = S.lv[con ^ 1], Lc = S.lv[con];
+                wrap_add(J, Ln.u1, 0, cx, cz);
+                wrap_add(J, Ln.u2, 0, cx, cz);
+                wrap_add(J, Ln.u3, 0, cx, cz);
+                wrap_add(J, Ln.ro, 0, cx, cz);
+                wrap_add(J, Lc.ro, 0, px ? GH_WRAP : GH_NONE, cz);
+                const FaceSet<float> &X = S.fc[fc][0], &Z = S.fc[fc][2];
+                float *fx[4] = {X.p, X.u[0], X.u[1], X.u[2]};
+                float *fz[4] = {Z.p, Z.u[0], Z.u[1], Z.u[2]};
+                for (int a = 0; a < 4; ++a) wrap_add(J, fx[a], 1, px ? GH_WRAP : GH_NONE, GH_NONE);
+                for (int a = 0; a < 4; ++a) wrap_add(J, fz[a], 1, GH_NONE, cz);
+                jobs[(size_t)(2 + 2 * con + fc) * E->n + q] = J;
+            }
+    }
+    if (!E->d_jobs)
+        if (int rc = ens_alloc(E, &E->d_jobs, jobs.size())) return rc;
+    ENS_CUDA(cudaMemcpy(E->d_jobs, jobs.data(), sizeof(WrapJob) * jobs.size(), cudaMemcpyHostToDevice));
+    return ARK_OK;
+}
+
+WorkList wl(const ark_ensemble *E, int kind) {
+    WorkList W = {E->d_info[kind], E->d_extra[kind], E->n, E->total[kind]};
+    return W;
+}
+
+int grid_of(const ark_ensemble *E, int kind) { return std::max(1, std::min(E->total[kind], E->persist)); }
+
+template <int MODE> void launch_p1(ark_ensemble *E, bool march, int src, int dst, int fcur) {
+    const dim3 blk(kTileX, kTileY);
+    if (march)
+        kb_phase1<MODE, true><<<grid_of(E, WL_TILES), blk, 0, E->st>>>(E->d_inst, wl(E, WL_TILES), src, dst, fcur);
+    else
+        kb_phase1<MODE, false><<<grid_of(E, WL_CELLS), blk, 0, E->st>>>(E->d_inst, wl(E, WL_CELLS), src, dst, fcur);
+}
+
+// One step of every member (the order of main.cpp:82-91, as the single-context fused step).
+void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
+    const int y = x ^ 1;
+    auto mark = [&](int q) {
+        if (ev) cudaEventRecord(ev[q], E->st);
+    };
+    kb_finalize<<<E->n, 1024, 0, E->st>>>(E->d_inst, 1);
+    mark(0);
+    kb_wrap<<<grid_of(E, WL_WRAP), 128, 0, E->st>>>(E->d_inst, E->d_jobs + (size_t)y * E->n, wl(E, WL_WRAP));
+    mark(1);
+    // every member of an ensemble runs the bulk forcing or none does (checked at creation)
+    if (E->K[0].forcing)
+        launch_p1<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(E, E->shape.march_a, y, x, fc);
+    else
+        launch_p1<P1_STRESS | P1_FORCES | P1_RMAX>(E, E->shape.march_a, y, x, fc);
+    mark(2);
+    kb_wrap<<<grid_of(E, WL_WRAP), 128, 0, E->st>>>(E->d_inst, E->d_jobs + (size_t)(2 + 2 * y + fc) * E->n,
+                                                     wl(E, WL_WRAP));
+    mark(3);
+    kb_sweep_x<<<grid_of(E, WL_SWEEPX), 128, 0, E->st>>>(E->d_inst, wl(E, WL_SWEEPX), y, fc);
+    mark(4);
+    kb_sweep_col<1><<<grid_of(E, WL_COL1), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL1), y, fc);
+    mark(5);
+    kb_sweep_col<2><<<grid_of(E, WL_COL2), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL2), y, fc);
+    mark(6);
+    launch_p1<P1_FORCES | P1_RSUM>(E, E->shape.march_b, x, y, fc ^ 1);
+    mark(7);
+}
+
+void drop_graphs(ark_ensemble *E) {
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            if (E->graph[a][b]) {
+                cudaGraphExecDestroy(E->graph[a][b]);
+                E->graph[a][b] = nullptr;
+            }
+}
+
+int ensure_parts(ark_ensemble *E) {
+    if (E->parts_valid) return ARK_OK;
+    for (int q = 0; q < E->n; ++q) {
+        cudaMemsetAsync(E->S[q].part_max, 0, sizeof(unsigned long long) * 3 * kBuckets, E->st);
+        cudaMemsetAsync(E->S[q].part_sum, 0, sizeof(long long) * kBuckets, E->st);
+    }
+    kb_reduce<<<grid_of(E, WL_TILES), dim3(kTileX, kTileY), 0, E->st>>>(E->d_inst, wl(E, WL_TILES), E->con);
+    ENS_CUDA(cudaGetLastError());
+    E->parts_valid = true;
+    return ARK_OK;
+}
+
+int ensure_graph(ark_ensemble *E) {
+    const int x = E->con, fc = E->fcur;
+    if (E->graph[x][fc]) return ARK_OK;
+    cudaGraph_t g = nullptr;
+    ENS_CUDA(cudaStreamBeginCapture(E->st, cudaStreamCaptureModeThreadLocal));
+    ens_step(E, x, fc, nullptr);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(E->st, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return efail(ARK_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
+    }
+    cudaError_t ie = cudaGraphInstantiate(&E->graph[x][fc], g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        E->graph[x][fc] = nullptr;
+        return efail(ARK_ERR_CUDA, std::string("ensemble graph: ") + cudaGetErrorString(ie));
+    }
+    return ARK_OK;
+}
+
+int check_member(ark_ensemble *E, int q) {
+    if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
+    if (q < 0 || q >= E->n) return efail(ARK_ERR_PARAM, "member index out of range");
+    return ARK_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *ark_ensemble_last_error(void) { return g_ens_error.c_str(); }
+
+ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) {
+    int dummy;
+    if (!status) status = &dummy;
+    *status = ARK_ERR_PARAM;
+    if (!params || n < 1) {
+        efail(ARK_ERR_PARAM, "need at least one member");
+        return nullptr;
+    }
+    for (int q = 0; q < n; ++q) {
+        const ark_params &p = params[q];
+        if (p.precision != ARK_FP32) {
+            *status = efail(ARK_ERR_UNSUPPORTED, "ensemble members are FP32 contexts");
+            return nullptr;
+        }
+        if (p.n1_cells < 1 || p.n2_cells < 1 || p.n3_cells < 1 || !(p.sound > 0) || !(p.ro0 > 0) || !(p.cfl > 0) ||
+            !(p.vis >= 0) || !(p.lx > 0) || !(p.ly > 0) || !(p.lz > 0) || p.device != params[0].device ||
+            p.forcing != params[0].forcing) {
+            efail(ARK_ERR_PARAM, "bad member parameters (or members on different devices / forcing modes)");
+            return nullptr;
+        }
+        if ((double)(p.n1_cells + 3) * (p.n2_cells + 3) * (p.n3_cells + 3) >= 2147483647.0) {
+            efail(ARK_ERR_PARAM, "member grid too large for 32-bit indexing");
+            return nullptr;
+        }
+    }
+    if (cudaSetDevice(params[0].device) != cudaSuccess) {
+        *status = efail(ARK_ERR_CUDA, "cudaSetDevice failed");
+        return nullptr;
+    }
+    std::unique_ptr<ark_ensemble> E(new ark_ensemble());
+    E->n = n;
+    E->P.assign(params, params + n);
+    E->S.resize(n);
+    E->K.resize(n);
+    E->cond_host.resize(n);
+    E->uploaded.assign(n, 0);
+    size_t maxf = 0;
+    for (int q = 0; q < n; ++q) {
+        E->K[q] = make_run_consts(params[q]);
+        DS &S = E->S[q];
+        std::memset(&S, 0, sizeof(S));
+        S.g = geom_of(params[q]);
+        S.k = E->K[q];
+        if ((*status = alloc_member(E.get(), S))) return nullptr;
+        maxf = std::max(maxf, (size_t)S.g.nface());
+    }
+    if ((*status = ens_alloc(E.get(), &E->d_inst, (size_t)n))) return nullptr;
+    if (cudaMemcpy(E->d_inst, E->S.data(), sizeof(DS) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+        *status = efail(ARK_ERR_CUDA, "member table copy failed");
+        return nullptr;
+    }
+    if ((*status = ens_alloc(E.get(), &E->stage, maxf))) return nullptr;
+    if (cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking) != cudaSuccess) {
+        *status = efail(ARK_ERR_CUDA, "stream creation failed");
+        return nullptr;
+    }
+    int dev = params[0].device, sms = 152, per = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_phase1<P1_FORCES | P1_RSUM, false>, kTileX * kTileY, 0);
+    E->persist = sms * std::max(per, 1) * 2;
+    if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get()))) return nullptr;
+    cudaEventCreate(&E->ev0);
+    cudaEventCreate(&E->ev1);
+    *status = ARK_OK;
+    return E.release();
+}
+
+int ark_ensemble_destroy(ark_ensemble *E) {
+    if (!E) return ARK_OK;
+    cudaStreamSynchronize(E->st);
+    drop_graphs(E);
+    for (void *p : E->allocs) cudaFree(p);
+    if (E->ev0) cudaEventDestroy(E->ev0);
+    if (E->ev1) cudaEventDestroy(E->ev1);
+    if (E->st) cudaStreamDestroy(E->st);
+    delete E;
+    return ARK_OK;
+}
+
+int ark_ensemble_size(const ark_ensemble *E) { return E ? E->n : 0; }
+
+int ark_ensemble_upload(ark_ensemble *E, int q, const ark_host_state *h) {
+    if (int rc = check_member(E, q)) return rc;
+    if (!h) return efail(ARK_ERR_PARAM, "host state is NULL");
+    double *cells[8] = {h->roCon, h->u1Con, h->u2Con, h->u3Con, h->ronCon, h->u1nCon, h->u2nCon, h->u3nCon};
+    double *faces[3][4] = {{h->p1, h->u11, h->u21, h->u31}, {h->p2, h->u12, h->u22, h->u32}, {h->p3, h->u13, h->u23, h->u33}};
+    for (double *a : cells)
+        if (!a) return efail(ARK_ERR_PARAM, "NULL cell array");
+    for (auto &d : faces)
+        for (double *a : d)
+            if (!a) return efail(ARK_ERR_PARAM, "NULL face array");
+    if (!h->condition) return efail(ARK_ERR_PARAM, "NULL condition");
+    ENS_CUDA(cudaStreamSynchronize(E->st));
+    DS &S = E->S[q];
+    const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
+    const double ro0 = E->P[q].ro0;
+    // into the current roles of the levels and the current face generation (shared by all
+    // members)
+    const int lc = E->con, ln = E->con ^ 1;
+    float *dcell[8] = {S.lv[lc].ro, S.lv[lc].u1, S.lv[lc].u2, S.lv[lc].u3,
+                       S.lv[ln].ro, S.lv[ln].u1, S.lv[ln].u2, S.lv[ln].u3};
+    for (int a = 0; a < 8; ++a) {
+        ENS_CUDA(cudaMemcpy(E->stage, cells[a], nc * sizeof(double), cudaMemcpyHostToDevice));
+        convert_from_double<float>(dcell[a], E->stage, (int64_t)nc, (a % 4 == 0) ? ro0 : 0.0, E->st);
+        ENS_CUDA(cudaStreamSynchronize(E->st));
+    }
+    for (int d = 0; d < 3; ++d) {
+        const FaceSet<float> &F = S.fc[E->fcur][d];
+        float *df[4] = {F.p, F.u[0], F.u[1], F.u[2]};
+        for (int a = 0; a < 4; ++a) {
+            ENS_CUDA(cudaMemcpy(E->stage, faces[d][a], nf * sizeof(double), cudaMemcpyHostToDevice));
+            convert_from_double<float>(df[a], E->stage, (int64_t)nf, 0.0, E->st);
+            ENS_CUDA(cudaStreamSynchronize(E->st));
+        }
+    }
+    E->cond_host[q].assign(h->condition, h->condition + nc);
+    std::vector<uint8_t> fl(nc);
+    long long nfluid = 0;
+    for (size_t c = 0; c < nc; ++c) {
+        const double v = h->condition[c];
+        fl[c] = (uint8_t)((v < 0.5 ? FL_LT : 0) | (v > 0.5 ? FL_GT : 0) | (v == 0 ? FL_EQ0 : 0));
+    }
+    for (int k = 1; k <= S.g.C3; ++k)
+        for (int j = 1; j <= S.g.C2; ++j)
+            for (int i = 1; i <= S.g.C1; ++i)
+                if (fl[(size_t)S.g.cell(i, j, k)] & FL_EQ0) ++nfluid;
+    ENS_CUDA(cudaMemcpy(S.flags, fl.data(), nc, cudaMemcpyHostToDevice));
+    DevScalars sc;
+    std::memset(&sc, 0, sizeof(sc));
+    sc.nfluid = nfluid;
+    ENS_CUDA(cudaMemcpy(S.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice));
+    E->uploaded[q] = 1;
+    E->parts_valid = false;
+    return ARK_OK;
+}
+
+int ark_ensemble_download(ark_ensemble *E, int q, ark_host_state *h) {
+    if (int rc = check_member(E, q)) return rc;
+    if (!h) return efail(ARK_ERR_PARAM, "host state is NULL");
+    ENS_CUDA(cudaStreamSynchronize(E->st));
+    DS &S = E->S[q];
+    const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
+    const double ro0 = E->P[q].ro0;
+    const int c = E->con, n = E->con ^ 1, fc = E->fcur;
+    double *cells[8] = {h->roCon, h->u1Con, h->u2Con, h->u3Con, h->ronCon, h->u1nCon, h->u2nCon, h->u3nCon};
+    float *dcell[8] = {S.lv[c].ro, S.lv[c].u1, S.lv[c].u2, S.lv[c].u3, S.lv[n].ro, S.lv[n].u1, S.lv[n].u2, S.lv[n].u3};
+    for (int a = 0; a < 8; ++a) {
+        if (!cells[a]) continue;
+        convert_to_double<float>(E->stage, dcell[a], (int64_t)nc, (a % 4 == 0) ? ro0 : 0.0, E->st);
+        ENS_CUDA(cudaStreamSynchronize(E->st));
+        ENS_CUDA(cudaMemcpy(cells[a], E->stage, nc * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    double *faces[3][5] = {{h->p1, h->ro1, h->u11, h->u21, h->u31},
+                           {h->p2, h->ro2, h->u12, h->u22, h->u32},
+                           {h->p3, h->ro3, h->u13, h->u23, h->u33}};
+    for (int d = 0; d < 3; ++d) {
+        const FaceSet<float> &F = S.fc[fc][d];
+        const float *df[5] = {F.p, nullptr, F.u[0], F.u[1], F.u[2]};
+        for (int a = 0; a < 5; ++a) {
+            if (!faces[d][a]) continue;
+            if (a == 1) face_density_to_double<float>(E->stage, F.p, (int64_t)nf, E->K[q].ro0, E->K[q].rc2, E->st);
+            else convert_to_double<float>(E->stage, df[a], (int64_t)nf, 0.0, E->st);
+            ENS_CUDA(cudaStreamSynchronize(E->st));
+            ENS_CUDA(cudaMemcpy(faces[d][a], E->stage, nf * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+    }
+    if (h->condition) std::memcpy(h->condition, E->cond_host[q].data(), sizeof(double) * nc);
+    return ARK_OK;
+}
+
+int ark_ensemble_step(ark_ensemble *E, int nsteps) {
+    if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
+    for (char u : E->uploaded)
+        if (!u) return efail(ARK_ERR_STATE, "every member needs a state before stepping");
+    if (nsteps < 0) return efail(ARK_ERR_PARAM, "nsteps < 0");
+    if (int rc = ensure_parts(E)) return rc;
+    for (int s = 0; s < nsteps; ++s) {
+        if (int rc = ensure_graph(E)) return rc;
+        ENS_CUDA(cudaGraphLaunch(E->graph[E->con][E->fcur], E->st));
+        E->fcur ^= 1;
+    }
+    return ARK_OK;
+}
+
+int ark_ensemble_sync(ark_ensemble *E) {
+    if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
+    ENS_CUDA(cudaStreamSynchronize(E->st));
+    for (int q = 0; q < E->n; ++q) {
+        int status = 0;
+        ENS_CUDA(cudaMemcpy(&status, &E->S[q].sc->status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (status & STATUS_NONFINITE) return efail(ARK_ERR_NONFINITE, "non-finite velocity in member " + std::to_string(q));
+    }
+    return ARK_OK;
+}
+
+int ark_ensemble_time_steps(ark_ensemble *E, int nsteps, double *ms) {
+    if (!E || !ms) return efail(ARK_ERR_PARAM, "NULL argument");
+    if (int rc = ensure_parts(E)) return rc;
+    if (int rc = ensure_graph(E)) return rc;
+    E->fcur ^= 1;
+    int rc2 = ensure_graph(E);
+    E->fcur ^= 1;
+    if (rc2) return rc2;
+    ENS_CUDA(cudaStreamSynchronize(E->st));
+    ENS_CUDA(cudaEventRecord(E->ev0, E->st));
+    if (int rc = ark_ensemble_step(E, nsteps)) return rc;
+    ENS_CUDA(cudaEventRecord(E->ev1, E->st));
+    ENS_CUDA(cudaEventSynchronize(E->ev1));
+    float f = 0.f;
+    ENS_CUDA(cudaEventElapsedTime(&f, E->ev0, E->ev1));
+    *ms = (double)f;
+    return ark_ensemble_sync(E);
+}
+
+// The launches of a step in the order ark_kernel_name lists them (the same eight phases as
+// the single-context step), each timed with events around it, averaged over nsteps.
+int ark_ensemble_kernel_times(ark_ensemble *E, int nsteps, double *ms, int cap, int *count) {
+    constexpr int kPhases = 8;
+    if (!E || !ms || !count || nsteps < 1) return efail(ARK_ERR_PARAM, "bad arguments");
+    for (char u : E->uploaded)
+        if (!u) return efail(ARK_ERR_STATE, "every member needs a state before stepping");
+    *count = kPhases;
+    if (int rc = ensure_parts(E)) return rc;
+    cudaEvent_t ev[kPhases + 1] = {};
+    for (auto &e : ev) ENS_CUDA(cudaEventCreate(&e));
+    double acc[kPhases] = {};
+    cudaError_t err = cudaSuccess;
+    for (int s = 0; s < nsteps && err == cudaSuccess; ++s) {
+        cudaEventRecord(ev[0], E->st);
+        ens_step(E, E->con, E->fcur, ev + 1);
+        E->fcur ^= 1;
+        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaEventSynchronize(ev[kPhases]);
+        for (int q = 0; q < kPhases && err == cudaSuccess; ++q) {
+            float f = 0.f;
+            cudaEventElapsedTime(&f, ev[q], ev[q + 1]);
+            acc[q] += f;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (err != cudaSuccess) return efail(ARK_ERR_CUDA, std::string("kernel times: ") + cudaGetErrorString(err));
+    for (int q = 0; q < kPhases && q < cap; ++q) ms[q] = acc[q] / nsteps;
+    return ark_ensemble_sync(E);
+}
+
+int ark_ensemble_get_scalars(ark_ensemble *E, int q, ark_scalars *out) {
+    if (int rc = check_member(E, q)) return rc;
+    if (!out) return efail(ARK_ERR_PARAM, "out is NULL");
+    DevScalars sc;
+    ENS_CUDA(cudaStreamSynchronize(E->st));
+    ENS_CUDA(cudaMemcpy(&sc, E->S[q].sc, sizeof(sc), cudaMemcpyDeviceToHost));
+    out->dt = sc.dt;
+    out->time = sc.time;
+    out->nstep = sc.nstep;
+    out->bulk_velocity = sc.ub;
+    out->bulk_force = sc.G;
+    return ARK_OK;
+}
+
+int ark_ensemble_mean_profile(ark_ensemble *E, int q, double *mean_u1, double *wall_shear) {
+    if (int rc = check_member(E, q)) return rc;
+    if (!mean_u1) return efail(ARK_ERR_PARAM, "mean_u1 is NULL");
+    const DS &S = E->S[q];
+    const int n = S.g.C2;
+    long long *acc = nullptr;
+    ENS_CUDA(cudaMalloc(&acc, sizeof(long long) * 2 * n));
+    Launch<float>::mean_profile(S, E->con ^ 1, acc, E->st);
+    std::vector<long long> h(2 * (size_t)n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(E->st);
+    if (e == cudaSuccess) e = cudaMemcpy(h.data(), acc, sizeof(long long) * 2 * n, cudaMemcpyDeviceToHost);
+    cudaFree(acc);
+    if (e != cudaSuccess) return efail(ARK_ERR_CUDA, std::string("profile: ") + cudaGetErrorString(e));
+    for (int j = 0; j < n; ++j)
+        mean_u1[j] = h[2 * j + 1] > 0 ? ((double)h[2 * j] * (1.0 / 4294967296.0)) / (double)h[2 * j + 1] : 0.0;
+    if (wall_shear) {
+        wall_shear[0] = 2 * E->P[q].vis * mean_u1[0] / S.k.dx[1];
+        wall_shear[1] = 2 * E->P[q].vis * mean_u1[n - 1] / S.k.dx[1];
+    }
+    return ARK_OK;
+}
+
+// Times every candidate shape for steps_per_candidate steps on the live state (the results do
+// not depend on the shape) and keeps the fastest.  choice (4 ints, may be NULL) receives the
+// chosen {march_a, march_b, segment target, ms per step x 1000}.
+int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice) {
+    if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
+    if (steps_per_candidate < 1) return efail(ARK_ERR_PARAM, "steps_per_candidate < 1");
+    for (char u : E->uploaded)
+        if (!u) return efail(ARK_ERR_STATE, "every member needs a state before tuning");
+    const Shape cands[] = {{1, 0, 32}, {0, 0, 32}, {1, 1, 32}, {0, 1, 32}, {1, 0, 16}, {1, 0, 64},
+                           {0, 0, 16}, {0, 0, 64}};
+    Shape best = E->shape;
+    double best_ms = 1e300;
+    if (int rc = ensure_parts(E)) return rc;
+    for (const Shape &c : cands) {
+        E->shape = c;
+        if (int rc = build_lists(E)) return rc;
+        drop_graphs(E);
+        // one untimed step to build both graphs, then the timed ones
+        if (int rc = ark_ensemble_step(E, 2)) return rc;
+        double ms = 0;
+        if (int rc = ark_ensemble_time_steps(E, steps_per_candidate, &ms)) return rc;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
+    E->shape = best;
+    drop_graphs(E);
+    if (int rc = build_lists(E)) return rc;
+    if (choice) {
+        choice[0] = best.march_a;
+        choice[1] = best.march_b;
+        choice[2] = best.seg;
+        choice[3] = (int)(1000.0 * best_ms / steps_per_candidate);
+    }
+    return ARK_OK;
+}
+
+int ark_ensemble_set_shape(ark_ensemble *E, int march_a, int march_b, int segment) {
+    if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
+    if (segment < 1) return efail(ARK_ERR_PARAM, "segment < 1");
+    E->shape = Shape{march_a != 0, march_b != 0, segment};
+    drop_graphs(E);
+    return build_lists(E);
+}
+
+} // extern "C"

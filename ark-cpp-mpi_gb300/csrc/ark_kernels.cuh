@@ -142,15 +142,23 @@ __device__ __forceinline__ unsigned long long key_to_double_bits(unsigned long l
     return (unsigned long long)__double_as_longlong((double)__uint_as_float((unsigned)m));
 }
 
-__device__ __forceinline__ int tile_index() {
-    return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+// Block coordinates of one unit of work.  A single-grid launch takes them from blockIdx; a
+// batched (ensemble) launch decodes them from its work list, so both run the same bodies.
+struct BIx {
+    int x, y, z, gx, gy;
+    __device__ __forceinline__ int linear() const { return x + gx * (y + gy * z); }
+};
+__device__ __forceinline__ BIx bix_here() {
+    BIx b = {(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y};
+    return b;
 }
 
 // Block-wide combination of the per-thread partials into the block's slot.  Every thread of
 // the block must call it.
 template <class T>
-__device__ __forceinline__ void tile_store(const DevState<T> &S, bool do_max, bool do_sum, unsigned long long m0,
-                                           unsigned long long m1, unsigned long long m2, long long s) {
+__device__ __forceinline__ void tile_store(const DevState<T> &S, const BIx &bx, bool do_max, bool do_sum,
+                                           unsigned long long m0, unsigned long long m1, unsigned long long m2,
+                                           long long s) {
     __shared__ unsigned long long smax[3][kTileX * kTileY / 32];
     __shared__ long long ssum[kTileX * kTileY / 32];
     m0 = warp_max_u64(m0);
@@ -165,7 +173,7 @@ __device__ __forceinline__ void tile_store(const DevState<T> &S, bool do_max, bo
         ssum[w] = s;
     }
     __syncthreads();
-    const int slot = tile_index() % kBuckets;
+    const int slot = bx.linear() % kBuckets;
     if (t < 3 && do_max) {
         unsigned long long m = 0;
         for (int v = 0; v < kTileX * kTileY / 32; ++v) m = smax[t][v] > m ? smax[t][v] : m;
@@ -183,11 +191,11 @@ __device__ __forceinline__ void tile_store(const DevState<T> &S, bool do_max, bo
 // clear.
 // dt is monotone in max |u|: min over cells of CFL*dx/(c + |u|) is CFL*dx/(c + max|u|)
 // exactly, since IEEE + and / are monotone.  Max and integer sums are order independent.
-template <class T> __global__ void __launch_bounds__(kTileX *kTileY) k_reduce_start(DevState<T> S, int con) {
+template <class T> __device__ __forceinline__ void reduce_start_body(const DevState<T> &S, int con, const BIx &bx) {
     const Geom g = S.g;
-    const int i = blockIdx.x * kTileX + threadIdx.x + 1;
-    const int j = blockIdx.y * kTileY + threadIdx.y + 1;
-    const int k0 = blockIdx.z * kTileK + 1;
+    const int i = bx.x * kTileX + threadIdx.x + 1;
+    const int j = bx.y * kTileY + threadIdx.y + 1;
+    const int k0 = bx.z * kTileK + 1;
     const int k1 = k0 + kTileK - 1 < g.C3 ? k0 + kTileK - 1 : g.C3;
     const T *__restrict__ cu1 = S.lv[con].u1;
     const T *__restrict__ cu2 = S.lv[con].u2;
@@ -208,12 +216,16 @@ template <class T> __global__ void __launch_bounds__(kTileX *kTileY) k_reduce_st
             if (fl[c] & FL_EQ0) s += fixed_sum_term(nu1[c]);
         }
     }
-    tile_store(S, true, true, m0, m1, m2, s);
+    tile_store(S, bx, true, true, m0, m1, m2, s);
+}
+template <class T>
+__global__ void __launch_bounds__(kTileX *kTileY) k_reduce_start(const __grid_constant__ DevState<T> S, int con) {
+    reduce_start_body(S, con, bix_here());
 }
 
 // One block: combine (and clear) the partial slots, form dt as TimeStepSize does, then the
 // bulk force.
-template <class T> __global__ void __launch_bounds__(1024) k_finalize_dt(DevState<T> S, int advance_time) {
+template <class T> __device__ __forceinline__ void finalize_dt_body(const DevState<T> &S, int advance_time) {
     __shared__ unsigned long long smax[3][32];
     __shared__ long long ssum[32];
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
@@ -279,6 +291,10 @@ template <class T> __global__ void __launch_bounds__(1024) k_finalize_dt(DevStat
         sc->time += 0.5 * dt;
     }
 }
+template <class T>
+__global__ void __launch_bounds__(1024) k_finalize_dt(const __grid_constant__ DevState<T> S, int advance_time) {
+    finalize_dt_body(S, advance_time);
+}
 
 // ---------------------------------------------------------------------------------------
 // ghost fill (periodic x and z)
@@ -299,9 +315,8 @@ struct WrapJob {
 //   GH_COPY (bounded axis): zero-gradient ghost 0 <- cell 1, ghost C+1 <- cell C; faces:
 //           halo 0 <- face 1, halo C+2 <- face C+1 (main.cpp:803-845, 1633-1698);
 // over the interior of the other two axes.
-template <class T> __global__ void k_wrap(Geom g, WrapJob J) {
+template <class T> __device__ __forceinline__ void wrap_body(const Geom &g, const WrapJob &J, int64_t t) {
     const int64_t nx = (int64_t)g.C2 * g.C3, nz = (int64_t)g.C1 * g.C2;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < nx) {
         const int j = (int)(t % g.C2) + 1, k = (int)(t / g.C2) + 1;
         for (int q = 0; q < J.n; ++q) {
@@ -332,6 +347,10 @@ template <class T> __global__ void k_wrap(Geom g, WrapJob J) {
             }
         }
     }
+}
+
+template <class T> __global__ void k_wrap(Geom g, const __grid_constant__ WrapJob J) {
+    wrap_body<T>(g, J, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // BoundaryConditions::alongX1/2/3 (source/BoundaryConditions.cpp:22-83) on one cell level,
@@ -509,13 +528,13 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
 // stress force (+ bulk force) of the src level, UseForces, and the partials of the next
 // step's dt (max |u| of dst) or bulk flow (sum of u1 of dst).
 template <class T, int MODE>
-__global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int src, int dst, int fcur) {
+__device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src, int dst, int fcur, const BIx &bx) {
     constexpr bool DEV = Storage<T>::deviation;
     constexpr bool STRESS = MODE & P1_STRESS;
     const Geom g = S.g;
-    const int i = blockIdx.x * kTileX + threadIdx.x + 1;
-    const int j = blockIdx.y * kTileY + threadIdx.y + 1;
-    const int k0 = blockIdx.z * kTileK + 1;
+    const int i = bx.x * kTileX + threadIdx.x + 1;
+    const int j = bx.y * kTileY + threadIdx.y + 1;
+    const int k0 = bx.z * kTileK + 1;
     const int k1 = k0 + kTileK - 1 < g.C3 ? k0 + kTileK - 1 : g.C3;
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long rsum = 0;
@@ -651,18 +670,23 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1(DevState<T> S, int sr
             bot = top;
         }
     }
-    if (MODE & (P1_RMAX | P1_RSUM)) tile_store(S, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+    if (MODE & (P1_RMAX | P1_RSUM)) tile_store(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+}
+template <class T, int MODE>
+__global__ void __launch_bounds__(kTileX *kTileY)
+    k_phase1(const __grid_constant__ DevState<T> S, int src, int dst, int fcur) {
+    phase1_march_body<T, MODE>(S, src, dst, fcur, bix_here());
 }
 
 // Phase1 with one cell per thread (grid z over all planes): fewer registers than the marching
 // kernel, so more warps in flight.  Same arithmetic and outputs as k_phase1.
 template <class T, int MODE>
-__global__ void __launch_bounds__(kTileX *kTileY) k_phase1_cell(DevState<T> S, int src, int dst, int fcur) {
+__device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, int dst, int fcur, const BIx &bx) {
     constexpr bool DEV = Storage<T>::deviation;
     const Geom g = S.g;
-    const int i = blockIdx.x * kTileX + threadIdx.x + 1;
-    const int j = blockIdx.y * kTileY + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
+    const int i = bx.x * kTileX + threadIdx.x + 1;
+    const int j = bx.y * kTileY + threadIdx.y + 1;
+    const int k = bx.z + 1;
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long rsum = 0;
     if (i <= g.C1 && j <= g.C2) {
@@ -740,7 +764,12 @@ __global__ void __launch_bounds__(kTileX *kTileY) k_phase1_cell(DevState<T> S, i
         }
         if ((MODE & P1_RSUM) && (fl & FL_EQ0)) rsum = fixed_sum_term(ucn[0]);
     }
-    if (MODE & (P1_RMAX | P1_RSUM)) tile_store(S, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+    if (MODE & (P1_RMAX | P1_RSUM)) tile_store(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+}
+template <class T, int MODE>
+__global__ void __launch_bounds__(kTileX *kTileY)
+    k_phase1_cell(const __grid_constant__ DevState<T> S, int src, int dst, int fcur) {
+    phase1_cell_body<T, MODE>(S, src, dst, fcur, bix_here());
 }
 
 // StressTensor's face stresses into the sigm arrays (kept only on request), faces normal
@@ -1074,10 +1103,10 @@ __device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, 
 // computed.  A face needs the forward values of the cell behind it: a shuffle from the
 // neighbouring lane, or the carry from the previous chunk's last lane.  Old faces come from
 // generation fcur, new faces go to fcur^1.
-template <class T> __global__ void __launch_bounds__(128) k_sweep_x(DevState<T> S, int con, int fcur) {
+template <class T> __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, const BIx &bx) {
     const Geom g = S.g;
     const int lane = threadIdx.x & 31;
-    const int line = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int line = bx.x * 4 + (threadIdx.x >> 5);
     if (line >= g.C2 * g.C3) return;
     const int j = line % g.C2 + 1, k = line / g.C2 + 1;
     const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
@@ -1157,6 +1186,10 @@ template <class T> __global__ void __launch_bounds__(128) k_sweep_x(DevState<T> 
     }
 }
 
+template <class T> __global__ void __launch_bounds__(128) k_sweep_x(const __grid_constant__ DevState<T> S, int con, int fcur) {
+    sweep_x_body(S, con, fcur, bix_here());
+}
+
 // x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,
 // threads on consecutive i (coalesced), marching along the sweep axis with the next cell's
 // loads issued before the current cell is computed.  A segment of faces s0+1..s1 needs
@@ -1164,12 +1197,12 @@ template <class T> __global__ void __launch_bounds__(128) k_sweep_x(DevState<T> 
 // the current cell is carried in registers.  Old faces come from generation fcur, new
 // faces go to fcur^1, so segments are independent.
 template <class T, int AX>
-__global__ void __launch_bounds__(128) k_sweep_col(DevState<T> S, int con, int fcur, int seg) {
+__device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, int fcur, int seg, const BIx &bx) {
     const Geom g = S.g;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int o = blockIdx.y + 1;
+    const int i = bx.x * 128 + threadIdx.x + 1;
+    const int o = bx.y + 1;
     const int nd = (AX == 1 ? g.C2 : g.C3) + 1;
-    const int s0 = blockIdx.z * seg;
+    const int s0 = bx.z * seg;
     if (i > g.C1 || s0 >= nd) return;
     const int s1 = s0 + seg < nd ? s0 + seg : nd;
     const SweepSrc<T> R = sweep_src(S, con, fcur, AX);
@@ -1200,6 +1233,11 @@ __global__ void __launch_bounds__(128) k_sweep_col(DevState<T> S, int con, int f
         p_b = cur.p_f;
         cur = nxt;
     }
+}
+
+template <class T, int AX>
+__global__ void __launch_bounds__(128) k_sweep_col(const __grid_constant__ DevState<T> S, int con, int fcur, int seg) {
+    sweep_col_body<T, AX>(S, con, fcur, seg, bix_here());
 }
 
 // ---------------------------------------------------------------------------------------

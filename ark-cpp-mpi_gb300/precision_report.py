@@ -1,4 +1,5 @@
-"""Error of the FP32 path against the FP64 path, as BASELINE asks it reported.
+"""Error of the FP32 path against the FP64 path, on the channel's mean profile
+and its wall shear.
 
     python ark-cpp-mpi_gb300/precision_report.py [--grid 512 256 256] [--steps 2000] [--re 5600]
 

@@ -6,7 +6,8 @@
 Workload: the FP64 channel at 256x128x128 cells, Re_b 5600, c = 10, CFL 0.2, bulk forcing,
 seeded perturbations (the reference-parity configuration).  One "step" is one full time
 step (main.cpp:82-91).  Metric: Mcell-steps/s = cells * steps / seconds.  The FP32 path at
-512x256x256 is measured beside it (key "fp32").  Synthetic data: the seeded channel state
+512x256x256 is measured beside it (key "fp32"), and so is a batched ensemble of 64
+independent FP32 channels of mixed sizes (key "ensemble").  Synthetic data: the seeded channel state
 is the benchmark input (the reference has no dataset).
 
 --impl reference times the reference's CPU step on the host cores instead: the compiled
@@ -249,6 +250,49 @@ def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
                                            "h2d_bytes_per_step": down, "d2h_bytes_per_step": down, "steps": n_rt}}
 
 
+ENSEMBLE_GRIDS = ((32, 32, 32), (64, 32, 32), (64, 48, 48), (96, 64, 64), (128, 64, 64))
+
+
+def ensemble_leg(arkgpu, members, steps, warmup, device, seed=4242):
+    """A batched ensemble of independent FP32 channels: grids drawn from ENSEMBLE_GRIDS, Re_b
+    uniform in [2000, 6000], perturbation amplitude uniform in [0.05, 0.15], bulk forcing;
+    one persistent launch per phase under a CUDA graph, kernel shapes autotuned first."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    params, states = [], []
+    for q in range(members):
+        C = ENSEMBLE_GRIDS[int(rng.integers(len(ENSEMBLE_GRIDS)))]
+        p = channel_params(arkgpu, C, float(rng.uniform(2000.0, 6000.0)), arkgpu.FP32)
+        p.device = device
+        params.append(p)
+        states.append((C, float(rng.uniform(0.05, 0.15))))
+    cells = sum(C[0] * C[1] * C[2] for C, _ in states)
+    with arkgpu.Ensemble(params) as E:
+        for q, (p, (C, amp)) in enumerate(zip(params, states)):
+            E.upload(q, arkgpu.channel_init(p, seed=seed + q, amp=amp))
+        t0 = time.perf_counter()
+        shape = E.autotune(3)
+        tune_s = time.perf_counter() - t0
+        E.step(warmup)
+        E.sync()
+        with ClockSampler(device) as clk:
+            ms = E.time_steps(steps)
+        clocks = clk.summary()
+        ktimes = E.kernel_times(5)
+        finite = all(math.isfinite(E.scalars(q).dt) for q in range(members))
+    step_s = ms * 1e-3 / steps
+    counts = {f"{a}x{b}x{c}": sum(1 for C, _ in states if C == (a, b, c)) for a, b, c in ENSEMBLE_GRIDS}
+    return {"value": round(cells * steps / (ms * 1e-3) / 1e6, 3), "unit": UNIT, "members": members,
+            "cells": cells, "grids": counts, "steps": steps, "ms_per_step": round(ms / steps, 4),
+            "dtype": "f32 (f64 reductions)", "launches_per_step": 8, "autotuned_shape": shape,
+            "autotune_s": round(tune_s, 3), "finite": finite,
+            "kernels_ms": {k: round(v, 4) for k, v in ktimes}, "ktimes": ktimes,
+            "step_roofline": {"bytes_per_cell": STEP_VALUES * 4,
+                              "achieved": round(cells * STEP_VALUES * 4 / step_s / 1e9, 1), "unit": "GB/s"},
+            "clocks": clocks}
+
+
 def cpu_leg(C, re_b, budget_s=12.0, max_steps=400, threads=None):
     """The oracle's C restatement of the reference step on the host cores."""
     import oracle
@@ -314,6 +358,8 @@ def main():
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--ensemble", type=int, default=64, help="ensemble members (0: no ensemble leg)")
+    ap.add_argument("--ensemble-steps", type=int, default=500)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -371,6 +417,13 @@ def main():
                                           "frac": round(f["cells"] * STEP_VALUES * 4 / f_step_s / 1e9 / peak, 4)},
                         "kernels_ms": {k: round(v, 4) for k, v in f["ktimes"]}, "clocks": f["clocks"]}
         line["gpu_launches"] += launches_per_step * f_steps
+
+    if rank == 0 and args.ensemble > 0:
+        e = ensemble_leg(arkgpu, args.ensemble, args.ensemble_steps, args.warmup, device)
+        e["step_roofline"].update(peak=peak, frac=round(e["step_roofline"]["achieved"] / peak, 4))
+        e["roofline"] = roofline(e.pop("ktimes"), e["cells"], 4, peak, peak_kind, traffic, "fp32")
+        line["ensemble"] = e
+        line["gpu_launches"] += e["launches_per_step"] * args.ensemble_steps
 
     if rank == 0:
         line["e2e"] = e2e_leg(arkgpu, C, args.re, arkgpu.FP64, args.e2e_steps, device, seed=5)

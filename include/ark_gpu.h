@@ -192,6 +192,35 @@ int ark_mean_profile(ark_ctx *ctx, double *mean_u1, double *wall_shear);
  * Runs on the current device. */
 int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches);
 
+/* ---- ensembles: many independent channels in one launch per phase ------------------------
+ * The members (FP32 contexts, each with its own grid size and parameters, all on one device
+ * and all with or all without bulk forcing) advance together: every phase of the step is one
+ * persistent launch over a table of the members' blocks, and the step is one CUDA graph.
+ * Each member's result is bit-identical to running it alone in an FP32 ark_ctx.  The
+ * single-device analogue of the reference running independent problems side by side, one
+ * per MPI job. */
+typedef struct ark_ensemble ark_ensemble;
+
+ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status);
+int ark_ensemble_destroy(ark_ensemble *ens);
+const char *ark_ensemble_last_error(void);
+int ark_ensemble_size(const ark_ensemble *ens);
+int ark_ensemble_upload(ark_ensemble *ens, int member, const ark_host_state *host);
+int ark_ensemble_download(ark_ensemble *ens, int member, ark_host_state *host);
+int ark_ensemble_step(ark_ensemble *ens, int nsteps);
+int ark_ensemble_sync(ark_ensemble *ens);
+int ark_ensemble_time_steps(ark_ensemble *ens, int nsteps, double *ms);
+/* Per-launch times of a step (ms, averaged over nsteps; names from ark_kernel_name). */
+int ark_ensemble_kernel_times(ark_ensemble *ens, int nsteps, double *ms, int cap, int *count);
+int ark_ensemble_get_scalars(ark_ensemble *ens, int member, ark_scalars *out);
+int ark_ensemble_mean_profile(ark_ensemble *ens, int member, double *mean_u1, double *wall_shear);
+/* Times each candidate kernel shape (Phase1 marching or one cell per thread for each Phase1,
+ * x2/x3 sweep segment length) for steps_per_candidate steps on the live state -- the
+ * results do not depend on the shape -- and keeps the fastest.  choice (4 ints, or NULL):
+ * {Phase1+stress marching, second Phase1 marching, segment target, microseconds per step}. */
+int ark_ensemble_autotune(ark_ensemble *ens, int steps_per_candidate, int *choice);
+int ark_ensemble_set_shape(ark_ensemble *ens, int march_a, int march_b, int segment);
+
 /* ---- host-side helpers (no GPU needed) ----------------------------------------------------- */
 
 /* Seeded channel-flow initial state (a project definition, not part of the reference):

@@ -1,0 +1,81 @@
+"""Ensembles: independent FP32 channels of different sizes and parameters, one launch per
+phase.  Every member must equal the same channel advanced alone in an FP32 ark_ctx, bit for
+bit, whatever kernel shapes the autotuner picks."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CELLS = ["roCon", "u1Con", "u2Con", "u3Con", "ronCon", "u1nCon", "u2nCon", "u3nCon"]
+FACES = ["p1", "ro1", "u11", "u21", "u31", "p2", "ro2", "u12", "u22", "u32", "p3", "ro3", "u13", "u23", "u33"]
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint64), np.ascontiguousarray(b).view(np.uint64))
+
+
+def members(ark):
+    spec = [((32, 16, 16), 2000.0, 0.05, 1, 1), ((40, 24, 20), 3500.0, 0.10, 1, 1),
+            ((24, 12, 30), 6000.0, 0.15, 0, 1), ((17, 9, 11), 2800.0, 0.08, 1, 0)]
+    out = []
+    for q, (C, re, amp, px, pz) in enumerate(spec):
+        p = ark.make_params(*C, re_b=re, precision=ark.FP32)
+        p.periodic_x, p.periodic_z = px, pz
+        out.append((p, ark.channel_init(p, seed=100 + q, amp=amp)))
+    return out
+
+
+def singles(ark, mem, steps):
+    res = []
+    for p, st in mem:
+        with ark.Context(p) as c:
+            c.upload(st)
+            c.step(steps)
+            c.sync()
+            res.append((c.download(CELLS + FACES), c.scalars().dt))
+    return res
+
+
+def test_ensemble_matches_single_contexts(ark, port):
+    mem = members(ark)
+    want = singles(ark, mem, 9)
+    with ark.Ensemble([p for p, _ in mem]) as E:
+        for q, (_, st) in enumerate(mem):
+            E.upload(q, st)
+        E.step(9)
+        E.sync()
+        for q in range(len(mem)):
+            got = E.download(q, CELLS + FACES)
+            assert E.scalars(q).dt == want[q][1]
+            for n in CELLS + FACES:
+                assert bits_equal(port.interior(n, got[n]), port.interior(n, want[q][0][n])), (q, n)
+
+
+def test_ensemble_autotune_keeps_results(ark, port):
+    """The autotuner advances the live state while it times the candidate shapes; the
+    result is the same as plain steps."""
+    mem = members(ark)
+    with ark.Ensemble([p for p, _ in mem]) as E:
+        for q, (_, st) in enumerate(mem):
+            E.upload(q, st)
+        E.step(2)
+        choice = E.autotune(1)
+        assert choice["segment"] in (16, 32, 64)
+        kt = E.kernel_times(2)
+        assert [n for n, _ in kt][2] == "phase1_stress_forces" and len(kt) == 8
+        assert all(ms > 0 for _, ms in kt)
+        done = E.scalars(0).nstep
+        E.sync()
+        want = singles(ark, mem, done)
+        for q in range(len(mem)):
+            got = E.download(q, CELLS + FACES)
+            for n in CELLS + FACES:
+                assert bits_equal(port.interior(n, got[n]), port.interior(n, want[q][0][n])), (q, n)
+        prof, ws = E.mean_profile(1)
+        assert prof.shape == (24,) and np.isfinite(ws).all()
+
+
+def test_ensemble_rejects_fp64_members(ark):
+    p = ark.make_params(16, 8, 8)
+    with pytest.raises(ark.ArkError):
+        ark.Ensemble([p])

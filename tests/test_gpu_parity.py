@@ -84,7 +84,7 @@ def test_fused_step_matches_reference_small(ark, port):
 
 @pytest.mark.parametrize("key", ["33x17x9_50", "64x32x32_100"])
 def test_fused_step_matches_reference_digests(ark, port, key):
-    """BASELINE's parity case (64x32x32, Re_b 2800, 100 steps) and an odd-sized grid: every
+    """The 64x32x32 parity case (Re_b 2800, 100 steps) and an odd-sized grid: every
     interior array bit-identical to the reference (sha256), so rel. L2 = 0 <= 1e-12."""
     with open(os.path.join(GOLD, "digests.json")) as f:
         d = json.load(f)[key]
@@ -127,7 +127,7 @@ def test_per_phase_api_equals_fused_step(ark, port):
 
 @pytest.mark.parametrize("C,steps", [((128, 64, 64), 6), ((256, 128, 128), 2)])
 def test_fused_step_matches_oracle_large(ark, port, C, steps):
-    """Full-size grids (256x128x128 is BASELINE's GPU parity grid) against the C restatement
+    """Full-size grids (256x128x128 is the FP64 benchmark grid) against the C restatement
     for a few steps, bit for bit."""
     p = port.channel_params(*C, re_b=5600.0, seed=2024)
     st0 = port.channel_state(p)
