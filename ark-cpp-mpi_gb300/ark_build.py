@@ -10,6 +10,8 @@ Translation units are compiled in parallel:
   ark_api.cu   C ABI, context, CUDA-graph step
   ark_noalloc.cu  conservation sums over caller-owned device arrays, static scratch (--fmad=false)
   ark_ensemble.cu batched ensembles: persistent kernels over a member table (--fmad=false)
+  ark_output.cu   VTK packing, time averages, kinetic energy (--fmad=false: the averages and
+                  the energy terms round as the reference's)
   ark_host.cpp host-only helpers (seeded channel init)
 Outputs go to ark-cpp-mpi_gb300/lib/ (git-ignored).
 """
@@ -72,6 +74,8 @@ def build(force=False, verbose=False):
                          os.path.join(OBJ, "ark_noalloc.o")],
         [nv] + common + ["--fmad=false", "-c", os.path.join(SRC, "ark_ensemble.cu"), "-o",
                          os.path.join(OBJ, "ark_ensemble.o")],
+        [nv] + common + ["--fmad=false", "-c", os.path.join(SRC, "ark_output.cu"), "-o",
+                         os.path.join(OBJ, "ark_output.o")],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-c",
          os.path.join(SRC, "ark_host.cpp"), "-o", os.path.join(OBJ, "ark_host.o")],
         ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-c",
@@ -93,7 +97,7 @@ def build(force=False, verbose=False):
         msg = "\n".join(" ".join(c) + "\n" + o for c, o in failed)
         raise RuntimeError("build failed:\n" + msg)
     objs = [os.path.join(OBJ, n) for n in ("ark_fp64.o", "ark_fp32.o", "ark_api.o", "ark_noalloc.o", "ark_ensemble.o",
-                                           "ark_host.o")]
+                                           "ark_output.o", "ark_host.o")]
     subprocess.run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static"], check=True)
     subprocess.run(["g++", "-o", RUN, os.path.join(OBJ, "ark_run.o"), "-L", OUT, "-lark_gb300",
                     "-Wl,-rpath,$ORIGIN"], check=True)

@@ -34,7 +34,12 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_ensemble_create", "ark_ensemble_destroy", "ark_ensemble_last_error", "ark_ensemble_size",
            "ark_ensemble_upload", "ark_ensemble_download", "ark_ensemble_step", "ark_ensemble_sync",
            "ark_ensemble_time_steps", "ark_ensemble_get_scalars", "ark_ensemble_mean_profile",
-           "ark_ensemble_autotune", "ark_ensemble_set_shape", "ark_ensemble_kernel_times")
+           "ark_ensemble_autotune", "ark_ensemble_set_shape", "ark_ensemble_kernel_times",
+           "ark_write_vtk", "ark_average_values", "ark_set_averaging", "ark_write_average_vtk",
+           "ark_kinetic_energy", "ark_write_energy", "ark_vorticity")
+
+
+VTK_LAYOUTS = {"full": 0, "reference": 1}
 
 
 class ArkError(RuntimeError):
@@ -112,6 +117,13 @@ def lib():
         L.ark_alloc_host_state.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(HostState)]
         L.ark_free_host_state.argtypes = [ctypes.POINTER(HostState)]
         L.ark_mean_profile.argtypes = [vp, _DP, _DP]
+        L.ark_write_vtk.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
+        L.ark_average_values.argtypes = [vp]
+        L.ark_set_averaging.argtypes = [vp, ctypes.c_int]
+        L.ark_write_average_vtk.argtypes = [vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_int]
+        L.ark_kinetic_energy.argtypes = [vp, _DP]
+        L.ark_write_energy.argtypes = [vp, ctypes.c_char_p]
+        L.ark_vorticity.argtypes = [vp, _DP]
         L.ark_ensemble_create.restype = vp
         L.ark_ensemble_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
         L.ark_ensemble_last_error.restype = ctypes.c_char_p
@@ -262,6 +274,10 @@ class Context:
         self._call("ark_download", ctypes.byref(host_struct(st)))
 
     def get(self, name, face=None):
+        if name.startswith("averageU"):
+            out = np.empty((self.p.n3_cells + 2, self.p.n2_cells + 3, self.p.n1_cells + 2))
+            self._call("ark_get_array", name.encode(), out.ctypes.data_as(_DP))
+            return out
         if face is None:
             face = not (name in CELL_FIELDS or name in ("f1", "f2", "f3"))
         out = np.empty(self.fshape if face else self.cshape)
@@ -336,6 +352,33 @@ class Context:
         s = Sums()
         self._call("ark_conservation_sums", ctypes.byref(s))
         return s
+
+    # output and statistics (WriteDataParaView, AverageValues, WriteAverageValues, WriteEnergy)
+    def write_vtk(self, path, layout="full"):
+        self._call("ark_write_vtk", os.fsencode(path), VTK_LAYOUTS[layout])
+
+    def average_values(self):
+        self._call("ark_average_values")
+
+    def set_averaging(self, on=True):
+        self._call("ark_set_averaging", int(bool(on)))
+
+    def write_average_vtk(self, path, start_time, layout="full"):
+        self._call("ark_write_average_vtk", os.fsencode(path), float(start_time), VTK_LAYOUTS[layout])
+
+    def kinetic_energy(self):
+        e = ctypes.c_double(0.0)
+        self._call("ark_kinetic_energy", ctypes.byref(e))
+        return e.value
+
+    def write_energy(self, path):
+        self._call("ark_write_energy", os.fsencode(path))
+
+    def vorticity(self):
+        """(n3_cells, n2_cells, n1_cells, 3) array of the vorticity R of WriteDataParaView."""
+        out = np.empty((self.p.n3_cells, self.p.n2_cells, self.p.n1_cells, 3))
+        self._call("ark_vorticity", out.ctypes.data_as(_DP))
+        return out
 
 
 class Ensemble:

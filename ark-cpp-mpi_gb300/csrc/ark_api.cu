@@ -2,6 +2,9 @@
 // reference's step pieces and the fused, graph-captured time step.
 #include <cuda_runtime.h>
 
+#include <fcntl.h>
+#include <unistd.h>
+
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -149,6 +152,9 @@ struct Engine {
     virtual void boundary_fill(int ncon, int axis, int periodic) = 0;
     virtual void sums(int ncon) = 0;
     virtual void mean_profile(int ncon, long long *acc) = 0;
+    virtual void pack(int ncon, int fcur, const CellPack &a) = 0;
+    virtual void average_add(int ncon) = 0;
+    virtual void energy(int ncon, double *scratch, double *out) = 0;
     virtual DevScalars *scalars() = 0;
     virtual uint8_t *flags() = 0;
 };
@@ -175,6 +181,12 @@ struct ark_ctx {
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [con][fcur]
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double *stage = nullptr; // device double staging for FP32 contexts
+    AvgArrays avg = {{nullptr, nullptr, nullptr}}; // averageU1..3 (FP64, reference layout)
+    bool averaging = false;  // AverageValues at the end of every step
+    // output streaming: two device and two pinned host slab buffers of io_cap doubles
+    double *io_dev[2] = {nullptr, nullptr};
+    double *io_host[2] = {nullptr, nullptr};
+    size_t io_cap = 0;
 };
 
 namespace {
@@ -376,12 +388,17 @@ template <class T> struct EngineT : Engine {
         }
         Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
         mark(7);
+        // AverageValues after the step (main.cpp:93-96 when enabled), outside the timed marks
+        if (ctx->averaging) output_average_add<T>(S, y, ctx->avg, st);
     }
     void boundary_fill(int ncon, int axis, int periodic) override {
         Launch<T>::boundary_fill(S, ncon, axis, periodic, ctx->st);
     }
     void sums(int ncon) override { Launch<T>::sums(S, ncon, ctx->st); }
     void mean_profile(int ncon, long long *acc) override { Launch<T>::mean_profile(S, ncon, acc, ctx->st); }
+    void pack(int ncon, int fcur, const CellPack &a) override { output_pack<T>(S, ncon, fcur, a, ctx->st); }
+    void average_add(int ncon) override { output_average_add<T>(S, ncon, ctx->avg, ctx->st); }
+    void energy(int ncon, double *scratch, double *out) override { output_energy<T>(S, ncon, scratch, out, ctx->st); }
     DevScalars *scalars() override { return S.sc; }
     uint8_t *flags() override { return S.flags; }
 };
@@ -434,6 +451,7 @@ const char *ark_status_string(int s) {
     case ARK_ERR_STATE: return "call out of order";
     case ARK_ERR_NOMEM: return "device allocation failed";
     case ARK_ERR_UNSUPPORTED: return "unsupported configuration";
+    case ARK_ERR_IO: return "file could not be opened or written";
     default: return "unknown status";
     }
 }
@@ -495,6 +513,12 @@ int ark_destroy(ark_ctx *ctx) {
             if (ctx->graph[a][b]) cudaGraphExecDestroy(ctx->graph[a][b]);
     ctx->eng.reset();
     if (ctx->stage) cudaFree(ctx->stage);
+    for (double *a : ctx->avg.a)
+        if (a) cudaFree(a);
+    for (int b = 0; b < 2; ++b) {
+        if (ctx->io_dev[b]) cudaFree(ctx->io_dev[b]);
+        if (ctx->io_host[b]) cudaFreeHost(ctx->io_host[b]);
+    }
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -556,6 +580,30 @@ int ark_download(ark_ctx *ctx, ark_host_state *h) {
     return ARK_OK;
 }
 
+// "averageU1".."averageU3" -> 1..3, anything else -> 0
+static int average_name(const char *name) {
+    if (std::strncmp(name, "averageU", 8) == 0 && name[8] >= '1' && name[8] <= '3' && name[9] == 0) return name[8] - '0';
+    return 0;
+}
+
+// The averageU arrays, allocated and zeroed on first use.
+static int ensure_averages(ark_ctx *ctx) {
+    if (ctx->avg.a[0]) return ARK_OK;
+    const size_t n = (size_t)avg_count(ctx->g);
+    for (int m = 0; m < 3; ++m) {
+        cudaError_t e = cudaMalloc(&ctx->avg.a[m], sizeof(double) * n);
+        if (e != cudaSuccess) {
+            for (double *&a : ctx->avg.a) {
+                if (a) cudaFree(a);
+                a = nullptr;
+            }
+            return fail(ARK_ERR_NOMEM, std::string("averageU: ") + cudaGetErrorString(e));
+        }
+        ARK_CUDA(cudaMemset(ctx->avg.a[m], 0, sizeof(double) * n));
+    }
+    return ARK_OK;
+}
+
 int ark_get_array(ark_ctx *ctx, const char *name, double *host) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (!name || !host) return fail(ARK_ERR_PARAM, "NULL name or buffer");
@@ -566,6 +614,11 @@ int ark_get_array(ark_ctx *ctx, const char *name, double *host) {
     }
     for (int w = 0; w < 24; ++w)
         if (w != 8 && std::strcmp(name, kFields[w].name) == 0) return ctx->eng->download_field(w, kFields[w].face, host);
+    if (int m = average_name(name)) {
+        if (int rc = ensure_averages(ctx)) return rc;
+        ARK_CUDA(cudaMemcpy(host, ctx->avg.a[m - 1], sizeof(double) * avg_count(ctx->g), cudaMemcpyDeviceToHost));
+        return ARK_OK;
+    }
     int face = 0;
     void *p = ctx->eng->field_ptr(name, &face);
     if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
@@ -581,6 +634,11 @@ int ark_put_array(ark_ctx *ctx, const char *name, const double *host) {
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
     for (int w = 0; w < 24; ++w)
         if (w != 8 && std::strcmp(name, kFields[w].name) == 0) return ctx->eng->upload_field(w, kFields[w].face, host);
+    if (int m = average_name(name)) {
+        if (int rc = ensure_averages(ctx)) return rc;
+        ARK_CUDA(cudaMemcpy(ctx->avg.a[m - 1], host, sizeof(double) * avg_count(ctx->g), cudaMemcpyHostToDevice));
+        return ARK_OK;
+    }
     int face = 0;
     void *p = ctx->eng->field_ptr(name, &face);
     if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
@@ -867,6 +925,270 @@ int ark_mean_profile(ark_ctx *ctx, double *mean_u1, double *wall_shear) {
         wall_shear[1] = 2 * ctx->P.vis * mean_u1[n - 1] / ctx->k.dx[1];
     }
     return ARK_OK;
+}
+
+} // extern "C"
+
+// ---- output and statistics -------------------------------------------------------------
+
+namespace {
+
+void drop_graphs(ark_ctx *ctx) {
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            if (ctx->graph[a][b]) {
+                cudaGraphExecDestroy(ctx->graph[a][b]);
+                ctx->graph[a][b] = nullptr;
+            }
+}
+
+// The two slab buffers (device and pinned host) of at least n doubles each.
+int ensure_io(ark_ctx *ctx, size_t n) {
+    if (ctx->io_cap >= n) return ARK_OK;
+    for (int b = 0; b < 2; ++b) {
+        if (ctx->io_dev[b]) cudaFree(ctx->io_dev[b]);
+        if (ctx->io_host[b]) cudaFreeHost(ctx->io_host[b]);
+        ctx->io_dev[b] = ctx->io_host[b] = nullptr;
+    }
+    ctx->io_cap = 0;
+    for (int b = 0; b < 2; ++b) {
+        if (cudaMalloc(&ctx->io_dev[b], n * sizeof(double)) != cudaSuccess ||
+            cudaMallocHost(&ctx->io_host[b], n * sizeof(double)) != cudaSuccess)
+            return fail(ARK_ERR_NOMEM, "output slab buffers");
+    }
+    ctx->io_cap = n;
+    return ARK_OK;
+}
+
+bool write_all(int fd, const void *buf, size_t n, off_t off) {
+    const char *p = (const char *)buf;
+    while (n > 0) {
+        const ssize_t w = pwrite(fd, p, n, off);
+        if (w <= 0) return false;
+        p += w;
+        n -= (size_t)w;
+        off += w;
+    }
+    return true;
+}
+
+void put_be64(std::string &s, double v) {
+    unsigned char b[8];
+    std::memcpy(b, &v, 8);
+    // host byte order is little-endian on every supported host (x86-64, aarch64)
+    for (int q = 7; q >= 0; --q) s.push_back((char)b[q]);
+}
+
+// Everything before the first data block of the reference's VTK files (main.cpp:2585-2645):
+// headers and node coordinates (i-1)*dx with n_g = C + 1 nodes per axis.
+std::string vtk_head(const ark_ctx *ctx) {
+    const Geom &g = ctx->g;
+    const int ng[3] = {g.C1 + 1, g.C2 + 1, g.C3 + 1};
+    char buf[256];
+    std::string s = "# vtk DataFile Version 3.0\nvtk output\nBINARY\n";
+    std::snprintf(buf, sizeof buf, "DATASET RECTILINEAR_GRID\nDIMENSIONS %d %d %d", ng[0], ng[1], ng[2]);
+    s += buf;
+    const char axis[3] = {'X', 'Y', 'Z'};
+    for (int d = 0; d < 3; ++d) {
+        std::snprintf(buf, sizeof buf, "\n%c_COORDINATES %d double\n", axis[d], ng[d]);
+        s += buf;
+        for (int i = 1; i <= ng[d]; ++i) put_be64(s, (i - 1) * ctx->k.dx[d]);
+    }
+    std::snprintf(buf, sizeof buf, "\nCELL_DATA %d\nVECTORS U double\n", g.C1 * g.C2 * g.C3);
+    s += buf;
+    return s;
+}
+
+enum BlockKind { BK_U, BK_PC, BK_R, BK_AVG };
+struct Block {
+    const char *header;
+    int comps;
+    BlockKind kind;
+};
+
+// Writes head + blocks to path.  Slabs of k planes are packed on the device into one of two
+// buffers and copied to pinned memory while the host writes the previous slab.
+int write_vtk_blocks(ark_ctx *ctx, const char *path, int layout, const Block *blocks, int nb, double avg_div) {
+    if (!path) return fail(ARK_ERR_PARAM, "path is NULL");
+    if (layout != ARK_VTK_FULL && layout != ARK_VTK_REFERENCE) return fail(ARK_ERR_PARAM, "unknown VTK layout");
+    const Geom &g = ctx->g;
+    const int64_t plane = (int64_t)g.C1 * g.C2, ncell = plane * g.C3;
+    int comps = 0;
+    for (int b = 0; b < nb; ++b) comps += blocks[b].comps;
+    // slabs of about 2^20 cells; the reference layout writes only the last plane
+    const int kslab = layout == ARK_VTK_REFERENCE ? 1 : (int)std::max<int64_t>(1, std::min<int64_t>(g.C3, (1 << 20) / std::max<int64_t>(plane, 1)));
+    if (int rc = ensure_io(ctx, (size_t)(kslab * plane * comps))) return rc;
+
+    const std::string head = vtk_head(ctx);
+    std::vector<off_t> data_off(nb);
+    const int fd = open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+    if (fd < 0) return fail(ARK_ERR_IO, std::string("cannot open ") + path);
+    bool ok = write_all(fd, head.data(), head.size(), 0);
+    off_t off = (off_t)head.size();
+    for (int b = 0; b < nb && ok; ++b) {
+        const size_t hl = std::strlen(blocks[b].header);
+        ok = write_all(fd, blocks[b].header, hl, off);
+        off += (off_t)hl;
+        data_off[b] = off;
+        off += (off_t)(ncell * blocks[b].comps * 8);
+    }
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (auto &e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    const int kfirst = layout == ARK_VTK_REFERENCE ? g.C3 : 1;
+    struct Slab {
+        int k0, k1;
+    } pending[2] = {{0, 0}, {0, 0}};
+    int rc = ARK_OK;
+    auto flush = [&](int buf) {
+        const Slab sl = pending[buf];
+        if (sl.k1 <= sl.k0) return;
+        if (cudaEventSynchronize(ev[buf]) != cudaSuccess) {
+            rc = fail(ARK_ERR_CUDA, "output copy failed");
+            return;
+        }
+        const int64_t ns = (int64_t)(sl.k1 - sl.k0) * plane;
+        const double *h = ctx->io_host[buf];
+        for (int b = 0; b < nb && ok; ++b) {
+            const off_t at = layout == ARK_VTK_REFERENCE ? data_off[b] : data_off[b] + (off_t)((sl.k0 - 1) * plane * blocks[b].comps * 8);
+            ok = write_all(fd, h, (size_t)(ns * blocks[b].comps * 8), at);
+            h += ns * blocks[b].comps;
+        }
+        pending[buf] = Slab{0, 0};
+    };
+    int buf = 0;
+    for (int k0 = kfirst; k0 <= g.C3 && ok && rc == ARK_OK; k0 += kslab, buf ^= 1) {
+        const int k1 = std::min(g.C3 + 1, k0 + kslab);
+        flush(buf); // the buffer about to be reused
+        const int64_t ns = (int64_t)(k1 - k0) * plane;
+        double *d = ctx->io_dev[buf];
+        CellPack a;
+        std::memset(&a, 0, sizeof a);
+        a.k0 = k0;
+        a.k1 = k1;
+        a.swap = 1;
+        a.avg_div = avg_div;
+        for (int m = 0; m < 3; ++m) a.avg[m] = ctx->avg.a[m];
+        for (int b = 0; b < nb; ++b) {
+            switch (blocks[b].kind) {
+            case BK_U: a.u = d; break;
+            case BK_PC: a.pc = d; break;
+            case BK_R: a.r = d; break;
+            case BK_AVG: a.avg_out = d; break;
+            }
+            d += ns * blocks[b].comps;
+        }
+        ctx->eng->pack(ctx->con ^ 1, ctx->fcur, a);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(ctx->io_host[buf], ctx->io_dev[buf], (size_t)(ns * comps) * sizeof(double),
+                            cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess) {
+            rc = fail(ARK_ERR_CUDA, "output pack failed");
+            break;
+        }
+        cudaEventRecord(ev[buf], ctx->st);
+        pending[buf] = Slab{k0, k1};
+    }
+    flush(buf ^ 1);
+    flush(buf);
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (close(fd) != 0) ok = false;
+    if (rc) return rc;
+    if (!ok) return fail(ARK_ERR_IO, std::string("write failed: ") + path);
+    return ARK_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int ark_write_vtk(ark_ctx *ctx, const char *path, int layout) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    const Block blocks[3] = {{"", 3, BK_U},
+                             {"\nscalars PC double\nLOOKUP_TABLE default\n", 1, BK_PC},
+                             {"\nVECTORS R double\n", 3, BK_R}};
+    return write_vtk_blocks(ctx, path, layout, blocks, 3, 1.0);
+}
+
+int ark_average_values(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (int rc = ensure_averages(ctx)) return rc;
+    ctx->eng->average_add(ctx->con ^ 1);
+    return launch_status(ctx);
+}
+
+int ark_set_averaging(ark_ctx *ctx, int on) {
+    if (int rc = check_ctx(ctx, false)) return rc;
+    if (on)
+        if (int rc = ensure_averages(ctx)) return rc;
+    if ((on != 0) != ctx->averaging) {
+        ARK_CUDA(cudaStreamSynchronize(ctx->st));
+        drop_graphs(ctx);
+        ctx->averaging = on != 0;
+    }
+    return ARK_OK;
+}
+
+int ark_write_average_vtk(ark_ctx *ctx, const char *path, double start_time, int layout) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (int rc = ensure_averages(ctx)) return rc;
+    DevScalars sc;
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ARK_CUDA(cudaMemcpy(&sc, ctx->eng->scalars(), sizeof sc, cudaMemcpyDeviceToHost));
+    const Block blocks[1] = {{"", 3, BK_AVG}};
+    return write_vtk_blocks(ctx, path, layout, blocks, 1, sc.time - start_time);
+}
+
+int ark_kinetic_energy(ark_ctx *ctx, double *energy) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!energy) return fail(ARK_ERR_PARAM, "energy is NULL");
+    const int np = energy_scratch_count(ctx->g);
+    double *scratch = nullptr;
+    ARK_CUDA(cudaMallocAsync((void **)&scratch, sizeof(double) * (np + 1), ctx->st));
+    ctx->eng->energy(ctx->con ^ 1, scratch + 1, scratch);
+    int rc = launch_status(ctx);
+    double sum = 0.0;
+    if (!rc && cudaMemcpyAsync(&sum, scratch, sizeof(double), cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess)
+        rc = fail(ARK_ERR_CUDA, "energy copy failed");
+    cudaFreeAsync(scratch, ctx->st);
+    if (!rc) ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    if (rc) return rc;
+    // allEnergy *= (x3_t - x3_b) * (x2_n - x2_s) * (x1_e - x1_w)  (main.cpp:2869-2870)
+    const double volume = ctx->P.lz * ctx->P.ly * ctx->P.lx;
+    *energy = sum * volume;
+    return ARK_OK;
+}
+
+int ark_write_energy(ark_ctx *ctx, const char *path) {
+    if (!path) return fail(ARK_ERR_PARAM, "path is NULL");
+    double e = 0.0;
+    if (int rc = ark_kinetic_energy(ctx, &e)) return rc;
+    DevScalars sc;
+    ARK_CUDA(cudaMemcpy(&sc, ctx->eng->scalars(), sizeof sc, cudaMemcpyDeviceToHost));
+    FILE *fd = std::fopen(path, "a");
+    if (!fd) return fail(ARK_ERR_IO, std::string("cannot open ") + path);
+    const bool ok = std::fprintf(fd, "(%f; %f) ", sc.time, e) > 0;
+    if (std::fclose(fd) != 0 || !ok) return fail(ARK_ERR_IO, std::string("write failed: ") + path);
+    return ARK_OK;
+}
+
+int ark_vorticity(ark_ctx *ctx, double *out) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!out) return fail(ARK_ERR_PARAM, "out is NULL");
+    const size_t n = (size_t)ctx->g.C1 * ctx->g.C2 * ctx->g.C3 * 3;
+    double *d = nullptr;
+    ARK_CUDA(cudaMallocAsync((void **)&d, sizeof(double) * n, ctx->st));
+    CellPack a;
+    std::memset(&a, 0, sizeof a);
+    a.r = d;
+    a.k0 = 1;
+    a.k1 = ctx->g.C3 + 1;
+    ctx->eng->pack(ctx->con ^ 1, ctx->fcur, a);
+    int rc = launch_status(ctx);
+    if (!rc && cudaMemcpyAsync(out, d, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess)
+        rc = fail(ARK_ERR_CUDA, "vorticity copy failed");
+    cudaFreeAsync(d, ctx->st);
+    if (!rc) ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    return rc;
 }
 
 } // extern "C"

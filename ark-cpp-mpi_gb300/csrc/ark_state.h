@@ -157,6 +157,34 @@ template <class T> struct Launch {
     static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);
 };
 
+// ---- output and statistics (ark_output.cu) ----
+// The reference's averageU arrays are (n1+1) x (n2+2) x (n3+1) = (C1+2) x (C2+3) x (C3+2)
+// (main.cpp:225-227): one j row more than the cell arrays.
+__host__ __device__ inline int64_t avg_index(const Geom &g, int i, int j, int k) {
+    return ((int64_t)k * (g.C2 + 3) + j) * (g.C1 + 2) + i;
+}
+__host__ __device__ inline int64_t avg_count(const Geom &g) { return (int64_t)(g.C1 + 2) * (g.C2 + 3) * (g.C3 + 2); }
+
+struct AvgArrays {
+    double *a[3];
+};
+
+// Cells of planes [k0, k1) (1-based) in file order, i fastest; a null pointer skips a field.
+// u, r: 3 doubles per cell; pc: 1; avg_out: 3 (avg[m] / avg_div).  swap: big-endian bytes.
+struct CellPack {
+    double *u, *pc, *r, *avg_out;
+    const double *avg[3];
+    double avg_div;
+    int k0, k1, swap;
+};
+
+template <class T> void output_pack(const DevState<T> &S, int ncon, int fcur, const CellPack &a, cudaStream_t st);
+template <class T> void output_average_add(const DevState<T> &S, int ncon, const AvgArrays &A, cudaStream_t st);
+// sum over interior cells of (u1^2 + u2^2 + u3^2)/2 of level ncon into *out (device), in a
+// fixed order; scratch holds energy_scratch_count(g) doubles
+int energy_scratch_count(const Geom &g);
+template <class T> void output_energy(const DevState<T> &S, int ncon, double *scratch, double *out, cudaStream_t st);
+
 // div_rn against the hardware division on n random operand pairs (mismatches added to *bad)
 void selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st);
 

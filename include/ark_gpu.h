@@ -36,7 +36,8 @@ enum ark_status {
     ARK_ERR_NONFINITE = 3,   /* a NaN or Inf reached the velocity field                    */
     ARK_ERR_STATE = 4,       /* call out of order (e.g. a step before ark_upload)          */
     ARK_ERR_NOMEM = 5,       /* device allocation failed                                   */
-    ARK_ERR_UNSUPPORTED = 6  /* a valid request this build does not implement              */
+    ARK_ERR_UNSUPPORTED = 6, /* a valid request this build does not implement              */
+    ARK_ERR_IO = 7           /* a file could not be opened or written                       */
 };
 
 enum ark_precision {
@@ -185,6 +186,46 @@ int ark_conservation_sums(ark_ctx *ctx, ark_sums *out);
  * y = -ly/2 and y = +ly/2 in StressTensor's one-sided wall form 2*VIS*u_c/dx2
  * (main.cpp:924-927).  Synchronous. */
 int ark_mean_profile(ark_ctx *ctx, double *mean_u1, double *wall_shear);
+
+/* ---- output and statistics ---------------------------------------------------------------
+ * VTK files as WriteDataParaView (main.cpp:2577-2745) and WriteAverageValues
+ * (main.cpp:2747-2849) write them: legacy binary rectilinear grid, node coordinates (i-1)*dx,
+ * cell data as big-endian doubles.  The data are packed on the device in file order and
+ * streamed to the file in k slabs.  The file is created or truncated.
+ *   ARK_VTK_FULL: every k plane at its place (the layout the file's header declares).
+ *   ARK_VTK_REFERENCE: byte for byte the reference's file.  Its row offsets carry no k term
+ *     (main.cpp:2670-2671, 2693-2694, 2737-2738, 2843-2844), so each k plane overwrites the
+ *     first plane's slot: the file holds the last plane (k = C3) at the start of each block,
+ *     zero bytes for the rest of the block, and ends after the last block's first plane.
+ *     Identical to ARK_VTK_FULL when n3_cells == 1 (the reference's own 2-D case). */
+typedef enum { ARK_VTK_FULL = 0, ARK_VTK_REFERENCE = 1 } ark_vtk_layout;
+
+/* WriteDataParaView: U = (u1, u2, u3) and "scalars PC" = density of the "nCon" level, and
+ * the vorticity R of the current face values (main.cpp:2716-2733).  The reference names the
+ * file <dirPath>out_<nStep>.vtk; here the caller passes the path.  Synchronous. */
+int ark_write_vtk(ark_ctx *ctx, const char *path, int layout);
+
+/* AverageValues (main.cpp:2878-2891): averageU_m += u_m(nCon) * dt over interior cells, dt
+ * of the last step.  The averages are FP64 device arrays in the reference's averageU layout
+ * ((n1_cells+2) x (n2_cells+3) x (n3_cells+2), one j row more than a cell array), zero until
+ * first used; ark_get_array / ark_put_array reach them as "averageU1".."averageU3". */
+int ark_average_values(ark_ctx *ctx);
+/* on != 0: every step of ark_step ends with AverageValues (inside the step's CUDA graph). */
+int ark_set_averaging(ark_ctx *ctx, int on);
+/* WriteAverageValues(start_time): averageU / (TIME - start_time) as the U vectors. */
+int ark_write_average_vtk(ark_ctx *ctx, const char *path, double start_time, int layout);
+
+/* WriteEnergy's value (main.cpp:2851-2870): the sum over interior cells of
+ * (u1^2 + u2^2 + u3^2)/2 of the "nCon" level, times the domain volume lz*ly*lx.  The sum
+ * is FP64 in a fixed tree order (deterministic; the reference's sequential order differs
+ * from it in the last bits).  Synchronous. */
+int ark_kinetic_energy(ark_ctx *ctx, double *energy);
+/* WriteEnergy: appends "(TIME; energy) " (printf "(%f; %f) ") to the file at path. */
+int ark_write_energy(ark_ctx *ctx, const char *path);
+
+/* The vorticity R of WriteDataParaView for every interior cell: out[3*n + m], n = (i-1) +
+ * n1_cells*((j-1) + n2_cells*(k-1)), host byte order.  Synchronous. */
+int ark_vorticity(ark_ctx *ctx, double *out);
 
 /* Self-check of the correctly rounded division by a run constant that the FP64 kernels use
  * (q = a*RN(1/b) plus two Markstein corrections) against the GPU's IEEE division, on n

@@ -286,6 +286,11 @@ class Reference:
             for fn in ("ref_get_dt", "ref_get_time", "ref_last_ub", "ref_last_g"):
                 getattr(L, fn).restype = ctypes.c_double
             L.ref_run.argtypes = [ctypes.c_int]
+            L.ref_write_paraview.argtypes = [ctypes.c_char_p]
+            L.ref_write_average.argtypes = [ctypes.c_char_p, ctypes.c_double]
+            L.ref_write_energy.argtypes = [ctypes.c_char_p]
+            L.ref_average_len.restype = ctypes.c_size_t
+            L.ref_get_average.argtypes = [ctypes.c_int, _dbl_p]
             cls._lib = L
         return cls._lib
 
@@ -376,3 +381,129 @@ class Reference:
     @property
     def last_g(self):
         return self.lib().ref_last_g()
+
+    # the reference's writers and statistics (dir must end in '/')
+    def write_paraview(self, dir_):
+        assert self.lib().ref_write_paraview(dir_.encode()) == 0
+
+    def average_values(self):
+        assert self.lib().ref_average_values() == 0
+
+    def write_average(self, dir_, start_time):
+        assert self.lib().ref_write_average(dir_.encode(), float(start_time)) == 0
+
+    def write_energy(self, dir_):
+        assert self.lib().ref_write_energy(dir_.encode()) == 0
+
+    def get_average(self, m):
+        out = np.empty((self.p["C3"] + 2, self.p["C2"] + 3, self.p["C1"] + 2))
+        assert self.lib().ref_get_average(int(m), _ptr(out)) == 0
+        return out
+
+
+# ---- writers and statistics, restated (numpy; host arrays in Arr3d layout [k, j, i]) ----
+
+def _vtk_head(p):
+    """Headers and coordinate blocks of WriteDataParaView / WriteAverageValues
+    (main.cpp:2585-2645, 2755-2812): node counts n_g = C + 1, coordinates (i-1)*dx."""
+    ng = (p["C1"] + 1, p["C2"] + 1, p["C3"] + 1)
+    dx = (p["lx"] / p["C1"], (0.5 * p["ly"] - (-0.5 * p["ly"])) / p["C2"], p["lz"] / p["C3"])
+    out = [b"# vtk DataFile Version 3.0\nvtk output\nBINARY\n",
+           f"DATASET RECTILINEAR_GRID\nDIMENSIONS {ng[0]} {ng[1]} {ng[2]}".encode()]
+    for name, n, d in zip("XYZ", ng, dx):
+        out.append(f"\n{name}_COORDINATES {n} double\n".encode())
+        out.append((np.arange(n, dtype=np.float64) * d).astype(">f8").tobytes())
+    cells = p["C1"] * p["C2"] * p["C3"]
+    out.append(f"\nCELL_DATA {cells}\nVECTORS U double\n".encode())
+    return b"".join(out)
+
+
+def _interior(a):
+    return a[1:-1, 1:-1, 1:-1]
+
+
+def vorticity(p, st):
+    """The R vectors of WriteDataParaView (main.cpp:2716-2733) from the face arrays:
+    shape (C3, C2, C1, 3)."""
+    C1, C2, C3 = p["C1"], p["C2"], p["C3"]
+    dx1, dx2, dx3 = p["lx"] / C1, (0.5 * p["ly"] - (-0.5 * p["ly"])) / C2, p["lz"] / C3
+    I = np.s_[1:C3 + 1, 1:C2 + 1, 1:C1 + 1]
+    Jp = np.s_[1:C3 + 1, 2:C2 + 2, 1:C1 + 1]
+    Kp = np.s_[2:C3 + 2, 1:C2 + 1, 1:C1 + 1]
+    Ip = np.s_[1:C3 + 1, 1:C2 + 1, 2:C1 + 2]
+    d2u3 = (st["u32"][Jp] - st["u32"][I]) / dx2
+    d3u2 = (st["u23"][Kp] - st["u23"][I]) / dx3
+    d3u1 = (st["u13"][Kp] - st["u13"][I]) / dx3
+    d1u3 = (st["u31"][Ip] - st["u31"][I]) / dx1
+    d1u2 = (st["u21"][Ip] - st["u21"][I]) / dx1
+    d2u1 = (st["u12"][Jp] - st["u12"][I]) / dx2
+    return np.stack([d2u3 - d3u2, d3u1 - d1u3, d1u2 - d2u1], axis=-1)
+
+
+def _place(parts, length):
+    buf = bytearray(length)
+    for off, b in parts:
+        buf[off:off + len(b)] = b
+    return bytes(buf)
+
+
+def _blocks(p, blocks, layout):
+    """Lay out a VTK file: the head, then for each (header, per-cell values of shape
+    (C3, C2, C1, m)) its header and its big-endian block.  layout "full": every k plane at
+    its place.  layout "reference": the reference's row offsets (main.cpp:2670-2671, 2693-2694,
+    2737-2738, 2843-2844) have no k term, so each k plane overwrites the first plane's slot and
+    only the last plane (k = C3) is in the file, at the start of its block; the rest of the
+    block is a hole (zero bytes) and the file ends after the last block's first plane."""
+    head = _vtk_head(p)
+    parts, off = [(0, head)], len(head)
+    end = off
+    for hdr, v in blocks:
+        if hdr:
+            parts.append((off, hdr))
+            off += len(hdr)
+        data = v.astype(">f8")
+        b = data.tobytes() if layout == "full" else data[-1].tobytes()
+        parts.append((off, b))
+        end = off + len(b)
+        off += data.nbytes
+    return _place(parts, end)
+
+
+def paraview_bytes(p, st, layout="full"):
+    """The bytes of WriteDataParaView's out_<nStep>.vtk (main.cpp:2577-2745) for the state
+    st (u?nCon, ronCon and the face arrays): big-endian doubles (needSwap, main.cpp:120)."""
+    u = np.stack([_interior(st[n]) for n in ("u1nCon", "u2nCon", "u3nCon")], axis=-1)
+    return _blocks(p, [(b"", u), (b"\nscalars PC double\nLOOKUP_TABLE default\n", _interior(st["ronCon"])[..., None]),
+                       (b"\nVECTORS R double\n", vorticity(p, st))], layout)
+
+
+def average_add(avg, st, dt):
+    """AverageValues (main.cpp:2878-2891): averageU_m += u_m nCon * dt over interior cells.
+    avg: three arrays in the averageU layout (C3+2, C2+3, C1+2)."""
+    for m, n in enumerate(("u1nCon", "u2nCon", "u3nCon")):
+        a = st[n]
+        avg[m][1:a.shape[0] - 1, 1:a.shape[1] - 1, 1:a.shape[2] - 1] += _interior(a) * dt
+
+
+def average_bytes(p, avg, time_now, start_time, layout="full"):
+    """The bytes of WriteAverageValues(start_time)'s average.vtk (main.cpp:2747-2849)."""
+    C1, C2, C3 = p["C1"], p["C2"], p["C3"]
+    v = np.stack([a[1:C3 + 1, 1:C2 + 1, 1:C1 + 1] / (time_now - start_time) for a in avg], axis=-1)
+    return _blocks(p, [(b"", v)], layout)
+
+
+def kinetic_energy_terms(st):
+    """The per-cell terms of WriteEnergy (main.cpp:2853-2860), in the reference's loop order
+    (i outer, then j, then k): (u1^2 + u2^2 + u3^2)/2 of the nCon level."""
+    u1, u2, u3 = (_interior(st[n]) for n in ("u1nCon", "u2nCon", "u3nCon"))
+    t = (u1 * u1 + u2 * u2 + u3 * u3) / 2
+    return np.transpose(t, (2, 1, 0)).ravel()
+
+
+def kinetic_energy(p, st):
+    """WriteEnergy's value: the terms summed in the reference's order, times the domain volume
+    (x3_t - x3_b) * (x2_n - x2_s) * (x1_e - x1_w) (main.cpp:2870)."""
+    e = 0.0
+    for t in kinetic_energy_terms(st).tolist():
+        e += t
+    return e * (p["lz"] * (0.5 * p["ly"] - (-0.5 * p["ly"])) * p["lx"])

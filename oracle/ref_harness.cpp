@@ -28,6 +28,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <mpi.h>
 
 #include "Arr3d.h"
@@ -52,6 +53,13 @@ extern bool x1Period, x2Period, x3Period, needSwap, useTecplot;
 extern int left, right, up, down, top, bottom, nproc, rank, px, py, pz, coordX, coordY, coordZ;
 extern int coords[3], dims[3];
 extern MPI_Comm newComm;
+extern const char *dirPath;
+/* the reference's output and statistics functions (main.cpp:2577-2891) */
+void WriteDataParaView();
+void WriteAverageValues(double time);
+void WriteEnergy();
+void AverageValues();
+
 
 /* ---- the reference's solver functions (main.cpp:12-21) ---- */
 void Input();
@@ -307,6 +315,63 @@ int ref_run(int nsteps) {
         UseForces();
         TIME += 0.5 * dt;
     }
+    return 0;
+}
+
+/* ---- output and statistics (the golden files of the writers) ----
+ * The reference writes as rank 0 of its decomposition, with coordX = coordZ = 0 in the row
+ * offsets of main.cpp:2670-2671; the harness keeps them at -1 on periodic axes only to keep
+ * the bounded-edge code of the step from firing, so they are 0 while a writer runs. */
+static std::string g_dir;
+
+struct WriterCoords {
+    int cx, cz;
+    WriterCoords() : cx(coordX), cz(coordZ) { coordX = 0; coordZ = 0; }
+    ~WriterCoords() { coordX = cx; coordZ = cz; }
+};
+
+/* WriteDataParaView (main.cpp:2577-2745): dir/out_<nStep>.vtk; dir ends in '/'. */
+int ref_write_paraview(const char *dir) {
+    if (!g_ready || !dir) return 1;
+    g_dir = dir;
+    dirPath = g_dir.c_str();
+    WriterCoords wc;
+    WriteDataParaView();
+    return 0;
+}
+
+/* AverageValues (main.cpp:2878-2891): averageU += u?nCon * dt. */
+int ref_average_values() {
+    if (!g_ready) return 1;
+    AverageValues();
+    return 0;
+}
+
+/* WriteAverageValues(start_time) (main.cpp:2747-2849): dir/average.vtk. */
+int ref_write_average(const char *dir, double start_time) {
+    if (!g_ready || !dir) return 1;
+    g_dir = dir;
+    dirPath = g_dir.c_str();
+    WriterCoords wc;
+    WriteAverageValues(start_time);
+    return 0;
+}
+
+/* WriteEnergy (main.cpp:2851-2876): appends "(TIME; energy) " to dir/energy.txt. */
+int ref_write_energy(const char *dir) {
+    if (!g_ready || !dir) return 1;
+    g_dir = dir;
+    dirPath = g_dir.c_str();
+    WriteEnergy();
+    return 0;
+}
+
+/* averageU1..3 (layout (n1+1) x (n2+2) x (n3+1), main.cpp:225-227). */
+size_t ref_average_len() { return g_ready ? (size_t)(n1 + 1) * (n2 + 2) * (n3 + 1) : 0; }
+int ref_get_average(int m, double *out) {
+    if (!g_ready || m < 1 || m > 3 || !out) return 1;
+    Arr3d *a = m == 1 ? averageU1 : m == 2 ? averageU2 : averageU3;
+    std::memcpy(out, a->ref(), sizeof(double) * ref_average_len());
     return 0;
 }
 

@@ -18,6 +18,12 @@ Files:
   stock_case.npz     the reference's own case, set up by its Input() and InitializeData()
                      (200x60x1 backward-facing step): the initial state and the interior
                      arrays after 40 steps
+  writers.npz        the files of the reference's writers (WriteDataParaView's out_5.vtk,
+                     WriteAverageValues' average.vtk, WriteEnergy's energy.txt) and its
+                     averageU arrays after 5 steps with AverageValues after each, for a 3-D
+                     10x6x4 grid and a 2-D 9x5x1 grid
+
+    python tests/golden/make_golden.py writers   # only writers.npz
 """
 from __future__ import annotations
 
@@ -25,6 +31,7 @@ import hashlib
 import json
 import os
 import sys
+import tempfile
 
 import numpy as np
 
@@ -67,8 +74,39 @@ def perturbed_state(p, seed):
     return st
 
 
+def writers():
+    """Section 6: the reference's writers on two grids (C3 > 1 shows its row offsets without
+    a k term; C3 = 1 is its own 2-D case)."""
+    out = {}
+    for tag, C, seed in (("3d", (10, 6, 4), 21), ("2d", (9, 5, 1), 22)):
+        p = oracle.channel_params(*C, seed=seed)
+        ref = oracle.Reference(p)
+        ref.load(oracle.channel_state(p))
+        for _ in range(5):
+            ref.run(1)
+            ref.average_values()
+        d = tempfile.mkdtemp(prefix="ark_golden_") + "/"
+        ref.write_paraview(d)
+        ref.write_average(d, 0.0)
+        ref.write_energy(d)
+        out[f"{tag}/params"] = json.dumps(p)
+        for name, fn in (("paraview", "out_5.vtk"), ("average", "average.vtk"), ("energy", "energy.txt")):
+            with open(d + fn, "rb") as f:
+                out[f"{tag}/{name}"] = np.frombuffer(f.read(), dtype=np.uint8)
+            os.remove(d + fn)
+        os.rmdir(d)
+        for m in (1, 2, 3):
+            out[f"{tag}/averageU{m}"] = ref.get_average(m)
+        out[f"{tag}/time"] = ref.time
+    np.savez_compressed(os.path.join(HERE, "writers.npz"), steps=5, **out)
+
+
 def main():
     assert oracle.Reference.available(), "build oracle/_ref first: make -C oracle ref"
+    if sys.argv[1:] == ["writers"]:
+        writers()
+        print("writers.npz written to", HERE)
+        return
     out = {}
 
     # 1. short forced run, full interior arrays
@@ -135,6 +173,9 @@ def main():
                     "l2": {n: float(np.linalg.norm(oracle.interior(n, ref.get(n)))) for n in CHECK}}
     with open(os.path.join(HERE, "digests.json"), "w") as f:
         json.dump(dig, f, indent=1, sort_keys=True)
+
+    # 6. the writers
+    writers()
     print("golden fixtures written to", HERE)
 
 

@@ -169,3 +169,31 @@ def test_port_matches_reference_stock_case(port):
     assert o.dt == float(g["dt"])
     for n in CELLS + list(port.FACE_NAMES):
         assert bits_equal(port.interior(n, o.get(n)), g[n]), n
+
+
+@pytest.mark.parametrize("tag", ["3d", "2d"])
+def test_writers_restated_match_reference_files(port, tag):
+    """The numpy restatement of WriteDataParaView / AverageValues / WriteAverageValues /
+    WriteEnergy against the files the reference wrote (tests/golden/writers.npz).  In 3-D the
+    reference's file keeps only the last k plane (its row offsets have no k term); in 2-D the
+    full layout and the reference's coincide."""
+    g = np.load(os.path.join(GOLD, "writers.npz"))
+    p = json.loads(str(g[f"{tag}/params"]))
+    o = port.Port(p)
+    o.load(port.channel_state(p))
+    avg = [np.zeros((p["C3"] + 2, p["C2"] + 3, p["C1"] + 2)) for _ in range(3)]
+    for _ in range(int(g["steps"])):
+        o.run(1)
+        port.average_add(avg, {n: o.get(n) for n in ("u1nCon", "u2nCon", "u3nCon")}, o.dt)
+    assert o.time == float(g[f"{tag}/time"])
+    for m in range(3):
+        assert bits_equal(avg[m], g[f"{tag}/averageU{m + 1}"]), m
+    st = {n: o.get(n) for n in ["u1nCon", "u2nCon", "u3nCon", "ronCon"] + list(port.FACE_NAMES)}
+    ref_vtk = g[f"{tag}/paraview"].tobytes()
+    assert port.paraview_bytes(p, st, "reference") == ref_vtk
+    assert port.average_bytes(p, avg, o.time, 0.0, "reference") == g[f"{tag}/average"].tobytes()
+    full = port.paraview_bytes(p, st, "full")
+    assert (full == ref_vtk) == (p["C3"] == 1)
+    assert len(full) >= len(ref_vtk)
+    text = "(%f; %f) " % (o.time, port.kinetic_energy(p, st))
+    assert text.encode() == g[f"{tag}/energy"].tobytes()
