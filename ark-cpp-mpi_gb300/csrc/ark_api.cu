@@ -55,17 +55,7 @@ const FieldRef kFields[] = {
     {"u23", &ark_host_state::u23, 1}, {"u33", &ark_host_state::u33, 1},
 };
 
-Geom make_geom(const ark_params &p) {
-    Geom g;
-    g.C1 = p.n1_cells;
-    g.C2 = p.n2_cells;
-    g.C3 = p.n3_cells;
-    g.cs1 = g.C1 + 2;
-    g.cs2 = (int64_t)(g.C1 + 2) * (g.C2 + 2);
-    g.fs1 = g.C1 + 3;
-    g.fs2 = (int64_t)(g.C1 + 3) * (g.C2 + 3);
-    return g;
-}
+Geom make_geom(const ark_params &p) { return device_geom(p.n1_cells, p.n2_cells, p.n3_cells); }
 
 template <class T> void fill_kt(const Consts &k, KT<T> &t) {
     for (int d = 0; d < 3; ++d) {
@@ -140,8 +130,8 @@ struct Engine {
     virtual int upload_field(int which, int face, const double *host) = 0;
     virtual int download_field(int which, int face, double *host) = 0;
     virtual void *field_ptr(const char *name, int *face) = 0;
-    virtual int download_raw(void *p, size_t n, double *host) = 0;
-    virtual int upload_raw(void *p, size_t n, const double *host) = 0;
+    virtual int download_raw(void *p, int face, double *host) = 0;
+    virtual int upload_raw(void *p, int face, const double *host) = 0;
     virtual void time_step_size(int con, int advance) = 0;
     virtual void reduce(int con) = 0;
     virtual void phase1(int src, int dst, int fcur, int mode) = 0;
@@ -266,27 +256,30 @@ template <class T> struct EngineT : Engine {
         return nullptr;
     }
 
-    // FP64: plain copies.  FP32: through the double staging buffer, density fields shifted
-    // by ro0 (the device holds rho - ro0).
-    int copy_in(T *dev, const double *host, size_t n, double offset) {
+    // Host arrays in the Arr3d layout <-> device arrays with padded rows.  FP64: pitched
+    // copies.  FP32: through the double staging buffer (same padded rows), density fields
+    // shifted by ro0 (the device holds rho - ro0).
+    size_t padded(int face) const { return face ? (size_t)S.g.nface() : (size_t)S.g.ncell(); }
+
+    int copy_in(T *dev, const double *host, int face, double offset) {
         if (sizeof(T) == sizeof(double)) {
-            ARK_CUDA(cudaMemcpy(dev, host, n * sizeof(double), cudaMemcpyHostToDevice));
+            ARK_CUDA(copy_rows(dev, host, S.g, face, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
         } else {
-            ARK_CUDA(cudaMemcpy(ctx->stage, host, n * sizeof(double), cudaMemcpyHostToDevice));
-            convert_from_double<T>(dev, ctx->stage, (int64_t)n, offset, ctx->st);
-            ARK_CUDA(cudaStreamSynchronize(ctx->st));
+            ARK_CUDA(copy_rows(ctx->stage, host, S.g, face, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+            convert_from_double<T>(dev, ctx->stage, (int64_t)padded(face), offset, ctx->st);
         }
+        ARK_CUDA(cudaStreamSynchronize(ctx->st));
         return ARK_OK;
     }
 
-    int copy_out(double *host, const T *dev, size_t n, double offset) {
+    int copy_out(double *host, const T *dev, int face, double offset) {
         if (sizeof(T) == sizeof(double)) {
-            ARK_CUDA(cudaMemcpy(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost));
+            ARK_CUDA(copy_rows(host, dev, S.g, face, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
         } else {
-            convert_to_double<T>(ctx->stage, dev, (int64_t)n, offset, ctx->st);
-            ARK_CUDA(cudaStreamSynchronize(ctx->st));
-            ARK_CUDA(cudaMemcpy(host, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost));
+            convert_to_double<T>(ctx->stage, dev, (int64_t)padded(face), offset, ctx->st);
+            ARK_CUDA(copy_rows(host, ctx->stage, S.g, face, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
         }
+        ARK_CUDA(cudaStreamSynchronize(ctx->st));
         return ARK_OK;
     }
 
@@ -294,27 +287,24 @@ template <class T> struct EngineT : Engine {
     static bool is_face_density(int which) { return which >= 9 && which < 24 && (which - 9) % 5 == 1; }
 
     int upload_field(int which, int face, const double *host) override {
-        const size_t n = face ? (size_t)S.g.nface() : (size_t)S.g.ncell();
         if (Storage<T>::deviation && is_face_density(which)) return ARK_OK; // derived from p
         const double off = (Storage<T>::deviation && is_cell_density(which)) ? ctx->P.ro0 : 0.0;
-        return copy_in(dev_of(which), host, n, off);
+        return copy_in(dev_of(which), host, face, off);
     }
     int download_field(int which, int face, double *host) override {
-        const size_t n = face ? (size_t)S.g.nface() : (size_t)S.g.ncell();
         if (Storage<T>::deviation && is_face_density(which)) {
             const int d = (which - 9) / 5;
-            face_density_to_double<T>(ctx->stage, S.fc[ctx->fcur][d].p, (int64_t)n, ctx->k.ro0, ctx->k.rc2, ctx->st);
+            face_density_to_double<T>(ctx->stage, S.fc[ctx->fcur][d].p, (int64_t)padded(1), ctx->k.ro0, ctx->k.rc2,
+                                      ctx->st);
+            ARK_CUDA(copy_rows(host, ctx->stage, S.g, 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
             ARK_CUDA(cudaStreamSynchronize(ctx->st));
-            ARK_CUDA(cudaMemcpy(host, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost));
             return ARK_OK;
         }
         const double off = (Storage<T>::deviation && is_cell_density(which)) ? ctx->P.ro0 : 0.0;
-        return copy_out(host, dev_of(which), n, off);
+        return copy_out(host, dev_of(which), face, off);
     }
-    int download_raw(void *p, size_t n, double *host) override {
-        return copy_out(host, (const T *)p, n, 0.0);
-    }
-    int upload_raw(void *p, size_t n, const double *host) override { return copy_in((T *)p, host, n, 0.0); }
+    int download_raw(void *p, int face, double *host) override { return copy_out(host, (const T *)p, face, 0.0); }
+    int upload_raw(void *p, int face, const double *host) override { return copy_in((T *)p, host, face, 0.0); }
 
     void *field_ptr(const char *name, int *face) override {
         for (int w = 0; w < 24; ++w)
@@ -406,8 +396,8 @@ template <class T> struct EngineT : Engine {
 int check_params(const ark_params *p) {
     if (!p) return fail(ARK_ERR_PARAM, "params is NULL");
     if (p->n1_cells < 1 || p->n2_cells < 1 || p->n3_cells < 1) return fail(ARK_ERR_PARAM, "need at least one cell per axis");
-    const double faces = (double)(p->n1_cells + 3) * (p->n2_cells + 3) * (p->n3_cells + 3);
-    if (faces >= 2147483647.0) return fail(ARK_ERR_PARAM, "grid too large: arrays are indexed with 32 bits");
+    const double faces = (double)device_pitch(p->n1_cells) * (p->n2_cells + 3) * (p->n3_cells + 3);
+    if (p->n1_cells > (1 << 28) || faces >= 2147483647.0) return fail(ARK_ERR_PARAM, "grid too large: arrays are indexed with 32 bits");
     if (!(p->lx > 0) || !(p->ly > 0) || !(p->lz > 0)) return fail(ARK_ERR_PARAM, "domain extents must be > 0");
     if (!(p->sound > 0) || !(p->ro0 > 0) || !(p->cfl > 0) || !(p->vis >= 0))
         return fail(ARK_ERR_PARAM, "sound, ro0, cfl must be > 0 and vis >= 0");
@@ -542,7 +532,8 @@ int ark_upload(ark_ctx *ctx, const ark_host_state *h) {
     }
     if (!h->condition) return ARK_OK; // keep the condition (and the scalars) of the last upload
     // condition: kept on the host for download, turned into flag bits on the device
-    const size_t nc = (size_t)ctx->g.ncell();
+    const Geom hg = host_geom(ctx->g.C1, ctx->g.C2, ctx->g.C3);
+    const size_t nc = (size_t)hg.ncell();
     ctx->cond_host.assign(h->condition, h->condition + nc);
     std::vector<uint8_t> fl(nc);
     long long nfluid = 0;
@@ -550,12 +541,12 @@ int ark_upload(ark_ctx *ctx, const ark_host_state *h) {
         const double v = h->condition[c];
         fl[c] = (uint8_t)((v < 0.5 ? FL_LT : 0) | (v > 0.5 ? FL_GT : 0) | (v == 0 ? FL_EQ0 : 0));
     }
-    const Geom &g = ctx->g;
-    for (int k = 1; k <= g.C3; ++k)
-        for (int j = 1; j <= g.C2; ++j)
-            for (int i = 1; i <= g.C1; ++i)
-                if (fl[(size_t)g.cell(i, j, k)] & FL_EQ0) ++nfluid;
-    ARK_CUDA(cudaMemcpy(ctx->eng->flags(), fl.data(), nc, cudaMemcpyHostToDevice));
+    for (int k = 1; k <= hg.C3; ++k)
+        for (int j = 1; j <= hg.C2; ++j)
+            for (int i = 1; i <= hg.C1; ++i)
+                if (fl[(size_t)hg.cell(i, j, k)] & FL_EQ0) ++nfluid;
+    ARK_CUDA(copy_rows(ctx->eng->flags(), fl.data(), ctx->g, 0, 1, cudaMemcpyHostToDevice, ctx->st));
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
     DevScalars sc;
     std::memset(&sc, 0, sizeof(sc));
     sc.nfluid = nfluid;
@@ -622,8 +613,7 @@ int ark_get_array(ark_ctx *ctx, const char *name, double *host) {
     int face = 0;
     void *p = ctx->eng->field_ptr(name, &face);
     if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
-    const size_t n = face ? (size_t)ctx->g.nface() : (size_t)ctx->g.ncell();
-    return ctx->eng->download_raw(p, n, host);
+    return ctx->eng->download_raw(p, face, host);
 }
 
 int ark_put_array(ark_ctx *ctx, const char *name, const double *host) {
@@ -642,8 +632,7 @@ int ark_put_array(ark_ctx *ctx, const char *name, const double *host) {
     int face = 0;
     void *p = ctx->eng->field_ptr(name, &face);
     if (!p) return fail(ARK_ERR_PARAM, std::string("no device array named ") + name);
-    const size_t n = face ? (size_t)ctx->g.nface() : (size_t)ctx->g.ncell();
-    return ctx->eng->upload_raw(p, n, host);
+    return ctx->eng->upload_raw(p, face, host);
 }
 
 int ark_time_step_size(ark_ctx *ctx) {

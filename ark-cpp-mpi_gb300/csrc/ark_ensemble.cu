@@ -177,17 +177,7 @@ template <class U> int ens_alloc(ark_ensemble *E, U **out, size_t n) {
     return ARK_OK;
 }
 
-Geom geom_of(const ark_params &p) {
-    Geom g;
-    g.C1 = p.n1_cells;
-    g.C2 = p.n2_cells;
-    g.C3 = p.n3_cells;
-    g.cs1 = g.C1 + 2;
-    g.cs2 = (int64_t)(g.C1 + 2) * (g.C2 + 2);
-    g.fs1 = g.C1 + 3;
-    g.fs2 = (int64_t)(g.C1 + 3) * (g.C2 + 3);
-    return g;
-}
+Geom geom_of(const ark_params &p) { return device_geom(p.n1_cells, p.n2_cells, p.n3_cells); }
 
 int alloc_member(ark_ensemble *E, DS &S) {
     const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
@@ -423,7 +413,8 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
             efail(ARK_ERR_PARAM, "bad member parameters (or members on different devices / forcing modes)");
             return nullptr;
         }
-        if ((double)(p.n1_cells + 3) * (p.n2_cells + 3) * (p.n3_cells + 3) >= 2147483647.0) {
+        if (p.n1_cells > (1 << 28) ||
+            (double)device_pitch(p.n1_cells) * (p.n2_cells + 3) * (p.n3_cells + 3) >= 2147483647.0) {
             efail(ARK_ERR_PARAM, "member grid too large for 32-bit indexing");
             return nullptr;
         }
@@ -505,7 +496,7 @@ int ark_ensemble_upload(ark_ensemble *E, int q, const ark_host_state *h) {
     float *dcell[8] = {S.lv[lc].ro, S.lv[lc].u1, S.lv[lc].u2, S.lv[lc].u3,
                        S.lv[ln].ro, S.lv[ln].u1, S.lv[ln].u2, S.lv[ln].u3};
     for (int a = 0; a < 8; ++a) {
-        ENS_CUDA(cudaMemcpy(E->stage, cells[a], nc * sizeof(double), cudaMemcpyHostToDevice));
+        ENS_CUDA(copy_rows(E->stage, cells[a], S.g, 0, sizeof(double), cudaMemcpyHostToDevice, E->st));
         convert_from_double<float>(dcell[a], E->stage, (int64_t)nc, (a % 4 == 0) ? ro0 : 0.0, E->st);
         ENS_CUDA(cudaStreamSynchronize(E->st));
     }
@@ -513,23 +504,26 @@ int ark_ensemble_upload(ark_ensemble *E, int q, const ark_host_state *h) {
         const FaceSet<float> &F = S.fc[E->fcur][d];
         float *df[4] = {F.p, F.u[0], F.u[1], F.u[2]};
         for (int a = 0; a < 4; ++a) {
-            ENS_CUDA(cudaMemcpy(E->stage, faces[d][a], nf * sizeof(double), cudaMemcpyHostToDevice));
+            ENS_CUDA(copy_rows(E->stage, faces[d][a], S.g, 1, sizeof(double), cudaMemcpyHostToDevice, E->st));
             convert_from_double<float>(df[a], E->stage, (int64_t)nf, 0.0, E->st);
             ENS_CUDA(cudaStreamSynchronize(E->st));
         }
     }
-    E->cond_host[q].assign(h->condition, h->condition + nc);
-    std::vector<uint8_t> fl(nc);
+    const Geom hg = host_geom(S.g.C1, S.g.C2, S.g.C3);
+    const size_t hnc = (size_t)hg.ncell();
+    E->cond_host[q].assign(h->condition, h->condition + hnc);
+    std::vector<uint8_t> fl(hnc);
     long long nfluid = 0;
-    for (size_t c = 0; c < nc; ++c) {
+    for (size_t c = 0; c < hnc; ++c) {
         const double v = h->condition[c];
         fl[c] = (uint8_t)((v < 0.5 ? FL_LT : 0) | (v > 0.5 ? FL_GT : 0) | (v == 0 ? FL_EQ0 : 0));
     }
-    for (int k = 1; k <= S.g.C3; ++k)
-        for (int j = 1; j <= S.g.C2; ++j)
-            for (int i = 1; i <= S.g.C1; ++i)
-                if (fl[(size_t)S.g.cell(i, j, k)] & FL_EQ0) ++nfluid;
-    ENS_CUDA(cudaMemcpy(S.flags, fl.data(), nc, cudaMemcpyHostToDevice));
+    for (int k = 1; k <= hg.C3; ++k)
+        for (int j = 1; j <= hg.C2; ++j)
+            for (int i = 1; i <= hg.C1; ++i)
+                if (fl[(size_t)hg.cell(i, j, k)] & FL_EQ0) ++nfluid;
+    ENS_CUDA(copy_rows(S.flags, fl.data(), S.g, 0, 1, cudaMemcpyHostToDevice, E->st));
+    ENS_CUDA(cudaStreamSynchronize(E->st));
     DevScalars sc;
     std::memset(&sc, 0, sizeof(sc));
     sc.nfluid = nfluid;
@@ -552,8 +546,8 @@ int ark_ensemble_download(ark_ensemble *E, int q, ark_host_state *h) {
     for (int a = 0; a < 8; ++a) {
         if (!cells[a]) continue;
         convert_to_double<float>(E->stage, dcell[a], (int64_t)nc, (a % 4 == 0) ? ro0 : 0.0, E->st);
+        ENS_CUDA(copy_rows(cells[a], E->stage, S.g, 0, sizeof(double), cudaMemcpyDeviceToHost, E->st));
         ENS_CUDA(cudaStreamSynchronize(E->st));
-        ENS_CUDA(cudaMemcpy(cells[a], E->stage, nc * sizeof(double), cudaMemcpyDeviceToHost));
     }
     double *faces[3][5] = {{h->p1, h->ro1, h->u11, h->u21, h->u31},
                            {h->p2, h->ro2, h->u12, h->u22, h->u32},
@@ -565,11 +559,11 @@ int ark_ensemble_download(ark_ensemble *E, int q, ark_host_state *h) {
             if (!faces[d][a]) continue;
             if (a == 1) face_density_to_double<float>(E->stage, F.p, (int64_t)nf, E->K[q].ro0, E->K[q].rc2, E->st);
             else convert_to_double<float>(E->stage, df[a], (int64_t)nf, 0.0, E->st);
+            ENS_CUDA(copy_rows(faces[d][a], E->stage, S.g, 1, sizeof(double), cudaMemcpyDeviceToHost, E->st));
             ENS_CUDA(cudaStreamSynchronize(E->st));
-            ENS_CUDA(cudaMemcpy(faces[d][a], E->stage, nf * sizeof(double), cudaMemcpyDeviceToHost));
         }
     }
-    if (h->condition) std::memcpy(h->condition, E->cond_host[q].data(), sizeof(double) * nc);
+    if (h->condition) std::memcpy(h->condition, E->cond_host[q].data(), sizeof(double) * E->cond_host[q].size());
     return ARK_OK;
 }
 

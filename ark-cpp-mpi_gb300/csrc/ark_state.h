@@ -34,6 +34,51 @@ struct Geom {
     __host__ __device__ int64_t nface() const { return fs2 * (C3 + 3); }
 };
 
+// The reference's Arr3d layout (source/Arr3d.cpp:19-21, i fastest): rows of C1+2 cells or
+// C1+3 faces.  Host arrays always have it.
+inline Geom host_geom(int C1, int C2, int C3) {
+    Geom g;
+    g.C1 = C1;
+    g.C2 = C2;
+    g.C3 = C3;
+    g.cs1 = C1 + 2;
+    g.cs2 = (int64_t)(C1 + 2) * (C2 + 2);
+    g.fs1 = C1 + 3;
+    g.fs2 = (int64_t)(C1 + 3) * (C2 + 3);
+    return g;
+}
+
+// Device arrays keep the same (i, j, k) indexing with every row padded to one pitch for cells
+// and faces: a multiple of 32 elements (rows start on 128-byte boundaries, as bulk copies need),
+// and long enough that the row segment a 64-cell tile stages (68 elements from x = 64*tile, or
+// 80 flag bytes) never leaves its row.
+constexpr int kRowAlign = 32;
+inline int device_pitch(int C1) {
+    const int need_seg = 64 * ((C1 + 63) / 64) + 16;
+    const int need = C1 + 3 > need_seg ? C1 + 3 : need_seg;
+    return (need + kRowAlign - 1) / kRowAlign * kRowAlign;
+}
+inline Geom device_geom(int C1, int C2, int C3) {
+    Geom g = host_geom(C1, C2, C3);
+    const int P = device_pitch(C1);
+    g.cs1 = P;
+    g.cs2 = (int64_t)P * (C2 + 2);
+    g.fs1 = P;
+    g.fs2 = (int64_t)P * (C2 + 3);
+    return g;
+}
+
+// One array between the host's Arr3d layout and the device's padded rows (rows of C1+2 cells
+// or C1+3 faces; elem bytes per element).  Asynchronous on st.
+inline cudaError_t copy_rows(void *dst, const void *src, const Geom &dg, int face, size_t elem, cudaMemcpyKind kind,
+                             cudaStream_t st) {
+    const size_t w = (size_t)(face ? dg.C1 + 3 : dg.C1 + 2) * elem;
+    const size_t rows = face ? (size_t)(dg.C2 + 3) * (dg.C3 + 3) : (size_t)(dg.C2 + 2) * (dg.C3 + 2);
+    const size_t dpitch = (size_t)(face ? dg.fs1 : dg.cs1) * elem;
+    if (kind == cudaMemcpyHostToDevice) return cudaMemcpy2DAsync(dst, dpitch, src, w, w, rows, kind, st);
+    return cudaMemcpy2DAsync(dst, w, src, dpitch, w, rows, kind, st);
+}
+
 // Tiling of the per-cell kernels: a block covers kTileX x kTileY cells of a k-column chunk
 // of kTileK planes and marches through it in k.  The reductions that TimeStepSize and the
 // bulk forcing need are taken per block into partial slots (one per block).

@@ -1,5 +1,6 @@
 """One rank of the CPU (gloo) check of bench.py's replica helpers; started by torchrun from
-tests/test_dist_replicas.py.  Prints one JSON line per rank."""
+tests/test_dist_replicas.py.  Each rank writes rank<r>.json into the folder given as the
+first argument (two ranks printing at once could interleave their lines)."""
 import json
 import os
 import sys
@@ -16,8 +17,9 @@ def main():
     # each rank's "time" differs; every rank must see the maximum
     got = bench.max_over_ranks(dist, 1.5 + rank)
     bench.barrier(dist)
-    print(json.dumps({"rank": rank, "world": world, "local": local, "max": got,
-                      "backend": dist.get_backend() if dist else None}), flush=True)
+    with open(os.path.join(sys.argv[1], f"rank{rank}.json"), "w") as f:
+        json.dump({"rank": rank, "world": world, "local": local, "max": got,
+                   "backend": dist.get_backend() if dist else None}, f)
     if dist is not None:
         dist.destroy_process_group()
 

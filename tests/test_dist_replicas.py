@@ -31,10 +31,13 @@ def json_lines(out):
     return [json.loads(l) for l in out.splitlines() if l.startswith("{")]
 
 
-def test_two_gloo_ranks_agree_on_max():
-    r = torchrun([os.path.join("tests", "dist_worker.py")])
+def test_two_gloo_ranks_agree_on_max(tmp_path):
+    r = torchrun([os.path.join("tests", "dist_worker.py"), str(tmp_path)])
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = sorted(json_lines(r.stdout), key=lambda d: d["rank"])
+    lines = []
+    for q in (0, 1):
+        with open(tmp_path / f"rank{q}.json") as f:
+            lines.append(json.load(f))
     assert [d["rank"] for d in lines] == [0, 1]
     assert all(d["world"] == 2 and d["backend"] == "gloo" for d in lines)
     assert all(d["max"] == 2.5 for d in lines)
