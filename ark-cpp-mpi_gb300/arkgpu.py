@@ -36,10 +36,17 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_ensemble_time_steps", "ark_ensemble_get_scalars", "ark_ensemble_mean_profile",
            "ark_ensemble_autotune", "ark_ensemble_set_shape", "ark_ensemble_kernel_times",
            "ark_write_vtk", "ark_average_values", "ark_set_averaging", "ark_write_average_vtk",
-           "ark_kinetic_energy", "ark_write_energy", "ark_vorticity")
+           "ark_kinetic_energy", "ark_write_energy", "ark_vorticity", "ark_selftest_staging")
 
 
 VTK_LAYOUTS = {"full": 0, "reference": 1}
+
+
+def staging_selftest(C1, C2, C3, planes_per_block=0):
+    """(problems, first message) of the staged Phase1's copy plan for a grid (host only)."""
+    buf = ctypes.create_string_buffer(512)
+    n = lib().ark_selftest_staging(int(C1), int(C2), int(C3), int(planes_per_block), buf, 512)
+    return n, buf.value.decode()
 
 
 class ArkError(RuntimeError):
@@ -124,6 +131,7 @@ def lib():
         L.ark_kinetic_energy.argtypes = [vp, _DP]
         L.ark_write_energy.argtypes = [vp, ctypes.c_char_p]
         L.ark_vorticity.argtypes = [vp, _DP]
+        L.ark_selftest_staging.argtypes = [ctypes.c_int] * 4 + [ctypes.c_char_p, ctypes.c_int]
         L.ark_ensemble_create.restype = vp
         L.ark_ensemble_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
         L.ark_ensemble_last_error.restype = ctypes.c_char_p

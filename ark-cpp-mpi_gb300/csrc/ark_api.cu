@@ -480,15 +480,19 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
             return nullptr;
         }
     }
-    // Phase1 kernel shapes measured fastest on GB300: FP32 marches the stress Phase1 in k
-    // (1.05 vs 1.27 ms at 512x256x256) and runs the second Phase1 one cell per thread (0.78 vs
-    // 0.93 ms); FP64 is ALU-bound and prefers one cell per thread for both (2.88 vs 2.98 ms).
-    ctx->march[0] = params->precision == ARK_FP32 ? 1 : 0;
-    ctx->march[1] = 0;
+    // Phase1 kernel shapes measured fastest on GB300: FP32 stages its planes in shared memory
+    // for both Phase1 launches (0.81 vs 1.13 ms marching and 0.64 vs 0.71 ms one cell per
+    // thread at 512x256x256); FP64 is ALU-bound and prefers one cell per thread for both
+    // (2.88 vs 2.98 ms marching).
+    ctx->march[0] = params->precision == ARK_FP32 ? 2 : 0;
+    ctx->march[1] = params->precision == ARK_FP32 ? 2 : 0;
     if (const char *e = std::getenv("ARK_PHASE1_MARCH")) { // "ab": a for Phase1 with stress, b without
-        if (e[0] == '0' || e[0] == '1') ctx->march[0] = e[0] - '0';
-        if (e[0] && (e[1] == '0' || e[1] == '1')) ctx->march[1] = e[1] - '0';
+        // 0: one cell per thread, 1: marching, 2: planes staged in shared memory (FP32 only)
+        const char top = params->precision == ARK_FP32 ? '2' : '1';
+        if (e[0] >= '0' && e[0] <= top) ctx->march[0] = e[0] - '0';
+        if (e[0] && e[1] >= '0' && e[1] <= top) ctx->march[1] = e[1] - '0';
     }
+    Launch<float>::prepare();
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
     *status = ARK_OK;

@@ -8,3 +8,175 @@ template void convert_from_double<float>(float *, const double *, int64_t, doubl
 template void convert_to_double<float>(double *, const float *, int64_t, double, cudaStream_t);
 template void face_density_to_double<float>(double *, const float *, int64_t, double, double, cudaStream_t);
 } // namespace ark
+
+// ---- host check of the staged Phase1's copy plan ----
+#include <cstdio>
+#include <string>
+#include <vector>
+
+namespace ark {
+namespace {
+
+// Fake array bases, 2^40 bytes apart: a byte's "address" tells its array and offset.
+constexpr long long kSpan = 1ll << 40;
+enum { A_CU = 0, A_CR = 3, A_FL = 4, A_FC = 5, A_FF = 17, A_N = 20 };
+
+template <int MODE> struct PlanCheck {
+    using L = stg::Layout<MODE>;
+    const Geom g;
+    long long size[A_N];
+    std::string err;
+    int bad = 0;
+
+    explicit PlanCheck(const Geom &gg) : g(gg) {
+        for (int a = 0; a < A_N; ++a) size[a] = g.ncell() * 4;
+        size[A_FL] = g.ncell();
+        for (int a = A_FC; a < A_FC + 12; ++a) size[a] = g.nface() * 4;
+    }
+    void fail(const char *what, int bx, int by, int p, long long x) {
+        if (bad++ == 0) {
+            char b[256];
+            std::snprintf(b, sizeof b, "mode %d tile (%d,%d) plane %d: %s (%lld)", MODE, bx, by, p, what, x);
+            err = b;
+        }
+    }
+    stg::Bases bases() const {
+        stg::Bases b;
+        for (int m = 0; m < 3; ++m) b.cu[m] = (const void *)((A_CU + m) * kSpan);
+        b.cr = (const void *)(A_CR * kSpan);
+        b.fl = (const void *)(A_FL * kSpan);
+        for (int d = 0; d < 3; ++d)
+            for (int a = 0; a < 4; ++a) b.fc[d][a] = (const void *)((A_FC + 4 * d + a) * kSpan);
+        for (int m = 0; m < 3; ++m) b.ff[m] = (const void *)((A_FF + m) * kSpan);
+        return b;
+    }
+    // expected "address" of element e (elements of elem bytes) of array a
+    static long long addr(int a, long long e, int elem) { return a * kSpan + e * elem; }
+
+    void run(int kch) {
+        const dim3 grid = stg::staged_grid(g, kch);
+        stg::Group G[stg::kMaxGroups];
+        const stg::Bases b = bases();
+        std::vector<std::vector<long long>> map;
+        for (int bz = 0; bz < (int)grid.z; ++bz)
+            for (int by = 0; by < (int)grid.y; ++by)
+                for (int bx = 0; bx < (int)grid.x; ++bx) {
+                    const int n = stg::build_groups<MODE>(G, g, b, bx, by);
+                    if (n > stg::kMaxGroups) fail("too many groups", bx, by, 0, n);
+                    const int k0 = bz * kch + 1, k1 = std::min(k0 + kch - 1, g.C3);
+                    stg::Row fr[stg::kMaxRows], gr[stg::kMaxFlagRows];
+                    int nfr = 0, ngr = 0;
+                    if (n <= stg::kMaxGroups) stg::expand_rows(G, n, fr, nfr, gr, ngr);
+                    if (nfr > stg::kMaxRows || ngr > stg::kMaxFlagRows) fail("too many rows", bx, by, 0, nfr);
+                    const int pfirst = L::STRESS ? k0 - 1 : k0, plast = k1 + 1;
+                    map.assign(plast - pfirst + 1, std::vector<long long>(L::STAGE, -1));
+                    for (int p = pfirst; p <= plast; ++p) {
+                        const unsigned kind = p < k0 ? stg::DOWN : (p > k1 ? stg::TOP : stg::MID);
+                        unsigned total = 0;
+                        std::vector<long long> &M = map[p - pfirst];
+                        for (int fg = 0; fg < 2; ++fg)
+                            for (int R = 0; R < (fg ? ngr : nfr); ++R) {
+                                const stg::Row &w = fg ? gr[R] : fr[R];
+                                if (!((w.dw >> 24) & kind)) continue;
+                                const int chunks = fg ? stg::kFlagChunks : stg::kChunks;
+                                for (int c = 0; c < chunks; ++c) {
+                                    const long long src = (long long)w.src + (long long)p * w.plane + 16 * c;
+                                    const long long dst = (w.dw & 0xFFFFFFu) + 16ll * c;
+                                    const int arr = (int)(src / kSpan);
+                                    const long long off = src % kSpan;
+                                    total += 16;
+                                    if (arr < 0 || arr >= A_N) {
+                                        fail("copy from no array", bx, by, p, src);
+                                        continue;
+                                    }
+                                    if (src % 16 || dst % 16) fail("unaligned copy", bx, by, p, src);
+                                    if (off < 0 || off + 16 > size[arr]) fail("copy outside its array", bx, by, p, off);
+                                    if (dst < 0 || dst + 16 > L::STAGE) fail("copy outside its stage", bx, by, p, dst);
+                                    for (int y = 0; y < 16 && dst + y < L::STAGE; ++y) {
+                                        if (M[dst + y] != -1) fail("two copies into one byte", bx, by, p, dst + y);
+                                        M[dst + y] = src + y;
+                                    }
+                                }
+                            }
+                        if (total != stg::plan_bytes(G, n, kind)) fail("byte count", bx, by, p, total);
+                    }
+                    for (int ty = 0; ty < stg::SY; ++ty)
+                        for (int tx = 0; tx < stg::SX; ++tx) {
+                            const int i = bx * stg::SX + tx + 1, j = by * stg::SY + ty + 1;
+                            if (i > g.C1 || j > g.C2) continue;
+                            for (int k = k0; k <= k1; ++k) reads(map, pfirst, bx, by, tx, ty, i, j, k);
+                        }
+                }
+    }
+    void want(const std::vector<std::vector<long long>> &map, int pfirst, int bx, int by, int p, int off_bytes,
+              int nbytes, long long expect) {
+        if (p - pfirst < 0 || p - pfirst >= (int)map.size()) {
+            fail("read of a plane not staged", bx, by, p, off_bytes);
+            return;
+        }
+        const std::vector<long long> &M = map[p - pfirst];
+        for (int y = 0; y < nbytes; ++y)
+            if (off_bytes + y >= L::STAGE || M[off_bytes + y] != expect + y) {
+                fail("shared-memory read maps to the wrong element", bx, by, p, off_bytes);
+                return;
+            }
+    }
+    void reads(const std::vector<std::vector<long long>> &map, int pfirst, int bx, int by, int tx, int ty, int i, int j,
+               int k) {
+        const int cr = ty - L::CROW0, cx = tx + 1;
+        auto cell = [&](int ii, int jj, int kk) { return g.cell(ii, jj, kk); };
+        auto face = [&](int ii, int jj, int kk) { return g.face(ii, jj, kk); };
+        want(map, pfirst, bx, by, k, stg::off_flag<MODE>(cr, cx), 1, addr(A_FL, cell(i, j, k), 1));
+        want(map, pfirst, bx, by, k, stg::off_cr<MODE>(ty, cx) * 4, 4, addr(A_CR, cell(i, j, k), 4));
+        for (int m = 0; m < 3; ++m) want(map, pfirst, bx, by, k, stg::off_cu<MODE>(m, cr, cx) * 4, 4, addr(A_CU + m, cell(i, j, k), 4));
+        for (int a = 0; a < 4; ++a) {
+            want(map, pfirst, bx, by, k, stg::off_face<MODE>(0, a, ty, cx) * 4, 4, addr(A_FC + a, face(i, j, k), 4));
+            want(map, pfirst, bx, by, k, stg::off_face<MODE>(0, a, ty, cx + 1) * 4, 4, addr(A_FC + a, face(i + 1, j, k), 4));
+            want(map, pfirst, bx, by, k, stg::off_face<MODE>(1, a, ty, cx) * 4, 4, addr(A_FC + 4 + a, face(i, j, k), 4));
+            want(map, pfirst, bx, by, k, stg::off_face<MODE>(1, a, ty + 1, cx) * 4, 4, addr(A_FC + 4 + a, face(i, j + 1, k), 4));
+            want(map, pfirst, bx, by, k, stg::off_face<MODE>(2, a, ty, cx) * 4, 4, addr(A_FC + 8 + a, face(i, j, k), 4));
+            want(map, pfirst, bx, by, k + 1, stg::off_face<MODE>(2, a, ty, cx) * 4, 4, addr(A_FC + 8 + a, face(i, j, k + 1), 4));
+        }
+        if (L::STRESS) {
+            const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
+            for (int q = 0; q < 4; ++q) {
+                want(map, pfirst, bx, by, k, stg::off_flag<MODE>(cr + dj[q], cx + di[q]), 1,
+                     addr(A_FL, cell(i + di[q], j + dj[q], k), 1));
+                for (int m = 0; m < 3; ++m)
+                    want(map, pfirst, bx, by, k, stg::off_cu<MODE>(m, cr + dj[q], cx + di[q]) * 4, 4,
+                         addr(A_CU + m, cell(i + di[q], j + dj[q], k), 4));
+            }
+            for (int dk = -1; dk <= 1; dk += 2) {
+                want(map, pfirst, bx, by, k + dk, stg::off_flag<MODE>(cr, cx), 1, addr(A_FL, cell(i, j, k + dk), 1));
+                for (int m = 0; m < 3; ++m)
+                    want(map, pfirst, bx, by, k + dk, stg::off_cu<MODE>(m, cr, cx) * 4, 4, addr(A_CU + m, cell(i, j, k + dk), 4));
+            }
+        }
+        if (L::FIN)
+            for (int m = 0; m < 3; ++m)
+                want(map, pfirst, bx, by, k, stg::off_ff<MODE>(m, ty, cx) * 4, 4, addr(A_FF + m, cell(i, j, k), 4));
+    }
+};
+
+} // namespace
+
+int staging_plan_check(int C1, int C2, int C3, int kch, char *msg, int cap) {
+    const Geom g = device_geom(C1, C2, C3);
+    if (kch <= 0) kch = stg::staged_chunk(g);
+    PlanCheck<P1_STRESS | P1_FORCES | P1_RMAX> a(g);
+    a.run(kch);
+    PlanCheck<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX> b(g);
+    b.run(kch);
+    PlanCheck<P1_FORCES | P1_RSUM> c(g);
+    c.run(kch);
+    const std::string &e = !a.err.empty() ? a.err : (!b.err.empty() ? b.err : c.err);
+    if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", e.c_str());
+    return a.bad + b.bad + c.bad;
+}
+
+} // namespace ark
+
+extern "C" int ark_selftest_staging(int n1_cells, int n2_cells, int n3_cells, int planes_per_block, char *msg, int cap) {
+    if (n1_cells < 1 || n2_cells < 1 || n3_cells < 1 || planes_per_block < 0) return -1;
+    return ark::staging_plan_check(n1_cells, n2_cells, n3_cells, planes_per_block, msg, cap);
+}

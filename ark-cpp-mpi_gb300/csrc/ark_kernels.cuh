@@ -21,6 +21,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "ark_state.h"
 
 namespace ark {
@@ -154,13 +156,13 @@ __device__ __forceinline__ BIx bix_here() {
 }
 
 // Block-wide combination of the per-thread partials into the block's slot.  Every thread of
-// the block must call it.
-template <class T>
+// the block (NT threads) must call it.
+template <class T, int NT = kTileX * kTileY>
 __device__ __forceinline__ void tile_store(const DevState<T> &S, const BIx &bx, bool do_max, bool do_sum,
                                            unsigned long long m0, unsigned long long m1, unsigned long long m2,
                                            long long s) {
-    __shared__ unsigned long long smax[3][kTileX * kTileY / 32];
-    __shared__ long long ssum[kTileX * kTileY / 32];
+    __shared__ unsigned long long smax[3][NT / 32];
+    __shared__ long long ssum[NT / 32];
     m0 = warp_max_u64(m0);
     m1 = warp_max_u64(m1);
     m2 = warp_max_u64(m2);
@@ -176,11 +178,11 @@ __device__ __forceinline__ void tile_store(const DevState<T> &S, const BIx &bx, 
     const int slot = bx.linear() % kBuckets;
     if (t < 3 && do_max) {
         unsigned long long m = 0;
-        for (int v = 0; v < kTileX * kTileY / 32; ++v) m = smax[t][v] > m ? smax[t][v] : m;
+        for (int v = 0; v < NT / 32; ++v) m = smax[t][v] > m ? smax[t][v] : m;
         if (m) atomicMax(&S.part_max[3 * slot + t], key_to_double_bits(m, T()));
     } else if (t == 3 && do_sum) {
         long long z = 0;
-        for (int v = 0; v < kTileX * kTileY / 32; ++v) z += ssum[v];
+        for (int v = 0; v < NT / 32; ++v) z += ssum[v];
         if (z) atomicAdd((unsigned long long *)&S.part_sum[slot], (unsigned long long)z);
     }
 }
@@ -1417,13 +1419,38 @@ template <class T, int MODE> struct CellK {
     }
 };
 
-// march = 1: k_phase1 (a block marches kTileK planes); 0: k_phase1_cell (one plane per block)
+#include "ark_staged.cuh"
+
+// march = 2: k_phase1_staged (FP32, the two Phase1 modes of a step; others fall back to the
+// one-cell kernel); 1: k_phase1 (a block marches kTileK planes); 0: k_phase1_cell
 template <class T>
 void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st) {
-    if (march)
+    if constexpr (std::is_same<T, float>::value) {
+        if (march == 2) {
+            switch (mode) {
+            case P1_STRESS | P1_FORCES | P1_RMAX:
+                stg::launch_staged<P1_STRESS | P1_FORCES | P1_RMAX>(S, src, dst, fcur, st);
+                return;
+            case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
+                stg::launch_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(S, src, dst, fcur, st);
+                return;
+            case P1_FORCES | P1_RSUM: stg::launch_staged<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st); return;
+            default: march = 0; break;
+            }
+        }
+    }
+    if (march == 1)
         launch_phase1<T, MarchK>(S, src, dst, fcur, mode, tile_grid(S.g), st);
     else
         launch_phase1<T, CellK>(S, src, dst, fcur, mode, dim3(tiles_x(S.g), tiles_y(S.g), S.g.C3), st);
+}
+
+template <class T> void Launch<T>::prepare() {
+    if constexpr (std::is_same<T, float>::value) {
+        stg::prepare_staged<P1_STRESS | P1_FORCES | P1_RMAX>();
+        stg::prepare_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>();
+        stg::prepare_staged<P1_FORCES | P1_RSUM>();
+    }
 }
 
 template <class T> void Launch<T>::stress(const DevState<T> &S, int con, int bulk, cudaStream_t st) {

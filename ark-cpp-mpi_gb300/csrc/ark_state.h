@@ -200,7 +200,16 @@ template <class T> struct Launch {
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
     static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);
+    // one-time launch attributes (the staged Phase1's shared memory); host only
+    static void prepare();
 };
+
+// Checks the staged Phase1's copy plan of a C1 x C2 x C3 grid with kch planes per block (0:
+// the launch's choice) on the host: every 16-byte copy in bounds, aligned, inside its stage,
+// and every shared-memory read of every thread mapped to the global element the one-cell
+// kernel reads.  Returns the number of problems
+// (a description of the first in msg).
+int staging_plan_check(int C1, int C2, int C3, int kch, char *msg, int cap);
 
 // ---- output and statistics (ark_output.cu) ----
 // The reference's averageU arrays are (n1+1) x (n2+2) x (n3+1) = (C1+2) x (C2+3) x (C3+2)

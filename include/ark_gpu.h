@@ -233,6 +233,14 @@ int ark_vorticity(ark_ctx *ctx, double *out);
  * Runs on the current device. */
 int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches);
 
+/* Host-only check (no GPU needed) of the copy plan of the FP32 Phase1 kernel that stages its
+ * planes in shared memory, for an n1 x n2 x n3-cell grid and planes_per_block planes per block
+ * (0: the kernel's own choice): every 16-byte copy inside its array and its stage and aligned,
+ * no two copies into one byte, and every shared-memory read of every thread mapped to the
+ * element the one-cell kernel reads.  Returns the number of problems (msg receives the first),
+ * or -1 for a bad size. */
+int ark_selftest_staging(int n1_cells, int n2_cells, int n3_cells, int planes_per_block, char *msg, int cap);
+
 /* ---- ensembles: many independent channels in one launch per phase ------------------------
  * The members (FP32 contexts, each with its own grid size and parameters, all on one device
  * and all with or all without bulk forcing) advance together: every phase of the step is one

@@ -27,7 +27,7 @@ def test_exports_every_declared_symbol(ark):
 
 def test_status_strings(ark):
     L = ark.lib()
-    for s in range(7):
+    for s in range(8):
         assert L.ark_status_string(s)
     assert L.ark_status_string(0) == b"ok"
 
@@ -90,3 +90,15 @@ def test_no_gpu_means_error_not_crash(ark):
     rc = ctypes.c_int(-1)
     assert not ark.lib().ark_create(ctypes.byref(p), ctypes.byref(rc))
     assert rc.value == 2
+
+
+@pytest.mark.parametrize("C", [(1, 1, 1), (5, 3, 2), (64, 4, 32), (65, 5, 33), (130, 9, 70), (200, 7, 31),
+                               (63, 12, 64), (17, 3, 1), (512, 8, 33), (96, 64, 64)])
+@pytest.mark.parametrize("kch", [0, 8, 32])
+def test_staged_phase1_copy_plan(ark, C, kch):
+    """The staged FP32 Phase1 copies row segments into shared memory 16 bytes at a time;
+    before it runs anywhere its copy plan is checked on the host: every copy inside its array
+    and stage and aligned, no byte copied twice, and every shared-memory read of every thread
+    mapped to the element the one-cell kernel reads."""
+    n, msg = ark.staging_selftest(*C, planes_per_block=kch)
+    assert n == 0, msg
