@@ -12,6 +12,7 @@ Translation units are compiled in parallel:
   ark_ensemble.cu batched ensembles: persistent kernels over a member table (--fmad=false)
   ark_output.cu   VTK packing, time averages, kinetic energy (--fmad=false: the averages and
                   the energy terms round as the reference's)
+  ark_closure.cu  learned eddy-viscosity closure: training data, network kernels, inference
   ark_host.cpp host-only helpers (seeded channel init)
 Outputs go to ark-cpp-mpi_gb300/lib/ (git-ignored).
 """
@@ -76,6 +77,7 @@ def build(force=False, verbose=False):
                          os.path.join(OBJ, "ark_ensemble.o")],
         [nv] + common + ["--fmad=false", "-c", os.path.join(SRC, "ark_output.cu"), "-o",
                          os.path.join(OBJ, "ark_output.o")],
+        [nv] + common + ["-c", os.path.join(SRC, "ark_closure.cu"), "-o", os.path.join(OBJ, "ark_closure.o")],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-c",
          os.path.join(SRC, "ark_host.cpp"), "-o", os.path.join(OBJ, "ark_host.o")],
         ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-c",
@@ -97,7 +99,7 @@ def build(force=False, verbose=False):
         msg = "\n".join(" ".join(c) + "\n" + o for c, o in failed)
         raise RuntimeError("build failed:\n" + msg)
     objs = [os.path.join(OBJ, n) for n in ("ark_fp64.o", "ark_fp32.o", "ark_api.o", "ark_noalloc.o", "ark_ensemble.o",
-                                           "ark_output.o", "ark_host.o")]
+                                           "ark_output.o", "ark_closure.o", "ark_host.o")]
     subprocess.run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static"], check=True)
     subprocess.run(["g++", "-o", RUN, os.path.join(OBJ, "ark_run.o"), "-L", OUT, "-lark_gb300",
                     "-Wl,-rpath,$ORIGIN"], check=True)

@@ -36,7 +36,11 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_ensemble_time_steps", "ark_ensemble_get_scalars", "ark_ensemble_mean_profile",
            "ark_ensemble_autotune", "ark_ensemble_set_shape", "ark_ensemble_kernel_times",
            "ark_write_vtk", "ark_average_values", "ark_set_averaging", "ark_write_average_vtk",
-           "ark_kinetic_energy", "ark_write_energy", "ark_vorticity", "ark_selftest_staging")
+           "ark_kinetic_energy", "ark_write_energy", "ark_vorticity", "ark_selftest_staging",
+           "ark_closure_last_error", "ark_closure_data_create", "ark_closure_data_destroy", "ark_closure_data_size",
+           "ark_closure_data_clear", "ark_closure_data_get", "ark_closure_data_append", "ark_closure_sample",
+           "ark_mlp_create", "ark_mlp_destroy", "ark_mlp_set", "ark_mlp_get", "ark_mlp_fit_normalization",
+           "ark_mlp_gradient", "ark_mlp_train", "ark_mlp_predict", "ark_set_closure")
 
 
 VTK_LAYOUTS = {"full": 0, "reference": 1}
@@ -89,7 +93,7 @@ def lib():
     global _lib
     if _lib is None:
         if not os.path.isfile(LIB_PATH):
-            raise FileNotFoundError(f"{LIB_PATH} missing: run ark-cpp-mpi_gb300/build.py")
+            raise FileNotFoundError(f"{LIB_PATH} missing: run ark-cpp-mpi_gb300/ark_build.py")
         L = ctypes.CDLL(LIB_PATH)
         vp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)
         L.ark_create.restype = vp
@@ -132,6 +136,27 @@ def lib():
         L.ark_write_energy.argtypes = [vp, ctypes.c_char_p]
         L.ark_vorticity.argtypes = [vp, _DP]
         L.ark_selftest_staging.argtypes = [ctypes.c_int] * 4 + [ctypes.c_char_p, ctypes.c_int]
+        ll, FP = ctypes.c_longlong, ctypes.POINTER(ctypes.c_float)
+        L.ark_closure_last_error.restype = ctypes.c_char_p
+        L.ark_closure_data_create.restype = vp
+        L.ark_closure_data_create.argtypes = [ll, ctypes.c_int, ip]
+        L.ark_closure_data_destroy.argtypes = [vp]
+        L.ark_closure_data_size.restype = ll
+        L.ark_closure_data_size.argtypes = [vp]
+        L.ark_closure_data_clear.argtypes = [vp]
+        L.ark_closure_data_get.argtypes = [vp, ll, ll, FP, FP]
+        L.ark_closure_data_append.argtypes = [vp, ll, FP, FP]
+        L.ark_closure_sample.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.ark_mlp_create.restype = vp
+        L.ark_mlp_create.argtypes = [ctypes.c_ulonglong, ctypes.c_int, ip]
+        L.ark_mlp_destroy.argtypes = [vp]
+        L.ark_mlp_set.argtypes = [vp, _DP, _DP, _DP]
+        L.ark_mlp_get.argtypes = [vp, _DP, _DP, _DP]
+        L.ark_mlp_fit_normalization.argtypes = [vp, vp]
+        L.ark_mlp_gradient.argtypes = [vp, vp, ll, ll, _DP, _DP]
+        L.ark_mlp_train.argtypes = [vp, vp, ctypes.c_int, ll, ctypes.c_double, _DP]
+        L.ark_mlp_predict.argtypes = [vp, vp, ll, ll, FP]
+        L.ark_set_closure.argtypes = [vp, vp, ctypes.c_double]
         L.ark_ensemble_create.restype = vp
         L.ark_ensemble_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
         L.ark_ensemble_last_error.restype = ctypes.c_char_p
@@ -287,7 +312,7 @@ class Context:
             self._call("ark_get_array", name.encode(), out.ctypes.data_as(_DP))
             return out
         if face is None:
-            face = not (name in CELL_FIELDS or name in ("f1", "f2", "f3"))
+            face = not (name in CELL_FIELDS or name in ("f1", "f2", "f3", "nut"))
         out = np.empty(self.fshape if face else self.cshape)
         self._call("ark_get_array", name.encode(), out.ctypes.data_as(_DP))
         return out
@@ -382,6 +407,13 @@ class Context:
     def write_energy(self, path):
         self._call("ark_write_energy", os.fsencode(path))
 
+    def set_closure(self, mlp, u_tau=0.0):
+        """Turn the learned closure on (mlp: an Mlp) or off (None) for ark_step."""
+        self._call("ark_set_closure", mlp.h if mlp is not None else None, float(u_tau))
+
+    def closure_sample(self, data, sx=4, sz=4, ox=0, oz=0, u_tau=1.0):
+        self._call("ark_closure_sample", data.h, int(sx), int(sz), int(ox), int(oz), float(u_tau))
+
     def vorticity(self):
         """(n3_cells, n2_cells, n1_cells, 3) array of the vorticity R of WriteDataParaView."""
         out = np.empty((self.p.n3_cells, self.p.n2_cells, self.p.n1_cells, 3))
@@ -465,3 +497,121 @@ class Ensemble:
 
     def set_shape(self, march_a, march_b, segment):
         self._call("ark_ensemble_set_shape", int(march_a), int(march_b), int(segment))
+
+
+# ---- learned closure ------------------------------------------------------------------------
+
+NIN, NH = 10, 32
+NPARAM = NH * NIN + NH + NH * NH + NH + NH + 1
+
+
+def _cl_check(fn, rc):
+    if rc != 0:
+        raise ArkError(fn, rc, lib().ark_closure_last_error().decode(errors="replace"))
+
+
+class ClosureData:
+    """Training samples (10 features, 1 target per row) on the device."""
+
+    def __init__(self, capacity, device=0):
+        rc = ctypes.c_int(0)
+        self.h = lib().ark_closure_data_create(int(capacity), int(device), ctypes.byref(rc))
+        if not self.h:
+            raise ArkError("ark_closure_data_create", rc.value or 2, lib().ark_closure_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ark_closure_data_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return int(lib().ark_closure_data_size(self.h))
+
+    def clear(self):
+        _cl_check("ark_closure_data_clear", lib().ark_closure_data_clear(self.h))
+
+    def get(self, first=0, count=None):
+        count = len(self) - first if count is None else count
+        f = np.empty((count, NIN), np.float32)
+        t = np.empty(count, np.float32)
+        _cl_check("ark_closure_data_get", lib().ark_closure_data_get(
+            self.h, int(first), int(count), f.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+            t.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return f, t
+
+    def append(self, features, targets):
+        f = np.ascontiguousarray(features, np.float32)
+        t = np.ascontiguousarray(targets, np.float32)
+        assert f.shape == (t.size, NIN)
+        _cl_check("ark_closure_data_append", lib().ark_closure_data_append(
+            self.h, int(t.size), f.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+            t.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+
+class Mlp:
+    """The closure network: BF16 working weights, FP32 master weights and Adam state."""
+
+    def __init__(self, seed=1, device=0):
+        rc = ctypes.c_int(0)
+        self.h = lib().ark_mlp_create(int(seed), int(device), ctypes.byref(rc))
+        if not self.h:
+            raise ArkError("ark_mlp_create", rc.value or 2, lib().ark_closure_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ark_mlp_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set(self, params, mu, sd):
+        p = np.ascontiguousarray(params, np.float64)
+        m = np.ascontiguousarray(mu, np.float64)
+        s = np.ascontiguousarray(sd, np.float64)
+        assert p.size == NPARAM and m.size == NIN and s.size == NIN
+        _cl_check("ark_mlp_set", lib().ark_mlp_set(self.h, p.ctypes.data_as(_DP), m.ctypes.data_as(_DP),
+                                                    s.ctypes.data_as(_DP)))
+
+    def get(self):
+        p, m, s = np.empty(NPARAM), np.empty(NIN), np.empty(NIN)
+        _cl_check("ark_mlp_get", lib().ark_mlp_get(self.h, p.ctypes.data_as(_DP), m.ctypes.data_as(_DP),
+                                                    s.ctypes.data_as(_DP)))
+        return p, m, s
+
+    def fit_normalization(self, data):
+        _cl_check("ark_mlp_fit_normalization", lib().ark_mlp_fit_normalization(self.h, data.h))
+
+    def gradient(self, data, first=0, count=None):
+        count = len(data) - first if count is None else count
+        g = np.empty(NPARAM)
+        loss = ctypes.c_double(0.0)
+        _cl_check("ark_mlp_gradient", lib().ark_mlp_gradient(self.h, data.h, int(first), int(count),
+                                                              g.ctypes.data_as(_DP), ctypes.byref(loss)))
+        return loss.value, g
+
+    def train(self, data, epochs=1, batch=4096, lr=1e-3):
+        loss = ctypes.c_double(0.0)
+        _cl_check("ark_mlp_train", lib().ark_mlp_train(self.h, data.h, int(epochs), int(batch), float(lr),
+                                                        ctypes.byref(loss)))
+        return loss.value
+
+    def predict(self, data, first=0, count=None):
+        count = len(data) - first if count is None else count
+        out = np.empty(count, np.float32)
+        _cl_check("ark_mlp_predict", lib().ark_mlp_predict(self.h, data.h, int(first), int(count),
+                                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out

@@ -143,6 +143,8 @@ struct Engine {
     virtual void sums(int ncon) = 0;
     virtual void mean_profile(int ncon, long long *acc) = 0;
     virtual void pack(int ncon, int fcur, const CellPack &a) = 0;
+    virtual int alloc_nut() = 0;
+    virtual void gather(int lvl, double *u0, double *u1, double *u2) = 0;
     virtual void average_add(int ncon) = 0;
     virtual void energy(int ncon, double *scratch, double *out) = 0;
     virtual DevScalars *scalars() = 0;
@@ -173,6 +175,8 @@ struct ark_ctx {
     double *stage = nullptr; // device double staging for FP32 contexts
     AvgArrays avg = {{nullptr, nullptr, nullptr}}; // averageU1..3 (FP64, reference layout)
     bool averaging = false;  // AverageValues at the end of every step
+    const void *closure_net = nullptr; // learned closure: the network's device constants
+    float closure_scale = 0.f;         // u_tau / vis for the y+ feature
     // output streaming: two device and two pinned host slab buffers of io_cap doubles
     double *io_dev[2] = {nullptr, nullptr};
     double *io_host[2] = {nullptr, nullptr};
@@ -312,6 +316,10 @@ template <class T> struct EngineT : Engine {
                 *face = kFields[w].face;
                 return dev_of(w);
             }
+        if (std::strcmp(name, "nut") == 0 && S.nut) {
+            *face = 0;
+            return S.nut;
+        }
         if (name[0] == 'f' && name[1] >= '1' && name[1] <= '3' && name[2] == 0) {
             *face = 0;
             return S.f[name[1] - '1'];
@@ -367,8 +375,12 @@ template <class T> struct EngineT : Engine {
         mark(0);
         Launch<T>::wrap_con(S, y, 1, st);
         mark(1);
-        Launch<T>::phase1(S, y, x, fcur, P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0),
-                          ctx->march[0], st);
+        int mode = P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0);
+        if (ctx->closure_net) { // the learned closure: nu_t of the level the stress reads
+            closure_nut<T>(S, y, ctx->closure_net, ctx->closure_scale, st);
+            mode |= P1_NUT;
+        }
+        Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st);
         mark(2);
         Launch<T>::wrap_phase2(S, y, fcur, st);
         mark(3);
@@ -387,6 +399,8 @@ template <class T> struct EngineT : Engine {
     void sums(int ncon) override { Launch<T>::sums(S, ncon, ctx->st); }
     void mean_profile(int ncon, long long *acc) override { Launch<T>::mean_profile(S, ncon, acc, ctx->st); }
     void pack(int ncon, int fcur, const CellPack &a) override { output_pack<T>(S, ncon, fcur, a, ctx->st); }
+    int alloc_nut() override { return S.nut ? ARK_OK : get(&S.nut, (size_t)S.g.ncell()); }
+    void gather(int lvl, double *u0, double *u1, double *u2) override { closure_gather<T>(S, lvl, u0, u1, u2, ctx->st); }
     void average_add(int ncon) override { output_average_add<T>(S, ncon, ctx->avg, ctx->st); }
     void energy(int ncon, double *scratch, double *out) override { output_energy<T>(S, ncon, scratch, out, ctx->st); }
     DevScalars *scalars() override { return S.sc; }
@@ -1092,6 +1106,41 @@ int write_vtk_blocks(ark_ctx *ctx, const char *path, int layout, const Block *bl
 } // namespace
 
 extern "C" {
+
+int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau) {
+    if (int rc = check_ctx(ctx, false)) return rc;
+    if (mlp && ctx->P.precision != ARK_FP32) return fail(ARK_ERR_UNSUPPORTED, "the learned closure runs in FP32 contexts");
+    if (mlp && !(u_tau > 0)) return fail(ARK_ERR_PARAM, "u_tau must be > 0");
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    if (mlp)
+        if (int rc = ctx->eng->alloc_nut()) return rc;
+    ctx->closure_net = mlp ? mlp_device_net(mlp) : nullptr;
+    ctx->closure_scale = mlp ? (float)(u_tau / ctx->P.vis) : 0.f;
+    drop_graphs(ctx);
+    return ARK_OK;
+}
+
+int ark_closure_sample(ark_ctx *ctx, ark_closure_data *data, int sx, int sz, int ox, int oz, double u_tau) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!data) return fail(ARK_ERR_PARAM, "dataset is NULL");
+    const Geom &g = ctx->g;
+    if (!ctx->P.periodic_x || !ctx->P.periodic_z) return fail(ARK_ERR_UNSUPPORTED, "closure samples need periodic x and z");
+    DevScalars sc;
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    ARK_CUDA(cudaMemcpy(&sc, ctx->eng->scalars(), sizeof sc, cudaMemcpyDeviceToHost));
+    if (sc.nfluid != (long long)g.C1 * g.C2 * g.C3) return fail(ARK_ERR_UNSUPPORTED, "closure samples need a channel without solids");
+    const long long count = closure_count(g.C1, g.C2, g.C3, sx, sz, ox, oz);
+    if (count < 0) return fail(ARK_ERR_PARAM, "bad sampling lattice");
+    if (count > closure_room(data)) return fail(ARK_ERR_PARAM, "dataset full");
+    double *u = nullptr;
+    const long long cells = (long long)g.C1 * g.C2 * g.C3;
+    if (int rc = closure_scratch(data, cells, &u)) return fail(rc, ark_closure_last_error());
+    ctx->eng->gather(ctx->con ^ 1, u, u + cells, u + 2 * cells);
+    if (int rc = closure_sample(data, g.C1, g.C2, g.C3, ctx->P.lx, ctx->P.ly, ctx->P.lz, ctx->P.vis, sx, sz, ox, oz, u_tau,
+                                ctx->st))
+        return fail(rc, ark_closure_last_error());
+    return ARK_OK;
+}
 
 int ark_write_vtk(ark_ctx *ctx, const char *path, int layout) {
     if (int rc = check_ctx(ctx, true)) return rc;

@@ -409,9 +409,10 @@ __device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const 
 // * ds_d * ro_c.  fln/un: flags and velocities of the six neighbours in the order
 // (i-1, i+1, j-1, j+1, k-1, k+1).  FP64 evaluates every face stress exactly as the reference
 // does; FP32 uses the equivalent coefficient form sigma = a_c u_c - a_w u_w per face.
+// nuf (FP32 only; nullptr: none): eddy viscosity per face in the same order, added to vis.
 template <class T>
 __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6][3], uint8_t fl, const T uc[3],
-                                             T ro_c, const K<T> &kk, T f[3]) {
+                                             T ro_c, const K<T> &kk, T f[3], const T *nuf = nullptr) {
     if (!Storage<T>::deviation) {
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
@@ -433,8 +434,9 @@ __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6]
                 const uint8_t fw = side ? fl : fln[2 * d], fc = side ? fln[2 * d + 1] : fl;
                 const bool wl = fw & FL_LT, wg = fw & FL_GT, cl = fc & FL_LT, cg = fc & FL_GT;
                 const int q = 2 * d + side;
-                aw[q] = (wl && cl) ? v : (wl && cg) ? (T)2 * v : (T)0;
-                ac[q] = (wl && cl) ? v : (wg && cl) ? (T)2 * v : (T)0;
+                const T vq = nuf ? v + nuf[q] * kk.rdx[d] : v;
+                aw[q] = (wl && cl) ? vq : (wl && cg) ? (T)2 * vq : (T)0;
+                ac[q] = (wl && cl) ? vq : (wg && cl) ? (T)2 * vq : (T)0;
             }
         }
 #pragma unroll
@@ -732,7 +734,16 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
                     un[q][2] = su3[nb[q]];
                 }
                 const T ro_cf = DEV ? kk.ro0 + ro_c : ro_c;
-                stress_force(fln, un, fl, uc, ro_cf, kk, f);
+                if (MODE & P1_NUT) {
+                    // eddy viscosity on each face: the mean of the two cells' nu_t
+                    const T nc = S.nut[c];
+                    T nuf[6];
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) nuf[q] = (T)0.5 * (nc + S.nut[nb[q]]);
+                    stress_force(fln, un, fl, uc, ro_cf, kk, f, nuf);
+                } else {
+                    stress_force(fln, un, fl, uc, ro_cf, kk, f);
+                }
                 if (MODE & P1_BULK) f[0] = f[0] + (ro_cf * kk.dvc) * sc_G<T>(S.sc);
             }
             S.f[0][c] = f[0];
@@ -1408,6 +1419,20 @@ void launch_phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, d
     default: break;
     }
 }
+// the learned-closure modes exist for the one-cell kernel only
+template <class T>
+void launch_phase1_nut(const DevState<T> &S, int src, int dst, int fcur, int mode, dim3 grid, cudaStream_t st) {
+    const dim3 block(kTileX, kTileY);
+    switch (mode) {
+    case P1_STRESS | P1_FORCES | P1_RMAX | P1_NUT:
+        k_phase1_cell<T, P1_STRESS | P1_FORCES | P1_RMAX | P1_NUT><<<grid, block, 0, st>>>(S, src, dst, fcur);
+        break;
+    case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX | P1_NUT:
+        k_phase1_cell<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX | P1_NUT><<<grid, block, 0, st>>>(S, src, dst, fcur);
+        break;
+    default: break;
+    }
+}
 template <class T, int MODE> struct MarchK {
     static void launch(dim3 g, dim3 b, cudaStream_t st, const DevState<T> &S, int src, int dst, int fcur) {
         k_phase1<T, MODE><<<g, b, 0, st>>>(S, src, dst, fcur);
@@ -1425,6 +1450,10 @@ template <class T, int MODE> struct CellK {
 // one-cell kernel); 1: k_phase1 (a block marches kTileK planes); 0: k_phase1_cell
 template <class T>
 void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st) {
+    if (mode & P1_NUT) {
+        launch_phase1_nut<T>(S, src, dst, fcur, mode, dim3(tiles_x(S.g), tiles_y(S.g), S.g.C3), st);
+        return;
+    }
     if constexpr (std::is_same<T, float>::value) {
         if (march == 2) {
             switch (mode) {

@@ -175,6 +175,7 @@ template <class T> struct DevState {
     // slot) and the fixed-point sum of u1 over fluid cells of the "nCon" level (1 per slot)
     unsigned long long *part_max;
     long long *part_sum;
+    T *nut; // eddy viscosity of the learned closure, cell layout (nullptr unless enabled)
 };
 
 // FP32 contexts store the density deviation rho - ro0 in the cell levels and derive face
@@ -186,7 +187,8 @@ template <> struct Storage<float> { static constexpr bool deviation = true; };
 // Launch entry points (defined per precision in ark_fp64.cu / ark_fp32.cu).
 // P1_RMAX / P1_RSUM: also take the dt partials (max |u| of the level written) or the bulk-flow
 // partials (sum of u1 of the level written) for the next step.
-enum Phase1Mode { P1_PLAIN = 0, P1_STRESS = 1, P1_FORCES = 2, P1_BULK = 4, P1_RMAX = 8, P1_RSUM = 16 };
+// P1_NUT: the stress uses vis + nu_t averaged to each face (learned closure; one-cell kernel).
+enum Phase1Mode { P1_PLAIN = 0, P1_STRESS = 1, P1_FORCES = 2, P1_BULK = 4, P1_RMAX = 8, P1_RSUM = 16, P1_NUT = 32 };
 
 template <class T> struct Launch {
     static void reduce_start(const DevState<T> &S, int con, cudaStream_t st);
@@ -239,6 +241,15 @@ template <class T> void output_average_add(const DevState<T> &S, int ncon, const
 int energy_scratch_count(const Geom &g);
 template <class T> void output_energy(const DevState<T> &S, int ncon, double *scratch, double *out, cudaStream_t st);
 
+// ---- learned closure (ark_closure.cu) ----
+// nu_t of level lvl into S.nut (interior cells and periodic ghost images); net: the network's
+// device constants (mlp_device_net); yplus_scale = u_tau / vis.
+template <class T> void closure_nut(const DevState<T> &S, int lvl, const void *net, float yplus_scale, cudaStream_t st);
+// the interior velocities of level lvl into three compact FP64 arrays
+template <class T> void closure_gather(const DevState<T> &S, int lvl, double *u0, double *u1, double *u2, cudaStream_t st);
+// samples of a C1 x C2 x C3 grid on the lattice (sx, sz, ox, oz), or -1 for a bad lattice
+long long closure_count(int C1, int C2, int C3, int sx, int sz, int ox, int oz);
+
 // div_rn against the hardware division on n random operand pairs (mismatches added to *bad)
 void selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st);
 
@@ -252,4 +263,14 @@ void convert_to_double(double *dst, const T *src, int64_t n, double offset, cuda
 template <class T>
 void face_density_to_double(double *dst, const T *p, int64_t n, double ro0, double rc2, cudaStream_t st);
 
+} // namespace ark
+
+struct ark_closure_data;
+struct ark_mlp;
+namespace ark {
+long long closure_room(const ark_closure_data *d);
+int closure_scratch(ark_closure_data *d, long long cells, double **u);
+int closure_sample(ark_closure_data *d, int C1, int C2, int C3, double lx, double ly, double lz, double vis, int sx,
+                   int sz, int ox, int oz, double u_tau, cudaStream_t ctx_st);
+const void *mlp_device_net(const ark_mlp *M);
 } // namespace ark

@@ -241,6 +241,50 @@ int ark_selftest_division(long long n, unsigned long long seed, long long *misma
  * or -1 for a bad size. */
 int ark_selftest_staging(int n1_cells, int n2_cells, int n3_cells, int planes_per_block, char *msg, int cap);
 
+/* ---- learned eddy-viscosity closure (a project extension; the reference has none) --------
+ * A network nu_t / nu = softplus(w3 . GELU(W2 GELU(W1 x_n + b1) + b2) + b3) (10 -> 32 -> 32 ->
+ * 1, BF16 weights, FP32 arithmetic) of 10 features of the local velocity gradient (the seven
+ * integrity-basis invariants of S and W as signed roots, the wall-frame shear -sgn(y) S_12 and
+ * vorticity -sgn(y) W_12, and y+ = (ly/2 - |y|) u_tau / vis), normalised x_n = (x - mu) / sd.
+ * Trained on 3 x 3 x 3 box-filtered fields of fine runs against the least-squares eddy
+ * viscosity of the filtered-out stress, max(0, -tau^d : S^d / (2 S^d : S^d)), by the library's
+ * own forward / backward kernels and Adam (FP32 master weights).  Parameters (1441, FP64 in
+ * these calls) are ordered W1[32][10], b1[32], W2[32][32], b2[32], w3[32], b3. */
+typedef struct ark_closure_data ark_closure_data; /* training samples on the device */
+typedef struct ark_mlp ark_mlp;                   /* the network and its optimiser state */
+
+const char *ark_closure_last_error(void);
+ark_closure_data *ark_closure_data_create(long long capacity, int device, int *status);
+int ark_closure_data_destroy(ark_closure_data *data);
+long long ark_closure_data_size(const ark_closure_data *data);
+int ark_closure_data_clear(ark_closure_data *data);
+/* rows [first, first + count): features (10 floats per row) and targets (nu* / nu) */
+int ark_closure_data_get(ark_closure_data *data, long long first, long long count, float *features, float *targets);
+int ark_closure_data_append(ark_closure_data *data, long long count, const float *features, const float *targets);
+/* Appends the samples of the context's "nCon" level: the interior velocities box-filtered
+ * 3 x 3 x 3 (x, z periodic; the walls reflect velocities), then on the lattice i = ox + sx*a,
+ * k = oz + sz*b (1-based i = 1 + ox + ..., every j) the features of the filtered field and the
+ * target.  FP32 or FP64 context of a periodic channel without interior solids. */
+int ark_closure_sample(ark_ctx *ctx, ark_closure_data *data, int sx, int sz, int ox, int oz, double u_tau);
+
+ark_mlp *ark_mlp_create(unsigned long long seed, int device, int *status);
+int ark_mlp_destroy(ark_mlp *mlp);
+int ark_mlp_set(ark_mlp *mlp, const double *params, const double *mu, const double *sd);
+int ark_mlp_get(ark_mlp *mlp, double *params, double *mu, double *sd);
+/* mu, sd of the dataset's features */
+int ark_mlp_fit_normalization(ark_mlp *mlp, ark_closure_data *data);
+/* gradient of the mean squared error over rows [first, first + count) (FP32 accumulation in a
+ * fixed order) and the error itself */
+int ark_mlp_gradient(ark_mlp *mlp, ark_closure_data *data, long long first, long long count, double *grad, double *loss);
+int ark_mlp_train(ark_mlp *mlp, ark_closure_data *data, int epochs, long long batch, double lr, double *loss);
+/* nu_t / nu of rows [first, first + count) */
+int ark_mlp_predict(ark_mlp *mlp, ark_closure_data *data, long long first, long long count, float *out);
+/* mlp != NULL: every ark_step of this FP32 context evaluates nu_t from the "Con" velocities
+ * before the stress and uses vis + (nu_t(c) + nu_t(neighbour))/2 on each face; the network is
+ * read at each step (train it further and the steps follow).  mlp == NULL: the plain step.
+ * The step pieces called one by one stay plain.  The array is readable as "nut". */
+int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
+
 /* ---- ensembles: many independent channels in one launch per phase ------------------------
  * The members (FP32 contexts, each with its own grid size and parameters, all on one device
  * and all with or all without bulk forcing) advance together: every phase of the step is one

@@ -197,3 +197,36 @@ def test_writers_restated_match_reference_files(port, tag):
     assert len(full) >= len(ref_vtk)
     text = "(%f; %f) " % (o.time, port.kinetic_energy(p, st))
     assert text.encode() == g[f"{tag}/energy"].tobytes()
+
+
+def test_closure_oracle_gradient_is_the_derivative():
+    """The numpy network's analytic gradient against central finite differences (FP64)."""
+    import oracle.closure as oc
+
+    rng = np.random.default_rng(5)
+    theta = rng.normal(0, 0.3, oc.NPARAM)
+    mu, sd = rng.normal(0, 1, oc.NIN), rng.uniform(0.5, 2.0, oc.NIN)
+    X = rng.normal(0, 1, (40, oc.NIN)) * sd + mu
+    t = rng.uniform(0, 3, 40)
+    loss, g = oc.loss_and_grad(theta, mu, sd, X, t)
+    idx = rng.choice(oc.NPARAM, 60, replace=False)
+    for p in idx:
+        e = np.zeros(oc.NPARAM)
+        e[p] = 1e-6
+        num = (oc.loss_and_grad(theta + e, mu, sd, X, t)[0] - oc.loss_and_grad(theta - e, mu, sd, X, t)[0]) / 2e-6
+        assert abs(num - g[p]) <= 1e-6 + 1e-5 * abs(g[p]), (p, num, g[p])
+    assert abs(loss - np.mean((oc.forward(theta, mu, sd, X) - t) ** 2)) < 1e-12
+
+
+def test_closure_oracle_filter_and_target_properties():
+    """The box filter keeps a constant interior field away from walls and the least-squares
+    target is zero for a uniform flow."""
+    import oracle.closure as oc
+
+    u = np.ones((6, 8, 10))
+    b = oc.box_filter(u, 1.0)
+    assert np.allclose(b, 1.0)
+    bv = oc.box_filter(u, -1.0)  # velocities reflect at the walls
+    assert np.allclose(bv[:, 2:-2, :], 1.0) and np.all(bv[:, 0, :] < 1.0)
+    nut, _ = oc.target([u, 0 * u, 0 * u], (0.1, 0.2, 0.3), 1e-3)
+    assert np.all(nut[:, 2:-2, :] == 0.0)
