@@ -40,7 +40,8 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_closure_last_error", "ark_closure_data_create", "ark_closure_data_destroy", "ark_closure_data_size",
            "ark_closure_data_clear", "ark_closure_data_get", "ark_closure_data_append", "ark_closure_sample",
            "ark_mlp_create", "ark_mlp_destroy", "ark_mlp_set", "ark_mlp_get", "ark_mlp_fit_normalization",
-           "ark_mlp_gradient", "ark_mlp_train", "ark_mlp_predict", "ark_set_closure")
+           "ark_mlp_gradient", "ark_mlp_train", "ark_mlp_predict", "ark_set_closure",
+           "ark_closure_data_filtered_stats", "ark_plane_stats")
 
 
 VTK_LAYOUTS = {"full": 0, "reference": 1}
@@ -157,6 +158,8 @@ def lib():
         L.ark_mlp_train.argtypes = [vp, vp, ctypes.c_int, ll, ctypes.c_double, _DP]
         L.ark_mlp_predict.argtypes = [vp, vp, ll, ll, FP]
         L.ark_set_closure.argtypes = [vp, vp, ctypes.c_double]
+        L.ark_closure_data_filtered_stats.argtypes = [vp, _DP]
+        L.ark_plane_stats.argtypes = [vp, _DP]
         L.ark_ensemble_create.restype = vp
         L.ark_ensemble_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
         L.ark_ensemble_last_error.restype = ctypes.c_char_p
@@ -413,6 +416,13 @@ class Context:
 
     def closure_sample(self, data, sx=4, sz=4, ox=0, oz=0, u_tau=1.0):
         self._call("ark_closure_sample", data.h, int(sx), int(sz), int(ox), int(oz), float(u_tau))
+        data._last_c2 = self.p.n2_cells
+
+    def plane_stats(self):
+        """(n2_cells, 9): per y plane the means of u1, u2, u3, u1^2, u2^2, u3^2, u1u2, u1u3, u2u3."""
+        out = np.empty((self.p.n2_cells, 9))
+        self._call("ark_plane_stats", out.ctypes.data_as(_DP))
+        return out
 
     def vorticity(self):
         """(n3_cells, n2_cells, n1_cells, 3) array of the vorticity R of WriteDataParaView."""
@@ -546,6 +556,12 @@ class ClosureData:
             self.h, int(first), int(count), f.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
             t.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
         return f, t
+
+    def filtered_stats(self):
+        """(n2_cells, 9) plane statistics of the field filtered by the last closure_sample."""
+        out = np.empty((self._last_c2, 9))
+        _cl_check("ark_closure_data_filtered_stats", lib().ark_closure_data_filtered_stats(self.h, out.ctypes.data_as(_DP)))
+        return out
 
     def append(self, features, targets):
         f = np.ascontiguousarray(features, np.float32)

@@ -144,6 +144,7 @@ struct Engine {
     virtual void mean_profile(int ncon, long long *acc) = 0;
     virtual void pack(int ncon, int fcur, const CellPack &a) = 0;
     virtual int alloc_nut() = 0;
+    virtual void plane_stats(int ncon, double *out) = 0;
     virtual void gather(int lvl, double *u0, double *u1, double *u2) = 0;
     virtual void average_add(int ncon) = 0;
     virtual void energy(int ncon, double *scratch, double *out) = 0;
@@ -400,6 +401,7 @@ template <class T> struct EngineT : Engine {
     void mean_profile(int ncon, long long *acc) override { Launch<T>::mean_profile(S, ncon, acc, ctx->st); }
     void pack(int ncon, int fcur, const CellPack &a) override { output_pack<T>(S, ncon, fcur, a, ctx->st); }
     int alloc_nut() override { return S.nut ? ARK_OK : get(&S.nut, (size_t)S.g.ncell()); }
+    void plane_stats(int ncon, double *out) override { output_plane_stats<T>(S, ncon, out, ctx->st); }
     void gather(int lvl, double *u0, double *u1, double *u2) override { closure_gather<T>(S, lvl, u0, u1, u2, ctx->st); }
     void average_add(int ncon) override { output_average_add<T>(S, ncon, ctx->avg, ctx->st); }
     void energy(int ncon, double *scratch, double *out) override { output_energy<T>(S, ncon, scratch, out, ctx->st); }
@@ -1211,6 +1213,21 @@ int ark_write_energy(ark_ctx *ctx, const char *path) {
     const bool ok = std::fprintf(fd, "(%f; %f) ", sc.time, e) > 0;
     if (std::fclose(fd) != 0 || !ok) return fail(ARK_ERR_IO, std::string("write failed: ") + path);
     return ARK_OK;
+}
+
+int ark_plane_stats(ark_ctx *ctx, double *out) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (!out) return fail(ARK_ERR_PARAM, "out is NULL");
+    const size_t n = 9 * (size_t)ctx->g.C2;
+    double *d = nullptr;
+    ARK_CUDA(cudaMallocAsync((void **)&d, sizeof(double) * n, ctx->st));
+    ctx->eng->plane_stats(ctx->con ^ 1, d);
+    int rc = launch_status(ctx);
+    if (!rc && cudaMemcpyAsync(out, d, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess)
+        rc = fail(ARK_ERR_CUDA, "plane statistics copy failed");
+    cudaFreeAsync(d, ctx->st);
+    if (!rc) ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    return rc;
 }
 
 int ark_vorticity(ark_ctx *ctx, double *out) {

@@ -235,6 +235,38 @@ __global__ void k_samples(SampleArgs s) {
     }
 }
 
+// Plane statistics of the filtered velocities (compact FP64 arrays): block j, the same nine
+// means as the context's plane statistics, fixed-order sums.
+__global__ void __launch_bounds__(256) k_plane_stats_compact(const double *u0, const double *u1, const double *u2, int C1,
+                                                             int C2, int C3, double *out) {
+    __shared__ double red[9][256];
+    const int j = blockIdx.x;
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int n = C1 * C3;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = t % C1, k = t / C1;
+        const size_t c = ((size_t)k * C2 + j) * C1 + i;
+        const double v1 = u0[c], v2 = u1[c], v3 = u2[c];
+        a[0] += v1;
+        a[1] += v2;
+        a[2] += v3;
+        a[3] += v1 * v1;
+        a[4] += v2 * v2;
+        a[5] += v3 * v3;
+        a[6] += v1 * v2;
+        a[7] += v1 * v3;
+        a[8] += v2 * v3;
+    }
+    for (int q = 0; q < 9; ++q) red[q][threadIdx.x] = a[q];
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int q = 0; q < 9; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x < 9) out[9 * j + threadIdx.x] = red[threadIdx.x][0] / (double)n;
+}
+
 // ---- training kernels ---------------------------------------------------------------------
 
 constexpr int TS = 128; // samples per tile (one per thread)
@@ -548,6 +580,7 @@ struct ark_closure_data {
     // FP64 filter scratch for the grid last sampled: 3 velocities, 6 products, 9 filtered, 1 temp
     double *scratch = nullptr;
     long long scratch_cells = 0;
+    int last[3] = {0, 0, 0}; // grid of the last filtered field (in the scratch)
 };
 
 struct ark_mlp {
@@ -612,6 +645,23 @@ int ark_closure_data_get(ark_closure_data *d, long long first, long long count, 
     CL_CUDA(cudaStreamSynchronize(d->st));
     if (features) CL_CUDA(cudaMemcpy(features, d->feat + first * cl::NIN, sizeof(float) * cl::NIN * count, cudaMemcpyDeviceToHost));
     if (targets) CL_CUDA(cudaMemcpy(targets, d->targ + first, sizeof(float) * count, cudaMemcpyDeviceToHost));
+    return ARK_OK;
+}
+
+int ark_closure_data_filtered_stats(ark_closure_data *d, double *out) {
+    if (!d || !out) return cfail(ARK_ERR_PARAM, "NULL argument");
+    const int C1 = d->last[0], C2 = d->last[1], C3 = d->last[2];
+    if (C1 < 1) return cfail(ARK_ERR_STATE, "no field has been sampled");
+    const long long cells = (long long)C1 * C2 * C3;
+    const double *ub = d->scratch + 9 * cells;
+    double *o = nullptr;
+    CL_CUDA(cudaMalloc(&o, sizeof(double) * 9 * C2));
+    cl::k_plane_stats_compact<<<C2, 256, 0, d->st>>>(ub, ub + cells, ub + 2 * cells, C1, C2, C3, o);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+    if (e == cudaSuccess) e = cudaMemcpy(out, o, sizeof(double) * 9 * C2, cudaMemcpyDeviceToHost);
+    cudaFree(o);
+    if (e != cudaSuccess) return cfail(ARK_ERR_CUDA, std::string("filtered statistics: ") + cudaGetErrorString(e));
     return ARK_OK;
 }
 
@@ -697,6 +747,9 @@ int closure_sample(ark_closure_data *d, int C1, int C2, int C3, double lx, doubl
     CL_CUDA(cudaGetLastError());
     CL_CUDA(cudaStreamSynchronize(d->st));
     d->n += count;
+    d->last[0] = C1;
+    d->last[1] = C2;
+    d->last[2] = C3;
     return ARK_OK;
 }
 } // namespace ark

@@ -115,6 +115,40 @@ __global__ void __launch_bounds__(1024) k_energy_total(const double *part, int n
     if (threadIdx.x == 0) *out = red[0];
 }
 
+// Plane statistics (one block per y plane, fixed-order sums): over the interior cells of plane
+// j of level ncon, the means of u1, u2, u3, u1^2, u2^2, u3^2, u1 u2, u1 u3, u2 u3 into
+// out[9*(j-1) + q].
+template <class T> __global__ void __launch_bounds__(256) k_plane_stats(const __grid_constant__ DevState<T> S, int ncon, double *out) {
+    __shared__ double red[9][256];
+    const Geom g = S.g;
+    const int j = blockIdx.x + 1;
+    const Level<T> L = S.lv[ncon];
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int n = g.C1 * g.C3;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = t % g.C1 + 1, k = t / g.C1 + 1;
+        const int64_t c = g.cell(i, j, k);
+        const double u1 = L.u1[c], u2 = L.u2[c], u3 = L.u3[c];
+        a[0] += u1;
+        a[1] += u2;
+        a[2] += u3;
+        a[3] += u1 * u1;
+        a[4] += u2 * u2;
+        a[5] += u3 * u3;
+        a[6] += u1 * u2;
+        a[7] += u1 * u3;
+        a[8] += u2 * u3;
+    }
+    for (int q = 0; q < 9; ++q) red[q][threadIdx.x] = a[q];
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int q = 0; q < 9; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x < 9) out[9 * (j - 1) + threadIdx.x] = red[threadIdx.x][0] / (double)n;
+}
+
 int grid_for(int64_t n) {
     const int64_t b = (n + 255) / 256;
     return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
@@ -139,6 +173,12 @@ template <class T> void output_energy(const DevState<T> &S, int ncon, double *sc
     k_energy_tiles<T><<<grid, dim3(kTileX, kTileY), 0, st>>>(S, ncon, scratch);
     k_energy_total<<<1, 1024, 0, st>>>(scratch, (int)(grid.x * grid.y), out);
 }
+
+template <class T> void output_plane_stats(const DevState<T> &S, int ncon, double *out, cudaStream_t st) {
+    k_plane_stats<T><<<S.g.C2, 256, 0, st>>>(S, ncon, out);
+}
+template void output_plane_stats<double>(const DevState<double> &, int, double *, cudaStream_t);
+template void output_plane_stats<float>(const DevState<float> &, int, double *, cudaStream_t);
 
 template void output_pack<double>(const DevState<double> &, int, int, const CellPack &, cudaStream_t);
 template void output_pack<float>(const DevState<float> &, int, int, const CellPack &, cudaStream_t);

@@ -239,6 +239,8 @@ template <class T> void output_average_add(const DevState<T> &S, int ncon, const
 // sum over interior cells of (u1^2 + u2^2 + u3^2)/2 of level ncon into *out (device), in a
 // fixed order; scratch holds energy_scratch_count(g) doubles
 int energy_scratch_count(const Geom &g);
+// per y plane of level ncon: means of u1, u2, u3, u1^2, u2^2, u3^2, u1u2, u1u3, u2u3 (9 * C2, device)
+template <class T> void output_plane_stats(const DevState<T> &S, int ncon, double *out, cudaStream_t st);
 template <class T> void output_energy(const DevState<T> &S, int ncon, double *scratch, double *out, cudaStream_t st);
 
 // ---- learned closure (ark_closure.cu) ----

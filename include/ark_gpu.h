@@ -223,6 +223,11 @@ int ark_kinetic_energy(ark_ctx *ctx, double *energy);
 /* WriteEnergy: appends "(TIME; energy) " (printf "(%f; %f) ") to the file at path. */
 int ark_write_energy(ark_ctx *ctx, const char *path);
 
+/* Per y plane of the "nCon" level: the means over the interior cells of the plane of u1, u2,
+ * u3, u1^2, u2^2, u3^2, u1u2, u1u3, u2u3 (out[9*(j-1) + q], 9 * n2_cells doubles): the mean
+ * profiles and, with the means, the Reynolds stresses.  Fixed-order FP64 sums.  Synchronous. */
+int ark_plane_stats(ark_ctx *ctx, double *out);
+
 /* The vorticity R of WriteDataParaView for every interior cell: out[3*n + m], n = (i-1) +
  * n1_cells*((j-1) + n2_cells*(k-1)), host byte order.  Synchronous. */
 int ark_vorticity(ark_ctx *ctx, double *out);
@@ -266,6 +271,9 @@ int ark_closure_data_append(ark_closure_data *data, long long count, const float
  * k = oz + sz*b (1-based i = 1 + ox + ..., every j) the features of the filtered field and the
  * target.  FP32 or FP64 context of a periodic channel without interior solids. */
 int ark_closure_sample(ark_ctx *ctx, ark_closure_data *data, int sx, int sz, int ox, int oz, double u_tau);
+/* Per y plane of the field filtered by the last ark_closure_sample: the means over x and z of
+ * u1, u2, u3, u1^2, u2^2, u3^2, u1u2, u1u3, u2u3 (out[9*(j-1) + q], 9 * n2_cells doubles). */
+int ark_closure_data_filtered_stats(ark_closure_data *data, double *out);
 
 ark_mlp *ark_mlp_create(unsigned long long seed, int device, int *status);
 int ark_mlp_destroy(ark_mlp *mlp);
