@@ -31,15 +31,30 @@ namespace ark {
 // scalar helpers
 // ---------------------------------------------------------------------------------------
 
-// min3d / max3d of main.cpp:2963-2973: ternaries, a NaN argument is skipped.
+// Ordered comparisons.  FP64 ones run on the integer pipe (GB300 issues FP64 instructions at a
+// small fraction of the integer rate): dkey maps a double to an int64 whose order is the IEEE
+// order, with -0 and +0 equal, so every comparison of non-NaN values gives the IEEE answer.
+// Only NaN orders differently (above everything); a NaN velocity has already raised the
+// non-finite status by then.
+__device__ __forceinline__ long long dkey(double x) {
+    const long long s = __double_as_longlong(x);
+    return s < 0 ? (s ^ 0x7FFFFFFFFFFFFFFFll) + 1 : s;
+}
+template <class T> __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+template <> __device__ __forceinline__ bool lt<double>(double a, double b) { return dkey(a) < dkey(b); }
+template <class T> __device__ __forceinline__ bool gt(T a, T b) { return lt(b, a); }
+template <class T> __device__ __forceinline__ bool ge0(T a) { return !lt(a, (T)0); }
+template <class T> __device__ __forceinline__ bool le0(T a) { return !lt((T)0, a); }
+
+// min3d / max3d of main.cpp:2963-2973: the same ternaries.
 template <class T> __device__ __forceinline__ T min3d(T x1, T x2, T x3) {
-    x1 = x1 > x2 ? x2 : x1;
-    x1 = x1 > x3 ? x3 : x1;
+    x1 = gt(x1, x2) ? x2 : x1;
+    x1 = gt(x1, x3) ? x3 : x1;
     return x1;
 }
 template <class T> __device__ __forceinline__ T max3d(T x1, T x2, T x3) {
-    x1 = x1 < x2 ? x2 : x1;
-    x1 = x1 < x3 ? x3 : x1;
+    x1 = lt(x1, x2) ? x2 : x1;
+    x1 = lt(x1, x3) ? x3 : x1;
     return x1;
 }
 
@@ -921,18 +936,18 @@ __device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T
     const T u3_max = max3d(u3_f, u3_c, u3_b) + q.dt * gu3;
     const T u3_min = min3d(u3_f, u3_c, u3_b) + q.dt * gu3;
 
-    if (r_fn > rmax) r_fn = rmax;
-    if (r_fn < rmin) r_fn = rmin;
-    if (q_bn > qmax) q_bn = qmax;
-    if (q_bn < qmin) q_bn = qmin;
-    if (u2_fn > u2_max) u2_fn = u2_max;
-    if (u2_fn < u2_min) u2_fn = u2_min;
-    if (u2_bn > u2_max) u2_bn = u2_max;
-    if (u2_bn < u2_min) u2_bn = u2_min;
-    if (u3_fn > u3_max) u3_fn = u3_max;
-    if (u3_fn < u3_min) u3_fn = u3_min;
-    if (u3_bn > u3_max) u3_bn = u3_max;
-    if (u3_bn < u3_min) u3_bn = u3_min;
+    if (gt(r_fn, rmax)) r_fn = rmax;
+    if (lt(r_fn, rmin)) r_fn = rmin;
+    if (gt(q_bn, qmax)) q_bn = qmax;
+    if (lt(q_bn, qmin)) q_bn = qmin;
+    if (gt(u2_fn, u2_max)) u2_fn = u2_max;
+    if (lt(u2_fn, u2_min)) u2_fn = u2_min;
+    if (gt(u2_bn, u2_max)) u2_bn = u2_max;
+    if (lt(u2_bn, u2_min)) u2_bn = u2_min;
+    if (gt(u3_fn, u3_max)) u3_fn = u3_max;
+    if (lt(u3_fn, u3_min)) u3_fn = u3_min;
+    if (gt(u3_bn, u3_max)) u3_bn = u3_max;
+    if (lt(u3_bn, u3_min)) u3_bn = u3_min;
     Ext<T> e;
     e.rf = r_fn;
     e.qb = q_bn;
@@ -976,14 +991,14 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
         un = (rn + qn) / (T)2;
         pn = (rn - qn) * q.sound * q.ro0 / (T)2;
         ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
-        if (ucf >= (T)0 && ucb >= (T)0) {
+        if (ge0(ucf) && ge0(ucb)) {
             ua = prev.af;
             ub = prev.bf;
-        } else if (ucf <= (T)0 && ucb <= (T)0) {
+        } else if (le0(ucf) && le0(ucb)) {
             ua = cur.ab;
             ub = cur.bb;
-        } else if (ucb >= (T)0 && ucf <= (T)0) {
-            if (ucb > -ucf) {
+        } else if (ge0(ucb) && le0(ucf)) {
+            if (gt(ucb, -ucf)) {
                 ua = prev.af;
                 ub = prev.bf;
             } else {
@@ -997,7 +1012,7 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
     } else {
         un = (T)0;
         if ((flb & FL_GT) && (flf & FL_LT)) {
-            if (ucf <= (T)0) {
+            if (le0(ucf)) {
                 const T qn = cur.qb;
                 pn = -qn * q.sound * q.ro0;
                 ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
@@ -1010,7 +1025,7 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
                 ub = N.nB[cf];
             }
         } else if ((flb & FL_LT) && (flf & FL_GT)) {
-            if (ucb >= (T)0) {
+            if (ge0(ucb)) {
                 const T rn = prev.rf;
                 pn = rn * q.sound * q.ro0;
                 ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
