@@ -41,7 +41,7 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_closure_data_clear", "ark_closure_data_get", "ark_closure_data_append", "ark_closure_sample",
            "ark_mlp_create", "ark_mlp_destroy", "ark_mlp_set", "ark_mlp_get", "ark_mlp_fit_normalization",
            "ark_mlp_gradient", "ark_mlp_train", "ark_mlp_predict", "ark_set_closure",
-           "ark_closure_data_filtered_stats", "ark_plane_stats")
+           "ark_closure_data_filtered_stats", "ark_plane_stats", "ark_autotune", "ark_mlp_predict_tc")
 
 
 VTK_LAYOUTS = {"full": 0, "reference": 1}
@@ -157,9 +157,11 @@ def lib():
         L.ark_mlp_gradient.argtypes = [vp, vp, ll, ll, _DP, _DP]
         L.ark_mlp_train.argtypes = [vp, vp, ctypes.c_int, ll, ctypes.c_double, _DP]
         L.ark_mlp_predict.argtypes = [vp, vp, ll, ll, FP]
+        L.ark_mlp_predict_tc.argtypes = [vp, vp, ll, ll, FP]
         L.ark_set_closure.argtypes = [vp, vp, ctypes.c_double]
         L.ark_closure_data_filtered_stats.argtypes = [vp, _DP]
         L.ark_plane_stats.argtypes = [vp, _DP]
+        L.ark_autotune.argtypes = [vp, ctypes.c_int, ip]
         L.ark_ensemble_create.restype = vp
         L.ark_ensemble_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
         L.ark_ensemble_last_error.restype = ctypes.c_char_p
@@ -410,6 +412,12 @@ class Context:
     def write_energy(self, path):
         self._call("ark_write_energy", os.fsencode(path))
 
+    def autotune(self, steps_per_candidate=3):
+        """Pick the fastest kernel shapes on the live state (which advances)."""
+        c = (ctypes.c_int * 4)()
+        self._call("ark_autotune", int(steps_per_candidate), c)
+        return {"phase1_stress": c[0], "phase1": c[1], "segment": c[2], "us_per_step": c[3]}
+
     def set_closure(self, mlp, u_tau=0.0):
         """Turn the learned closure on (mlp: an Mlp) or off (None) for ark_step."""
         self._call("ark_set_closure", mlp.h if mlp is not None else None, float(u_tau))
@@ -625,9 +633,10 @@ class Mlp:
                                                         ctypes.byref(loss)))
         return loss.value
 
-    def predict(self, data, first=0, count=None):
+    def predict(self, data, first=0, count=None, tensor_cores=False):
         count = len(data) - first if count is None else count
         out = np.empty(count, np.float32)
-        _cl_check("ark_mlp_predict", lib().ark_mlp_predict(self.h, data.h, int(first), int(count),
-                                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        fn = "ark_mlp_predict_tc" if tensor_cores else "ark_mlp_predict"
+        _cl_check(fn, getattr(lib(), fn)(self.h, data.h, int(first), int(count),
+                                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
         return out

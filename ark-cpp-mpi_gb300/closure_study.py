@@ -171,7 +171,11 @@ def main():
 
     pf = params(tuple(a.fine))
     fine = arkgpu.Context(pf)
-    fine.upload(streaks(pf, arkgpu.channel_init(pf, seed=a.seed, amp=0.1)))
+    st0 = streaks(pf, arkgpu.channel_init(pf, seed=a.seed, amp=0.1))
+    fine.upload(st0)
+    rep["fine_shapes"] = fine.autotune(3)  # then start again from the initial state
+    fine.upload(st0)
+    del st0
     hist = []
     chunk = max(1, a.spin // 30)
     done = 0
@@ -231,11 +235,14 @@ def main():
     del st
     pc = params(Cc)
     coarse = {}
+    stc = state_from_cells(pc, ro, uc)
     for mode in ("plain", "closure"):
         with arkgpu.Context(pc) as c:
-            c.upload(state_from_cells(pc, ro, uc))
             if mode == "closure":
                 c.set_closure(net, u_tau=u_tau)
+            c.upload(stc)
+            rep[f"coarse_shapes_{mode}"] = c.autotune(20)
+            c.upload(stc)
             c.step(2)
             c.sync()
             stats = Stats()

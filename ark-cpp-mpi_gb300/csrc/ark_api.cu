@@ -176,8 +176,11 @@ struct ark_ctx {
     double *stage = nullptr; // device double staging for FP32 contexts
     AvgArrays avg = {{nullptr, nullptr, nullptr}}; // averageU1..3 (FP64, reference layout)
     bool averaging = false;  // AverageValues at the end of every step
-    const void *closure_net = nullptr; // learned closure: the network's device constants
-    float closure_scale = 0.f;         // u_tau / vis for the y+ feature
+    void *closure_net = nullptr;          // learned closure: the network's constants (device copy)
+    cudaStream_t side = nullptr;          // the closure's branch of the step
+    cudaEvent_t fork = nullptr, join = nullptr;
+    float closure_scale = 0.f;            // u_tau / vis for the y+ feature
+    int seg_target = 32;                  // x2/x3 sweep segment length (faces)
     // output streaming: two device and two pinned host slab buffers of io_cap doubles
     double *io_dev[2] = {nullptr, nullptr};
     double *io_host[2] = {nullptr, nullptr};
@@ -361,7 +364,7 @@ template <class T> struct EngineT : Engine {
     void use_forces(int ncon) override { Launch<T>::use_forces(S, ncon, ctx->st); }
     void phase2(int con, int fcur) override {
         Launch<T>::wrap_phase2(S, con, fcur, ctx->st);
-        for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, con, fcur, ax, ctx->st);
+        for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, con, fcur, ax, ctx->st, ctx->seg_target);
     }
     // One full step of main.cpp:82-91 with "Con" = level x at entry and exit, reading the
     // dt / bulk-flow partials of the current state and leaving those of the next one.  With
@@ -372,21 +375,27 @@ template <class T> struct EngineT : Engine {
         auto mark = [&](int q) {
             if (ev) cudaEventRecord(ev[q], st);
         };
+        int mode = P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0);
+        if (ctx->closure_net) {
+            // the learned closure: nu_t of the level the stress reads, on a branch beside dt and
+            // the ghost fill (it reads only that level's interior and the flags)
+            cudaEventRecord(ctx->fork, st);
+            cudaStreamWaitEvent(ctx->side, ctx->fork, 0);
+            closure_nut<T>(S, y, ctx->closure_net, ctx->closure_scale, ctx->side);
+            cudaEventRecord(ctx->join, ctx->side);
+            mode |= P1_NUT;
+        }
         Launch<T>::finalize_dt(S, 1, st);
         mark(0);
         Launch<T>::wrap_con(S, y, 1, st);
         mark(1);
-        int mode = P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0);
-        if (ctx->closure_net) { // the learned closure: nu_t of the level the stress reads
-            closure_nut<T>(S, y, ctx->closure_net, ctx->closure_scale, st);
-            mode |= P1_NUT;
-        }
+        if (ctx->closure_net) cudaStreamWaitEvent(st, ctx->join, 0);
         Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st);
         mark(2);
         Launch<T>::wrap_phase2(S, y, fcur, st);
         mark(3);
         for (int ax = 0; ax < 3; ++ax) {
-            Launch<T>::sweep(S, y, fcur, ax, st);
+            Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target);
             mark(4 + ax);
         }
         Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
@@ -525,6 +534,13 @@ int ark_destroy(ark_ctx *ctx) {
     if (ctx->stage) cudaFree(ctx->stage);
     for (double *a : ctx->avg.a)
         if (a) cudaFree(a);
+    if (ctx->closure_net) cudaFree(ctx->closure_net);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->join) cudaEventDestroy(ctx->join);
     for (int b = 0; b < 2; ++b) {
         if (ctx->io_dev[b]) cudaFree(ctx->io_dev[b]);
         if (ctx->io_host[b]) cudaFreeHost(ctx->io_host[b]);
@@ -1109,6 +1125,55 @@ int write_vtk_blocks(ark_ctx *ctx, const char *path, int layout, const Block *bl
 
 extern "C" {
 
+// Times the candidate kernel shapes on the live state (results do not depend on the shape)
+// one setting at a time: the shape of the Phase1 with stress (one cell per thread, marching,
+// staged), then of the second Phase1, then the x2/x3 sweep segment (8, 16, 32, 64 faces).
+// choice (may be NULL): {shape 1, shape 2, segment, microseconds per step}.
+int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (steps_per_candidate < 1) return fail(ARK_ERR_PARAM, "steps_per_candidate < 1");
+    const int top = ctx->P.precision == ARK_FP32 ? 2 : 1;
+    auto measure = [&](double *us) -> int {
+        ARK_CUDA(cudaStreamSynchronize(ctx->st));
+        drop_graphs(ctx);
+        if (int rc = ark_step(ctx, 2)) return rc; // captures both face-generation graphs
+        double ms = 0.0;
+        if (int rc = ark_time_steps(ctx, steps_per_candidate, &ms)) return rc;
+        *us = 1000.0 * ms / steps_per_candidate;
+        return ARK_OK;
+    };
+    double best = 0.0;
+    if (int rc = measure(&best)) return rc;
+    for (int which = 0; which < 3; ++which) {
+        const int ncand = which < 2 ? top + 1 : 4;
+        const int segs[4] = {8, 16, 32, 64};
+        int keep = which < 2 ? ctx->march[which] : ctx->seg_target;
+        for (int c = 0; c < ncand; ++c) {
+            const int v = which < 2 ? c : segs[c];
+            if (v == keep) continue;
+            if (which < 2) ctx->march[which] = v;
+            else ctx->seg_target = v;
+            double us = 0.0;
+            if (int rc = measure(&us)) return rc;
+            if (us < best) {
+                best = us;
+                keep = v;
+            }
+        }
+        if (which < 2) ctx->march[which] = keep;
+        else ctx->seg_target = keep;
+    }
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
+    drop_graphs(ctx);
+    if (choice) {
+        choice[0] = ctx->march[0];
+        choice[1] = ctx->march[1];
+        choice[2] = ctx->seg_target;
+        choice[3] = (int)std::lround(best);
+    }
+    return ARK_OK;
+}
+
 int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau) {
     if (int rc = check_ctx(ctx, false)) return rc;
     if (mlp && ctx->P.precision != ARK_FP32) return fail(ARK_ERR_UNSUPPORTED, "the learned closure runs in FP32 contexts");
@@ -1116,7 +1181,23 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau) {
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
     if (mlp)
         if (int rc = ctx->eng->alloc_nut()) return rc;
-    ctx->closure_net = mlp ? mlp_device_net(mlp) : nullptr;
+    if (ctx->closure_net) {
+        cudaFree(ctx->closure_net);
+        ctx->closure_net = nullptr;
+    }
+    if (mlp && !ctx->side) {
+        ARK_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        ARK_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+        ARK_CUDA(cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming));
+    }
+    if (mlp) {
+        ARK_CUDA(cudaMalloc(&ctx->closure_net, mlp_bytes()));
+        if (mlp_snapshot_device(mlp, ctx->closure_net) != ARK_OK) {
+            cudaFree(ctx->closure_net);
+            ctx->closure_net = nullptr;
+            return fail(ARK_ERR_CUDA, "could not copy the network");
+        }
+    }
     ctx->closure_scale = mlp ? (float)(u_tau / ctx->P.vis) : 0.f;
     drop_graphs(ctx);
     return ARK_OK;

@@ -33,10 +33,21 @@ static_assert(O_B3 + 1 == NPARAM, "parameter layout");
 
 // ---- network ------------------------------------------------------------------------------
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form, z (1 + tanh(k0 (z + k1 z^3))) / 2, and its derivative (training:
+// accurate tanhf)
+constexpr float GK0 = 0.79788456080286536f, GK1 = 0.044715f;
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + tanhf(GK0 * (z + GK1 * z * z * z))); }
 __device__ __forceinline__ float gelu_grad(float z) {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
+    const float th = tanhf(GK0 * (z + GK1 * z * z * z));
+    return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * GK0 * (1.0f + 3.0f * GK1 * z * z);
 }
+// inference: the same form with the hardware tanh approximation (relative error below 2^-10)
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu_fast(float z) { return 0.5f * z * (1.0f + tanh_approx(GK0 * (z + GK1 * z * z * z))); }
 __device__ __forceinline__ float softplus(float z) { return fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z))); }
 __device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + expf(-z)); }
 
@@ -46,6 +57,28 @@ struct Net {
     float w[NPARAM];
     float mu[NIN], rsd[NIN];
 };
+
+// nu_t / nu of one normalised input, fully unrolled (with the parameters a kernel argument,
+// every multiply-add takes its weight from the constant bank)
+__device__ __forceinline__ float mlp_forward_unrolled(const float *w, const float xn[NIN]) {
+    float h1[NH];
+#pragma unroll
+    for (int k = 0; k < NH; ++k) {
+        float z = w[O_B1 + k];
+#pragma unroll
+        for (int i = 0; i < NIN; ++i) z += w[O_W1 + k * NIN + i] * xn[i];
+        h1[k] = gelu(z);
+    }
+    float z3 = w[O_B3];
+#pragma unroll
+    for (int k = 0; k < NH; ++k) {
+        float z = w[O_B2 + k];
+#pragma unroll
+        for (int m = 0; m < NH; ++m) z += w[O_W2 + k * NH + m] * h1[m];
+        z3 += w[O_W3 + k] * gelu(z);
+    }
+    return softplus(z3);
+}
 
 // nu_t / nu of one normalised input (w: the parameters, in shared memory)
 __device__ __forceinline__ float mlp_forward(const float *w, const float xn[NIN]) {
@@ -68,10 +101,126 @@ __device__ __forceinline__ float mlp_forward(const float *w, const float xn[NIN]
     return softplus(z3);
 }
 
+// ---- tensor-core inference ----------------------------------------------------------------
+// A warp evaluates 32 inputs at once with warp-level BF16 matrix multiply-accumulate
+// (m16n8k16, FP32 accumulation): layer 1 is [16 x 16] x [16 x 32] per half-warp tile (inputs
+// padded from 10 to 16), layer 2 [16 x 32] x [32 x 32]; the FP32 accumulator fragment of a
+// layer, after bias and GELU, is in exactly the register layout of the next layer's A fragment
+// (rows = inputs, columns = units), packed to BF16 pairs.  Layer 3 (32 -> 1) is a dot product
+// reduced over the four threads of a quad.  Activations enter the multiplies as BF16.
+
+__device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<unsigned *>(&v);
+}
+__device__ __forceinline__ void mma_bf16(float c[4], const unsigned a[4], unsigned b0, unsigned b1) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// The B fragments of a thread (lane = 4 g + t): layer 1 n-tile j: W1 rows 8j+g, inputs 2t, 2t+1
+// and 2t+8, 2t+9 (inputs >= 10 are zero); layer 2 n-tile j, k-step s: W2 row 8j+g, inputs
+// 16s+2t(+1), 16s+2t+8(+9).
+struct TcWeights {
+    unsigned b1[4][2], b2[4][2][2];
+};
+__device__ __forceinline__ TcWeights tc_weights(const float *w, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    TcWeights r;
+    auto w1 = [&](int n, int k) { return k < NIN ? w[O_W1 + n * NIN + k] : 0.f; };
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int n = 8 * j + g;
+        r.b1[j][0] = pack_bf16(w1(n, 2 * t), w1(n, 2 * t + 1));
+        r.b1[j][1] = pack_bf16(w1(n, 2 * t + 8), w1(n, 2 * t + 9));
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            r.b2[j][s][0] = pack_bf16(w[O_W2 + n * NH + 16 * s + 2 * t], w[O_W2 + n * NH + 16 * s + 2 * t + 1]);
+            r.b2[j][s][1] = pack_bf16(w[O_W2 + n * NH + 16 * s + 2 * t + 8], w[O_W2 + n * NH + 16 * s + 2 * t + 9]);
+        }
+    }
+    return r;
+}
+
+// nu_t / nu of the 16 inputs of one m16 tile, whose normalised features (BF16, 16 per row, the
+// last 6 zero) are rows X[0..15] in shared memory; out[0] gets row g, out[1] row g + 8 (every
+// thread of the quad holds both).
+__device__ __forceinline__ void tc_tile(const float *w, const TcWeights &B, const __nv_bfloat16 *X, int lane, float out[2]) {
+    const int g = lane >> 2, t = lane & 3;
+    const unsigned *Xw = reinterpret_cast<const unsigned *>(X); // 8 words per row
+    unsigned a[4];
+    a[0] = Xw[g * 8 + t];
+    a[1] = Xw[(g + 8) * 8 + t];
+    a[2] = Xw[g * 8 + 4 + t];
+    a[3] = Xw[(g + 8) * 8 + 4 + t];
+    float h[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_bf16(c, a, B.b1[j][0], B.b1[j][1]);
+        const float bl = w[O_B1 + 8 * j + 2 * t], bh = w[O_B1 + 8 * j + 2 * t + 1];
+        h[j][0] = gelu_fast(c[0] + bl);
+        h[j][1] = gelu_fast(c[1] + bh);
+        h[j][2] = gelu_fast(c[2] + bl);
+        h[j][3] = gelu_fast(c[3] + bh);
+    }
+    unsigned a2[2][4];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        a2[s][0] = pack_bf16(h[2 * s][0], h[2 * s][1]);
+        a2[s][1] = pack_bf16(h[2 * s][2], h[2 * s][3]);
+        a2[s][2] = pack_bf16(h[2 * s + 1][0], h[2 * s + 1][1]);
+        a2[s][3] = pack_bf16(h[2 * s + 1][2], h[2 * s + 1][3]);
+    }
+    float z_lo = 0.f, z_hi = 0.f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_bf16(c, a2[0], B.b2[j][0][0], B.b2[j][0][1]);
+        mma_bf16(c, a2[1], B.b2[j][1][0], B.b2[j][1][1]);
+        const int n = 8 * j + 2 * t;
+        const float bl = w[O_B2 + n], bh = w[O_B2 + n + 1], wl = w[O_W3 + n], wh = w[O_W3 + n + 1];
+        z_lo += gelu_fast(c[0] + bl) * wl + gelu_fast(c[1] + bh) * wh;
+        z_hi += gelu_fast(c[2] + bl) * wl + gelu_fast(c[3] + bh) * wh;
+    }
+    z_lo += __shfl_xor_sync(0xffffffffu, z_lo, 1);
+    z_lo += __shfl_xor_sync(0xffffffffu, z_lo, 2);
+    z_hi += __shfl_xor_sync(0xffffffffu, z_hi, 1);
+    z_hi += __shfl_xor_sync(0xffffffffu, z_hi, 2);
+    out[0] = softplus(z_lo + w[O_B3]);
+    out[1] = softplus(z_hi + w[O_B3]);
+}
+
+// A warp's 32 inputs: this lane's normalised features x into row `lane` of the warp's X (32
+// rows of 16 BF16), then both m16 tiles; returns nu_t / nu of this lane's input.
+__device__ __forceinline__ float tc_warp(const float *w, const TcWeights &B, __nv_bfloat16 *X, const float x[NIN], int lane) {
+    unsigned *row = reinterpret_cast<unsigned *>(X + lane * 16);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) row[q] = pack_bf16(x[2 * q], x[2 * q + 1]);
+    row[5] = row[6] = row[7] = 0u;
+    __syncwarp();
+    float o0[2], o1[2];
+    tc_tile(w, B, X, lane, o0);
+    tc_tile(w, B, X + 16 * 16, lane, o1);
+    __syncwarp();
+    // row r of tile m: held by every thread of quad (r mod 8); hand each lane its own row
+    const int src = (lane & 7) * 4;
+    const float a0 = __shfl_sync(0xffffffffu, o0[0], src), a1 = __shfl_sync(0xffffffffu, o0[1], src);
+    const float b0 = __shfl_sync(0xffffffffu, o1[0], src), b1 = __shfl_sync(0xffffffffu, o1[1], src);
+    return lane < 8 ? a0 : lane < 16 ? a1 : lane < 24 ? b0 : b1;
+}
+
 // ---- features -----------------------------------------------------------------------------
 
-__device__ __forceinline__ float sroot(float x, float p) { return copysignf(powf(fabsf(x), p), x); }
-__device__ __forceinline__ double sroot(double x, double p) { return copysign(pow(fabs(x), p), x); }
+// signed roots x^(1/3), x^(1/4), x^(1/6) of |x| with the sign of x
+__device__ __forceinline__ float sroot3(float x) { return cbrtf(x); }
+__device__ __forceinline__ float sroot4(float x) { return copysignf(sqrtf(sqrtf(fabsf(x))), x); }
+__device__ __forceinline__ float sroot6(float x) { return copysignf(cbrtf(sqrtf(fabsf(x))), x); }
+__device__ __forceinline__ double sroot3(double x) { return cbrt(x); }
+__device__ __forceinline__ double sroot4(double x) { return copysign(sqrt(sqrt(fabs(x))), x); }
+__device__ __forceinline__ double sroot6(double x) { return copysign(cbrt(sqrt(fabs(x))), x); }
 
 // The 10 raw features from the velocity gradient A[m][d] = d u_m / d x_d of a cell at height y
 // (R = float for inference, double for training data).
@@ -111,10 +260,10 @@ __device__ __forceinline__ void features_of(const R A[3][3], R y, R ly, R yplus_
     f[0] = trS;
     f[1] = sqrt(trS2 > 0 ? trS2 : (R)0);
     f[2] = sqrt(-trW2 > 0 ? -trW2 : (R)0);
-    f[3] = sroot(tr_of(S2, S), (R)1 / (R)3);
-    f[4] = sroot(W2S[0][0] + W2S[1][1] + W2S[2][2], (R)1 / (R)3);
-    f[5] = sroot(W2S2[0][0] + W2S2[1][1] + W2S2[2][2], (R)0.25);
-    f[6] = sroot(tr_of(W2S, WS2), (R)1 / (R)6);
+    f[3] = sroot3(tr_of(S2, S));
+    f[4] = sroot3(W2S[0][0] + W2S[1][1] + W2S[2][2]);
+    f[5] = sroot4(W2S2[0][0] + W2S2[1][1] + W2S2[2][2]);
+    f[6] = sroot6(tr_of(W2S, WS2));
     const R sg = y > 0 ? (R)-1 : (y < 0 ? (R)1 : (R)0);
     f[7] = sg * S[0][1];
     f[8] = sg * W[0][1];
@@ -484,33 +633,56 @@ __global__ void k_feature_moments(const float *feat, long long n, double *mom) {
 // ---- inference in a context ---------------------------------------------------------------
 
 // nu_t of every interior cell of level lvl, and of the ghost cells of periodic x and z (their
-// images); solid cells 0.  The velocity ghosts of lvl must be filled (wrap_con).
-template <class T> __global__ void k_nut(const __grid_constant__ DevState<T> S, int lvl, const Net *__restrict__ net,
-                                         float yplus_scale) {
-    __shared__ float w[NPARAM];
-    __shared__ float mu[NIN], rsd[NIN];
-    for (int q = threadIdx.x; q < NPARAM; q += blockDim.x) w[q] = net->w[q];
+// images); solid cells 0.  Reads interior cells and flags only.
+// The network staged in shared memory (coalesced loads; the fragments then read it with
+// per-lane addresses, which shared memory serves without serialising).
+struct NetSmem {
+    float w[NPARAM];
+    float mu[NIN], rsd[NIN];
+};
+__device__ __forceinline__ void stage_net(NetSmem &sm, const Net *__restrict__ net) {
+    for (int q = threadIdx.x; q < NPARAM; q += blockDim.x) sm.w[q] = net->w[q];
     if (threadIdx.x < NIN) {
-        mu[threadIdx.x] = net->mu[threadIdx.x];
-        rsd[threadIdx.x] = net->rsd[threadIdx.x];
+        sm.mu[threadIdx.x] = net->mu[threadIdx.x];
+        sm.rsd[threadIdx.x] = net->rsd[threadIdx.x];
     }
     __syncthreads();
+}
+
+template <class T> __global__ void __launch_bounds__(128)
+    k_nut(const __grid_constant__ DevState<T> S, int lvl, const Net *__restrict__ netd, float yplus_scale) {
+    __shared__ __align__(16) __nv_bfloat16 X[4][32 * 16];
+    __shared__ NetSmem net;
+    stage_net(net, netd);
+    const float *w = net.w;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const TcWeights B = tc_weights(w, lane);
     const Geom g = S.g;
     const Level<T> L = S.lv[lvl];
     const int nx = g.C1 + 2, nz = g.C3 + 2;
     const int n = nx * g.C2 * nz;
     const float rdx2[3] = {(float)(0.5 / S.k.dx[0]), (float)(0.5 / S.k.dx[1]), (float)(0.5 / S.k.dx[2])};
     const float ly = (float)(S.k.dx[1] * g.C2);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int ig = t % nx, r = t / nx, j = r % g.C2 + 1, kg = r / g.C2;
+    const int nwarps = gridDim.x * 4;
+    // warp-uniform loop: every lane of a warp takes part in each multiply
+    for (int base = (blockIdx.x * 4 + wid) * 32; base < n; base += nwarps * 32) {
+        const int t = base + lane;
+        const bool live = t < n;
+        const int tt = live ? t : n - 1;
+        const int ig = tt % nx, r = tt / nx, j = r % g.C2 + 1, kg = r / g.C2;
         // the interior cell whose value this position takes (periodic image, else nearest)
         const int i = ig == 0 ? (S.k.periodic_x ? g.C1 : 1) : (ig == g.C1 + 1 ? (S.k.periodic_x ? 1 : g.C1) : ig);
         const int k = kg == 0 ? (S.k.periodic_z ? g.C3 : 1) : (kg == g.C3 + 1 ? (S.k.periodic_z ? 1 : g.C3) : kg);
         const int64_t c = g.cell(i, j, k);
-        float nut = 0.f;
-        if (S.flags[c] & FL_EQ0) {
+        const bool fluid = (S.flags[c] & FL_EQ0) != 0;
+        float f[NIN];
+        {
             float A[3][3];
-            const int64_t nb[6] = {c - 1, c + 1, c - g.cs1, c + g.cs1, c - g.cs2, c + g.cs2};
+            // neighbours in x and z by index (periodic image or the zero-gradient copy), so the
+            // level's ghost cells are not needed: this runs beside the step's ghost fill
+            const int im = i > 1 ? i - 1 : (S.k.periodic_x ? g.C1 : 1), ip = i < g.C1 ? i + 1 : (S.k.periodic_x ? 1 : g.C1);
+            const int km = k > 1 ? k - 1 : (S.k.periodic_z ? g.C3 : 1), kp = k < g.C3 ? k + 1 : (S.k.periodic_z ? 1 : g.C3);
+            const int64_t nb[6] = {g.cell(im, j, k), g.cell(ip, j, k), c - g.cs1, c + g.cs1, g.cell(i, j, km), g.cell(i, j, kp)};
             const T *u[3] = {L.u1, L.u2, L.u3};
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
@@ -523,26 +695,44 @@ template <class T> __global__ void k_nut(const __grid_constant__ DevState<T> S, 
                 A[m][2] = (v[5] - v[4]) * rdx2[2];
             }
             const float y = -0.5f * ly + ((float)j - 0.5f) * (float)S.k.dx[1];
-            float f[NIN];
             features_of<float>(A, y, ly, yplus_scale, f);
 #pragma unroll
-            for (int q = 0; q < NIN; ++q) f[q] = (f[q] - mu[q]) * rsd[q];
-            nut = mlp_forward(w, f) * (float)S.k.vis;
+            for (int q = 0; q < NIN; ++q) f[q] = (f[q] - net.mu[q]) * net.rsd[q];
         }
-        S.nut[g.cell(ig, j, kg)] = (T)nut;
+        const float y_nu = tc_warp(w, B, X[wid], f, lane);
+        if (live) S.nut[g.cell(ig, j, kg)] = fluid ? (T)(y_nu * (float)S.k.vis) : (T)0;
+    }
+}
+
+// nu_t / nu of dataset rows through the tensor-core inference of the step (tests)
+__global__ void __launch_bounds__(128) k_mlp_predict_tc(const float *feat, long long n, const Net *__restrict__ netd,
+                                                        float *out) {
+    __shared__ __align__(16) __nv_bfloat16 X[4][32 * 16];
+    __shared__ NetSmem net;
+    stage_net(net, netd);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const TcWeights B = tc_weights(net.w, lane);
+    const long long nwarps = (long long)gridDim.x * 4;
+    for (long long base = ((long long)blockIdx.x * 4 + wid) * 32; base < n; base += nwarps * 32) {
+        const long long s = base + lane < n ? base + lane : n - 1;
+        float x[NIN];
+#pragma unroll
+        for (int i = 0; i < NIN; ++i) x[i] = (feat[s * NIN + i] - net.mu[i]) * net.rsd[i];
+        const float y = tc_warp(net.w, B, X[wid], x, lane);
+        if (base + lane < n) out[base + lane] = y;
     }
 }
 
 int grid_for(long long n, int threads = 256) {
     const long long b = (n + threads - 1) / threads;
-    return (int)(b < 152 * 8 ? (b < 1 ? 1 : b) : 152 * 8);
+    return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
 }
 
 } // namespace cl
 
 template <class T> void closure_nut(const DevState<T> &S, int lvl, const void *net, float yplus_scale, cudaStream_t st) {
     const long long n = (long long)(S.g.C1 + 2) * S.g.C2 * (S.g.C3 + 2);
-    cl::k_nut<T><<<cl::grid_for(n), 256, 0, st>>>(S, lvl, (const cl::Net *)net, yplus_scale);
+    cl::k_nut<T><<<cl::grid_for(n, 128), 128, 0, st>>>(S, lvl, (const cl::Net *)net, yplus_scale);
 }
 template void closure_nut<float>(const DevState<float> &, int, const void *, float, cudaStream_t);
 template void closure_nut<double>(const DevState<double> &, int, const void *, float, cudaStream_t);
@@ -967,6 +1157,21 @@ int ark_mlp_train(ark_mlp *M, ark_closure_data *d, int epochs, long long batch, 
     return ARK_OK;
 }
 
+int ark_mlp_predict_tc(ark_mlp *M, ark_closure_data *d, long long first, long long count, float *out) {
+    if (!M || !d || !out || first < 0 || count < 0 || first + count > d->n) return cfail(ARK_ERR_PARAM, "bad range");
+    if (count == 0) return ARK_OK;
+    float *o = nullptr;
+    CL_CUDA(cudaStreamSynchronize(d->st));
+    CL_CUDA(cudaMalloc(&o, sizeof(float) * count));
+    cl::k_mlp_predict_tc<<<cl::grid_for(count, 128), 128, 0, M->st>>>(d->feat + first * cl::NIN, count, M->net, o);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(M->st);
+    if (e == cudaSuccess) e = cudaMemcpy(out, o, sizeof(float) * count, cudaMemcpyDeviceToHost);
+    cudaFree(o);
+    if (e != cudaSuccess) return cfail(ARK_ERR_CUDA, std::string("predict: ") + cudaGetErrorString(e));
+    return ARK_OK;
+}
+
 int ark_mlp_predict(ark_mlp *M, ark_closure_data *d, long long first, long long count, float *out) {
     if (!M || !d || !out || first < 0 || count < 0 || first + count > d->n) return cfail(ARK_ERR_PARAM, "bad range");
     if (count == 0) return ARK_OK;
@@ -984,8 +1189,14 @@ int ark_mlp_predict(ark_mlp *M, ark_closure_data *d, long long first, long long 
 
 } // extern "C"
 
-// the network constants on the device, for ark_api.cu's closure step
+// the network constants, for ark_api.cu's closure step
 namespace ark {
 const void *mlp_device_net(const ark_mlp *M) { return M ? (const void *)M->net : nullptr; }
-cudaStream_t mlp_stream(const ark_mlp *M) { return M ? M->st : nullptr; }
+size_t mlp_bytes() { return sizeof(cl::Net); }
+int mlp_snapshot_device(const ark_mlp *M, void *dev_out) {
+    if (!M || !dev_out) return ARK_ERR_PARAM;
+    if (cudaStreamSynchronize(M->st) != cudaSuccess) return ARK_ERR_CUDA;
+    if (cudaMemcpy(dev_out, M->net, sizeof(cl::Net), cudaMemcpyDeviceToDevice) != cudaSuccess) return ARK_ERR_CUDA;
+    return ARK_OK;
+}
 } // namespace ark

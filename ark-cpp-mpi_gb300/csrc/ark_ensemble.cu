@@ -235,8 +235,8 @@ int build_lists(ark_ensemble *E) {
                 gx = (g.C1 + 127) / 128, gy = g.C2, gz = (g.C3 + 1 + seg - 1) / seg;
                 break;
             }
-            case WL_WRAP: {
-                const int64_t tot = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
+            case WL_WRAP: { // every line of up to 16 arrays (the longest ghost-fill job)
+                const int64_t tot = ((int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2) * 16;
                 gx = (int)((tot + 127) / 128);
                 break;
             }

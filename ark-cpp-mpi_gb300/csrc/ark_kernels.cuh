@@ -332,36 +332,36 @@ struct WrapJob {
 //   GH_COPY (bounded axis): zero-gradient ghost 0 <- cell 1, ghost C+1 <- cell C; faces:
 //           halo 0 <- face 1, halo C+2 <- face C+1 (main.cpp:803-845, 1633-1698);
 // over the interior of the other two axes.
+// Thread t copies the two ghosts of one line of one array: arrays q = t / (lines), lines
+// first the (j, k) lines of x, then the (i, j) lines of z.
 template <class T> __device__ __forceinline__ void wrap_body(const Geom &g, const WrapJob &J, int64_t t) {
-    const int64_t nx = (int64_t)g.C2 * g.C3, nz = (int64_t)g.C1 * g.C2;
-    if (t < nx) {
-        const int j = (int)(t % g.C2) + 1, k = (int)(t / g.C2) + 1;
-        for (int q = 0; q < J.n; ++q) {
-            const uint8_t m = J.mode[q][0];
-            if (m == GH_NONE) continue;
-            T *a = (T *)J.a[q];
-            if (J.face[q]) {
-                a[g.face(0, j, k)] = a[g.face(m == GH_WRAP ? g.C1 : 1, j, k)];
-                a[g.face(g.C1 + 2, j, k)] = a[g.face(m == GH_WRAP ? 2 : g.C1 + 1, j, k)];
-            } else {
-                a[g.cell(0, j, k)] = a[g.cell(m == GH_WRAP ? g.C1 : 1, j, k)];
-                a[g.cell(g.C1 + 1, j, k)] = a[g.cell(m == GH_WRAP ? 1 : g.C1, j, k)];
-            }
+    const int64_t nx = (int64_t)g.C2 * g.C3, nz = (int64_t)g.C1 * g.C2, nl = nx + nz;
+    const int q = (int)(t / nl);
+    if (q >= J.n) return;
+    const int64_t r = t - (int64_t)q * nl;
+    T *a = (T *)J.a[q];
+    if (r < nx) {
+        const uint8_t m = J.mode[q][0];
+        if (m == GH_NONE) return;
+        const int j = (int)(r % g.C2) + 1, k = (int)(r / g.C2) + 1;
+        if (J.face[q]) {
+            a[g.face(0, j, k)] = a[g.face(m == GH_WRAP ? g.C1 : 1, j, k)];
+            a[g.face(g.C1 + 2, j, k)] = a[g.face(m == GH_WRAP ? 2 : g.C1 + 1, j, k)];
+        } else {
+            a[g.cell(0, j, k)] = a[g.cell(m == GH_WRAP ? g.C1 : 1, j, k)];
+            a[g.cell(g.C1 + 1, j, k)] = a[g.cell(m == GH_WRAP ? 1 : g.C1, j, k)];
         }
-    } else if (t < nx + nz) {
-        const int64_t u = t - nx;
+    } else {
+        const uint8_t m = J.mode[q][1];
+        if (m == GH_NONE) return;
+        const int64_t u = r - nx;
         const int i = (int)(u % g.C1) + 1, j = (int)(u / g.C1) + 1;
-        for (int q = 0; q < J.n; ++q) {
-            const uint8_t m = J.mode[q][1];
-            if (m == GH_NONE) continue;
-            T *a = (T *)J.a[q];
-            if (J.face[q]) {
-                a[g.face(i, j, 0)] = a[g.face(i, j, m == GH_WRAP ? g.C3 : 1)];
-                a[g.face(i, j, g.C3 + 2)] = a[g.face(i, j, m == GH_WRAP ? 2 : g.C3 + 1)];
-            } else {
-                a[g.cell(i, j, 0)] = a[g.cell(i, j, m == GH_WRAP ? g.C3 : 1)];
-                a[g.cell(i, j, g.C3 + 1)] = a[g.cell(i, j, m == GH_WRAP ? 1 : g.C3)];
-            }
+        if (J.face[q]) {
+            a[g.face(i, j, 0)] = a[g.face(i, j, m == GH_WRAP ? g.C3 : 1)];
+            a[g.face(i, j, g.C3 + 2)] = a[g.face(i, j, m == GH_WRAP ? 2 : g.C3 + 1)];
+        } else {
+            a[g.cell(i, j, 0)] = a[g.cell(i, j, m == GH_WRAP ? g.C3 : 1)];
+            a[g.cell(i, j, g.C3 + 1)] = a[g.cell(i, j, m == GH_WRAP ? 1 : g.C3)];
         }
     }
 }
@@ -1379,7 +1379,7 @@ inline void wrap_add(WrapJob &J, void *a, int face, uint8_t mx, uint8_t mz) {
 
 template <class T> inline void wrap_launch(const DevState<T> &S, const WrapJob &J, cudaStream_t st) {
     if (J.n == 0) return;
-    const int64_t tot = (int64_t)S.g.C2 * S.g.C3 + (int64_t)S.g.C1 * S.g.C2;
+    const int64_t tot = ((int64_t)S.g.C2 * S.g.C3 + (int64_t)S.g.C1 * S.g.C2) * J.n;
     k_wrap<T><<<grid_for(tot, 256, 1 << 30), 256, 0, st>>>(S.g, J);
 }
 
@@ -1514,23 +1514,24 @@ template <class T> void Launch<T>::use_forces(const DevState<T> &S, int ncon, cu
 }
 
 // Segments of at most 32 faces, balanced so no thread gets a short tail.
-inline int sweep_segment(int nd, int *nseg) {
-    const int n = (nd + 31) / 32;
+// segments of at most `target` faces, balanced
+inline int sweep_segment(int nd, int target, int *nseg) {
+    const int n = (nd + target - 1) / target;
     *nseg = n;
     return (nd + n - 1) / n;
 }
 
-template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st) {
+template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target) {
     if (axis == 0) {
         const int lines_x = S.g.C2 * S.g.C3;
         k_sweep_x<T><<<(lines_x + 3) / 4, 128, 0, st>>>(S, con, fcur);
     } else if (axis == 1) {
         int nseg;
-        const int seg = sweep_segment(S.g.C2 + 1, &nseg);
+        const int seg = sweep_segment(S.g.C2 + 1, target, &nseg);
         k_sweep_col<T, 1><<<dim3((S.g.C1 + 127) / 128, S.g.C3, nseg), 128, 0, st>>>(S, con, fcur, seg);
     } else {
         int nseg;
-        const int seg = sweep_segment(S.g.C3 + 1, &nseg);
+        const int seg = sweep_segment(S.g.C3 + 1, target, &nseg);
         k_sweep_col<T, 2><<<dim3((S.g.C1 + 127) / 128, S.g.C2, nseg), 128, 0, st>>>(S, con, fcur, seg);
     }
 }

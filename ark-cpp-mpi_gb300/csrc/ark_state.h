@@ -198,7 +198,8 @@ template <class T> struct Launch {
     static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st);
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
-    static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st);
+    // x2/x3 sweeps: lines cut into balanced segments of at most `target` faces
+    static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target = 32);
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
     static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);
@@ -244,9 +245,16 @@ template <class T> void output_plane_stats(const DevState<T> &S, int ncon, doubl
 template <class T> void output_energy(const DevState<T> &S, int ncon, double *scratch, double *out, cudaStream_t st);
 
 // ---- learned closure (ark_closure.cu) ----
+} // namespace ark
+struct ark_mlp;
+namespace ark {
 // nu_t of level lvl into S.nut (interior cells and periodic ghost images); net: the network's
 // device constants (mlp_device_net); yplus_scale = u_tau / vis.
 template <class T> void closure_nut(const DevState<T> &S, int lvl, const void *net, float yplus_scale, cudaStream_t st);
+// the network's constants (weights, normalisation) copied into a device buffer of mlp_bytes()
+// bytes, which closure_nut reads
+size_t mlp_bytes();
+int mlp_snapshot_device(const ark_mlp *M, void *dev_out);
 // the interior velocities of level lvl into three compact FP64 arrays
 template <class T> void closure_gather(const DevState<T> &S, int lvl, double *u0, double *u1, double *u2, cudaStream_t st);
 // samples of a C1 x C2 x C3 grid on the lattice (sx, sz, ox, oz), or -1 for a bad lattice

@@ -248,7 +248,7 @@ int ark_selftest_staging(int n1_cells, int n2_cells, int n3_cells, int planes_pe
 
 /* ---- learned eddy-viscosity closure (a project extension; the reference has none) --------
  * A network nu_t / nu = softplus(w3 . GELU(W2 GELU(W1 x_n + b1) + b2) + b3) (10 -> 32 -> 32 ->
- * 1, BF16 weights, FP32 arithmetic) of 10 features of the local velocity gradient (the seven
+ * 1, BF16 weights, FP32 accumulation; GELU in its tanh form) of 10 features of the local velocity gradient (the seven
  * integrity-basis invariants of S and W as signed roots, the wall-frame shear -sgn(y) S_12 and
  * vorticity -sgn(y) W_12, and y+ = (ly/2 - |y|) u_tau / vis), normalised x_n = (x - mu) / sd.
  * Trained on 3 x 3 x 3 box-filtered fields of fine runs against the least-squares eddy
@@ -285,13 +285,23 @@ int ark_mlp_fit_normalization(ark_mlp *mlp, ark_closure_data *data);
  * fixed order) and the error itself */
 int ark_mlp_gradient(ark_mlp *mlp, ark_closure_data *data, long long first, long long count, double *grad, double *loss);
 int ark_mlp_train(ark_mlp *mlp, ark_closure_data *data, int epochs, long long batch, double lr, double *loss);
-/* nu_t / nu of rows [first, first + count) */
+/* nu_t / nu of rows [first, first + count): FP32 throughout (as trained) ... */
 int ark_mlp_predict(ark_mlp *mlp, ark_closure_data *data, long long first, long long count, float *out);
+/* ... and through the step's inference: the two hidden layers as BF16 tensor-core multiplies
+ * (FP32 accumulation, BF16 activations) and GELU with the hardware tanh approximation. */
+int ark_mlp_predict_tc(ark_mlp *mlp, ark_closure_data *data, long long first, long long count, float *out);
 /* mlp != NULL: every ark_step of this FP32 context evaluates nu_t from the "Con" velocities
- * before the stress and uses vis + (nu_t(c) + nu_t(neighbour))/2 on each face; the network is
- * read at each step (train it further and the steps follow).  mlp == NULL: the plain step.
- * The step pieces called one by one stay plain.  The array is readable as "nut". */
+ * before the stress and uses vis + (nu_t(c) + nu_t(neighbour))/2 on each face, with the
+ * network as it is at this call (call again after further training).  mlp == NULL: the plain
+ * step.  The step pieces called one by one stay plain.  The array is readable as "nut". */
 int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
+
+/* Times the kernel shapes of the step on the live state (it advances) and keeps the fastest,
+ * one setting at a time: the shape of the Phase1 with stress (0 one cell per thread, 1
+ * marching, 2 staged in shared memory, FP32 only), of the second Phase1, and the x2/x3 sweep
+ * segment length (8, 16, 32, 64 faces).  The results do not depend on the shapes.  choice (4
+ * ints, may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step}. */
+int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice);
 
 /* ---- ensembles: many independent channels in one launch per phase ------------------------
  * The members (FP32 contexts, each with its own grid size and parameters, all on one device

@@ -16,7 +16,8 @@ Definitions:
   * target: nu* / nu with nu* = max(0, -tau^d : S^d / (2 S^d : S^d)), tau = filter(u_i u_j) -
     filter(u_i) filter(u_j), ^d the deviatoric parts; 0 where S^d : S^d < 1e-30.
   * network: x_n = (x - mu) / sd; h1 = GELU(W1 x_n + b1) (32); h2 = GELU(W2 h1 + b2) (32);
-    y = softplus(w3 . h2 + b3) = nu_t / nu.  GELU(z) = z (1 + erf(z / sqrt 2)) / 2.
+    y = softplus(w3 . h2 + b3) = nu_t / nu.  GELU in its tanh form:
+    GELU(z) = z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))) / 2.
     Parameters (1441) in the order W1[32][10], b1[32], W2[32][32], b2[32], w3[32], b3[1]; the
     forward and backward passes use them rounded to BF16 (nearest even).
   * loss: mean over the batch of (y - target)^2.
@@ -51,15 +52,16 @@ def bf16(a):
     return r.view(np.float32).astype(np.float64)
 
 
-_erf = np.vectorize(math.erf, otypes=[np.float64])
+_K0, _K1 = math.sqrt(2.0 / math.pi), 0.044715
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(_K0 * (z + _K1 * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    th = np.tanh(_K0 * (z + _K1 * z ** 3))
+    return 0.5 * (1.0 + th) + 0.5 * z * (1.0 - th * th) * _K0 * (1.0 + 3.0 * _K1 * z * z)
 
 
 def softplus(z):

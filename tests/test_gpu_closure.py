@@ -158,3 +158,25 @@ def test_trained_network_beats_no_closure_on_held_out_samples(ark, port):
         _, ttrain = train.get()
         mse_const = float(np.mean((np.mean(ttrain) - t) ** 2))
         assert mse_net < 0.9 * mse_const < 0.9 * mse_zero, (mse_net, mse_const, mse_zero)
+
+
+def test_tensor_core_inference_matches_oracle(ark):
+    """The step's inference (hidden layers as BF16 tensor-core multiplies, FP32 accumulation,
+    GELU with the hardware tanh) against the FP64 network: BF16 activations bound the error."""
+    m = oc()
+    rng = np.random.default_rng(17)
+    theta, mu, sd = rand_net(rng)
+    n = 5000  # a ragged last warp
+    X = (rng.normal(0, 1, (n, m.NIN)) * sd + mu).astype(np.float32)
+    with ark.ClosureData(n) as d, ark.Mlp() as net:
+        d.append(X, np.zeros(n, np.float32))
+        net.set(theta, mu, sd)
+        wq = m.bf16(theta)
+        mu32, sd32 = np.float32(mu).astype(np.float64), 1.0 / np.float32(1.0 / sd).astype(np.float64)
+        want = m.forward(wq, mu32, sd32, X.astype(np.float64))
+        tc = net.predict(d, tensor_cores=True)
+        fp32 = net.predict(d)
+        assert np.allclose(fp32, want, rtol=2e-4, atol=2e-5)
+        err = np.abs(tc - want)
+        assert np.all(err <= 0.03 * np.abs(want) + 0.02 * np.mean(np.abs(want))), err.max()
+        assert np.mean(err) <= 0.01 * np.mean(np.abs(want))

@@ -368,3 +368,24 @@ def test_bounded_axes_match_oracle(ark, port, px, pz):
             st = ctx.download(CELLS + FACES)
         for n in CELLS + FACES:
             assert bits_equal(port.interior(n, st[n]), port.interior(n, o.get(n))), (fused, n)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_autotune_keeps_results(ark, port, prec):
+    """ark_autotune advances the state while it times the shapes; the result equals the same
+    number of plain steps bit for bit."""
+    p = port.channel_params(40, 24, 20, seed=8)
+    P = params_from(ark, p, precision=ark.FP64 if prec == "fp64" else ark.FP32)
+    st0 = port.channel_state(p)
+    with ark.Context(P) as a, ark.Context(P) as b:
+        a.upload(st0)
+        b.upload(st0)
+        choice = a.autotune(1)
+        assert choice["segment"] in (8, 16, 32, 64) and choice["phase1"] in (0, 1, 2)
+        n = a.scalars().nstep
+        b.step(n)
+        a.sync()
+        b.sync()
+        ra, rb = a.download(CELLS + FACES), b.download(CELLS + FACES)
+        for name in CELLS + FACES:
+            assert bits_equal(ra[name], rb[name]), name
