@@ -505,17 +505,18 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
             return nullptr;
         }
     }
-    // Phase1 kernel shapes measured fastest on GB300: FP32 stages its planes in shared memory
-    // for both Phase1 launches (0.81 vs 1.13 ms marching and 0.64 vs 0.71 ms one cell per
-    // thread at 512x256x256); FP64 is ALU-bound and prefers one cell per thread for both
-    // (2.88 vs 2.98 ms marching).
-    ctx->march[0] = params->precision == ARK_FP32 ? 2 : 0;
-    ctx->march[1] = params->precision == ARK_FP32 ? 2 : 0;
+    // Phase1 kernel shapes measured fastest on GB300 at the benchmark sizes: FP32 stages its
+    // planes in shared memory (0.76 vs 1.10 ms marching and 0.61 vs 0.70 ms one cell per
+    // thread at 512x256x256); FP64 computes each face's quantities once (1.94 vs 2.37 ms and
+    // 1.10 vs 1.18 ms one cell per thread at 256x128x128).  ark_autotune picks per grid.
+    ctx->march[0] = params->precision == ARK_FP32 ? 2 : 3;
+    ctx->march[1] = params->precision == ARK_FP32 ? 2 : 3;
     if (const char *e = std::getenv("ARK_PHASE1_MARCH")) { // "ab": a for Phase1 with stress, b without
         // 0: one cell per thread, 1: marching, 2: planes staged in shared memory (FP32 only)
-        const char top = params->precision == ARK_FP32 ? '2' : '1';
-        if (e[0] >= '0' && e[0] <= top) ctx->march[0] = e[0] - '0';
-        if (e[0] && e[1] >= '0' && e[1] <= top) ctx->march[1] = e[1] - '0';
+        // 3: face quantities computed once (FP64 only)
+        auto ok = [&](char ch) { return ch >= '0' && ch <= '1' ? true : (params->precision == ARK_FP32 ? ch == '2' : ch == '3'); };
+        if (ok(e[0])) ctx->march[0] = e[0] - '0';
+        if (e[0] && ok(e[1])) ctx->march[1] = e[1] - '0';
     }
     Launch<float>::prepare();
     cudaEventCreate(&ctx->ev0);
@@ -1132,7 +1133,9 @@ extern "C" {
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (steps_per_candidate < 1) return fail(ARK_ERR_PARAM, "steps_per_candidate < 1");
-    const int top = ctx->P.precision == ARK_FP32 ? 2 : 1;
+    // Phase1 shapes: one cell per thread, marching, and the precision's own (staged for FP32,
+    // face-centric for FP64)
+    const int shapes[3] = {0, 1, ctx->P.precision == ARK_FP32 ? 2 : 3};
     auto measure = [&](double *us) -> int {
         ARK_CUDA(cudaStreamSynchronize(ctx->st));
         drop_graphs(ctx);
@@ -1145,11 +1148,11 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     double best = 0.0;
     if (int rc = measure(&best)) return rc;
     for (int which = 0; which < 3; ++which) {
-        const int ncand = which < 2 ? top + 1 : 4;
+        const int ncand = which < 2 ? 3 : 4;
         const int segs[4] = {8, 16, 32, 64};
         int keep = which < 2 ? ctx->march[which] : ctx->seg_target;
         for (int c = 0; c < ncand; ++c) {
-            const int v = which < 2 ? c : segs[c];
+            const int v = which < 2 ? shapes[c] : segs[c];
             if (v == keep) continue;
             if (which < 2) ctx->march[which] = v;
             else ctx->seg_target = v;

@@ -800,6 +800,187 @@ __global__ void __launch_bounds__(kTileX *kTileY)
     phase1_cell_body<T, MODE>(S, src, dst, fcur, bix_here());
 }
 
+// ---------------------------------------------------------------------------------------
+// Phase1 with each face's quantities computed once (FP64 contexts, bound by the FP64 pipe).
+// The one-cell kernel evaluates the mass flux, the three momentum fluxes and (with the
+// stress) the three face stresses of every face twice, once for each cell beside it.  Here a
+// block owns a 64 x 4 tile of columns and marches up a chunk of planes: per plane, each thread
+// evaluates the x and y faces below its cell (the last column and row of the tile also the
+// faces above) into shared memory and the z face above its cell in registers (the face below
+// is the previous plane's face above).  Every face value is the expression the one-cell kernel
+// evaluates, in the same operation order, and every cell combines them in the same order, so
+// the results are bit-identical (tested).
+// ---------------------------------------------------------------------------------------
+namespace fcs {
+constexpr int SX = 64, SY = 4;
+template <class T> struct FaceQ {
+    T mf, mom[3], sig[3];
+};
+
+// The quantities of the face normal to d with values V: the mass flux ro u_d, the momentum
+// fluxes (ro u_m) u_d (+ p when m == d) of half_step, and StressTensor's sigma_md between the
+// cell below (flags flo, velocity ulo) and the cell above (fhi, uhi).
+template <class T, bool STRESS>
+__device__ __forceinline__ FaceQ<T> face_q(const FaceVal<T> &V, int d, uint8_t flo, uint8_t fhi, const T ulo[3],
+                                           const T uhi[3], const K<T> &kk) {
+    FaceQ<T> q;
+    q.mf = V.ro * V.u[d];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        q.mom[m] = (m == d) ? V.ro * V.u[m] * V.u[d] + V.p : V.ro * V.u[m] * V.u[d];
+        q.sig[m] = STRESS ? sigma(flo, fhi, ulo[m], uhi[m], kk, d) : (T)0;
+    }
+    return q;
+}
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constant__ DevState<T> S, int src, int dst, int fcur, int kch) {
+    static_assert(!Storage<T>::deviation, "face-centric Phase1: FP64 storage form");
+    constexpr bool STRESS = (MODE & P1_STRESS) != 0;
+    __shared__ FaceQ<T> Fx[SY][SX + 1], Fy[SY + 1][SX];
+    const Geom g = S.g;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = blockIdx.x * SX + tx + 1, j = blockIdx.y * SY + ty + 1;
+    const int k0 = blockIdx.z * kch + 1;
+    const int k1 = k0 + kch - 1 < g.C3 ? k0 + kch - 1 : g.C3;
+    const bool valid = i <= g.C1 && j <= g.C2;
+    const int ilast = blockIdx.x * SX + SX < g.C1 ? blockIdx.x * SX + SX : g.C1;
+    const int jlast = blockIdx.y * SY + SY < g.C2 ? blockIdx.y * SY + SY : g.C2;
+    const K<T> &kk = kconst<T>(S.k);
+    const T dt = sc_dt<T>(S.sc);
+    const T G = (MODE & P1_BULK) ? sc_G<T>(S.sc) : (T)0;
+    const Level<T> L = S.lv[src];
+    const uint8_t *__restrict__ flags = S.flags;
+    const int cs1 = (int)g.cs1, cs2 = (int)g.cs2, fs1 = (int)g.fs1, fs2 = (int)g.fs2;
+    const T zero3[3] = {(T)0, (T)0, (T)0};
+    auto cellu = [&](int c, T u[3]) {
+        u[0] = L.u1[c];
+        u[1] = L.u2[c];
+        u[2] = L.u3[c];
+    };
+    unsigned long long m0 = 0, m1 = 0, m2 = 0;
+    long long rsum = 0;
+    FaceQ<T> zlo = {};
+    uint8_t fl = 0;
+    T uc[3] = {(T)0, (T)0, (T)0};
+    if (valid) {
+        const int c = g.ci(i, j, k0), f = g.fi(i, j, k0);
+        fl = flags[c];
+        cellu(c, uc);
+        T ud[3];
+        if (STRESS) cellu(c - cs2, ud);
+        zlo = face_q<T, STRESS>(load_face(S.fc[fcur][2], f, kk), 2, STRESS ? flags[c - cs2] : 0, fl, STRESS ? ud : zero3,
+                                uc, kk);
+    }
+    for (int k = k0; k <= k1; ++k) {
+        FaceQ<T> zhi = {};
+        uint8_t flu = 0;
+        T uu[3] = {(T)0, (T)0, (T)0};
+        const int c = valid ? g.ci(i, j, k) : 0, f = valid ? g.fi(i, j, k) : 0;
+        if (valid) {
+            T un[3] = {(T)0, (T)0, (T)0};
+            uint8_t fn = 0;
+            if (STRESS) {
+                fn = flags[c - 1];
+                cellu(c - 1, un);
+            }
+            Fx[ty][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][0], f, kk), 0, fn, fl, un, uc, kk);
+            if (i == ilast) {
+                if (STRESS) {
+                    fn = flags[c + 1];
+                    cellu(c + 1, un);
+                }
+                Fx[ty][tx + 1] = face_q<T, STRESS>(load_face(S.fc[fcur][0], f + 1, kk), 0, fl, fn, uc, un, kk);
+            }
+            if (STRESS) {
+                fn = flags[c - cs1];
+                cellu(c - cs1, un);
+            }
+            Fy[ty][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][1], f, kk), 1, fn, fl, un, uc, kk);
+            if (j == jlast) {
+                if (STRESS) {
+                    fn = flags[c + cs1];
+                    cellu(c + cs1, un);
+                }
+                Fy[ty + 1][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][1], f + fs1, kk), 1, fl, fn, uc, un, kk);
+            }
+            flu = flags[c + cs2];
+            cellu(c + cs2, uu);
+            zhi = face_q<T, STRESS>(load_face(S.fc[fcur][2], f + fs2, kk), 2, fl, flu, uc, uu, kk);
+        }
+        __syncthreads();
+        if (valid) {
+            const FaceQ<T> &Lx = Fx[ty][tx], &Hx = Fx[ty][tx + 1], &Ly = Fy[ty][tx], &Hy = Fy[ty + 1][tx];
+            const T ro_c = L.ro[c];
+            T ro_cn, ucn[3], rden = (T)0;
+            if (fl & FL_LT) {
+                // half_step (main.cpp:530-551) over the face quantities
+                ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((Hx.mf - Lx.mf) * kk.ds[0] + (Hy.mf - Ly.mf) * kk.ds[1] +
+                                                            (zhi.mf - zlo.mf) * kk.ds[2]),
+                             kk.dvc, kk.rdvc);
+                const T den = ro_cn * kk.dvc;
+                const T rd = recip(den);
+                rden = rd;
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    const T fx0 = Hx.mom[m] - Lx.mom[m], fx1 = Hy.mom[m] - Ly.mom[m], fx2 = zhi.mom[m] - zlo.mom[m];
+                    ucn[m] = divr(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx0 * kk.ds[0] + fx1 * kk.ds[1] + fx2 * kk.ds[2]),
+                                  den, rd);
+                }
+            } else {
+                ucn[0] = ucn[1] = ucn[2] = (T)0;
+                ro_cn = kk.ro0;
+            }
+            T fv[3] = {(T)0, (T)0, (T)0};
+            if (STRESS) {
+                if (fl & FL_EQ0) {
+#pragma unroll
+                    for (int m = 0; m < 3; ++m)
+                        fv[m] = ((Hx.sig[m] - Lx.sig[m]) * kk.ds[0] + (Hy.sig[m] - Ly.sig[m]) * kk.ds[1] +
+                                 (zhi.sig[m] - zlo.sig[m]) * kk.ds[2]) *
+                                ro_c;
+                    if (MODE & P1_BULK) fv[0] = fv[0] + (ro_c * kk.dvc) * G;
+                }
+                S.f[0][c] = fv[0];
+                S.f[1][c] = fv[1];
+                S.f[2][c] = fv[2];
+            } else if (MODE & P1_FORCES) {
+                fv[0] = __ldg(S.f[0] + c);
+                fv[1] = __ldg(S.f[1] + c);
+                fv[2] = __ldg(S.f[2] + c);
+            }
+            if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
+                // UseForces (main.cpp:1035-1041)
+                const T den = kk.dvc * ro_cn;
+#pragma unroll
+                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * fv[m], den, rden);
+            }
+            S.lv[dst].ro[c] = ro_cn;
+            S.lv[dst].u1[c] = ucn[0];
+            S.lv[dst].u2[c] = ucn[1];
+            S.lv[dst].u3[c] = ucn[2];
+            if (MODE & P1_RMAX) {
+                const unsigned long long b0 = abs_key(ucn[0]), b1 = abs_key(ucn[1]), b2 = abs_key(ucn[2]);
+                m0 = b0 > m0 ? b0 : m0;
+                m1 = b1 > m1 ? b1 : m1;
+                m2 = b2 > m2 ? b2 : m2;
+            }
+            if ((MODE & P1_RSUM) && (fl & FL_EQ0)) rsum += fixed_sum_term(ucn[0]);
+        }
+        __syncthreads();
+        zlo = zhi;
+        fl = flu;
+        uc[0] = uu[0];
+        uc[1] = uu[1];
+        uc[2] = uu[2];
+    }
+    if (MODE & (P1_RMAX | P1_RSUM)) {
+        const BIx bx = {(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y};
+        tile_store<T, SX * SY>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+    }
+}
+} // namespace fcs
+
 // StressTensor's face stresses into the sigm arrays (kept only on request), faces normal
 // to d with index 1..C_d+1 along d (main.cpp:856-982).
 template <class T> __global__ void k_stress_faces(DevState<T> S, int con, int d) {
@@ -1461,13 +1642,33 @@ template <class T, int MODE> struct CellK {
 
 #include "ark_staged.cuh"
 
-// march = 2: k_phase1_staged (FP32, the two Phase1 modes of a step; others fall back to the
-// one-cell kernel); 1: k_phase1 (a block marches kTileK planes); 0: k_phase1_cell
+// march = 3: fcs::k_phase1_faces (FP64, face quantities computed once); 2: k_phase1_staged
+// (FP32); both for the two Phase1 modes of a step, other modes fall back to the one-cell
+// kernel; 1: k_phase1 (a block marches kTileK planes); 0: k_phase1_cell
 template <class T>
 void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st) {
     if (mode & P1_NUT) {
         launch_phase1_nut<T>(S, src, dst, fcur, mode, dim3(tiles_x(S.g), tiles_y(S.g), S.g.C3), st);
         return;
+    }
+    if constexpr (std::is_same<T, double>::value) {
+        if (march == 3) {
+            const int kch = stg::staged_chunk(S.g);
+            const dim3 grid((S.g.C1 + fcs::SX - 1) / fcs::SX, (S.g.C2 + fcs::SY - 1) / fcs::SY, (S.g.C3 + kch - 1) / kch);
+            const dim3 block(fcs::SX, fcs::SY);
+            switch (mode) {
+            case P1_STRESS | P1_FORCES | P1_RMAX:
+                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                return;
+            case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
+                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                return;
+            case P1_FORCES | P1_RSUM:
+                fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                return;
+            default: march = 0; break;
+            }
+        }
     }
     if constexpr (std::is_same<T, float>::value) {
         if (march == 2) {

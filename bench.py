@@ -178,6 +178,8 @@ def gpu_leg(arkgpu, C, re_b, precision, steps, warmup, device, seed, kernel_step
     cells = C[0] * C[1] * C[2]
     with arkgpu.Context(p) as ctx:
         ctx.upload(st)
+        shapes = ctx.autotune(3)  # the library's shape autotuner, then the same start state
+        ctx.upload(st)
         del st
         ctx.step(warmup)
         ctx.sync()
@@ -186,7 +188,8 @@ def gpu_leg(arkgpu, C, re_b, precision, steps, warmup, device, seed, kernel_step
         clocks = clk.summary()
         ktimes = ctx.kernel_times(kernel_steps)
         sc = ctx.scalars()
-    return {"cells": cells, "ms": ms, "clocks": clocks, "ktimes": ktimes, "dt": sc.dt, "ub": sc.bulk_velocity}
+    return {"cells": cells, "ms": ms, "clocks": clocks, "ktimes": ktimes, "dt": sc.dt, "ub": sc.bulk_velocity,
+            "shapes": shapes}
 
 
 def roofline(kt, cells, word, peak, peak_kind, traffic_tab, prec_name):
@@ -214,6 +217,8 @@ def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
     del st
     cells = C[0] * C[1] * C[2]
     with arkgpu.Context(p) as ctx:
+        ctx.upload_struct(hs.struct(True))
+        ctx.autotune(3)  # kernel shapes, before anything is timed
         ctx.upload_struct(hs.struct(True))  # warm-up: graphs, first transfers
         ctx.step(2)
         ctx.scalars()
@@ -396,7 +401,7 @@ def main():
             "config": {"workload": f"channel {C[0]}x{C[1]}x{C[2]} FP64 Re_b={args.re:g}, c=10, CFL 0.2, bulk forcing",
                        "grid": list(C), "precision": "fp64", "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"inputs larger than L2: {g['cells'] * 8 * 41 / 1e9:.2f} GB of state streamed per step"},
-            "clocks": g["clocks"],
+            "clocks": g["clocks"], "kernel_shapes": g["shapes"],
             "gpu_launches": launches_per_step * args.steps}
     line["roofline"] = roofline(g["ktimes"], g["cells"], 8, peak, peak_kind, traffic, "fp64")
     step_s = ms * 1e-3 / args.steps
@@ -419,7 +424,8 @@ def main():
                                           "achieved": round(f["cells"] * STEP_VALUES * 4 / f_step_s / 1e9, 1),
                                           "peak": peak, "unit": "GB/s",
                                           "frac": round(f["cells"] * STEP_VALUES * 4 / f_step_s / 1e9 / peak, 4)},
-                        "kernels_ms": {k: round(v, 4) for k, v in f["ktimes"]}, "clocks": f["clocks"]}
+                        "kernels_ms": {k: round(v, 4) for k, v in f["ktimes"]}, "clocks": f["clocks"],
+                        "kernel_shapes": f["shapes"]}
         line["gpu_launches"] += launches_per_step * f_steps
 
     if rank == 0 and args.ensemble > 0:
