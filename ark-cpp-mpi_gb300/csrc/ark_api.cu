@@ -173,7 +173,7 @@ struct ark_ctx {
     int march[2] = {1, 0};    // Phase1 kernel shape of the two Phase1 launches of a step
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [con][fcur]
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    double *stage = nullptr; // device double staging for FP32 contexts
+    double *stage = nullptr; // contiguous double staging for host transfers
     AvgArrays avg = {{nullptr, nullptr, nullptr}}; // averageU1..3 (FP64, reference layout)
     bool averaging = false;  // AverageValues at the end of every step
     void *closure_net = nullptr;          // learned closure: the network's constants (device copy)
@@ -264,29 +264,21 @@ template <class T> struct EngineT : Engine {
         return nullptr;
     }
 
-    // Host arrays in the Arr3d layout <-> device arrays with padded rows.  FP64: pitched
-    // copies.  FP32: through the double staging buffer (same padded rows), density fields
-    // shifted by ro0 (the device holds rho - ro0).
-    size_t padded(int face) const { return face ? (size_t)S.g.nface() : (size_t)S.g.ncell(); }
-
+    // Host arrays in the Arr3d layout <-> device arrays with padded rows, through the contiguous
+    // double staging buffer: one plain copy across the bus, then a kernel moves the rows (and
+    // converts for FP32 contexts, whose density fields hold rho - ro0).
     int copy_in(T *dev, const double *host, int face, double offset) {
-        if (sizeof(T) == sizeof(double)) {
-            ARK_CUDA(copy_rows(dev, host, S.g, face, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-        } else {
-            ARK_CUDA(copy_rows(ctx->stage, host, S.g, face, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-            convert_from_double<T>(dev, ctx->stage, (int64_t)padded(face), offset, ctx->st);
-        }
+        const RowShape r = row_shape(S.g, face);
+        ARK_CUDA(cudaMemcpyAsync(ctx->stage, host, sizeof(double) * r.w * r.rows, cudaMemcpyHostToDevice, ctx->st));
+        rows_from_double<T>(dev, ctx->stage, r.w, r.rows, r.pitch, offset, ctx->st);
         ARK_CUDA(cudaStreamSynchronize(ctx->st));
         return ARK_OK;
     }
 
     int copy_out(double *host, const T *dev, int face, double offset) {
-        if (sizeof(T) == sizeof(double)) {
-            ARK_CUDA(copy_rows(host, dev, S.g, face, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-        } else {
-            convert_to_double<T>(ctx->stage, dev, (int64_t)padded(face), offset, ctx->st);
-            ARK_CUDA(copy_rows(host, ctx->stage, S.g, face, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-        }
+        const RowShape r = row_shape(S.g, face);
+        rows_to_double<T>(ctx->stage, dev, r.w, r.rows, r.pitch, offset, ctx->st);
+        ARK_CUDA(cudaMemcpyAsync(host, ctx->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, ctx->st));
         ARK_CUDA(cudaStreamSynchronize(ctx->st));
         return ARK_OK;
     }
@@ -302,9 +294,9 @@ template <class T> struct EngineT : Engine {
     int download_field(int which, int face, double *host) override {
         if (Storage<T>::deviation && is_face_density(which)) {
             const int d = (which - 9) / 5;
-            face_density_to_double<T>(ctx->stage, S.fc[ctx->fcur][d].p, (int64_t)padded(1), ctx->k.ro0, ctx->k.rc2,
-                                      ctx->st);
-            ARK_CUDA(copy_rows(host, ctx->stage, S.g, 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+            const RowShape r = row_shape(S.g, 1);
+            rows_face_density<T>(ctx->stage, S.fc[ctx->fcur][d].p, r.w, r.rows, r.pitch, ctx->k.ro0, ctx->k.rc2, ctx->st);
+            ARK_CUDA(cudaMemcpyAsync(host, ctx->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, ctx->st));
             ARK_CUDA(cudaStreamSynchronize(ctx->st));
             return ARK_OK;
         }
@@ -499,11 +491,10 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     else ctx->eng.reset(new EngineT<float>(ctx.get()));
     *status = ctx->eng->alloc();
     if (*status) return nullptr;
-    if (params->precision == ARK_FP32) {
-        if (cudaMalloc(&ctx->stage, sizeof(double) * (size_t)ctx->g.nface()) != cudaSuccess) {
-            *status = fail(ARK_ERR_NOMEM, "staging allocation failed");
-            return nullptr;
-        }
+    // the transfer staging buffer: one host face array (the largest host array)
+    if (cudaMalloc(&ctx->stage, sizeof(double) * ark_face_count(params)) != cudaSuccess) {
+        *status = fail(ARK_ERR_NOMEM, "staging allocation failed");
+        return nullptr;
     }
     // Phase1 kernel shapes measured fastest on GB300 at the benchmark sizes: FP32 stages its
     // planes in shared memory (0.76 vs 1.10 ms marching and 0.61 vs 0.70 ms one cell per

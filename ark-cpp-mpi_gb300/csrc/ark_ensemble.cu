@@ -496,16 +496,18 @@ int ark_ensemble_upload(ark_ensemble *E, int q, const ark_host_state *h) {
     float *dcell[8] = {S.lv[lc].ro, S.lv[lc].u1, S.lv[lc].u2, S.lv[lc].u3,
                        S.lv[ln].ro, S.lv[ln].u1, S.lv[ln].u2, S.lv[ln].u3};
     for (int a = 0; a < 8; ++a) {
-        ENS_CUDA(copy_rows(E->stage, cells[a], S.g, 0, sizeof(double), cudaMemcpyHostToDevice, E->st));
-        convert_from_double<float>(dcell[a], E->stage, (int64_t)nc, (a % 4 == 0) ? ro0 : 0.0, E->st);
+        const RowShape r = row_shape(S.g, 0);
+        ENS_CUDA(cudaMemcpyAsync(E->stage, cells[a], sizeof(double) * r.w * r.rows, cudaMemcpyHostToDevice, E->st));
+        rows_from_double<float>(dcell[a], E->stage, r.w, r.rows, r.pitch, (a % 4 == 0) ? ro0 : 0.0, E->st);
         ENS_CUDA(cudaStreamSynchronize(E->st));
     }
     for (int d = 0; d < 3; ++d) {
         const FaceSet<float> &F = S.fc[E->fcur][d];
         float *df[4] = {F.p, F.u[0], F.u[1], F.u[2]};
         for (int a = 0; a < 4; ++a) {
-            ENS_CUDA(copy_rows(E->stage, faces[d][a], S.g, 1, sizeof(double), cudaMemcpyHostToDevice, E->st));
-            convert_from_double<float>(df[a], E->stage, (int64_t)nf, 0.0, E->st);
+            const RowShape r = row_shape(S.g, 1);
+            ENS_CUDA(cudaMemcpyAsync(E->stage, faces[d][a], sizeof(double) * r.w * r.rows, cudaMemcpyHostToDevice, E->st));
+            rows_from_double<float>(df[a], E->stage, r.w, r.rows, r.pitch, 0.0, E->st);
             ENS_CUDA(cudaStreamSynchronize(E->st));
         }
     }
@@ -545,8 +547,9 @@ int ark_ensemble_download(ark_ensemble *E, int q, ark_host_state *h) {
     float *dcell[8] = {S.lv[c].ro, S.lv[c].u1, S.lv[c].u2, S.lv[c].u3, S.lv[n].ro, S.lv[n].u1, S.lv[n].u2, S.lv[n].u3};
     for (int a = 0; a < 8; ++a) {
         if (!cells[a]) continue;
-        convert_to_double<float>(E->stage, dcell[a], (int64_t)nc, (a % 4 == 0) ? ro0 : 0.0, E->st);
-        ENS_CUDA(copy_rows(cells[a], E->stage, S.g, 0, sizeof(double), cudaMemcpyDeviceToHost, E->st));
+        const RowShape r = row_shape(S.g, 0);
+        rows_to_double<float>(E->stage, dcell[a], r.w, r.rows, r.pitch, (a % 4 == 0) ? ro0 : 0.0, E->st);
+        ENS_CUDA(cudaMemcpyAsync(cells[a], E->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, E->st));
         ENS_CUDA(cudaStreamSynchronize(E->st));
     }
     double *faces[3][5] = {{h->p1, h->ro1, h->u11, h->u21, h->u31},
@@ -557,9 +560,10 @@ int ark_ensemble_download(ark_ensemble *E, int q, ark_host_state *h) {
         const float *df[5] = {F.p, nullptr, F.u[0], F.u[1], F.u[2]};
         for (int a = 0; a < 5; ++a) {
             if (!faces[d][a]) continue;
-            if (a == 1) face_density_to_double<float>(E->stage, F.p, (int64_t)nf, E->K[q].ro0, E->K[q].rc2, E->st);
-            else convert_to_double<float>(E->stage, df[a], (int64_t)nf, 0.0, E->st);
-            ENS_CUDA(copy_rows(faces[d][a], E->stage, S.g, 1, sizeof(double), cudaMemcpyDeviceToHost, E->st));
+            const RowShape r = row_shape(S.g, 1);
+            if (a == 1) rows_face_density<float>(E->stage, F.p, r.w, r.rows, r.pitch, E->K[q].ro0, E->K[q].rc2, E->st);
+            else rows_to_double<float>(E->stage, df[a], r.w, r.rows, r.pitch, 0.0, E->st);
+            ENS_CUDA(cudaMemcpyAsync(faces[d][a], E->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, E->st));
             ENS_CUDA(cudaStreamSynchronize(E->st));
         }
     }

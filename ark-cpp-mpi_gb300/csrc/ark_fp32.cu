@@ -4,9 +4,10 @@
 
 namespace ark {
 template struct Launch<float>;
-template void convert_from_double<float>(float *, const double *, int64_t, double, cudaStream_t);
-template void convert_to_double<float>(double *, const float *, int64_t, double, cudaStream_t);
-template void face_density_to_double<float>(double *, const float *, int64_t, double, double, cudaStream_t);
+template void rows_from_double<float>(float *, const double *, int, int64_t, int, double, cudaStream_t);
+template void rows_to_double<float>(double *, const float *, int, int64_t, int, double, cudaStream_t);
+template void rows_face_density<float>(double *, const float *, int, int64_t, int, double, double, cudaStream_t);
+
 } // namespace ark
 
 // ---- host check of the staged Phase1's copy plan ----

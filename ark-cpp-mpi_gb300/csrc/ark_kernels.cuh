@@ -1754,31 +1754,47 @@ template <class T> void Launch<T>::sums(const DevState<T> &S, int ncon, cudaStre
 }
 
 // Precision conversion for FP32 contexts (host arrays are always double).
-template <class T> __global__ void k_from_double(T *dst, const double *src, int64_t n, double offset) {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-        dst[t] = (T)(src[t] - offset);
+// Host arrays reach the device through a contiguous double staging buffer (one plain copy
+// each way); these kernels move between it (rows of w elements) and the device's padded rows
+// (pitch elements), converting for FP32 contexts.  With offset 0 FP64 values are copied as
+// they are.
+template <class T> __global__ void k_rows_in(T *dst, const double *src, int w, int64_t rows, int pitch, double offset) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w) return;
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+        const double v = src[r * w + c];
+        dst[r * pitch + c] = (T)(offset == 0.0 ? v : v - offset);
+    }
 }
-template <class T> __global__ void k_to_double(double *dst, const T *src, int64_t n, double offset) {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-        dst[t] = (double)src[t] + offset;
+template <class T> __global__ void k_rows_out(double *dst, const T *src, int w, int64_t rows, int pitch, double offset) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w) return;
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+        const double v = (double)src[r * pitch + c];
+        dst[r * w + c] = offset == 0.0 ? v : v + offset;
+    }
 }
 template <class T>
-__global__ void k_face_density(double *dst, const T *p, int64_t n, double ro0, double rc2) {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-        dst[t] = ro0 + (double)p[t] * rc2;
+__global__ void k_rows_face_density(double *dst, const T *p, int w, int64_t rows, int pitch, double ro0, double rc2) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w) return;
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) dst[r * w + c] = ro0 + (double)p[r * pitch + c] * rc2;
+}
+inline dim3 rows_grid(int w, int64_t rows) {
+    return dim3((w + 127) / 128, (unsigned)(rows < 16384 ? (rows < 1 ? 1 : rows) : 16384));
 }
 
 template <class T>
-void convert_from_double(T *dst, const double *src, int64_t n, double offset, cudaStream_t st) {
-    k_from_double<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, n, offset);
+void rows_from_double(T *dst, const double *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st) {
+    k_rows_in<T><<<rows_grid(w, rows), 128, 0, st>>>(dst, src, w, rows, pitch, offset);
 }
 template <class T>
-void convert_to_double(double *dst, const T *src, int64_t n, double offset, cudaStream_t st) {
-    k_to_double<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, n, offset);
+void rows_to_double(double *dst, const T *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st) {
+    k_rows_out<T><<<rows_grid(w, rows), 128, 0, st>>>(dst, src, w, rows, pitch, offset);
 }
 template <class T>
-void face_density_to_double(double *dst, const T *p, int64_t n, double ro0, double rc2, cudaStream_t st) {
-    k_face_density<T><<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, p, n, ro0, rc2);
+void rows_face_density(double *dst, const T *p, int w, int64_t rows, int pitch, double ro0, double rc2, cudaStream_t st) {
+    k_rows_face_density<T><<<rows_grid(w, rows), 128, 0, st>>>(dst, p, w, rows, pitch, ro0, rc2);
 }
 
 } // namespace ark

@@ -263,15 +263,28 @@ long long closure_count(int C1, int C2, int C3, int sx, int sz, int ox, int oz);
 // div_rn against the hardware division on n random operand pairs (mismatches added to *bad)
 void selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st);
 
-// double <-> T copies for FP32 contexts (host arrays are always double):
-// dst = (T)(src - offset) and dst = (double)src + offset.
+// Between a contiguous double staging buffer (rows of w values) and the device's padded rows
+// (pitch): dst = (T)(src - offset), dst = (double)src + offset, and for FP32 contexts the face
+// density dst = ro0 + (double)p * rc2.
 template <class T>
-void convert_from_double(T *dst, const double *src, int64_t n, double offset, cudaStream_t st);
+void rows_from_double(T *dst, const double *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st);
 template <class T>
-void convert_to_double(double *dst, const T *src, int64_t n, double offset, cudaStream_t st);
-// face density of an FP32 context: dst = ro0 + (double)p * rc2
+void rows_to_double(double *dst, const T *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st);
 template <class T>
-void face_density_to_double(double *dst, const T *p, int64_t n, double ro0, double rc2, cudaStream_t st);
+void rows_face_density(double *dst, const T *p, int w, int64_t rows, int pitch, double ro0, double rc2, cudaStream_t st);
+// the row shape of a cell (face = 0) or face (1) array: w values per row, rows, pitch
+struct RowShape {
+    int w;
+    int64_t rows;
+    int pitch;
+};
+inline RowShape row_shape(const Geom &dg, int face) {
+    RowShape r;
+    r.w = face ? dg.C1 + 3 : dg.C1 + 2;
+    r.rows = face ? (int64_t)(dg.C2 + 3) * (dg.C3 + 3) : (int64_t)(dg.C2 + 2) * (dg.C3 + 2);
+    r.pitch = (int)(face ? dg.fs1 : dg.cs1);
+    return r;
+}
 
 } // namespace ark
 
