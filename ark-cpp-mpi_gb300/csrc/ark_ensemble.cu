@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(128) kb_wrap(const DS *__restrict__ inst, cons
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
         const BIx bx = decode(W, q, b);
-        wrap_body<float>(inst[q].g, jobs[q], (int64_t)bx.x * 128 + threadIdx.x);
+        wrap_body_lines<float>(inst[q].g, jobs[q], (int64_t)bx.x * 128 + threadIdx.x);
     }
 }
 
@@ -177,7 +177,7 @@ template <class U> int ens_alloc(ark_ensemble *E, U **out, size_t n) {
     return ARK_OK;
 }
 
-Geom geom_of(const ark_params &p) { return device_geom(p.n1_cells, p.n2_cells, p.n3_cells); }
+Geom geom_of(const ark_params &p) { return device_geom(p.n1_cells, p.n2_cells, p.n3_cells, false); }
 
 int alloc_member(ark_ensemble *E, DS &S) {
     const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
@@ -235,8 +235,8 @@ int build_lists(ark_ensemble *E) {
                 gx = (g.C1 + 127) / 128, gy = g.C2, gz = (g.C3 + 1 + seg - 1) / seg;
                 break;
             }
-            case WL_WRAP: { // every line of up to 16 arrays (the longest ghost-fill job)
-                const int64_t tot = ((int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2) * 16;
+            case WL_WRAP: { // one thread per ghost line, looping over the job's arrays
+                const int64_t tot = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
                 gx = (int)((tot + 127) / 128);
                 break;
             }

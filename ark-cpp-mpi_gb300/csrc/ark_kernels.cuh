@@ -332,13 +332,10 @@ struct WrapJob {
 //   GH_COPY (bounded axis): zero-gradient ghost 0 <- cell 1, ghost C+1 <- cell C; faces:
 //           halo 0 <- face 1, halo C+2 <- face C+1 (main.cpp:803-845, 1633-1698);
 // over the interior of the other two axes.
-// Thread t copies the two ghosts of one line of one array: arrays q = t / (lines), lines
-// first the (j, k) lines of x, then the (i, j) lines of z.
-template <class T> __device__ __forceinline__ void wrap_body(const Geom &g, const WrapJob &J, int64_t t) {
-    const int64_t nx = (int64_t)g.C2 * g.C3, nz = (int64_t)g.C1 * g.C2, nl = nx + nz;
-    const int q = (int)(t / nl);
-    if (q >= J.n) return;
-    const int64_t r = t - (int64_t)q * nl;
+// The two ghosts of line r of array q: lines first the (j, k) lines of x, then the (i, j)
+// lines of z.
+template <class T> __device__ __forceinline__ void wrap_copy(const Geom &g, const WrapJob &J, int q, int64_t r) {
+    const int64_t nx = (int64_t)g.C2 * g.C3;
     T *a = (T *)J.a[q];
     if (r < nx) {
         const uint8_t m = J.mode[q][0];
@@ -364,6 +361,22 @@ template <class T> __device__ __forceinline__ void wrap_body(const Geom &g, cons
             a[g.cell(i, j, g.C3 + 1)] = a[g.cell(i, j, m == GH_WRAP ? 1 : g.C3)];
         }
     }
+}
+
+// Thread t copies line t mod (lines) of array t / (lines).
+template <class T> __device__ __forceinline__ void wrap_body(const Geom &g, const WrapJob &J, int64_t t) {
+    const int64_t nl = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
+    const int q = (int)(t / nl);
+    if (q >= J.n) return;
+    wrap_copy<T>(g, J, q, t - (int64_t)q * nl);
+}
+
+// The same copies with one thread per line looping over the arrays (the ensemble's batched
+// ghost fill, whose parallelism comes from the members).
+template <class T> __device__ __forceinline__ void wrap_body_lines(const Geom &g, const WrapJob &J, int64_t t) {
+    const int64_t nl = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
+    if (t >= nl) return;
+    for (int q = 0; q < J.n; ++q) wrap_copy<T>(g, J, q, t);
 }
 
 template <class T> __global__ void k_wrap(Geom g, const __grid_constant__ WrapJob J) {

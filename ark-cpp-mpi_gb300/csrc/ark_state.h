@@ -58,9 +58,11 @@ inline int device_pitch(int C1) {
     const int need = C1 + 3 > need_seg ? C1 + 3 : need_seg;
     return (need + kRowAlign - 1) / kRowAlign * kRowAlign;
 }
-inline Geom device_geom(int C1, int C2, int C3) {
+// staged = false: rows only aligned (a multiple of 32 elements, at least C1 + 3), for arrays the
+// shared-memory-staged kernels never read (ensemble members)
+inline Geom device_geom(int C1, int C2, int C3, bool staged = true) {
     Geom g = host_geom(C1, C2, C3);
-    const int P = device_pitch(C1);
+    const int P = staged ? device_pitch(C1) : (C1 + 3 + kRowAlign - 1) / kRowAlign * kRowAlign;
     g.cs1 = P;
     g.cs2 = (int64_t)P * (C2 + 2);
     g.fs1 = P;
