@@ -414,9 +414,9 @@ class Context:
 
     def autotune(self, steps_per_candidate=3):
         """Pick the fastest kernel shapes on the live state (which advances)."""
-        c = (ctypes.c_int * 4)()
+        c = (ctypes.c_int * 5)()
         self._call("ark_autotune", int(steps_per_candidate), c)
-        return {"phase1_stress": c[0], "phase1": c[1], "segment": c[2], "us_per_step": c[3]}
+        return {"phase1_stress": c[0], "phase1": c[1], "segment": c[2], "us_per_step": c[3], "phase2_fused": c[4]}
 
     def set_closure(self, mlp, u_tau=0.0):
         """Turn the learned closure on (mlp: an Mlp) or off (None) for ark_step."""

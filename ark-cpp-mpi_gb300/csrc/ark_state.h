@@ -202,6 +202,8 @@ template <class T> struct Launch {
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
     // x2/x3 sweeps: lines cut into balanced segments of at most `target` faces
     static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target = 32);
+    // the three sweeps in one kernel (same results)
+    static void phase2_fused(const DevState<T> &S, int con, int fcur, cudaStream_t st);
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
     static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);

@@ -298,9 +298,11 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
 
 /* Times the kernel shapes of the step on the live state (it advances) and keeps the fastest,
  * one setting at a time: the shape of the Phase1 with stress (0 one cell per thread, 1
- * marching, 2 staged in shared memory, FP32 only), of the second Phase1, and the x2/x3 sweep
- * segment length (8, 16, 32, 64 faces).  The results do not depend on the shapes.  choice (4
- * ints, may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step}. */
+ * marching, 2 staged in shared memory (FP32), 3 face quantities computed once (FP64)), of the
+ * second Phase1, and the x2/x3 sweeps' segment length (8, 16, 32, 64 faces), each candidate
+ * timed three times (best kept).  The results do not depend on the shapes.  choice (5 ints,
+ * may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step, fused Phase2
+ * (set by ARK_PHASE2_FUSED=1 only)}. */
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice);
 
 /* ---- ensembles: many independent channels in one launch per phase ------------------------

@@ -389,3 +389,25 @@ def test_autotune_keeps_results(ark, port, prec):
         ra, rb = a.download(CELLS + FACES), b.download(CELLS + FACES)
         for name in CELLS + FACES:
             assert bits_equal(ra[name], rb[name]), name
+
+
+@pytest.mark.parametrize("C,px,pz", [((40, 20, 36), True, True), ((130, 9, 70), True, True), ((70, 6, 5), False, False),
+                                     ((64, 4, 1), True, False)])
+def test_fused_phase2_agrees(ark, port, monkeypatch, C, px, pz):
+    """The three sweeps fused in one kernel (ARK_PHASE2_FUSED) give the bits of the separate
+    sweeps in both precisions, periodic and bounded axes, ragged tiles."""
+    p = port.channel_params(*C, seed=23)
+    st0 = port.channel_state(p)
+    for prec in (ark.FP64, ark.FP32):
+        outs = []
+        for fused in ("0", "1"):
+            monkeypatch.setenv("ARK_PHASE2_FUSED", fused)
+            P = params_from(ark, p, precision=prec)
+            P.periodic_x, P.periodic_z = int(px), int(pz)
+            with ark.Context(P) as c:
+                c.upload(st0)
+                c.step(4)
+                c.sync()
+                outs.append(c.download(CELLS + FACES))
+        for n in CELLS + FACES:
+            assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), (prec, n)
