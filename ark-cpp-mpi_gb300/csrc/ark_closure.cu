@@ -649,8 +649,16 @@ __device__ __forceinline__ void stage_net(NetSmem &sm, const Net *__restrict__ n
     __syncthreads();
 }
 
+// Run constants of the inference in FP32, computed once on the host (no FP64 per cell).
+struct NutConst {
+    float rdx2[3];   // 1 / (2 dx_d)
+    float ly, dy;    // channel height, cell height
+    float vis;       // nu
+    float yplus;     // u_tau / nu
+};
+
 template <class T> __global__ void __launch_bounds__(128)
-    k_nut(const __grid_constant__ DevState<T> S, int lvl, const Net *__restrict__ netd, float yplus_scale) {
+    k_nut(const __grid_constant__ DevState<T> S, int lvl, const Net *__restrict__ netd, const NutConst K) {
     __shared__ __align__(16) __nv_bfloat16 X[4][32 * 16];
     __shared__ NetSmem net;
     stage_net(net, netd);
@@ -661,8 +669,6 @@ template <class T> __global__ void __launch_bounds__(128)
     const Level<T> L = S.lv[lvl];
     const int nx = g.C1 + 2, nz = g.C3 + 2;
     const int n = nx * g.C2 * nz;
-    const float rdx2[3] = {(float)(0.5 / S.k.dx[0]), (float)(0.5 / S.k.dx[1]), (float)(0.5 / S.k.dx[2])};
-    const float ly = (float)(S.k.dx[1] * g.C2);
     const int nwarps = gridDim.x * 4;
     // warp-uniform loop: every lane of a warp takes part in each multiply
     for (int base = (blockIdx.x * 4 + wid) * 32; base < n; base += nwarps * 32) {
@@ -684,23 +690,26 @@ template <class T> __global__ void __launch_bounds__(128)
             const int km = k > 1 ? k - 1 : (S.k.periodic_z ? g.C3 : 1), kp = k < g.C3 ? k + 1 : (S.k.periodic_z ? 1 : g.C3);
             const int64_t nb[6] = {g.cell(im, j, k), g.cell(ip, j, k), c - g.cs1, c + g.cs1, g.cell(i, j, km), g.cell(i, j, kp)};
             const T *u[3] = {L.u1, L.u2, L.u3};
+            bool solid[6];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) solid[q] = (S.flags[nb[q]] & FL_GT) != 0;
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
                 const float uc = (float)u[m][c];
                 float v[6];
 #pragma unroll
-                for (int q = 0; q < 6; ++q) v[q] = (S.flags[nb[q]] & FL_GT) ? -uc : (float)u[m][nb[q]];
-                A[m][0] = (v[1] - v[0]) * rdx2[0];
-                A[m][1] = (v[3] - v[2]) * rdx2[1];
-                A[m][2] = (v[5] - v[4]) * rdx2[2];
+                for (int q = 0; q < 6; ++q) v[q] = solid[q] ? -uc : (float)u[m][nb[q]];
+                A[m][0] = (v[1] - v[0]) * K.rdx2[0];
+                A[m][1] = (v[3] - v[2]) * K.rdx2[1];
+                A[m][2] = (v[5] - v[4]) * K.rdx2[2];
             }
-            const float y = -0.5f * ly + ((float)j - 0.5f) * (float)S.k.dx[1];
-            features_of<float>(A, y, ly, yplus_scale, f);
+            const float y = -0.5f * K.ly + ((float)j - 0.5f) * K.dy;
+            features_of<float>(A, y, K.ly, K.yplus, f);
 #pragma unroll
             for (int q = 0; q < NIN; ++q) f[q] = (f[q] - net.mu[q]) * net.rsd[q];
         }
         const float y_nu = tc_warp(w, B, X[wid], f, lane);
-        if (live) S.nut[g.cell(ig, j, kg)] = fluid ? (T)(y_nu * (float)S.k.vis) : (T)0;
+        if (live) S.nut[g.cell(ig, j, kg)] = fluid ? (T)(y_nu * K.vis) : (T)0;
     }
 }
 
@@ -732,7 +741,13 @@ int grid_for(long long n, int threads = 256) {
 
 template <class T> void closure_nut(const DevState<T> &S, int lvl, const void *net, float yplus_scale, cudaStream_t st) {
     const long long n = (long long)(S.g.C1 + 2) * S.g.C2 * (S.g.C3 + 2);
-    cl::k_nut<T><<<cl::grid_for(n, 128), 128, 0, st>>>(S, lvl, (const cl::Net *)net, yplus_scale);
+    cl::NutConst K;
+    for (int d = 0; d < 3; ++d) K.rdx2[d] = (float)(0.5 / S.k.dx[d]);
+    K.ly = (float)(S.k.dx[1] * S.g.C2);
+    K.dy = (float)S.k.dx[1];
+    K.vis = (float)S.k.vis;
+    K.yplus = yplus_scale;
+    cl::k_nut<T><<<cl::grid_for(n, 128), 128, 0, st>>>(S, lvl, (const cl::Net *)net, K);
 }
 template void closure_nut<float>(const DevState<float> &, int, const void *, float, cudaStream_t);
 template void closure_nut<double>(const DevState<double> &, int, const void *, float, cudaStream_t);
