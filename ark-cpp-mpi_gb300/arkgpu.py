@@ -29,7 +29,7 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_time_step_size", "ark_phase1", "ark_stress_tensor", "ark_use_forces", "ark_phase2",
            "ark_boundary_fill", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
            "ark_get_scalars", "ark_set_scalars", "ark_conservation_sums", "ark_channel_init",
-           "ark_kernel_times", "ark_kernel_name", "ark_alloc_host_state", "ark_free_host_state",
+           "ark_kernel_times", "ark_kernel_name", "ark_step_kernel_name", "ark_alloc_host_state", "ark_free_host_state",
            "ark_conservation_sums_noalloc", "ark_mean_profile", "ark_selftest_division",
            "ark_ensemble_create", "ark_ensemble_destroy", "ark_ensemble_last_error", "ark_ensemble_size",
            "ark_ensemble_upload", "ark_ensemble_download", "ark_ensemble_step", "ark_ensemble_sync",
@@ -126,6 +126,8 @@ def lib():
         L.ark_kernel_times.argtypes = [vp, ctypes.c_int, _DP, ctypes.c_int, ip]
         L.ark_kernel_name.restype = ctypes.c_char_p
         L.ark_kernel_name.argtypes = [ctypes.c_int]
+        L.ark_step_kernel_name.restype = ctypes.c_char_p
+        L.ark_step_kernel_name.argtypes = [vp, ctypes.c_int]
         L.ark_alloc_host_state.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(HostState)]
         L.ark_free_host_state.argtypes = [ctypes.POINTER(HostState)]
         L.ark_mean_profile.argtypes = [vp, _DP, _DP]
@@ -363,7 +365,7 @@ class Context:
         ms = (ctypes.c_double * 32)()
         cnt = ctypes.c_int(0)
         self._call("ark_kernel_times", int(nsteps), ms, 32, ctypes.byref(cnt))
-        return [(lib().ark_kernel_name(q).decode(), ms[q]) for q in range(cnt.value)]
+        return [(lib().ark_step_kernel_name(self.h, q).decode(), ms[q]) for q in range(cnt.value)]
 
     def upload_struct(self, h: HostState):
         self._call("ark_upload", ctypes.byref(h))
@@ -416,7 +418,8 @@ class Context:
         """Pick the fastest kernel shapes on the live state (which advances)."""
         c = (ctypes.c_int * 5)()
         self._call("ark_autotune", int(steps_per_candidate), c)
-        return {"phase1_stress": c[0], "phase1": c[1], "segment": c[2], "us_per_step": c[3], "phase2_fused": c[4]}
+        # phase2_form: 0 three sweep kernels, 1 one sweep kernel, 2 sweeps + second Phase1 in one kernel
+        return {"phase1_stress": c[0], "phase1": c[1], "segment": c[2], "us_per_step": c[3], "phase2_form": c[4]}
 
     def set_closure(self, mlp, u_tau=0.0):
         """Turn the learned closure on (mlp: an Mlp) or off (None) for ark_step."""

@@ -150,6 +150,13 @@ struct Engine {
     virtual void energy(int ncon, double *scratch, double *out) = 0;
     virtual DevScalars *scalars() = 0;
     virtual uint8_t *flags() = 0;
+    // launches of one step in the current configuration, and their names
+    virtual int step_launches() = 0;
+    virtual const char *step_kernel_name(int q) = 0;
+    // after each step: the level the step wrote into the spare takes the place of "nCon"
+    virtual void after_step(int con) = 0;
+    // identity of the cell-level buffers (0, 1: the two levels, 2: the spare), for graph reuse
+    virtual const void *level_ptr(int l) = 0;
 };
 
 } // namespace
@@ -172,6 +179,7 @@ struct ark_ctx {
     bool parts_valid = false; // the dt / bulk-flow partials describe the current state
     int march[2] = {1, 0};    // Phase1 kernel shape of the two Phase1 launches of a step
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [con][fcur]
+    const void *graph_levels[2][2][3] = {};  // the level buffers each graph was captured with
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double *stage = nullptr; // contiguous double staging for host transfers
     AvgArrays avg = {{nullptr, nullptr, nullptr}}; // averageU1..3 (FP64, reference layout)
@@ -181,7 +189,8 @@ struct ark_ctx {
     cudaEvent_t fork = nullptr, join = nullptr;
     float closure_scale = 0.f;            // u_tau / vis for the y+ feature
     int seg_target = 32;                  // x2/x3 sweep segment length (faces)
-    int p2fused = 0;                      // 1: the three sweeps as one kernel
+    int p2mode = 0; // Phase2: 0 three sweep kernels, 1 one kernel for the three sweeps, 2 (FP32)
+                    // one kernel for the three sweeps and the second Phase1
     // output streaming: two device and two pinned host slab buffers of io_cap doubles
     double *io_dev[2] = {nullptr, nullptr};
     double *io_host[2] = {nullptr, nullptr};
@@ -220,6 +229,12 @@ template <class T> struct EngineT : Engine {
             rc |= get(&S.lv[l].u1, nc);
             rc |= get(&S.lv[l].u2, nc);
             rc |= get(&S.lv[l].u3, nc);
+        }
+        if (Storage<T>::deviation) { // FP32: the level the one-kernel Phase2 + second Phase1 writes
+            rc |= get(&S.spare.ro, nc);
+            rc |= get(&S.spare.u1, nc);
+            rc |= get(&S.spare.u2, nc);
+            rc |= get(&S.spare.u3, nc);
         }
         for (int m = 0; m < 3; ++m) rc |= get(&S.f[m], nc);
         for (int gen = 0; gen < 2; ++gen)
@@ -387,7 +402,19 @@ template <class T> struct EngineT : Engine {
         mark(2);
         Launch<T>::wrap_phase2(S, y, fcur, st);
         mark(3);
-        if (ctx->p2fused) { // one kernel for the three sweeps: timed in the first sweep's slot
+        if (use_step2()) {
+            // Phase2 and the second Phase1 in one kernel; the new level goes to the spare, which
+            // after_step swaps in as "nCon"
+            Launch<T>::phase2_phase1(S, y, fcur, S.spare, st);
+            mark(4);
+            if (ctx->averaging) {
+                DevState<T> Sn = S;
+                Sn.lv[y] = S.spare;
+                output_average_add<T>(Sn, y, ctx->avg, st);
+            }
+            return;
+        }
+        if (ctx->p2mode == 1) { // one kernel for the three sweeps: timed in the first sweep's slot
             Launch<T>::phase2_fused(S, y, fcur, st);
             for (int ax = 0; ax < 3; ++ax) mark(4 + ax);
         } else {
@@ -414,6 +441,16 @@ template <class T> struct EngineT : Engine {
     void energy(int ncon, double *scratch, double *out) override { output_energy<T>(S, ncon, scratch, out, ctx->st); }
     DevScalars *scalars() override { return S.sc; }
     uint8_t *flags() override { return S.flags; }
+    bool use_step2() const { return ctx->p2mode == 2 && S.spare.ro; }
+    int step_launches() override { return use_step2() ? 5 : kNumStepKernels; }
+    const char *step_kernel_name(int q) override {
+        if (q < 0 || q >= step_launches()) return "";
+        return use_step2() && q == 4 ? "phase2_phase1_forces" : kStepKernels[q];
+    }
+    void after_step(int con) override {
+        if (use_step2()) std::swap(S.lv[con ^ 1], S.spare);
+    }
+    const void *level_ptr(int l) override { return l < 2 ? (const void *)S.lv[l].ro : (const void *)S.spare.ro; }
 };
 
 int check_params(const ark_params *p) {
@@ -516,7 +553,7 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
         if (e[0] && ok(e[1])) ctx->march[1] = e[1] - '0';
     }
     if (const char *e = std::getenv("ARK_PHASE2_FUSED"))
-        if (e[0] == '0' || e[0] == '1') ctx->p2fused = e[0] - '0';
+        if (e[0] >= '0' && e[0] <= '2' && (e[0] != '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
     Launch<float>::prepare();
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
@@ -729,10 +766,19 @@ int ark_set_dt(ark_ctx *ctx, double dt) {
     return ARK_OK;
 }
 
-// Captures the fused step for the current role of the two cell levels (once per role).
+// Captures the fused step for the current role of the two cell levels (once per role).  A graph
+// holds the level buffers it was captured with; when the one-kernel Phase2 + second Phase1
+// rotates them through the spare, each face generation meets its own buffers again every
+// other step, and a graph that meets other buffers is captured again.
 static int ensure_graph(ark_ctx *ctx) {
     const int x = ctx->con, fc = ctx->fcur;
+    const void *lv[3] = {ctx->eng->level_ptr(0), ctx->eng->level_ptr(1), ctx->eng->level_ptr(2)};
+    if (ctx->graph[x][fc] && std::memcmp(ctx->graph_levels[x][fc], lv, sizeof lv) != 0) {
+        cudaGraphExecDestroy(ctx->graph[x][fc]);
+        ctx->graph[x][fc] = nullptr;
+    }
     if (!ctx->graph[x][fc]) {
+        std::memcpy(ctx->graph_levels[x][fc], lv, sizeof lv);
         cudaGraph_t graph = nullptr;
         ARK_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
         ctx->eng->step(x, fc, nullptr);
@@ -766,6 +812,7 @@ int ark_step(ark_ctx *ctx, int nsteps) {
         if (int rc = ensure_graph(ctx)) return rc;
         ARK_CUDA(cudaGraphLaunch(ctx->graph[ctx->con][ctx->fcur], ctx->st));
         ctx->fcur ^= 1;
+        ctx->eng->after_step(ctx->con);
     }
     return ARK_OK;
 }
@@ -782,11 +829,14 @@ int ark_sync(ark_ctx *ctx) {
 int ark_time_steps(ark_ctx *ctx, int nsteps, double *ms) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (!ms) return fail(ARK_ERR_PARAM, "ms is NULL");
-    // both face-generation graphs are built outside the timed region
+    // both face-generation graphs are built outside the timed region (each with the level
+    // buffers the step will meet; after_step is its own inverse)
     if (int rc = ensure_graph(ctx)) return rc;
     ctx->fcur ^= 1;
+    ctx->eng->after_step(ctx->con);
     int rc2 = ensure_graph(ctx);
     ctx->fcur ^= 1;
+    ctx->eng->after_step(ctx->con);
     if (rc2) return rc2;
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
     ARK_CUDA(cudaEventRecord(ctx->ev0, ctx->st));
@@ -802,7 +852,8 @@ int ark_time_steps(ark_ctx *ctx, int nsteps, double *ms) {
 int ark_kernel_times(ark_ctx *ctx, int nsteps, double *ms, int cap, int *count) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (!ms || !count || nsteps < 1) return fail(ARK_ERR_PARAM, "bad arguments");
-    *count = kNumStepKernels;
+    const int nk = ctx->eng->step_launches();
+    *count = nk;
     std::vector<cudaEvent_t> ev(kNumStepKernels + 1);
     for (auto &e : ev) ARK_CUDA(cudaEventCreate(&e));
     std::vector<double> acc(kNumStepKernels, 0.0);
@@ -815,25 +866,31 @@ int ark_kernel_times(ark_ctx *ctx, int nsteps, double *ms, int cap, int *count) 
         cudaEventRecord(ev[0], ctx->st);
         ctx->eng->step(ctx->con, ctx->fcur, ev.data() + 1);
         ctx->fcur ^= 1;
+        ctx->eng->after_step(ctx->con);
         if ((rc = launch_status(ctx))) break;
-        if (cudaEventSynchronize(ev[kNumStepKernels]) != cudaSuccess) {
+        if (cudaEventSynchronize(ev[nk]) != cudaSuccess) {
             rc = fail(ARK_ERR_CUDA, "event synchronize failed");
             break;
         }
-        for (int q = 0; q < kNumStepKernels; ++q) {
+        for (int q = 0; q < nk; ++q) {
             float f = 0.f;
             cudaEventElapsedTime(&f, ev[q], ev[q + 1]);
             acc[q] += f;
         }
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    for (int q = 0; q < kNumStepKernels && q < cap; ++q) ms[q] = acc[q] / nsteps;
+    for (int q = 0; q < nk && q < cap; ++q) ms[q] = acc[q] / nsteps;
     if (rc) return rc;
     return ark_sync(ctx);
 }
 
 const char *ark_kernel_name(int index) {
     return index >= 0 && index < kNumStepKernels ? kStepKernels[index] : nullptr;
+}
+
+const char *ark_step_kernel_name(ark_ctx *ctx, int index) {
+    if (!ctx || !ctx->eng || index < 0 || index >= ctx->eng->step_launches()) return nullptr;
+    return ctx->eng->step_kernel_name(index);
 }
 
 int ark_alloc_host_state(const ark_params *p, ark_host_state *out) {
@@ -1152,19 +1209,22 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     if (int rc = measure(&best)) return rc;
     auto set = [&](int which, int v) {
         if (which < 2) ctx->march[which] = v;
-        else if (which == 2) ctx->p2fused = v;
+        else if (which == 2) ctx->p2mode = v;
         else ctx->seg_target = v;
     };
+    const bool fp32 = ctx->P.precision == ARK_FP32;
     for (int which = 0; which < 4; ++which) {
         const int segs[4] = {8, 16, 32, 64};
-        // the fused Phase2 is correct but slower at every size measured (it is latency-bound):
-        // left to ARK_PHASE2_FUSED, not tried here
-        if (which == 2) continue;
-        const int ncand = which < 2 ? 3 : 4;
-        int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2fused : ctx->seg_target;
-        if (which == 3 && ctx->p2fused) continue; // the fused Phase2 has no segments
+        // Phase2 forms: the three sweep kernels, or (FP32) one kernel for the sweeps and the
+        // second Phase1.  The one-kernel Phase2 alone (mode 1) is correct but slower at every
+        // size measured: left to ARK_PHASE2_FUSED=1, not tried here.
+        const int p2cand[2] = {0, 2};
+        if (which == 2 && !fp32) continue;
+        const int ncand = which < 2 ? 3 : which == 2 ? 2 : 4;
+        int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : ctx->seg_target;
+        if (which == 3 && ctx->p2mode) continue; // the one-kernel forms have no segments
         for (int c = 0; c < ncand; ++c) {
-            const int v = which < 2 ? shapes[c] : which == 2 ? c : segs[c];
+            const int v = which < 2 ? shapes[c] : which == 2 ? p2cand[c] : segs[c];
             if (v == keep) continue;
             set(which, v);
             double us = 0.0;
@@ -1183,7 +1243,7 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         choice[1] = ctx->march[1];
         choice[2] = ctx->seg_target;
         choice[3] = (int)std::lround(best);
-        choice[4] = ctx->p2fused;
+        choice[4] = ctx->p2mode;
     }
     return ARK_OK;
 }

@@ -159,20 +159,193 @@ template <int MODE> struct PlanCheck {
     }
 };
 
+// The copy plan of the one-kernel Phase2 + second Phase1 (s2), checked the same way: every
+// copy, then every shared-memory read the kernel makes (the thread's own cell for the three
+// sweeps, the halo jobs, the old tangential face values, the bounded-x edge flag) against the
+// element of the global arrays that the separate sweep kernels read for it.
+struct Plan2Check {
+    enum { B_CELL = 0, B_FL = 8, B_FX = 9, B_FY = 13, B_N = 17 };
+    const Geom g;
+    long long size[B_N];
+    std::string err;
+    int bad = 0;
+    explicit Plan2Check(const Geom &gg) : g(gg) {
+        for (int a = 0; a < B_N; ++a) size[a] = a < B_FL ? g.ncell() * 4 : (a == B_FL ? g.ncell() : g.nface() * 4);
+    }
+    void fail(const char *what, int bx, int by, int p, long long x) {
+        if (bad++ == 0) {
+            char b[256];
+            std::snprintf(b, sizeof b, "phase2+phase1 tile (%d,%d) plane %d: %s (%lld)", bx, by, p, what, x);
+            err = b;
+        }
+    }
+    static long long addr(int a, long long e, int elem) { return a * kSpan + e * elem; }
+    void run(int kch) {
+        using namespace s2;
+        const dim3 grd = s2::grid(g, kch);
+        s2::Bases b;
+        for (int q = 0; q < 8; ++q) b.cell[q] = (const void *)((B_CELL + q) * kSpan);
+        b.fl = (const void *)(B_FL * kSpan);
+        for (int a = 0; a < 4; ++a) {
+            b.fx[a] = (const void *)((B_FX + a) * kSpan);
+            b.fy[a] = (const void *)((B_FY + a) * kSpan);
+        }
+        stg::Group G[s2::kMaxGroups];
+        std::vector<std::vector<long long>> map;
+        for (int bz = 0; bz < (int)grd.z; ++bz)
+            for (int by = 0; by < (int)grd.y; ++by)
+                for (int bx = 0; bx < (int)grd.x; ++bx) {
+                    const int n = s2::build_groups(G, g, b, bx, by);
+                    if (n > s2::kMaxGroups) {
+                        fail("too many groups", bx, by, 0, n);
+                        continue;
+                    }
+                    stg::Row fr[stg::kMaxRows], gr[stg::kMaxFlagRows];
+                    int nfr = 0, ngr = 0;
+                    stg::expand_rows(G, n, fr, nfr, gr, ngr);
+                    if (nfr > stg::kMaxRows || ngr > stg::kMaxFlagRows) fail("too many rows", bx, by, 0, nfr);
+                    const int k0 = bz * kch + 1, k1 = std::min(k0 + kch - 1, g.C3);
+                    const int pfirst = k0 - 1, plast = k1 + 1;
+                    map.assign(plast - pfirst + 1, std::vector<long long>(STAGE, -1));
+                    for (int p = pfirst; p <= plast; ++p) {
+                        const unsigned kind = (p < k0 || p > k1) ? EDGE : MID;
+                        std::vector<long long> &M = map[p - pfirst];
+                        unsigned total = 0;
+                        for (int fg = 0; fg < 2; ++fg)
+                            for (int R = 0; R < (fg ? ngr : nfr); ++R) {
+                                const stg::Row &w = fg ? gr[R] : fr[R];
+                                if (!((w.dw >> 24) & kind)) continue;
+                                const int chunks = fg ? stg::kFlagChunks : stg::kChunks;
+                                for (int c = 0; c < chunks; ++c) {
+                                    const long long src = (long long)w.src + (long long)p * w.plane + 16 * c;
+                                    const long long dst = (w.dw & 0xFFFFFFu) + 16ll * c;
+                                    const int arr = (int)(src / kSpan);
+                                    const long long off = src % kSpan;
+                                    total += 16;
+                                    if (arr < 0 || arr >= B_N) {
+                                        fail("copy from no array", bx, by, p, src);
+                                        continue;
+                                    }
+                                    if (src % 16 || dst % 16) fail("unaligned copy", bx, by, p, src);
+                                    if (off < 0 || off + 16 > size[arr]) fail("copy outside its array", bx, by, p, off);
+                                    if (dst < 0 || dst + 16 > STAGE) fail("copy outside its stage", bx, by, p, dst);
+                                    for (int y = 0; y < 16 && dst + y < STAGE; ++y) {
+                                        if (M[dst + y] != -1) fail("two copies into one byte", bx, by, p, dst + y);
+                                        M[dst + y] = src + y;
+                                    }
+                                }
+                            }
+                        if (total != stg::plan_bytes(G, n, kind)) fail("byte count", bx, by, p, total);
+                    }
+                    reads(map, pfirst, k0, k1, bx, by);
+                }
+    }
+    void want(const std::vector<std::vector<long long>> &map, int pfirst, int bx, int by, int p, int off_bytes,
+              int nbytes, long long expect) {
+        if (p - pfirst < 0 || p - pfirst >= (int)map.size()) {
+            fail("read of a plane not staged", bx, by, p, off_bytes);
+            return;
+        }
+        const std::vector<long long> &M = map[p - pfirst];
+        for (int y = 0; y < nbytes; ++y)
+            if (off_bytes + y >= s2::STAGE || M[off_bytes + y] != expect + y) {
+                fail("shared-memory read maps to the wrong element", bx, by, p, off_bytes);
+                return;
+            }
+    }
+    // all eight cell values and the flag of cell (ic, jc) read at stage row r, column x
+    void cell_at(const std::vector<std::vector<long long>> &map, int pfirst, int bx, int by, int p, int r, int x,
+                 int ic, int jc) {
+        for (int q = 0; q < 8; ++q)
+            want(map, pfirst, bx, by, p, s2::off_cell(q, r, x) * 4, 4, addr(B_CELL + q, g.cell(ic, jc, p), 4));
+        want(map, pfirst, bx, by, p, s2::off_flag(r, x), 1, addr(B_FL, g.cell(ic, jc, p), 1));
+    }
+    void fx_at(const std::vector<std::vector<long long>> &map, int pfirst, int bx, int by, int p, int r, int x, int ic,
+               int jc) {
+        for (int a = 0; a < 4; ++a)
+            want(map, pfirst, bx, by, p, s2::off_fx(a, r, x) * 4, 4, addr(B_FX + a, g.face(ic, jc, p), 4));
+    }
+    void fy_at(const std::vector<std::vector<long long>> &map, int pfirst, int bx, int by, int p, int r, int x, int ic,
+               int jc) {
+        for (int a = 0; a < 4; ++a)
+            want(map, pfirst, bx, by, p, s2::off_fy(a, r, x) * 4, 4, addr(B_FY + a, g.face(ic, jc, p), 4));
+    }
+    void reads(const std::vector<std::vector<long long>> &map, int pfirst, int k0, int k1, int bx, int by) {
+        using namespace s2;
+        const int i0 = bx * SX + 1, j0 = by * SY + 1;
+        const int tx_last = std::min(SX - 1, g.C1 - i0), ty_last = std::min(SY - 1, g.C2 - j0);
+        for (int p = pfirst; p <= k1 + 1; ++p)
+            for (int ty = 0; ty <= ty_last; ++ty)
+                for (int tx = 0; tx <= tx_last; ++tx) {
+                    const int i = i0 + tx, j = j0 + ty;
+                    cell_at(map, pfirst, bx, by, p, ty + 1, tx + 1, i, j); // z sweep (every plane)
+                    if (p < k0 || p > k1) continue;
+                    fx_at(map, pfirst, bx, by, p, ty, tx + 1, i, j);     // x faces i, i+1
+                    fx_at(map, pfirst, bx, by, p, ty, tx + 2, i + 1, j);
+                    fy_at(map, pfirst, bx, by, p, ty + 1, tx + 1, i, j); // y faces j, j+1
+                    fy_at(map, pfirst, bx, by, p, ty + 2, tx + 1, i, j + 1);
+                }
+        // ghost cells copied from the "Con" level (the block's share of the ghost shell)
+        for (int p = pfirst; p <= k1 + 1; ++p) {
+            const bool gp = p == 0 || p == g.C3 + 1;
+            const int ia = i0 == 1 ? 0 : i0, ib = tx_last == g.C1 - i0 ? g.C1 + 1 : i0 + tx_last;
+            const int ja = j0 == 1 ? 0 : j0, jb = ty_last == g.C2 - j0 ? g.C2 + 1 : j0 + ty_last;
+            for (int jj = ja; jj <= jb; ++jj)
+                for (int ii = ia; ii <= ib; ++ii)
+                    if (gp || ii == 0 || ii == g.C1 + 1 || jj == 0 || jj == g.C2 + 1)
+                        for (int q = 0; q < 4; ++q)
+                            want(map, pfirst, bx, by, p, s2::off_cell(q, jj - (j0 - 1), ii - (i0 - 1)) * 4, 4,
+                                 addr(B_CELL + q, g.cell(ii, jj, p), 4));
+        }
+        for (int p = k0; p <= k1; ++p) {
+            for (int c = 0; c <= tx_last; ++c) {
+                const int i = i0 + c, jt = j0 + ty_last + 1, ry = ty_last + 2;
+                cell_at(map, pfirst, bx, by, p, 0, c + 1, i, j0 - 1); // below the tile
+                fy_at(map, pfirst, bx, by, p, 0, c + 1, i, j0 - 1);
+                fy_at(map, pfirst, bx, by, p, 1, c + 1, i, j0);
+                cell_at(map, pfirst, bx, by, p, ry, c + 1, i, jt); // above the tile's last row
+                fy_at(map, pfirst, bx, by, p, ry, c + 1, i, jt);
+                fy_at(map, pfirst, bx, by, p, ry + 1, c + 1, i, jt + 1);
+            }
+            for (int rr = 0; rr <= ty_last; ++rr) {
+                const int j = j0 + rr, it = i0 + tx_last + 1, xc = tx_last + 2;
+                cell_at(map, pfirst, bx, by, p, rr + 1, 0, i0 - 1, j); // left of the row
+                fx_at(map, pfirst, bx, by, p, rr, 0, i0 - 1, j);
+                fx_at(map, pfirst, bx, by, p, rr, 1, i0, j);
+                if (i0 == 1) want(map, pfirst, bx, by, p, s2::off_flag(rr + 1, 1), 1, addr(B_FL, g.cell(1, j, p), 1));
+                cell_at(map, pfirst, bx, by, p, rr + 1, xc, it, j); // right of the row's last cell
+                fx_at(map, pfirst, bx, by, p, rr, xc, it, j);
+                fx_at(map, pfirst, bx, by, p, rr, xc + 1, it + 1, j);
+            }
+        }
+    }
+};
+
 } // namespace
 
-int staging_plan_check(int C1, int C2, int C3, int kch, char *msg, int cap) {
+int step2_plan_check(int C1, int C2, int C3, int kch, char *msg, int cap) {
     const Geom g = device_geom(C1, C2, C3);
-    if (kch <= 0) kch = stg::staged_chunk(g);
+    if (kch <= 0) kch = s2::chunk(g);
+    Plan2Check a(g);
+    a.run(kch);
+    if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", a.err.c_str());
+    return a.bad;
+}
+
+int staging_plan_check(int C1, int C2, int C3, int kch_in, char *msg, int cap) {
+    const Geom g = device_geom(C1, C2, C3);
+    const int kch = kch_in > 0 ? kch_in : stg::staged_chunk(g);
     PlanCheck<P1_STRESS | P1_FORCES | P1_RMAX> a(g);
     a.run(kch);
     PlanCheck<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX> b(g);
     b.run(kch);
     PlanCheck<P1_FORCES | P1_RSUM> c(g);
     c.run(kch);
-    const std::string &e = !a.err.empty() ? a.err : (!b.err.empty() ? b.err : c.err);
+    char m2[256] = {0};
+    const int d = step2_plan_check(C1, C2, C3, kch_in, m2, (int)sizeof m2);
+    const std::string e = !a.err.empty() ? a.err : (!b.err.empty() ? b.err : (!c.err.empty() ? c.err : std::string(m2)));
     if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", e.c_str());
-    return a.bad + b.bad + c.bad;
+    return a.bad + b.bad + c.bad + d;
 }
 
 } // namespace ark

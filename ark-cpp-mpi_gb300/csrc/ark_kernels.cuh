@@ -1169,15 +1169,18 @@ template <class T> struct FaceOut {
     T *__restrict__ b;
 };
 
+// The new values of one face: pressure, density, normal and tangential velocities.
+template <class T> struct FaceNew { T p, ro, n, a, b; };
+
 // Face update (main.cpp:1920-2008).  prev = the cell behind the face (index f-1), cur = the
-// cell ahead (index f); cb/cf index those cells, fc the face; flb/flf their flags and
-// ucb/ucf their half-step normal velocities.  uA_old/uB_old: the face's previous tangential
-// velocities.  WALL_A_FROM_N: the x2 sweep takes the tangential u1 from u2nCon in its wall
-// branches (main.cpp:2219, 2238).
+// cell ahead (index f); cb/cf index those cells; flb/flf their flags and ucb/ucf their
+// half-step normal velocities.  uA_old/uB_old: the face's previous tangential velocities.
+// WALL_A_FROM_N: the x2 sweep takes the tangential u1 from u2nCon in its wall branches
+// (main.cpp:2219, 2238).
 template <class T, bool WALL_A_FROM_N>
-__device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> &W, int cb, int cf, int fc,
-                                            uint8_t flb, uint8_t flf, T ucb, T ucf, const Ext<T> &prev,
-                                            const Ext<T> &cur, T uA_old, T uB_old, const SweepK<T> &q) {
+__device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int cf, uint8_t flb, uint8_t flf, T ucb,
+                                                  T ucf, const Ext<T> &prev, const Ext<T> &cur, T uA_old, T uB_old,
+                                                  const SweepK<T> &q) {
     constexpr bool DEV = Storage<T>::deviation;
     T un, pn, ro_n, ua, ub;
     if ((flb & FL_LT) && (flf & FL_LT)) {
@@ -1238,11 +1241,29 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
             ub = (T)0;
         }
     }
-    W.p[fc] = pn;
-    W.n[fc] = un;
-    if (!DEV) W.ro[fc] = ro_n;
-    W.a[fc] = ua;
-    W.b[fc] = ub;
+    FaceNew<T> v;
+    v.p = pn;
+    v.ro = ro_n;
+    v.n = un;
+    v.a = ua;
+    v.b = ub;
+    return v;
+}
+
+template <class T> __device__ __forceinline__ void face_store(const FaceOut<T> &W, int fc, const FaceNew<T> &v) {
+    W.p[fc] = v.p;
+    W.n[fc] = v.n;
+    if (!Storage<T>::deviation) W.ro[fc] = v.ro;
+    W.a[fc] = v.a;
+    W.b[fc] = v.b;
+}
+
+// face_values stored into the new face generation at face fc
+template <class T, bool WALL_A_FROM_N>
+__device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> &W, int cb, int cf, int fc,
+                                            uint8_t flb, uint8_t flf, T ucb, T ucf, const Ext<T> &prev,
+                                            const Ext<T> &cur, T uA_old, T uB_old, const SweepK<T> &q) {
+    face_store(W, fc, face_values<T, WALL_A_FROM_N>(N, cb, cf, flb, flf, ucb, ucf, prev, cur, uA_old, uB_old, q));
 }
 
 template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d) {
@@ -1781,6 +1802,7 @@ template <class T, int MODE> struct CellK {
 };
 
 #include "ark_staged.cuh"
+#include "ark_fused.cuh"
 
 // march = 3: fcs::k_phase1_faces (FP64, face quantities computed once); 2: k_phase1_staged
 // (FP32); both for the two Phase1 modes of a step, other modes fall back to the one-cell
@@ -1835,6 +1857,7 @@ template <class T> void Launch<T>::prepare() {
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_RMAX>();
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>();
         stg::prepare_staged<P1_FORCES | P1_RSUM>();
+        s2::prepare<float>();
     }
 }
 
@@ -1877,6 +1900,10 @@ template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur
     }
 }
 
+template <class T>
+void Launch<T>::phase2_phase1(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) s2::launch<float>(S, con, fcur, out, st);
+}
 template <class T> void Launch<T>::phase2_fused(const DevState<T> &S, int con, int fcur, cudaStream_t st) {
     const int kch = stg::staged_chunk(S.g);
     const dim3 grid((S.g.C1 + p2f::SX - 1) / p2f::SX, (S.g.C2 + p2f::SY - 1) / p2f::SY, (S.g.C3 + kch - 1) / kch);

@@ -168,6 +168,7 @@ template <class T> struct DevState {
     Geom g;
     Consts k;
     Level<T> lv[2];  // the two cell levels; which one is "Con" is passed to each kernel
+    Level<T> spare;  // FP32: where the one-kernel Phase2 + second Phase1 writes the new level
     T *f[3];
     FaceSet<T> fc[2][3]; // two face generations: Phase2 reads fc[cur] and writes fc[cur^1]
     T *sig[3][3];        // sig[d][m]: component m on faces normal to d (nullptr unless kept)
@@ -204,6 +205,10 @@ template <class T> struct Launch {
     static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target = 32);
     // the three sweeps in one kernel (same results)
     static void phase2_fused(const DevState<T> &S, int con, int fcur, cudaStream_t st);
+    // FP32: the three sweeps and the second Phase1 (UseForces, bulk-flow partials) in one kernel,
+    // the new level written to `out` (not a level the launch reads); same results as the
+    // separate kernels.  No-op for FP64.
+    static void phase2_phase1(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st);
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
     static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);
@@ -217,6 +222,9 @@ template <class T> struct Launch {
 // kernel reads.  Returns the number of problems
 // (a description of the first in msg).
 int staging_plan_check(int C1, int C2, int C3, int kch, char *msg, int cap);
+// The same check for the one-kernel Phase2 + second Phase1 (s2 namespace): every copy, and every
+// shared-memory read of every thread and halo job mapped to the element the sweeps read.
+int step2_plan_check(int C1, int C2, int C3, int kch, char *msg, int cap);
 
 // ---- output and statistics (ark_output.cu) ----
 // The reference's averageU arrays are (n1+1) x (n2+2) x (n3+1) = (C1+2) x (C2+3) x (C3+2)

@@ -176,6 +176,10 @@ int ark_time_steps(ark_ctx *ctx, int nsteps, double *ms);
  * number of launches per step.  ark_kernel_name(i) names launch i. */
 int ark_kernel_times(ark_ctx *ctx, int nsteps, double *ms, int cap, int *count);
 const char *ark_kernel_name(int index);
+/* The name of launch `index` of ctx's step as currently configured (FP32 contexts that run Phase2
+ * and the second Phase1 as one kernel have 5 launches, the last "phase2_phase1_forces"); NULL
+ * past the end. */
+const char *ark_step_kernel_name(ark_ctx *ctx, int index);
 
 int ark_get_scalars(ark_ctx *ctx, ark_scalars *out);
 int ark_set_scalars(ark_ctx *ctx, const ark_scalars *in);
@@ -242,8 +246,9 @@ int ark_selftest_division(long long n, unsigned long long seed, long long *misma
  * planes in shared memory, for an n1 x n2 x n3-cell grid and planes_per_block planes per block
  * (0: the kernel's own choice): every 16-byte copy inside its array and its stage and aligned,
  * no two copies into one byte, and every shared-memory read of every thread mapped to the
- * element the one-cell kernel reads.  Returns the number of problems (msg receives the first),
- * or -1 for a bad size. */
+ * element the one-cell kernel reads; and the same for the FP32 kernel that runs Phase2 and the
+ * second Phase1 together (its reads mapped to the elements the sweep kernels read).  Returns the
+ * number of problems (msg receives the first), or -1 for a bad size. */
 int ark_selftest_staging(int n1_cells, int n2_cells, int n3_cells, int planes_per_block, char *msg, int cap);
 
 /* ---- learned eddy-viscosity closure (a project extension; the reference has none) --------
@@ -299,10 +304,12 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
 /* Times the kernel shapes of the step on the live state (it advances) and keeps the fastest,
  * one setting at a time: the shape of the Phase1 with stress (0 one cell per thread, 1
  * marching, 2 staged in shared memory (FP32), 3 face quantities computed once (FP64)), of the
- * second Phase1, and the x2/x3 sweeps' segment length (8, 16, 32, 64 faces), each candidate
- * timed three times (best kept).  The results do not depend on the shapes.  choice (5 ints,
- * may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step, fused Phase2
- * (set by ARK_PHASE2_FUSED=1 only)}. */
+ * second Phase1, the Phase2 form (FP32: three sweep kernels, or one kernel for the three sweeps
+ * and the second Phase1), and the x2/x3 sweeps' segment length (8, 16, 32, 64 faces), each
+ * candidate timed three times (best kept).  The results do not depend on the shapes.  choice
+ * (5 ints, may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step, Phase2
+ * form: 0 sweep kernels, 1 one sweep kernel (only by ARK_PHASE2_FUSED=1), 2 sweeps and second
+ * Phase1 in one kernel}. */
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice);
 
 /* ---- ensembles: many independent channels in one launch per phase ------------------------

@@ -411,3 +411,33 @@ def test_fused_phase2_agrees(ark, port, monkeypatch, C, px, pz):
                 outs.append(c.download(CELLS + FACES))
         for n in CELLS + FACES:
             assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), (prec, n)
+
+
+@pytest.mark.parametrize("C,px,pz", [((40, 20, 36), True, True), ((130, 9, 70), True, True), ((70, 6, 5), False, False),
+                                     ((64, 4, 1), True, False), ((65, 31, 17), True, True), ((33, 3, 9), False, True)])
+def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
+    """FP32: Phase2 and the second Phase1 in one kernel (ARK_PHASE2_FUSED=2, new level through
+    the spare buffer) give the bits of the separate kernels, ghost cells and faces included,
+    over several steps (both face generations, both buffer rotations), periodic and bounded
+    axes, ragged tiles; the per-launch timings name its five launches."""
+    p = port.channel_params(*C, seed=29)
+    st0 = port.channel_state(p)
+    outs = []
+    for mode in ("0", "2"):
+        monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
+        P = params_from(ark, p, precision=ark.FP32)
+        P.periodic_x, P.periodic_z = int(px), int(pz)
+        with ark.Context(P) as c:
+            c.upload(st0)
+            c.step(3)
+            kt = c.kernel_times(2)
+            c.step(2)
+            c.sync()
+            outs.append(c.download(CELLS + FACES))
+            names = [n for n, _ in kt]
+            if mode == "2":
+                assert names == ["finalize_dt", "wrap_con", "phase1_stress_forces", "wrap_phase2", "phase2_phase1_forces"]
+            else:
+                assert len(names) == 8 and names[-1] == "phase1_forces"
+    for n in CELLS + FACES:
+        assert bits_equal(outs[1][n], outs[0][n]), n
