@@ -184,6 +184,8 @@ __global__ void __launch_bounds__(NT, 2)
         nfrow = b;
     }
     __syncthreads();
+    // copies issued from the row table each plane (resolving them into registers, as the staged
+    // Phase1 does, costs this kernel 22 registers it does not have: spills, 11% slower)
     const int ch = t % stg::kChunks, r0 = t / stg::kChunks;
     constexpr int kRowsPerPass = NT / stg::kChunks;
     auto issue = [&](int p) {

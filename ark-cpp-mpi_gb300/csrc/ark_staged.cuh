@@ -171,6 +171,51 @@ __device__ __forceinline__ void cp16(unsigned dst, const void *src) {
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// One thread's share of a block's copy plan, resolved once before the plane loop: float rows
+// r0, r0 + NT/kChunks, ... at 16-byte chunk ch of each row, and (for the first kFlagChunks *
+// nfrow threads) one chunk of a flag row.  Per plane a copy is then one address computation.
+template <int MAXR> struct MyCopies {
+    const char *src[MAXR + 1]; // the copy's source in plane 0
+    int plane[MAXR + 1];       // bytes per plane of its array
+    unsigned dw[MAXR + 1];     // destination in the stage | stage kinds << 24 (0: no copy)
+    template <int NT>
+    __device__ __forceinline__ void resolve(const Row *rows, int nrow, const Row *frows, int nfrow, int t) {
+        constexpr int kRowsPerPass = NT / kChunks;
+        const int ch = t % kChunks, r0 = t / kChunks;
+#pragma unroll
+        for (int q = 0; q < MAXR; ++q) {
+            const int R = r0 + q * kRowsPerPass;
+            if (r0 < kRowsPerPass && R < nrow) {
+                const Row w = rows[R];
+                src[q] = w.src + 16 * ch;
+                plane[q] = w.plane;
+                dw[q] = w.dw + 16u * ch;
+            } else {
+                src[q] = nullptr;
+                plane[q] = 0;
+                dw[q] = 0;
+            }
+        }
+        if (t < kFlagChunks * nfrow) {
+            const Row w = frows[t / kFlagChunks];
+            const int c = t % kFlagChunks;
+            src[MAXR] = w.src + 16 * c;
+            plane[MAXR] = w.plane;
+            dw[MAXR] = w.dw + 16u * c;
+        } else {
+            src[MAXR] = nullptr;
+            plane[MAXR] = 0;
+            dw[MAXR] = 0;
+        }
+    }
+    // the copies of plane p whose kinds include `kind`, into the stage at shared address `to`
+    __device__ __forceinline__ void issue(unsigned to, int p, unsigned kind) const {
+#pragma unroll
+        for (int q = 0; q <= MAXR; ++q)
+            if ((dw[q] >> 24) & kind) cp16(to + (dw[q] & 0xFFFFFFu), src[q] + (long long)p * plane[q]);
+    }
+};
+
 template <int MODE>
 __global__ void __launch_bounds__(NT, 2)
     k_phase1_staged(const __grid_constant__ DevState<float> S, int src, int dst, int fcur, int kch) {
@@ -199,21 +244,13 @@ __global__ void __launch_bounds__(NT, 2)
     __syncthreads();
     // float rows: thread t copies chunk t % 17 of rows t / 17, t / 17 + 15, ...; flag rows: the
     // first 5 * (flag rows) threads one chunk each
-    const int ch = t % kChunks, r0 = t / kChunks;
-    constexpr int kRowsPerPass = NT / kChunks;
+    constexpr int kMine = (L::ROWS + NT / kChunks - 1) / (NT / kChunks);
+    MyCopies<kMine> mine;
+    mine.template resolve<NT>(rows, nrow, frows, nfrow, t);
     auto issue = [&](int p) {
         const unsigned to = sbase + (unsigned)(((p - pfirst) % NS) * L::STAGE);
         const unsigned kind = p < k0 ? DOWN : (p > k1 ? TOP : MID);
-        if (r0 < kRowsPerPass)
-            for (int R = r0; R < nrow; R += kRowsPerPass) {
-                const Row w = rows[R];
-                if ((w.dw >> 24) & kind) cp16(to + (w.dw & 0xFFFFFFu) + 16u * ch, w.src + (long long)p * w.plane + 16 * ch);
-            }
-        if (t < kFlagChunks * nfrow) {
-            const Row w = frows[t / kFlagChunks];
-            const int c = t % kFlagChunks;
-            if ((w.dw >> 24) & kind) cp16(to + (w.dw & 0xFFFFFFu) + 16u * c, w.src + (long long)p * w.plane + 16 * c);
-        }
+        mine.issue(to, p, kind);
     };
     // Pipeline: planes pfirst .. pfirst+NS-2 are issued up front; at plane k, once plane k+1
     // has landed and every thread is past plane k-1, the slot of the plane no longer needed
