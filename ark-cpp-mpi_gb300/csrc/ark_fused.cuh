@@ -142,7 +142,7 @@ __device__ __forceinline__ Ext<float> stage_ext(const float *st, int r, int x, i
 __device__ __forceinline__ FaceVal<float> face_val(float p, float u1, float u2, float u3, const K<float> &kk) {
     FaceVal<float> v;
     v.p = p;
-    v.ro = kk.ro0 + v.p * kk.rc2;
+    v.ro = face_ro(v.p, kk);
     v.u[0] = u1;
     v.u[1] = u2;
     v.u[2] = u3;
@@ -306,12 +306,7 @@ __global__ void __launch_bounds__(NT, 2)
                     ucn[0] = ucn[1] = ucn[2] = (T)0;
                     ro_cn = (T)0;
                 }
-                if (hfl & FL_EQ0) {
-                    // UseForces (main.cpp:1035-1041) in the FP32 form of the Phase1 kernels
-                    const T g2 = (T)0.5 * dt * kk.rdvc * rden;
-#pragma unroll
-                    for (int m = 0; m < 3; ++m) ucn[m] += g2 * ff[m];
-                }
+                if (hfl & FL_EQ0) use_forces_f32(ucn, ff, dt, kk, rden); // UseForces (main.cpp:1035-1041)
                 const int c = g.ci(i, j, p - 1);
                 out.ro[c] = ro_cn;
                 out.u1[c] = ucn[0];

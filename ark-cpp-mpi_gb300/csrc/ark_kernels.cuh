@@ -106,6 +106,12 @@ __device__ __forceinline__ float divr(float a, float b, float rb) {
 // Run constants rounded to T (filled on the host).
 template <class T> using K = KT<T>;
 
+// a*b + c.  FP64: the product and the sum rounded separately, as the reference computes them
+// (the FP64 code is built with --fmad=false).  FP32: one fused multiply-add.  Every FP32 kernel
+// shape calls the same helpers, so all of them keep identical bits.
+__device__ __forceinline__ double mad(double a, double b, double c) { return a * b + c; }
+__device__ __forceinline__ float mad(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
 // ---------------------------------------------------------------------------------------
 // TimeStepSize + bulk flow rate
 // ---------------------------------------------------------------------------------------
@@ -441,7 +447,7 @@ __device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const 
 template <class T>
 __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6][3], uint8_t fl, const T uc[3],
                                              T ro_c, const K<T> &kk, T f[3], const T *nuf = nullptr) {
-    if (!Storage<T>::deviation) {
+    if constexpr (!Storage<T>::deviation) {
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
             T sw[3], se[3];
@@ -462,7 +468,7 @@ __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6]
                 const uint8_t fw = side ? fl : fln[2 * d], fc = side ? fln[2 * d + 1] : fl;
                 const bool wl = fw & FL_LT, wg = fw & FL_GT, cl = fc & FL_LT, cg = fc & FL_GT;
                 const int q = 2 * d + side;
-                const T vq = nuf ? v + nuf[q] * kk.rdx[d] : v;
+                const T vq = nuf ? mad(nuf[q], kk.rdx[d], v) : v;
                 aw[q] = (wl && cl) ? vq : (wl && cg) ? (T)2 * vq : (T)0;
                 ac[q] = (wl && cl) ? vq : (wg && cl) ? (T)2 * vq : (T)0;
             }
@@ -472,9 +478,9 @@ __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6]
             T acc = (T)0;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const T sw = ac[2 * d] * uc[m] - aw[2 * d] * un[2 * d][m];
-                const T se = ac[2 * d + 1] * un[2 * d + 1][m] - aw[2 * d + 1] * uc[m];
-                acc += (se - sw) * kk.ds[d];
+                const T sw = mad(ac[2 * d], uc[m], -(aw[2 * d] * un[2 * d][m]));
+                const T se = mad(ac[2 * d + 1], un[2 * d + 1][m], -(aw[2 * d + 1] * uc[m]));
+                acc = mad(se - sw, kk.ds[d], acc);
             }
             f[m] = acc * ro_c;
         }
@@ -488,11 +494,32 @@ __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6]
 // One face's values: pressure, density, velocity components.
 template <class T> struct FaceVal { T p, ro, u[3]; };
 
+// FP32 face density from face pressure: ro0 + p / c^2
+__device__ __forceinline__ float face_ro(float p, const K<float> &kk) { return __fmaf_rn(p, kk.rc2, kk.ro0); }
+
+// The bulk force on a cell's x1 momentum: f1 + (ro dvc) G (main.cpp:1013-1015 with the
+// forcing term); FP32 fused.
+__device__ __forceinline__ double bulk_force(double f1, double ro, const K<double> &kk, double G) {
+    return f1 + (ro * kk.dvc) * G;
+}
+__device__ __forceinline__ float bulk_force(float f1, float ro, const K<float> &kk, float G) {
+    return __fmaf_rn(ro * kk.dvc, G, f1);
+}
+
+// UseForces (main.cpp:1035-1041) in the FP32 form: u += (dt/2) f / (dvc ro) with rden = 1/ro
+// already formed, one fused multiply-add per component.
+__device__ __forceinline__ void use_forces_f32(float u[3], const float f[3], float dt, const K<float> &kk, float rden) {
+    const float g2 = 0.5f * dt * kk.rdvc * rden;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) u[m] = __fmaf_rn(g2, f[m], u[m]);
+}
+
 template <class T>
 __device__ __forceinline__ FaceVal<T> load_face(const FaceSet<T> &F, int f, const K<T> &kk) {
     FaceVal<T> v;
     v.p = __ldg(F.p + f);
-    v.ro = Storage<T>::deviation ? kk.ro0 + v.p * kk.rc2 : __ldg(F.ro + f);
+    if constexpr (Storage<T>::deviation) v.ro = face_ro(v.p, kk);
+    else v.ro = __ldg(F.ro + f);
     v.u[0] = __ldg(F.u[0] + f);
     v.u[1] = __ldg(F.u[1] + f);
     v.u[2] = __ldg(F.u[2] + f);
@@ -504,7 +531,7 @@ __device__ __forceinline__ FaceVal<T> load_face(const FaceSet<T> &F, int f, cons
 template <class T>
 __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<T> hi[3], T ro_c, const T uc[3],
                                           T dt, const K<T> &kk, T &ro_cn, T ucn[3], T &rden_out) {
-    if (!Storage<T>::deviation) {
+    if constexpr (!Storage<T>::deviation) {
         // new density (main.cpp:530-533)
         ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
                                                     (hi[1].ro * hi[1].u[1] - lo[1].ro * lo[1].u[1]) * kk.ds[1] +
@@ -532,11 +559,19 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
         }
     } else {
         // the same balance with the volume divided out and the density as a deviation:
-        // ro'_new = ro'_c - (dt/2/dvc) sum_d (rho u_d)|_faces ds_d
+        // ro'_new = ro'_c - (dt/2/dvc) sum_d (rho u_d)|_faces ds_d.  The momentum flux of u_m
+        // through a face is the face's mass flux times u_m; products fused with the sums.
         const T h = (T)0.5 * dt * kk.rdvc;
-        ro_cn = ro_c - h * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
-                            (hi[1].ro * hi[1].u[1] - lo[1].ro * lo[1].u[1]) * kk.ds[1] +
-                            (hi[2].ro * hi[2].u[2] - lo[2].ro * lo[2].u[2]) * kk.ds[2]);
+        T mh[3], ml[3]; // mass flux through the hi and lo face of each direction
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            mh[d] = hi[d].ro * hi[d].u[d];
+            ml[d] = lo[d].ro * lo[d].u[d];
+        }
+        T sm = (mh[0] - ml[0]) * kk.ds[0];
+        sm = mad(mh[1] - ml[1], kk.ds[1], sm);
+        sm = mad(mh[2] - ml[2], kk.ds[2], sm);
+        ro_cn = mad(-h, sm, ro_c);
         const T rden = (T)1 / (kk.ro0 + ro_cn);
         rden_out = rden;
         const T ro_cf = kk.ro0 + ro_c;
@@ -545,10 +580,13 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
             T fx[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                fx[d] = hi[d].ro * hi[d].u[m] * hi[d].u[d] - lo[d].ro * lo[d].u[m] * lo[d].u[d];
+                fx[d] = mad(mh[d], hi[d].u[m], -(ml[d] * lo[d].u[m]));
                 if (m == d) fx[d] += hi[d].p - lo[d].p;
             }
-            ucn[m] = (ro_cf * uc[m] - h * (fx[0] * kk.ds[0] + fx[1] * kk.ds[1] + fx[2] * kk.ds[2])) * rden;
+            T sx = fx[0] * kk.ds[0];
+            sx = mad(fx[1], kk.ds[1], sx);
+            sx = mad(fx[2], kk.ds[2], sx);
+            ucn[m] = mad(-h, sx, ro_cf * uc[m]) * rden;
         }
     }
 }
@@ -656,7 +694,7 @@ __device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src,
                     }
                     const T ro_cf = DEV ? kk.ro0 + ro_c : ro_c;
                     stress_force(fln, un, fl, uc, ro_cf, kk, f);
-                    if (MODE & P1_BULK) f[0] = f[0] + (ro_cf * kk.dvc) * G;
+                    if (MODE & P1_BULK) f[0] = bulk_force(f[0], ro_cf, kk, G);
                 }
                 S.f[0][c] = f[0];
                 S.f[1][c] = f[1];
@@ -678,14 +716,12 @@ __device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src,
             if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
                 // UseForces (main.cpp:1035-1041); a fluid cell always went through half_step,
                 // so rden is 1/(dvc*ro_cn) (FP64) or 1/(ro0 + ro'_cn) (FP32)
-                if (!DEV) {
+                if constexpr (!DEV) {
                     const T den = kk.dvc * ro_cn;
 #pragma unroll
                     for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
                 } else {
-                    const T g2 = (T)0.5 * dt * kk.rdvc * rden;
-#pragma unroll
-                    for (int m = 0; m < 3; ++m) ucn[m] += g2 * f[m];
+                    use_forces_f32(ucn, f, dt, kk, rden);
                 }
             }
             dro[c] = ro_cn;
@@ -772,7 +808,7 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
                 } else {
                     stress_force(fln, un, fl, uc, ro_cf, kk, f);
                 }
-                if (MODE & P1_BULK) f[0] = f[0] + (ro_cf * kk.dvc) * sc_G<T>(S.sc);
+                if (MODE & P1_BULK) f[0] = bulk_force(f[0], ro_cf, kk, sc_G<T>(S.sc));
             }
             S.f[0][c] = f[0];
             S.f[1][c] = f[1];
@@ -784,14 +820,12 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
         }
         if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
             // UseForces (main.cpp:1035-1041), with the reciprocal half_step formed
-            if (!DEV) {
+            if constexpr (!DEV) {
                 const T den = kk.dvc * ro_cn;
 #pragma unroll
                 for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
             } else {
-                const T g2 = (T)0.5 * dt * kk.rdvc * rden;
-#pragma unroll
-                for (int m = 0; m < 3; ++m) ucn[m] += g2 * f[m];
+                use_forces_f32(ucn, f, dt, kk, rden);
             }
         }
         S.lv[dst].ro[c] = ro_cn;
@@ -952,7 +986,7 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
                         fv[m] = ((Hx.sig[m] - Lx.sig[m]) * kk.ds[0] + (Hy.sig[m] - Ly.sig[m]) * kk.ds[1] +
                                  (zhi.sig[m] - zlo.sig[m]) * kk.ds[2]) *
                                 ro_c;
-                    if (MODE & P1_BULK) fv[0] = fv[0] + (ro_c * kk.dvc) * G;
+                    if (MODE & P1_BULK) fv[0] = bulk_force(fv[0], ro_c, kk, G);
                 }
                 S.f[0][c] = fv[0];
                 S.f[1][c] = fv[1];
@@ -1043,7 +1077,7 @@ template <class T> __global__ void k_stress_force(DevState<T> S, int con, int bu
             un[q][2] = L.u3[nb[q]];
         }
         stress_force(fln, un, fl, uc, ro_c, kk, f);
-        if (bulk) f[0] = f[0] + (ro_c * kk.dvc) * sc_G<T>(S.sc);
+        if (bulk) f[0] = bulk_force(f[0], ro_c, kk, sc_G<T>(S.sc));
     }
     S.f[0][c] = f[0];
     S.f[1][c] = f[1];
@@ -1063,7 +1097,7 @@ template <class T> __global__ void k_use_forces(DevState<T> S, int ncon) {
     const K<T> &kk = kconst<T>(S.k);
     const T dt = sc_dt<T>(S.sc);
     const Level<T> L = S.lv[ncon];
-    if (!DEV) {
+    if constexpr (!DEV) {
         const T ro_cn = L.ro[c];
         const T den = kk.dvc * ro_cn;
         const T rden = recip(den);
@@ -1071,10 +1105,12 @@ template <class T> __global__ void k_use_forces(DevState<T> S, int ncon) {
         L.u2[c] = divr(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den, rden);
         L.u3[c] = divr(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den, rden);
     } else {
-        const T g2 = (T)0.5 * dt * kk.rdvc * recip(kk.ro0 + L.ro[c]);
-        L.u1[c] += g2 * S.f[0][c];
-        L.u2[c] += g2 * S.f[1][c];
-        L.u3[c] += g2 * S.f[2][c];
+        T u[3] = {L.u1[c], L.u2[c], L.u3[c]};
+        const T f[3] = {S.f[0][c], S.f[1][c], S.f[2][c]};
+        use_forces_f32(u, f, dt, kk, recip(kk.ro0 + L.ro[c]));
+        L.u1[c] = u[0];
+        L.u2[c] = u[1];
+        L.u3[c] = u[2];
     }
 }
 
@@ -1089,6 +1125,13 @@ template <class T> struct Ext { T rf, qb, af, ab, bf, bb; };
 template <class T> struct SweepK {
     T sound, ro0, c2, rc2, roc, rroc, dt, rdt, dx, rdx;
 };
+
+// The gradient term of a limiter bound: a / dt + b / dx.  FP64: the two correctly rounded
+// quotients summed, as the reference evaluates it; FP32: a * (1/dt) + b * (1/dx), fused.
+__device__ __forceinline__ double grad_sum(double a, double b, const SweepK<double> &q) {
+    return divk(a, q.dt, q.rdt) + divk(b, q.dx, q.rdx);
+}
+__device__ __forceinline__ float grad_sum(float a, float b, const SweepK<float> &q) { return __fmaf_rn(a, q.rdt, b * q.rdx); }
 
 // One cell of a sweep (main.cpp:1756-1873 for x1; the x2 and x3 sweeps are the same with
 // the axes permuted).  u1: the velocity component normal to the sweep, u2/u3: tangential.
@@ -1105,30 +1148,30 @@ __device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T
     const T pf = divk(p_f, q.roc, q.rroc), pb = divk(p_b, q.roc, q.rroc);
     const T pcn = divk(p_cn, q.roc, q.rroc), pc = divk(p_c, q.roc, q.rroc);
 
+    // 2x - y and max + dt*g: mad rounds these exactly as written in FP64, fused in FP32
     const T r_f = u1_f + pf, r_b = u1_b + pb, r_cn = u1_cn + pcn, r_c = u1_c + pc;
-    T r_fn = (T)2 * r_cn - r_b;
+    T r_fn = mad((T)2, r_cn, -r_b);
     const T q_f = u1_f - pf, q_b = u1_b - pb, q_cn = u1_cn - pcn, q_c = u1_c - pc;
-    T q_bn = (T)2 * q_cn - q_f;
+    T q_bn = mad((T)2, q_cn, -q_f);
 
-    T u2_fn = (T)2 * u2_cn - u2_b;
-    T u2_bn = (T)2 * u2_cn - u2_f;
-    T u3_fn = (T)2 * u3_cn - u3_b;
-    T u3_bn = (T)2 * u3_cn - u3_f;
+    T u2_fn = mad((T)2, u2_cn, -u2_b);
+    T u2_bn = mad((T)2, u2_cn, -u2_f);
+    T u3_fn = mad((T)2, u3_cn, -u3_b);
+    T u3_bn = mad((T)2, u3_cn, -u3_f);
 
-    const T gr = divk((T)2 * (r_cn - r_c), q.dt, q.rdt) + divk((u1_cn + q.sound) * (r_f - r_b), q.dx, q.rdx);
-    const T gq = divk((T)2 * (Q_USES_R ? (r_cn - r_c) : (q_cn - q_c)), q.dt, q.rdt) +
-                 divk((u1_cn - q.sound) * (q_f - q_b), q.dx, q.rdx);
-    const T gu2 = divk((T)2 * (u2_cn - u2_c), q.dt, q.rdt) + divk(u1_cn * (u2_f - u2_b), q.dx, q.rdx);
-    const T gu3 = divk((T)2 * (u3_cn - u3_c), q.dt, q.rdt) + divk(u1_cn * (u3_f - u3_b), q.dx, q.rdx);
+    const T gr = grad_sum((T)2 * (r_cn - r_c), (u1_cn + q.sound) * (r_f - r_b), q);
+    const T gq = grad_sum((T)2 * (Q_USES_R ? (r_cn - r_c) : (q_cn - q_c)), (u1_cn - q.sound) * (q_f - q_b), q);
+    const T gu2 = grad_sum((T)2 * (u2_cn - u2_c), u1_cn * (u2_f - u2_b), q);
+    const T gu3 = grad_sum((T)2 * (u3_cn - u3_c), u1_cn * (u3_f - u3_b), q);
 
-    const T rmax = max3d(r_f, r_c, r_b) + q.dt * gr;
-    const T rmin = min3d(r_f, r_c, r_b) + q.dt * gr;
-    const T qmax = max3d(q_f, q_c, q_b) + q.dt * gq;
-    const T qmin = min3d(q_f, q_c, q_b) + q.dt * gq;
-    const T u2_max = max3d(u2_f, u2_c, u2_b) + q.dt * gu2;
-    const T u2_min = min3d(u2_f, u2_c, u2_b) + q.dt * gu2;
-    const T u3_max = max3d(u3_f, u3_c, u3_b) + q.dt * gu3;
-    const T u3_min = min3d(u3_f, u3_c, u3_b) + q.dt * gu3;
+    const T rmax = mad(q.dt, gr, max3d(r_f, r_c, r_b));
+    const T rmin = mad(q.dt, gr, min3d(r_f, r_c, r_b));
+    const T qmax = mad(q.dt, gq, max3d(q_f, q_c, q_b));
+    const T qmin = mad(q.dt, gq, min3d(q_f, q_c, q_b));
+    const T u2_max = mad(q.dt, gu2, max3d(u2_f, u2_c, u2_b));
+    const T u2_min = mad(q.dt, gu2, min3d(u2_f, u2_c, u2_b));
+    const T u3_max = mad(q.dt, gu3, max3d(u3_f, u3_c, u3_b));
+    const T u3_min = mad(q.dt, gu3, min3d(u3_f, u3_c, u3_b));
 
     if (gt(r_fn, rmax)) r_fn = rmax;
     if (lt(r_fn, rmin)) r_fn = rmin;

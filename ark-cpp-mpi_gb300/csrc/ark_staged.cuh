@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(NT, 2)
                 auto fv = [&](const T *f, int d, int r, int x) {
                     FaceVal<T> v;
                     v.p = f[off_face<MODE>(d, 0, r, x)];
-                    v.ro = kk.ro0 + v.p * kk.rc2;
+                    v.ro = face_ro(v.p, kk);
                     v.u[0] = f[off_face<MODE>(d, 1, r, x)];
                     v.u[1] = f[off_face<MODE>(d, 2, r, x)];
                     v.u[2] = f[off_face<MODE>(d, 3, r, x)];
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(NT, 2)
                     }
                     const T ro_cf = kk.ro0 + ro_c;
                     stress_force(fln, un, fl, uc, ro_cf, kk, f);
-                    if (MODE & P1_BULK) f[0] = f[0] + (ro_cf * kk.dvc) * G1;
+                    if (MODE & P1_BULK) f[0] = bulk_force(f[0], ro_cf, kk, G1);
                 }
                 S.f[0][c] = f[0];
                 S.f[1][c] = f[1];
@@ -344,12 +344,7 @@ __global__ void __launch_bounds__(NT, 2)
                 f[1] = fm[off_ff<MODE>(1, ty, cx)];
                 f[2] = fm[off_ff<MODE>(2, ty, cx)];
             }
-            if ((MODE & P1_FORCES) && (fl & FL_EQ0)) {
-                // UseForces (main.cpp:1035-1041) in the FP32 form of the other Phase1 kernels
-                const T g2 = (T)0.5 * dt * kk.rdvc * rden;
-#pragma unroll
-                for (int m = 0; m < 3; ++m) ucn[m] += g2 * f[m];
-            }
+            if ((MODE & P1_FORCES) && (fl & FL_EQ0)) use_forces_f32(ucn, f, dt, kk, rden); // UseForces
             S.lv[dst].ro[c] = ro_cn;
             S.lv[dst].u1[c] = ucn[0];
             S.lv[dst].u2[c] = ucn[1];
