@@ -240,9 +240,12 @@ __global__ void __launch_bounds__(NT, 2)
         v[2] = FZ.u[1][f];
         v[3] = FZ.u[2][f];
     };
+    // (the next face is loaded one plane ahead and moved into place at the start of the next
+    // plane, so each load has a plane's work to land)
     if (valid) {
         zload(pfirst, zlo);
         zload(pfirst + 1, zhi);
+        zload(pfirst + 2, znx);
     }
     Behind zb = {0, 0, 0, 0, 0};           // the z extrapolation of plane p-1, behind face p
     T zn_lo[4] = {0, 0, 0, 0};             // the new z face p-1 (below plane p-1): p, u1, u2, u3
@@ -265,7 +268,14 @@ __global__ void __launch_bounds__(NT, 2)
 
         // ---- z sweep of plane p, the z face p, the second Phase1 of plane p-1 ----
         if (valid) {
-            if (p + 2 <= plast + 1) zload(p + 2, znx);
+            if (p > pfirst) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    zlo[a] = zhi[a];
+                    zhi[a] = znx[a];
+                }
+                if (p + 2 <= plast + 1) zload(p + 2, znx);
+            }
             const Ext<T> ez = extrapolate<T, true>(zhi[3], zlo[3], st[off_cell(7, r, x)], st[off_cell(3, r, x)], zhi[1],
                                                    zlo[1], st[off_cell(5, r, x)], st[off_cell(1, r, x)], zhi[2], zlo[2],
                                                    st[off_cell(6, r, x)], st[off_cell(2, r, x)], st[off_cell(4, r, x)],
@@ -320,11 +330,7 @@ __global__ void __launch_bounds__(NT, 2)
             zb.un = un;
             zb.fl = fl;
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                zn_lo[a] = zn[a];
-                zlo[a] = zhi[a];
-                zhi[a] = znx[a];
-            }
+            for (int a = 0; a < 4; ++a) zn_lo[a] = zn[a];
         }
         // ghost cells of the new level: the "Con" level's, as the separate kernels leave them
         // (they write interior cells only).  Each ghost cell belongs to the one block whose tile,
