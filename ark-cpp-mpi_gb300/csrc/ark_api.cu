@@ -526,7 +526,11 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     ctx->P = *params;
     ctx->g = make_geom(*params);
     ctx->k = make_consts(*params);
-    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+    // the step's stream at the highest priority, so that work on lower-priority branches (the
+    // learned closure's inference) only takes SMs the step's kernels leave idle
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, prio_high) != cudaSuccess) {
         *status = fail(ARK_ERR_CUDA, "cudaStreamCreate failed");
         return nullptr;
     }
@@ -1260,7 +1264,9 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau) {
         ctx->closure_net = nullptr;
     }
     if (mlp && !ctx->side) {
-        ARK_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        int prio_low = 0, prio_high = 0;
+        ARK_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+        ARK_CUDA(cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, prio_low));
         ARK_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
         ARK_CUDA(cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming));
     }

@@ -104,11 +104,13 @@ __host__ __device__ inline Bases bases_of(const DevState<float> &S, int con, int
     return b;
 }
 
-// Planes per block: about eight waves of two blocks per SM on 152 SMs, 8 to 64 planes.
+// Planes per block: about eight waves of two blocks per SM on 152 SMs, 2 to 64 planes (small
+// grids: short chunks, so that enough blocks run; each block also sweeps the two planes at its
+// ends in z).
 inline int chunk(const Geom &g) {
     const long long cols = (long long)((g.C1 + SX - 1) / SX) * ((g.C2 + SY - 1) / SY);
     long long k = (long long)g.C3 * cols / (152 * 2 * 8);
-    k = k < 8 ? 8 : (k > 64 ? 64 : k);
+    k = k < 2 ? 2 : (k > 64 ? 64 : k);
     return (int)k;
 }
 inline dim3 grid(const Geom &g, int kch) { return dim3((g.C1 + SX - 1) / SX, (g.C2 + SY - 1) / SY, (g.C3 + kch - 1) / kch); }
