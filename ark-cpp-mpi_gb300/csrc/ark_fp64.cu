@@ -11,7 +11,9 @@ template void rows_face_density<double>(double *, const double *, int, int64_t, 
 // Self-check of div_rn against the hardware IEEE division: n operand pairs from splitmix64
 // (random signs and mantissas; numerator exponents over the whole range, subnormals and
 // zeros included, divisor exponents in [-120, 120]); divisors are reused 8 times so the
-// reciprocal is a "run constant" like dx or dt.  Also the small exact cases the step meets.
+// reciprocal is a "run constant" like dx or dt.  Where the divisor's reciprocal is within a
+// quarter ulp (recip_tight, about 70% of random divisors) the one-correction form is checked
+// too.  Also the small exact cases the step meets.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -34,6 +36,7 @@ __global__ void k_selftest_division(long long n, unsigned long long seed, unsign
         const double rb = 1.0 / b;
         const double want = a / b, got = div_rn(a, b, rb);
         if (__double_as_longlong(want) != __double_as_longlong(got)) ++local;
+        if (recip_tight(b, rb) && __double_as_longlong(want) != __double_as_longlong(div_rn(a, b, rb, true))) ++local;
         const double a2 = (double)(long long)(t % 2001 - 1000) * 0.5, b2 = 10.0;
         if (__double_as_longlong(a2 / b2) != __double_as_longlong(div_rn(a2, b2, 1.0 / b2))) ++local;
     }

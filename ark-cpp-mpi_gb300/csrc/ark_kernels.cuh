@@ -64,27 +64,35 @@ template <class T> __device__ __forceinline__ T max3d(T x1, T x2, T x3) {
 // within one ulp of a/b, then with the exact residual r = a - b*q (one FMA),
 // RN(q + r*rb) = RN(a/b), provided nothing underflows or overflows.  q = RN(a*rb) may be up
 // to 1.5 ulp off, so one correction makes it faithful and a second one makes it correctly
-// rounded: 1 multiply + 4 FMA.  Operands outside 2^-895 <= |a| < 2^897 and
-// 2^-100 <= |b| < 2^101 (where the residual could leave the normal range), zeros included,
-// take the IEEE division instead; the exponent test is integer work.  The FP64 parity tests
-// check every quotient of the step against the reference bit for bit, and
-// ark_selftest_division compares with the hardware division, tiny and subnormal operands
-// included.
-__device__ __forceinline__ double div_rn(double a, double b, double rb) {
+// rounded: 1 multiply + 4 FMA.  One correction is enough when rb is within a quarter ulp,
+// |rb*b - 1| <= 2^-54 (one = true): then |a*rb - a/b| < ulp(a/b)/2, and rounding a*rb adds at
+// most another half ulp of the same binade (at a binade edge the rounding lands on the power of
+// two, within half an ulp of a/b), so q = RN(a*rb) is within one ulp and the theorem applies:
+// 1 multiply + 2 FMA.  Operands outside 2^-895 <= |a| < 2^897 and 2^-100 <= |b| < 2^101
+// (where the residual could leave the normal range), zeros included, take the IEEE division
+// instead; the exponent test is integer work.  The FP64 parity tests check every quotient of
+// the step against the reference bit for bit, and ark_selftest_division compares both forms
+// with the hardware division, tiny and subnormal operands included.
+__device__ __forceinline__ double div_rn(double a, double b, double rb, bool one = false) {
     const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7FFu;
     const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7FFu;
     if (ea - 128u > 1792u || eb - 923u > 200u) return a / b;
     double q = a * rb;
     double r = __fma_rn(-q, b, a);
     q = __fma_rn(r, rb, q);
+    if (one) return q;
     r = __fma_rn(-q, b, a);
     return __fma_rn(r, rb, q);
 }
 
+// rb = RN(1/b) within a quarter ulp (the residual rb*b - 1 is exact in one FMA)
+__device__ __forceinline__ bool recip_tight(double b, double rb) { return fabs(__fma_rn(rb, b, -1.0)) <= 0x1p-54; }
+
 // Division by a run constant b whose reciprocal rb is known.  FP64: the correctly rounded
 // quotient (the parity bar).  FP32: multiplication by the reciprocal.
-__device__ __forceinline__ double divk(double a, double b, double rb) { return div_rn(a, b, rb); }
-__device__ __forceinline__ float divk(float a, float b, float rb) {
+// one: rb is within a quarter ulp (the run constant's flag), so one correction suffices.
+__device__ __forceinline__ double divk(double a, double b, double rb, bool one) { return div_rn(a, b, rb, one); }
+__device__ __forceinline__ float divk(float a, float b, float rb, bool) {
     (void)b;
     return a * rb;
 }
@@ -96,9 +104,9 @@ __device__ __forceinline__ float divv(float a, float b) { return __fdiv_rn(a, b)
 // Reciprocal of a cell-dependent value for divr below: IEEE 1/b (FP64), or 1/b (FP32).
 __device__ __forceinline__ double recip(double b) { return __drcp_rn(b); }
 __device__ __forceinline__ float recip(float b) { return __frcp_rn(b); }
-// a / b with rb = recip(b): correctly rounded in FP64, a*rb in FP32.
-__device__ __forceinline__ double divr(double a, double b, double rb) { return div_rn(a, b, rb); }
-__device__ __forceinline__ float divr(float a, float b, float rb) {
+// a / b with rb = recip(b): correctly rounded in FP64 (one: recip_tight(b, rb)), a*rb in FP32.
+__device__ __forceinline__ double divr(double a, double b, double rb, bool one) { return div_rn(a, b, rb, one); }
+__device__ __forceinline__ float divr(float a, float b, float rb, bool) {
     (void)b;
     return a * rb;
 }
@@ -431,11 +439,12 @@ constexpr int kCellBX = 64, kCellBY = 2; // block shape of the one-cell-per-thre
 // viscous stress on one face (main.cpp:856-982), component by component
 // ---------------------------------------------------------------------------------------
 
+// one: the kernel was built for grid steps whose reciprocals are within a quarter ulp (div_rn)
 template <class T>
-__device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const K<T> &kk, int d) {
-    if ((fw & FL_LT) && (fc & FL_LT)) return divk(kk.vis * (u_c - u_cw), kk.dx[d], kk.rdx[d]);
-    if ((fw & FL_LT) && (fc & FL_GT)) return divk(kk.two_vis * (-u_cw), kk.dx[d], kk.rdx[d]);
-    if ((fw & FL_GT) && (fc & FL_LT)) return divk(kk.two_vis * u_c, kk.dx[d], kk.rdx[d]);
+__device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const K<T> &kk, int d, bool one = false) {
+    if ((fw & FL_LT) && (fc & FL_LT)) return divk(kk.vis * (u_c - u_cw), kk.dx[d], kk.rdx[d], one);
+    if ((fw & FL_LT) && (fc & FL_GT)) return divk(kk.two_vis * (-u_cw), kk.dx[d], kk.rdx[d], one);
+    if ((fw & FL_GT) && (fc & FL_LT)) return divk(kk.two_vis * u_c, kk.dx[d], kk.rdx[d], one);
     return (T)0;
 }
 
@@ -446,15 +455,15 @@ __device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const 
 // nuf (FP32 only; nullptr: none): eddy viscosity per face in the same order, added to vis.
 template <class T>
 __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6][3], uint8_t fl, const T uc[3],
-                                             T ro_c, const K<T> &kk, T f[3], const T *nuf = nullptr) {
+                                             T ro_c, const K<T> &kk, T f[3], const T *nuf = nullptr, bool one = false) {
     if constexpr (!Storage<T>::deviation) {
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
             T sw[3], se[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                sw[d] = sigma(fln[2 * d], fl, un[2 * d][m], uc[m], kk, d);
-                se[d] = sigma(fl, fln[2 * d + 1], uc[m], un[2 * d + 1][m], kk, d);
+                sw[d] = sigma(fln[2 * d], fl, un[2 * d][m], uc[m], kk, d, one);
+                se[d] = sigma(fl, fln[2 * d + 1], uc[m], un[2 * d + 1][m], kk, d, one);
             }
             f[m] = ((se[0] - sw[0]) * kk.ds[0] + (se[1] - sw[1]) * kk.ds[1] + (se[2] - sw[2]) * kk.ds[2]) * ro_c;
         }
@@ -530,13 +539,13 @@ __device__ __forceinline__ FaceVal<T> load_face(const FaceSet<T> &F, int f, cons
 // lo[d] (west/south/bottom) and hi[d] (east/north/top).  ro_c: density (FP64) or deviation.
 template <class T>
 __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<T> hi[3], T ro_c, const T uc[3],
-                                          T dt, const K<T> &kk, T &ro_cn, T ucn[3], T &rden_out) {
+                                          T dt, const K<T> &kk, T &ro_cn, T ucn[3], T &rden_out, bool one = false) {
     if constexpr (!Storage<T>::deviation) {
         // new density (main.cpp:530-533)
         ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
                                                     (hi[1].ro * hi[1].u[1] - lo[1].ro * lo[1].u[1]) * kk.ds[1] +
                                                     (hi[2].ro * hi[2].u[2] - lo[2].ro * lo[2].u[2]) * kk.ds[2]),
-                     kk.dvc, kk.rdvc);
+                     kk.dvc, kk.rdvc, one);
         // momentum (main.cpp:536-551): the flux of u_m through faces normal to d is
         // (ro*u_m)*u_d, plus p when m == d
         // one reciprocal serves the three momentum quotients (and UseForces, whose divisor
@@ -555,7 +564,7 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
                     fx[d] = hi[d].ro * hi[d].u[m] * hi[d].u[d] - lo[d].ro * lo[d].u[m] * lo[d].u[d];
             }
             ucn[m] = divr(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx[0] * kk.ds[0] + fx[1] * kk.ds[1] + fx[2] * kk.ds[2]),
-                          den, rden);
+                          den, rden, false);
         }
     } else {
         // the same balance with the volume divided out and the density as a deviation:
@@ -719,7 +728,7 @@ __device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src,
                 if constexpr (!DEV) {
                     const T den = kk.dvc * ro_cn;
 #pragma unroll
-                    for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
+                    for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden, false);
                 } else {
                     use_forces_f32(ucn, f, dt, kk, rden);
                 }
@@ -823,7 +832,7 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
             if constexpr (!DEV) {
                 const T den = kk.dvc * ro_cn;
 #pragma unroll
-                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
+                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden, false);
             } else {
                 use_forces_f32(ucn, f, dt, kk, rden);
             }
@@ -867,7 +876,7 @@ template <class T> struct FaceQ {
 // The quantities of the face normal to d with values V: the mass flux ro u_d, the momentum
 // fluxes (ro u_m) u_d (+ p when m == d) of half_step, and StressTensor's sigma_md between the
 // cell below (flags flo, velocity ulo) and the cell above (fhi, uhi).
-template <class T, bool STRESS>
+template <class T, bool STRESS, bool ONE = false>
 __device__ __forceinline__ FaceQ<T> face_q(const FaceVal<T> &V, int d, uint8_t flo, uint8_t fhi, const T ulo[3],
                                            const T uhi[3], const K<T> &kk) {
     FaceQ<T> q;
@@ -875,12 +884,13 @@ __device__ __forceinline__ FaceQ<T> face_q(const FaceVal<T> &V, int d, uint8_t f
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         q.mom[m] = (m == d) ? V.ro * V.u[m] * V.u[d] + V.p : V.ro * V.u[m] * V.u[d];
-        q.sig[m] = STRESS ? sigma(flo, fhi, ulo[m], uhi[m], kk, d) : (T)0;
+        q.sig[m] = STRESS ? sigma(flo, fhi, ulo[m], uhi[m], kk, d, ONE) : (T)0;
     }
     return q;
 }
 
-template <class T, int MODE>
+// ONE: built for grid steps and cell volume whose reciprocals are within a quarter ulp (div_rn)
+template <class T, int MODE, bool ONE = false>
 __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constant__ DevState<T> S, int src, int dst, int fcur, int kch) {
     static_assert(!Storage<T>::deviation, "face-centric Phase1: FP64 storage form");
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
@@ -916,7 +926,7 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
         cellu(c, uc);
         T ud[3];
         if (STRESS) cellu(c - cs2, ud);
-        zlo = face_q<T, STRESS>(load_face(S.fc[fcur][2], f, kk), 2, STRESS ? flags[c - cs2] : 0, fl, STRESS ? ud : zero3,
+        zlo = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][2], f, kk), 2, STRESS ? flags[c - cs2] : 0, fl, STRESS ? ud : zero3,
                                 uc, kk);
     }
     for (int k = k0; k <= k1; ++k) {
@@ -931,29 +941,29 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
                 fn = flags[c - 1];
                 cellu(c - 1, un);
             }
-            Fx[ty][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][0], f, kk), 0, fn, fl, un, uc, kk);
+            Fx[ty][tx] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][0], f, kk), 0, fn, fl, un, uc, kk);
             if (i == ilast) {
                 if (STRESS) {
                     fn = flags[c + 1];
                     cellu(c + 1, un);
                 }
-                Fx[ty][tx + 1] = face_q<T, STRESS>(load_face(S.fc[fcur][0], f + 1, kk), 0, fl, fn, uc, un, kk);
+                Fx[ty][tx + 1] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][0], f + 1, kk), 0, fl, fn, uc, un, kk);
             }
             if (STRESS) {
                 fn = flags[c - cs1];
                 cellu(c - cs1, un);
             }
-            Fy[ty][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][1], f, kk), 1, fn, fl, un, uc, kk);
+            Fy[ty][tx] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][1], f, kk), 1, fn, fl, un, uc, kk);
             if (j == jlast) {
                 if (STRESS) {
                     fn = flags[c + cs1];
                     cellu(c + cs1, un);
                 }
-                Fy[ty + 1][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][1], f + fs1, kk), 1, fl, fn, uc, un, kk);
+                Fy[ty + 1][tx] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][1], f + fs1, kk), 1, fl, fn, uc, un, kk);
             }
             flu = flags[c + cs2];
             cellu(c + cs2, uu);
-            zhi = face_q<T, STRESS>(load_face(S.fc[fcur][2], f + fs2, kk), 2, fl, flu, uc, uu, kk);
+            zhi = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][2], f + fs2, kk), 2, fl, flu, uc, uu, kk);
         }
         __syncthreads();
         if (valid) {
@@ -964,7 +974,7 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
                 // half_step (main.cpp:530-551) over the face quantities
                 ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((Hx.mf - Lx.mf) * kk.ds[0] + (Hy.mf - Ly.mf) * kk.ds[1] +
                                                             (zhi.mf - zlo.mf) * kk.ds[2]),
-                             kk.dvc, kk.rdvc);
+                             kk.dvc, kk.rdvc, ONE);
                 const T den = ro_cn * kk.dvc;
                 const T rd = recip(den);
                 rden = rd;
@@ -972,7 +982,7 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
                 for (int m = 0; m < 3; ++m) {
                     const T fx0 = Hx.mom[m] - Lx.mom[m], fx1 = Hy.mom[m] - Ly.mom[m], fx2 = zhi.mom[m] - zlo.mom[m];
                     ucn[m] = divr(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx0 * kk.ds[0] + fx1 * kk.ds[1] + fx2 * kk.ds[2]),
-                                  den, rd);
+                                  den, rd, false);
                 }
             } else {
                 ucn[0] = ucn[1] = ucn[2] = (T)0;
@@ -1000,7 +1010,7 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
                 // UseForces (main.cpp:1035-1041)
                 const T den = kk.dvc * ro_cn;
 #pragma unroll
-                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * fv[m], den, rden);
+                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * fv[m], den, rden, false);
             }
             S.lv[dst].ro[c] = ro_cn;
             S.lv[dst].u1[c] = ucn[0];
@@ -1101,9 +1111,9 @@ template <class T> __global__ void k_use_forces(DevState<T> S, int ncon) {
         const T ro_cn = L.ro[c];
         const T den = kk.dvc * ro_cn;
         const T rden = recip(den);
-        L.u1[c] = divr(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den, rden);
-        L.u2[c] = divr(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den, rden);
-        L.u3[c] = divr(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den, rden);
+        L.u1[c] = divr(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den, rden, false);
+        L.u2[c] = divr(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den, rden, false);
+        L.u3[c] = divr(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den, rden, false);
     } else {
         T u[3] = {L.u1[c], L.u2[c], L.u3[c]};
         const T f[3] = {S.f[0][c], S.f[1][c], S.f[2][c]};
@@ -1124,12 +1134,13 @@ template <class T> struct Ext { T rf, qb, af, ab, bf, bb; };
 
 template <class T> struct SweepK {
     T sound, ro0, c2, rc2, roc, rroc, dt, rdt, dx, rdx;
+    bool one_c2, one_roc, one_dt, one_dx; // FP64: one correction suffices (div_rn)
 };
 
 // The gradient term of a limiter bound: a / dt + b / dx.  FP64: the two correctly rounded
 // quotients summed, as the reference evaluates it; FP32: a * (1/dt) + b * (1/dx), fused.
 __device__ __forceinline__ double grad_sum(double a, double b, const SweepK<double> &q) {
-    return divk(a, q.dt, q.rdt) + divk(b, q.dx, q.rdx);
+    return divk(a, q.dt, q.rdt, q.one_dt) + divk(b, q.dx, q.rdx, q.one_dx);
 }
 __device__ __forceinline__ float grad_sum(float a, float b, const SweepK<float> &q) { return __fmaf_rn(a, q.rdt, b * q.rdx); }
 
@@ -1145,8 +1156,8 @@ __device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T
     constexpr bool DEV = Storage<T>::deviation;
     const T p_cn = DEV ? q.c2 * ro_cn : q.c2 * (ro_cn - q.ro0);
     const T p_c = DEV ? q.c2 * ro_c : q.c2 * (ro_c - q.ro0);
-    const T pf = divk(p_f, q.roc, q.rroc), pb = divk(p_b, q.roc, q.rroc);
-    const T pcn = divk(p_cn, q.roc, q.rroc), pc = divk(p_c, q.roc, q.rroc);
+    const T pf = divk(p_f, q.roc, q.rroc, q.one_roc), pb = divk(p_b, q.roc, q.rroc, q.one_roc);
+    const T pcn = divk(p_cn, q.roc, q.rroc, q.one_roc), pc = divk(p_c, q.roc, q.rroc, q.one_roc);
 
     // 2x - y and max + dt*g: mad rounds these exactly as written in FP64, fused in FP32
     const T r_f = u1_f + pf, r_b = u1_b + pb, r_cn = u1_cn + pcn, r_c = u1_c + pc;
@@ -1230,7 +1241,7 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
         const T rn = prev.rf, qn = cur.qb;
         un = (rn + qn) / (T)2;
         pn = (rn - qn) * q.sound * q.ro0 / (T)2;
-        ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
+        ro_n = q.ro0 + divk(pn, q.c2, q.rc2, q.one_c2);
         if (ge0(ucf) && ge0(ucb)) {
             ua = prev.af;
             ub = prev.bf;
@@ -1255,7 +1266,7 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
             if (le0(ucf)) {
                 const T qn = cur.qb;
                 pn = -qn * q.sound * q.ro0;
-                ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
+                ro_n = q.ro0 + divk(pn, q.c2, q.rc2, q.one_c2);
                 ua = cur.ab;
                 ub = cur.bb;
             } else {
@@ -1268,7 +1279,7 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
             if (ge0(ucb)) {
                 const T rn = prev.rf;
                 pn = rn * q.sound * q.ro0;
-                ro_n = q.ro0 + divk(pn, q.c2, q.rc2);
+                ro_n = q.ro0 + divk(pn, q.c2, q.rc2, q.one_c2);
                 ua = prev.af;
                 ub = prev.bf;
             } else {
@@ -1309,7 +1320,10 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
     face_store(W, fc, face_values<T, WALL_A_FROM_N>(N, cb, cf, flb, flf, ucb, ucf, prev, cur, uA_old, uB_old, q));
 }
 
-template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d) {
+// one: the kernel was built for constants (rho0*c, c^2, the grid step) whose reciprocals are
+// within a quarter ulp, so their FP64 quotients take one correction (div_rn); dt, which changes
+// every step, always takes two
+template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d, bool one = false) {
     const KT<T> &k = kconst<T>(S.k);
     SweepK<T> q;
     q.sound = k.sound;
@@ -1322,6 +1336,10 @@ template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevSt
     q.rdt = sc_rdt<T>(S.sc);
     q.dx = k.dx[d];
     q.rdx = k.rdx[d];
+    q.one_c2 = one;
+    q.one_roc = one;
+    q.one_dx = one;
+    q.one_dt = false;
     return q;
 }
 
@@ -1389,7 +1407,8 @@ __device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, 
 // computed.  A face needs the forward values of the cell behind it: a shuffle from the
 // neighbouring lane, or the carry from the previous chunk's last lane.  Old faces come from
 // generation fcur, new faces go to fcur^1.
-template <class T> __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, const BIx &bx) {
+template <class T, bool ONE = false>
+__device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, const BIx &bx) {
     const Geom g = S.g;
     const int lane = threadIdx.x & 31;
     const int line = bx.x * 4 + (threadIdx.x >> 5);
@@ -1398,7 +1417,7 @@ template <class T> __device__ __forceinline__ void sweep_x_body(const DevState<T
     const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
     const FaceOut<T> W = sweep_out(S, fcur, 0);
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
-    const SweepK<T> q = sweep_consts(S, 0);
+    const SweepK<T> q = sweep_consts(S, 0, ONE);
     const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k);
     const int nd = g.C1 + 1;
     const bool bounded = !S.k.periodic_x;
@@ -1474,9 +1493,9 @@ template <class T> __device__ __forceinline__ void sweep_x_body(const DevState<T
 
 // FP32: capped at 80 registers for 6 blocks (24 warps) per SM (0.47 vs 0.50 ms at 512x256x256);
 // FP64: 3 blocks per SM, as without a bound.
-template <class T>
+template <class T, bool ONE = false>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_sweep_x(const __grid_constant__ DevState<T> S, int con, int fcur) {
-    sweep_x_body(S, con, fcur, bix_here());
+    sweep_x_body<T, ONE>(S, con, fcur, bix_here());
 }
 
 // x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,
@@ -1485,7 +1504,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_sweep_x(const _
 // cells s0..s1 (cell s0 is the one overlap with the previous segment); the face behind
 // the current cell is carried in registers.  Old faces come from generation fcur, new
 // faces go to fcur^1, so segments are independent.
-template <class T, int AX>
+template <class T, int AX, bool ONE = false>
 __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, int fcur, int seg, const BIx &bx) {
     const Geom g = S.g;
     const int i = bx.x * 128 + threadIdx.x + 1;
@@ -1497,7 +1516,7 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     const SweepSrc<T> R = sweep_src(S, con, fcur, AX);
     const FaceOut<T> W = sweep_out(S, fcur, AX);
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
-    const SweepK<T> q = sweep_consts(S, AX);
+    const SweepK<T> q = sweep_consts(S, AX, ONE);
     const int cst = AX == 1 ? (int)g.cs1 : (int)g.cs2, fst = AX == 1 ? (int)g.fs1 : (int)g.fs2;
     int c = (AX == 1 ? g.ci(i, 0, o) : g.ci(i, o, 0)) + s0 * cst;
     int fb = (AX == 1 ? g.fi(i, 0, o) : g.fi(i, o, 0)) + s0 * fst;
@@ -1524,9 +1543,9 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     }
 }
 
-template <class T, int AX>
+template <class T, int AX, bool ONE = false>
 __global__ void __launch_bounds__(128) k_sweep_col(const __grid_constant__ DevState<T> S, int con, int fcur, int seg) {
-    sweep_col_body<T, AX>(S, con, fcur, seg, bix_here());
+    sweep_col_body<T, AX, ONE>(S, con, fcur, seg, bix_here());
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1861,15 +1880,24 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
             const int kch = stg::staged_chunk(S.g);
             const dim3 grid((S.g.C1 + fcs::SX - 1) / fcs::SX, (S.g.C2 + fcs::SY - 1) / fcs::SY, (S.g.C3 + kch - 1) / kch);
             const dim3 block(fcs::SX, fcs::SY);
+            // the one-correction quotients where every constant this kernel divides by allows them
+            const KT<double> &kd = S.k.kd;
+            const bool one = kd.one_dx[0] && kd.one_dx[1] && kd.one_dx[2] && kd.one_dvc;
+            auto go = [&](auto k1, auto k0) {
+                if (one) k1<<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                else k0<<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+            };
             switch (mode) {
             case P1_STRESS | P1_FORCES | P1_RMAX:
-                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                go(fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX, true>,
+                   fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX, false>);
                 return;
             case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
-                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                go(fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, true>,
+                   fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, false>);
                 return;
             case P1_FORCES | P1_RSUM:
-                fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                go(fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM, true>, fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM, false>);
                 return;
             default: march = 0; break;
             }
@@ -1928,18 +1956,28 @@ inline int sweep_segment(int nd, int target, int *nseg) {
     return (nd + n - 1) / n;
 }
 
+// FP64: the one-correction quotients (div_rn) where rho0*c, c^2 and the sweep's grid step all
+// have reciprocals within a quarter ulp
 template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target) {
+    const KT<double> &kd = S.k.kd;
+    const bool one = std::is_same<T, double>::value && kd.one_roc && kd.one_c2 && kd.one_dx[axis];
     if (axis == 0) {
         const int lines_x = S.g.C2 * S.g.C3;
-        k_sweep_x<T><<<(lines_x + 3) / 4, 128, 0, st>>>(S, con, fcur);
+        const dim3 grid((lines_x + 3) / 4);
+        if (one) k_sweep_x<T, true><<<grid, 128, 0, st>>>(S, con, fcur);
+        else k_sweep_x<T, false><<<grid, 128, 0, st>>>(S, con, fcur);
     } else if (axis == 1) {
         int nseg;
         const int seg = sweep_segment(S.g.C2 + 1, target, &nseg);
-        k_sweep_col<T, 1><<<dim3((S.g.C1 + 127) / 128, S.g.C3, nseg), 128, 0, st>>>(S, con, fcur, seg);
+        const dim3 grid((S.g.C1 + 127) / 128, S.g.C3, nseg);
+        if (one) k_sweep_col<T, 1, true><<<grid, 128, 0, st>>>(S, con, fcur, seg);
+        else k_sweep_col<T, 1, false><<<grid, 128, 0, st>>>(S, con, fcur, seg);
     } else {
         int nseg;
         const int seg = sweep_segment(S.g.C3 + 1, target, &nseg);
-        k_sweep_col<T, 2><<<dim3((S.g.C1 + 127) / 128, S.g.C2, nseg), 128, 0, st>>>(S, con, fcur, seg);
+        const dim3 grid((S.g.C1 + 127) / 128, S.g.C2, nseg);
+        if (one) k_sweep_col<T, 2, true><<<grid, 128, 0, st>>>(S, con, fcur, seg);
+        else k_sweep_col<T, 2, false><<<grid, 128, 0, st>>>(S, con, fcur, seg);
     }
 }
 

@@ -238,7 +238,9 @@ int ark_vorticity(ark_ctx *ctx, double *out);
 
 /* Self-check of the correctly rounded division by a run constant that the FP64 kernels use
  * (q = a*RN(1/b) plus two Markstein corrections) against the GPU's IEEE division, on n
- * random operand pairs and on small exact cases; *mismatches receives the count (0 expected).
+ * random operand pairs and on small exact cases, in both its forms (two correction steps, and
+ * one where the divisor's reciprocal is within a quarter ulp); *mismatches receives the count
+ * (0 expected).
  * Runs on the current device. */
 int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches);
 
