@@ -1149,26 +1149,41 @@ __device__ __forceinline__ float grad_sum(float a, float b, const SweepK<float> 
 // ro_cn/ro_c: density (FP64) or density deviation (FP32).  Q_USES_R selects the x1/x3 form
 // of the Q-limiter source, 2*(r_cn - r_c)/dt (main.cpp:1804, 2321); the x2 sweep uses
 // 2*(q_cn - q_c)/dt (main.cpp:2083).
+// 2x - y.  The product 2x is exact, so one fused multiply-add rounds it exactly as the
+// reference's separate multiply and subtract do (both precisions).
+__device__ __forceinline__ double twice_minus(double x, double y) { return __fma_rn(2.0, x, -y); }
+__device__ __forceinline__ float twice_minus(float x, float y) { return __fmaf_rn(2.f, x, -y); }
+
+// The Riemann invariants of a face, R = u_n + p/(ro0 c) and Q = u_n - p/(ro0 c)
+// (main.cpp:1790-1797).  The sweeps compute them once per face and hand them to the cell ahead.
+template <class T> struct RQ { T r, q; };
+template <class T> __device__ __forceinline__ RQ<T> face_rq(T u_n, T p, const SweepK<T> &q) {
+    const T pf = divk(p, q.roc, q.rroc, q.one_roc);
+    RQ<T> v;
+    v.r = u_n + pf;
+    v.q = u_n - pf;
+    return v;
+}
+
+// The extrapolation with the invariants of the forward (f) and backward (b) face given.
 template <class T, bool Q_USES_R>
-__device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T u2_f, T u2_b, T u2_cn,
-                                              T u2_c, T u3_f, T u3_b, T u3_cn, T u3_c, T ro_cn, T ro_c,
-                                              T p_f, T p_b, const SweepK<T> &q) {
+__device__ __forceinline__ Ext<T> extrapolate_rq(RQ<T> f, RQ<T> b, T u1_cn, T u1_c, T u2_f, T u2_b, T u2_cn, T u2_c,
+                                                 T u3_f, T u3_b, T u3_cn, T u3_c, T ro_cn, T ro_c, const SweepK<T> &q) {
     constexpr bool DEV = Storage<T>::deviation;
     const T p_cn = DEV ? q.c2 * ro_cn : q.c2 * (ro_cn - q.ro0);
     const T p_c = DEV ? q.c2 * ro_c : q.c2 * (ro_c - q.ro0);
-    const T pf = divk(p_f, q.roc, q.rroc, q.one_roc), pb = divk(p_b, q.roc, q.rroc, q.one_roc);
     const T pcn = divk(p_cn, q.roc, q.rroc, q.one_roc), pc = divk(p_c, q.roc, q.rroc, q.one_roc);
 
-    // 2x - y and max + dt*g: mad rounds these exactly as written in FP64, fused in FP32
-    const T r_f = u1_f + pf, r_b = u1_b + pb, r_cn = u1_cn + pcn, r_c = u1_c + pc;
-    T r_fn = mad((T)2, r_cn, -r_b);
-    const T q_f = u1_f - pf, q_b = u1_b - pb, q_cn = u1_cn - pcn, q_c = u1_c - pc;
-    T q_bn = mad((T)2, q_cn, -q_f);
+    // max + dt*g: mad rounds it exactly as written in FP64, fused in FP32
+    const T r_f = f.r, r_b = b.r, r_cn = u1_cn + pcn, r_c = u1_c + pc;
+    T r_fn = twice_minus(r_cn, r_b);
+    const T q_f = f.q, q_b = b.q, q_cn = u1_cn - pcn, q_c = u1_c - pc;
+    T q_bn = twice_minus(q_cn, q_f);
 
-    T u2_fn = mad((T)2, u2_cn, -u2_b);
-    T u2_bn = mad((T)2, u2_cn, -u2_f);
-    T u3_fn = mad((T)2, u3_cn, -u3_b);
-    T u3_bn = mad((T)2, u3_cn, -u3_f);
+    T u2_fn = twice_minus(u2_cn, u2_b);
+    T u2_bn = twice_minus(u2_cn, u2_f);
+    T u3_fn = twice_minus(u3_cn, u3_b);
+    T u3_bn = twice_minus(u3_cn, u3_f);
 
     const T gr = grad_sum((T)2 * (r_cn - r_c), (u1_cn + q.sound) * (r_f - r_b), q);
     const T gq = grad_sum((T)2 * (Q_USES_R ? (r_cn - r_c) : (q_cn - q_c)), (u1_cn - q.sound) * (q_f - q_b), q);
@@ -1204,6 +1219,15 @@ __device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T
     e.bf = u3_fn;
     e.bb = u3_bn;
     return e;
+}
+
+// The same from the faces' normal velocities and pressures.
+template <class T, bool Q_USES_R>
+__device__ __forceinline__ Ext<T> extrapolate(T u1_f, T u1_b, T u1_cn, T u1_c, T u2_f, T u2_b, T u2_cn,
+                                              T u2_c, T u3_f, T u3_b, T u3_cn, T u3_c, T ro_cn, T ro_c,
+                                              T p_f, T p_b, const SweepK<T> &q) {
+    return extrapolate_rq<T, Q_USES_R>(face_rq(u1_f, p_f, q), face_rq(u1_b, p_b, q), u1_cn, u1_c, u2_f, u2_b, u2_cn,
+                                       u2_c, u3_f, u3_b, u3_cn, u3_c, ro_cn, ro_c, q);
 }
 
 // Half-step cell values a face update may need in its rarer branches (loaded on demand).
@@ -1425,29 +1449,38 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     T carry_u = 0;
     uint8_t carry_fl = 0;
     SweepIn<T> cur = {}, nxt = {};
-    T uN_b = 0, uA_b = 0, uB_b = 0, p_b = 0, nuN_b = 0, nuA_b = 0, nuB_b = 0, np_b = 0;
+    T uA_b = 0, uB_b = 0, nuA_b = 0, nuB_b = 0;
+    // the invariants of a cell's backward face are those the cell behind computed for its
+    // forward face: a shuffle from the neighbouring lane, across chunks the carry from the last
+    // lane, and for cell 0 the face 0 itself
+    RQ<T> carry_rq = {(T)0, (T)0};
     if (lane <= nd) {
         sweep_load(R, c0 + lane, f0 + lane + 1, cur);
-        uN_b = R.FN[f0 + lane];
         uA_b = R.FA[f0 + lane];
         uB_b = R.FB[f0 + lane];
-        p_b = R.FP[f0 + lane];
     }
+    if (lane == 0) carry_rq = face_rq(R.FN[f0], R.FP[f0], q);
     for (int s0 = 0; s0 <= nd; s0 += 32) {
         const int s = s0 + lane;
         const bool act = s <= nd;
         const int sn = s + 32;
         if (sn <= nd) {
             sweep_load(R, c0 + sn, f0 + sn + 1, nxt);
-            nuN_b = R.FN[f0 + sn];
             nuA_b = R.FA[f0 + sn];
             nuB_b = R.FB[f0 + sn];
-            np_b = R.FP[f0 + sn];
         }
+        RQ<T> rqf = {(T)0, (T)0};
+        if (act) rqf = face_rq(cur.uN_f, cur.p_f, q);
+        RQ<T> rqb;
+        rqb.r = __shfl_up_sync(0xffffffffu, rqf.r, 1);
+        rqb.q = __shfl_up_sync(0xffffffffu, rqf.q, 1);
+        if (lane == 0) rqb = carry_rq;
+        carry_rq.r = __shfl_sync(0xffffffffu, rqf.r, 31);
+        carry_rq.q = __shfl_sync(0xffffffffu, rqf.q, 31);
         Ext<T> e = {};
         if (act)
-            e = extrapolate<T, true>(cur.uN_f, uN_b, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA, cur.uB_f, uB_b,
-                                     cur.nB, cur.cB, cur.nR, cur.cR, cur.p_f, p_b, q);
+            e = extrapolate_rq<T, true>(rqf, rqb, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA, cur.uB_f, uB_b, cur.nB,
+                                        cur.cB, cur.nR, cur.cR, q);
         if (bounded) {
             // a bounded x axis sweeps cells 1..C1 only; the edge faces take the reference's
             // inflow invariant R = 1 (0 behind a solid first cell) and outflow Q = 5/6 with
@@ -1484,10 +1517,8 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         if (act && s >= 1)
             face_update<T, false>(N, W, c0 + s - 1, c0 + s, f0 + s, flb, cur.fl, ucb, cur.nN, prev, e, uA_b, uB_b, q);
         cur = nxt;
-        uN_b = nuN_b;
         uA_b = nuA_b;
         uB_b = nuB_b;
-        p_b = np_b;
     }
 }
 
@@ -1520,7 +1551,8 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     const int cst = AX == 1 ? (int)g.cs1 : (int)g.cs2, fst = AX == 1 ? (int)g.fs1 : (int)g.fs2;
     int c = (AX == 1 ? g.ci(i, 0, o) : g.ci(i, o, 0)) + s0 * cst;
     int fb = (AX == 1 ? g.fi(i, 0, o) : g.fi(i, o, 0)) + s0 * fst;
-    T uN_b = R.FN[fb], uA_b = R.FA[fb], uB_b = R.FB[fb], p_b = R.FP[fb];
+    T uA_b = R.FA[fb], uB_b = R.FB[fb];
+    RQ<T> rqb = face_rq(R.FN[fb], R.FP[fb], q); // then the forward face's, carried
     SweepIn<T> cur, nxt = {};
     sweep_load(R, c, fb + fst, cur);
     Ext<T> prev = {};
@@ -1528,17 +1560,17 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     uint8_t flprev = 0;
     for (int s = s0; s <= s1; ++s, c += cst, fb += fst) {
         if (s < s1) sweep_load(R, c + cst, fb + 2 * fst, nxt);
-        const Ext<T> e = extrapolate<T, AX == 2>(cur.uN_f, uN_b, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA,
-                                                 cur.uB_f, uB_b, cur.nB, cur.cB, cur.nR, cur.cR, cur.p_f, p_b, q);
+        const RQ<T> rqf = face_rq(cur.uN_f, cur.p_f, q);
+        const Ext<T> e = extrapolate_rq<T, AX == 2>(rqf, rqb, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA, cur.uB_f,
+                                                    uB_b, cur.nB, cur.cB, cur.nR, cur.cR, q);
         if (s > s0)
             face_update<T, AX == 1>(N, W, c - cst, c, fb, flprev, cur.fl, uprev, cur.nN, prev, e, uA_b, uB_b, q);
         prev = e;
         uprev = cur.nN;
         flprev = cur.fl;
-        uN_b = cur.uN_f;
+        rqb = rqf;
         uA_b = cur.uA_f;
         uB_b = cur.uB_f;
-        p_b = cur.p_f;
         cur = nxt;
     }
 }
