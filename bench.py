@@ -82,6 +82,20 @@ def ncu_traffic_per_cell():
     return out
 
 
+def ncu_fp64_pipe():
+    """FP64 pipe activity (fraction of its peak) of each FP64 kernel from the committed ncu
+    summary (or {})."""
+    path = os.path.join(ROOT, "profiles", "fp64_pipe_per_kernel.txt")
+    out = {}
+    if os.path.isfile(path):
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 3 and not line.startswith("#"):
+                    out[(parts[0], parts[1])] = float(parts[2]) / 100.0
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
 
@@ -201,10 +215,16 @@ def roofline(kt, cells, word, peak, peak_kind, traffic_tab, prec_name):
     algo = cells * (vals * word + flag_b)
     achieved = algo / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
     tpc = traffic_tab.get((prec_name, name))
-    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-            "traffic": (round(tpc * cells) if tpc is not None else None),
-            "algorithmic_bytes": algo, "launch_ms": round(ms, 4)}
+    r = {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+         "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+         "traffic": (round(tpc * cells) if tpc is not None else None),
+         "algorithmic_bytes": algo, "launch_ms": round(ms, 4)}
+    pipe = ncu_fp64_pipe().get((prec_name, name)) if prec_name == "fp64" else None
+    if pipe is not None:
+        # the FP64 kernels issue FP64 arithmetic at the pipe's limit; HBM is far from it
+        r["fp64_pipe"] = {"active_frac": pipe, "source": "ncu sm__pipe_fp64_cycles_active (profiles)",
+                          "note": "bound by FP64 issue (GB300 FP64 is about 1.2 TFLOP/s), not by HBM"}
+    return r
 
 
 def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
