@@ -114,6 +114,20 @@ __global__ void __launch_bounds__(kTileX *kTileY) kb_phase1(const DS *__restrict
     }
 }
 
+// Phase1 with its planes staged in shared memory: work item = a member's 64 x 4 tile and chunk of
+// planes (the member's chunk length in W.extra), the single-context kernel's body.
+template <int MODE>
+__global__ void __launch_bounds__(stg::NT, 2) kb_phase1_staged(const DS *__restrict__ inst, WorkList W, int src, int dst,
+                                                               int fcur) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ stg::RowTable rt;
+    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+        const int q = find_member(W, b);
+        stg::phase1_staged_body<MODE>(inst[q], src, dst, fcur, W.extra[q], decode(W, q, b), sm, rt);
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(128) kb_sweep_x(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
@@ -130,11 +144,12 @@ __global__ void __launch_bounds__(128) kb_sweep_col(const DS *__restrict__ inst,
 }
 
 // Kinds of work list.
-enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_COUNT };
+enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, WL_COUNT };
 
 // The candidate kernel shapes the autotuner chooses between.
 struct Shape {
-    int march_a, march_b; // Phase1 with stress / second Phase1: 1 marching, 0 one cell per thread
+    int march_a, march_b; // Phase1 with stress / second Phase1: 0 one cell per thread, 1 marching,
+                          // 2 planes staged in shared memory
     int seg;              // target faces per thread segment in the x2/x3 sweeps
 };
 
@@ -156,6 +171,7 @@ struct ark_ensemble {
     int total[WL_COUNT] = {};
     WrapJob *d_jobs = nullptr; // [6][n]: wrap_con for level 0/1, wrap_phase2 for (con, fcur)
     int persist = 1;           // persistent blocks per launch (all SMs x resident blocks)
+    int persist_staged = 1;    // the same for the staged Phase1 (2 blocks of 256 threads per SM)
     Shape shape = {1, 0, 32};
     int con = 0, fcur = 0;
     bool parts_valid = false;
@@ -177,7 +193,8 @@ template <class U> int ens_alloc(ark_ensemble *E, U **out, size_t n) {
     return ARK_OK;
 }
 
-Geom geom_of(const ark_params &p) { return device_geom(p.n1_cells, p.n2_cells, p.n3_cells, false); }
+// rows padded as the staged Phase1 needs (its 68-value row segments stay inside a row)
+Geom geom_of(const ark_params &p) { return device_geom(p.n1_cells, p.n2_cells, p.n3_cells, true); }
 
 int alloc_member(ark_ensemble *E, DS &S) {
     const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
@@ -238,6 +255,13 @@ int build_lists(ark_ensemble *E) {
             case WL_WRAP: { // one thread per ghost line, looping over the job's arrays
                 const int64_t tot = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
                 gx = (int)((tot + 127) / 128);
+                break;
+            }
+            case WL_STAGED: { // 64 x 4 tiles and chunks of planes of the staged Phase1
+                const int kch = stg::staged_chunk(g);
+                extra[q] = kch;
+                const dim3 gr = stg::staged_grid(g, kch);
+                gx = (int)gr.x, gy = (int)gr.y, gz = (int)gr.z;
                 break;
             }
             }
@@ -302,12 +326,33 @@ WorkList wl(const ark_ensemble *E, int kind) {
 
 int grid_of(const ark_ensemble *E, int kind) { return std::max(1, std::min(E->total[kind], E->persist)); }
 
-template <int MODE> void launch_p1(ark_ensemble *E, bool march, int src, int dst, int fcur) {
+template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst, int fcur) {
     const dim3 blk(kTileX, kTileY);
-    if (march)
+    if (march == 2) {
+        const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
+        kb_phase1_staged<MODE><<<grid, dim3(stg::SX, stg::SY), stg::Layout<MODE>::SMEM, E->st>>>(
+            E->d_inst, wl(E, WL_STAGED), src, dst, fcur);
+    } else if (march == 1) {
         kb_phase1<MODE, true><<<grid_of(E, WL_TILES), blk, 0, E->st>>>(E->d_inst, wl(E, WL_TILES), src, dst, fcur);
-    else
+    } else {
         kb_phase1<MODE, false><<<grid_of(E, WL_CELLS), blk, 0, E->st>>>(E->d_inst, wl(E, WL_CELLS), src, dst, fcur);
+    }
+}
+
+// The staged kernels' shared-memory limits (once per process) and their resident blocks per SM.
+int prepare_staged_kernels(int sms) {
+    auto one = [](auto kern, int smem) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, stg::NT, smem);
+        return per;
+    };
+    int per = one(kb_phase1_staged<P1_STRESS | P1_FORCES | P1_RMAX>, stg::Layout<P1_STRESS | P1_FORCES | P1_RMAX>::SMEM);
+    per = std::min(per, one(kb_phase1_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
+                            stg::Layout<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>::SMEM));
+    per = std::min(per, one(kb_phase1_staged<P1_FORCES | P1_RSUM>, stg::Layout<P1_FORCES | P1_RSUM>::SMEM));
+    return sms * std::max(per, 1);
 }
 
 // One step of every member (the order of main.cpp:82-91, as the single-context fused step).
@@ -454,6 +499,7 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_phase1<P1_FORCES | P1_RSUM, false>, kTileX * kTileY, 0);
     E->persist = sms * std::max(per, 1) * 2;
+    E->persist_staged = prepare_staged_kernels(sms);
     if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get()))) return nullptr;
     cudaEventCreate(&E->ev0);
     cudaEventCreate(&E->ev1);
@@ -692,7 +738,7 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
     for (char u : E->uploaded)
         if (!u) return efail(ARK_ERR_STATE, "every member needs a state before tuning");
     const Shape cands[] = {{1, 0, 32}, {0, 0, 32}, {1, 1, 32}, {0, 1, 32}, {1, 0, 16}, {1, 0, 64},
-                           {0, 0, 16}, {0, 0, 64}};
+                           {0, 0, 16}, {0, 0, 64}, {2, 2, 32}, {2, 0, 32}, {0, 2, 32}, {2, 2, 64}, {2, 0, 64}};
     Shape best = E->shape;
     double best_ms = 1e300;
     if (int rc = ensure_parts(E)) return rc;
@@ -724,7 +770,8 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
 int ark_ensemble_set_shape(ark_ensemble *E, int march_a, int march_b, int segment) {
     if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
     if (segment < 1) return efail(ARK_ERR_PARAM, "segment < 1");
-    E->shape = Shape{march_a != 0, march_b != 0, segment};
+    if (march_a < 0 || march_a > 2 || march_b < 0 || march_b > 2) return efail(ARK_ERR_PARAM, "march must be 0, 1 or 2");
+    E->shape = Shape{march_a, march_b, segment};
     drop_graphs(E);
     return build_lists(E);
 }

@@ -216,20 +216,27 @@ template <int MAXR> struct MyCopies {
     }
 };
 
+// A block's copy plan expanded into rows (shared memory; filled by thread 0).
+struct RowTable {
+    Row rows[kMaxRows], frows[kMaxFlagRows];
+    int nrow, nfrow;
+};
+
+// One block's work: tile (bx.x, bx.y) of 64 x 4 columns, planes of chunk bx.z (kch planes); sm
+// holds the stages (Layout<MODE>::SMEM bytes).  Every thread of the block calls it; it ends with
+// no copy in flight, so a persistent kernel may run it again for another tile.
 template <int MODE>
-__global__ void __launch_bounds__(NT, 2)
-    k_phase1_staged(const __grid_constant__ DevState<float> S, int src, int dst, int fcur, int kch) {
+__device__ __forceinline__ void phase1_staged_body(const DevState<float> &S, int src, int dst, int fcur, int kch,
+                                                   const BIx &bx, unsigned char *sm, RowTable &rt) {
     using L = Layout<MODE>;
     using T = float;
     constexpr bool STRESS = L::STRESS;
-    extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ Row rows[kMaxRows], frows[kMaxFlagRows];
-    __shared__ int nrow, nfrow;
+    Row *rows = rt.rows, *frows = rt.frows;
     const Geom g = S.g;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * SX + tx;
-    const int bxi = blockIdx.x, byi = blockIdx.y;
+    const int bxi = bx.x, byi = bx.y;
     const int i = bxi * SX + tx + 1, j = byi * SY + ty + 1;
-    const int k0 = blockIdx.z * kch + 1;
+    const int k0 = bx.z * kch + 1;
     const int k1 = k0 + kch - 1 < g.C3 ? k0 + kch - 1 : g.C3;
     const int pfirst = STRESS ? k0 - 1 : k0, plast = k1 + 1;
     const unsigned sbase = smem_u32(sm);
@@ -238,15 +245,15 @@ __global__ void __launch_bounds__(NT, 2)
         const int ng = build_groups<MODE>(G, g, bases_of<MODE>(S, src, fcur), bxi, byi);
         int a, b;
         expand_rows(G, ng, rows, a, frows, b);
-        nrow = a;
-        nfrow = b;
+        rt.nrow = a;
+        rt.nfrow = b;
     }
     __syncthreads();
     // float rows: thread t copies chunk t % 17 of rows t / 17, t / 17 + 15, ...; flag rows: the
     // first 5 * (flag rows) threads one chunk each
     constexpr int kMine = (L::ROWS + NT / kChunks - 1) / (NT / kChunks);
     MyCopies<kMine> mine;
-    mine.template resolve<NT>(rows, nrow, frows, nfrow, t);
+    mine.template resolve<NT>(rows, rt.nrow, frows, rt.nfrow, t);
     auto issue = [&](int p) {
         const unsigned to = sbase + (unsigned)(((p - pfirst) % NS) * L::STAGE);
         const unsigned kind = p < k0 ? DOWN : (p > k1 ? TOP : MID);
@@ -359,10 +366,15 @@ __global__ void __launch_bounds__(NT, 2)
         }
     }
     cp_wait<0>();
-    if (MODE & (P1_RMAX | P1_RSUM)) {
-        const BIx bx = {bxi, byi, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y};
-        tile_store<T, NT>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
-    }
+    if (MODE & (P1_RMAX | P1_RSUM)) tile_store<T, NT>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(NT, 2)
+    k_phase1_staged(const __grid_constant__ DevState<float> S, int src, int dst, int fcur, int kch) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ RowTable rt;
+    phase1_staged_body<MODE>(S, src, dst, fcur, kch, bix_here(), sm, rt);
 }
 
 template <int MODE> inline void launch_staged(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st) {

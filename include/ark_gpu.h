@@ -336,11 +336,13 @@ int ark_ensemble_time_steps(ark_ensemble *ens, int nsteps, double *ms);
 int ark_ensemble_kernel_times(ark_ensemble *ens, int nsteps, double *ms, int cap, int *count);
 int ark_ensemble_get_scalars(ark_ensemble *ens, int member, ark_scalars *out);
 int ark_ensemble_mean_profile(ark_ensemble *ens, int member, double *mean_u1, double *wall_shear);
-/* Times each candidate kernel shape (Phase1 marching or one cell per thread for each Phase1,
- * x2/x3 sweep segment length) for steps_per_candidate steps on the live state -- the
- * results do not depend on the shape -- and keeps the fastest.  choice (4 ints, or NULL):
- * {Phase1+stress marching, second Phase1 marching, segment target, microseconds per step}. */
+/* Times each candidate kernel shape (for each Phase1: 0 one cell per thread, 1 marching, 2 planes
+ * staged in shared memory; the x2/x3 sweep segment length) for steps_per_candidate steps on the
+ * live state -- the results do not depend on the shape -- and keeps the fastest.  choice (4
+ * ints, or NULL): {Phase1+stress shape, second Phase1 shape, segment target, microseconds per
+ * step}. */
 int ark_ensemble_autotune(ark_ensemble *ens, int steps_per_candidate, int *choice);
+/* Sets the kernel shape directly (march_a / march_b: 0, 1 or 2 as above). */
 int ark_ensemble_set_shape(ark_ensemble *ens, int march_a, int march_b, int segment);
 
 /* ---- host-side helpers (no GPU needed) ----------------------------------------------------- */

@@ -93,12 +93,15 @@ def test_no_gpu_means_error_not_crash(ark):
 
 
 @pytest.mark.parametrize("C", [(1, 1, 1), (5, 3, 2), (64, 4, 32), (65, 5, 33), (130, 9, 70), (200, 7, 31),
-                               (63, 12, 64), (17, 3, 1), (512, 8, 33), (96, 64, 64)])
+                               (63, 12, 64), (17, 3, 1), (512, 8, 33), (96, 64, 64),
+                               # the benchmark ensemble's member grids (the ensemble runs the same plan)
+                               (32, 32, 32), (64, 32, 32), (64, 48, 48), (128, 64, 64)])
 @pytest.mark.parametrize("kch", [0, 8, 32])
 def test_staged_phase1_copy_plan(ark, C, kch):
     """The staged FP32 Phase1 copies row segments into shared memory 16 bytes at a time;
     before it runs anywhere its copy plan is checked on the host: every copy inside its array
     and stage and aligned, no byte copied twice, and every shared-memory read of every thread
-    mapped to the element the one-cell kernel reads."""
+    mapped to the element the one-cell kernel reads (and the same for the one-kernel Phase2 +
+    second Phase1)."""
     n, msg = ark.staging_selftest(*C, planes_per_block=kch)
     assert n == 0, msg

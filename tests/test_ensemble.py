@@ -51,6 +51,24 @@ def test_ensemble_matches_single_contexts(ark, port):
                 assert bits_equal(port.interior(n, got[n]), port.interior(n, want[q][0][n])), (q, n)
 
 
+@pytest.mark.parametrize("shape", [(2, 2, 32), (2, 0, 16), (0, 2, 64), (1, 2, 32)])
+def test_ensemble_shapes_match_single_contexts(ark, port, shape):
+    """Every Phase1 shape (one cell per thread, marching, planes staged in shared memory: a
+    persistent kernel over every member's tiles) gives each member the single-context bits."""
+    mem = members(ark)
+    want = singles(ark, mem, 5)
+    with ark.Ensemble([p for p, _ in mem]) as E:
+        E.set_shape(*shape)
+        for q, (_, st) in enumerate(mem):
+            E.upload(q, st)
+        E.step(5)
+        E.sync()
+        for q in range(len(mem)):
+            got = E.download(q, CELLS + FACES)
+            for n in CELLS + FACES:
+                assert bits_equal(port.interior(n, got[n]), port.interior(n, want[q][0][n])), (shape, q, n)
+
+
 def test_ensemble_autotune_keeps_results(ark, port):
     """The autotuner advances the live state while it times the candidate shapes; the
     result is the same as plain steps."""
