@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import hashlib
+import platform
 import os
 import shutil
 import subprocess
@@ -60,7 +61,7 @@ def _digest(extra=()):
 def build(force=False, verbose=False):
     os.makedirs(OBJ, exist_ok=True)
     stamp = os.path.join(OUT, ".stamp")
-    dig = _digest()
+    dig = _digest((platform.machine(),))  # a build for another architecture never counts as current
     if not force and os.path.isfile(LIB) and os.path.isfile(RUN) and os.path.isfile(stamp):
         with open(stamp) as f:
             if f.read().strip() == dig:

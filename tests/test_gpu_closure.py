@@ -132,6 +132,33 @@ def test_closure_changes_the_flow_and_fp64_is_refused(ark, port):
             assert e.value.status == 6
 
 
+def test_closure_step_in_both_phase2_forms(ark, port, monkeypatch):
+    """The closure's branch (nu_t beside dt and the ghost fill) joins before the stress; the rest
+    of the step may run as separate kernels or as the one-kernel Phase2 + second Phase1: the same
+    bits either way, with a network that makes nu_t vary from cell to cell."""
+    m = oc()
+    p = port.channel_params(40, 12, 10, seed=6)
+    gp = ark.make_params(40, 12, 10, vis=p["nu"], sound=p["sound"], rho0=p["rho0"], cfl=p["cfl"], lx=p["lx"],
+                         ly=p["ly"], lz=p["lz"], ub=p["ub"], precision=ark.FP32)
+    theta = np.random.default_rng(3).normal(0.0, 0.3, m.NPARAM)
+    names = ["u1nCon", "u2nCon", "u3nCon", "ronCon", "p1", "u11", "p2", "u32", "nut"]
+    got = []
+    with ark.Mlp() as net:
+        net.set(theta, np.zeros(m.NIN), np.ones(m.NIN))
+        for form in ("0", "2"):
+            monkeypatch.setenv("ARK_PHASE2_FUSED", form)
+            with ark.Context(gp) as c:
+                c.upload(port.channel_state(p))
+                c.set_closure(net, u_tau=0.05)
+                c.step(4)
+                c.sync()
+                got.append(c.download(names[:-1]))
+                got[-1]["nut"] = c.get("nut")
+    assert np.any(got[0]["nut"])
+    for n in names:
+        assert np.array_equal(got[0][n].view(np.uint64), got[1][n].view(np.uint64)), n
+
+
 def test_trained_network_beats_no_closure_on_held_out_samples(ark, port):
     """A-priori: trained on the filtered fields of one perturbed channel, the network predicts
     the eddy viscosity of another (held out) with a smaller error than no closure (nu_t = 0)

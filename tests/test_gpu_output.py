@@ -73,6 +73,29 @@ def test_average_values_call_equals_averaging_in_step(ark, port):
         assert bits_equal(a.get("averageU1"), b.get("averageU1"))
 
 
+def test_fp32_averages_in_both_phase2_forms(ark, port, monkeypatch):
+    """FP32: the averaging kernel at the end of the step reads the new level, which the one-kernel
+    Phase2 + second Phase1 writes into the spare level; averages, and the step, equal the
+    separate kernels' bit for bit, and the per-step calls equal the in-step averaging."""
+    p = port.channel_params(40, 12, 10, seed=5)
+    got = []
+    for form in ("0", "2"):
+        monkeypatch.setenv("ARK_PHASE2_FUSED", form)
+        with ctx_from(ark, port, p, precision=ark.FP32) as a, ctx_from(ark, port, p, precision=ark.FP32) as b:
+            a.set_averaging(True)
+            a.step(5)
+            for _ in range(5):
+                b.step(1)
+                b.average_values()
+            a.sync()
+            b.sync()
+            for m in (1, 2, 3):
+                assert bits_equal(a.get(f"averageU{m}"), b.get(f"averageU{m}")), (form, m)
+            got.append([a.get(f"averageU{m}") for m in (1, 2, 3)] + [a.get("u1nCon")])
+    for x, y in zip(got[0], got[1]):
+        assert bits_equal(x, y)
+
+
 @pytest.mark.parametrize("C,prec", [((64, 32, 32), "fp64"), ((128, 96, 96), "fp64"), ((40, 24, 20), "fp32")])
 def test_vtk_full_and_vorticity_match_restatement(ark, port, tmp_path, C, prec):
     """128x96x96 is streamed in two slabs of k planes (double-buffered); FP32 contexts write
