@@ -284,6 +284,35 @@ def test_fp32_per_phase_equals_fused(ark, port):
         assert bits_equal(port.interior(n, outs[0][n]), port.interior(n, outs[1][n])), n
 
 
+def test_fp32_steps_and_pieces_interleaved_in_both_phase2_forms(ark, port, monkeypatch):
+    """Graph-captured steps, a step made of the reference-order calls, per-launch timed steps and
+    steps again: the one-kernel Phase2 + second Phase1 rotates the cell levels through its spare
+    (and recaptures its graphs when the rotation meets them with other buffers) and ends with
+    the separate kernels' bits."""
+    p = port.channel_params(40, 12, 10, seed=9)
+    st0 = port.channel_state(p)
+    outs = []
+    for form in ("0", "2"):
+        monkeypatch.setenv("ARK_PHASE2_FUSED", form)
+        with ark.Context(params_from(ark, p, precision=ark.FP32)) as c:
+            c.upload(st0)
+            c.step(3)
+            c.time_step_size()
+            c.phase1()
+            c.stress_tensor()
+            c.use_forces()
+            c.phase2()
+            c.phase1()
+            c.use_forces()
+            c.step(2)
+            c.kernel_times(1)
+            c.step(1)
+            c.sync()
+            outs.append(c.download(CELLS + FACES))
+    for n in CELLS + FACES:
+        assert bits_equal(port.interior(n, outs[0][n]), port.interior(n, outs[1][n])), n
+
+
 @pytest.mark.parametrize("C", [(40, 20, 36), (130, 9, 70), (64, 4, 32), (7, 3, 1)])
 def test_phase1_kernel_shapes_agree(ark, port, monkeypatch, C):
     """The marching, the one-cell-per-thread, the shared-memory-staged (FP32) and the
