@@ -1345,9 +1345,10 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
 }
 
 // one: the kernel was built for constants (rho0*c, c^2, the grid step) whose reciprocals are
-// within a quarter ulp, so their FP64 quotients take one correction (div_rn); dt, which changes
-// every step, always takes two
-template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d, bool one = false) {
+// within a quarter ulp, so their FP64 quotients take one correction (div_rn); one_dt: the same for
+// this step's dt (the sweep kernels test it once and run the matching build of their body)
+template <class T>
+__device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d, bool one = false, bool one_dt = false) {
     const KT<T> &k = kconst<T>(S.k);
     SweepK<T> q;
     q.sound = k.sound;
@@ -1363,7 +1364,7 @@ template <class T> __device__ __forceinline__ SweepK<T> sweep_consts(const DevSt
     q.one_c2 = one;
     q.one_roc = one;
     q.one_dx = one;
-    q.one_dt = false;
+    q.one_dt = one_dt;
     return q;
 }
 
@@ -1431,7 +1432,7 @@ __device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, 
 // computed.  A face needs the forward values of the cell behind it: a shuffle from the
 // neighbouring lane, or the carry from the previous chunk's last lane.  Old faces come from
 // generation fcur, new faces go to fcur^1.
-template <class T, bool ONE = false>
+template <class T, bool ONE = false, bool ONE_DT = false>
 __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, const BIx &bx) {
     const Geom g = S.g;
     const int lane = threadIdx.x & 31;
@@ -1441,7 +1442,7 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
     const FaceOut<T> W = sweep_out(S, fcur, 0);
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
-    const SweepK<T> q = sweep_consts(S, 0, ONE);
+    const SweepK<T> q = sweep_consts(S, 0, ONE, ONE_DT);
     const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k);
     const int nd = g.C1 + 1;
     const bool bounded = !S.k.periodic_x;
@@ -1524,9 +1525,18 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
 
 // FP32: capped at 80 registers for 6 blocks (24 warps) per SM (0.47 vs 0.50 ms at 512x256x256);
 // FP64: 3 blocks per SM, as without a bound.
+// FP64: whether this step's dt has a reciprocal within a quarter ulp (its quotients then take one
+// correction); the same answer in every thread, so the branch between the two builds of a sweep
+// body is uniform
+template <class T> __device__ __forceinline__ bool dt_tight(const DevState<T> &S) {
+    if constexpr (sizeof(T) == 8) return recip_tight(sc_dt<T>(S.sc), sc_rdt<T>(S.sc));
+    else return false;
+}
+
 template <class T, bool ONE = false>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_sweep_x(const __grid_constant__ DevState<T> S, int con, int fcur) {
-    sweep_x_body<T, ONE>(S, con, fcur, bix_here());
+    if (dt_tight(S)) sweep_x_body<T, ONE, true>(S, con, fcur, bix_here());
+    else sweep_x_body<T, ONE, false>(S, con, fcur, bix_here());
 }
 
 // x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,
@@ -1535,7 +1545,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_sweep_x(const _
 // cells s0..s1 (cell s0 is the one overlap with the previous segment); the face behind
 // the current cell is carried in registers.  Old faces come from generation fcur, new
 // faces go to fcur^1, so segments are independent.
-template <class T, int AX, bool ONE = false>
+template <class T, int AX, bool ONE = false, bool ONE_DT = false>
 __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, int fcur, int seg, const BIx &bx) {
     const Geom g = S.g;
     const int i = bx.x * 128 + threadIdx.x + 1;
@@ -1547,7 +1557,7 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     const SweepSrc<T> R = sweep_src(S, con, fcur, AX);
     const FaceOut<T> W = sweep_out(S, fcur, AX);
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
-    const SweepK<T> q = sweep_consts(S, AX, ONE);
+    const SweepK<T> q = sweep_consts(S, AX, ONE, ONE_DT);
     const int cst = AX == 1 ? (int)g.cs1 : (int)g.cs2, fst = AX == 1 ? (int)g.fs1 : (int)g.fs2;
     int c = (AX == 1 ? g.ci(i, 0, o) : g.ci(i, o, 0)) + s0 * cst;
     int fb = (AX == 1 ? g.fi(i, 0, o) : g.fi(i, o, 0)) + s0 * fst;
@@ -1577,7 +1587,8 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
 
 template <class T, int AX, bool ONE = false>
 __global__ void __launch_bounds__(128) k_sweep_col(const __grid_constant__ DevState<T> S, int con, int fcur, int seg) {
-    sweep_col_body<T, AX, ONE>(S, con, fcur, seg, bix_here());
+    if (dt_tight(S)) sweep_col_body<T, AX, ONE, true>(S, con, fcur, seg, bix_here());
+    else sweep_col_body<T, AX, ONE, false>(S, con, fcur, seg, bix_here());
 }
 
 // ---------------------------------------------------------------------------------------
