@@ -37,7 +37,7 @@ sys.path.insert(0, HERE)
 
 import arkgpu  # noqa: E402
 
-RE_B = 5600.0
+RE_B = 5600.0  # the study's Reynolds number (--re changes it)
 
 
 def params(C, precision=arkgpu.FP32):
@@ -153,6 +153,7 @@ def compare(coarse, fine):
 
 
 def main():
+    global RE_B
     ap = argparse.ArgumentParser()
     ap.add_argument("--fine", type=int, nargs=3, default=(256, 128, 128))
     ap.add_argument("--coarse", type=int, nargs=3, default=(64, 48, 48))
@@ -165,7 +166,9 @@ def main():
     ap.add_argument("--lattice", type=int, default=4)
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--re", type=float, default=RE_B, help="bulk Reynolds number U_b h / nu (default 5600)")
     a = ap.parse_args()
+    RE_B = a.re
     rep = {"config": vars(a).copy(), "re_b": RE_B}
     t_start = time.time()
 
