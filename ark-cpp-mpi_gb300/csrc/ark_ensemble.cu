@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(stg::NT, 2) kb_phase1_staged(const DS *__restr
 __global__ void __launch_bounds__(128) kb_sweep_x(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
-        sweep_x_body<float>(inst[q], con, fcur, decode(W, q, b));
+        sweep_x_body<float>(inst[q], con, fcur, W.extra[q], decode(W, q, b));
     }
 }
 
@@ -239,7 +239,12 @@ int build_lists(ark_ensemble *E) {
             switch (kind) {
             case WL_TILES: gx = tiles_x(g), gy = tiles_y(g), gz = tiles_k(g); break;
             case WL_CELLS: gx = tiles_x(g), gy = tiles_y(g), gz = g.C3; break;
-            case WL_SWEEPX: gx = (g.C2 * g.C3 + 3) / 4; break;
+            case WL_SWEEPX: {
+                const int gl = x_lines_per_warp(g);
+                extra[q] = gl;
+                gx = (g.C2 * g.C3 + 4 * gl - 1) / (4 * gl);
+                break;
+            }
             case WL_COL1: {
                 const int seg = segment_for(g.C2 + 1, E->shape.seg);
                 extra[q] = seg;

@@ -1432,20 +1432,53 @@ __device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, 
 // computed.  A face needs the forward values of the cell behind it: a shuffle from the
 // neighbouring lane, or the carry from the previous chunk's last lane.  Old faces come from
 // generation fcur, new faces go to fcur^1.
+// Lines per warp in the x1 sweep: a warp walks the cells 0..C1+1 of that many consecutive lines as
+// one stream of positions, 32 at a time, so a chunk that ends one line carries on with the next
+// instead of leaving lanes idle (a 32-cell line alone fills 34 of 64 lanes).  Short lines: 4;
+// long lines waste little and take 1, which keeps enough warps for the waves to come out even
+// (4 lines per warp made the FP64 256x128x128 sweep 20% slower).
+__host__ __device__ inline int x_lines_per_warp(const Geom &g) { return g.C1 < 200 ? 4 : 1; }
+
 template <class T, bool ONE = false, bool ONE_DT = false>
-__device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, const BIx &bx) {
+__device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, int glines, const BIx &bx) {
     const Geom g = S.g;
     const int lane = threadIdx.x & 31;
-    const int line = bx.x * 4 + (threadIdx.x >> 5);
-    if (line >= g.C2 * g.C3) return;
-    const int j = line % g.C2 + 1, k = line / g.C2 + 1;
+    const int nlines = g.C2 * g.C3;
+    const int first = (bx.x * 4 + (threadIdx.x >> 5)) * glines; // the warp's first line
+    if (first >= nlines) return;
+    const int nl = nlines - first < glines ? nlines - first : glines;
+    const int nd = g.C1 + 1, npos = g.C1 + 2; // cells 0..C1+1 of a line
+    const int total = nl * npos;              // positions of the warp's stream
     const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
     const FaceOut<T> W = sweep_out(S, fcur, 0);
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
     const SweepK<T> q = sweep_consts(S, 0, ONE, ONE_DT);
-    const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k);
-    const int nd = g.C1 + 1;
     const bool bounded = !S.k.periodic_x;
+    // a lane's position: line li of the group, cell s, and the line's cell / face 0 indices
+    struct Pos {
+        int li, s, c0, f0;
+    };
+    auto locate = [&](Pos &P) {
+        const int L = first + P.li;
+        const int j = L % g.C2 + 1, k = L / g.C2 + 1;
+        P.c0 = g.ci(0, j, k);
+        P.f0 = g.fi(0, j, k);
+    };
+    auto advance = [&](Pos &P) { // 32 positions on
+        P.s += 32;
+        bool moved = false;
+        while (P.s >= npos) {
+            P.s -= npos;
+            ++P.li;
+            moved = true;
+        }
+        if (moved && P.li < nl) locate(P);
+    };
+    Pos cp;
+    cp.li = lane / npos;
+    cp.s = lane - cp.li * npos;
+    cp.c0 = cp.f0 = 0;
+    if (cp.li < nl) locate(cp);
     Ext<T> carry = {};
     T carry_u = 0;
     uint8_t carry_fl = 0;
@@ -1453,22 +1486,22 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     T uA_b = 0, uB_b = 0, nuA_b = 0, nuB_b = 0;
     // the invariants of a cell's backward face are those the cell behind computed for its
     // forward face: a shuffle from the neighbouring lane, across chunks the carry from the last
-    // lane, and for cell 0 the face 0 itself
+    // lane, and for cell 0 of a line the face 0 itself
     RQ<T> carry_rq = {(T)0, (T)0};
-    if (lane <= nd) {
-        sweep_load(R, c0 + lane, f0 + lane + 1, cur);
-        uA_b = R.FA[f0 + lane];
-        uB_b = R.FB[f0 + lane];
+    if (cp.li < nl) {
+        sweep_load(R, cp.c0 + cp.s, cp.f0 + cp.s + 1, cur);
+        uA_b = R.FA[cp.f0 + cp.s];
+        uB_b = R.FB[cp.f0 + cp.s];
     }
-    if (lane == 0) carry_rq = face_rq(R.FN[f0], R.FP[f0], q);
-    for (int s0 = 0; s0 <= nd; s0 += 32) {
-        const int s = s0 + lane;
-        const bool act = s <= nd;
-        const int sn = s + 32;
-        if (sn <= nd) {
-            sweep_load(R, c0 + sn, f0 + sn + 1, nxt);
-            nuA_b = R.FA[f0 + sn];
-            nuB_b = R.FB[f0 + sn];
+    for (int p0 = 0; p0 < total; p0 += 32) {
+        const bool act = cp.li < nl;
+        const int s = cp.s, c0 = cp.c0, f0 = cp.f0;
+        Pos np = cp;
+        advance(np);
+        if (np.li < nl) {
+            sweep_load(R, np.c0 + np.s, np.f0 + np.s + 1, nxt);
+            nuA_b = R.FA[np.f0 + np.s];
+            nuB_b = R.FB[np.f0 + np.s];
         }
         RQ<T> rqf = {(T)0, (T)0};
         if (act) rqf = face_rq(cur.uN_f, cur.p_f, q);
@@ -1476,13 +1509,14 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         rqb.r = __shfl_up_sync(0xffffffffu, rqf.r, 1);
         rqb.q = __shfl_up_sync(0xffffffffu, rqf.q, 1);
         if (lane == 0) rqb = carry_rq;
+        if (act && s == 0) rqb = face_rq(R.FN[f0], R.FP[f0], q);
         carry_rq.r = __shfl_sync(0xffffffffu, rqf.r, 31);
         carry_rq.q = __shfl_sync(0xffffffffu, rqf.q, 31);
         Ext<T> e = {};
         if (act)
             e = extrapolate_rq<T, true>(rqf, rqb, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA, cur.uB_f, uB_b, cur.nB,
                                         cur.cB, cur.nR, cur.cR, q);
-        if (bounded) {
+        if (bounded && act) {
             // a bounded x axis sweeps cells 1..C1 only; the edge faces take the reference's
             // inflow invariant R = 1 (0 behind a solid first cell) and outflow Q = 5/6 with
             // zero tangential velocity (main.cpp:1731-1745)
@@ -1520,11 +1554,10 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         cur = nxt;
         uA_b = nuA_b;
         uB_b = nuB_b;
+        cp = np;
     }
 }
 
-// FP32: capped at 80 registers for 6 blocks (24 warps) per SM (0.47 vs 0.50 ms at 512x256x256);
-// FP64: 3 blocks per SM, as without a bound.
 // FP64: whether this step's dt has a reciprocal within a quarter ulp (its quotients then take one
 // correction); the same answer in every thread, so the branch between the two builds of a sweep
 // body is uniform
@@ -1534,9 +1567,10 @@ template <class T> __device__ __forceinline__ bool dt_tight(const DevState<T> &S
 }
 
 template <class T, bool ONE = false>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3) k_sweep_x(const __grid_constant__ DevState<T> S, int con, int fcur) {
-    if (dt_tight(S)) sweep_x_body<T, ONE, true>(S, con, fcur, bix_here());
-    else sweep_x_body<T, ONE, false>(S, con, fcur, bix_here());
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3)
+    k_sweep_x(const __grid_constant__ DevState<T> S, int con, int fcur, int glines) {
+    if (dt_tight(S)) sweep_x_body<T, ONE, true>(S, con, fcur, glines, bix_here());
+    else sweep_x_body<T, ONE, false>(S, con, fcur, glines, bix_here());
 }
 
 // x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,
@@ -2005,10 +2039,10 @@ template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur
     const KT<double> &kd = S.k.kd;
     const bool one = std::is_same<T, double>::value && kd.one_roc && kd.one_c2 && kd.one_dx[axis];
     if (axis == 0) {
-        const int lines_x = S.g.C2 * S.g.C3;
-        const dim3 grid((lines_x + 3) / 4);
-        if (one) k_sweep_x<T, true><<<grid, 128, 0, st>>>(S, con, fcur);
-        else k_sweep_x<T, false><<<grid, 128, 0, st>>>(S, con, fcur);
+        const int lines_x = S.g.C2 * S.g.C3, gl = x_lines_per_warp(S.g);
+        const dim3 grid((lines_x + 4 * gl - 1) / (4 * gl)); // 4 warps of gl lines
+        if (one) k_sweep_x<T, true><<<grid, 128, 0, st>>>(S, con, fcur, gl);
+        else k_sweep_x<T, false><<<grid, 128, 0, st>>>(S, con, fcur, gl);
     } else if (axis == 1) {
         int nseg;
         const int seg = sweep_segment(S.g.C2 + 1, target, &nseg);
