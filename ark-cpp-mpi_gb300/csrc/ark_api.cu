@@ -80,6 +80,10 @@ template <class T> void fill_kt(const Consts &k, KT<T> &t) {
     t.one_dvc = tight(k.dvc, 1.0 / k.dvc);
     t.one_roc = tight(k.roc, k.rroc);
     t.one_c2 = tight(k.c2, k.rc2);
+    for (int d = 0; d < 3; ++d) t.q_dx[d] = make_qrecip(k.dx[d]);
+    t.q_dvc = make_qrecip(k.dvc);
+    t.q_roc = make_qrecip(k.roc);
+    t.q_c2 = make_qrecip(k.c2);
 }
 
 // Run constants, evaluated exactly as the reference evaluates them: grid steps as
@@ -477,6 +481,7 @@ void set_dt_fields(DevScalars &sc, double dt) {
     sc.rdt = 1.0 / dt;
     sc.dtf = (float)dt;
     sc.rdtf = (float)(1.0 / dt);
+    sc.qdt = make_qrecip(dt);
 }
 
 int check_ctx(ark_ctx *ctx, bool need_state) {
@@ -985,8 +990,9 @@ int ark_selftest_division(long long n, unsigned long long seed, long long *misma
     unsigned long long *bad = nullptr;
     ARK_CUDA(cudaMalloc(&bad, sizeof(unsigned long long)));
     cudaMemset(bad, 0, sizeof(unsigned long long));
-    selftest_division(n, seed, bad, 0);
+    const int rc = selftest_division(n, seed, bad, 0);
     cudaError_t e = cudaGetLastError();
+    if (rc && e == cudaSuccess) e = cudaErrorMemoryAllocation;
     unsigned long long h = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
     cudaFree(bad);

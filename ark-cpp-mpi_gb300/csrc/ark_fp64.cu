@@ -2,6 +2,9 @@
 // every operation rounds as the reference's does when built with -ffp-contract=off.
 #include "ark_kernels.cuh"
 
+#include <cstring>
+#include <vector>
+
 namespace ark {
 template struct Launch<double>;
 template void rows_from_double<double>(double *, const double *, int, int64_t, int, double, cudaStream_t);
@@ -13,7 +16,10 @@ template void rows_face_density<double>(double *, const double *, int, int64_t, 
 // zeros included, divisor exponents in [-120, 120]); divisors are reused 8 times so the
 // reciprocal is a "run constant" like dx or dt.  Where the divisor's reciprocal is within a
 // quarter ulp (recip_tight, about 70% of random divisors) the one-correction form is checked
-// too.  Also the small exact cases the step meets.
+// too.  Also the small exact cases the step meets.  qdiv is checked on the same pairs, and on
+// a table of divisors prepared by make_qrecip on the host (powers of two, the significands
+// 2^52 + 1 and 2^53 - 1, the channel's constants, random values), where the device's own
+// make_qrecip must also agree with the host's.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -27,7 +33,13 @@ __device__ __forceinline__ double rnd_double(unsigned long long z, int emin, int
     if (e <= 0) return __longlong_as_double((long long)(sign | (mant >> (1 - e)))); // subnormal / zero
     return __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | mant));
 }
-__global__ void k_selftest_division(long long n, unsigned long long seed, unsigned long long *bad) {
+struct QCase {
+    double b;
+    QRecip q;
+};
+__device__ __forceinline__ bool same(double x, double y) { return __double_as_longlong(x) == __double_as_longlong(y); }
+__global__ void k_selftest_division(long long n, unsigned long long seed, const QCase *qc, int nqc,
+                                    unsigned long long *bad) {
     unsigned long long local = 0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         const unsigned long long za = mix64(seed + 2 * (unsigned long long)t);
@@ -39,11 +51,44 @@ __global__ void k_selftest_division(long long n, unsigned long long seed, unsign
         if (recip_tight(b, rb) && __double_as_longlong(want) != __double_as_longlong(div_rn(a, b, rb, true))) ++local;
         const double a2 = (double)(long long)(t % 2001 - 1000) * 0.5, b2 = 10.0;
         if (__double_as_longlong(a2 / b2) != __double_as_longlong(div_rn(a2, b2, 1.0 / b2))) ++local;
+        if (!same(want, qdiv(a, b, rb, make_qrecip(b)))) ++local;
+        const QCase &c = qc[t % nqc];
+        if (t < nqc) {
+            const QRecip d = make_qrecip(c.b);
+            if (d.r0 != c.q.r0 || d.r1 != c.q.r1 || d.k != c.q.k || d.sgn != c.q.sgn) ++local;
+        }
+        if (!same(a / c.b, qdiv(a, c.b, 1.0 / c.b, c.q))) ++local;
+        if (!same(a2 / c.b, qdiv(a2, c.b, 1.0 / c.b, c.q))) ++local;
+        // a numerator with the divisor's significand bits: exact and near-exact quotients
+        const double a3 = c.b * (double)(long long)(t % 4097 - 2048) * ((t & 4) ? 0.75 : 1.0);
+        if (!same(a3 / c.b, qdiv(a3, c.b, 1.0 / c.b, c.q))) ++local;
     }
     if (local) atomicAdd(bad, local);
 }
 
-void selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st) {
-    k_selftest_division<<<152 * 4, 256, 0, st>>>(n, seed, bad);
+int selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st) {
+    std::vector<double> bs = {1.0, 0.5, 2.0, -4.0, 0x1p-100, 0x1p100, 10.0, 100.0, 1.0 / 3.0, -7.0,
+                              0x1.0000000000001p0, 0x1.fffffffffffffp0, -0x1.0000000000001p-7, 0x1.fffffffffffffp9,
+                              6.283185307179586 / 256, 2.0 / 128, 3.141592653589793 / 128,
+                              6.283185307179586 / 512, 3.141592653589793 / 256};
+    unsigned long long z = seed ^ 0x5DEECE66Dull;
+    while (bs.size() < 256) { // random significands, exponents in [-60, 60], both signs
+        z = z * 6364136223846793005ull + 1442695040888963407ull;
+        const unsigned long long m = (z >> 11) & 0x000FFFFFFFFFFFFFull;
+        const unsigned long long e = (unsigned long long)(1023 - 60 + (int)((z >> 1) % 121));
+        const unsigned long long bits = ((z & 1ull) << 63) | (e << 52) | m;
+        double b;
+        std::memcpy(&b, &bits, sizeof b);
+        bs.push_back(b);
+    }
+    std::vector<QCase> h(bs.size());
+    for (size_t i = 0; i < bs.size(); ++i) h[i] = {bs[i], make_qrecip(bs[i])};
+    QCase *d = nullptr;
+    if (cudaMalloc(&d, sizeof(QCase) * h.size()) != cudaSuccess) return 1;
+    cudaMemcpy(d, h.data(), sizeof(QCase) * h.size(), cudaMemcpyHostToDevice);
+    k_selftest_division<<<152 * 4, 256, 0, st>>>(n, seed, d, (int)h.size(), bad);
+    cudaStreamSynchronize(st);
+    cudaFree(d);
+    return 0;
 }
 } // namespace ark

@@ -88,11 +88,64 @@ __device__ __forceinline__ double div_rn(double a, double b, double rb, bool one
 // rb = RN(1/b) within a quarter ulp (the residual rb*b - 1 is exact in one FMA)
 __device__ __forceinline__ bool recip_tight(double b, double rb) { return fabs(__fma_rn(rb, b, -1.0)) <= 0x1p-54; }
 
+// RN(a / b) on the integer pipes, for a divisor b prepared by make_qrecip.  GB300 runs FP64 at
+// 1/64 of its FP32 rate, so one warp-wide FP64 instruction holds the FP64 pipe for about 64
+// cycles while integer instructions issue one per cycle: the step's FP64 kernels are bound by
+// that pipe, and a quotient taken here (about 30 integer instructions) frees the three FP64
+// operations of div_rn's one-correction form.
+// With a = Ma 2^(ea-1075), Ma in [2^52, 2^53), and r = ceil(2^116 / Mb) = 2^116 / Mb + e,
+// 0 <= e < 1: the product Ma r = Ma 2^116 / Mb + Ma e with Ma e < 2^53, so T = floor(Ma r / 2^53)
+// and X = (Ma / Mb) 2^63 (the exact quotient's significand, in (2^62, 2^64)) satisfy
+// T - 1 < X < T + 1.  The significand is RN(X / 2^(10+s)), s = 1 when T >= 2^63.  A quotient of
+// two 53-bit significands is never a midpoint of 53-bit values (that would make an odd number
+// of 54 or more bits a product of the divisor's significand and a 53-bit integer), so X lies on
+// the same side of the rounding midpoint as T unless T's low 10+s bits are exactly the
+// midpoint pattern; that case (about 1 in 2048), a zero, subnormal or non-finite a, and a
+// result outside the normal range take div_rn.  For Mb = 2^52, r = 2^64 - 1 gives
+// T = Ma 2^11 - 1, which rounds up to the exact quotient Ma 2^11.  ark_selftest_division
+// compares this with the hardware division.
+__device__ __forceinline__ double qdiv(double a, double b, double rb, const QRecip &Q) {
+    const unsigned ha = (unsigned)__double2hiint(a), la = (unsigned)__double2loint(a);
+    const unsigned ea = (ha >> 20) & 0x7FFu;
+    const unsigned a1 = (ha & 0xFFFFFu) | 0x100000u; // significand high word with the hidden bit
+    // w3:w2:w1 = bits 32..127 of (a1:la) * (r1:r0); bits 0..31 do not carry into them
+    unsigned w1, w2, w3;
+    asm("mul.hi.u32 %0, %3, %5;\n\t"
+        "mad.lo.cc.u32 %0, %3, %6, %0;\n\t"
+        "madc.hi.u32 %1, %3, %6, 0;\n\t"
+        "mad.lo.cc.u32 %0, %4, %5, %0;\n\t"
+        "madc.hi.cc.u32 %1, %4, %5, %1;\n\t"
+        "addc.u32 %2, 0, 0;\n\t"
+        "mad.lo.cc.u32 %1, %4, %6, %1;\n\t"
+        "madc.hi.u32 %2, %4, %6, %2;"
+        : "=&r"(w1), "=&r"(w2), "=&r"(w3)
+        : "r"(la), "r"(a1), "r"(Q.r0), "r"(Q.r1));
+    const unsigned thi = __funnelshift_l(w2, w3, 11), tlo = __funnelshift_l(w1, w2, 11); // T = P >> 53
+    const unsigned s = thi >> 31, sh = 10u + s;
+    const unsigned below = tlo << (32u - sh); // T's low sh bits, at the top of the word
+    const int E = (int)ea + (int)s + Q.k;     // the quotient's biased exponent
+    if (ea - 1u >= 2046u || (unsigned)(E - 1) >= 2046u || below == 0x80000000u) return div_rn(a, b, rb);
+    const unsigned long long sig =
+        (((unsigned long long)(thi >> sh) << 32) | __funnelshift_r(tlo, thi, sh)) + (below > 0x80000000u ? 1ull : 0ull);
+    // the significand's hidden bit (bit 52) adds one to the exponent field E - 1; a carry out of
+    // the rounding (sig = 2^53) adds another, and at E = 2046 gives the infinity RN gives
+    const unsigned long long bits = sig + ((unsigned long long)(unsigned)(E - 1) << 52);
+    return __hiloint2double((int)((unsigned)(bits >> 32) | ((ha & 0x80000000u) ^ Q.sgn)), (int)(unsigned)bits);
+}
+
 // Division by a run constant b whose reciprocal rb is known.  FP64: the correctly rounded
 // quotient (the parity bar).  FP32: multiplication by the reciprocal.
 // one: rb is within a quarter ulp (the run constant's flag), so one correction suffices.
 __device__ __forceinline__ double divk(double a, double b, double rb, bool one) { return div_rn(a, b, rb, one); }
 __device__ __forceinline__ float divk(float a, float b, float rb, bool) {
+    (void)b;
+    return a * rb;
+}
+
+// Division by a run constant or by dt, with the divisor's reciprocals: FP64 on the integer pipes
+// (qdiv, correctly rounded), FP32 multiplication by the reciprocal.
+__device__ __forceinline__ double divq(double a, double b, double rb, const QRecip &Q) { return qdiv(a, b, rb, Q); }
+__device__ __forceinline__ float divq(float a, float b, float rb, const QRecip &) {
     (void)b;
     return a * rb;
 }
@@ -310,6 +363,7 @@ template <class T> __device__ __forceinline__ void finalize_dt_body(const DevSta
     sc->rdt = 1.0 / dt;
     sc->dtf = (float)dt;
     sc->rdtf = (float)(1.0 / dt);
+    sc->qdt = make_qrecip(dt);
     if (k.forcing) {
         const double ub = sc->nfluid > 0 ? ((double)s * FixedScale<T>::inv) / (double)sc->nfluid : 0.0;
         sc->ub = ub;
@@ -442,9 +496,9 @@ constexpr int kCellBX = 64, kCellBY = 2; // block shape of the one-cell-per-thre
 // one: the kernel was built for grid steps whose reciprocals are within a quarter ulp (div_rn)
 template <class T>
 __device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const K<T> &kk, int d, bool one = false) {
-    if ((fw & FL_LT) && (fc & FL_LT)) return divk(kk.vis * (u_c - u_cw), kk.dx[d], kk.rdx[d], one);
-    if ((fw & FL_LT) && (fc & FL_GT)) return divk(kk.two_vis * (-u_cw), kk.dx[d], kk.rdx[d], one);
-    if ((fw & FL_GT) && (fc & FL_LT)) return divk(kk.two_vis * u_c, kk.dx[d], kk.rdx[d], one);
+    if ((fw & FL_LT) && (fc & FL_LT)) return divq(kk.vis * (u_c - u_cw), kk.dx[d], kk.rdx[d], kk.q_dx[d]);
+    if ((fw & FL_LT) && (fc & FL_GT)) return divq(kk.two_vis * (-u_cw), kk.dx[d], kk.rdx[d], kk.q_dx[d]);
+    if ((fw & FL_GT) && (fc & FL_LT)) return divq(kk.two_vis * u_c, kk.dx[d], kk.rdx[d], kk.q_dx[d]);
     return (T)0;
 }
 
@@ -542,10 +596,10 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
                                           T dt, const K<T> &kk, T &ro_cn, T ucn[3], T &rden_out, bool one = false) {
     if constexpr (!Storage<T>::deviation) {
         // new density (main.cpp:530-533)
-        ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
+        ro_cn = divq(ro_c * kk.dvc - (T)0.5 * dt * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
                                                     (hi[1].ro * hi[1].u[1] - lo[1].ro * lo[1].u[1]) * kk.ds[1] +
                                                     (hi[2].ro * hi[2].u[2] - lo[2].ro * lo[2].u[2]) * kk.ds[2]),
-                     kk.dvc, kk.rdvc, one);
+                     kk.dvc, kk.rdvc, kk.q_dvc);
         // momentum (main.cpp:536-551): the flux of u_m through faces normal to d is
         // (ro*u_m)*u_d, plus p when m == d
         // one reciprocal serves the three momentum quotients (and UseForces, whose divisor
@@ -972,9 +1026,9 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
             T ro_cn, ucn[3], rden = (T)0;
             if (fl & FL_LT) {
                 // half_step (main.cpp:530-551) over the face quantities
-                ro_cn = divk(ro_c * kk.dvc - (T)0.5 * dt * ((Hx.mf - Lx.mf) * kk.ds[0] + (Hy.mf - Ly.mf) * kk.ds[1] +
+                ro_cn = divq(ro_c * kk.dvc - (T)0.5 * dt * ((Hx.mf - Lx.mf) * kk.ds[0] + (Hy.mf - Ly.mf) * kk.ds[1] +
                                                             (zhi.mf - zlo.mf) * kk.ds[2]),
-                             kk.dvc, kk.rdvc, ONE);
+                             kk.dvc, kk.rdvc, kk.q_dvc);
                 const T den = ro_cn * kk.dvc;
                 const T rd = recip(den);
                 rden = rd;
@@ -1135,12 +1189,13 @@ template <class T> struct Ext { T rf, qb, af, ab, bf, bb; };
 template <class T> struct SweepK {
     T sound, ro0, c2, rc2, roc, rroc, dt, rdt, dx, rdx;
     bool one_c2, one_roc, one_dt, one_dx; // FP64: one correction suffices (div_rn)
+    QRecip qc2, qroc, qdt, qdx;           // FP64: the divisors for qdiv
 };
 
 // The gradient term of a limiter bound: a / dt + b / dx.  FP64: the two correctly rounded
 // quotients summed, as the reference evaluates it; FP32: a * (1/dt) + b * (1/dx), fused.
 __device__ __forceinline__ double grad_sum(double a, double b, const SweepK<double> &q) {
-    return divk(a, q.dt, q.rdt, q.one_dt) + divk(b, q.dx, q.rdx, q.one_dx);
+    return divq(a, q.dt, q.rdt, q.qdt) + divq(b, q.dx, q.rdx, q.qdx);
 }
 __device__ __forceinline__ float grad_sum(float a, float b, const SweepK<float> &q) { return __fmaf_rn(a, q.rdt, b * q.rdx); }
 
@@ -1158,7 +1213,7 @@ __device__ __forceinline__ float twice_minus(float x, float y) { return __fmaf_r
 // (main.cpp:1790-1797).  The sweeps compute them once per face and hand them to the cell ahead.
 template <class T> struct RQ { T r, q; };
 template <class T> __device__ __forceinline__ RQ<T> face_rq(T u_n, T p, const SweepK<T> &q) {
-    const T pf = divk(p, q.roc, q.rroc, q.one_roc);
+    const T pf = divq(p, q.roc, q.rroc, q.qroc);
     RQ<T> v;
     v.r = u_n + pf;
     v.q = u_n - pf;
@@ -1172,7 +1227,7 @@ __device__ __forceinline__ Ext<T> extrapolate_rq(RQ<T> f, RQ<T> b, T u1_cn, T u1
     constexpr bool DEV = Storage<T>::deviation;
     const T p_cn = DEV ? q.c2 * ro_cn : q.c2 * (ro_cn - q.ro0);
     const T p_c = DEV ? q.c2 * ro_c : q.c2 * (ro_c - q.ro0);
-    const T pcn = divk(p_cn, q.roc, q.rroc, q.one_roc), pc = divk(p_c, q.roc, q.rroc, q.one_roc);
+    const T pcn = divq(p_cn, q.roc, q.rroc, q.qroc), pc = divq(p_c, q.roc, q.rroc, q.qroc);
 
     // max + dt*g: mad rounds it exactly as written in FP64, fused in FP32
     const T r_f = f.r, r_b = b.r, r_cn = u1_cn + pcn, r_c = u1_c + pc;
@@ -1265,7 +1320,7 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
         const T rn = prev.rf, qn = cur.qb;
         un = (rn + qn) / (T)2;
         pn = (rn - qn) * q.sound * q.ro0 / (T)2;
-        ro_n = q.ro0 + divk(pn, q.c2, q.rc2, q.one_c2);
+        ro_n = q.ro0 + divq(pn, q.c2, q.rc2, q.qc2);
         if (ge0(ucf) && ge0(ucb)) {
             ua = prev.af;
             ub = prev.bf;
@@ -1290,7 +1345,7 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
             if (le0(ucf)) {
                 const T qn = cur.qb;
                 pn = -qn * q.sound * q.ro0;
-                ro_n = q.ro0 + divk(pn, q.c2, q.rc2, q.one_c2);
+                ro_n = q.ro0 + divq(pn, q.c2, q.rc2, q.qc2);
                 ua = cur.ab;
                 ub = cur.bb;
             } else {
@@ -1303,7 +1358,7 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
             if (ge0(ucb)) {
                 const T rn = prev.rf;
                 pn = rn * q.sound * q.ro0;
-                ro_n = q.ro0 + divk(pn, q.c2, q.rc2, q.one_c2);
+                ro_n = q.ro0 + divq(pn, q.c2, q.rc2, q.qc2);
                 ua = prev.af;
                 ub = prev.bf;
             } else {
@@ -1365,6 +1420,10 @@ __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d, b
     q.one_roc = one;
     q.one_dx = one;
     q.one_dt = one_dt;
+    q.qc2 = k.q_c2;
+    q.qroc = k.q_roc;
+    q.qdx = k.q_dx[d];
+    q.qdt = sc_qdt(S.sc);
     return q;
 }
 

@@ -9,9 +9,53 @@
 // (Phase1's nCon -> Con copy, main.cpp:419-432, becomes a relabelling).
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace ark {
+
+// A divisor known before its quotients are taken (a run constant, or dt for one step), for
+// FP64 division on the integer pipes (qdiv): r = ceil(2^116 / M) for the divisor's 53-bit
+// significand M in [2^52, 2^53) (2^64 - 1 when M = 2^52), k = 1022 - the divisor's biased
+// exponent, sgn = its sign bit in the high word.  A zero, subnormal or non-finite divisor gets
+// k = -100000, which sends every quotient to the FP64 path.
+struct QRecip {
+    unsigned r0, r1; // r: low and high words
+    int k;
+    unsigned sgn;
+};
+
+__host__ __device__ inline QRecip make_qrecip(double b) {
+    unsigned long long bits;
+#ifdef __CUDA_ARCH__
+    bits = (unsigned long long)__double_as_longlong(b);
+#else
+    std::memcpy(&bits, &b, sizeof bits);
+#endif
+    QRecip q;
+    const int eb = (int)((bits >> 52) & 0x7FFull);
+    q.sgn = (unsigned)(bits >> 32) & 0x80000000u;
+    q.r0 = q.r1 = 0u;
+    q.k = -100000;
+    if (eb == 0 || eb == 0x7FF) return q;
+    const unsigned long long M = (bits & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned long long r = ~0ull;
+    if (M != (1ull << 52)) {
+        // d = RN(2^116 / M) is an integer within 2^10 of the quotient (its ulp is 2^11), so the
+        // remainder 2^116 - M d lies within M 2^10 < 2^63 of zero: its low 64 bits are exact.
+        const double d = 0x1p116 / (double)M;
+        const unsigned long long q0 = (unsigned long long)d;
+        const long long rem = (long long)(0ull - M * q0);
+        long long c = rem / (long long)M;
+        if (rem - c * (long long)M < 0) c -= 1; // floor division
+        // 2^116 / M is not an integer (M is not a power of two): ceil = floor + 1
+        r = q0 + (unsigned long long)c + 1ull;
+    }
+    q.r0 = (unsigned)r;
+    q.r1 = (unsigned)(r >> 32);
+    q.k = 1022 - eb;
+    return q;
+}
 
 struct Geom {
     int C1, C2, C3;
@@ -120,6 +164,7 @@ template <class T> struct KT {
     // FP64: 1 where the constant's reciprocal is within a quarter ulp (|rb*b - 1| <= 2^-54), so
     // that one correction step gives its correctly rounded quotients (div_rn)
     unsigned char one_dx[3], one_dvc, one_roc, one_c2;
+    QRecip q_dx[3], q_dvc, q_roc, q_c2; // FP64: the same divisors for qdiv
 };
 
 // Constants of a run, computed once on the host in double, plus their per-precision copies.
@@ -155,6 +200,7 @@ struct DevScalars {
     long long sum_cells;
     double rdt;        // 1/dt
     float dtf, rdtf, Gf, padf; // dt, 1/dt and G rounded to FP32 for the FP32 kernels
+    QRecip qdt;        // dt for qdiv
 };
 
 template <class T> __device__ __forceinline__ T sc_dt(const DevScalars *s);
@@ -163,6 +209,7 @@ template <> __device__ __forceinline__ float sc_dt<float>(const DevScalars *s) {
 template <class T> __device__ __forceinline__ T sc_rdt(const DevScalars *s);
 template <> __device__ __forceinline__ double sc_rdt<double>(const DevScalars *s) { return s->rdt; }
 template <> __device__ __forceinline__ float sc_rdt<float>(const DevScalars *s) { return s->rdtf; }
+__device__ __forceinline__ QRecip sc_qdt(const DevScalars *s) { return s->qdt; }
 template <class T> __device__ __forceinline__ T sc_G(const DevScalars *s);
 template <> __device__ __forceinline__ double sc_G<double>(const DevScalars *s) { return s->G; }
 template <> __device__ __forceinline__ float sc_G<float>(const DevScalars *s) { return s->Gf; }
@@ -275,8 +322,8 @@ template <class T> void closure_gather(const DevState<T> &S, int lvl, double *u0
 // samples of a C1 x C2 x C3 grid on the lattice (sx, sz, ox, oz), or -1 for a bad lattice
 long long closure_count(int C1, int C2, int C3, int sx, int sz, int ox, int oz);
 
-// div_rn against the hardware division on n random operand pairs (mismatches added to *bad)
-void selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st);
+// div_rn and qdiv against the hardware division on n random operand pairs (mismatches added to *bad)
+int selftest_division(long long n, unsigned long long seed, unsigned long long *bad, cudaStream_t st);
 
 // Between a contiguous double staging buffer (rows of w values) and the device's padded rows
 // (pitch): dst = (T)(src - offset), dst = (double)src + offset, and for FP32 contexts the face
