@@ -74,12 +74,6 @@ template <class T> void fill_kt(const Consts &k, KT<T> &t) {
     t.rc2 = (T)k.rc2;
     t.roc = (T)k.roc;
     t.rroc = (T)k.rroc;
-    // |rb*b - 1| is exact in one fused multiply-add when rb = RN(1/b)
-    auto tight = [](double b, double rb) { return (unsigned char)(std::fabs(std::fma(rb, b, -1.0)) <= 0x1p-54); };
-    for (int d = 0; d < 3; ++d) t.one_dx[d] = tight(k.dx[d], k.rdx[d]);
-    t.one_dvc = tight(k.dvc, 1.0 / k.dvc);
-    t.one_roc = tight(k.roc, k.rroc);
-    t.one_c2 = tight(k.c2, k.rc2);
     for (int d = 0; d < 3; ++d) t.q_dx[d] = make_qrecip(k.dx[d]);
     t.q_dvc = make_qrecip(k.dvc);
     t.q_roc = make_qrecip(k.roc);

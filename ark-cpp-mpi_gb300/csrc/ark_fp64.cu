@@ -14,12 +14,11 @@ template void rows_face_density<double>(double *, const double *, int, int64_t, 
 // Self-check of div_rn against the hardware IEEE division: n operand pairs from splitmix64
 // (random signs and mantissas; numerator exponents over the whole range, subnormals and
 // zeros included, divisor exponents in [-120, 120]); divisors are reused 8 times so the
-// reciprocal is a "run constant" like dx or dt.  Where the divisor's reciprocal is within a
-// quarter ulp (recip_tight, about 70% of random divisors) the one-correction form is checked
-// too.  Also the small exact cases the step meets.  qdiv is checked on the same pairs, and on
-// a table of divisors prepared by make_qrecip on the host (powers of two, the significands
-// 2^52 + 1 and 2^53 - 1, the channel's constants, random values), where the device's own
-// make_qrecip must also agree with the host's.
+// reciprocal is a "run constant" like dx or dt.  Also the small exact cases the step meets.
+// qdiv is checked on the same pairs, and on a table of divisors prepared by make_qrecip on the
+// host (powers of two, the significands 2^52 + 1 and 2^53 - 1, the channel's constants, random
+// values), where the device's own make_qrecip must also agree with the host's, and qrecip_var
+// (the per-cell divisor's reciprocal) with make_qrecip.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -48,16 +47,21 @@ __global__ void k_selftest_division(long long n, unsigned long long seed, const 
         const double rb = 1.0 / b;
         const double want = a / b, got = div_rn(a, b, rb);
         if (__double_as_longlong(want) != __double_as_longlong(got)) ++local;
-        if (recip_tight(b, rb) && __double_as_longlong(want) != __double_as_longlong(div_rn(a, b, rb, true))) ++local;
         const double a2 = (double)(long long)(t % 2001 - 1000) * 0.5, b2 = 10.0;
         if (__double_as_longlong(a2 / b2) != __double_as_longlong(div_rn(a2, b2, 1.0 / b2))) ++local;
-        if (!same(want, qdiv(a, b, rb, make_qrecip(b)))) ++local;
+        const QRecip qm = make_qrecip(b), qv = qrecip_var(b);
+        if (!same(want, qdiv(a, b, rb, qm))) ++local;
+        if (qv.r0 != qm.r0 || qv.r1 != qm.r1 || qv.k != qm.k || qv.sgn != qm.sgn) ++local;
+        if (!same(want, qdiv_v(a, b, qv))) ++local;
         const QCase &c = qc[t % nqc];
         if (t < nqc) {
             const QRecip d = make_qrecip(c.b);
             if (d.r0 != c.q.r0 || d.r1 != c.q.r1 || d.k != c.q.k || d.sgn != c.q.sgn) ++local;
         }
         if (!same(a / c.b, qdiv(a, c.b, 1.0 / c.b, c.q))) ++local;
+        const QRecip cv = qrecip_var(c.b);
+        if (cv.r0 != c.q.r0 || cv.r1 != c.q.r1 || cv.k != c.q.k || cv.sgn != c.q.sgn) ++local;
+        if (!same(a / c.b, qdiv_v(a, c.b, cv))) ++local;
         if (!same(a2 / c.b, qdiv(a2, c.b, 1.0 / c.b, c.q))) ++local;
         // a numerator with the divisor's significand bits: exact and near-exact quotients
         const double a3 = c.b * (double)(long long)(t % 4097 - 2048) * ((t & 4) ? 0.75 : 1.0);

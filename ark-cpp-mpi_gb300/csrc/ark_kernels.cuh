@@ -64,29 +64,21 @@ template <class T> __device__ __forceinline__ T max3d(T x1, T x2, T x3) {
 // within one ulp of a/b, then with the exact residual r = a - b*q (one FMA),
 // RN(q + r*rb) = RN(a/b), provided nothing underflows or overflows.  q = RN(a*rb) may be up
 // to 1.5 ulp off, so one correction makes it faithful and a second one makes it correctly
-// rounded: 1 multiply + 4 FMA.  One correction is enough when rb is within a quarter ulp,
-// |rb*b - 1| <= 2^-54 (one = true): then |a*rb - a/b| < ulp(a/b)/2, and rounding a*rb adds at
-// most another half ulp of the same binade (at a binade edge the rounding lands on the power of
-// two, within half an ulp of a/b), so q = RN(a*rb) is within one ulp and the theorem applies:
-// 1 multiply + 2 FMA.  Operands outside 2^-895 <= |a| < 2^897 and 2^-100 <= |b| < 2^101
-// (where the residual could leave the normal range), zeros included, take the IEEE division
-// instead; the exponent test is integer work.  The FP64 parity tests check every quotient of
-// the step against the reference bit for bit, and ark_selftest_division compares both forms
-// with the hardware division, tiny and subnormal operands included.
-__device__ __forceinline__ double div_rn(double a, double b, double rb, bool one = false) {
+// rounded: 1 multiply + 4 FMA.  Operands outside 2^-895 <= |a| < 2^897 and
+// 2^-100 <= |b| < 2^101 (where the residual could leave the normal range), zeros included, take
+// the IEEE division instead; the exponent test is integer work.  The FP64 parity tests check
+// every quotient of the step against the reference bit for bit, and ark_selftest_division
+// compares it with the hardware division, tiny and subnormal operands included.
+__device__ __forceinline__ double div_rn(double a, double b, double rb) {
     const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7FFu;
     const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7FFu;
     if (ea - 128u > 1792u || eb - 923u > 200u) return a / b;
     double q = a * rb;
     double r = __fma_rn(-q, b, a);
     q = __fma_rn(r, rb, q);
-    if (one) return q;
     r = __fma_rn(-q, b, a);
     return __fma_rn(r, rb, q);
 }
-
-// rb = RN(1/b) within a quarter ulp (the residual rb*b - 1 is exact in one FMA)
-__device__ __forceinline__ bool recip_tight(double b, double rb) { return fabs(__fma_rn(rb, b, -1.0)) <= 0x1p-54; }
 
 // RN(a / b) on the integer pipes, for a divisor b prepared by make_qrecip.  GB300 runs FP64 at
 // 1/64 of its FP32 rate, so one warp-wide FP64 instruction holds the FP64 pipe for about 64
@@ -103,8 +95,9 @@ __device__ __forceinline__ bool recip_tight(double b, double rb) { return fabs(_
 // midpoint pattern; that case (about 1 in 2048), a zero, subnormal or non-finite a, and a
 // result outside the normal range take div_rn.  For Mb = 2^52, r = 2^64 - 1 gives
 // T = Ma 2^11 - 1, which rounds up to the exact quotient Ma 2^11.  ark_selftest_division
-// compares this with the hardware division.
-__device__ __forceinline__ double qdiv(double a, double b, double rb, const QRecip &Q) {
+// compares this with the hardware division.  qdiv_try returns ok = false where the quotient
+// needs another path.
+__device__ __forceinline__ double qdiv_try(double a, const QRecip &Q, bool &ok) {
     const unsigned ha = (unsigned)__double2hiint(a), la = (unsigned)__double2loint(a);
     const unsigned ea = (ha >> 20) & 0x7FFu;
     const unsigned a1 = (ha & 0xFFFFFu) | 0x100000u; // significand high word with the hidden bit
@@ -124,7 +117,7 @@ __device__ __forceinline__ double qdiv(double a, double b, double rb, const QRec
     const unsigned s = thi >> 31, sh = 10u + s;
     const unsigned below = tlo << (32u - sh); // T's low sh bits, at the top of the word
     const int E = (int)ea + (int)s + Q.k;     // the quotient's biased exponent
-    if (ea - 1u >= 2046u || (unsigned)(E - 1) >= 2046u || below == 0x80000000u) return div_rn(a, b, rb);
+    ok = ea - 1u < 2046u && (unsigned)(E - 1) < 2046u && below != 0x80000000u;
     const unsigned long long sig =
         (((unsigned long long)(thi >> sh) << 32) | __funnelshift_r(tlo, thi, sh)) + (below > 0x80000000u ? 1ull : 0ull);
     // the significand's hidden bit (bit 52) adds one to the exponent field E - 1; a carry out of
@@ -132,14 +125,78 @@ __device__ __forceinline__ double qdiv(double a, double b, double rb, const QRec
     const unsigned long long bits = sig + ((unsigned long long)(unsigned)(E - 1) << 52);
     return __hiloint2double((int)((unsigned)(bits >> 32) | ((ha & 0x80000000u) ^ Q.sgn)), (int)(unsigned)bits);
 }
+// The fallbacks as calls of their own, so that a rarely taken one is not evaluated ahead of the
+// branch (a division has no side effects, so the compiler may otherwise compute it for every
+// quotient and select).
+static __device__ __noinline__ double ieee_div(double a, double b) { return a / b; }
+static __device__ __noinline__ double div_rn_call(double a, double b, double rb) { return div_rn(a, b, rb); }
+// b a run constant or dt (rb = RN(1/b)): the other path is div_rn
+__device__ __forceinline__ double qdiv(double a, double b, double rb, const QRecip &Q) {
+    bool ok;
+    const double q = qdiv_try(a, Q, ok);
+    return ok ? q : div_rn_call(a, b, rb);
+}
+// b that changes from cell to cell (Q from qrecip_var): the other path is the IEEE division
+__device__ __forceinline__ double qdiv_v(double a, double b, const QRecip &Q) {
+    bool ok;
+    const double q = qdiv_try(a, Q, ok);
+    return ok ? q : ieee_div(a, b);
+}
 
-// Division by a run constant b whose reciprocal rb is known.  FP64: the correctly rounded
-// quotient (the parity bar).  FP32: multiplication by the reciprocal.
-// one: rb is within a quarter ulp (the run constant's flag), so one correction suffices.
-__device__ __forceinline__ double divk(double a, double b, double rb, bool one) { return div_rn(a, b, rb, one); }
-__device__ __forceinline__ float divk(float a, float b, float rb, bool) {
-    (void)b;
-    return a * rb;
+// make_qrecip on the integer pipes, for a divisor that changes from cell to cell.  Seed: the FP32
+// reciprocal approximation of f = M / 2^52 (its top 24 bits), absolute error below 2^-23 on
+// (1/2, 1], so R0 = RN32(1/f) 2^64 has relative error below 2^-21.4.  Two Newton steps
+// R <- R + R (2^116 - M R) / 2^116 in 64-bit fixed point (Newton's iteration for the
+// reciprocal; R. Brent, P. Zimmermann, "Modern Computer Arithmetic", 2010, sec. 4.2.2)
+// square the relative error twice (2^-42.8, then 2^-85.6).  An exact Newton step never lands
+// above 2^116 / M (the new error is -(2^116 / M) e^2); the products here are rounded down, and
+// (2^116 - M R) / 2^32 is rounded up by at most 2^-32, so after the second step R lies within
+// 1 + 2^-20 below 2^116 / M and at most 2^-20 above it.  The exact remainder 2^116 - M R then
+// counts the steps (one or two) to ceil(2^116 / M); for M = 2^52, where that is 2^64, R is
+// 2^64 - 1 as make_qrecip sets it.  A zero, subnormal or non-finite divisor
+// gets k = -100000 (every quotient takes the IEEE division).
+__device__ __forceinline__ QRecip qrecip_var(double b) {
+    const unsigned hb = (unsigned)__double2hiint(b), m0 = (unsigned)__double2loint(b);
+    const unsigned eb = (hb >> 20) & 0x7FFu;
+    const unsigned m1 = (hb & 0xFFFFFu) | 0x100000u; // M = m1:m0
+    QRecip q;
+    q.sgn = hb & 0x80000000u;
+    q.k = eb - 1u < 2046u ? 1022 - (int)eb : -100000;
+    const float f = __uint_as_float(0x3F800000u | ((hb & 0xFFFFFu) << 3) | (m0 >> 29));
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f));
+    unsigned long long R = (unsigned long long)__float2uint_rz(rf * 0x1p32f) << 32; // saturates at 1/f = 1
+    const unsigned long long M = ((unsigned long long)m1 << 32) | m0;
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        // w2:w1 = bits 32..95 of M R; (2^116 - M R) / 2^32 lies within 2^63 of zero, so its low
+        // 64 bits, -(w2:w1), hold it
+        unsigned w1, w2;
+        asm("mul.hi.u32 %0, %2, %4;\n\t"
+            "mad.lo.cc.u32 %0, %2, %5, %0;\n\t"
+            "madc.hi.u32 %1, %2, %5, 0;\n\t"
+            "mad.lo.cc.u32 %0, %3, %4, %0;\n\t"
+            "madc.hi.u32 %1, %3, %4, %1;\n\t"
+            "mad.lo.u32 %1, %3, %5, %1;"
+            : "=&r"(w1), "=&r"(w2)
+            : "r"(m0), "r"(m1), "r"((unsigned)R), "r"((unsigned)(R >> 32)));
+        const long long D = (long long)(0ull - (((unsigned long long)w2 << 32) | w1));
+        // floor(R D / 2^84): the signed high word of R * D (R is unsigned), shifted
+        long long hi = (long long)__umul64hi(R, (unsigned long long)D);
+        if (D < 0) hi -= (long long)R;
+        R += (unsigned long long)(hi >> 20);
+    }
+    long long rem = (long long)(0ull - M * R); // 2^116 - M R, exact: |rem| < 2^63
+#pragma unroll
+    for (int it = 0; it < 3; ++it) {
+        const bool up = rem > 0;
+        R += up ? 1ull : 0ull;
+        rem -= up ? (long long)M : 0ll;
+    }
+    if (M == (1ull << 52)) R = ~0ull; // 2^116 / M = 2^64: make_qrecip's 2^64 - 1 (see qdiv)
+    q.r0 = (unsigned)R;
+    q.r1 = (unsigned)(R >> 32);
+    return q;
 }
 
 // Division by a run constant or by dt, with the divisor's reciprocals: FP64 on the integer pipes
@@ -157,9 +214,9 @@ __device__ __forceinline__ float divv(float a, float b) { return __fdiv_rn(a, b)
 // Reciprocal of a cell-dependent value for divr below: IEEE 1/b (FP64), or 1/b (FP32).
 __device__ __forceinline__ double recip(double b) { return __drcp_rn(b); }
 __device__ __forceinline__ float recip(float b) { return __frcp_rn(b); }
-// a / b with rb = recip(b): correctly rounded in FP64 (one: recip_tight(b, rb)), a*rb in FP32.
-__device__ __forceinline__ double divr(double a, double b, double rb, bool one) { return div_rn(a, b, rb, one); }
-__device__ __forceinline__ float divr(float a, float b, float rb, bool) {
+// a / b with rb = recip(b): correctly rounded in FP64, a*rb in FP32.
+__device__ __forceinline__ double divr(double a, double b, double rb) { return div_rn(a, b, rb); }
+__device__ __forceinline__ float divr(float a, float b, float rb) {
     (void)b;
     return a * rb;
 }
@@ -495,7 +552,7 @@ constexpr int kCellBX = 64, kCellBY = 2; // block shape of the one-cell-per-thre
 
 // one: the kernel was built for grid steps whose reciprocals are within a quarter ulp (div_rn)
 template <class T>
-__device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const K<T> &kk, int d, bool one = false) {
+__device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const K<T> &kk, int d) {
     if ((fw & FL_LT) && (fc & FL_LT)) return divq(kk.vis * (u_c - u_cw), kk.dx[d], kk.rdx[d], kk.q_dx[d]);
     if ((fw & FL_LT) && (fc & FL_GT)) return divq(kk.two_vis * (-u_cw), kk.dx[d], kk.rdx[d], kk.q_dx[d]);
     if ((fw & FL_GT) && (fc & FL_LT)) return divq(kk.two_vis * u_c, kk.dx[d], kk.rdx[d], kk.q_dx[d]);
@@ -509,15 +566,15 @@ __device__ __forceinline__ T sigma(uint8_t fw, uint8_t fc, T u_cw, T u_c, const 
 // nuf (FP32 only; nullptr: none): eddy viscosity per face in the same order, added to vis.
 template <class T>
 __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6][3], uint8_t fl, const T uc[3],
-                                             T ro_c, const K<T> &kk, T f[3], const T *nuf = nullptr, bool one = false) {
+                                             T ro_c, const K<T> &kk, T f[3], const T *nuf = nullptr) {
     if constexpr (!Storage<T>::deviation) {
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
             T sw[3], se[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                sw[d] = sigma(fln[2 * d], fl, un[2 * d][m], uc[m], kk, d, one);
-                se[d] = sigma(fl, fln[2 * d + 1], uc[m], un[2 * d + 1][m], kk, d, one);
+                sw[d] = sigma(fln[2 * d], fl, un[2 * d][m], uc[m], kk, d);
+                se[d] = sigma(fl, fln[2 * d + 1], uc[m], un[2 * d + 1][m], kk, d);
             }
             f[m] = ((se[0] - sw[0]) * kk.ds[0] + (se[1] - sw[1]) * kk.ds[1] + (se[2] - sw[2]) * kk.ds[2]) * ro_c;
         }
@@ -593,7 +650,7 @@ __device__ __forceinline__ FaceVal<T> load_face(const FaceSet<T> &F, int f, cons
 // lo[d] (west/south/bottom) and hi[d] (east/north/top).  ro_c: density (FP64) or deviation.
 template <class T>
 __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<T> hi[3], T ro_c, const T uc[3],
-                                          T dt, const K<T> &kk, T &ro_cn, T ucn[3], T &rden_out, bool one = false) {
+                                          T dt, const K<T> &kk, T &ro_cn, T ucn[3], T &rden_out) {
     if constexpr (!Storage<T>::deviation) {
         // new density (main.cpp:530-533)
         ro_cn = divq(ro_c * kk.dvc - (T)0.5 * dt * ((hi[0].ro * hi[0].u[0] - lo[0].ro * lo[0].u[0]) * kk.ds[0] +
@@ -618,7 +675,7 @@ __device__ __forceinline__ void half_step(const FaceVal<T> lo[3], const FaceVal<
                     fx[d] = hi[d].ro * hi[d].u[m] * hi[d].u[d] - lo[d].ro * lo[d].u[m] * lo[d].u[d];
             }
             ucn[m] = divr(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx[0] * kk.ds[0] + fx[1] * kk.ds[1] + fx[2] * kk.ds[2]),
-                          den, rden, false);
+                          den, rden);
         }
     } else {
         // the same balance with the volume divided out and the density as a deviation:
@@ -782,7 +839,7 @@ __device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src,
                 if constexpr (!DEV) {
                     const T den = kk.dvc * ro_cn;
 #pragma unroll
-                    for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden, false);
+                    for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
                 } else {
                     use_forces_f32(ucn, f, dt, kk, rden);
                 }
@@ -886,7 +943,7 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
             if constexpr (!DEV) {
                 const T den = kk.dvc * ro_cn;
 #pragma unroll
-                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden, false);
+                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * f[m], den, rden);
             } else {
                 use_forces_f32(ucn, f, dt, kk, rden);
             }
@@ -930,7 +987,7 @@ template <class T> struct FaceQ {
 // The quantities of the face normal to d with values V: the mass flux ro u_d, the momentum
 // fluxes (ro u_m) u_d (+ p when m == d) of half_step, and StressTensor's sigma_md between the
 // cell below (flags flo, velocity ulo) and the cell above (fhi, uhi).
-template <class T, bool STRESS, bool ONE = false>
+template <class T, bool STRESS>
 __device__ __forceinline__ FaceQ<T> face_q(const FaceVal<T> &V, int d, uint8_t flo, uint8_t fhi, const T ulo[3],
                                            const T uhi[3], const K<T> &kk) {
     FaceQ<T> q;
@@ -938,13 +995,12 @@ __device__ __forceinline__ FaceQ<T> face_q(const FaceVal<T> &V, int d, uint8_t f
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         q.mom[m] = (m == d) ? V.ro * V.u[m] * V.u[d] + V.p : V.ro * V.u[m] * V.u[d];
-        q.sig[m] = STRESS ? sigma(flo, fhi, ulo[m], uhi[m], kk, d, ONE) : (T)0;
+        q.sig[m] = STRESS ? sigma(flo, fhi, ulo[m], uhi[m], kk, d) : (T)0;
     }
     return q;
 }
 
-// ONE: built for grid steps and cell volume whose reciprocals are within a quarter ulp (div_rn)
-template <class T, int MODE, bool ONE = false>
+template <class T, int MODE>
 __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constant__ DevState<T> S, int src, int dst, int fcur, int kch) {
     static_assert(!Storage<T>::deviation, "face-centric Phase1: FP64 storage form");
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
@@ -980,7 +1036,7 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
         cellu(c, uc);
         T ud[3];
         if (STRESS) cellu(c - cs2, ud);
-        zlo = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][2], f, kk), 2, STRESS ? flags[c - cs2] : 0, fl, STRESS ? ud : zero3,
+        zlo = face_q<T, STRESS>(load_face(S.fc[fcur][2], f, kk), 2, STRESS ? flags[c - cs2] : 0, fl, STRESS ? ud : zero3,
                                 uc, kk);
     }
     for (int k = k0; k <= k1; ++k) {
@@ -995,48 +1051,50 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
                 fn = flags[c - 1];
                 cellu(c - 1, un);
             }
-            Fx[ty][tx] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][0], f, kk), 0, fn, fl, un, uc, kk);
+            Fx[ty][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][0], f, kk), 0, fn, fl, un, uc, kk);
             if (i == ilast) {
                 if (STRESS) {
                     fn = flags[c + 1];
                     cellu(c + 1, un);
                 }
-                Fx[ty][tx + 1] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][0], f + 1, kk), 0, fl, fn, uc, un, kk);
+                Fx[ty][tx + 1] = face_q<T, STRESS>(load_face(S.fc[fcur][0], f + 1, kk), 0, fl, fn, uc, un, kk);
             }
             if (STRESS) {
                 fn = flags[c - cs1];
                 cellu(c - cs1, un);
             }
-            Fy[ty][tx] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][1], f, kk), 1, fn, fl, un, uc, kk);
+            Fy[ty][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][1], f, kk), 1, fn, fl, un, uc, kk);
             if (j == jlast) {
                 if (STRESS) {
                     fn = flags[c + cs1];
                     cellu(c + cs1, un);
                 }
-                Fy[ty + 1][tx] = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][1], f + fs1, kk), 1, fl, fn, uc, un, kk);
+                Fy[ty + 1][tx] = face_q<T, STRESS>(load_face(S.fc[fcur][1], f + fs1, kk), 1, fl, fn, uc, un, kk);
             }
             flu = flags[c + cs2];
             cellu(c + cs2, uu);
-            zhi = face_q<T, STRESS, ONE>(load_face(S.fc[fcur][2], f + fs2, kk), 2, fl, flu, uc, uu, kk);
+            zhi = face_q<T, STRESS>(load_face(S.fc[fcur][2], f + fs2, kk), 2, fl, flu, uc, uu, kk);
         }
         __syncthreads();
         if (valid) {
             const FaceQ<T> &Lx = Fx[ty][tx], &Hx = Fx[ty][tx + 1], &Ly = Fy[ty][tx], &Hy = Fy[ty + 1][tx];
             const T ro_c = L.ro[c];
-            T ro_cn, ucn[3], rden = (T)0;
+            T ro_cn, ucn[3];
+            QRecip qden = {0u, 0u, -100000, 0u};
             if (fl & FL_LT) {
                 // half_step (main.cpp:530-551) over the face quantities
                 ro_cn = divq(ro_c * kk.dvc - (T)0.5 * dt * ((Hx.mf - Lx.mf) * kk.ds[0] + (Hy.mf - Ly.mf) * kk.ds[1] +
                                                             (zhi.mf - zlo.mf) * kk.ds[2]),
                              kk.dvc, kk.rdvc, kk.q_dvc);
+                // one reciprocal of the divisor ro_cn dvc serves the three momentum quotients and
+                // UseForces' three, whose divisor dvc ro_cn is the same product
                 const T den = ro_cn * kk.dvc;
-                const T rd = recip(den);
-                rden = rd;
+                qden = qrecip_var(den);
 #pragma unroll
                 for (int m = 0; m < 3; ++m) {
                     const T fx0 = Hx.mom[m] - Lx.mom[m], fx1 = Hy.mom[m] - Ly.mom[m], fx2 = zhi.mom[m] - zlo.mom[m];
-                    ucn[m] = divr(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx0 * kk.ds[0] + fx1 * kk.ds[1] + fx2 * kk.ds[2]),
-                                  den, rd, false);
+                    ucn[m] = qdiv_v(ro_c * uc[m] * kk.dvc - (T)0.5 * dt * (fx0 * kk.ds[0] + fx1 * kk.ds[1] + fx2 * kk.ds[2]),
+                                    den, qden);
                 }
             } else {
                 ucn[0] = ucn[1] = ucn[2] = (T)0;
@@ -1064,7 +1122,7 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constan
                 // UseForces (main.cpp:1035-1041)
                 const T den = kk.dvc * ro_cn;
 #pragma unroll
-                for (int m = 0; m < 3; ++m) ucn[m] = divr(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * fv[m], den, rden, false);
+                for (int m = 0; m < 3; ++m) ucn[m] = qdiv_v(ro_cn * kk.dvc * ucn[m] + (T)0.5 * dt * fv[m], den, qden);
             }
             S.lv[dst].ro[c] = ro_cn;
             S.lv[dst].u1[c] = ucn[0];
@@ -1165,9 +1223,9 @@ template <class T> __global__ void k_use_forces(DevState<T> S, int ncon) {
         const T ro_cn = L.ro[c];
         const T den = kk.dvc * ro_cn;
         const T rden = recip(den);
-        L.u1[c] = divr(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den, rden, false);
-        L.u2[c] = divr(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den, rden, false);
-        L.u3[c] = divr(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den, rden, false);
+        L.u1[c] = divr(ro_cn * kk.dvc * L.u1[c] + (T)0.5 * dt * S.f[0][c], den, rden);
+        L.u2[c] = divr(ro_cn * kk.dvc * L.u2[c] + (T)0.5 * dt * S.f[1][c], den, rden);
+        L.u3[c] = divr(ro_cn * kk.dvc * L.u3[c] + (T)0.5 * dt * S.f[2][c], den, rden);
     } else {
         T u[3] = {L.u1[c], L.u2[c], L.u3[c]};
         const T f[3] = {S.f[0][c], S.f[1][c], S.f[2][c]};
@@ -1188,8 +1246,7 @@ template <class T> struct Ext { T rf, qb, af, ab, bf, bb; };
 
 template <class T> struct SweepK {
     T sound, ro0, c2, rc2, roc, rroc, dt, rdt, dx, rdx;
-    bool one_c2, one_roc, one_dt, one_dx; // FP64: one correction suffices (div_rn)
-    QRecip qc2, qroc, qdt, qdx;           // FP64: the divisors for qdiv
+    QRecip qc2, qroc, qdt, qdx; // FP64: the divisors for qdiv
 };
 
 // The gradient term of a limiter bound: a / dt + b / dx.  FP64: the two correctly rounded
@@ -1399,11 +1456,8 @@ __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> 
     face_store(W, fc, face_values<T, WALL_A_FROM_N>(N, cb, cf, flb, flf, ucb, ucf, prev, cur, uA_old, uB_old, q));
 }
 
-// one: the kernel was built for constants (rho0*c, c^2, the grid step) whose reciprocals are
-// within a quarter ulp, so their FP64 quotients take one correction (div_rn); one_dt: the same for
-// this step's dt (the sweep kernels test it once and run the matching build of their body)
 template <class T>
-__device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d, bool one = false, bool one_dt = false) {
+__device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d) {
     const KT<T> &k = kconst<T>(S.k);
     SweepK<T> q;
     q.sound = k.sound;
@@ -1416,10 +1470,6 @@ __device__ __forceinline__ SweepK<T> sweep_consts(const DevState<T> &S, int d, b
     q.rdt = sc_rdt<T>(S.sc);
     q.dx = k.dx[d];
     q.rdx = k.rdx[d];
-    q.one_c2 = one;
-    q.one_roc = one;
-    q.one_dx = one;
-    q.one_dt = one_dt;
     q.qc2 = k.q_c2;
     q.qroc = k.q_roc;
     q.qdx = k.q_dx[d];
@@ -1498,7 +1548,7 @@ __device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, 
 // (4 lines per warp made the FP64 256x128x128 sweep 20% slower).
 __host__ __device__ inline int x_lines_per_warp(const Geom &g) { return g.C1 < 200 ? 4 : 1; }
 
-template <class T, bool ONE = false, bool ONE_DT = false>
+template <class T>
 __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, int glines, const BIx &bx) {
     const Geom g = S.g;
     const int lane = threadIdx.x & 31;
@@ -1511,7 +1561,7 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
     const FaceOut<T> W = sweep_out(S, fcur, 0);
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
-    const SweepK<T> q = sweep_consts(S, 0, ONE, ONE_DT);
+    const SweepK<T> q = sweep_consts(S, 0);
     const bool bounded = !S.k.periodic_x;
     // a lane's position: line li of the group, cell s, and the line's cell / face 0 indices
     struct Pos {
@@ -1617,19 +1667,10 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     }
 }
 
-// FP64: whether this step's dt has a reciprocal within a quarter ulp (its quotients then take one
-// correction); the same answer in every thread, so the branch between the two builds of a sweep
-// body is uniform
-template <class T> __device__ __forceinline__ bool dt_tight(const DevState<T> &S) {
-    if constexpr (sizeof(T) == 8) return recip_tight(sc_dt<T>(S.sc), sc_rdt<T>(S.sc));
-    else return false;
-}
-
-template <class T, bool ONE = false>
+template <class T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3)
     k_sweep_x(const __grid_constant__ DevState<T> S, int con, int fcur, int glines) {
-    if (dt_tight(S)) sweep_x_body<T, ONE, true>(S, con, fcur, glines, bix_here());
-    else sweep_x_body<T, ONE, false>(S, con, fcur, glines, bix_here());
+    sweep_x_body<T>(S, con, fcur, glines, bix_here());
 }
 
 // x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,
@@ -1638,7 +1679,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3)
 // cells s0..s1 (cell s0 is the one overlap with the previous segment); the face behind
 // the current cell is carried in registers.  Old faces come from generation fcur, new
 // faces go to fcur^1, so segments are independent.
-template <class T, int AX, bool ONE = false, bool ONE_DT = false>
+template <class T, int AX>
 __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, int fcur, int seg, const BIx &bx) {
     const Geom g = S.g;
     const int i = bx.x * 128 + threadIdx.x + 1;
@@ -1650,7 +1691,7 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     const SweepSrc<T> R = sweep_src(S, con, fcur, AX);
     const FaceOut<T> W = sweep_out(S, fcur, AX);
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
-    const SweepK<T> q = sweep_consts(S, AX, ONE, ONE_DT);
+    const SweepK<T> q = sweep_consts(S, AX);
     const int cst = AX == 1 ? (int)g.cs1 : (int)g.cs2, fst = AX == 1 ? (int)g.fs1 : (int)g.fs2;
     int c = (AX == 1 ? g.ci(i, 0, o) : g.ci(i, o, 0)) + s0 * cst;
     int fb = (AX == 1 ? g.fi(i, 0, o) : g.fi(i, o, 0)) + s0 * fst;
@@ -1678,10 +1719,9 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     }
 }
 
-template <class T, int AX, bool ONE = false>
+template <class T, int AX>
 __global__ void __launch_bounds__(128) k_sweep_col(const __grid_constant__ DevState<T> S, int con, int fcur, int seg) {
-    if (dt_tight(S)) sweep_col_body<T, AX, ONE, true>(S, con, fcur, seg, bix_here());
-    else sweep_col_body<T, AX, ONE, false>(S, con, fcur, seg, bix_here());
+    sweep_col_body<T, AX>(S, con, fcur, seg, bix_here());
 }
 
 // ---------------------------------------------------------------------------------------
@@ -2016,24 +2056,16 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
             const int kch = stg::staged_chunk(S.g);
             const dim3 grid((S.g.C1 + fcs::SX - 1) / fcs::SX, (S.g.C2 + fcs::SY - 1) / fcs::SY, (S.g.C3 + kch - 1) / kch);
             const dim3 block(fcs::SX, fcs::SY);
-            // the one-correction quotients where every constant this kernel divides by allows them
-            const KT<double> &kd = S.k.kd;
-            const bool one = kd.one_dx[0] && kd.one_dx[1] && kd.one_dx[2] && kd.one_dvc;
-            auto go = [&](auto k1, auto k0) {
-                if (one) k1<<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
-                else k0<<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
-            };
             switch (mode) {
             case P1_STRESS | P1_FORCES | P1_RMAX:
-                go(fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX, true>,
-                   fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX, false>);
+                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
                 return;
             case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
-                go(fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, true>,
-                   fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, false>);
+                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur,
+                                                                                                      kch);
                 return;
             case P1_FORCES | P1_RSUM:
-                go(fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM, true>, fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM, false>);
+                fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
                 return;
             default: march = 0; break;
             }
@@ -2092,28 +2124,21 @@ inline int sweep_segment(int nd, int target, int *nseg) {
     return (nd + n - 1) / n;
 }
 
-// FP64: the one-correction quotients (div_rn) where rho0*c, c^2 and the sweep's grid step all
-// have reciprocals within a quarter ulp
 template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target) {
-    const KT<double> &kd = S.k.kd;
-    const bool one = std::is_same<T, double>::value && kd.one_roc && kd.one_c2 && kd.one_dx[axis];
     if (axis == 0) {
         const int lines_x = S.g.C2 * S.g.C3, gl = x_lines_per_warp(S.g);
         const dim3 grid((lines_x + 4 * gl - 1) / (4 * gl)); // 4 warps of gl lines
-        if (one) k_sweep_x<T, true><<<grid, 128, 0, st>>>(S, con, fcur, gl);
-        else k_sweep_x<T, false><<<grid, 128, 0, st>>>(S, con, fcur, gl);
+        k_sweep_x<T><<<grid, 128, 0, st>>>(S, con, fcur, gl);
     } else if (axis == 1) {
         int nseg;
         const int seg = sweep_segment(S.g.C2 + 1, target, &nseg);
         const dim3 grid((S.g.C1 + 127) / 128, S.g.C3, nseg);
-        if (one) k_sweep_col<T, 1, true><<<grid, 128, 0, st>>>(S, con, fcur, seg);
-        else k_sweep_col<T, 1, false><<<grid, 128, 0, st>>>(S, con, fcur, seg);
+        k_sweep_col<T, 1><<<grid, 128, 0, st>>>(S, con, fcur, seg);
     } else {
         int nseg;
         const int seg = sweep_segment(S.g.C3 + 1, target, &nseg);
         const dim3 grid((S.g.C1 + 127) / 128, S.g.C2, nseg);
-        if (one) k_sweep_col<T, 2, true><<<grid, 128, 0, st>>>(S, con, fcur, seg);
-        else k_sweep_col<T, 2, false><<<grid, 128, 0, st>>>(S, con, fcur, seg);
+        k_sweep_col<T, 2><<<grid, 128, 0, st>>>(S, con, fcur, seg);
     }
 }
 

@@ -161,10 +161,7 @@ template <class T> struct KT {
     T vrdx[3];        // VIS / dx_d (FP32 stress coefficients)
     T ds[3], dvc, rdvc;
     T vis, two_vis, sound, ro0, c2, rc2, roc, rroc;
-    // FP64: 1 where the constant's reciprocal is within a quarter ulp (|rb*b - 1| <= 2^-54), so
-    // that one correction step gives its correctly rounded quotients (div_rn)
-    unsigned char one_dx[3], one_dvc, one_roc, one_c2;
-    QRecip q_dx[3], q_dvc, q_roc, q_c2; // FP64: the same divisors for qdiv
+    QRecip q_dx[3], q_dvc, q_roc, q_c2; // FP64: the divisors dx, dvc, ro0*c and c^2 for qdiv
 };
 
 // Constants of a run, computed once on the host in double, plus their per-precision copies.

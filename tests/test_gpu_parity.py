@@ -145,20 +145,10 @@ def test_fused_step_matches_oracle_large(ark, port, C, steps):
         assert bits_equal(a, b), (n, rel_l2(a, b))
 
 
-def _recip_tight(b):
-    """RN(1/b) within a quarter ulp, exactly (the FP64 kernels' one-correction condition)."""
-    from fractions import Fraction
-    return abs(Fraction(1.0 / b) * Fraction(b) - 1) <= Fraction(1, 2 ** 54)
-
-
-def test_two_correction_quotients_match_oracle(ark, port):
-    """Constants whose reciprocals are not within a quarter ulp (c^2 = 10.3^2 for the sweeps, the
-    cell volume of a 4.1 x 2 x pi box for Phase1) select the kernels with two correction steps
-    in every division; the result is the oracle's, bit for bit."""
+def test_other_constants_match_oracle(ark, port):
+    """Other run constants (c = 10.3, so c^2 = 106.09; a 4.1 x 2 x pi box) give the integer-pipe
+    quotients other significand reciprocals; the result is the oracle's, bit for bit."""
     p = port.channel_params(64, 32, 32, re_b=2800.0, sound=10.3, lx=4.1, seed=77)
-    dx = [p["lx"] / 64, p["ly"] / 32, p["lz"] / 32]
-    assert not _recip_tight(p["sound"] * p["sound"])
-    assert not _recip_tight(dx[0] * dx[1] * dx[2])
     st0 = port.channel_state(p)
     o = port.Port(p)
     o.load(st0)
