@@ -18,7 +18,8 @@ template void rows_face_density<double>(double *, const double *, int, int64_t, 
 // qdiv is checked on the same pairs, and on a table of divisors prepared by make_qrecip on the
 // host (powers of two, the significands 2^52 + 1 and 2^53 - 1, the channel's constants, random
 // values), where the device's own make_qrecip must also agree with the host's, and qrecip_var
-// (the per-cell divisor's reciprocal) with make_qrecip.
+// (the per-cell divisor's reciprocal) with make_qrecip; qdiv2 against the division of 2a, and
+// dhalf against a / 2.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -53,6 +54,8 @@ __global__ void k_selftest_division(long long n, unsigned long long seed, const 
         if (!same(want, qdiv(a, b, rb, qm))) ++local;
         if (qv.r0 != qm.r0 || qv.r1 != qm.r1 || qv.k != qm.k || qv.sgn != qm.sgn) ++local;
         if (!same(want, qdiv_v(a, b, qv))) ++local;
+        if (!same((2.0 * a) / b, qdiv2(a, b, rb, qm))) ++local;
+        if (!same(a / 2.0, dhalf(a))) ++local;
         const QCase &c = qc[t % nqc];
         if (t < nqc) {
             const QRecip d = make_qrecip(c.b);

@@ -96,8 +96,9 @@ __device__ __forceinline__ double div_rn(double a, double b, double rb) {
 // result outside the normal range take div_rn.  For Mb = 2^52, r = 2^64 - 1 gives
 // T = Ma 2^11 - 1, which rounds up to the exact quotient Ma 2^11.  ark_selftest_division
 // compares this with the hardware division.  qdiv_try returns ok = false where the quotient
-// needs another path.
-__device__ __forceinline__ double qdiv_try(double a, const QRecip &Q, bool &ok) {
+// needs another path.  TWICE: the quotient of 2a (exact for a below 2^1023), which is twice
+// that of a wherever both are normal: the exponent takes the factor.
+template <bool TWICE = false> __device__ __forceinline__ double qdiv_try(double a, const QRecip &Q, bool &ok) {
     const unsigned ha = (unsigned)__double2hiint(a), la = (unsigned)__double2loint(a);
     const unsigned ea = (ha >> 20) & 0x7FFu;
     const unsigned a1 = (ha & 0xFFFFFu) | 0x100000u; // significand high word with the hidden bit
@@ -116,8 +117,8 @@ __device__ __forceinline__ double qdiv_try(double a, const QRecip &Q, bool &ok) 
     const unsigned thi = __funnelshift_l(w2, w3, 11), tlo = __funnelshift_l(w1, w2, 11); // T = P >> 53
     const unsigned s = thi >> 31, sh = 10u + s;
     const unsigned below = tlo << (32u - sh); // T's low sh bits, at the top of the word
-    const int E = (int)ea + (int)s + Q.k;     // the quotient's biased exponent
-    ok = ea - 1u < 2046u && (unsigned)(E - 1) < 2046u && below != 0x80000000u;
+    const int E = (int)ea + (int)s + Q.k + (TWICE ? 1 : 0); // the quotient's biased exponent
+    ok = ea - 1u < (TWICE ? 2045u : 2046u) && (unsigned)(E - 1) < 2046u && below != 0x80000000u;
     const unsigned long long sig =
         (((unsigned long long)(thi >> sh) << 32) | __funnelshift_r(tlo, thi, sh)) + (below > 0x80000000u ? 1ull : 0ull);
     // the significand's hidden bit (bit 52) adds one to the exponent field E - 1; a carry out of
@@ -136,6 +137,21 @@ __device__ __forceinline__ double qdiv(double a, double b, double rb, const QRec
     const double q = qdiv_try(a, Q, ok);
     return ok ? q : div_rn_call(a, b, rb);
 }
+// RN(2a / b), b as for qdiv
+__device__ __forceinline__ double qdiv2(double a, double b, double rb, const QRecip &Q) {
+    bool ok;
+    const double q = qdiv_try<true>(a, Q, ok);
+    return ok ? q : div_rn_call(2.0 * a, b, rb);
+}
+// x / 2: FP64 subtracts one from the exponent field when that is at least 2 (exact, as the
+// multiply by 0.5 is); a zero, tiny or non-finite x takes the multiply.
+static __device__ __noinline__ double halve_call(double x) { return x * 0.5; }
+__device__ __forceinline__ double dhalf(double x) {
+    const unsigned h = (unsigned)__double2hiint(x);
+    if (((h >> 20) & 0x7FFu) - 2u < 2045u) return __hiloint2double((int)(h - 0x100000u), __double2loint(x));
+    return halve_call(x);
+}
+__device__ __forceinline__ float dhalf(float x) { return x / 2.f; }
 // b that changes from cell to cell (Q from qrecip_var): the other path is the IEEE division
 __device__ __forceinline__ double qdiv_v(double a, double b, const QRecip &Q) {
     bool ok;
@@ -1001,7 +1017,7 @@ __device__ __forceinline__ FaceQ<T> face_q(const FaceVal<T> &V, int d, uint8_t f
 }
 
 template <class T, int MODE>
-__global__ void __launch_bounds__(SX *SY, 2) k_phase1_faces(const __grid_constant__ DevState<T> S, int src, int dst, int fcur, int kch) {
+__global__ void __launch_bounds__(SX *SY, 3) k_phase1_faces(const __grid_constant__ DevState<T> S, int src, int dst, int fcur, int kch) {
     static_assert(!Storage<T>::deviation, "face-centric Phase1: FP64 storage form");
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
     __shared__ FaceQ<T> Fx[SY][SX + 1], Fy[SY + 1][SX];
@@ -1249,12 +1265,15 @@ template <class T> struct SweepK {
     QRecip qc2, qroc, qdt, qdx; // FP64: the divisors for qdiv
 };
 
-// The gradient term of a limiter bound: a / dt + b / dx.  FP64: the two correctly rounded
-// quotients summed, as the reference evaluates it; FP32: a * (1/dt) + b * (1/dx), fused.
-__device__ __forceinline__ double grad_sum(double a, double b, const SweepK<double> &q) {
-    return divq(a, q.dt, q.rdt, q.qdt) + divq(b, q.dx, q.rdx, q.qdx);
+// The gradient term of a limiter bound, (2 d) / dt + b / dx.  FP64: the two correctly rounded
+// quotients summed, as the reference evaluates it, the first one with the factor 2 taken by its
+// exponent (qdiv2); FP32: (2 d) * (1/dt) + b * (1/dx), fused.
+__device__ __forceinline__ double grad_sum(double d, double b, const SweepK<double> &q) {
+    return qdiv2(d, q.dt, q.rdt, q.qdt) + divq(b, q.dx, q.rdx, q.qdx);
 }
-__device__ __forceinline__ float grad_sum(float a, float b, const SweepK<float> &q) { return __fmaf_rn(a, q.rdt, b * q.rdx); }
+__device__ __forceinline__ float grad_sum(float d, float b, const SweepK<float> &q) {
+    return __fmaf_rn(2.f * d, q.rdt, b * q.rdx);
+}
 
 // One cell of a sweep (main.cpp:1756-1873 for x1; the x2 and x3 sweeps are the same with
 // the axes permuted).  u1: the velocity component normal to the sweep, u2/u3: tangential.
@@ -1297,10 +1316,10 @@ __device__ __forceinline__ Ext<T> extrapolate_rq(RQ<T> f, RQ<T> b, T u1_cn, T u1
     T u3_fn = twice_minus(u3_cn, u3_b);
     T u3_bn = twice_minus(u3_cn, u3_f);
 
-    const T gr = grad_sum((T)2 * (r_cn - r_c), (u1_cn + q.sound) * (r_f - r_b), q);
-    const T gq = grad_sum((T)2 * (Q_USES_R ? (r_cn - r_c) : (q_cn - q_c)), (u1_cn - q.sound) * (q_f - q_b), q);
-    const T gu2 = grad_sum((T)2 * (u2_cn - u2_c), u1_cn * (u2_f - u2_b), q);
-    const T gu3 = grad_sum((T)2 * (u3_cn - u3_c), u1_cn * (u3_f - u3_b), q);
+    const T gr = grad_sum(r_cn - r_c, (u1_cn + q.sound) * (r_f - r_b), q);
+    const T gq = grad_sum(Q_USES_R ? (r_cn - r_c) : (q_cn - q_c), (u1_cn - q.sound) * (q_f - q_b), q);
+    const T gu2 = grad_sum(u2_cn - u2_c, u1_cn * (u2_f - u2_b), q);
+    const T gu3 = grad_sum(u3_cn - u3_c, u1_cn * (u3_f - u3_b), q);
 
     const T rmax = mad(q.dt, gr, max3d(r_f, r_c, r_b));
     const T rmin = mad(q.dt, gr, min3d(r_f, r_c, r_b));
@@ -1375,8 +1394,8 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
     T un, pn, ro_n, ua, ub;
     if ((flb & FL_LT) && (flf & FL_LT)) {
         const T rn = prev.rf, qn = cur.qb;
-        un = (rn + qn) / (T)2;
-        pn = (rn - qn) * q.sound * q.ro0 / (T)2;
+        un = dhalf(rn + qn);
+        pn = dhalf((rn - qn) * q.sound * q.ro0);
         ro_n = q.ro0 + divq(pn, q.c2, q.rc2, q.qc2);
         if (ge0(ucf) && ge0(ucb)) {
             ua = prev.af;
