@@ -595,6 +595,23 @@ __device__ __forceinline__ void stress_force(const uint8_t fln[6], const T un[6]
             f[m] = ((se[0] - sw[0]) * kk.ds[0] + (se[1] - sw[1]) * kk.ds[1] + (se[2] - sw[2]) * kk.ds[2]) * ro_c;
         }
     } else {
+        if (!nuf && (fl & fln[0] & fln[1] & fln[2] & fln[3] & fln[4] & fln[5] & FL_LT)) {
+            // a fluid cell among fluid neighbours: every coefficient is VIS / dx_d, the values the
+            // general form below selects for such faces, in the same arithmetic
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                T acc = (T)0;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const T v = kk.vrdx[d];
+                    const T sw = mad(v, uc[m], -(v * un[2 * d][m]));
+                    const T se = mad(v, un[2 * d + 1][m], -(v * uc[m]));
+                    acc = mad(se - sw, kk.ds[d], acc);
+                }
+                f[m] = acc * ro_c;
+            }
+            return;
+        }
         T aw[6], ac[6]; // per face: coefficient on the cell behind (w) and ahead (c)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
