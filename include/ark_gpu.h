@@ -236,11 +236,14 @@ int ark_plane_stats(ark_ctx *ctx, double *out);
  * n1_cells*((j-1) + n2_cells*(k-1)), host byte order.  Synchronous. */
 int ark_vorticity(ark_ctx *ctx, double *out);
 
-/* Self-check of the correctly rounded division by a run constant that the FP64 kernels use
- * (q = a*RN(1/b) plus two Markstein corrections) against the GPU's IEEE division, on n
- * random operand pairs and on small exact cases, in both its forms (two correction steps, and
- * one where the divisor's reciprocal is within a quarter ulp); *mismatches receives the count
- * (0 expected).
+/* Self-check of the correctly rounded FP64 divisions the FP64 kernels use, against the GPU's
+ * IEEE division, on n random operand pairs (numerators over the whole exponent range, zeros
+ * and subnormals included) and on small exact cases: the integer-pipe quotient by a divisor
+ * with a prepared significand reciprocal (run constants, dt), the same with the numerator
+ * doubled, the per-cell divisor's reciprocal built by integer Newton steps and its quotients,
+ * the exact halving, and the Markstein form q = a*RN(1/b) with two corrections that the rare
+ * cases fall back to; also that the device prepares the same reciprocals as the host.
+ * *mismatches receives the count (0 expected).
  * Runs on the current device. */
 int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches);
 
