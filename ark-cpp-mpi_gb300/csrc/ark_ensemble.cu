@@ -248,13 +248,13 @@ int build_lists(ark_ensemble *E) {
             case WL_COL1: {
                 const int seg = segment_for(g.C2 + 1, E->shape.seg);
                 extra[q] = seg;
-                gx = (g.C1 + 127) / 128, gy = g.C3, gz = (g.C2 + 1 + seg - 1) / seg;
+                gx = col_sweep_blocks(g, 1), gz = (g.C2 + 1 + seg - 1) / seg;
                 break;
             }
             case WL_COL2: {
                 const int seg = segment_for(g.C3 + 1, E->shape.seg);
                 extra[q] = seg;
-                gx = (g.C1 + 127) / 128, gy = g.C2, gz = (g.C3 + 1 + seg - 1) / seg;
+                gx = col_sweep_blocks(g, 2), gz = (g.C3 + 1 + seg - 1) / seg;
                 break;
             }
             case WL_WRAP: { // one thread per ghost line, looping over the job's arrays

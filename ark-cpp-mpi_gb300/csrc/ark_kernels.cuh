@@ -1714,15 +1714,22 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3)
 // loads issued before the current cell is computed.  A segment of faces s0+1..s1 needs
 // cells s0..s1 (cell s0 is the one overlap with the previous segment); the face behind
 // the current cell is carried in registers.  Old faces come from generation fcur, new
-// faces go to fcur^1, so segments are independent.
+// faces go to fcur^1, so segments are independent.  Each warp takes 32 consecutive i of one
+// line row o: warp q of the grid covers chunk q % ceil(C1/32) of row q / ceil(C1/32), so rows
+// narrower than a block (an ensemble's 32- and 64-cell members) still fill every lane.
+__host__ __device__ inline int col_sweep_blocks(const Geom &g, int axis) {
+    return (((g.C1 + 31) >> 5) * (axis == 1 ? g.C3 : g.C2) + 3) >> 2;
+}
 template <class T, int AX>
 __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, int fcur, int seg, const BIx &bx) {
     const Geom g = S.g;
-    const int i = bx.x * 128 + threadIdx.x + 1;
-    const int o = bx.y + 1;
+    const int nic = (g.C1 + 31) >> 5;
+    const int wq = bx.x * 4 + (threadIdx.x >> 5); // this warp's (chunk, row)
+    const int i = (wq % nic) * 32 + (threadIdx.x & 31) + 1;
+    const int o = wq / nic + 1;
     const int nd = (AX == 1 ? g.C2 : g.C3) + 1;
     const int s0 = bx.z * seg;
-    if (i > g.C1 || s0 >= nd) return;
+    if (i > g.C1 || o > (AX == 1 ? g.C3 : g.C2) || s0 >= nd) return;
     const int s1 = s0 + seg < nd ? s0 + seg : nd;
     const SweepSrc<T> R = sweep_src(S, con, fcur, AX);
     const FaceOut<T> W = sweep_out(S, fcur, AX);
@@ -2168,12 +2175,12 @@ template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur
     } else if (axis == 1) {
         int nseg;
         const int seg = sweep_segment(S.g.C2 + 1, target, &nseg);
-        const dim3 grid((S.g.C1 + 127) / 128, S.g.C3, nseg);
+        const dim3 grid(col_sweep_blocks(S.g, 1), 1, nseg);
         k_sweep_col<T, 1><<<grid, 128, 0, st>>>(S, con, fcur, seg);
     } else {
         int nseg;
         const int seg = sweep_segment(S.g.C3 + 1, target, &nseg);
-        const dim3 grid((S.g.C1 + 127) / 128, S.g.C2, nseg);
+        const dim3 grid(col_sweep_blocks(S.g, 2), 1, nseg);
         k_sweep_col<T, 2><<<grid, 128, 0, st>>>(S, con, fcur, seg);
     }
 }
