@@ -19,7 +19,7 @@ template void rows_face_density<double>(double *, const double *, int, int64_t, 
 // host (powers of two, the significands 2^52 + 1 and 2^53 - 1, the channel's constants, random
 // values), where the device's own make_qrecip must also agree with the host's, and qrecip_var
 // (the per-cell divisor's reciprocal) with make_qrecip; qdiv2 against the division of 2a, and
-// dhalf against a / 2.
+// dhalf against a / 2, and the integer fixed-point image (fixed32) against its FP64 form.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -56,6 +56,9 @@ __global__ void k_selftest_division(long long n, unsigned long long seed, const 
         if (!same(want, qdiv_v(a, b, qv))) ++local;
         if (!same((2.0 * a) / b, qdiv2(a, b, rb, qm))) ++local;
         if (!same(a / 2.0, dhalf(a))) ++local;
+        // the fixed-point image, over the whole range and near ties (values of 2^-33 multiples)
+        const double v1 = (t & 1) ? a : (double)(long long)(za >> 20) * 0x1p-33 * ((t & 2) ? -1.0 : 1.0);
+        if (fixed32(v1) != fixed32_fp64(v1)) ++local;
         const QCase &c = qc[t % nqc];
         if (t < nqc) {
             const QRecip d = make_qrecip(c.b);

@@ -258,11 +258,33 @@ __device__ __forceinline__ unsigned long long abs_bits(float v) {
     return (unsigned long long)__double_as_longlong((double)fabsf(v));
 }
 
-// Fixed-point image of a value: round(v * 2^32), NaN -> 0, clamped to +-2^30.
-__device__ __forceinline__ long long fixed32(double v) {
+// Fixed-point image of a value: round(v * 2^32) (to nearest, ties to even), NaN -> 0, v clamped
+// to +-2^30.  The FP64 form (fixed32_fp64) costs five FP64-pipe instructions; this one takes the
+// same integer from the bits: v = M 2^(e-1075), so v 2^32 = M 2^(e-1043), a left shift for
+// e >= 1043 and a rounded right shift below.  ark_selftest_division compares the two.
+__device__ __forceinline__ long long fixed32_fp64(double v) {
     if (v != v) v = 0.0;
     v = fmin(fmax(v, -1073741824.0), 1073741824.0);
     return __double2ll_rn(v * 4294967296.0);
+}
+__device__ __forceinline__ long long fixed32(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    const unsigned long long M = (b & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned long long m;
+    if (e >= 1053) { // |v| >= 2^30, infinities and NaN
+        if (e == 0x7FF && (b & 0x000FFFFFFFFFFFFFull)) return 0;
+        m = 1ull << 62;
+    } else if (e >= 1043) {
+        m = M << (e - 1043);
+    } else if (e >= 1043 - 54) { // shifts of 1..54: round to nearest, ties to even
+        const int k = 1043 - e;
+        const unsigned long long q = M >> k, r = M & ((1ull << k) - 1), half = 1ull << (k - 1);
+        m = q + ((r > half || (r == half && (q & 1))) ? 1ull : 0ull);
+    } else {
+        m = 0; // below 2^-33: rounds to zero (zeros and subnormals included)
+    }
+    return (b >> 63) ? -(long long)m : (long long)m;
 }
 
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
