@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(128) kb_wrap(const DS *__restrict__ inst, cons
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
         const BIx bx = decode(W, q, b);
-        wrap_body_lines<float>(inst[q].g, jobs[q], (int64_t)bx.x * 128 + threadIdx.x);
+        wrap_body_lines<float>(inst[q].g, jobs[q], bx.x * 128 + (int)threadIdx.x);
     }
 }
 

@@ -495,15 +495,30 @@ struct WrapJob {
 //   GH_COPY (bounded axis): zero-gradient ghost 0 <- cell 1, ghost C+1 <- cell C; faces:
 //           halo 0 <- face 1, halo C+2 <- face C+1 (main.cpp:803-845, 1633-1698);
 // over the interior of the other two axes.
-// The two ghosts of line r of array q: lines first the (j, k) lines of x, then the (i, j)
-// lines of z.
-template <class T> __device__ __forceinline__ void wrap_copy(const Geom &g, const WrapJob &J, int q, int64_t r) {
-    const int64_t nx = (int64_t)g.C2 * g.C3;
+// Ghost line r: first the (j, k) lines of x, then the (i, j) lines of z.  Its position is found
+// once per line, in 32-bit arithmetic (line counts stay below 2^31), and serves every array.
+struct WrapLine {
+    int a, b; // (j, k) of an x line, (i, j) of a z line
+    bool z;
+};
+__device__ __forceinline__ WrapLine wrap_line(const Geom &g, int r) {
+    const int nx = g.C2 * g.C3;
+    WrapLine L;
+    L.z = r >= nx;
+    const int u = L.z ? r - nx : r, w = L.z ? g.C1 : g.C2;
+    const int hi = u / w;
+    L.a = u - hi * w + 1;
+    L.b = hi + 1;
+    return L;
+}
+__host__ __device__ inline int wrap_lines(const Geom &g) { return g.C2 * g.C3 + g.C1 * g.C2; }
+// The two ghosts of line L of array q.
+template <class T> __device__ __forceinline__ void wrap_copy(const Geom &g, const WrapJob &J, int q, const WrapLine &L) {
     T *a = (T *)J.a[q];
-    if (r < nx) {
+    if (!L.z) {
         const uint8_t m = J.mode[q][0];
         if (m == GH_NONE) return;
-        const int j = (int)(r % g.C2) + 1, k = (int)(r / g.C2) + 1;
+        const int j = L.a, k = L.b;
         if (J.face[q]) {
             a[g.face(0, j, k)] = a[g.face(m == GH_WRAP ? g.C1 : 1, j, k)];
             a[g.face(g.C1 + 2, j, k)] = a[g.face(m == GH_WRAP ? 2 : g.C1 + 1, j, k)];
@@ -514,8 +529,7 @@ template <class T> __device__ __forceinline__ void wrap_copy(const Geom &g, cons
     } else {
         const uint8_t m = J.mode[q][1];
         if (m == GH_NONE) return;
-        const int64_t u = r - nx;
-        const int i = (int)(u % g.C1) + 1, j = (int)(u / g.C1) + 1;
+        const int i = L.a, j = L.b;
         if (J.face[q]) {
             a[g.face(i, j, 0)] = a[g.face(i, j, m == GH_WRAP ? g.C3 : 1)];
             a[g.face(i, j, g.C3 + 2)] = a[g.face(i, j, m == GH_WRAP ? 2 : g.C3 + 1)];
@@ -526,24 +540,19 @@ template <class T> __device__ __forceinline__ void wrap_copy(const Geom &g, cons
     }
 }
 
-// Thread t copies line t mod (lines) of array t / (lines).
-template <class T> __device__ __forceinline__ void wrap_body(const Geom &g, const WrapJob &J, int64_t t) {
-    const int64_t nl = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
-    const int q = (int)(t / nl);
-    if (q >= J.n) return;
-    wrap_copy<T>(g, J, q, t - (int64_t)q * nl);
+// One thread per line looping over the arrays (the ensemble's batched ghost fill, whose
+// parallelism comes from the members).
+template <class T> __device__ __forceinline__ void wrap_body_lines(const Geom &g, const WrapJob &J, int t) {
+    if (t >= wrap_lines(g)) return;
+    const WrapLine L = wrap_line(g, t);
+    for (int q = 0; q < J.n; ++q) wrap_copy<T>(g, J, q, L);
 }
 
-// The same copies with one thread per line looping over the arrays (the ensemble's batched
-// ghost fill, whose parallelism comes from the members).
-template <class T> __device__ __forceinline__ void wrap_body_lines(const Geom &g, const WrapJob &J, int64_t t) {
-    const int64_t nl = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
-    if (t >= nl) return;
-    for (int q = 0; q < J.n; ++q) wrap_copy<T>(g, J, q, t);
-}
-
+// Thread x copies line x of array blockIdx.y.
 template <class T> __global__ void k_wrap(Geom g, const __grid_constant__ WrapJob J) {
-    wrap_body<T>(g, J, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= wrap_lines(g)) return;
+    wrap_copy<T>(g, J, blockIdx.y, wrap_line(g, t));
 }
 
 // BoundaryConditions::alongX1/2/3 (source/BoundaryConditions.cpp:22-83) on one cell level,
@@ -2024,8 +2033,7 @@ inline void wrap_add(WrapJob &J, void *a, int face, uint8_t mx, uint8_t mz) {
 
 template <class T> inline void wrap_launch(const DevState<T> &S, const WrapJob &J, cudaStream_t st) {
     if (J.n == 0) return;
-    const int64_t tot = ((int64_t)S.g.C2 * S.g.C3 + (int64_t)S.g.C1 * S.g.C2) * J.n;
-    k_wrap<T><<<grid_for(tot, 256, 1 << 30), 256, 0, st>>>(S.g, J);
+    k_wrap<T><<<dim3((wrap_lines(S.g) + 255) / 256, J.n), 256, 0, st>>>(S.g, J);
 }
 
 // StressTensor's exchange of u1Con, u2Con, u3Con (main.cpp:603-845): periodic axes wrap,
