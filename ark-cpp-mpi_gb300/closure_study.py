@@ -13,7 +13,7 @@
    held out.
 3. The network is trained on the device (ark_mlp_train) and scored on the held-out samples
    against no closure (nu_t = 0) and the best constant eddy viscosity.
-4. The judge: the fine state at the start of a window, volume-averaged onto the coarse grid,
+4. The assessment: the fine state at the start of a window, volume-averaged onto the coarse grid,
    runs `coarse-steps` coarse steps twice, without and with the closure; the fine run covers
    the same physical time.  Plane statistics (means over x, z and time of u and of the
    products u_i u_j) of the coarse runs are compared with those of the box-filtered fine
@@ -228,7 +228,7 @@ def main():
     heldd.close()
     del ttr
 
-    # the judge window
+    # the assessment window
     names = ["ronCon", "u1nCon", "u2nCon", "u3nCon"]
     st = fine.download(names)
     t_window = fine.scalars().time
@@ -274,13 +274,13 @@ def main():
         fstats.add(scratch.filtered_stats())
     scratch.close()
     fres = fstats.result(pf.ly)
-    rep["judge"] = {"window_start_time": t_window, "physical_time": t_phys, "fine_steps": steps_f,
+    rep["assessment"] = {"window_start_time": t_window, "physical_time": t_phys, "fine_steps": steps_f,
                     "fine_gpu_ms": ms_f, "coarse_steps": a.coarse_steps}
     for mode in ("plain", "closure"):
         e = compare(coarse[mode]["stats"], fres)
-        rep["judge"][mode] = {"errors": e, "gpu_ms": coarse[mode]["gpu_ms"],
+        rep["assessment"][mode] = {"errors": e, "gpu_ms": coarse[mode]["gpu_ms"],
                               "gpu_time_ratio_fine_over_coarse": ms_f / coarse[mode]["gpu_ms"]}
-    rep["judge"]["profiles"] = {
+    rep["assessment"]["profiles"] = {
         "y_coarse": coarse["plain"]["stats"]["y"].tolist(),
         "U_fine_filtered": np.interp(coarse["plain"]["stats"]["y"], fres["y"], fres["U"]).tolist(),
         "U_plain": coarse["plain"]["stats"]["U"].tolist(), "U_closure": coarse["closure"]["stats"]["U"].tolist(),
@@ -296,7 +296,7 @@ def main():
         with open(a.out, "w") as f:
             f.write(txt)
     short = {k: v for k, v in rep.items() if k not in ("network",)}
-    short["judge"] = {k: v for k, v in rep["judge"].items() if k != "profiles"}
+    short["assessment"] = {k: v for k, v in rep["assessment"].items() if k != "profiles"}
     print(json.dumps(short, indent=1))
 
 
