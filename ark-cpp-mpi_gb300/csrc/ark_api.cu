@@ -564,6 +564,7 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     if (const char *e = std::getenv("ARK_PHASE2_FUSED"))
         if (e[0] >= '0' && e[0] <= '2' && (e[0] != '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
     Launch<float>::prepare();
+    Launch<double>::prepare();
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
     *status = ARK_OK;

@@ -1047,6 +1047,9 @@ constexpr int SX = 64, SY = 4;
 template <class T> struct FaceQ {
     T mf, mom[3], sig[3];
 };
+// dynamic shared memory of k_phase1_faces: two generations of SY x (SX + 1) x faces and
+// (SY + 1) x SX y faces
+template <class T> constexpr int face_smem() { return 2 * (SY * (SX + 1) + (SY + 1) * SX) * (int)sizeof(FaceQ<T>); }
 
 // The quantities of the face normal to d with values V: the mass flux ro u_d, the momentum
 // fluxes (ro u_m) u_d (+ p when m == d) of half_step, and StressTensor's sigma_md between the
@@ -1068,7 +1071,15 @@ template <class T, int MODE>
 __global__ void __launch_bounds__(SX *SY, 3) k_phase1_faces(const __grid_constant__ DevState<T> S, int src, int dst, int fcur, int kch) {
     static_assert(!Storage<T>::deviation, "face-centric Phase1: FP64 storage form");
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
-    __shared__ FaceQ<T> Fx[SY][SX + 1], Fy[SY + 1][SX];
+    // two generations of a plane's x and y face quantities (face_smem bytes), alternating by
+    // plane: a thread may write plane k+1's while others still read plane k's, and the barrier
+    // of plane k+1 keeps plane k+2's writes behind every read of plane k, so one barrier per
+    // plane suffices
+    extern __shared__ __align__(16) unsigned char fcs_sm[];
+    typedef FaceQ<T> RowX[SX + 1];
+    typedef FaceQ<T> RowY[SX];
+    RowX *const FxAll = reinterpret_cast<RowX *>(fcs_sm);
+    RowY *const FyAll = reinterpret_cast<RowY *>(fcs_sm + 2 * SY * sizeof(RowX));
     const Geom g = S.g;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i = blockIdx.x * SX + tx + 1, j = blockIdx.y * SY + ty + 1;
@@ -1104,6 +1115,8 @@ __global__ void __launch_bounds__(SX *SY, 3) k_phase1_faces(const __grid_constan
                                 uc, kk);
     }
     for (int k = k0; k <= k1; ++k) {
+        RowX *const Fx = FxAll + ((k - k0) & 1) * SY;
+        RowY *const Fy = FyAll + ((k - k0) & 1) * (SY + 1);
         FaceQ<T> zhi = {};
         uint8_t flu = 0;
         T uu[3] = {(T)0, (T)0, (T)0};
@@ -1200,7 +1213,6 @@ __global__ void __launch_bounds__(SX *SY, 3) k_phase1_faces(const __grid_constan
             }
             if ((MODE & P1_RSUM) && (fl & FL_EQ0)) rsum += fixed_sum_term(ucn[0]);
         }
-        __syncthreads();
         zlo = zhi;
         fl = flu;
         uc[0] = uu[0];
@@ -2131,14 +2143,14 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
             const dim3 block(fcs::SX, fcs::SY);
             switch (mode) {
             case P1_STRESS | P1_FORCES | P1_RMAX:
-                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_RMAX><<<grid, block, fcs::face_smem<T>(), st>>>(S, src, dst, fcur, kch);
                 return;
             case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
-                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX><<<grid, block, 0, st>>>(S, src, dst, fcur,
+                fcs::k_phase1_faces<T, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX><<<grid, block, fcs::face_smem<T>(), st>>>(S, src, dst, fcur,
                                                                                                       kch);
                 return;
             case P1_FORCES | P1_RSUM:
-                fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM><<<grid, block, 0, st>>>(S, src, dst, fcur, kch);
+                fcs::k_phase1_faces<T, P1_FORCES | P1_RSUM><<<grid, block, fcs::face_smem<T>(), st>>>(S, src, dst, fcur, kch);
                 return;
             default: march = 0; break;
             }
@@ -2165,6 +2177,14 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
 }
 
 template <class T> void Launch<T>::prepare() {
+    if constexpr (std::is_same<T, double>::value) {
+        constexpr int fb = fcs::face_smem<double>();
+        cudaFuncSetAttribute(fcs::k_phase1_faces<double, P1_STRESS | P1_FORCES | P1_RMAX>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, fb);
+        cudaFuncSetAttribute(fcs::k_phase1_faces<double, P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, fb);
+        cudaFuncSetAttribute(fcs::k_phase1_faces<double, P1_FORCES | P1_RSUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, fb);
+    }
     if constexpr (std::is_same<T, float>::value) {
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_RMAX>();
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>();
