@@ -8,6 +8,8 @@
   integer path takes the quotient, including ties of short significands and the power-of-two
   divisors.  The FP32 seed of the Newton steps is modelled as RN32(1/f) moved by up to two
   units in the last place, the approximation's error bound.
+* A model of the integer fixed-point image of the bulk-flow sum (fixed32) equals the FP64 form's
+  round(v * 2^32), ties to even, clamping and NaN included.
 The GPU's own check of the same code is ark_selftest_division (tests/test_gpu_parity.py).
 """
 import os
@@ -176,3 +178,40 @@ def test_newton_reciprocal_reaches_the_ceiling():
         want = exact_recip(b)[0]
         for u in (-2, -1, 0, 1, 2):
             assert newton_model(b, u) == want, (M, u)
+
+
+def fixed32_model(v):
+    """The device's integer fixed32: round(v * 2^32) to nearest even, v clamped to +-2^30, NaN -> 0."""
+    b = bits(v)
+    e = (b >> 52) & 0x7FF
+    M = (b & ((1 << 52) - 1)) | (1 << 52)
+    if e >= 1053:
+        if e == 0x7FF and (b & ((1 << 52) - 1)):
+            return 0
+        m = 1 << 62
+    elif e >= 1043:
+        m = M << (e - 1043)
+    elif e >= 1043 - 54:
+        k = 1043 - e
+        q, r, half = M >> k, M & ((1 << k) - 1), 1 << (k - 1)
+        m = q + (1 if (r > half or (r == half and (q & 1))) else 0)
+    else:
+        m = 0
+    return -m if b >> 63 else m
+
+
+def test_fixed_point_image_model_matches_the_fp64_form():
+    """round(v * 2^32) as the FP64 form computes it: clamp to +-2^30, scale (exact), round to
+    nearest even; over the whole exponent range, ties, zeros, infinities and NaN."""
+    rng = random.Random(17)
+    vals = [0.0, -0.0, float("inf"), -float("inf"), float("nan"), 2.0 ** 30, -2.0 ** 30, 2.0 ** 31, 5e-324,
+            2.0 ** -33, 3 * 2.0 ** -33, -2.0 ** -33, 2.0 ** -34, 2.0 ** 29 + 0.5]
+    vals += [from_bits(rng.getrandbits(64)) for _ in range(20000)]
+    vals += [rng.randint(-2 ** 44, 2 ** 44) * 2.0 ** -33 for _ in range(20000)]  # ties
+    for v in vals:
+        if v != v:
+            want = 0
+        else:
+            c = min(max(v, -2.0 ** 30), 2.0 ** 30)
+            want = int(np.rint(np.float64(c) * np.float64(2.0 ** 32)))  # exact scaling, ties to even
+        assert fixed32_model(v) == want, v
