@@ -172,7 +172,7 @@ struct ark_ensemble {
     WrapJob *d_jobs = nullptr; // [6][n]: wrap_con for level 0/1, wrap_phase2 for (con, fcur)
     int persist = 1;           // persistent blocks per launch (all SMs x resident blocks)
     int persist_staged = 1;    // the same for the staged Phase1 (2 blocks of 256 threads per SM)
-    Shape shape = {1, 0, 32};
+    Shape shape = {2, 2, 32}; // staged Phase1 for both launches: what the autotuner picks on mixed ensembles
     int con = 0, fcur = 0;
     bool parts_valid = false;
     bool uploaded_all = false;

@@ -345,7 +345,8 @@ int ark_ensemble_mean_profile(ark_ensemble *ens, int member, double *mean_u1, do
  * ints, or NULL): {Phase1+stress shape, second Phase1 shape, segment target, microseconds per
  * step}. */
 int ark_ensemble_autotune(ark_ensemble *ens, int steps_per_candidate, int *choice);
-/* Sets the kernel shape directly (march_a / march_b: 0, 1 or 2 as above). */
+/* Sets the kernel shape directly (march_a / march_b: 0, 1 or 2 as above).  Until this or
+ * ark_ensemble_autotune is called, an ensemble uses 2, 2 and 32-face segments. */
 int ark_ensemble_set_shape(ark_ensemble *ens, int march_a, int march_b, int segment);
 
 /* ---- host-side helpers (no GPU needed) ----------------------------------------------------- */
