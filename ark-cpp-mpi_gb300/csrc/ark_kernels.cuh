@@ -2,7 +2,9 @@
 //
 // ark_fp64.cu instantiates T = double in a translation unit compiled with --fmad=false:
 // every FP64 expression below keeps the reference's operand order (source/main.cpp), so the
-// FP64 path rounds exactly like the reference built with -ffp-contract=off.
+// FP64 path rounds exactly like the reference built with -ffp-contract=off.  Its quotients are
+// the correctly rounded IEEE ones, taken on the integer pipes where they can be (qdiv,
+// qrecip_var), with the Markstein form (div_rn) and the IEEE division for the rest.
 // ark_fp32.cu instantiates T = float (also without FMA contraction) with the density stored as
 // the deviation rho - ro0 and face density derived from face pressure (Storage<T>).
 //
