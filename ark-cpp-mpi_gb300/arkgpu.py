@@ -27,7 +27,7 @@ STATE_FIELDS = CELL_FIELDS + FACE_FIELDS
 EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "ark_cell_count",
            "ark_face_count", "ark_upload", "ark_download", "ark_get_array", "ark_put_array",
            "ark_time_step_size", "ark_phase1", "ark_stress_tensor", "ark_use_forces", "ark_phase2",
-           "ark_boundary_fill", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
+           "ark_boundary_fill", "ark_boundary_conditions", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
            "ark_get_scalars", "ark_set_scalars", "ark_conservation_sums", "ark_channel_init",
            "ark_kernel_times", "ark_kernel_name", "ark_step_kernel_name", "ark_alloc_host_state", "ark_free_host_state",
            "ark_conservation_sums_noalloc", "ark_mean_profile", "ark_selftest_division",
@@ -115,6 +115,7 @@ def lib():
                    "ark_sync"):
             getattr(L, fn).argtypes = [vp]
         L.ark_boundary_fill.argtypes = [vp, ctypes.c_int]
+        L.ark_boundary_conditions.argtypes = [vp] + [ctypes.c_int] * 4
         L.ark_set_dt.argtypes = [vp, ctypes.c_double]
         L.ark_step.argtypes = [vp, ctypes.c_int]
         L.ark_time_steps.argtypes = [vp, ctypes.c_int, _DP]
@@ -345,6 +346,10 @@ class Context:
 
     def boundary_fill(self, axis):
         self._call("ark_boundary_fill", int(axis))
+
+    def boundary_conditions(self, axis, x1_period, x2_period, x3_period):
+        """BoundaryConditions(..., x1Period, x2Period, x3Period, ...).alongX<axis>() on "nCon"."""
+        self._call("ark_boundary_conditions", int(axis), int(x1_period), int(x2_period), int(x3_period))
 
     def set_dt(self, dt):
         self._call("ark_set_dt", float(dt))

@@ -168,6 +168,7 @@ struct Engine {
 namespace ark {
 // Run constants of a parameter set (shared with the ensemble code).
 Consts make_run_consts(const ark_params &p) { return make_consts(p); }
+int api_fail(int status, const std::string &msg) { return fail(status, msg); }
 } // namespace ark
 
 struct ark_ctx {
@@ -762,6 +763,16 @@ int ark_boundary_fill(ark_ctx *ctx, int axis) {
     ctx->parts_valid = false;
     if (axis < 1 || axis > 3) return fail(ARK_ERR_PARAM, "axis must be 1, 2 or 3");
     const int periodic = axis == 2 ? 0 : axis == 3 ? ctx->P.periodic_z : 0;
+    ctx->eng->boundary_fill(ctx->con ^ 1, axis, periodic);
+    return launch_status(ctx);
+}
+
+int ark_boundary_conditions(ark_ctx *ctx, int axis, int x1_period, int x2_period, int x3_period) {
+    (void)x1_period; // BoundaryConditions::alongX1 never reads it (source/BoundaryConditions.cpp:22-42)
+    if (int rc = check_ctx(ctx, true)) return rc;
+    ctx->parts_valid = false;
+    if (axis < 1 || axis > 3) return fail(ARK_ERR_PARAM, "axis must be 1, 2 or 3");
+    const int periodic = axis == 2 ? (x2_period != 0) : axis == 3 ? (x3_period != 0) : 0;
     ctx->eng->boundary_fill(ctx->con ^ 1, axis, periodic);
     return launch_status(ctx);
 }

@@ -59,6 +59,11 @@ __global__ void k_selftest_division(long long n, unsigned long long seed, const 
         // the fixed-point image, over the whole range and near ties (values of 2^-33 multiples)
         const double v1 = (t & 1) ? a : (double)(long long)(za >> 20) * 0x1p-33 * ((t & 2) ? -1.0 : 1.0);
         if (fixed32(v1) != fixed32_fp64(v1)) ++local;
+        // the FP32 path's image from the FP32 bits: every bit pattern (NaN, infinities and
+        // subnormals included) and values near ties, against the image of the widened value
+        const float f1 = (t & 8) ? __uint_as_float((unsigned)(za >> 32))
+                                 : (float)((double)(long long)(za >> 40) * 0x1p-33 * ((t & 16) ? -1.0 : 1.0));
+        if (fixed32(f1) != fixed32((double)f1)) ++local;
         const QCase &c = qc[t % nqc];
         if (t < nqc) {
             const QRecip d = make_qrecip(c.b);

@@ -301,18 +301,35 @@ __device__ __forceinline__ long long warp_sum_i64(long long v) {
     return v;
 }
 
-// Fixed-point image of an FP32 value for the FP32 path's bulk-flow sum: round(v * 2^16) in a
-// 32-bit integer (|v| < 2^15), NaN -> 0.  Integer sums are order independent, and nothing
-// here uses the FP64 pipe (1/64 of the FP32 rate on this part).
-__device__ __forceinline__ long long fixed16(float v) {
-    if (v != v) v = 0.f;
-    v = fminf(fmaxf(v, -32767.f), 32767.f);
-    return (long long)__float2int_rn(v * 65536.f);
+// Fixed-point image of an FP32 value for the FP32 path's bulk-flow sum: the same integer
+// round(v * 2^32) (ties to even, NaN -> 0, |v| clamped to 2^30) that fixed32 gives for the value
+// widened to FP64, taken from the FP32 bits with integer instructions only (the FP64 pipe runs
+// at 1/64 of the FP32 rate on this part): v = M 2^(e-150), so v 2^32 = M 2^(e-118), a left
+// shift for e >= 118 and a rounded right shift below.  Every |v| >= 2^-9 is represented
+// exactly, smaller ones to 2^-33.
+__device__ __forceinline__ long long fixed32(float v) {
+    const unsigned b = __float_as_uint(v);
+    const int e = (int)((b >> 23) & 0xFFu);
+    const unsigned M = (b & 0x7FFFFFu) | 0x800000u;
+    unsigned long long m;
+    if (e >= 157) { // |v| >= 2^30, infinities and NaN
+        if (e == 0xFF && (b & 0x7FFFFFu)) return 0;
+        m = 1ull << 62;
+    } else if (e >= 118) {
+        m = (unsigned long long)M << (e - 118);
+    } else if (e >= 118 - 25) { // shifts of 1..25: round to nearest, ties to even
+        const int k = 118 - e;
+        const unsigned q = M >> k, r = M & ((1u << k) - 1u), half = 1u << (k - 1);
+        m = q + ((r > half || (r == half && (q & 1u))) ? 1u : 0u);
+    } else {
+        m = 0; // below 2^-33: rounds to zero (zeros and subnormals included)
+    }
+    return (b >> 31) ? -(long long)m : (long long)m;
 }
 __device__ __forceinline__ long long fixed_sum_term(double v) { return fixed32(v); }
-__device__ __forceinline__ long long fixed_sum_term(float v) { return fixed16(v); }
+__device__ __forceinline__ long long fixed_sum_term(float v) { return fixed32(v); }
+// both precisions sum in units of 2^-32
 template <class T> struct FixedScale { static constexpr double inv = 1.0 / 4294967296.0; };
-template <> struct FixedScale<float> { static constexpr double inv = 1.0 / 65536.0; };
 
 // |v| as an order-preserving integer: FP64 bit pattern, or FP32 bit pattern (widened to an
 // FP64 bit pattern once per tile, see tile_store).

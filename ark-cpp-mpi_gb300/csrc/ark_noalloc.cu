@@ -8,19 +8,22 @@
 // pair per call would synchronize the device and can fail when the pool holds all memory.
 //
 // Scratch: one file-scope __device__ array of (kMaxBlocks + 1) x kCols 64-bit integers
-// (66,048 bytes), which every GPU that loads the library keeps until the process exits.
+// (65,600 bytes), which every GPU that loads the library keeps until the process exits.
 // Each block writes one row of partial sums; a second kernel adds the rows into the last
 // row.  Nothing in it has to start at zero: a call writes every row it reads.  All calls
 // share the array, so calls that overlap on the GPU (different streams or host threads at
 // the same time) race and must be serialized by the caller.
 //
-// The device address of the array is looked up with cudaGetSymbolAddress once per device,
-// on the first call made while that device is current; make that first call before any
-// stream capture on the device.
+// The device address of the array is looked up with cudaGetSymbolAddress once per device, on
+// the first call made while that device is current, and kept; make that first call before any
+// stream capture on the device.  A cudaDeviceReset of that device after the first call is not
+// supported: the module can load again at another address, which the kept one would miss.
+// Errors are reported through the status and ark_last_error(), like every other entry point.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 #include <mutex>
+#include <string>
 
 #include "../../include/ark_gpu.h"
 #include "ark_kernels.cuh"
@@ -34,10 +37,11 @@ constexpr int kCols = 8;                                            // 6 used: 5
 constexpr int kThreads = 256;
 
 static __device__ __align__(256) long long g_sums_scratch[(kMaxBlocks + 1) * kCols];
+static_assert(sizeof(g_sums_scratch) == 65600, "scratch size stated in ark_gpu.h");
 
+constexpr int kMaxDevices = 128;
 std::mutex g_mu;
-long long *g_scratch_addr[128];
-bool g_scratch_ready[128];
+long long *g_scratch_addr[kMaxDevices]; // the array's device address, per device once looked up
 
 // Per-block partial sums of the same fixed-point terms k_sums accumulates.
 __global__ void __launch_bounds__(kThreads)
@@ -94,41 +98,55 @@ __global__ void __launch_bounds__(kThreads) k_sums_total(long long *scratch, int
 
 } // namespace
 
+namespace {
+int cuda_fail(const char *what, cudaError_t e) {
+    return ark::api_fail(ARK_ERR_CUDA, std::string("ark_conservation_sums_noalloc: ") + what + ": " +
+                                           cudaGetErrorString(e));
+}
+} // namespace
+
 extern "C" int ark_conservation_sums_noalloc(const ark_params *p, const double *ro, const double *u1,
                                              const double *u2, const double *u3, const double *condition,
                                              ark_sums *out) {
-    if (!p || !ro || !u1 || !u2 || !u3 || !condition || !out) return ARK_ERR_PARAM;
-    if (p->n1_cells < 1 || p->n2_cells < 1 || p->n3_cells < 1) return ARK_ERR_PARAM;
+    if (!p || !ro || !u1 || !u2 || !u3 || !condition || !out)
+        return ark::api_fail(ARK_ERR_PARAM, "ark_conservation_sums_noalloc: NULL argument");
+    if (p->n1_cells < 1 || p->n2_cells < 1 || p->n3_cells < 1)
+        return ark::api_fail(ARK_ERR_PARAM, "ark_conservation_sums_noalloc: need at least one cell per axis");
     const long long n = (long long)p->n1_cells * p->n2_cells * p->n3_cells;
-    if (n > kMaxCells) return ARK_ERR_PARAM; // beyond the preallocated scratch (see header)
+    if (n > kMaxCells)
+        return ark::api_fail(ARK_ERR_PARAM, "ark_conservation_sums_noalloc: " + std::to_string(n) +
+                                                " interior cells exceed the static scratch's limit of 67,108,864");
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return ARK_ERR_CUDA;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
+    if (dev < 0 || dev >= kMaxDevices)
+        return ark::api_fail(ARK_ERR_UNSUPPORTED, "ark_conservation_sums_noalloc: device ordinal beyond 127");
     long long *scratch = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratch_ready[dev]) {
+        if (!g_scratch_addr[dev]) {
             void *addr = nullptr;
-            if (cudaGetSymbolAddress(&addr, g_sums_scratch) != cudaSuccess || !addr) return ARK_ERR_CUDA;
+            e = cudaGetSymbolAddress(&addr, g_sums_scratch);
+            if (e != cudaSuccess || !addr)
+                return cuda_fail("cudaGetSymbolAddress", e != cudaSuccess ? e : cudaErrorInvalidSymbol);
             g_scratch_addr[dev] = (long long *)addr;
-            g_scratch_ready[dev] = true;
         }
         scratch = g_scratch_addr[dev];
     }
-    ark::Geom g;
-    g.C1 = p->n1_cells;
-    g.C2 = p->n2_cells;
-    g.C3 = p->n3_cells;
-    g.cs1 = g.C1 + 2;
-    g.cs2 = (int64_t)(g.C1 + 2) * (g.C2 + 2);
-    g.fs1 = g.C1 + 3;
-    g.fs2 = (int64_t)(g.C1 + 3) * (g.C2 + 3);
-    const int rows = (int)((n + kCellsPerBlock - 1) / kCellsPerBlock);
-    k_sums_rows<<<rows, kThreads>>>(ro, u1, u2, u3, condition, g, n, scratch);
-    k_sums_total<<<1, kThreads>>>(scratch, rows);
-    if (cudaGetLastError() != cudaSuccess) return ARK_ERR_CUDA;
+    ark::Geom g = ark::host_geom(p->n1_cells, p->n2_cells, p->n3_cells);
+    int rows = (int)((n + kCellsPerBlock - 1) / kCellsPerBlock);
+    // launched through cudaLaunchKernel, whose return value is this launch's own error (an
+    // earlier error of the caller's stays where it is)
+    void *a1[] = {(void *)&ro, (void *)&u1, (void *)&u2, (void *)&u3, (void *)&condition, (void *)&g, (void *)&n,
+                  (void *)&scratch};
+    e = cudaLaunchKernel((const void *)k_sums_rows, dim3(rows), dim3(kThreads), a1, 0, 0);
+    if (e != cudaSuccess) return cuda_fail("row sums launch", e);
+    void *a2[] = {(void *)&scratch, (void *)&rows};
+    e = cudaLaunchKernel((const void *)k_sums_total, dim3(1), dim3(kThreads), a2, 0, 0);
+    if (e != cudaSuccess) return cuda_fail("total launch", e);
     long long v[6];
-    if (cudaMemcpy(v, scratch + (long long)kMaxBlocks * kCols, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return ARK_ERR_CUDA;
+    e = cudaMemcpy(v, scratch + (long long)kMaxBlocks * kCols, sizeof(v), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail("result copy", e);
     const double q = 1.0 / 4294967296.0;
     out->mass = (double)v[0] * q;
     out->momentum1 = (double)v[1] * q;

@@ -10,6 +10,7 @@
 #pragma once
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace ark {
@@ -345,6 +346,11 @@ inline RowShape row_shape(const Geom &dg, int face) {
     return r;
 }
 
+} // namespace ark
+
+namespace ark {
+// Records msg as the calling thread's ark_last_error() text and returns status (ark_api.cu).
+int api_fail(int status, const std::string &msg);
 } // namespace ark
 
 struct ark_closure_data;

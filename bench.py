@@ -10,8 +10,10 @@ step (main.cpp:82-91).  Metric: Mcell-steps/s = cells * steps / seconds.  The FP
 independent FP32 channels of mixed sizes (key "ensemble").  Synthetic data: the seeded channel state
 is the benchmark input (the reference has no dataset).
 
---impl reference times the reference's CPU step on the host cores instead: the compiled
-reference (oracle/_ref) where it exists, else its C restatement (oracle/), with all threads.
+--impl reference times the reference's CPU step on the host cores instead: its C restatement
+(oracle/ark_oracle.c, bit-identical to the reference on every pinned case), with all host
+threads.  The reference compiled in place (oracle/_ref) cannot stand in here: its sources are
+not part of this repository, so it exists only where the reference checkout does.
 
 Under torchrun (N > 1) every rank advances its own independent channel (replicas; the
 path has no exchange on one GPU per rank), timed between barriers; value = all ranks'
@@ -183,6 +185,14 @@ def max_over_ranks(dist, v):
     return float(t.item())
 
 
+SEED = 1000  # seed of the channel state of rank 0 (rank r: SEED + r), both arms
+
+
+def workload(C, re_b, precision):
+    """The workload string both arms report for a grid (identical for identical work)."""
+    return f"channel {C[0]}x{C[1]}x{C[2]} {precision.upper()} Re_b={re_b:g}, c=10, CFL 0.2, bulk forcing"
+
+
 def channel_params(arkgpu, C, re_b, precision):
     return arkgpu.make_params(*C, re_b=re_b, sound=10.0, rho0=1.0, cfl=0.2, precision=precision)
 
@@ -228,7 +238,7 @@ def roofline(kt, cells, word, peak, peak_kind, traffic_tab, prec_name):
     return r
 
 
-def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
+def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed, roundtrip=True):
     """Through the C ABI with host buffers, as a program replacing the reference's main loop
     uses it: upload the whole state from pinned host memory, then every step run ark_step and
     read the step's scalars back (dt, TIME, bulk velocity: a synchronous device->host read),
@@ -255,28 +265,52 @@ def e2e_leg(arkgpu, C, re_b, precision, steps, device, seed):
         ctx.download_struct(hs.struct(False))
         secs = time.perf_counter() - t0
         ctx.sync()
-        # per-step full-state round trip (the state kept on the host between steps)
-        h = hs.struct(False)
-        ctx.upload_struct(h)
-        ctx.step(1)
-        ctx.download_struct(h)
-        n_rt = max(3, steps // 10)
-        t1 = time.perf_counter()
-        for _ in range(n_rt):
-            ctx.upload_struct(h)
-            ctx.step(1)
-            ctx.download_struct(h)
-        rt_secs = time.perf_counter() - t1
+        rt = None
+        if roundtrip:
+            rt = full_state_roundtrip(ctx, hs, cells, steps)
     up = hs.nbytes(True)
     down = hs.nbytes(False)
     scal = 5 * 8  # the ark_scalars read every step
     hs.close()
-    return {"value": round(cells * steps / secs / 1e6, 3), "unit": UNIT,
-            "h2d_bytes_per_step": round(up / steps), "d2h_bytes_per_step": round(down / steps) + scal,
-            "steps": steps,
-            "note": "one job: state upload, steps each with a synchronous scalar read-back, state download",
-            "state_roundtrip_every_step": {"value": round(cells * n_rt / rt_secs / 1e6, 3), "unit": UNIT,
-                                           "h2d_bytes_per_step": down, "d2h_bytes_per_step": down, "steps": n_rt}}
+    out = {"value": round(cells * steps / secs / 1e6, 3), "unit": UNIT,
+           "h2d_bytes_per_step": round(up / steps), "d2h_bytes_per_step": round(down / steps) + scal,
+           "steps": steps, "precision": "fp64" if precision == arkgpu.FP64 else "fp32", "grid": list(C),
+           "note": "one job: state upload, steps each with a synchronous scalar read-back, state download"}
+    if rt is not None:
+        out["state_roundtrip_every_step"] = rt
+    return out
+
+
+def full_state_roundtrip(ctx, hs, cells, steps):
+    """The whole state uploaded, stepped once and downloaded, every step (a caller that keeps
+    the state on the host between steps)."""
+    h = hs.struct(False)
+    ctx.upload_struct(h)
+    ctx.step(1)
+    ctx.download_struct(h)
+    n_rt = max(3, steps // 10)
+    t1 = time.perf_counter()
+    for _ in range(n_rt):
+        ctx.upload_struct(h)
+        ctx.step(1)
+        ctx.download_struct(h)
+    rt_secs = time.perf_counter() - t1
+    down = hs.nbytes(False)
+    return {"value": round(cells * n_rt / rt_secs / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": down,
+            "d2h_bytes_per_step": down, "steps": n_rt}
+
+
+def fp32_error_report():
+    """The committed FP32-vs-FP64 error report of the 512x256x256 channel after 2000 steps
+    (ark-cpp-mpi_gb300/precision_report.py, profiles/fp32_error_512x256x256_2000_steps.json),
+    or None."""
+    path = os.path.join(ROOT, "profiles", "fp32_error_512x256x256_2000_steps.json")
+    if not os.path.isfile(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    return {"grid": d["grid"], "steps": d["steps"], "re_b": d["re_b"], **d["errors"],
+            "source": "profiles/fp32_error_512x256x256_2000_steps.json (precision_report.py on the GPU)"}
 
 
 ENSEMBLE_GRIDS = ((32, 32, 32), (64, 32, 32), (64, 48, 48), (96, 64, 64), (128, 64, 64))
@@ -322,13 +356,13 @@ def ensemble_leg(arkgpu, members, steps, warmup, device, seed=4242):
             "clocks": clocks}
 
 
-def cpu_leg(C, re_b, budget_s=12.0, max_steps=400, threads=None):
-    """The oracle's C restatement of the reference step on the host cores."""
+def cpu_sample(C, re_b, threads, budget_s, max_steps=400):
+    """Full steps of the oracle's C restatement of the reference step on `threads` host
+    threads, for about budget_s seconds: (Mcell-steps/s, steps, seconds)."""
     import oracle
 
     oracle.build(port=True, ref=False)
-    threads = threads or os.cpu_count() or 1
-    p = oracle.channel_params(*C, re_b=re_b, seed=7)
+    p = oracle.channel_params(*C, re_b=re_b, seed=SEED)
     o = oracle.Port(p, threads=threads)
     o.load(oracle.channel_state(p))
     o.run(1)  # warm-up
@@ -337,10 +371,18 @@ def cpu_leg(C, re_b, budget_s=12.0, max_steps=400, threads=None):
         o.run(1)
         n += 1
     secs = time.perf_counter() - t0
-    cells = C[0] * C[1] * C[2]
-    return {"value": round(cells * n / secs / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} full steps of the {C[0]}x{C[1]}x{C[2]} FP64 channel, {threads} OpenMP threads "
-                      f"({secs:.1f} s)"}
+    return C[0] * C[1] * C[2] * n / secs / 1e6, n, secs
+
+
+def cpu_leg(C, re_b, budget_s=12.0):
+    """The oracle's C restatement of the reference step on all host cores, and on one."""
+    threads = os.cpu_count() or 1
+    v, n, secs = cpu_sample(C, re_b, threads, budget_s)
+    v1, n1, secs1 = cpu_sample(C, re_b, 1, budget_s)
+    return {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} full steps of the {workload(C, re_b, 'fp64')}, {threads} OpenMP threads ({secs:.1f} s)",
+            "one_core": {"value": round(v1, 4), "unit": UNIT, "cores": 1,
+                         "sample": f"{n1} full steps, 1 thread ({secs1:.1f} s)"}}
 
 
 def reference_arm(args, world, rank, dist):
@@ -352,7 +394,7 @@ def reference_arm(args, world, rank, dist):
     oracle.build(port=True, ref=False)
     threads = os.cpu_count() or 1
     C = tuple(args.grid)
-    p = oracle.channel_params(*C, re_b=args.re, seed=7)
+    p = oracle.channel_params(*C, re_b=args.re, seed=SEED)
     o = oracle.Port(p, threads=threads)
     o.load(oracle.channel_state(p))
     tw = time.perf_counter()
@@ -369,8 +411,8 @@ def reference_arm(args, world, rank, dist):
             "steps": steps, "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded channel state)",
-            "config": {"workload": f"channel {C[0]}x{C[1]}x{C[2]} FP64 Re_b={args.re:g}, bulk forcing",
-                       "grid": list(C), "precision": "fp64", "parallelism": "host threads"},
+            "config": {"workload": workload(C, args.re, "fp64"), "grid": list(C), "precision": "fp64",
+                       "seed": SEED, "parallelism": "host threads"},
             "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{steps} full steps of the {C[0]}x{C[1]}x{C[2]} channel "
                                        f"({args.steps} asked), {threads} OpenMP threads"},
@@ -412,7 +454,7 @@ def main():
     traffic = ncu_traffic_per_cell()
 
     barrier(dist)
-    g = gpu_leg(arkgpu, C, args.re, arkgpu.FP64, args.steps, args.warmup, device, seed=1000 + rank)
+    g = gpu_leg(arkgpu, C, args.re, arkgpu.FP64, args.steps, args.warmup, device, seed=SEED + rank)
     barrier(dist)
     ms = max_over_ranks(dist, g["ms"])
     total_cells = g["cells"] * world
@@ -422,8 +464,8 @@ def main():
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded channel state)",
-            "config": {"workload": f"channel {C[0]}x{C[1]}x{C[2]} FP64 Re_b={args.re:g}, c=10, CFL 0.2, bulk forcing",
-                       "grid": list(C), "precision": "fp64", "parallelism": "replicas" if world > 1 else "single GPU",
+            "config": {"workload": workload(C, args.re, "fp64"), "grid": list(C), "precision": "fp64", "seed": SEED,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"inputs larger than L2: {g['cells'] * 8 * 41 / 1e9:.2f} GB of state streamed per step"},
             "clocks": g["clocks"], "kernel_shapes": g["shapes"],
             "gpu_launches": launches_per_step * args.steps}
@@ -449,7 +491,7 @@ def main():
                                           "peak": peak, "unit": "GB/s",
                                           "frac": round(f["cells"] * STEP_VALUES * 4 / f_step_s / 1e9 / peak, 4)},
                         "kernels_ms": {k: round(v, 4) for k, v in f["ktimes"]}, "clocks": f["clocks"],
-                        "kernel_shapes": f["shapes"]}
+                        "kernel_shapes": f["shapes"], "error": fp32_error_report()}
         line["gpu_launches"] += launches_per_step * f_steps
 
     if rank == 0 and args.ensemble > 0:
@@ -460,7 +502,10 @@ def main():
         line["gpu_launches"] += e["launches_per_step"] * args.ensemble_steps
 
     if rank == 0:
-        line["e2e"] = e2e_leg(arkgpu, C, args.re, arkgpu.FP64, args.e2e_steps, device, seed=5)
+        line["e2e"] = e2e_leg(arkgpu, C, args.re, arkgpu.FP64, args.e2e_steps, device, seed=SEED)
+        if "fp32" in line:
+            line["fp32"]["e2e"] = e2e_leg(arkgpu, tuple(args.fp32_grid), args.re, arkgpu.FP32, args.e2e_steps,
+                                          device, seed=77, roundtrip=False)
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_leg(C, args.re)
         print(json.dumps(line), flush=True)

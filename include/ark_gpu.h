@@ -149,9 +149,20 @@ int ark_use_forces(ark_ctx *ctx);
 int ark_phase2(ark_ctx *ctx);
 
 /* BoundaryConditions::alongX1/2/3 (source/BoundaryConditions.cpp:22-83) applied to the "nCon"
- * cell level on the device: axis 1 zero-gradient copy; axes 2 and 3 periodic copy when
- * that axis is periodic, else no-slip (u = 0, ro zero-gradient). */
+ * cell level on the device with the context's own periodicity: axis 1 zero-gradient copy;
+ * axis 2 no-slip (the channel's walls: u = 0, ro zero-gradient); axis 3 periodic copy when
+ * periodic_z, else no-slip. */
 int ark_boundary_fill(ark_ctx *ctx, int axis);
+
+/* BoundaryConditions(u1nCon, u2nCon, u3nCon, ronCon, tnCon, x1Period, x2Period, x3Period, n1,
+ * n2, n3, t0).alongX<axis>() (source/BoundaryConditions.cpp:7-83) with the periodicity given
+ * explicitly: on the interior of the other two axes, axis 1 copies the zero-gradient ghosts
+ * (x1_period is accepted and, as in the class, not read); axes 2 and 3 copy the periodic
+ * images when x2_period / x3_period, else set u = 0 and copy ro zero-gradient.  The passive
+ * temperature is not carried, so t0 and the class's periodic-x3 temperature line
+ * (BoundaryConditions.cpp:73, which copies ro into t) have no counterpart.  FP32 contexts copy
+ * their stored rho - ro0, which is the same copy. */
+int ark_boundary_conditions(ark_ctx *ctx, int axis, int x1_period, int x2_period, int x3_period);
 
 /* Sets / reads dt (used by the step pieces above). */
 int ark_set_dt(ark_ctx *ctx, double dt);
@@ -367,10 +378,11 @@ int ark_channel_init(const ark_params *params, uint64_t seed, double amp, ark_ho
  * point (their memory is held by a full grid or by another framework's pool, and a
  * cudaMalloc/cudaFree would synchronize the device or fail); it needs no ark_ctx.
  * Limit: at most 67,108,864 interior cells (larger grids return ARK_ERR_PARAM).  Scratch is
- * one static 66,048-byte device array per GPU, kept until exit and shared by all calls:
+ * one static 65,600-byte device array per GPU, kept until exit and shared by all calls:
  * calls that overlap on the GPU race.  Runs on the current device's legacy default stream
- * and waits for the result.  The first call on a device looks up the scratch address, so
- * make it before any stream capture. */
+ * and waits for the result.  The first call on a device looks up the scratch address and
+ * keeps it, so make that call before any stream capture; a cudaDeviceReset of the device
+ * after it is not supported.  Errors set ark_last_error(). */
 int ark_conservation_sums_noalloc(const ark_params *params, const double *ro, const double *u1,
                                   const double *u2, const double *u3, const double *condition,
                                   ark_sums *out);

@@ -28,7 +28,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libark_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libark_ref.so")
-REF_DIR_DEFAULT = "/root/reference"
+# The reference checkout: $REF_DIR, else a checkout named "reference" beside this repository.
+REF_DIR_DEFAULT = os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 CELL_NAMES = ("roCon", "u1Con", "u2Con", "u3Con", "ronCon", "u1nCon", "u2nCon", "u3nCon",
               "f1", "f2", "f3", "condition")
@@ -291,6 +292,7 @@ class Reference:
             L.ref_write_energy.argtypes = [ctypes.c_char_p]
             L.ref_average_len.restype = ctypes.c_size_t
             L.ref_get_average.argtypes = [ctypes.c_int, _dbl_p]
+            L.ref_boundary_conditions.argtypes = [ctypes.c_int] * 4 + [ctypes.c_double]
             cls._lib = L
         return cls._lib
 
@@ -382,6 +384,12 @@ class Reference:
     def last_g(self):
         return self.lib().ref_last_g()
 
+    def boundary_conditions(self, axis, x1_period, x2_period, x3_period, t0=1.0):
+        """BoundaryConditions(u1nCon, u2nCon, u3nCon, ronCon, tnCon, x1Period, x2Period, x3Period,
+        n1, n2, n3, t0).alongX<axis>() (source/BoundaryConditions.cpp:7-83)."""
+        assert self.lib().ref_boundary_conditions(int(axis), int(x1_period), int(x2_period), int(x3_period),
+                                                  float(t0)) == 0
+
     # the reference's writers and statistics (dir must end in '/')
     def write_paraview(self, dir_):
         assert self.lib().ref_write_paraview(dir_.encode()) == 0
@@ -399,6 +407,35 @@ class Reference:
         out = np.empty((self.p["C3"] + 2, self.p["C2"] + 3, self.p["C1"] + 2))
         assert self.lib().ref_get_average(int(m), _ptr(out)) == 0
         return out
+
+
+def boundary_conditions(level: dict, axis: int, x2_period: bool, x3_period: bool) -> dict:
+    """BoundaryConditions::alongX1/2/3 (source/BoundaryConditions.cpp:22-83) restated on a
+    level {"ronCon", "u1nCon", "u2nCon", "u3nCon"} of [k, j, i] arrays; returns new arrays.
+    On the interior of the other two axes: axis 1 copies the zero-gradient ghosts (the class
+    never reads x1Period); axes 2 and 3 copy the periodic images, or set u = 0 and copy rho
+    zero-gradient (no-slip).  The temperature lines are not restated (t is not carried)."""
+    out = {n: a.copy() for n, a in level.items()}
+    us = [out[n] for n in ("u1nCon", "u2nCon", "u3nCon")]
+    ro = out["ronCon"]
+    I, J, K = slice(1, -1), slice(1, -1), slice(1, -1)
+    if axis == 1:
+        for a in us + [ro]:
+            a[K, J, -1] = a[K, J, -2]
+            a[K, J, 0] = a[K, J, 1]
+    elif axis == 2:
+        for a in us:
+            a[K, -1, I] = a[K, 1, I] if x2_period else 0.0
+            a[K, 0, I] = a[K, -2, I] if x2_period else 0.0
+        ro[K, -1, I] = ro[K, 1, I] if x2_period else ro[K, -2, I]
+        ro[K, 0, I] = ro[K, -2, I] if x2_period else ro[K, 1, I]
+    else:
+        for a in us:
+            a[-1, J, I] = a[1, J, I] if x3_period else 0.0
+            a[0, J, I] = a[-2, J, I] if x3_period else 0.0
+        ro[-1, J, I] = ro[1, J, I] if x3_period else ro[-2, J, I]
+        ro[0, J, I] = ro[-2, J, I] if x3_period else ro[1, J, I]
+    return out
 
 
 # ---- writers and statistics, restated (numpy; host arrays in Arr3d layout [k, j, i]) ----

@@ -32,6 +32,7 @@
 #include <mpi.h>
 
 #include "Arr3d.h"
+#include "BoundaryConditions.h"
 
 /* ---- the reference's globals (defined in main.cpp through its headers) ---- */
 extern int l, n1, n2, n3, nStop, nPrint, nStep, n1_g, n2_g, n3_g;
@@ -292,6 +293,19 @@ double ref_get_time() { return TIME; }
 int ref_get_nstep() { return nStep; }
 double ref_last_ub() { return g_last_ub; }
 double ref_last_g() { return g_last_g; }
+
+/* The reference's BoundaryConditions class (source/BoundaryConditions.cpp:7-83), constructed
+ * on the "nCon" level (u1nCon, u2nCon, u3nCon, ronCon, tnCon) with the node counts n1, n2, n3
+ * and the given periodicity and t0, then alongX1/2/3 for axis 1/2/3. */
+int ref_boundary_conditions(int axis, int x1_period, int x2_period, int x3_period, double t0_bc) {
+    if (!g_ready || axis < 1 || axis > 3) return 1;
+    BoundaryConditions bc(u1nCon, u2nCon, u3nCon, ronCon, tnCon, x1_period != 0, x2_period != 0, x3_period != 0,
+                          n1, n2, n3, t0_bc);
+    if (axis == 1) bc.alongX1();
+    else if (axis == 2) bc.alongX2();
+    else bc.alongX3();
+    return 0;
+}
 
 /* nsteps full time steps in the order of main.cpp:80-91, plus the bulk forcing. */
 int ref_run(int nsteps) {

@@ -18,12 +18,17 @@ Files:
   stock_case.npz     the reference's own case, set up by its Input() and InitializeData()
                      (200x60x1 backward-facing step): the initial state and the interior
                      arrays after 40 steps
+  boundary.npz       the reference's BoundaryConditions class (alongX1/2/3) on the "nCon" level
+                     of a 9x6x5 grid with random values everywhere (ghosts included), for
+                     every combination of x2/x3 periodicity; the values are FP32-exact so
+                     FP32 contexts can be compared bit for bit too
   writers.npz        the files of the reference's writers (WriteDataParaView's out_5.vtk,
                      WriteAverageValues' average.vtk, WriteEnergy's energy.txt) and its
                      averageU arrays after 5 steps with AverageValues after each, for a 3-D
                      10x6x4 grid and a 2-D 9x5x1 grid
 
     python tests/golden/make_golden.py writers   # only writers.npz
+    python tests/golden/make_golden.py boundary  # only boundary.npz
 """
 from __future__ import annotations
 
@@ -101,11 +106,55 @@ def writers():
     np.savez_compressed(os.path.join(HERE, "writers.npz"), steps=5, **out)
 
 
+BOUNDARY_LEVEL = ("ronCon", "u1nCon", "u2nCon", "u3nCon")
+
+
+def boundary_state(p, seed):
+    """Random "nCon" cell arrays over every element (ghosts included), FP32-exact: u in
+    [-1, 1) rounded to FP32, rho = rho0 + an FP32 deviation below 1e-2 (exact in FP64, and
+    rho - rho0 is that FP32 value again)."""
+    shape = (p["C3"] + 2, p["C2"] + 2, p["C1"] + 2)
+    n = int(np.prod(shape))
+    out = {}
+    for q, name in enumerate(BOUNDARY_LEVEL):
+        r = (2.0 * oracle.uniform01(seed * 100 + q, n) - 1.0).reshape(shape)
+        if name == "ronCon":
+            out[name] = p["rho0"] + (0.01 * r).astype(np.float32).astype(np.float64)
+        else:
+            out[name] = r.astype(np.float32).astype(np.float64)
+    return out
+
+
+def boundary():
+    """Section 7: BoundaryConditions(u1nCon, u2nCon, u3nCon, ronCon, tnCon, x1Period, x2Period,
+    x3Period, n1, n2, n3, t0).alongX1/2/3 (source/BoundaryConditions.cpp:7-83), each axis from
+    the same start, for every combination of x2/x3 periodicity (x1Period, which the class never
+    reads, set equal to x2Period)."""
+    p = oracle.channel_params(9, 6, 5, seed=31)
+    st = boundary_state(p, 31)
+    out = {"params": json.dumps(p), "state_seed": 31}
+    for name in BOUNDARY_LEVEL:
+        out[f"state/{name}"] = st[name]
+    for x2p in (0, 1):
+        for x3p in (0, 1):
+            for axis in (1, 2, 3):
+                ref = oracle.Reference(p, forcing=False)
+                ref.load(st)
+                ref.boundary_conditions(axis, x2p, x2p, x3p)
+                for name in BOUNDARY_LEVEL:
+                    out[f"ax{axis}_p{x2p}{x3p}/{name}"] = ref.get(name)
+    np.savez_compressed(os.path.join(HERE, "boundary.npz"), **out)
+
+
 def main():
     assert oracle.Reference.available(), "build oracle/_ref first: make -C oracle ref"
     if sys.argv[1:] == ["writers"]:
         writers()
         print("writers.npz written to", HERE)
+        return
+    if sys.argv[1:] == ["boundary"]:
+        boundary()
+        print("boundary.npz written to", HERE)
         return
     out = {}
 
@@ -176,6 +225,9 @@ def main():
 
     # 6. the writers
     writers()
+
+    # 7. the BoundaryConditions class
+    boundary()
     print("golden fixtures written to", HERE)
 
 

@@ -215,3 +215,36 @@ def test_fixed_point_image_model_matches_the_fp64_form():
             c = min(max(v, -2.0 ** 30), 2.0 ** 30)
             want = int(np.rint(np.float64(c) * np.float64(2.0 ** 32)))  # exact scaling, ties to even
         assert fixed32_model(v) == want, v
+
+
+def fixed32f_model(f_bits):
+    """The device's fixed32 of an FP32 value, from its 32 bits: v = M 2^(e-150), so
+    v * 2^32 = M 2^(e-118), shifted left or rounded right to nearest even; clamp at 2^30."""
+    e = (f_bits >> 23) & 0xFF
+    M = (f_bits & 0x7FFFFF) | 0x800000
+    if e >= 157:
+        if e == 0xFF and (f_bits & 0x7FFFFF):
+            return 0
+        m = 1 << 62
+    elif e >= 118:
+        m = M << (e - 118)
+    elif e >= 118 - 25:
+        k = 118 - e
+        q, r, half = M >> k, M & ((1 << k) - 1), 1 << (k - 1)
+        m = q + (1 if (r > half or (r == half and (q & 1))) else 0)
+    else:
+        m = 0
+    return -m if f_bits >> 31 else m
+
+
+def test_fp32_fixed_point_image_equals_the_image_of_the_widened_value():
+    """The FP32 path's bulk-flow term taken from the FP32 bits is the FP64 path's image of the
+    same value widened to FP64: every exponent, ties, subnormals, infinities and NaN."""
+    rng = random.Random(23)
+    pats = [0, 0x80000000, 0x7F800000, 0xFF800000, 0x7FC00000, 0x00000001, 0x807FFFFF, 0x4E800000, 0x4E7FFFFF,
+            0x2F000000, 0x2F400000, 0x2E800000, 0x2EC00000]
+    pats += [rng.getrandbits(32) for _ in range(40000)]
+    pats += [e << 23 | rng.getrandbits(23) | (rng.getrandbits(1) << 31) for e in range(85, 130) for _ in range(200)]
+    for fb in pats:
+        v = float(np.frombuffer(struct.pack("<I", fb), dtype=np.float32)[0])
+        assert fixed32f_model(fb) == fixed32_model(v), hex(fb)

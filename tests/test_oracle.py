@@ -142,6 +142,45 @@ def test_port_matches_live_reference(port):
         assert bits_equal(port.interior(n, r.get(n)), port.interior(n, o.get(n))), n
 
 
+def _boundary_cases():
+    for x2p in (0, 1):
+        for x3p in (0, 1):
+            for axis in (1, 2, 3):
+                yield axis, x2p, x3p
+
+
+def test_boundary_conditions_restated_match_reference_class(port):
+    """The numpy restatement of BoundaryConditions::alongX1/2/3 against the reference class's
+    own outputs (tests/golden/boundary.npz): every element of every array, ghosts included,
+    for each axis and each x2/x3 periodicity."""
+    g = np.load(os.path.join(GOLD, "boundary.npz"))
+    level = {n[6:]: g[n] for n in g.files if n.startswith("state/")}
+    assert sorted(level) == ["ronCon", "u1nCon", "u2nCon", "u3nCon"]
+    for axis, x2p, x3p in _boundary_cases():
+        got = port.boundary_conditions(level, axis, bool(x2p), bool(x3p))
+        for n in level:
+            assert bits_equal(got[n], g[f"ax{axis}_p{x2p}{x3p}/{n}"]), (axis, x2p, x3p, n)
+
+
+def test_boundary_conditions_live_reference(port):
+    """Where the reference sources exist: the class on a fresh random level of another grid
+    against the restatement."""
+    port.build(port=False)
+    if not port.Reference.available():
+        pytest.skip("reference sources not present on this machine")
+    from make_golden import boundary_state
+
+    p = port.channel_params(6, 9, 4, seed=5)
+    level = boundary_state(p, 5)
+    for axis, x2p, x3p in _boundary_cases():
+        r = port.Reference(p, forcing=False)
+        r.load(level)
+        r.boundary_conditions(axis, 1 - x2p, x2p, x3p)
+        want = port.boundary_conditions(level, axis, bool(x2p), bool(x3p))
+        for n in level:
+            assert bits_equal(r.get(n), want[n]), (axis, x2p, x3p, n)
+
+
 def test_channel_init_matches_library(port, ark):
     """The numpy channel init (oracle side) and ark_channel_init (library side) agree."""
     p = ark.make_params(9, 6, 5)
