@@ -14,7 +14,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libark_gb300.so")
+# ARK_GPU_LIB selects another build of the library (the bounds-checked one in lib_check/)
+LIB_PATH = os.environ.get("ARK_GPU_LIB") or os.path.join(HERE, "lib", "libark_gb300.so")
 
 FP64, FP32 = 0, 1
 
@@ -41,7 +42,10 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_closure_data_clear", "ark_closure_data_get", "ark_closure_data_append", "ark_closure_sample",
            "ark_mlp_create", "ark_mlp_destroy", "ark_mlp_set", "ark_mlp_get", "ark_mlp_fit_normalization",
            "ark_mlp_gradient", "ark_mlp_train", "ark_mlp_predict", "ark_set_closure",
-           "ark_closure_data_filtered_stats", "ark_plane_stats", "ark_autotune", "ark_mlp_predict_tc")
+           "ark_closure_data_filtered_stats", "ark_plane_stats", "ark_autotune", "ark_mlp_predict_tc",
+           "ark_slabs_create", "ark_slabs_destroy", "ark_slabs_count", "ark_slabs_upload", "ark_slabs_download",
+           "ark_slabs_step", "ark_slabs_sync", "ark_slabs_time_steps", "ark_slabs_get_scalars",
+           "ark_slabs_conservation_sums", "ark_slab_plan", "ark_slab_halo_planes", "ark_bounds_check")
 
 
 VTK_LAYOUTS = {"full": 0, "reference": 1}
@@ -165,6 +169,19 @@ def lib():
         L.ark_closure_data_filtered_stats.argtypes = [vp, _DP]
         L.ark_plane_stats.argtypes = [vp, _DP]
         L.ark_autotune.argtypes = [vp, ctypes.c_int, ip]
+        L.ark_slabs_create.restype = vp
+        L.ark_slabs_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
+        for fn in ("ark_slabs_destroy", "ark_slabs_sync", "ark_slabs_count"):
+            getattr(L, fn).argtypes = [vp]
+        L.ark_slabs_upload.argtypes = [vp, ctypes.POINTER(HostState)]
+        L.ark_slabs_download.argtypes = [vp, ctypes.POINTER(HostState)]
+        L.ark_slabs_step.argtypes = [vp, ctypes.c_int]
+        L.ark_slabs_time_steps.argtypes = [vp, ctypes.c_int, _DP]
+        L.ark_slabs_get_scalars.argtypes = [vp, ctypes.POINTER(Scalars)]
+        L.ark_slabs_conservation_sums.argtypes = [vp, ctypes.POINTER(Sums)]
+        L.ark_slab_plan.argtypes = [ctypes.c_int] * 4 + [ip] * 4
+        L.ark_bounds_check.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+        L.ark_slab_halo_planes.argtypes = [ctypes.c_int] * 5 + [ip] * 2
         L.ark_ensemble_create.restype = vp
         L.ark_ensemble_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ip]
         L.ark_ensemble_last_error.restype = ctypes.c_char_p
@@ -445,6 +462,97 @@ class Context:
         out = np.empty((self.p.n3_cells, self.p.n2_cells, self.p.n1_cells, 3))
         self._call("ark_vorticity", out.ctypes.data_as(_DP))
         return out
+
+
+def slab_plan(n3_cells, nslabs, slab, periodic_z=True):
+    """(k_first, k_last, below, above) of one slab of a z split (host only)."""
+    v = [ctypes.c_int(0) for _ in range(4)]
+    rc = lib().ark_slab_plan(int(n3_cells), int(nslabs), int(slab), int(periodic_z), *[ctypes.byref(x) for x in v])
+    if rc != 0:
+        raise ArkError("ark_slab_plan", rc, lib().ark_last_error().decode())
+    return tuple(x.value for x in v)
+
+
+def slab_halo_planes(face, side, c3, c3_src, bounded):
+    """(ghost plane written, source plane read) of one side of a slab's z halo (host only)."""
+    d, s_ = ctypes.c_int(0), ctypes.c_int(0)
+    rc = lib().ark_slab_halo_planes(int(face), int(side), int(c3), int(c3_src), int(bounded), ctypes.byref(d),
+                                    ctypes.byref(s_))
+    if rc != 0:
+        raise ArkError("ark_slab_halo_planes", rc, lib().ark_last_error().decode())
+    return d.value, s_.value
+
+
+def bounds_check(reset=False):
+    """Bounds-checked builds (ARK_GPU_LIB=.../lib_check/libark_gb300.so): (violations, first
+    value, its bound, source line) recorded by the kernels so far; ArkError elsewhere."""
+    out = (ctypes.c_longlong * 4)()
+    rc = lib().ark_bounds_check(int(reset), out)
+    if rc != 0:
+        raise ArkError("ark_bounds_check", rc, lib().ark_last_error().decode())
+    return tuple(int(x) for x in out)
+
+
+class Slabs:
+    """An ark_slabs group: one channel split along z into nslabs slab contexts on one device,
+    with the z halo exchanges and shared reductions; host states are whole-domain."""
+
+    def __init__(self, params: Params, nslabs: int):
+        L = lib()
+        self.params = params
+        rc = ctypes.c_int(0)
+        self.h = L.ark_slabs_create(ctypes.byref(params), int(nslabs), ctypes.byref(rc))
+        if not self.h:
+            raise ArkError("ark_slabs_create", rc.value or 2, L.ark_last_error().decode())
+
+    def _call(self, fn, *args):
+        rc = getattr(lib(), fn)(self.h, *args)
+        if rc != 0:
+            raise ArkError(fn, rc, lib().ark_last_error().decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ark_slabs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, st: dict):
+        self._call("ark_slabs_upload", ctypes.byref(host_struct(st)))
+
+    def download(self, names=STATE_FIELDS) -> dict:
+        cs, fs = shapes(self.params)
+        st = {n: np.empty(cs if n in CELL_FIELDS else fs) for n in names}
+        self._call("ark_slabs_download", ctypes.byref(host_struct(st)))
+        return st
+
+    def step(self, n=1):
+        self._call("ark_slabs_step", int(n))
+
+    def sync(self):
+        self._call("ark_slabs_sync")
+
+    def time_steps(self, n):
+        ms = ctypes.c_double(0.0)
+        self._call("ark_slabs_time_steps", int(n), ctypes.byref(ms))
+        return ms.value
+
+    def scalars(self) -> Scalars:
+        s = Scalars()
+        self._call("ark_slabs_get_scalars", ctypes.byref(s))
+        return s
+
+    def sums(self) -> Sums:
+        s = Sums()
+        self._call("ark_slabs_conservation_sums", ctypes.byref(s))
+        return s
 
 
 class Ensemble:

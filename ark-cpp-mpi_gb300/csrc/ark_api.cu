@@ -14,7 +14,8 @@
 #include <vector>
 
 #include "../../include/ark_gpu.h"
-#include "ark_state.h"
+#include "ark_check.cuh"
+#include "ark_ctx.h"
 
 using namespace ark;
 
@@ -117,6 +118,7 @@ Consts make_consts(const ark_params &p) {
     k.forcing = p.forcing;
     k.periodic_x = p.periodic_x != 0;
     k.periodic_z = p.periodic_z != 0;
+    k.ext_z = 0;
     fill_kt(k, k.kd);
     fill_kt(k, k.kf);
     return k;
@@ -127,80 +129,42 @@ const char *const kStepKernels[] = {"finalize_dt", "wrap_con", "phase1_stress_fo
                                     "sweep_x1",    "sweep_x2", "sweep_x3",             "phase1_forces"};
 constexpr int kNumStepKernels = 8;
 
-// Precision-independent engine interface.
-struct Engine {
-    virtual ~Engine() {}
-    virtual int alloc() = 0;
-    virtual int upload_field(int which, int face, const double *host) = 0;
-    virtual int download_field(int which, int face, double *host) = 0;
-    virtual void *field_ptr(const char *name, int *face) = 0;
-    virtual int download_raw(void *p, int face, double *host) = 0;
-    virtual int upload_raw(void *p, int face, const double *host) = 0;
-    virtual void time_step_size(int con, int advance) = 0;
-    virtual void reduce(int con) = 0;
-    virtual void phase1(int src, int dst, int fcur, int mode) = 0;
-    virtual void stress(int con, int bulk) = 0;
-    virtual void use_forces(int ncon) = 0;
-    virtual void phase2(int con, int fcur) = 0;
-    virtual void step(int con, int fcur, cudaEvent_t *ev) = 0;
-    virtual void boundary_fill(int ncon, int axis, int periodic) = 0;
-    virtual void sums(int ncon) = 0;
-    virtual void mean_profile(int ncon, long long *acc) = 0;
-    virtual void pack(int ncon, int fcur, const CellPack &a) = 0;
-    virtual int alloc_nut() = 0;
-    virtual void plane_stats(int ncon, double *out) = 0;
-    virtual void gather(int lvl, double *u0, double *u1, double *u2) = 0;
-    virtual void average_add(int ncon) = 0;
-    virtual void energy(int ncon, double *scratch, double *out) = 0;
-    virtual DevScalars *scalars() = 0;
-    virtual uint8_t *flags() = 0;
-    // launches of one step in the current configuration, and their names
-    virtual int step_launches() = 0;
-    virtual const char *step_kernel_name(int q) = 0;
-    // after each step: the level the step wrote into the spare takes the place of "nCon"
-    virtual void after_step(int con) = 0;
-    // identity of the cell-level buffers (0, 1: the two levels, 2: the spare), for graph reuse
-    virtual const void *level_ptr(int l) = 0;
-};
-
 } // namespace
 
 namespace ark {
 // Run constants of a parameter set (shared with the ensemble code).
 Consts make_run_consts(const ark_params &p) { return make_consts(p); }
 int api_fail(int status, const std::string &msg) { return fail(status, msg); }
+
+// The bounds-check records of the translation units built with -DARK_CHECK (none otherwise).
+static std::vector<CheckReader> &check_readers() {
+    static std::vector<CheckReader> r;
+    return r;
+}
+int check_register(CheckReader reader) {
+    check_readers().push_back(reader);
+    return (int)check_readers().size();
+}
 } // namespace ark
 
-struct ark_ctx {
-    ark_params P;
-    Geom g;
-    Consts k;
-    cudaStream_t st = nullptr;
-    std::unique_ptr<Engine> eng;
-    std::vector<double> cond_host;
-    int con = 0;  // the cell level holding "Con"
-    int fcur = 0; // the current face generation
-    bool uploaded = false;
-    bool parts_valid = false; // the dt / bulk-flow partials describe the current state
-    int march[2] = {1, 0};    // Phase1 kernel shape of the two Phase1 launches of a step
-    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [con][fcur]
-    const void *graph_levels[2][2][3] = {};  // the level buffers each graph was captured with
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    double *stage = nullptr; // contiguous double staging for host transfers
-    AvgArrays avg = {{nullptr, nullptr, nullptr}}; // averageU1..3 (FP64, reference layout)
-    bool averaging = false;  // AverageValues at the end of every step
-    void *closure_net = nullptr;          // learned closure: the network's constants (device copy)
-    cudaStream_t side = nullptr;          // the closure's branch of the step
-    cudaEvent_t fork = nullptr, join = nullptr;
-    float closure_scale = 0.f;            // u_tau / vis for the y+ feature
-    int seg_target = 32;                  // x2/x3 sweep segment length (faces)
-    int p2mode = 0; // Phase2: 0 three sweep kernels, 1 one kernel for the three sweeps, 2 (FP32)
-                    // one kernel for the three sweeps and the second Phase1
-    // output streaming: two device and two pinned host slab buffers of io_cap doubles
-    double *io_dev[2] = {nullptr, nullptr};
-    double *io_host[2] = {nullptr, nullptr};
-    size_t io_cap = 0;
-};
+extern "C" int ark_bounds_check(int reset, long long *out) {
+    if (!out) return fail(ARK_ERR_PARAM, "out is NULL");
+    if (ark::check_readers().empty())
+        return fail(ARK_ERR_UNSUPPORTED, "not a bounds-checked build (compile with -DARK_CHECK)");
+    out[0] = out[1] = out[2] = out[3] = 0;
+    if (cudaError_t e = cudaDeviceSynchronize()) return fail(ARK_ERR_CUDA, std::string("ark_bounds_check: ") + cudaGetErrorString(e));
+    for (ark::CheckReader r : ark::check_readers()) {
+        ark::CheckRecord c;
+        if (r(&c, reset)) return fail(ARK_ERR_CUDA, "could not read a bounds-check record");
+        if (c.hits && !out[0]) {
+            out[1] = c.value;
+            out[2] = c.bound;
+            out[3] = c.line;
+        }
+        out[0] += (long long)c.hits;
+    }
+    return ARK_OK;
+}
 
 namespace {
 
@@ -456,6 +420,64 @@ template <class T> struct EngineT : Engine {
         if (use_step2()) std::swap(S.lv[con ^ 1], S.spare);
     }
     const void *level_ptr(int l) override { return l < 2 ? (const void *)S.lv[l].ro : (const void *)S.spare.ro; }
+
+    void set_consts(const Consts &k) override { S.k = k; }
+    void share_scalars(DevScalars *sc, unsigned long long *part_max, long long *part_sum) override {
+        S.sc = sc;
+        S.part_max = part_max;
+        S.part_sum = part_sum;
+    }
+    void reduce_into(int con) override { Launch<T>::reduce_start(S, con, ctx->st); }
+    // the launches of step() in the same order, cut where a slab group exchanges halos
+    void stage(int q, int x, int fcur) override {
+        const int y = x ^ 1;
+        cudaStream_t st = ctx->st;
+        switch (q) {
+        case 0: Launch<T>::finalize_dt(S, 1, st); break;
+        case 1: Launch<T>::wrap_con(S, y, 1, st); break;
+        case 2:
+            Launch<T>::phase1(S, y, x, fcur, P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0),
+                              ctx->march[0], st);
+            break;
+        case 3: Launch<T>::wrap_phase2(S, y, fcur, st); break;
+        default:
+            for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target);
+            Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
+            break;
+        }
+    }
+    int halo_arrays(int exchange, int x, int fcur, void **ptrs, int *face) override {
+        const int y = x ^ 1;
+        int n = 0;
+        auto add = [&](T *a, int f) {
+            if (!a) return; // FP32 contexts keep no face density
+            ptrs[n] = a;
+            face[n] = f;
+            ++n;
+        };
+        if (exchange == 0) { // wrap_con(y, with_ro = 1) along z
+            const Level<T> &L = S.lv[y];
+            add(L.u1, 0);
+            add(L.u2, 0);
+            add(L.u3, 0);
+            add(L.ro, 0);
+        } else { // wrap_phase2(y) along z
+            const Level<T> &Ln = S.lv[x], &Lc = S.lv[y];
+            add(Ln.u1, 0);
+            add(Ln.u2, 0);
+            add(Ln.u3, 0);
+            add(Ln.ro, 0);
+            add(Lc.ro, 0);
+            const FaceSet<T> &Z = S.fc[fcur][2];
+            add(Z.p, 1);
+            add(Z.u[0], 1);
+            add(Z.u[1], 1);
+            add(Z.u[2], 1);
+            add(Z.ro, 1);
+        }
+        return n;
+    }
+    void halo_exchange(const HaloJob *jobs, int njobs) override { Launch<T>::halo_exchange(S.g, jobs, njobs, ctx->st); }
 };
 
 int check_params(const ark_params *p) {

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/ark_gpu.h"
+#include "ark_check.cuh"
 #include "ark_state.h"
 
 namespace ark {
@@ -679,7 +680,8 @@ template <class T> __global__ void __launch_bounds__(128)
         // the interior cell whose value this position takes (periodic image, else nearest)
         const int i = ig == 0 ? (S.k.periodic_x ? g.C1 : 1) : (ig == g.C1 + 1 ? (S.k.periodic_x ? 1 : g.C1) : ig);
         const int k = kg == 0 ? (S.k.periodic_z ? g.C3 : 1) : (kg == g.C3 + 1 ? (S.k.periodic_z ? 1 : g.C3) : kg);
-        const int64_t c = g.cell(i, j, k);
+        const int64_t ncell = g.ncell();
+        const int64_t c = ARK_CK(g.cell(i, j, k), ncell);
         const bool fluid = (S.flags[c] & FL_EQ0) != 0;
         float f[NIN];
         {
@@ -688,7 +690,9 @@ template <class T> __global__ void __launch_bounds__(128)
             // level's ghost cells are not needed: this runs beside the step's ghost fill
             const int im = i > 1 ? i - 1 : (S.k.periodic_x ? g.C1 : 1), ip = i < g.C1 ? i + 1 : (S.k.periodic_x ? 1 : g.C1);
             const int km = k > 1 ? k - 1 : (S.k.periodic_z ? g.C3 : 1), kp = k < g.C3 ? k + 1 : (S.k.periodic_z ? 1 : g.C3);
-            const int64_t nb[6] = {g.cell(im, j, k), g.cell(ip, j, k), c - g.cs1, c + g.cs1, g.cell(i, j, km), g.cell(i, j, kp)};
+            int64_t nb[6] = {g.cell(im, j, k), g.cell(ip, j, k), c - g.cs1, c + g.cs1, g.cell(i, j, km), g.cell(i, j, kp)};
+#pragma unroll
+            for (int q = 0; q < 6; ++q) nb[q] = ARK_CK(nb[q], ncell);
             const T *u[3] = {L.u1, L.u2, L.u3};
             bool solid[6];
 #pragma unroll
@@ -709,7 +713,7 @@ template <class T> __global__ void __launch_bounds__(128)
             for (int q = 0; q < NIN; ++q) f[q] = (f[q] - net.mu[q]) * net.rsd[q];
         }
         const float y_nu = tc_warp(w, B, X[wid], f, lane);
-        if (live) S.nut[g.cell(ig, j, kg)] = fluid ? (T)(y_nu * K.vis) : (T)0;
+        if (live) S.nut[ARK_CK(g.cell(ig, j, kg), ncell)] = fluid ? (T)(y_nu * K.vis) : (T)0;
     }
 }
 

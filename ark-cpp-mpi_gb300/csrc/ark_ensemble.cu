@@ -68,6 +68,8 @@ __device__ __forceinline__ int find_member(const WorkList &W, int b) {
 }
 
 __device__ __forceinline__ BIx decode(const WorkList &W, int q, int b) {
+    // bounds-checked builds: the member found owns block b
+    if (!ARK_CK_IN(q, 0, W.n - 1) || !ARK_CK_IN(b, W.info[q].x, (q + 1 < W.n ? W.info[q + 1].x : W.total) - 1)) q = 0;
     const int4 f = W.info[q];
     const int local = b - f.x;
     BIx bx;

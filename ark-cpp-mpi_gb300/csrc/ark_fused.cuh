@@ -215,7 +215,9 @@ __global__ void __launch_bounds__(NT, 2)
     const T dt = sc_dt<T>(S.sc);
     const SweepK<T> qx = sweep_consts(S, 0), qy = sweep_consts(S, 1), qz = sweep_consts(S, 2);
     const Level<T> Ln = S.lv[con ^ 1];
-    const NCell<T> NCX = {Ln.u1, Ln.u2, Ln.u3, Ln.ro}, NCY = {Ln.u2, Ln.u1, Ln.u3, Ln.ro}, NCZ = {Ln.u3, Ln.u1, Ln.u2, Ln.ro};
+    const int nc_ = (int)g.ncell();
+    const NCell<T> NCX = {Ln.u1, Ln.u2, Ln.u3, Ln.ro, nc_}, NCY = {Ln.u2, Ln.u1, Ln.u3, Ln.ro, nc_},
+                   NCZ = {Ln.u3, Ln.u1, Ln.u2, Ln.ro, nc_};
     const FaceOut<T> WX = sweep_out(S, fcur, 0), WY = sweep_out(S, fcur, 1), WZ = sweep_out(S, fcur, 2);
     const FaceSet<T> FZ = S.fc[fcur][2];
     const bool bounded_x = !S.k.periodic_x;

@@ -25,6 +25,7 @@
 
 #include <type_traits>
 
+#include "ark_check.cuh"
 #include "ark_state.h"
 
 namespace ark {
@@ -402,7 +403,7 @@ template <class T> __device__ __forceinline__ void reduce_start_body(const DevSt
     const uint8_t *__restrict__ fl = S.flags;
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long s = 0;
-    if (i <= g.C1 && j <= g.C2) {
+    if (i <= g.C1 && j <= g.C2 && ARK_CK_IN(k0, 1, g.C3)) {
         const int cs2 = (int)g.cs2;
         int c = g.ci(i, j, k0);
 #pragma unroll 4
@@ -534,27 +535,29 @@ __host__ __device__ inline int wrap_lines(const Geom &g) { return g.C2 * g.C3 + 
 // The two ghosts of line L of array q.
 template <class T> __device__ __forceinline__ void wrap_copy(const Geom &g, const WrapJob &J, int q, const WrapLine &L) {
     T *a = (T *)J.a[q];
+    const int64_t n = J.face[q] ? g.nface() : g.ncell();
+    auto cp = [&](int64_t dst, int64_t src) { a[ARK_CK(dst, n)] = a[ARK_CK(src, n)]; };
     if (!L.z) {
         const uint8_t m = J.mode[q][0];
         if (m == GH_NONE) return;
         const int j = L.a, k = L.b;
         if (J.face[q]) {
-            a[g.face(0, j, k)] = a[g.face(m == GH_WRAP ? g.C1 : 1, j, k)];
-            a[g.face(g.C1 + 2, j, k)] = a[g.face(m == GH_WRAP ? 2 : g.C1 + 1, j, k)];
+            cp(g.face(0, j, k), g.face(m == GH_WRAP ? g.C1 : 1, j, k));
+            cp(g.face(g.C1 + 2, j, k), g.face(m == GH_WRAP ? 2 : g.C1 + 1, j, k));
         } else {
-            a[g.cell(0, j, k)] = a[g.cell(m == GH_WRAP ? g.C1 : 1, j, k)];
-            a[g.cell(g.C1 + 1, j, k)] = a[g.cell(m == GH_WRAP ? 1 : g.C1, j, k)];
+            cp(g.cell(0, j, k), g.cell(m == GH_WRAP ? g.C1 : 1, j, k));
+            cp(g.cell(g.C1 + 1, j, k), g.cell(m == GH_WRAP ? 1 : g.C1, j, k));
         }
     } else {
         const uint8_t m = J.mode[q][1];
         if (m == GH_NONE) return;
         const int i = L.a, j = L.b;
         if (J.face[q]) {
-            a[g.face(i, j, 0)] = a[g.face(i, j, m == GH_WRAP ? g.C3 : 1)];
-            a[g.face(i, j, g.C3 + 2)] = a[g.face(i, j, m == GH_WRAP ? 2 : g.C3 + 1)];
+            cp(g.face(i, j, 0), g.face(i, j, m == GH_WRAP ? g.C3 : 1));
+            cp(g.face(i, j, g.C3 + 2), g.face(i, j, m == GH_WRAP ? 2 : g.C3 + 1));
         } else {
-            a[g.cell(i, j, 0)] = a[g.cell(i, j, m == GH_WRAP ? g.C3 : 1)];
-            a[g.cell(i, j, g.C3 + 1)] = a[g.cell(i, j, m == GH_WRAP ? 1 : g.C3)];
+            cp(g.cell(i, j, 0), g.cell(i, j, m == GH_WRAP ? g.C3 : 1));
+            cp(g.cell(i, j, g.C3 + 1), g.cell(i, j, m == GH_WRAP ? 1 : g.C3));
         }
     }
 }
@@ -580,33 +583,35 @@ template <class T> __global__ void k_wrap(Geom g, const __grid_constant__ WrapJo
 template <class T> __global__ void k_boundary_fill(Geom g, Level<T> L, int axis, int periodic) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     T *a[4] = {L.u1, L.u2, L.u3, L.ro};
+    const int64_t n = g.ncell();
+    auto at = [&](int q, int64_t c) -> T & { return a[q][ARK_CK(c, n)]; };
     if (axis == 1) {
         if (t >= (int64_t)g.C2 * g.C3) return;
         const int j = (int)(t % g.C2) + 1, k = (int)(t / g.C2) + 1;
         for (int q = 0; q < 4; ++q) {
-            a[q][g.cell(g.C1 + 1, j, k)] = a[q][g.cell(g.C1, j, k)];
-            a[q][g.cell(0, j, k)] = a[q][g.cell(1, j, k)];
+            at(q, g.cell(g.C1 + 1, j, k)) = at(q, g.cell(g.C1, j, k));
+            at(q, g.cell(0, j, k)) = at(q, g.cell(1, j, k));
         }
     } else if (axis == 2) {
         if (t >= (int64_t)g.C1 * g.C3) return;
         const int i = (int)(t % g.C1) + 1, k = (int)(t / g.C1) + 1;
         const int64_t top = g.cell(i, g.C2 + 1, k), bot = g.cell(i, 0, k);
         for (int q = 0; q < 3; ++q) {
-            a[q][top] = periodic ? a[q][g.cell(i, 1, k)] : (T)0;
-            a[q][bot] = periodic ? a[q][g.cell(i, g.C2, k)] : (T)0;
+            at(q, top) = periodic ? at(q, g.cell(i, 1, k)) : (T)0;
+            at(q, bot) = periodic ? at(q, g.cell(i, g.C2, k)) : (T)0;
         }
-        a[3][top] = periodic ? a[3][g.cell(i, 1, k)] : a[3][g.cell(i, g.C2, k)];
-        a[3][bot] = periodic ? a[3][g.cell(i, g.C2, k)] : a[3][g.cell(i, 1, k)];
+        at(3, top) = periodic ? at(3, g.cell(i, 1, k)) : at(3, g.cell(i, g.C2, k));
+        at(3, bot) = periodic ? at(3, g.cell(i, g.C2, k)) : at(3, g.cell(i, 1, k));
     } else {
         if (t >= (int64_t)g.C1 * g.C2) return;
         const int i = (int)(t % g.C1) + 1, j = (int)(t / g.C1) + 1;
         const int64_t top = g.cell(i, j, g.C3 + 1), bot = g.cell(i, j, 0);
         for (int q = 0; q < 3; ++q) {
-            a[q][top] = periodic ? a[q][g.cell(i, j, 1)] : (T)0;
-            a[q][bot] = periodic ? a[q][g.cell(i, j, g.C3)] : (T)0;
+            at(q, top) = periodic ? at(q, g.cell(i, j, 1)) : (T)0;
+            at(q, bot) = periodic ? at(q, g.cell(i, j, g.C3)) : (T)0;
         }
-        a[3][top] = periodic ? a[3][g.cell(i, j, 1)] : a[3][g.cell(i, j, g.C3)];
-        a[3][bot] = periodic ? a[3][g.cell(i, j, g.C3)] : a[3][g.cell(i, j, 1)];
+        at(3, top) = periodic ? at(3, g.cell(i, j, 1)) : at(3, g.cell(i, j, g.C3));
+        at(3, bot) = periodic ? at(3, g.cell(i, j, g.C3)) : at(3, g.cell(i, j, 1));
     }
 }
 
@@ -811,7 +816,7 @@ __device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src,
     const int k1 = k0 + kTileK - 1 < g.C3 ? k0 + kTileK - 1 : g.C3;
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long rsum = 0;
-    if (i <= g.C1 && j <= g.C2) {
+    if (i <= g.C1 && j <= g.C2 && ARK_CK_IN(k0, 1, g.C3)) {
         const K<T> &kk = kconst<T>(S.k);
         const T dt = sc_dt<T>(S.sc);
         const T *__restrict__ sro = S.lv[src].ro;
@@ -960,7 +965,7 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
     const int k = bx.z + 1;
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long rsum = 0;
-    if (i <= g.C1 && j <= g.C2) {
+    if (i <= g.C1 && j <= g.C2 && ARK_CK_IN(k, 1, g.C3)) {
         const K<T> &kk = kconst<T>(S.k);
         const T dt = sc_dt<T>(S.sc);
         const T *__restrict__ sro = S.lv[src].ro;
@@ -1104,7 +1109,7 @@ __global__ void __launch_bounds__(SX *SY, 3) k_phase1_faces(const __grid_constan
     const int i = blockIdx.x * SX + tx + 1, j = blockIdx.y * SY + ty + 1;
     const int k0 = blockIdx.z * kch + 1;
     const int k1 = k0 + kch - 1 < g.C3 ? k0 + kch - 1 : g.C3;
-    const bool valid = i <= g.C1 && j <= g.C2;
+    const bool valid = i <= g.C1 && j <= g.C2 && ARK_CK_IN(k0, 1, g.C3);
     const int ilast = blockIdx.x * SX + SX < g.C1 ? blockIdx.x * SX + SX : g.C1;
     const int jlast = blockIdx.y * SY + SY < g.C2 ? blockIdx.y * SY + SY : g.C2;
     const K<T> &kk = kconst<T>(S.k);
@@ -1446,6 +1451,7 @@ template <class T> struct NCell {
     const T *__restrict__ nA;
     const T *__restrict__ nB;
     const T *__restrict__ ro;
+    int nc; // elements of a cell array (bounds-checked builds)
 };
 
 // The new face generation of one sweep direction.
@@ -1455,6 +1461,7 @@ template <class T> struct FaceOut {
     T *__restrict__ n;
     T *__restrict__ a;
     T *__restrict__ b;
+    int nf; // elements of a face array (bounds-checked builds)
 };
 
 // The new values of one face: pressure, density, normal and tangential velocities.
@@ -1551,6 +1558,9 @@ template <class T, bool WALL_A_FROM_N>
 __device__ __forceinline__ void face_update(const NCell<T> &N, const FaceOut<T> &W, int cb, int cf, int fc,
                                             uint8_t flb, uint8_t flf, T ucb, T ucf, const Ext<T> &prev,
                                             const Ext<T> &cur, T uA_old, T uB_old, const SweepK<T> &q) {
+    cb = ARK_CK(cb, N.nc);
+    cf = ARK_CK(cf, N.nc);
+    fc = ARK_CK(fc, W.nf);
     face_store(W, fc, face_values<T, WALL_A_FROM_N>(N, cb, cf, flb, flf, ucb, ucf, prev, cur, uA_old, uB_old, q));
 }
 
@@ -1598,6 +1608,7 @@ template <class T> struct SweepSrc {
     const T *__restrict__ cR;
     const T *__restrict__ nR;
     const uint8_t *__restrict__ fl;
+    int nc, nf; // elements of a cell and of a face array (bounds-checked builds)
 };
 
 template <class T>
@@ -1606,19 +1617,22 @@ __device__ __forceinline__ SweepSrc<T> sweep_src(const DevState<T> &S, int con, 
     const FaceSet<T> F = S.fc[fcur][ax];
     const int a = ax == 0 ? 1 : 0, b = ax == 2 ? 1 : 2;
     const T *cu[3] = {Lc.u1, Lc.u2, Lc.u3}, *nu[3] = {Ln.u1, Ln.u2, Ln.u3};
-    SweepSrc<T> r = {F.u[ax], F.u[a], F.u[b], F.p, cu[ax], nu[ax], cu[a], nu[a], cu[b], nu[b], Lc.ro, Ln.ro, S.flags};
+    SweepSrc<T> r = {F.u[ax], F.u[a], F.u[b], F.p, cu[ax], nu[ax], cu[a], nu[a], cu[b], nu[b], Lc.ro, Ln.ro, S.flags,
+                     (int)S.g.ncell(), (int)S.g.nface()};
     return r;
 }
 
 template <class T> __device__ __forceinline__ FaceOut<T> sweep_out(const DevState<T> &S, int fcur, int ax) {
     const FaceSet<T> W = S.fc[fcur ^ 1][ax];
     const int a = ax == 0 ? 1 : 0, b = ax == 2 ? 1 : 2;
-    FaceOut<T> o = {W.p, W.ro, W.u[ax], W.u[a], W.u[b]};
+    FaceOut<T> o = {W.p, W.ro, W.u[ax], W.u[a], W.u[b], (int)S.g.nface()};
     return o;
 }
 
 template <class T>
 __device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, SweepIn<T> &x) {
+    c = ARK_CK(c, R.nc);
+    ff = ARK_CK(ff, R.nf);
     x.uN_f = R.FN[ff];
     x.uA_f = R.FA[ff];
     x.uB_f = R.FB[ff];
@@ -1658,7 +1672,7 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     const int total = nl * npos;              // positions of the warp's stream
     const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
     const FaceOut<T> W = sweep_out(S, fcur, 0);
-    const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
+    const NCell<T> N = {R.nN, R.nA, R.nB, R.nR, R.nc};
     const SweepK<T> q = sweep_consts(S, 0);
     const bool bounded = !S.k.periodic_x;
     // a lane's position: line li of the group, cell s, and the line's cell / face 0 indices
@@ -1697,8 +1711,8 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     RQ<T> carry_rq = {(T)0, (T)0};
     if (cp.li < nl) {
         sweep_load(R, cp.c0 + cp.s, cp.f0 + cp.s + 1, cur);
-        uA_b = R.FA[cp.f0 + cp.s];
-        uB_b = R.FB[cp.f0 + cp.s];
+        uA_b = R.FA[ARK_CK(cp.f0 + cp.s, R.nf)];
+        uB_b = R.FB[ARK_CK(cp.f0 + cp.s, R.nf)];
     }
     for (int p0 = 0; p0 < total; p0 += 32) {
         const bool act = cp.li < nl;
@@ -1707,8 +1721,8 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         advance(np);
         if (np.li < nl) {
             sweep_load(R, np.c0 + np.s, np.f0 + np.s + 1, nxt);
-            nuA_b = R.FA[np.f0 + np.s];
-            nuB_b = R.FB[np.f0 + np.s];
+            nuA_b = R.FA[ARK_CK(np.f0 + np.s, R.nf)];
+            nuB_b = R.FB[ARK_CK(np.f0 + np.s, R.nf)];
         }
         RQ<T> rqf = {(T)0, (T)0};
         if (act) rqf = face_rq(cur.uN_f, cur.p_f, q);
@@ -1716,7 +1730,7 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         rqb.r = __shfl_up_sync(0xffffffffu, rqf.r, 1);
         rqb.q = __shfl_up_sync(0xffffffffu, rqf.q, 1);
         if (lane == 0) rqb = carry_rq;
-        if (act && s == 0) rqb = face_rq(R.FN[f0], R.FP[f0], q);
+        if (act && s == 0) rqb = face_rq(R.FN[ARK_CK(f0, R.nf)], R.FP[ARK_CK(f0, R.nf)], q);
         carry_rq.r = __shfl_sync(0xffffffffu, rqf.r, 31);
         carry_rq.q = __shfl_sync(0xffffffffu, rqf.q, 31);
         Ext<T> e = {};
@@ -1728,7 +1742,7 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
             // inflow invariant R = 1 (0 behind a solid first cell) and outflow Q = 5/6 with
             // zero tangential velocity (main.cpp:1731-1745)
             if (s == 0) {
-                e.rf = (R.fl[c0 + 1] & FL_LT) ? (T)1 : (T)0;
+                e.rf = (R.fl[ARK_CK(c0 + 1, R.nc)] & FL_LT) ? (T)1 : (T)0;
                 e.af = (T)0;
                 e.bf = (T)0;
             }
@@ -1795,13 +1809,13 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     const int s1 = s0 + seg < nd ? s0 + seg : nd;
     const SweepSrc<T> R = sweep_src(S, con, fcur, AX);
     const FaceOut<T> W = sweep_out(S, fcur, AX);
-    const NCell<T> N = {R.nN, R.nA, R.nB, R.nR};
+    const NCell<T> N = {R.nN, R.nA, R.nB, R.nR, R.nc};
     const SweepK<T> q = sweep_consts(S, AX);
     const int cst = AX == 1 ? (int)g.cs1 : (int)g.cs2, fst = AX == 1 ? (int)g.fs1 : (int)g.fs2;
     int c = (AX == 1 ? g.ci(i, 0, o) : g.ci(i, o, 0)) + s0 * cst;
     int fb = (AX == 1 ? g.fi(i, 0, o) : g.fi(i, o, 0)) + s0 * fst;
-    T uA_b = R.FA[fb], uB_b = R.FB[fb];
-    RQ<T> rqb = face_rq(R.FN[fb], R.FP[fb], q); // then the forward face's, carried
+    T uA_b = R.FA[ARK_CK(fb, R.nf)], uB_b = R.FB[ARK_CK(fb, R.nf)];
+    RQ<T> rqb = face_rq(R.FN[ARK_CK(fb, R.nf)], R.FP[ARK_CK(fb, R.nf)], q); // then the forward face's, carried
     SweepIn<T> cur, nxt = {};
     sweep_load(R, c, fb + fst, cur);
     Ext<T> prev = {};
@@ -1877,7 +1891,8 @@ __global__ void __launch_bounds__(SX *SY, 2) k_phase2_fused(const __grid_constan
     const bool valid = i <= g.C1 && j <= g.C2;
     const SweepSrc<T> RX = sweep_src(S, con, fcur, 0), RY = sweep_src(S, con, fcur, 1), RZ = sweep_src(S, con, fcur, 2);
     const FaceOut<T> WX = sweep_out(S, fcur, 0), WY = sweep_out(S, fcur, 1), WZ = sweep_out(S, fcur, 2);
-    const NCell<T> NX = {RX.nN, RX.nA, RX.nB, RX.nR}, NY = {RY.nN, RY.nA, RY.nB, RY.nR}, NZ = {RZ.nN, RZ.nA, RZ.nB, RZ.nR};
+    const NCell<T> NX = {RX.nN, RX.nA, RX.nB, RX.nR, RX.nc}, NY = {RY.nN, RY.nA, RY.nB, RY.nR, RY.nc},
+                   NZ = {RZ.nN, RZ.nA, RZ.nB, RZ.nR, RZ.nc};
     const SweepK<T> qx = sweep_consts(S, 0), qy = sweep_consts(S, 1), qz = sweep_consts(S, 2);
     const int cs1 = (int)g.cs1, cs2 = (int)g.cs2, fs1 = (int)g.fs1, fs2 = (int)g.fs2;
     const bool bounded_x = !S.k.periodic_x;
@@ -2071,8 +2086,10 @@ template <class T> inline void wrap_launch(const DevState<T> &S, const WrapJob &
 // bounded x and z take the zero-gradient copy.  with_ro also fills roCon's ghosts as Phase2's
 // exchange does (main.cpp:1049-1698: wrapped on periodic axes, copied on a bounded z, left
 // alone on a bounded x), for the fused step, which reads that level before Phase2.
+// A slab of a z split (ext_z) leaves its z ghosts to the slab group's halo exchange.
 template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st) {
-    const uint8_t ux = S.k.periodic_x ? GH_WRAP : GH_COPY, uz = S.k.periodic_z ? GH_WRAP : GH_COPY;
+    const uint8_t ux = S.k.periodic_x ? GH_WRAP : GH_COPY;
+    const uint8_t uz = S.k.ext_z ? GH_NONE : S.k.periodic_z ? GH_WRAP : GH_COPY;
     WrapJob J = {};
     const Level<T> L = S.lv[con];
     wrap_add(J, L.u1, 0, ux, uz);
@@ -2087,7 +2104,7 @@ template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int w
 // bounded x sweep never reads their halo); faces normal to x3 wrap or copy in z.
 template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st) {
     const bool px = S.k.periodic_x, pz = S.k.periodic_z;
-    const uint8_t cx = px ? GH_WRAP : GH_COPY, cz = pz ? GH_WRAP : GH_COPY;
+    const uint8_t cx = px ? GH_WRAP : GH_COPY, cz = S.k.ext_z ? GH_NONE : pz ? GH_WRAP : GH_COPY;
     WrapJob J = {};
     const Level<T> Ln = S.lv[con ^ 1], Lc = S.lv[con];
     wrap_add(J, Ln.u1, 0, cx, cz);
@@ -2101,6 +2118,24 @@ template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, in
     for (int q = 0; q < 5; ++q) wrap_add(J, fx[q], 1, px ? GH_WRAP : GH_NONE, GH_NONE);
     for (int q = 0; q < 5; ++q) wrap_add(J, fz[q], 1, GH_NONE, cz);
     wrap_launch(S, J, st);
+}
+
+// A slab group's halo exchange: thread (x, job) copies interior element x of one plane.  The
+// sources are interior planes of the slabs, the destinations ghost planes, so the copies of one
+// exchange are independent.
+template <class T> __global__ void k_halo(Geom g, const HaloJob *__restrict__ jobs) {
+    const HaloJob J = jobs[blockIdx.y];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.C1 * g.C2) return;
+    const int i = t % g.C1 + 1, j = t / g.C1 + 1;
+    const int64_t row = (int64_t)j * (J.face ? g.fs1 : g.cs1) + i;
+    const int64_t plane = J.face ? g.fs2 : g.cs2;
+    ((T *)J.dst)[ARK_CK((int64_t)J.dst_plane * plane + row, (int64_t)J.dst_planes * plane)] =
+        ((const T *)J.src)[ARK_CK((int64_t)J.src_plane * plane + row, (int64_t)J.src_planes * plane)];
+}
+template <class T> void Launch<T>::halo_exchange(const Geom &g, const HaloJob *jobs, int njobs, cudaStream_t st) {
+    if (njobs <= 0) return;
+    k_halo<T><<<dim3((g.C1 * g.C2 + 255) / 256, njobs), 256, 0, st>>>(g, jobs);
 }
 
 template <class T, template <class, int> class KERNEL>

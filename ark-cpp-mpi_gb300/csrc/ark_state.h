@@ -178,6 +178,7 @@ struct Consts {
     double u_target;
     int forcing;
     int periodic_x, periodic_z; // 0: the reference's bounded edges (see k_wrap, k_sweep_x)
+    int ext_z;                  // 1: the z ghosts are filled from outside (a slab of a z split)
     KT<double> kd;
     KT<float> kf;
 };
@@ -235,6 +236,52 @@ template <class T> struct DevState {
 template <class T> struct Storage { static constexpr bool deviation = false; };
 template <> struct Storage<float> { static constexpr bool deviation = true; };
 
+// ---- z-slab decomposition (ark_slabs.cu) ----
+// A grid of C3 planes split into n slabs: slab s owns the global interior planes
+// [k_first, k_last] (1-based), C3 / n planes each and one more for the first C3 % n slabs.
+struct SlabRange {
+    int k_first, k_last, below, above; // neighbour slabs; -1: bounded edge (zero-gradient)
+};
+__host__ __device__ inline SlabRange slab_range(int C3, int n, int s, int periodic) {
+    const int q = C3 / n, r = C3 % n;
+    SlabRange R;
+    R.k_first = 1 + s * q + (s < r ? s : r);
+    R.k_last = R.k_first + q + (s < r ? 1 : 0) - 1;
+    R.below = s > 0 ? s - 1 : (periodic ? n - 1 : -1);
+    R.above = s < n - 1 ? s + 1 : (periodic ? 0 : -1);
+    return R;
+}
+// The local plane a z ghost of a slab of c3 planes takes, and the plane of the source slab (a
+// neighbour of c3_src planes, or the slab itself at a bounded edge) it comes from, as the
+// periodic wrap and the zero-gradient copy of a whole domain take them (k_wrap): cells: ghost 0
+// <- the plane below's last interior plane, ghost c3+1 <- the plane above's first; faces normal
+// or parallel to z alike (face k lies below cell k): halo 0 <- the source's face c3_src (the
+// face below its last cell), halo c3+2 <- its face 2 (the face above its first cell).  At a
+// bounded edge the source is the slab itself: ghost 0 <- 1, ghost c3+1 <- c3, halo 0 <- face 1,
+// halo c3+2 <- face c3+1.  side 0: below, 1: above.
+struct HaloPlanes {
+    int dst, src;
+};
+__host__ __device__ inline HaloPlanes halo_planes(int face, int side, int c3, int c3_src, bool bounded) {
+    HaloPlanes h;
+    if (!face) {
+        h.dst = side ? c3 + 1 : 0;
+        h.src = bounded ? (side ? c3 : 1) : (side ? 1 : c3_src);
+    } else {
+        h.dst = side ? c3 + 2 : 0;
+        h.src = bounded ? (side ? c3 + 1 : 1) : (side ? 2 : c3_src);
+    }
+    return h;
+}
+// One plane copy of a halo exchange: the interior (i, j) of plane src_plane of src into plane
+// dst_plane of dst, arrays of one row and plane geometry (cells or faces: face) and
+// dst_planes / src_planes planes.
+struct HaloJob {
+    void *dst;
+    const void *src;
+    int dst_plane, src_plane, face, dst_planes, src_planes, pad;
+};
+
 // Launch entry points (defined per precision in ark_fp64.cu / ark_fp32.cu).
 // P1_RMAX / P1_RSUM: also take the dt partials (max |u| of the level written) or the bulk-flow
 // partials (sum of u1 of the level written) for the next step.
@@ -260,6 +307,9 @@ template <class T> struct Launch {
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
     static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);
+    // the plane copies of a slab group's halo exchange (device job table of njobs entries);
+    // g: the geometry of the slabs' rows and planes (all slabs share C1, C2 and the pitch)
+    static void halo_exchange(const Geom &g, const HaloJob *jobs, int njobs, cudaStream_t st);
     // one-time launch attributes (the staged Phase1's shared memory); host only
     static void prepare();
 };

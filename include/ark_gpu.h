@@ -258,6 +258,16 @@ int ark_vorticity(ark_ctx *ctx, double *out);
  * Runs on the current device. */
 int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches);
 
+/* Bounds-checked builds (compiled with -DARK_CHECK, the library's lib_check/ variant): the
+ * kernels compare the indices of their global-memory accesses (sweeps, ghost fills, halo
+ * exchange, boundary conditions, the closure's inference) and the cell coordinates their blocks
+ * decode (Phase1 kernels, the ensemble's work lists) with the extents they must stay inside; an
+ * index outside is replaced by 0 (the access stays inside the array) and recorded, nothing
+ * traps.  out[0..3] = {violations since the last reset, the first value, its bound, the source
+ * line in csrc/}; reset != 0 clears the record.  Ordinary builds return ARK_ERR_UNSUPPORTED.
+ * Call after ark_sync. */
+int ark_bounds_check(int reset, long long *out);
+
 /* Host-only check (no GPU needed) of the copy plan of the FP32 Phase1 kernel that stages its
  * planes in shared memory, for an n1 x n2 x n3-cell grid and planes_per_block planes per block
  * (0: the kernel's own choice): every 16-byte copy inside its array and its stage and aligned,
@@ -359,6 +369,45 @@ int ark_ensemble_autotune(ark_ensemble *ens, int steps_per_candidate, int *choic
 /* Sets the kernel shape directly (march_a / march_b: 0, 1 or 2 as above).  Until this or
  * ark_ensemble_autotune is called, an ensemble uses 2, 2 and 32-face segments. */
 int ark_ensemble_set_shape(ark_ensemble *ens, int march_a, int march_b, int segment);
+
+/* ---- slab groups: one channel split along z -------------------------------------------------
+ * The reference's domain decomposition (main.cpp:53-67: MPI_Dims_create / MPI_Cart_create,
+ * one-plane halos) applied along z on one device: the grid's C3 planes are split into nslabs
+ * slabs (C3 / nslabs planes each, one more for the first C3 % nslabs), each an ark_ctx of its
+ * own that keeps its x wrap and y walls, and the z ghosts are exchanged plane by plane at the
+ * reference's two exchange points of a step: the "Con" velocities and density before the stress
+ * (main.cpp:601-801) and, before Phase2, the half-step level, the old density and the faces
+ * normal to z (main.cpp:1049-1631).  dt (main.cpp:412, MPI_Allreduce MIN) and the bulk-flow sum
+ * are reduced exactly over all slabs (max |u| as integer bit patterns, fixed-point sums), so the
+ * group's result is the single context's bit for bit.  Periodic z wraps around the group; a
+ * bounded z copies zero-gradient at its ends.  A step is one CUDA graph on the group's stream.
+ * Upload and download take whole-domain host states (Arr3d layout); the step is the fused
+ * main.cpp:82-91 with the three separate Phase2 sweep kernels. */
+typedef struct ark_slabs ark_slabs;
+
+ark_slabs *ark_slabs_create(const ark_params *params, int nslabs, int *status);
+int ark_slabs_destroy(ark_slabs *group);
+int ark_slabs_count(const ark_slabs *group);
+int ark_slabs_upload(ark_slabs *group, const ark_host_state *host);
+int ark_slabs_download(ark_slabs *group, ark_host_state *host);
+int ark_slabs_step(ark_slabs *group, int nsteps);
+int ark_slabs_sync(ark_slabs *group);
+int ark_slabs_time_steps(ark_slabs *group, int nsteps, double *ms);
+int ark_slabs_get_scalars(ark_slabs *group, ark_scalars *out);
+int ark_slabs_conservation_sums(ark_slabs *group, ark_sums *out);
+
+/* The decomposition plan (host only, no GPU needed): the global interior planes
+ * [*k_first, *k_last] (1-based) of slab `slab` of nslabs over n3_cells planes, and its
+ * neighbour slabs below and above (-1 at a bounded end; periodic z wraps). */
+int ark_slab_plan(int n3_cells, int nslabs, int slab, int periodic_z, int *k_first, int *k_last, int *below,
+                  int *above);
+/* The halo schedule (host only): for a cell array (face = 0) or a face array (face = 1) of a
+ * slab of c3 planes, the ghost plane written on side 0 (below) or 1 (above) and the plane of
+ * the source slab (c3_src planes) it is copied from: cells ghost 0 <- plane c3_src of the slab
+ * below, ghost c3+1 <- plane 1 of the slab above; faces halo 0 <- face c3_src, halo c3+2 <-
+ * face 2; bounded != 0 (no neighbour): the slab's own zero-gradient planes 1, c3 (faces 1,
+ * c3+1). */
+int ark_slab_halo_planes(int face, int side, int c3, int c3_src, int bounded, int *dst_plane, int *src_plane);
 
 /* ---- host-side helpers (no GPU needed) ----------------------------------------------------- */
 

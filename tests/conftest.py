@@ -34,3 +34,17 @@ def ark():
 
     arkgpu.lib()
     return arkgpu
+
+
+@pytest.fixture(autouse=True)
+def _bounds_checked_build_clean(request):
+    """Under the bounds-checked library (ARK_GPU_LIB pointing at lib_check/), every GPU test also
+    asserts that its kernels recorded no out-of-range index (ark_bounds_check)."""
+    yield
+    if not os.environ.get("ARK_GPU_LIB") or "gpu" not in request.keywords:
+        return
+    import arkgpu
+
+    # ARK_GPU_LIB names the bounds-checked build: an ordinary library there (status 6) fails too
+    hits, value, bound, line = arkgpu.bounds_check(reset=True)
+    assert hits == 0, f"{hits} out-of-range kernel indices; first {value} (bound {bound}) at csrc line {line}"

@@ -290,8 +290,9 @@ def test_fp32_error_bounds_500_steps(ark, port):
     """The FP32 path's stated error after 500 steps of a 128x64x64 channel (Re_b 5600) against
     the FP64 path from the same seeded state (the FP64 path is the reference's arithmetic bit
     for bit): the mean u1(y) profile within 1e-3 of it (the FP32 target), the wall shear
-    2*VIS*U(wall)/dy (main.cpp:924-927) at both walls within 1e-2 relative, and the field
-    relative L2 errors (density as rho - ro0) within the bounds below."""
+    2*VIS*U(wall)/dy (main.cpp:924-927) at both walls within 5e-4 relative, and the field
+    relative L2 errors (density as rho - ro0) within the bounds below.  Measured on GB300: profile
+    1.8e-6, wall shear 2.3e-5 / 2.8e-5, rho - ro0 1.9e-3, u1 2.4e-5, u2 1.9e-3, u3 1.7e-3."""
     p = port.channel_params(128, 64, 64, re_b=5600.0, seed=321)
     st0 = port.channel_state(p)
     res = {}
@@ -313,9 +314,9 @@ def test_fp32_error_bounds_500_steps(ark, port):
         err[n] = rel_l2(a, b)
     print("fp32 vs fp64, 128x64x64, 500 steps:", err)
     assert err["profile_max_abs"] <= 1e-3
-    assert max(err["wall_shear_rel"]) <= 1e-2
-    assert err["u1nCon"] <= 1e-3 and err["ronCon"] <= 5e-2
-    assert err["u2nCon"] <= 5e-2 and err["u3nCon"] <= 5e-2
+    assert max(err["wall_shear_rel"]) <= 5e-4
+    assert err["u1nCon"] <= 2e-4 and err["ronCon"] <= 1e-2
+    assert err["u2nCon"] <= 1e-2 and err["u3nCon"] <= 1e-2
 
 
 def test_fp32_per_phase_equals_fused(ark, port):
