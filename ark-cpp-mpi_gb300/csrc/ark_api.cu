@@ -362,14 +362,16 @@ template <class T> struct EngineT : Engine {
             cudaEventRecord(ctx->join, ctx->side);
             mode |= P1_NUT;
         }
+        // the one-kernel Phase2 forms read x ghosts; the x1 sweep kernel does not
+        const int xg = ctx->p2mode != 0 ? 1 : 0;
         Launch<T>::finalize_dt(S, 1, st);
         mark(0);
-        Launch<T>::wrap_con(S, y, 1, st);
+        Launch<T>::wrap_con(S, y, xg ? 2 : 1, st);
         mark(1);
         if (ctx->closure_net) cudaStreamWaitEvent(st, ctx->join, 0);
         Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st);
         mark(2);
-        Launch<T>::wrap_phase2(S, y, fcur, st);
+        Launch<T>::wrap_phase2(S, y, fcur, st, xg);
         mark(3);
         if (use_step2()) {
             // Phase2 and the second Phase1 in one kernel; the new level goes to the spare, which

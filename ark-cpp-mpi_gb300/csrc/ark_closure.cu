@@ -4,8 +4,9 @@
 //     device, give per sampled cell 10 features of the filtered velocity gradient and the
 //     least-squares eddy viscosity of the filtered-out stress as the target;
 //   * network: 10 -> 32 (GELU) -> 32 (GELU) -> 1 (softplus) = nu_t / nu, BF16 weights, FP32
-//     arithmetic and accumulation; trained by the kernels here (per-sample forward and
-//     backward, tile-wise fixed-order gradient sums, Adam on FP32 master weights);
+//     accumulation; trained by the kernels here (the layers' products over a tile of samples as
+//     BF16 tensor-core multiplies with two-term BF16 operands, tile-wise fixed-order gradient
+//     sums, Adam on FP32 master weights);
 //   * inference: nu_t of every cell of a (coarse) FP32 context before its stress, which then
 //     uses nu + nu_t averaged to each face.
 // Definitions (filter, features, target, network) are restated in numpy in oracle/closure.py.
@@ -419,27 +420,84 @@ __global__ void __launch_bounds__(256) k_plane_stats_compact(const double *u0, c
 
 // ---- training kernels ---------------------------------------------------------------------
 
-constexpr int TS = 128; // samples per tile (one per thread)
+constexpr int TS = 128; // samples per tile (one per thread in the elementwise phases)
+
+// ---- training on the tensor cores ---------------------------------------------------------
+// The layers' products over a tile of TS samples are warp-level BF16 matrix multiply-accumulates
+// (m16n8k16, FP32 accumulation): the forward layers Z1 = X W1^T, Z2 = H1 W2^T, the backward
+// product D2 W2, and the weight gradients D1^T X and D2^T H1 summed over the tile.  The weights
+// are BF16 values already (the working weights), so they enter the multiplies exactly; every
+// activation or derivative a enters as a two-term BF16 expansion a = hi + lo (hi = bf16(a),
+// lo = bf16(a - hi)), and a product of two such operands as hi*hi + hi*lo + lo*hi, which keeps
+// about 16 significand bits (relative error near 2^-16 per product) where one BF16 product
+// keeps 8.  The elementwise parts (normalisation, GELU and its derivative, the softplus output,
+// the loss) stay in FP32 per sample.  All sums run in a fixed order, so the gradient is
+// deterministic.
+
+constexpr int LDX = 20;      // floats per staged input row (10 inputs padded to 16, + 4 against bank conflicts)
+constexpr int LDH = NH + 4;  // floats per staged hidden row
+
+// a two-term BF16 expansion of a pair of values, packed as the pair registers of a fragment
+struct Pair2 {
+    unsigned hi, lo;
+};
+__device__ __forceinline__ Pair2 split_pair(float a, float b) {
+    const __nv_bfloat16 ah = __float2bfloat16_rn(a), bh = __float2bfloat16_rn(b);
+    Pair2 r;
+    __nv_bfloat162 h;
+    h.x = ah;
+    h.y = bh;
+    r.hi = *reinterpret_cast<unsigned *>(&h);
+    r.lo = pack_bf16(a - __bfloat162float(ah), b - __bfloat162float(bh));
+    return r;
+}
+
+// C[16 x 8] += A[16 x 16k] B[16k x 8] for an operand A given by element reads a(row, col) (split
+// into two BF16 terms) and B by b(row, col): exact BF16 (wexact, one term) or split (three
+// products).  Thread lane = 4 g + t holds C[g][2t], C[g][2t+1], C[g+8][2t], C[g+8][2t+1].
+template <int KSTEPS, bool B_EXACT, class FA, class FB>
+__device__ __forceinline__ void mma_tile(float c[4], int lane, FA a, FB b) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int ks = 0; ks < KSTEPS; ++ks) {
+        const int k0 = 16 * ks;
+        const Pair2 a0 = split_pair(a(g, k0 + 2 * t), a(g, k0 + 2 * t + 1));
+        const Pair2 a1 = split_pair(a(g + 8, k0 + 2 * t), a(g + 8, k0 + 2 * t + 1));
+        const Pair2 a2 = split_pair(a(g, k0 + 2 * t + 8), a(g, k0 + 2 * t + 9));
+        const Pair2 a3 = split_pair(a(g + 8, k0 + 2 * t + 8), a(g + 8, k0 + 2 * t + 9));
+        const unsigned ahi[4] = {a0.hi, a1.hi, a2.hi, a3.hi}, alo[4] = {a0.lo, a1.lo, a2.lo, a3.lo};
+        if (B_EXACT) {
+            const unsigned b0 = pack_bf16(b(k0 + 2 * t, g), b(k0 + 2 * t + 1, g));
+            const unsigned b1 = pack_bf16(b(k0 + 2 * t + 8, g), b(k0 + 2 * t + 9, g));
+            mma_bf16(c, ahi, b0, b1);
+            mma_bf16(c, alo, b0, b1);
+        } else {
+            const Pair2 b0 = split_pair(b(k0 + 2 * t, g), b(k0 + 2 * t + 1, g));
+            const Pair2 b1 = split_pair(b(k0 + 2 * t + 8, g), b(k0 + 2 * t + 9, g));
+            mma_bf16(c, ahi, b0.hi, b1.hi);
+            mma_bf16(c, ahi, b0.lo, b1.lo);
+            mma_bf16(c, alo, b0.hi, b1.hi);
+        }
+    }
+}
 
 // Gradient of the mean squared error over samples [first, first + count) of the batch map
 // (sample index = (first + q) * stride + offset), into block partials part[block][NPARAM + 1]
-// (the last entry: the block's sum of squared errors).  Per tile: each thread runs one sample
-// forward and backward, keeping its activations in shared memory; the weight gradients are
-// then sums over the tile in a fixed order.  scale = 2 / (samples of the batch).
-__global__ void __launch_bounds__(TS) k_mlp_grad(const float *__restrict__ feat, const float *__restrict__ targ,
-                                                 long long first, long long count, long long stride, long long offset,
-                                                 const Net *__restrict__ net, float scale, float *part) {
+// (the last entry: the block's sum of squared errors).  scale = 2 / (samples of the batch).
+__global__ void __launch_bounds__(TS, 2) k_mlp_grad(const float *__restrict__ feat, const float *__restrict__ targ,
+                                                    long long first, long long count, long long stride, long long offset,
+                                                    const Net *__restrict__ net, float scale, float *part) {
     extern __shared__ float smem[];
-    float *w = smem;                       // NPARAM
-    float *Xs = w + NPARAM;                // TS x NIN
-    float *H1 = Xs + TS * NIN;             // TS x NH (gelu(z1))
-    float *D1 = H1 + TS * NH;              // TS x NH (dL/dz1)
-    float *H2 = D1 + TS * NH;              // TS x NH
-    float *D2 = H2 + TS * NH;              // TS x NH
-    float *D3 = D2 + TS * NH;              // TS
-    float *R2 = D3 + TS;                   // TS (squared errors)
-    float *acc = R2 + TS;                  // NPARAM + 1 (this block's sums)
-    const int t = threadIdx.x;
+    float *w = smem;                  // NPARAM (BF16-exact working weights)
+    float *acc = w + NPARAM;          // NPARAM + 1 (this block's sums)
+    float *X = acc + NPARAM + 1;      // TS x LDX: normalised inputs, zero past NIN
+    float *Z1 = X + TS * LDX;         // TS x LDH: z1, then dL/dz1
+    float *H1 = Z1 + TS * LDH;        // TS x LDH: gelu(z1)
+    float *Z2 = H1 + TS * LDH;        // TS x LDH: z2, then dL/dz2
+    float *H2 = Z2 + TS * LDH;        // TS x LDH: gelu(z2)
+    float *D3 = H2 + TS * LDH;        // TS: dL/dz3
+    float *R2 = D3 + TS;              // TS: squared errors
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5, g = lane >> 2, tq = lane & 3;
     for (int q = t; q < NPARAM; q += TS) {
         w[q] = net->w[q];
         acc[q] = 0.f;
@@ -455,86 +513,143 @@ __global__ void __launch_bounds__(TS) k_mlp_grad(const float *__restrict__ feat,
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long q = tile * TS + t;
         const bool live = q < count;
-        float xn[NIN], z1[NH], h1[NH];
-        if (live) {
-            const long long s = (first + q) * stride + offset;
+        const long long smp = live ? (first + q) * stride + offset : 0;
+        // inputs (a sample past the end enters as zeros; its error and derivatives are zero)
 #pragma unroll
-            for (int i = 0; i < NIN; ++i) xn[i] = (feat[s * NIN + i] - mu[i]) * rsd[i];
-            // forward
-#pragma unroll 4
-            for (int k = 0; k < NH; ++k) {
-                float z = w[O_B1 + k];
+        for (int i = 0; i < 16; ++i) X[t * LDX + i] = (live && i < NIN) ? (feat[smp * NIN + i] - mu[i]) * rsd[i] : 0.f;
+        __syncthreads();
+        // Z1 = X W1^T + b1: warp w takes sample rows 32w .. 32w+31 (two m-tiles), all four n-tiles
 #pragma unroll
-                for (int i = 0; i < NIN; ++i) z += w[O_W1 + k * NIN + i] * xn[i];
-                z1[k] = z;
-                h1[k] = gelu(z);
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int s0 = 32 * wid + 16 * mt, n0 = 8 * nt;
+                float c[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_tile<1, true>(c, lane, [&](int r, int k) { return X[(s0 + r) * LDX + k]; },
+                                  [&](int k, int n) { return k < NIN ? w[O_W1 + (n0 + n) * NIN + k] : 0.f; });
+                const int n = n0 + 2 * tq;
+                Z1[(s0 + g) * LDH + n] = c[0] + w[O_B1 + n];
+                Z1[(s0 + g) * LDH + n + 1] = c[1] + w[O_B1 + n + 1];
+                Z1[(s0 + g + 8) * LDH + n] = c[2] + w[O_B1 + n];
+                Z1[(s0 + g + 8) * LDH + n + 1] = c[3] + w[O_B1 + n + 1];
             }
-            float z3 = w[O_B3], z2[NH];
+        __syncthreads();
+        for (int k = 0; k < NH; ++k) H1[t * LDH + k] = gelu(Z1[t * LDH + k]);
+        __syncthreads();
+        // Z2 = H1 W2^T + b2
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int s0 = 32 * wid + 16 * mt, n0 = 8 * nt;
+                float c[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_tile<2, true>(c, lane, [&](int r, int k) { return H1[(s0 + r) * LDH + k]; },
+                                  [&](int k, int n) { return w[O_W2 + (n0 + n) * NH + k]; });
+                const int n = n0 + 2 * tq;
+                Z2[(s0 + g) * LDH + n] = c[0] + w[O_B2 + n];
+                Z2[(s0 + g) * LDH + n + 1] = c[1] + w[O_B2 + n + 1];
+                Z2[(s0 + g + 8) * LDH + n] = c[2] + w[O_B2 + n];
+                Z2[(s0 + g + 8) * LDH + n + 1] = c[3] + w[O_B2 + n + 1];
+            }
+        __syncthreads();
+        // per sample: the second activation, the output, the error and dL/dz3, then dL/dz2
+        {
+            float z3 = w[O_B3];
             for (int k = 0; k < NH; ++k) {
-                float z = w[O_B2 + k];
-#pragma unroll 8
-                for (int m = 0; m < NH; ++m) z += w[O_W2 + k * NH + m] * h1[m];
-                z2[k] = z;
-                const float h2 = gelu(z);
-                H2[t * NH + k] = h2;
+                const float h2 = gelu(Z2[t * LDH + k]);
+                H2[t * LDH + k] = h2;
                 z3 += w[O_W3 + k] * h2;
             }
-            const float y = softplus(z3), r = y - targ[s];
-            R2[t] = r * r;
-            // backward
-            const float d3 = scale * r * sigmoid(z3);
+            float d3 = 0.f, r2 = 0.f;
+            if (live) {
+                const float y = softplus(z3), r = y - targ[smp];
+                r2 = r * r;
+                d3 = scale * r * sigmoid(z3);
+            }
             D3[t] = d3;
-            float d2[NH];
-            for (int k = 0; k < NH; ++k) {
-                d2[k] = d3 * w[O_W3 + k] * gelu_grad(z2[k]);
-                D2[t * NH + k] = d2[k];
-            }
-            for (int m = 0; m < NH; ++m) {
-                float s1 = 0.f;
-#pragma unroll 8
-                for (int k = 0; k < NH; ++k) s1 += d2[k] * w[O_W2 + k * NH + m];
-                D1[t * NH + m] = s1 * gelu_grad(z1[m]);
-                H1[t * NH + m] = h1[m];
-            }
-#pragma unroll
-            for (int i = 0; i < NIN; ++i) Xs[t * NIN + i] = xn[i];
-        } else {
-            D3[t] = 0.f;
-            R2[t] = 0.f;
-            for (int k = 0; k < NH; ++k) {
-                D2[t * NH + k] = 0.f;
-                D1[t * NH + k] = 0.f;
-                H1[t * NH + k] = 0.f;
-                H2[t * NH + k] = 0.f;
-            }
-#pragma unroll
-            for (int i = 0; i < NIN; ++i) Xs[t * NIN + i] = 0.f;
+            R2[t] = r2;
+            for (int k = 0; k < NH; ++k) Z2[t * LDH + k] = d3 * w[O_W3 + k] * gelu_grad(Z2[t * LDH + k]);
         }
         __syncthreads();
-        // weight gradients (and the squared errors): sums over the tile's samples in order
-        for (int p = t; p <= NPARAM; p += TS) {
-            float g = 0.f;
-            if (p < O_B1) { // W1[k][i] = sum_s D1[s][k] * X[s][i]
-                const int k = p / NIN, i = p % NIN;
-                for (int s = 0; s < TS; ++s) g += D1[s * NH + k] * Xs[s * NIN + i];
-            } else if (p < O_W2) {
-                const int k = p - O_B1;
-                for (int s = 0; s < TS; ++s) g += D1[s * NH + k];
-            } else if (p < O_B2) { // W2[k][m] = sum_s D2[s][k] * H1[s][m]
-                const int k = (p - O_W2) / NH, m = (p - O_W2) % NH;
-                for (int s = 0; s < TS; ++s) g += D2[s * NH + k] * H1[s * NH + m];
-            } else if (p < O_W3) {
-                const int k = p - O_B2;
-                for (int s = 0; s < TS; ++s) g += D2[s * NH + k];
-            } else if (p < O_B3) {
-                const int k = p - O_W3;
-                for (int s = 0; s < TS; ++s) g += D3[s] * H2[s * NH + k];
-            } else if (p == O_B3) {
-                for (int s = 0; s < TS; ++s) g += D3[s];
-            } else {
-                for (int s = 0; s < TS; ++s) g += R2[s];
+        // dL/dz1 = (D2 W2) * gelu'(z1), in place of z1
+        {
+            float d1[2][4][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    const int s0 = 32 * wid + 16 * mt, n0 = 8 * nt;
+                    float *c = d1[mt][nt];
+                    c[0] = c[1] = c[2] = c[3] = 0.f;
+                    mma_tile<2, true>(c, lane, [&](int r, int k) { return Z2[(s0 + r) * LDH + k]; },
+                                      [&](int k, int n) { return w[O_W2 + k * NH + n0 + n]; });
+                }
+            // every warp reads only its own sample rows of Z1: no barrier between
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    const int s0 = 32 * wid + 16 * mt, n = 8 * nt + 2 * tq;
+                    const float *c = d1[mt][nt];
+                    float *z = &Z1[(s0 + g) * LDH + n];
+                    z[0] = c[0] * gelu_grad(z[0]);
+                    z[1] = c[1] * gelu_grad(z[1]);
+                    z = &Z1[(s0 + g + 8) * LDH + n];
+                    z[0] = c[2] * gelu_grad(z[0]);
+                    z[1] = c[3] * gelu_grad(z[1]);
+                }
+        }
+        __syncthreads();
+        // weight gradients over the tile: gW2 = D2^T H1 (warp w: unit rows 16 (w & 1) .. +15,
+        // n-tiles 2 (w >> 1), +1), gW1 = D1^T X (warp w: unit rows 16 (w & 1), input n-tile w >> 1)
+        {
+            const int k0 = 16 * (wid & 1);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int n0 = 8 * (2 * (wid >> 1) + j);
+                float c[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_tile<TS / 16, false>(c, lane, [&](int r, int s) { return Z2[s * LDH + k0 + r]; },
+                                         [&](int s, int n) { return H1[s * LDH + n0 + n]; });
+                const int n = n0 + 2 * tq;
+                acc[O_W2 + (k0 + g) * NH + n] += c[0];
+                acc[O_W2 + (k0 + g) * NH + n + 1] += c[1];
+                acc[O_W2 + (k0 + g + 8) * NH + n] += c[2];
+                acc[O_W2 + (k0 + g + 8) * NH + n + 1] += c[3];
             }
-            acc[p] += g;
+            const int i0 = 8 * (wid >> 1);
+            float c[4] = {0.f, 0.f, 0.f, 0.f};
+            mma_tile<TS / 16, false>(c, lane, [&](int r, int s) { return Z1[s * LDH + k0 + r]; },
+                                     [&](int s, int n) { return X[s * LDX + i0 + n]; });
+            const int i = i0 + 2 * tq;
+            if (i < NIN) {
+                acc[O_W1 + (k0 + g) * NIN + i] += c[0];
+                acc[O_W1 + (k0 + g + 8) * NIN + i] += c[2];
+            }
+            if (i + 1 < NIN) {
+                acc[O_W1 + (k0 + g) * NIN + i + 1] += c[1];
+                acc[O_W1 + (k0 + g + 8) * NIN + i + 1] += c[3];
+            }
+        }
+        // the bias gradients, the last layer's and the squared errors: sums over the tile in order
+        for (int p = t; p <= NPARAM; p += TS) {
+            float gsum = 0.f;
+            if (p >= O_B1 && p < O_W2) {
+                const int k = p - O_B1;
+                for (int s2 = 0; s2 < TS; ++s2) gsum += Z1[s2 * LDH + k];
+            } else if (p >= O_B2 && p < O_W3) {
+                const int k = p - O_B2;
+                for (int s2 = 0; s2 < TS; ++s2) gsum += Z2[s2 * LDH + k];
+            } else if (p >= O_W3 && p < O_B3) {
+                const int k = p - O_W3;
+                for (int s2 = 0; s2 < TS; ++s2) gsum += D3[s2] * H2[s2 * LDH + k];
+            } else if (p == O_B3) {
+                for (int s2 = 0; s2 < TS; ++s2) gsum += D3[s2];
+            } else if (p == NPARAM) {
+                for (int s2 = 0; s2 < TS; ++s2) gsum += R2[s2];
+            } else {
+                continue; // W1 and W2: taken by the multiplies above
+            }
+            acc[p] += gsum;
         }
         __syncthreads();
     }
@@ -1097,7 +1212,9 @@ int ark_mlp_fit_normalization(ark_mlp *M, ark_closure_data *d) {
 
 namespace {
 
-size_t grad_smem() { return sizeof(float) * (cl::NPARAM + cl::TS * cl::NIN + 4 * cl::TS * cl::NH + 2 * cl::TS + cl::NPARAM + 1); }
+size_t grad_smem() {
+    return sizeof(float) * (2 * cl::NPARAM + 1 + cl::TS * cl::LDX + 4 * cl::TS * cl::LDH + 2 * cl::TS);
+}
 
 // gradient (and summed squared error) of samples (first + q) * stride + offset, q < count,
 // with scale 2 / count, into M->grad on M->st

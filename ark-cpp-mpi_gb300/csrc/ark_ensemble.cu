@@ -300,7 +300,8 @@ int build_lists(ark_ensemble *E) {
 }
 
 // Ghost-fill jobs of every member for both level roles and face generations (the same
-// arrays and modes as Launch<float>::wrap_con / wrap_phase2).
+// arrays and modes as Launch<float>::wrap_con(with_ro = 1) / wrap_phase2(xlines = 0): the
+// ensemble's Phase2 is the three sweep kernels, whose x1 sweep reads no x ghosts).
 int build_jobs(ark_ensemble *E) {
     std::vector<WrapJob> jobs(6 * (size_t)E->n);
     for (int q = 0; q < E->n; ++q) {
@@ -313,22 +314,20 @@ int build_jobs(ark_ensemble *E) {
             wrap_add(J, L.u1, 0, cx, cz);
             wrap_add(J, L.u2, 0, cx, cz);
             wrap_add(J, L.u3, 0, cx, cz);
-            wrap_add(J, L.ro, 0, px ? GH_WRAP : GH_NONE, cz);
+            wrap_add(J, L.ro, 0, GH_NONE, cz);
             jobs[(size_t)lv * E->n + q] = J;
         }
         for (int con = 0; con < 2; ++con)
             for (int fc = 0; fc < 2; ++fc) {
                 WrapJob J = {};
                 const Level<float> Ln = S.lv[con ^ 1], Lc = S.lv[con];
-                wrap_add(J, Ln.u1, 0, cx, cz);
-                wrap_add(J, Ln.u2, 0, cx, cz);
-                wrap_add(J, Ln.u3, 0, cx, cz);
-                wrap_add(J, Ln.ro, 0, cx, cz);
-                wrap_add(J, Lc.ro, 0, px ? GH_WRAP : GH_NONE, cz);
-                const FaceSet<float> &X = S.fc[fc][0], &Z = S.fc[fc][2];
-                float *fx[4] = {X.p, X.u[0], X.u[1], X.u[2]};
+                wrap_add(J, Ln.u1, 0, GH_NONE, cz);
+                wrap_add(J, Ln.u2, 0, GH_NONE, cz);
+                wrap_add(J, Ln.u3, 0, GH_NONE, cz);
+                wrap_add(J, Ln.ro, 0, GH_NONE, cz);
+                wrap_add(J, Lc.ro, 0, GH_NONE, cz);
+                const FaceSet<float> &Z = S.fc[fc][2];
                 float *fz[4] = {Z.p, Z.u[0], Z.u[1], Z.u[2]};
-                for (int a = 0; a < 4; ++a) wrap_add(J, fx[a], 1, px ? GH_WRAP : GH_NONE, GH_NONE);
                 for (int a = 0; a < 4; ++a) wrap_add(J, fz[a], 1, GH_NONE, cz);
                 jobs[(size_t)(2 + 2 * con + fc) * E->n + q] = J;
             }

@@ -1629,8 +1629,11 @@ template <class T> __device__ __forceinline__ FaceOut<T> sweep_out(const DevStat
     return o;
 }
 
+// cf: the flag index of the cell, when its values come from another cell (the x1 sweep's ghost
+// positions, see xcell); -1: c itself
 template <class T>
-__device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, SweepIn<T> &x) {
+__device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, SweepIn<T> &x, int cf = -1) {
+    cf = ARK_CK(cf < 0 ? c : cf, R.nc);
     c = ARK_CK(c, R.nc);
     ff = ARK_CK(ff, R.nf);
     x.uN_f = R.FN[ff];
@@ -1645,7 +1648,19 @@ __device__ __forceinline__ void sweep_load(const SweepSrc<T> &R, int c, int ff, 
     x.cB = R.cB[c];
     x.nR = R.nR[c];
     x.cR = R.cR[c];
-    x.fl = R.fl[c];
+    x.fl = R.fl[cf];
+}
+
+// The x1 sweep reads its line's ghost positions from the cells and faces whose images the ghost
+// fill would copy there (k_wrap), so no ghost cell or halo face of x is read: position 0 is cell C1
+// (periodic) or 1 (bounded, zero-gradient), position C1+1 cell 1 or C1; face 0 is face C1 and face
+// C1+2 face 2 (periodic; a bounded x sweep overrides what it reads there).  The flags stay the
+// ghost cells' own (the ghost fill never copies them).
+__device__ __forceinline__ int xcell(int s, int C1, bool periodic) {
+    return s == 0 ? (periodic ? C1 : 1) : s == C1 + 1 ? (periodic ? 1 : C1) : s;
+}
+__device__ __forceinline__ int xface(int s, int C1, bool periodic) {
+    return !periodic ? s : s == 0 ? C1 : s == C1 + 2 ? 2 : s;
 }
 
 // x1 sweep: one warp per (j,k) line, lanes on consecutive cells (coalesced), marching along
@@ -1709,10 +1724,11 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     // forward face: a shuffle from the neighbouring lane, across chunks the carry from the last
     // lane, and for cell 0 of a line the face 0 itself
     RQ<T> carry_rq = {(T)0, (T)0};
+    const bool px = S.k.periodic_x;
     if (cp.li < nl) {
-        sweep_load(R, cp.c0 + cp.s, cp.f0 + cp.s + 1, cur);
-        uA_b = R.FA[ARK_CK(cp.f0 + cp.s, R.nf)];
-        uB_b = R.FB[ARK_CK(cp.f0 + cp.s, R.nf)];
+        sweep_load(R, cp.c0 + xcell(cp.s, g.C1, px), cp.f0 + xface(cp.s + 1, g.C1, px), cur, cp.c0 + cp.s);
+        uA_b = R.FA[ARK_CK(cp.f0 + xface(cp.s, g.C1, px), R.nf)];
+        uB_b = R.FB[ARK_CK(cp.f0 + xface(cp.s, g.C1, px), R.nf)];
     }
     for (int p0 = 0; p0 < total; p0 += 32) {
         const bool act = cp.li < nl;
@@ -1720,9 +1736,9 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         Pos np = cp;
         advance(np);
         if (np.li < nl) {
-            sweep_load(R, np.c0 + np.s, np.f0 + np.s + 1, nxt);
-            nuA_b = R.FA[ARK_CK(np.f0 + np.s, R.nf)];
-            nuB_b = R.FB[ARK_CK(np.f0 + np.s, R.nf)];
+            sweep_load(R, np.c0 + xcell(np.s, g.C1, px), np.f0 + xface(np.s + 1, g.C1, px), nxt, np.c0 + np.s);
+            nuA_b = R.FA[ARK_CK(np.f0 + xface(np.s, g.C1, px), R.nf)];
+            nuB_b = R.FB[ARK_CK(np.f0 + xface(np.s, g.C1, px), R.nf)];
         }
         RQ<T> rqf = {(T)0, (T)0};
         if (act) rqf = face_rq(cur.uN_f, cur.p_f, q);
@@ -1730,7 +1746,7 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         rqb.r = __shfl_up_sync(0xffffffffu, rqf.r, 1);
         rqb.q = __shfl_up_sync(0xffffffffu, rqf.q, 1);
         if (lane == 0) rqb = carry_rq;
-        if (act && s == 0) rqb = face_rq(R.FN[ARK_CK(f0, R.nf)], R.FP[ARK_CK(f0, R.nf)], q);
+        if (act && s == 0) rqb = face_rq(R.FN[ARK_CK(f0 + xface(0, g.C1, px), R.nf)], R.FP[ARK_CK(f0 + xface(0, g.C1, px), R.nf)], q);
         carry_rq.r = __shfl_sync(0xffffffffu, rqf.r, 31);
         carry_rq.q = __shfl_sync(0xffffffffu, rqf.q, 31);
         Ext<T> e = {};
@@ -1771,7 +1787,8 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         carry_u = __shfl_sync(0xffffffffu, cur.nN, 31);
         carry_fl = (uint8_t)__shfl_sync(0xffffffffu, (int)cur.fl, 31);
         if (act && s >= 1)
-            face_update<T, false>(N, W, c0 + s - 1, c0 + s, f0 + s, flb, cur.fl, ucb, cur.nN, prev, e, uA_b, uB_b, q);
+            face_update<T, false>(N, W, c0 + xcell(s - 1, g.C1, px), c0 + xcell(s, g.C1, px), f0 + s, flb, cur.fl, ucb,
+                                  cur.nN, prev, e, uA_b, uB_b, q);
         cur = nxt;
         uA_b = nuA_b;
         uB_b = nuB_b;
@@ -2084,8 +2101,9 @@ template <class T> inline void wrap_launch(const DevState<T> &S, const WrapJob &
 
 // StressTensor's exchange of u1Con, u2Con, u3Con (main.cpp:603-845): periodic axes wrap,
 // bounded x and z take the zero-gradient copy.  with_ro also fills roCon's ghosts as Phase2's
-// exchange does (main.cpp:1049-1698: wrapped on periodic axes, copied on a bounded z, left
-// alone on a bounded x), for the fused step, which reads that level before Phase2.
+// exchange does (main.cpp:1049-1698): copied or wrapped on z, for the fused step, which reads
+// that level before Phase2; on x only for the one-kernel Phase2 forms (with_ro = 2), as the x1
+// sweep kernel reads x ghost positions from the cells they stand for (xcell).
 // A slab of a z split (ext_z) leaves its z ghosts to the slab group's halo exchange.
 template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st) {
     const uint8_t ux = S.k.periodic_x ? GH_WRAP : GH_COPY;
@@ -2095,27 +2113,31 @@ template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int w
     wrap_add(J, L.u1, 0, ux, uz);
     wrap_add(J, L.u2, 0, ux, uz);
     wrap_add(J, L.u3, 0, ux, uz);
-    if (with_ro) wrap_add(J, L.ro, 0, S.k.periodic_x ? GH_WRAP : GH_NONE, uz);
+    if (with_ro) wrap_add(J, L.ro, 0, with_ro == 2 && S.k.periodic_x ? GH_WRAP : GH_NONE, uz);
     wrap_launch(S, J, st);
 }
 
 // The halo exchange before Phase2 (main.cpp:1049-1698): u?nCon and ronCon wrap or copy on
 // both axes; roCon wraps, or is copied on a bounded z only; faces normal to x1 wrap in x (a
-// bounded x sweep never reads their halo); faces normal to x3 wrap or copy in z.
-template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st) {
+// bounded x sweep never reads their halo); faces normal to x3 wrap or copy in z.  The x ghosts
+// only for the one-kernel Phase2 forms (xlines): the x1 sweep kernel reads its x ghost
+// positions from the cells and faces they stand for (xcell, xface), and no other Phase2 kernel
+// reads x ghosts.
+template <class T> void Launch<T>::wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st, int xlines) {
     const bool px = S.k.periodic_x, pz = S.k.periodic_z;
-    const uint8_t cx = px ? GH_WRAP : GH_COPY, cz = S.k.ext_z ? GH_NONE : pz ? GH_WRAP : GH_COPY;
+    const uint8_t cx = !xlines ? GH_NONE : px ? GH_WRAP : GH_COPY;
+    const uint8_t cz = S.k.ext_z ? GH_NONE : pz ? GH_WRAP : GH_COPY;
     WrapJob J = {};
     const Level<T> Ln = S.lv[con ^ 1], Lc = S.lv[con];
     wrap_add(J, Ln.u1, 0, cx, cz);
     wrap_add(J, Ln.u2, 0, cx, cz);
     wrap_add(J, Ln.u3, 0, cx, cz);
     wrap_add(J, Ln.ro, 0, cx, cz);
-    wrap_add(J, Lc.ro, 0, px ? GH_WRAP : GH_NONE, cz);
+    wrap_add(J, Lc.ro, 0, xlines && px ? GH_WRAP : GH_NONE, cz);
     const FaceSet<T> &X = S.fc[fcur][0], &Z = S.fc[fcur][2];
     T *fx[5] = {X.p, X.u[0], X.u[1], X.u[2], X.ro};
     T *fz[5] = {Z.p, Z.u[0], Z.u[1], Z.u[2], Z.ro};
-    for (int q = 0; q < 5; ++q) wrap_add(J, fx[q], 1, px ? GH_WRAP : GH_NONE, GH_NONE);
+    for (int q = 0; q < 5; ++q) wrap_add(J, fx[q], 1, xlines && px ? GH_WRAP : GH_NONE, GH_NONE);
     for (int q = 0; q < 5; ++q) wrap_add(J, fz[q], 1, GH_NONE, cz);
     wrap_launch(S, J, st);
 }

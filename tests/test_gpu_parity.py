@@ -505,7 +505,7 @@ def test_autotune_keeps_results(ark, port, prec):
         b.sync()
         ra, rb = a.download(CELLS + FACES), b.download(CELLS + FACES)
         for name in CELLS + FACES:
-            assert bits_equal(ra[name], rb[name]), name
+            assert bits_equal(port.interior(name, ra[name]), port.interior(name, rb[name])), name
 
 
 @pytest.mark.parametrize("C,px,pz", [((40, 20, 36), True, True), ((130, 9, 70), True, True), ((70, 6, 5), False, False),
@@ -534,9 +534,11 @@ def test_fused_phase2_agrees(ark, port, monkeypatch, C, px, pz):
                                      ((64, 4, 1), True, False), ((65, 31, 17), True, True), ((33, 3, 9), False, True)])
 def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
     """FP32: Phase2 and the second Phase1 in one kernel (ARK_PHASE2_FUSED=2, new level through
-    the spare buffer) give the bits of the separate kernels, ghost cells and faces included,
-    over several steps (both face generations, both buffer rotations), periodic and bounded
-    axes, ragged tiles; the per-launch timings name its five launches."""
+    the spare buffer) give the bits of the separate kernels over several steps (both face
+    generations, both buffer rotations), periodic and bounded axes, ragged tiles; the per-launch
+    timings name its five launches.  Interior cells and computed faces are compared: ghost cells
+    are each form's scratch (the separate kernels read no x ghost of the half-step level, so they
+    do not refresh them), and the state the next step reads is equal, as the later steps show."""
     p = port.channel_params(*C, seed=29)
     st0 = port.channel_state(p)
     outs = []
@@ -557,4 +559,4 @@ def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
             else:
                 assert len(names) == 8 and names[-1] == "phase1_forces"
     for n in CELLS + FACES:
-        assert bits_equal(outs[1][n], outs[0][n]), n
+        assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), n
