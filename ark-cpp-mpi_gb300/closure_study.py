@@ -256,6 +256,12 @@ def main():
                 ms += c.time_steps(min(every_c, a.coarse_steps - q))
                 stats.add(c.plane_stats())
             coarse[mode] = {"stats": stats.result(pc.ly), "gpu_ms": ms, "time": c.scalars().time - t_c0}
+            if mode == "closure":
+                # the eddy viscosity the network gives in the coarse run's last state
+                nut = c.get("nut")[1:-1, 1:-1, 1:-1] / pc.vis
+                prof = nut.mean(axis=(0, 2))
+                coarse[mode]["nut_over_nu"] = {"mean": float(nut.mean()), "max": float(nut.max()),
+                                               "mean_by_y": prof.tolist()}
     t_phys = coarse["plain"]["time"]
 
     # the fine run over the same physical time, filtered statistics ~400 times
@@ -280,12 +286,15 @@ def main():
         e = compare(coarse[mode]["stats"], fres)
         rep["assessment"][mode] = {"errors": e, "gpu_ms": coarse[mode]["gpu_ms"],
                               "gpu_time_ratio_fine_over_coarse": ms_f / coarse[mode]["gpu_ms"]}
+    rep["assessment"]["closure"]["nut_over_nu"] = coarse["closure"]["nut_over_nu"]
     rep["assessment"]["profiles"] = {
         "y_coarse": coarse["plain"]["stats"]["y"].tolist(),
         "U_fine_filtered": np.interp(coarse["plain"]["stats"]["y"], fres["y"], fres["U"]).tolist(),
         "U_plain": coarse["plain"]["stats"]["U"].tolist(), "U_closure": coarse["closure"]["stats"]["U"].tolist(),
         "uv_fine_filtered": np.interp(coarse["plain"]["stats"]["y"], fres["y"], fres["uv"]).tolist(),
-        "uv_plain": coarse["plain"]["stats"]["uv"].tolist(), "uv_closure": coarse["closure"]["stats"]["uv"].tolist()}
+        "uv_plain": coarse["plain"]["stats"]["uv"].tolist(), "uv_closure": coarse["closure"]["stats"]["uv"].tolist(),
+        "uu_fine_filtered": np.interp(coarse["plain"]["stats"]["y"], fres["y"], fres["uu"]).tolist(),
+        "uu_plain": coarse["plain"]["stats"]["uu"].tolist(), "uu_closure": coarse["closure"]["stats"]["uu"].tolist()}
     params_out, mu, sd = net.get()
     rep["network"] = {"params": params_out.tolist(), "mu": mu.tolist(), "sd": sd.tolist()}
     rep["wall_seconds"] = round(time.time() - t_start, 1)
