@@ -615,6 +615,13 @@ template <class T> __global__ void k_boundary_fill(Geom g, Level<T> L, int axis,
     }
 }
 
+// The stress's x neighbours of the edge cells, read from the cells the x ghost fill would copy
+// there: the neighbour i-1 of cell i = 1 is cell C1 (periodic) or cell 1 itself (bounded,
+// zero-gradient), the neighbour i+1 of i = C1 is cell 1 or C1.  Velocity indices only: the flags
+// stay the ghost cells' own (the ghost fill never copies flags).
+__device__ __forceinline__ int xnb_lo(int c, int i, int C1, bool periodic) { return i != 1 ? c - 1 : periodic ? c + C1 - 1 : c; }
+__device__ __forceinline__ int xnb_hi(int c, int i, int C1, bool periodic) { return i != C1 ? c + 1 : periodic ? c - C1 + 1 : c; }
+
 constexpr int kCellBX = 64, kCellBY = 2; // block shape of the one-cell-per-thread kernels
 
 // ---------------------------------------------------------------------------------------
@@ -884,14 +891,16 @@ __device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src,
                 const T uup[3] = {su1[c + cs2], su2[c + cs2], su3[c + cs2]};
                 if (fl & FL_EQ0) {
                     const int nb[4] = {c - 1, c + 1, c - cs1, c + cs1};
+                    const int nv[4] = {xnb_lo(c, i, g.C1, S.k.periodic_x), xnb_hi(c, i, g.C1, S.k.periodic_x), c - cs1,
+                                       c + cs1};
                     uint8_t fln[6];
                     T un[6][3];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         fln[q] = flags[nb[q]];
-                        un[q][0] = su1[nb[q]];
-                        un[q][1] = su2[nb[q]];
-                        un[q][2] = su3[nb[q]];
+                        un[q][0] = su1[nv[q]];
+                        un[q][1] = su2[nv[q]];
+                        un[q][2] = su3[nv[q]];
                     }
                     fln[4] = fdn;
                     fln[5] = fup;
@@ -996,14 +1005,16 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
         if (MODE & P1_STRESS) {
             if (fl & FL_EQ0) {
                 const int nb[6] = {c - 1, c + 1, c - cs1, c + cs1, c - cs2, c + cs2};
+                const int nv[6] = {xnb_lo(c, i, g.C1, S.k.periodic_x), xnb_hi(c, i, g.C1, S.k.periodic_x), c - cs1,
+                                   c + cs1, c - cs2, c + cs2};
                 uint8_t fln[6];
                 T un[6][3];
 #pragma unroll
                 for (int q = 0; q < 6; ++q) {
                     fln[q] = flags[nb[q]];
-                    un[q][0] = su1[nb[q]];
-                    un[q][1] = su2[nb[q]];
-                    un[q][2] = su3[nb[q]];
+                    un[q][0] = su1[nv[q]];
+                    un[q][1] = su2[nv[q]];
+                    un[q][2] = su3[nv[q]];
                 }
                 const T ro_cf = DEV ? kk.ro0 + ro_c : ro_c;
                 if (MODE & P1_NUT) {
@@ -1691,8 +1702,19 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     const SweepK<T> q = sweep_consts(S, 0);
     const bool bounded = !S.k.periodic_x;
     // a lane's position: line li of the group, cell s, and the line's cell / face 0 indices
+    // dc / db / df / dp: what the ghost positions add to the indices of the cell's values, its
+    // backward and forward faces and the cell behind (xcell, xface), nonzero only at s = 0, 1, C1+1
     struct Pos {
-        int li, s, c0, f0;
+        int li, s, c0, f0, dc, db, df, dp;
+    };
+    const bool px = S.k.periodic_x;
+    const int x0 = xcell(0, g.C1, px), x1 = xcell(g.C1 + 1, g.C1, px) - (g.C1 + 1);
+    auto deltas = [&](Pos &P) {
+        const bool e0 = P.s == 0, e1 = P.s == g.C1 + 1;
+        P.dc = e0 ? x0 : e1 ? x1 : 0;
+        P.db = e0 && px ? g.C1 : 0;
+        P.df = e1 && px ? -g.C1 : 0;
+        P.dp = P.s == 1 ? x0 : 0;
     };
     auto locate = [&](Pos &P) {
         const int L = first + P.li;
@@ -1709,12 +1731,14 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
             moved = true;
         }
         if (moved && P.li < nl) locate(P);
+        deltas(P);
     };
     Pos cp;
     cp.li = lane / npos;
     cp.s = lane - cp.li * npos;
     cp.c0 = cp.f0 = 0;
     if (cp.li < nl) locate(cp);
+    deltas(cp);
     Ext<T> carry = {};
     T carry_u = 0;
     uint8_t carry_fl = 0;
@@ -1724,21 +1748,20 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
     // forward face: a shuffle from the neighbouring lane, across chunks the carry from the last
     // lane, and for cell 0 of a line the face 0 itself
     RQ<T> carry_rq = {(T)0, (T)0};
-    const bool px = S.k.periodic_x;
     if (cp.li < nl) {
-        sweep_load(R, cp.c0 + xcell(cp.s, g.C1, px), cp.f0 + xface(cp.s + 1, g.C1, px), cur, cp.c0 + cp.s);
-        uA_b = R.FA[ARK_CK(cp.f0 + xface(cp.s, g.C1, px), R.nf)];
-        uB_b = R.FB[ARK_CK(cp.f0 + xface(cp.s, g.C1, px), R.nf)];
+        sweep_load(R, cp.c0 + cp.s + cp.dc, cp.f0 + cp.s + 1 + cp.df, cur, cp.c0 + cp.s);
+        uA_b = R.FA[ARK_CK(cp.f0 + cp.s + cp.db, R.nf)];
+        uB_b = R.FB[ARK_CK(cp.f0 + cp.s + cp.db, R.nf)];
     }
     for (int p0 = 0; p0 < total; p0 += 32) {
         const bool act = cp.li < nl;
-        const int s = cp.s, c0 = cp.c0, f0 = cp.f0;
+        const int s = cp.s, c0 = cp.c0, f0 = cp.f0, dc = cp.dc, db = cp.db, dp = cp.dp;
         Pos np = cp;
         advance(np);
         if (np.li < nl) {
-            sweep_load(R, np.c0 + xcell(np.s, g.C1, px), np.f0 + xface(np.s + 1, g.C1, px), nxt, np.c0 + np.s);
-            nuA_b = R.FA[ARK_CK(np.f0 + xface(np.s, g.C1, px), R.nf)];
-            nuB_b = R.FB[ARK_CK(np.f0 + xface(np.s, g.C1, px), R.nf)];
+            sweep_load(R, np.c0 + np.s + np.dc, np.f0 + np.s + 1 + np.df, nxt, np.c0 + np.s);
+            nuA_b = R.FA[ARK_CK(np.f0 + np.s + np.db, R.nf)];
+            nuB_b = R.FB[ARK_CK(np.f0 + np.s + np.db, R.nf)];
         }
         RQ<T> rqf = {(T)0, (T)0};
         if (act) rqf = face_rq(cur.uN_f, cur.p_f, q);
@@ -1746,7 +1769,7 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         rqb.r = __shfl_up_sync(0xffffffffu, rqf.r, 1);
         rqb.q = __shfl_up_sync(0xffffffffu, rqf.q, 1);
         if (lane == 0) rqb = carry_rq;
-        if (act && s == 0) rqb = face_rq(R.FN[ARK_CK(f0 + xface(0, g.C1, px), R.nf)], R.FP[ARK_CK(f0 + xface(0, g.C1, px), R.nf)], q);
+        if (act && s == 0) rqb = face_rq(R.FN[ARK_CK(f0 + db, R.nf)], R.FP[ARK_CK(f0 + db, R.nf)], q);
         carry_rq.r = __shfl_sync(0xffffffffu, rqf.r, 31);
         carry_rq.q = __shfl_sync(0xffffffffu, rqf.q, 31);
         Ext<T> e = {};
@@ -1787,8 +1810,8 @@ __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int 
         carry_u = __shfl_sync(0xffffffffu, cur.nN, 31);
         carry_fl = (uint8_t)__shfl_sync(0xffffffffu, (int)cur.fl, 31);
         if (act && s >= 1)
-            face_update<T, false>(N, W, c0 + xcell(s - 1, g.C1, px), c0 + xcell(s, g.C1, px), f0 + s, flb, cur.fl, ucb,
-                                  cur.nN, prev, e, uA_b, uB_b, q);
+            face_update<T, false>(N, W, c0 + s - 1 + dp, c0 + s + dc, f0 + s, flb, cur.fl, ucb, cur.nN, prev, e, uA_b,
+                                  uB_b, q);
         cur = nxt;
         uA_b = nuA_b;
         uB_b = nuB_b;
@@ -2105,8 +2128,8 @@ template <class T> inline void wrap_launch(const DevState<T> &S, const WrapJob &
 // that level before Phase2; on x only for the one-kernel Phase2 forms (with_ro = 2), as the x1
 // sweep kernel reads x ghost positions from the cells they stand for (xcell).
 // A slab of a z split (ext_z) leaves its z ghosts to the slab group's halo exchange.
-template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st) {
-    const uint8_t ux = S.k.periodic_x ? GH_WRAP : GH_COPY;
+template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st, int xlines) {
+    const uint8_t ux = !xlines ? GH_NONE : S.k.periodic_x ? GH_WRAP : GH_COPY;
     const uint8_t uz = S.k.ext_z ? GH_NONE : S.k.periodic_z ? GH_WRAP : GH_COPY;
     WrapJob J = {};
     const Level<T> L = S.lv[con];
