@@ -366,9 +366,7 @@ template <class T> struct EngineT : Engine {
         const int xg = ctx->p2mode != 0 ? 1 : 0;
         Launch<T>::finalize_dt(S, 1, st);
         mark(0);
-        // the face-centric FP64 Phase1 and the one-kernel Phase2 forms read the velocities' x
-        // ghosts; the other Phase1 kernels read the cells they stand for
-        Launch<T>::wrap_con(S, y, xg ? 2 : 1, st, xg || ctx->march[0] == 3 ? 1 : 0);
+        Launch<T>::wrap_con(S, y, xg ? 2 : 1, st);
         mark(1);
         if (ctx->closure_net) cudaStreamWaitEvent(st, ctx->join, 0);
         Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st);

@@ -96,14 +96,12 @@ __global__ void __launch_bounds__(kTileX *kTileY) kb_reduce(const DS *__restrict
     }
 }
 
-// jobs[q]: member q's ghost-fill job; threads of a block cover 128 plane points of its z ghost
-// lines (the members' kernels read no x ghost of the filled arrays)
+// jobs[q]: member q's ghost-fill job; threads of a block cover 128 plane points
 __global__ void __launch_bounds__(128) kb_wrap(const DS *__restrict__ inst, const WrapJob *__restrict__ jobs, WorkList W) {
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
         const BIx bx = decode(W, q, b);
-        const Geom &g = inst[q].g;
-        wrap_body_lines<float>(g, jobs[q], g.C2 * g.C3 + bx.x * 128 + (int)threadIdx.x);
+        wrap_body_lines<float>(inst[q].g, jobs[q], bx.x * 128 + (int)threadIdx.x);
     }
 }
 
@@ -273,8 +271,8 @@ int build_lists(ark_ensemble *E) {
                 gx = col_sweep_blocks(g, 2), gz = (g.C3 + 1 + seg - 1) / seg;
                 break;
             }
-            case WL_WRAP: { // one thread per z ghost line (the only ones filled), looping over the job's arrays
-                const int64_t tot = (int64_t)g.C1 * g.C2;
+            case WL_WRAP: { // one thread per ghost line, looping over the job's arrays
+                const int64_t tot = (int64_t)g.C2 * g.C3 + (int64_t)g.C1 * g.C2;
                 gx = (int)((tot + 127) / 128);
                 break;
             }
@@ -302,20 +300,20 @@ int build_lists(ark_ensemble *E) {
 }
 
 // Ghost-fill jobs of every member for both level roles and face generations (the same
-// arrays and modes as Launch<float>::wrap_con(with_ro = 1, xlines = 0) / wrap_phase2(xlines =
-// 0): the ensemble's Phase1 kernels read the stress's x neighbours, and its x1 sweep its x ghost
-// positions, from the cells they stand for, so only the z planes are filled).
+// arrays and modes as Launch<float>::wrap_con(with_ro = 1) / wrap_phase2(xlines = 0): the
+// ensemble's Phase2 is the three sweep kernels, whose x1 sweep reads no x ghosts).
 int build_jobs(ark_ensemble *E) {
     std::vector<WrapJob> jobs(6 * (size_t)E->n);
     for (int q = 0; q < E->n; ++q) {
         const DS &S = E->S[q];
-        const uint8_t cz = S.k.periodic_z ? GH_WRAP : GH_COPY;
+        const bool px = S.k.periodic_x, pz = S.k.periodic_z;
+        const uint8_t cx = px ? GH_WRAP : GH_COPY, cz = pz ? GH_WRAP : GH_COPY;
         for (int lv = 0; lv < 2; ++lv) {
             WrapJob J = {};
             const Level<float> L = S.lv[lv];
-            wrap_add(J, L.u1, 0, GH_NONE, cz);
-            wrap_add(J, L.u2, 0, GH_NONE, cz);
-            wrap_add(J, L.u3, 0, GH_NONE, cz);
+            wrap_add(J, L.u1, 0, cx, cz);
+            wrap_add(J, L.u2, 0, cx, cz);
+            wrap_add(J, L.u3, 0, cx, cz);
             wrap_add(J, L.ro, 0, GH_NONE, cz);
             jobs[(size_t)lv * E->n + q] = J;
         }

@@ -615,13 +615,6 @@ template <class T> __global__ void k_boundary_fill(Geom g, Level<T> L, int axis,
     }
 }
 
-// The stress's x neighbours of the edge cells, read from the cells the x ghost fill would copy
-// there: the neighbour i-1 of cell i = 1 is cell C1 (periodic) or cell 1 itself (bounded,
-// zero-gradient), the neighbour i+1 of i = C1 is cell 1 or C1.  Velocity indices only: the flags
-// stay the ghost cells' own (the ghost fill never copies flags).
-__device__ __forceinline__ int xnb_lo(int c, int i, int C1, bool periodic) { return i != 1 ? c - 1 : periodic ? c + C1 - 1 : c; }
-__device__ __forceinline__ int xnb_hi(int c, int i, int C1, bool periodic) { return i != C1 ? c + 1 : periodic ? c - C1 + 1 : c; }
-
 constexpr int kCellBX = 64, kCellBY = 2; // block shape of the one-cell-per-thread kernels
 
 // ---------------------------------------------------------------------------------------
@@ -891,16 +884,14 @@ __device__ __forceinline__ void phase1_march_body(const DevState<T> &S, int src,
                 const T uup[3] = {su1[c + cs2], su2[c + cs2], su3[c + cs2]};
                 if (fl & FL_EQ0) {
                     const int nb[4] = {c - 1, c + 1, c - cs1, c + cs1};
-                    const int nv[4] = {xnb_lo(c, i, g.C1, S.k.periodic_x), xnb_hi(c, i, g.C1, S.k.periodic_x), c - cs1,
-                                       c + cs1};
                     uint8_t fln[6];
                     T un[6][3];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         fln[q] = flags[nb[q]];
-                        un[q][0] = su1[nv[q]];
-                        un[q][1] = su2[nv[q]];
-                        un[q][2] = su3[nv[q]];
+                        un[q][0] = su1[nb[q]];
+                        un[q][1] = su2[nb[q]];
+                        un[q][2] = su3[nb[q]];
                     }
                     fln[4] = fdn;
                     fln[5] = fup;
@@ -1005,16 +996,14 @@ __device__ __forceinline__ void phase1_cell_body(const DevState<T> &S, int src, 
         if (MODE & P1_STRESS) {
             if (fl & FL_EQ0) {
                 const int nb[6] = {c - 1, c + 1, c - cs1, c + cs1, c - cs2, c + cs2};
-                const int nv[6] = {xnb_lo(c, i, g.C1, S.k.periodic_x), xnb_hi(c, i, g.C1, S.k.periodic_x), c - cs1,
-                                   c + cs1, c - cs2, c + cs2};
                 uint8_t fln[6];
                 T un[6][3];
 #pragma unroll
                 for (int q = 0; q < 6; ++q) {
                     fln[q] = flags[nb[q]];
-                    un[q][0] = su1[nv[q]];
-                    un[q][1] = su2[nv[q]];
-                    un[q][2] = su3[nv[q]];
+                    un[q][0] = su1[nb[q]];
+                    un[q][1] = su2[nb[q]];
+                    un[q][2] = su3[nb[q]];
                 }
                 const T ro_cf = DEV ? kk.ro0 + ro_c : ro_c;
                 if (MODE & P1_NUT) {
@@ -2128,8 +2117,8 @@ template <class T> inline void wrap_launch(const DevState<T> &S, const WrapJob &
 // that level before Phase2; on x only for the one-kernel Phase2 forms (with_ro = 2), as the x1
 // sweep kernel reads x ghost positions from the cells they stand for (xcell).
 // A slab of a z split (ext_z) leaves its z ghosts to the slab group's halo exchange.
-template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st, int xlines) {
-    const uint8_t ux = !xlines ? GH_NONE : S.k.periodic_x ? GH_WRAP : GH_COPY;
+template <class T> void Launch<T>::wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st) {
+    const uint8_t ux = S.k.periodic_x ? GH_WRAP : GH_COPY;
     const uint8_t uz = S.k.ext_z ? GH_NONE : S.k.periodic_z ? GH_WRAP : GH_COPY;
     WrapJob J = {};
     const Level<T> L = S.lv[con];

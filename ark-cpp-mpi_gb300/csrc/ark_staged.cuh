@@ -330,16 +330,10 @@ __device__ __forceinline__ void phase1_staged_body(const DevState<float> &S, int
                     fln[3] = flm[off_flag<MODE>(cr + 1, cx)];
                     fln[4] = fld[off_flag<MODE>(cr, cx)];
                     fln[5] = flu[off_flag<MODE>(cr, cx)];
-                    // the x neighbours of the row's edge cells from the cells the x ghost fill would
-                    // copy there (xnb_lo, xnb_hi): the other end of the row (periodic) or the cell
-                    // itself (bounded)
-                    const bool px = S.k.periodic_x;
-                    const Level<T> Ls = S.lv[src];
 #pragma unroll
                     for (int m = 0; m < 3; ++m) {
-                        const T *su = m == 0 ? Ls.u1 : m == 1 ? Ls.u2 : Ls.u3;
-                        un[0][m] = i != 1 ? fm[off_cu<MODE>(m, cr, cx - 1)] : px ? su[c + g.C1 - 1] : uc[m];
-                        un[1][m] = i != g.C1 ? fm[off_cu<MODE>(m, cr, cx + 1)] : px ? su[c - g.C1 + 1] : uc[m];
+                        un[0][m] = fm[off_cu<MODE>(m, cr, cx - 1)];
+                        un[1][m] = fm[off_cu<MODE>(m, cr, cx + 1)];
                         un[2][m] = fm[off_cu<MODE>(m, cr - 1, cx)];
                         un[3][m] = fm[off_cu<MODE>(m, cr + 1, cx)];
                         un[4][m] = fd[off_cu<MODE>(m, cr, cx)];

@@ -291,10 +291,8 @@ enum Phase1Mode { P1_PLAIN = 0, P1_STRESS = 1, P1_FORCES = 2, P1_BULK = 4, P1_RM
 template <class T> struct Launch {
     static void reduce_start(const DevState<T> &S, int con, cudaStream_t st);
     static void finalize_dt(const DevState<T> &S, int advance_time, cudaStream_t st);
-    // with_ro: 1 also roCon on z, 2 on x and z (for the one-kernel Phase2 forms); xlines = 0: no
-    // x ghosts of the velocities (the one-cell, marching and staged Phase1 kernels read the stress's
-    // x neighbours from the cells they stand for)
-    static void wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st, int xlines = 1);
+    // with_ro: 1 also roCon on z, 2 on x and z (for the one-kernel Phase2 forms)
+    static void wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st);
     // xlines: also the x ghosts (the one-kernel Phase2 forms read them; the x1 sweep does not)
     static void wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st, int xlines = 0);
     static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st);
