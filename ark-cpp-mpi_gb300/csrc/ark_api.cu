@@ -168,6 +168,12 @@ extern "C" int ark_bounds_check(int reset, long long *out) {
 
 namespace {
 
+// up to four destinations of get_block
+template <class T> struct U_ptrs {
+    T **p[4];
+    T **&operator[](int q) { return p[q]; }
+};
+
 template <class T> struct EngineT : Engine {
     ark_ctx *ctx;
     DevState<T> S;
@@ -188,31 +194,31 @@ template <class T> struct EngineT : Engine {
         return ARK_OK;
     }
 
+    // n arrays of `each` elements in one allocation, array q at out[q] = base + q * each (the
+    // staged Phase1 reads a level's four arrays, a face set's four or the three forces as one
+    // 4-D tensor: arrays a fixed stride apart)
+    int get_block(U_ptrs<T> out, int n, size_t each) {
+        T *base = nullptr;
+        if (int rc = get(&base, each * n)) return rc;
+        for (int q = 0; q < n; ++q) *out[q] = base + each * q;
+        return ARK_OK;
+    }
+
     int alloc() override {
         S.g = ctx->g;
         S.k = ctx->k;
         const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
         int rc = 0;
-        for (int l = 0; l < 2; ++l) {
-            rc |= get(&S.lv[l].ro, nc);
-            rc |= get(&S.lv[l].u1, nc);
-            rc |= get(&S.lv[l].u2, nc);
-            rc |= get(&S.lv[l].u3, nc);
-        }
-        if (Storage<T>::deviation) { // FP32: the level the one-kernel Phase2 + second Phase1 writes
-            rc |= get(&S.spare.ro, nc);
-            rc |= get(&S.spare.u1, nc);
-            rc |= get(&S.spare.u2, nc);
-            rc |= get(&S.spare.u3, nc);
-        }
-        for (int m = 0; m < 3; ++m) rc |= get(&S.f[m], nc);
+        for (int l = 0; l < 2; ++l) rc |= get_block({&S.lv[l].ro, &S.lv[l].u1, &S.lv[l].u2, &S.lv[l].u3}, 4, nc);
+        if (Storage<T>::deviation) // FP32: the level the one-kernel Phase2 + second Phase1 writes
+            rc |= get_block({&S.spare.ro, &S.spare.u1, &S.spare.u2, &S.spare.u3}, 4, nc);
+        rc |= get_block({&S.f[0], &S.f[1], &S.f[2], nullptr}, 3, nc);
         for (int gen = 0; gen < 2; ++gen)
             for (int d = 0; d < 3; ++d) {
                 FaceSet<T> &F = S.fc[gen][d];
-                rc |= get(&F.p, nf);
+                rc |= get_block({&F.p, &F.u[0], &F.u[1], &F.u[2]}, 4, nf);
                 if (Storage<T>::deviation) F.ro = nullptr; // derived from p
                 else rc |= get(&F.ro, nf);
-                for (int m = 0; m < 3; ++m) rc |= get(&F.u[m], nf);
             }
         for (int d = 0; d < 3; ++d)
             for (int m = 0; m < 3; ++m) {
@@ -574,15 +580,18 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
         return nullptr;
     }
     // Phase1 kernel shapes measured fastest on GB300 at the benchmark sizes: FP32 stages its
-    // planes in shared memory (0.76 vs 1.10 ms marching and 0.61 vs 0.70 ms one cell per
-    // thread at 512x256x256); FP64 computes each face's quantities once (1.94 vs 2.37 ms and
-    // 1.10 vs 1.18 ms one cell per thread at 256x128x128).  ark_autotune picks per grid.
-    ctx->march[0] = params->precision == ARK_FP32 ? 2 : 3;
-    ctx->march[1] = params->precision == ARK_FP32 ? 2 : 3;
+    // planes in shared memory with TMA tensor copies (Phase1 + stress 0.558 ms against 0.611
+    // with cp.async copies, 0.70 one cell per thread and 1.10 marching at 512x256x256; second
+    // Phase1 0.507 against 0.540); FP64 computes each face's quantities once (1.94 vs 2.37 ms
+    // and 1.10 vs 1.18 ms one cell per thread at 256x128x128).  ark_autotune picks per grid.
+    ctx->march[0] = params->precision == ARK_FP32 ? 4 : 3;
+    ctx->march[1] = params->precision == ARK_FP32 ? 4 : 3;
     if (const char *e = std::getenv("ARK_PHASE1_MARCH")) { // "ab": a for Phase1 with stress, b without
-        // 0: one cell per thread, 1: marching, 2: planes staged in shared memory (FP32 only)
-        // 3: face quantities computed once (FP64 only)
-        auto ok = [&](char ch) { return ch >= '0' && ch <= '1' ? true : (params->precision == ARK_FP32 ? ch == '2' : ch == '3'); };
+        // 0: one cell per thread, 1: marching, 2: planes staged in shared memory (FP32 only),
+        // 3: face quantities computed once (FP64 only), 4: staged with TMA copies (FP32 only)
+        auto ok = [&](char ch) {
+            return ch >= '0' && ch <= '1' ? true : (params->precision == ARK_FP32 ? ch == '2' || ch == '4' : ch == '3');
+        };
         if (ok(e[0])) ctx->march[0] = e[0] - '0';
         if (e[0] && ok(e[1])) ctx->march[1] = e[1] - '0';
     }
@@ -868,6 +877,7 @@ int ark_sync(ark_ctx *ctx) {
     int status = 0;
     ARK_CUDA(cudaMemcpy(&status, &ctx->eng->scalars()->status, sizeof(int), cudaMemcpyDeviceToHost));
     if (status & STATUS_NONFINITE) return fail(ARK_ERR_NONFINITE, "non-finite velocity detected on the device");
+    if (status & STATUS_STAGING) return fail(ARK_ERR_CUDA, "a staged Phase1 block gave up waiting for its TMA copies");
     return ARK_OK;
 }
 
@@ -1235,9 +1245,10 @@ extern "C" {
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (steps_per_candidate < 1) return fail(ARK_ERR_PARAM, "steps_per_candidate < 1");
-    // Phase1 shapes: one cell per thread, marching, and the precision's own (staged for FP32,
-    // face-centric for FP64)
-    const int shapes[3] = {0, 1, ctx->P.precision == ARK_FP32 ? 2 : 3};
+    // Phase1 shapes: one cell per thread, marching, and the precision's own (staged with
+    // cp.async or TMA copies for FP32, face-centric for FP64)
+    const bool fp32 = ctx->P.precision == ARK_FP32;
+    const int shapes[4] = {0, 1, fp32 ? 2 : 3, 4};
     // best of three timings of steps_per_candidate steps each
     auto measure = [&](double *us) -> int {
         ARK_CUDA(cudaStreamSynchronize(ctx->st));
@@ -1258,7 +1269,6 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         else if (which == 2) ctx->p2mode = v;
         else ctx->seg_target = v;
     };
-    const bool fp32 = ctx->P.precision == ARK_FP32;
     for (int which = 0; which < 4; ++which) {
         const int segs[4] = {8, 16, 32, 64};
         // Phase2 forms: the three sweep kernels, or (FP32) one kernel for the sweeps and the
@@ -1266,7 +1276,7 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         // size measured: left to ARK_PHASE2_FUSED=1, not tried here.
         const int p2cand[2] = {0, 2};
         if (which == 2 && !fp32) continue;
-        const int ncand = which < 2 ? 3 : which == 2 ? 2 : 4;
+        const int ncand = which < 2 ? (fp32 ? 4 : 3) : which == 2 ? 2 : 4;
         int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : ctx->seg_target;
         if (which == 3 && ctx->p2mode) continue; // the one-kernel forms have no segments
         for (int c = 0; c < ncand; ++c) {

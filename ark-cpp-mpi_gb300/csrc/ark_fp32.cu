@@ -22,6 +22,46 @@ namespace {
 constexpr long long kSpan = 1ll << 40;
 enum { A_CU = 0, A_CR = 3, A_FL = 4, A_FC = 5, A_FF = 17, A_N = 20 };
 
+// Array numbers of the fake bases: u1 (u2, u3 follow), ro, flags, faces (12 follow), forces.
+struct Ids {
+    int cu, cr, fl, fc, ff;
+};
+
+// Every shared-memory read a thread of tile column (tx, ty) makes for cell (i, j, k) of a
+// staged Phase1 with stage layout L, as want(plane, stage byte, bytes, expected address of the
+// first byte); addr(a, e, elem) is the fake address of element e of array a.
+template <int MODE, class L, class Want, class Addr>
+void staged_reads(const Geom &g, const Ids &id, Want &&want, Addr &&addr, int tx, int ty, int i, int j, int k) {
+    const int cr = ty - L::CROW0, cx = tx + 1;
+    auto cell = [&](int ii, int jj, int kk) { return g.cell(ii, jj, kk); };
+    auto face = [&](int ii, int jj, int kk) { return g.face(ii, jj, kk); };
+    want(k, L::flag(cr, cx), 1, addr(id.fl, cell(i, j, k), 1));
+    want(k, L::ro(ty, cx) * 4, 4, addr(id.cr, cell(i, j, k), 4));
+    for (int m = 0; m < 3; ++m) want(k, L::cu(m, cr, cx) * 4, 4, addr(id.cu + m, cell(i, j, k), 4));
+    for (int a = 0; a < 4; ++a) {
+        want(k, L::face(0, a, ty, cx) * 4, 4, addr(id.fc + a, face(i, j, k), 4));
+        want(k, L::face(0, a, ty, cx + 1) * 4, 4, addr(id.fc + a, face(i + 1, j, k), 4));
+        want(k, L::face(1, a, ty, cx) * 4, 4, addr(id.fc + 4 + a, face(i, j, k), 4));
+        want(k, L::face(1, a, ty + 1, cx) * 4, 4, addr(id.fc + 4 + a, face(i, j + 1, k), 4));
+        want(k, L::face(2, a, ty, cx) * 4, 4, addr(id.fc + 8 + a, face(i, j, k), 4));
+        want(k + 1, L::face(2, a, ty, cx) * 4, 4, addr(id.fc + 8 + a, face(i, j, k + 1), 4));
+    }
+    if (L::STRESS) {
+        const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
+        for (int q = 0; q < 4; ++q) {
+            want(k, L::flag(cr + dj[q], cx + di[q]), 1, addr(id.fl, cell(i + di[q], j + dj[q], k), 1));
+            for (int m = 0; m < 3; ++m)
+                want(k, L::cu(m, cr + dj[q], cx + di[q]) * 4, 4, addr(id.cu + m, cell(i + di[q], j + dj[q], k), 4));
+        }
+        for (int dk = -1; dk <= 1; dk += 2) {
+            want(k + dk, L::flag(cr, cx), 1, addr(id.fl, cell(i, j, k + dk), 1));
+            for (int m = 0; m < 3; ++m) want(k + dk, L::cu(m, cr, cx) * 4, 4, addr(id.cu + m, cell(i, j, k + dk), 4));
+        }
+    }
+    if (L::FIN)
+        for (int m = 0; m < 3; ++m) want(k, L::ff(m, ty, cx) * 4, 4, addr(id.ff + m, cell(i, j, k), 4));
+}
+
 template <int MODE> struct PlanCheck {
     using L = stg::Layout<MODE>;
     const Geom g;
@@ -124,38 +164,114 @@ template <int MODE> struct PlanCheck {
     }
     void reads(const std::vector<std::vector<long long>> &map, int pfirst, int bx, int by, int tx, int ty, int i, int j,
                int k) {
-        const int cr = ty - L::CROW0, cx = tx + 1;
-        auto cell = [&](int ii, int jj, int kk) { return g.cell(ii, jj, kk); };
-        auto face = [&](int ii, int jj, int kk) { return g.face(ii, jj, kk); };
-        want(map, pfirst, bx, by, k, stg::off_flag<MODE>(cr, cx), 1, addr(A_FL, cell(i, j, k), 1));
-        want(map, pfirst, bx, by, k, stg::off_cr<MODE>(ty, cx) * 4, 4, addr(A_CR, cell(i, j, k), 4));
-        for (int m = 0; m < 3; ++m) want(map, pfirst, bx, by, k, stg::off_cu<MODE>(m, cr, cx) * 4, 4, addr(A_CU + m, cell(i, j, k), 4));
-        for (int a = 0; a < 4; ++a) {
-            want(map, pfirst, bx, by, k, stg::off_face<MODE>(0, a, ty, cx) * 4, 4, addr(A_FC + a, face(i, j, k), 4));
-            want(map, pfirst, bx, by, k, stg::off_face<MODE>(0, a, ty, cx + 1) * 4, 4, addr(A_FC + a, face(i + 1, j, k), 4));
-            want(map, pfirst, bx, by, k, stg::off_face<MODE>(1, a, ty, cx) * 4, 4, addr(A_FC + 4 + a, face(i, j, k), 4));
-            want(map, pfirst, bx, by, k, stg::off_face<MODE>(1, a, ty + 1, cx) * 4, 4, addr(A_FC + 4 + a, face(i, j + 1, k), 4));
-            want(map, pfirst, bx, by, k, stg::off_face<MODE>(2, a, ty, cx) * 4, 4, addr(A_FC + 8 + a, face(i, j, k), 4));
-            want(map, pfirst, bx, by, k + 1, stg::off_face<MODE>(2, a, ty, cx) * 4, 4, addr(A_FC + 8 + a, face(i, j, k + 1), 4));
+        const Ids id = {A_CU, A_CR, A_FL, A_FC, A_FF};
+        staged_reads<MODE, L>(
+            g, id, [&](int p, int off, int nb, long long e) { want(map, pfirst, bx, by, p, off, nb, e); }, addr, tx, ty, i, j, k);
+    }
+};
+
+// The TMA form's plan, checked the same way: the boxes of tma_boxes (from fake bases whose
+// blocks of arrays are a fixed stride apart) are expanded byte by byte as the copy engine
+// lays them out (rows past a block's last row as zero fill), with the tensor copies' rules
+// checked (16-byte global strides, x offsets and box rows; 128-byte aligned destinations; box
+// sizes at most 256), then every read of every thread as above.
+template <int MODE> struct TmaCheck {
+    using L = stg::TLayout<MODE>;
+    static constexpr long long kS = 1ll << 36; // fake array spacing (tensor-map strides stay below 2^40)
+    enum { T_CR = 0, T_CU = 1, T_FL = 4, T_FC = 5, T_FF = 17, T_N = 20 };
+    const Geom g;
+    std::string err;
+    int bad = 0;
+    explicit TmaCheck(const Geom &gg) : g(gg) {}
+    void fail(const char *what, int bx, int by, int p, long long x) {
+        if (bad++ == 0) {
+            char b[256];
+            std::snprintf(b, sizeof b, "TMA mode %d tile (%d,%d) plane %d: %s (%lld)", MODE, bx, by, p, what, x);
+            err = b;
         }
-        if (L::STRESS) {
-            const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
-            for (int q = 0; q < 4; ++q) {
-                want(map, pfirst, bx, by, k, stg::off_flag<MODE>(cr + dj[q], cx + di[q]), 1,
-                     addr(A_FL, cell(i + di[q], j + dj[q], k), 1));
-                for (int m = 0; m < 3; ++m)
-                    want(map, pfirst, bx, by, k, stg::off_cu<MODE>(m, cr + dj[q], cx + di[q]) * 4, 4,
-                         addr(A_CU + m, cell(i + di[q], j + dj[q], k), 4));
-            }
-            for (int dk = -1; dk <= 1; dk += 2) {
-                want(map, pfirst, bx, by, k + dk, stg::off_flag<MODE>(cr, cx), 1, addr(A_FL, cell(i, j, k + dk), 1));
-                for (int m = 0; m < 3; ++m)
-                    want(map, pfirst, bx, by, k + dk, stg::off_cu<MODE>(m, cr, cx) * 4, 4, addr(A_CU + m, cell(i, j, k + dk), 4));
-            }
+    }
+    static long long addr(int a, long long e, int elem) { return a * kS + e * elem; }
+    void run(int kch) {
+        stg::Bases b;
+        b.cr = (const void *)(T_CR * kS);
+        for (int m = 0; m < 3; ++m) b.cu[m] = (const void *)((T_CU + m) * kS);
+        b.fl = (const void *)(T_FL * kS);
+        for (int d = 0; d < 3; ++d)
+            for (int a = 0; a < 4; ++a) b.fc[d][a] = (const void *)((T_FC + 4 * d + a) * kS);
+        for (int m = 0; m < 3; ++m) b.ff[m] = (const void *)((T_FF + m) * kS);
+        stg::TmaBox B[stg::kMaxBoxes];
+        const int n = stg::tma_boxes<MODE>(B, g, b);
+        if (n <= 0) {
+            fail("no TMA plan for these arrays", 0, 0, 0, n);
+            return;
         }
-        if (L::FIN)
-            for (int m = 0; m < 3; ++m)
-                want(map, pfirst, bx, by, k, stg::off_ff<MODE>(m, ty, cx) * 4, 4, addr(A_FF + m, cell(i, j, k), 4));
+        for (int q = 0; q < n; ++q) {
+            const stg::TmaBox &x = B[q];
+            if ((long long)x.box[0] * x.elem % 16) fail("box row not a multiple of 16 bytes", 0, 0, 0, q);
+            for (int d = 0; d < 4; ++d)
+                if (x.box[d] < 1 || x.box[d] > 256) fail("box size outside 1..256", 0, 0, 0, q);
+            for (int d = 0; d < 3; ++d)
+                if (x.stride[d] % 16 || x.stride[d] >= (1ll << 40)) fail("global stride", 0, 0, 0, q);
+            if (x.dst % 128) fail("destination not 128-byte aligned", 0, 0, 0, q);
+            if (x.dst + stg::box_bytes(x) > (unsigned)L::STAGE) fail("box outside its stage", 0, 0, 0, q);
+        }
+        const dim3 grid = stg::staged_grid(g, kch);
+        std::vector<std::vector<long long>> map;
+        for (int bz = 0; bz < (int)grid.z; ++bz)
+            for (int by = 0; by < (int)grid.y; ++by)
+                for (int bx = 0; bx < (int)grid.x; ++bx) {
+                    const int k0 = bz * kch + 1, k1 = std::min(k0 + kch - 1, g.C3);
+                    const int pfirst = L::STRESS ? k0 - 1 : k0, plast = k1 + 1;
+                    const int x0 = bx * stg::SX, j0 = by * stg::SY + 1;
+                    if ((long long)x0 * 4 % 16) fail("x offset not a multiple of 16 bytes", bx, by, 0, x0);
+                    map.assign(plast - pfirst + 1, std::vector<long long>(L::STAGE, -1));
+                    for (int p = pfirst; p <= plast; ++p) {
+                        const unsigned kind = p < k0 ? stg::DOWN : (p > k1 ? stg::TOP : stg::MID);
+                        std::vector<long long> &M = map[p - pfirst];
+                        for (int q = 0; q < n; ++q) {
+                            const stg::TmaBox &x = B[q];
+                            if (!(x.when & kind)) continue;
+                            if (p < 0 || p >= x.dim[2]) fail("plane outside its array", bx, by, p, q);
+                            if (j0 + x.row0 < 0) fail("box starts at a negative row", bx, by, p, q);
+                            if (x0 + x.box[0] > x.dim[0]) fail("box leaves its row", bx, by, p, q);
+                            for (int a = 0; a < x.box[3]; ++a)
+                                for (int r = 0; r < x.box[1]; ++r)
+                                    for (int e = 0; e < x.box[0]; ++e) {
+                                        const long long y = j0 + x.row0 + r;
+                                        const long long dst = x.dst + ((long long)(a * x.box[1] + r) * x.box[0] + e) * x.elem;
+                                        const long long src = (long long)x.base + a * x.stride[2] + p * x.stride[1] +
+                                                              y * x.stride[0] + (long long)(x0 + e) * x.elem;
+                                        for (int c = 0; c < x.elem; ++c) {
+                                            if (dst + c >= L::STAGE) continue;
+                                            if (M[dst + c] != -1) fail("two boxes into one byte", bx, by, p, dst + c);
+                                            M[dst + c] = y < x.dim[1] ? src + c : -2;
+                                        }
+                                    }
+                        }
+                    }
+                    for (int ty = 0; ty < stg::SY; ++ty)
+                        for (int tx = 0; tx < stg::SX; ++tx) {
+                            const int i = bx * stg::SX + tx + 1, j = by * stg::SY + ty + 1;
+                            if (i > g.C1 || j > g.C2) continue;
+                            const Ids id = {T_CU, T_CR, T_FL, T_FC, T_FF};
+                            for (int k = k0; k <= k1; ++k)
+                                staged_reads<MODE, L>(
+                                    g, id,
+                                    [&](int p, int off, int nb, long long want) {
+                                        if (p - pfirst < 0 || p - pfirst >= (int)map.size()) {
+                                            fail("read of a plane not staged", bx, by, p, off);
+                                            return;
+                                        }
+                                        const std::vector<long long> &M = map[p - pfirst];
+                                        for (int y = 0; y < nb; ++y)
+                                            if (off + y >= L::STAGE || M[off + y] != want + y) {
+                                                fail("shared-memory read maps to the wrong element", bx, by, p, off);
+                                                return;
+                                            }
+                                    },
+                                    addr, tx, ty, i, j, k);
+                        }
+                }
     }
 };
 
@@ -341,11 +457,19 @@ int staging_plan_check(int C1, int C2, int C3, int kch_in, char *msg, int cap) {
     b.run(kch);
     PlanCheck<P1_FORCES | P1_RSUM> c(g);
     c.run(kch);
+    TmaCheck<P1_STRESS | P1_FORCES | P1_RMAX> ta(g);
+    ta.run(kch);
+    TmaCheck<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX> tb(g);
+    tb.run(kch);
+    TmaCheck<P1_FORCES | P1_RSUM> tc(g);
+    tc.run(kch);
     char m2[256] = {0};
     const int d = step2_plan_check(C1, C2, C3, kch_in, m2, (int)sizeof m2);
-    const std::string e = !a.err.empty() ? a.err : (!b.err.empty() ? b.err : (!c.err.empty() ? c.err : std::string(m2)));
+    std::string e = std::string(m2);
+    for (const std::string *x : {&tc.err, &tb.err, &ta.err, &c.err, &b.err, &a.err})
+        if (!x->empty()) e = *x;
     if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", e.c_str());
-    return a.bad + b.bad + c.bad + d;
+    return a.bad + b.bad + c.bad + ta.bad + tb.bad + tc.bad + d;
 }
 
 } // namespace ark

@@ -21,6 +21,8 @@
 //   k_boundary_fill                  BoundaryConditions (source/BoundaryConditions.cpp:22-83)
 #pragma once
 #include <cstdint>
+#include <cstring>
+#include <cuda.h> // CUtensorMap and its enums (types only: the encoder comes through the runtime)
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -2256,6 +2258,17 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
             case P1_FORCES | P1_RSUM: stg::launch_staged<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st); return;
             default: march = 0; break;
             }
+        } else if (march == 4) {
+            switch (mode) {
+            case P1_STRESS | P1_FORCES | P1_RMAX:
+                stg::launch_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX>(S, src, dst, fcur, st);
+                return;
+            case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
+                stg::launch_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(S, src, dst, fcur, st);
+                return;
+            case P1_FORCES | P1_RSUM: stg::launch_staged_tma<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st); return;
+            default: march = 0; break;
+            }
         }
     }
     if (march == 1)
@@ -2277,6 +2290,9 @@ template <class T> void Launch<T>::prepare() {
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_RMAX>();
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>();
         stg::prepare_staged<P1_FORCES | P1_RSUM>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>();
+        stg::prepare_staged_tma<P1_FORCES | P1_RSUM>();
         s2::prepare<float>();
     }
 }

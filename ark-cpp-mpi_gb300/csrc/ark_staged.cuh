@@ -9,6 +9,12 @@
 // computed, so the block keeps many more bytes in flight than kernels that load their operands
 // into registers themselves.  The arithmetic is the same half_step / stress_force / UseForces
 // code, in the same order, as k_phase1 and k_phase1_cell, so all three give the same bits.
+//
+// The TMA form (k_phase1_tma) stages the same planes with tensor-map copies instead: one
+// thread issues, per plane, one 4-D box per block of arrays (a level's ro, u1, u2, u3; a face
+// set's p, u1, u2, u3; the forces; the flags), and the threads wait on the stage's mbarrier.
+// It needs each block of arrays in one allocation, a fixed stride apart (the contexts allocate
+// them that way), and lays the stage out with 128-byte aligned boxes.
 // Included by ark_kernels.cuh inside namespace ark.
 #pragma once
 
@@ -38,24 +44,55 @@ template <int MODE> struct Layout {
     static constexpr int FLAG_OFF = ROWS * W * 4;
     static constexpr int STAGE = FLAG_OFF + CROWS * WF;
     static constexpr int SMEM = NS * STAGE;
+    // offsets (floats; flags in bytes) of what the thread of tile column (tx, ty) reads:
+    // cr = ty - CROW0 is its cell row among the staged cell rows, cx = tx + 1 its column
+    __host__ __device__ static int cu(int m, int cr, int cx) { return (O_CU + m * CROWS + cr) * W + cx; }
+    __host__ __device__ static int ro(int ty, int cx) { return (O_CR + ty) * W + cx; }
+    __host__ __device__ static int flag(int cr, int cx) { return FLAG_OFF + cr * WF + cx; }
+    // face set d (0, 1, 2), array a (0 = p, 1..3 = u1..u3), staged row r, column x
+    __host__ __device__ static int face(int d, int a, int r, int x) {
+        return d == 0 ? (O_F1 + a * SY + r) * W + x : d == 1 ? (O_F2 + a * (SY + 1) + r) * W + x : (O_F3 + a * SY + r) * W + x;
+    }
+    __host__ __device__ static int ff(int m, int ty, int cx) { return (O_FF + m * SY + ty) * W + cx; }
 };
 
-// Offsets (floats / bytes within a stage) of what the thread of tile column (tx, ty) reads.
-// cr = ty - CROW0 is the thread's cell row among the staged cell rows, cx = tx + 1 its column.
-template <int MODE> __host__ __device__ inline int off_cu(int m, int cr, int cx) {
-    return (Layout<MODE>::O_CU + m * Layout<MODE>::CROWS + cr) * W + cx;
-}
-template <int MODE> __host__ __device__ inline int off_cr(int ty, int cx) { return (Layout<MODE>::O_CR + ty) * W + cx; }
-template <int MODE> __host__ __device__ inline int off_flag(int cr, int cx) { return Layout<MODE>::FLAG_OFF + cr * WF + cx; }
-// face set d (0, 1, 2), array a (0 = p, 1..3 = u1..u3), staged row r, column x
-template <int MODE> __host__ __device__ inline int off_face(int d, int a, int r, int x) {
-    using L = Layout<MODE>;
-    return d == 0 ? (L::O_F1 + a * SY + r) * W + x
-                  : d == 1 ? (L::O_F2 + a * (SY + 1) + r) * W + x : (L::O_F3 + a * SY + r) * W + x;
-}
-template <int MODE> __host__ __device__ inline int off_ff(int m, int ty, int cx) {
-    return (Layout<MODE>::O_FF + m * SY + ty) * W + cx;
-}
+// The TMA form's stage: one box per block of arrays, each at a 128-byte boundary.  The level's
+// four arrays (ro first) all take the cell rows (the stress's halo rows of ro are copied too).
+constexpr int pad32(int f) { return (f + 31) / 32 * 32; } // floats to a 128-byte boundary
+template <int MODE> struct TLayout {
+    static constexpr bool STRESS = (MODE & P1_STRESS) != 0;
+    static constexpr bool FIN = !STRESS && (MODE & P1_FORCES) != 0;
+    static constexpr int CROWS = STRESS ? SY + 2 : SY;
+    static constexpr int CROW0 = STRESS ? -1 : 0;
+    static constexpr int O_LV = 0;                                  // ro, u1, u2, u3: CROWS rows each
+    static constexpr int O_F1 = pad32(O_LV + 4 * CROWS * W);        // x1 faces p, u1, u2, u3: SY rows each
+    static constexpr int O_F2 = pad32(O_F1 + 4 * SY * W);           // x2 faces: SY + 1 rows each
+    static constexpr int O_F3 = pad32(O_F2 + 4 * (SY + 1) * W);     // x3 faces: SY rows each
+    static constexpr int O_FF = pad32(O_F3 + 4 * SY * W);           // f1, f2, f3: SY rows each
+    static constexpr int END = pad32(O_FF + (FIN ? 3 * SY * W : 0));
+    static constexpr int FLAG_OFF = END * 4;
+    static constexpr int STAGE = (FLAG_OFF + CROWS * WF + 127) / 128 * 128;
+    static constexpr int SMEM = NS * STAGE;
+    __host__ __device__ static int cu(int m, int cr, int cx) { return O_LV + ((m + 1) * CROWS + cr) * W + cx; }
+    __host__ __device__ static int ro(int ty, int cx) { return O_LV + (ty - CROW0) * W + cx; }
+    __host__ __device__ static int flag(int cr, int cx) { return FLAG_OFF + cr * WF + cx; }
+    __host__ __device__ static int face(int d, int a, int r, int x) {
+        return d == 0 ? O_F1 + (a * SY + r) * W + x : d == 1 ? O_F2 + (a * (SY + 1) + r) * W + x : O_F3 + (a * SY + r) * W + x;
+    }
+    __host__ __device__ static int ff(int m, int ty, int cx) { return O_FF + (m * SY + ty) * W + cx; }
+};
+// two blocks per SM (228 KB of shared memory, 1 KB of it reserved per block; 128 bytes for the
+// alignment of the stages, 512 of static shared memory)
+static_assert(2 * (TLayout<P1_FORCES | P1_RSUM>::SMEM + 128 + 512 + 1024) <= 228 * 1024, "TMA stages: two blocks per SM");
+static_assert(2 * (TLayout<P1_STRESS | P1_FORCES | P1_RMAX>::SMEM + 128 + 512 + 1024) <= 228 * 1024,
+              "TMA stages: two blocks per SM");
+
+// The cp.async form's offsets as free functions (the host plan check uses them).
+template <int MODE> __host__ __device__ inline int off_cu(int m, int cr, int cx) { return Layout<MODE>::cu(m, cr, cx); }
+template <int MODE> __host__ __device__ inline int off_cr(int ty, int cx) { return Layout<MODE>::ro(ty, cx); }
+template <int MODE> __host__ __device__ inline int off_flag(int cr, int cx) { return Layout<MODE>::flag(cr, cx); }
+template <int MODE> __host__ __device__ inline int off_face(int d, int a, int r, int x) { return Layout<MODE>::face(d, a, r, x); }
+template <int MODE> __host__ __device__ inline int off_ff(int m, int ty, int cx) { return Layout<MODE>::ff(m, ty, cx); }
 
 // A group of row segments of one array: row j (row0 <= j < row0 + nrows, j <= maxrow) of plane
 // p is copied from base + p*plane + j*pitch + xoff to stage + dst + (j - row0)*bytes.
@@ -163,6 +200,79 @@ inline int staged_chunk(const Geom &g) {
 }
 inline dim3 staged_grid(const Geom &g, int kch) { return dim3(tiles_x(g), (g.C2 + SY - 1) / SY, (g.C3 + kch - 1) / kch); }
 
+
+// ---- TMA form: the boxes of a plane ----
+// One block of n arrays (a level's ro, u1, u2, u3; a face set's p, u1, u2, u3; f1, f2, f3; or
+// the flags alone), each planes x rows x pitch elements, the arrays `stride[2]` bytes apart.
+// Per plane p a block copies elements x0 .. x0 + box[0] - 1 of rows j0 + row0 .. j0 + row0 +
+// box[1] - 1 of each array into the stage at dst, array a row r at dst + (a * box[1] + r) *
+// box[0] * elem.  Rows past the last come back as zeros (no valid cell reads them).
+struct TmaBox {
+    const void *base;
+    int elem;            // bytes per element: 4 or 1
+    long long dim[4];    // elements per row (the pitch), rows, planes, arrays
+    long long stride[3]; // bytes between rows, planes, arrays
+    int box[4];          // elements, rows, planes (1), arrays
+    int row0;            // first row, relative to the tile's first row j0
+    unsigned dst;        // byte offset in the stage
+    unsigned when;       // the stage kinds (DOWN, MID, TOP) that load it
+};
+constexpr int kMaxBoxes = 6;
+
+// The boxes of a launch of the TMA form, from the staged arrays (Bases); 0 when the arrays
+// of a block are not a fixed stride apart (then the cp.async form runs) or a stride is out of
+// the tensor maps' range.
+template <int MODE> inline int tma_boxes(TmaBox *B, const Geom &g, const Bases &b) {
+    using L = TLayout<MODE>;
+    const long long nc = g.ncell(), nf = g.nface();
+    auto gap = [](const void *x, const void *y) { return (long long)((const char *)x - (const char *)y); };
+    auto fits = [](long long st, long long min_bytes) { return st >= min_bytes && st % 16 == 0 && st < (1ll << 40); };
+    const long long lvs = gap(b.cu[0], b.cr);
+    if (!fits(lvs, nc * 4) || gap(b.cu[1], b.cr) != 2 * lvs || gap(b.cu[2], b.cr) != 3 * lvs) return 0;
+    long long fcs[3];
+    for (int d = 0; d < 3; ++d) {
+        fcs[d] = gap(b.fc[d][1], b.fc[d][0]);
+        if (!fits(fcs[d], nf * 4) || gap(b.fc[d][2], b.fc[d][0]) != 2 * fcs[d] || gap(b.fc[d][3], b.fc[d][0]) != 3 * fcs[d])
+            return 0;
+    }
+    long long ffs = 0;
+    if (L::FIN) {
+        ffs = gap(b.ff[1], b.ff[0]);
+        if (!fits(ffs, nc * 4) || gap(b.ff[2], b.ff[0]) != 2 * ffs) return 0;
+    }
+    if ((g.cs1 * 4) % 16 || (g.cs2 * 4) % 16 || (g.fs2 * 4) % 16 || g.cs1 % 16 || g.cs2 % 16) return 0;
+    const unsigned cells_when = L::STRESS ? (DOWN | MID | TOP) : MID;
+    int n = 0;
+    auto add = [&](const void *base, int elem, bool face, int narr, long long astride, int bw, int br, int row0,
+                   int dst, unsigned when) {
+        TmaBox &q = B[n++];
+        q.base = base;
+        q.elem = elem;
+        q.dim[0] = face ? g.fs1 : g.cs1;
+        q.dim[1] = face ? g.C2 + 3 : g.C2 + 2;
+        q.dim[2] = face ? g.C3 + 3 : g.C3 + 2;
+        q.dim[3] = narr;
+        q.stride[0] = (face ? g.fs1 : g.cs1) * elem;
+        q.stride[1] = (face ? g.fs2 : g.cs2) * elem;
+        q.stride[2] = astride;
+        q.box[0] = bw;
+        q.box[1] = br;
+        q.box[2] = 1;
+        q.box[3] = narr;
+        q.row0 = row0;
+        q.dst = (unsigned)dst;
+        q.when = when;
+    };
+    add(b.cr, 4, false, 4, lvs, W, L::CROWS, L::CROW0, L::O_LV * 4, cells_when);
+    add(b.fl, 1, false, 1, nc, WF, L::CROWS, L::CROW0, L::FLAG_OFF, cells_when);
+    add(b.fc[0][0], 4, true, 4, fcs[0], W, SY, 0, L::O_F1 * 4, MID);
+    add(b.fc[1][0], 4, true, 4, fcs[1], W, SY + 1, 0, L::O_F2 * 4, MID);
+    add(b.fc[2][0], 4, true, 4, fcs[2], W, SY, 0, L::O_F3 * 4, MID | TOP);
+    if (L::FIN) add(b.ff[0], 4, false, 3, ffs, W, SY, 0, L::O_FF * 4, MID);
+    return n;
+}
+inline unsigned box_bytes(const TmaBox &q) { return (unsigned)(q.box[0] * q.box[1] * q.box[2] * q.box[3] * q.elem); }
+
 #ifdef __CUDACC__
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void cp16(unsigned dst, const void *src) {
@@ -170,6 +280,95 @@ __device__ __forceinline__ void cp16(unsigned dst, const void *src) {
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// One cell (i, j, k) of a staged Phase1 from the stages of planes k - 1 (sd, read with the
+// stress), k (sk) and k + 1 (su), offsets by the stage layout L; the thread's tile column (tx, ty).
+// The arithmetic of k_phase1_cell, in the same order.
+template <int MODE, class L>
+__device__ __forceinline__ void staged_cell(const DevState<float> &S, int dst, const unsigned char *sd,
+                                            const unsigned char *sk, const unsigned char *su, int i, int j, int k,
+                                            int tx, int ty, const K<float> &kk, float dt, float G1, unsigned long long &m0,
+                                            unsigned long long &m1, unsigned long long &m2, long long &rsum) {
+    using T = float;
+    constexpr bool STRESS = L::STRESS;
+    const Geom &g = S.g;
+    const int cr = ty - L::CROW0, cx = tx + 1;
+    const T *fm = (const T *)sk, *fu = (const T *)su;
+    const uint8_t *flm = sk;
+    const int c = g.ci(i, j, k);
+    const uint8_t fl = flm[L::flag(cr, cx)];
+    const T ro_c = fm[L::ro(ty, cx)];
+    const T uc[3] = {fm[L::cu(0, cr, cx)], fm[L::cu(1, cr, cx)], fm[L::cu(2, cr, cx)]};
+    T ro_cn, ucn[3], rden = (T)0;
+    if (fl & FL_LT) {
+        FaceVal<T> lo[3], hi[3];
+        auto fv = [&](const T *f, int d, int r, int x) {
+            FaceVal<T> v;
+            v.p = f[L::face(d, 0, r, x)];
+            v.ro = face_ro(v.p, kk);
+            v.u[0] = f[L::face(d, 1, r, x)];
+            v.u[1] = f[L::face(d, 2, r, x)];
+            v.u[2] = f[L::face(d, 3, r, x)];
+            return v;
+        };
+        lo[0] = fv(fm, 0, ty, cx);
+        hi[0] = fv(fm, 0, ty, cx + 1);
+        lo[1] = fv(fm, 1, ty, cx);
+        hi[1] = fv(fm, 1, ty + 1, cx);
+        lo[2] = fv(fm, 2, ty, cx);
+        hi[2] = fv(fu, 2, ty, cx);
+        half_step(lo, hi, ro_c, uc, dt, kk, ro_cn, ucn, rden);
+    } else {
+        ucn[0] = ucn[1] = ucn[2] = (T)0;
+        ro_cn = (T)0;
+    }
+    T f[3] = {(T)0, (T)0, (T)0};
+    if (STRESS) {
+        if (fl & FL_EQ0) {
+            const T *fd = (const T *)sd;
+            const uint8_t *fld = sd, *flu = su;
+            uint8_t fln[6];
+            T un[6][3];
+            fln[0] = flm[L::flag(cr, cx - 1)];
+            fln[1] = flm[L::flag(cr, cx + 1)];
+            fln[2] = flm[L::flag(cr - 1, cx)];
+            fln[3] = flm[L::flag(cr + 1, cx)];
+            fln[4] = fld[L::flag(cr, cx)];
+            fln[5] = flu[L::flag(cr, cx)];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                un[0][m] = fm[L::cu(m, cr, cx - 1)];
+                un[1][m] = fm[L::cu(m, cr, cx + 1)];
+                un[2][m] = fm[L::cu(m, cr - 1, cx)];
+                un[3][m] = fm[L::cu(m, cr + 1, cx)];
+                un[4][m] = fd[L::cu(m, cr, cx)];
+                un[5][m] = fu[L::cu(m, cr, cx)];
+            }
+            const T ro_cf = kk.ro0 + ro_c;
+            stress_force(fln, un, fl, uc, ro_cf, kk, f);
+            if (MODE & P1_BULK) f[0] = bulk_force(f[0], ro_cf, kk, G1);
+        }
+        S.f[0][c] = f[0];
+        S.f[1][c] = f[1];
+        S.f[2][c] = f[2];
+    } else if (MODE & P1_FORCES) {
+        f[0] = fm[L::ff(0, ty, cx)];
+        f[1] = fm[L::ff(1, ty, cx)];
+        f[2] = fm[L::ff(2, ty, cx)];
+    }
+    if ((MODE & P1_FORCES) && (fl & FL_EQ0)) use_forces_f32(ucn, f, dt, kk, rden); // UseForces
+    S.lv[dst].ro[c] = ro_cn;
+    S.lv[dst].u1[c] = ucn[0];
+    S.lv[dst].u2[c] = ucn[1];
+    S.lv[dst].u3[c] = ucn[2];
+    if (MODE & P1_RMAX) {
+        const unsigned long long b0 = abs_key(ucn[0]), b1 = abs_key(ucn[1]), b2 = abs_key(ucn[2]);
+        m0 = b0 > m0 ? b0 : m0;
+        m1 = b1 > m1 ? b1 : m1;
+        m2 = b2 > m2 ? b2 : m2;
+    }
+    if ((MODE & P1_RSUM) && (fl & FL_EQ0)) rsum += fixed_sum_term(ucn[0]);
+}
 
 // One thread's share of a block's copy plan, resolved once before the plane loop: float rows
 // r0, r0 + NT/kChunks, ... at 16-byte chunk ch of each row, and (for the first kFlagChunks *
@@ -272,7 +471,6 @@ __device__ __forceinline__ void phase1_staged_body(const DevState<float> &S, int
     const T dt = sc_dt<T>(S.sc);
     const T G1 = (MODE & P1_BULK) ? sc_G<T>(S.sc) : (T)0;
     const bool valid = i <= g.C1 && j <= g.C2;
-    const int cr = ty - L::CROW0, cx = tx + 1;
     unsigned long long m0 = 0, m1 = 0, m2 = 0;
     long long rsum = 0;
     for (int k = k0; k <= k1; ++k) {
@@ -287,82 +485,10 @@ __device__ __forceinline__ void phase1_staged_body(const DevState<float> &S, int
             cp_commit();
         }
         if (valid) {
-            const T *fm = (const T *)(sm + ((k - pfirst) % NS) * L::STAGE);
-            const T *fu = (const T *)(sm + ((k + 1 - pfirst) % NS) * L::STAGE);
-            const uint8_t *flm = (const uint8_t *)fm;
-            const int c = g.ci(i, j, k);
-            const uint8_t fl = flm[off_flag<MODE>(cr, cx)];
-            const T ro_c = fm[off_cr<MODE>(ty, cx)];
-            const T uc[3] = {fm[off_cu<MODE>(0, cr, cx)], fm[off_cu<MODE>(1, cr, cx)], fm[off_cu<MODE>(2, cr, cx)]};
-            T ro_cn, ucn[3], rden = (T)0;
-            if (fl & FL_LT) {
-                FaceVal<T> lo[3], hi[3];
-                auto fv = [&](const T *f, int d, int r, int x) {
-                    FaceVal<T> v;
-                    v.p = f[off_face<MODE>(d, 0, r, x)];
-                    v.ro = face_ro(v.p, kk);
-                    v.u[0] = f[off_face<MODE>(d, 1, r, x)];
-                    v.u[1] = f[off_face<MODE>(d, 2, r, x)];
-                    v.u[2] = f[off_face<MODE>(d, 3, r, x)];
-                    return v;
-                };
-                lo[0] = fv(fm, 0, ty, cx);
-                hi[0] = fv(fm, 0, ty, cx + 1);
-                lo[1] = fv(fm, 1, ty, cx);
-                hi[1] = fv(fm, 1, ty + 1, cx);
-                lo[2] = fv(fm, 2, ty, cx);
-                hi[2] = fv(fu, 2, ty, cx);
-                half_step(lo, hi, ro_c, uc, dt, kk, ro_cn, ucn, rden);
-            } else {
-                ucn[0] = ucn[1] = ucn[2] = (T)0;
-                ro_cn = (T)0;
-            }
-            T f[3] = {(T)0, (T)0, (T)0};
-            if (STRESS) {
-                if (fl & FL_EQ0) {
-                    const T *fd = (const T *)(sm + ((k - 1 - pfirst) % NS) * L::STAGE);
-                    const uint8_t *fld = (const uint8_t *)fd, *flu = (const uint8_t *)fu;
-                    uint8_t fln[6];
-                    T un[6][3];
-                    fln[0] = flm[off_flag<MODE>(cr, cx - 1)];
-                    fln[1] = flm[off_flag<MODE>(cr, cx + 1)];
-                    fln[2] = flm[off_flag<MODE>(cr - 1, cx)];
-                    fln[3] = flm[off_flag<MODE>(cr + 1, cx)];
-                    fln[4] = fld[off_flag<MODE>(cr, cx)];
-                    fln[5] = flu[off_flag<MODE>(cr, cx)];
-#pragma unroll
-                    for (int m = 0; m < 3; ++m) {
-                        un[0][m] = fm[off_cu<MODE>(m, cr, cx - 1)];
-                        un[1][m] = fm[off_cu<MODE>(m, cr, cx + 1)];
-                        un[2][m] = fm[off_cu<MODE>(m, cr - 1, cx)];
-                        un[3][m] = fm[off_cu<MODE>(m, cr + 1, cx)];
-                        un[4][m] = fd[off_cu<MODE>(m, cr, cx)];
-                        un[5][m] = fu[off_cu<MODE>(m, cr, cx)];
-                    }
-                    const T ro_cf = kk.ro0 + ro_c;
-                    stress_force(fln, un, fl, uc, ro_cf, kk, f);
-                    if (MODE & P1_BULK) f[0] = bulk_force(f[0], ro_cf, kk, G1);
-                }
-                S.f[0][c] = f[0];
-                S.f[1][c] = f[1];
-                S.f[2][c] = f[2];
-            } else if (MODE & P1_FORCES) {
-                f[0] = fm[off_ff<MODE>(0, ty, cx)];
-                f[1] = fm[off_ff<MODE>(1, ty, cx)];
-                f[2] = fm[off_ff<MODE>(2, ty, cx)];
-            }
-            if ((MODE & P1_FORCES) && (fl & FL_EQ0)) use_forces_f32(ucn, f, dt, kk, rden); // UseForces
-            S.lv[dst].ro[c] = ro_cn;
-            S.lv[dst].u1[c] = ucn[0];
-            S.lv[dst].u2[c] = ucn[1];
-            S.lv[dst].u3[c] = ucn[2];
-            if (MODE & P1_RMAX) {
-                const unsigned long long b0 = abs_key(ucn[0]), b1 = abs_key(ucn[1]), b2 = abs_key(ucn[2]);
-                m0 = b0 > m0 ? b0 : m0;
-                m1 = b1 > m1 ? b1 : m1;
-                m2 = b2 > m2 ? b2 : m2;
-            }
-            if ((MODE & P1_RSUM) && (fl & FL_EQ0)) rsum += fixed_sum_term(ucn[0]);
+            const unsigned char *sk = sm + ((k - pfirst) % NS) * L::STAGE;
+            const unsigned char *su = sm + ((k + 1 - pfirst) % NS) * L::STAGE;
+            const unsigned char *sd = STRESS ? sm + ((k - 1 - pfirst) % NS) * L::STAGE : sk;
+            staged_cell<MODE, L>(S, dst, sd, sk, su, i, j, k, tx, ty, kk, dt, G1, m0, m1, m2, rsum);
         }
     }
     cp_wait<0>();
@@ -384,6 +510,205 @@ template <int MODE> inline void launch_staged(const DevState<float> &S, int src,
 template <int MODE> inline void prepare_staged() {
     cudaFuncSetAttribute(k_phase1_staged<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, Layout<MODE>::SMEM);
     cudaFuncSetAttribute(k_phase1_staged<MODE>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
+// ---- TMA form: the kernel ----
+// The tensor maps of a launch (kernel parameters) and what each box loads.
+struct TmaArgs {
+    CUtensorMap map[kMaxBoxes];
+    int row0[kMaxBoxes];
+    unsigned dst[kMaxBoxes], when[kMaxBoxes];
+    unsigned bytes[5]; // the bytes a plane of kind DOWN (1), MID (2) or TOP (4) brings
+    int n;
+};
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(unsigned bar) { asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Waits for the phase of the given parity to complete; false after about limit_ns.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, unsigned long long limit_ns) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try(bar, parity))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// One 4-D box (x, row, plane, array) into shared memory, completing on bar.
+__device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map, int x, int y, int z, int w, unsigned bar) {
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+                 ::"r"(dst), "l"(map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
+                 : "memory");
+}
+
+// The staged Phase1 with TMA copies: tile (blockIdx.x, blockIdx.y) of 64 x 4 columns, planes of
+// chunk blockIdx.z.  Thread 0 issues a plane's boxes into its stage (NS stages, one mbarrier
+// each); every thread waits for the planes it reads on their mbarriers.  Same plane order and
+// ring as the cp.async form: at plane k, once plane k + 1 has landed and every thread is past
+// plane k - 1, the slot of the plane no longer needed takes the next plane.  A wait that does
+// not end within half a second sets STATUS_STAGING, and the block lets its copies in flight
+// land (again with a limit) and leaves.
+template <int MODE>
+__global__ void __launch_bounds__(NT, 2)
+    k_phase1_tma(const __grid_constant__ DevState<float> S, const __grid_constant__ TmaArgs A, int src, int dst, int kch) {
+    using L = TLayout<MODE>;
+    using T = float;
+    constexpr bool STRESS = L::STRESS;
+    constexpr unsigned long long kLimitNs = 500000000ull;
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    __shared__ __align__(8) unsigned long long bar[NS];
+    // the stages from the first 128-byte boundary (tensor copies land on 128-byte boundaries)
+    unsigned char *const sm = sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u);
+    const Geom g = S.g;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * SX + tx;
+    const int i = blockIdx.x * SX + tx + 1, j = blockIdx.y * SY + ty + 1;
+    const int x0 = blockIdx.x * SX, j0 = blockIdx.y * SY + 1;
+    const int k0 = blockIdx.z * kch + 1;
+    const int k1 = k0 + kch - 1 < g.C3 ? k0 + kch - 1 : g.C3;
+    const int pfirst = STRESS ? k0 - 1 : k0, plast = k1 + 1;
+    const unsigned sbase = smem_u32(sm);
+    auto bar_of = [&](int p) { return smem_u32(&bar[(p - pfirst) % NS]); };
+    auto parity_of = [&](int p) { return (unsigned)(((p - pfirst) / NS) & 1); };
+    auto issue = [&](int p) { // thread 0
+        const unsigned kind = p < k0 ? DOWN : (p > k1 ? TOP : MID);
+        const unsigned to = sbase + (unsigned)(((p - pfirst) % NS) * L::STAGE), b = bar_of(p);
+        mbar_expect_tx(b, A.bytes[kind]);
+        for (int q = 0; q < A.n; ++q)
+            if (A.when[q] & kind) tma_load_4d(to + A.dst[q], &A.map[q], x0, j0 + A.row0[q], p, 0, b);
+    };
+    int issued = pfirst - 1; // thread 0: the last plane issued
+    if (t == 0) {
+        for (int q = 0; q < NS; ++q) mbar_init(smem_u32(&bar[q]), 1);
+        fence_mbar_init();
+        fence_proxy_async();
+        for (int p = pfirst; p < pfirst + NS - 1 && p <= plast; ++p) {
+            issue(p);
+            issued = p;
+        }
+    }
+    __syncthreads();
+
+    const K<T> &kk = kconst<T>(S.k);
+    const T dt = sc_dt<T>(S.sc);
+    const T G1 = (MODE & P1_BULK) ? sc_G<T>(S.sc) : (T)0;
+    const bool valid = i <= g.C1 && j <= g.C2;
+    unsigned long long m0 = 0, m1 = 0, m2 = 0;
+    long long rsum = 0;
+    bool failed = false;
+    for (int k = k0; k <= k1; ++k) {
+        bool ok = true;
+        if (k == k0) {
+            if (STRESS) ok = mbar_wait(bar_of(k - 1), parity_of(k - 1), kLimitNs);
+            ok = ok && mbar_wait(bar_of(k), parity_of(k), kLimitNs);
+        }
+        ok = ok && mbar_wait(bar_of(k + 1), parity_of(k + 1), kLimitNs);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        if (t == 0) {
+            const int pn = k + NS - (STRESS ? 2 : 1);
+            if (pn <= plast) {
+                fence_proxy_async();
+                issue(pn);
+                issued = pn;
+            }
+        }
+        if (valid) {
+            const unsigned char *sk = sm + ((k - pfirst) % NS) * L::STAGE;
+            const unsigned char *su = sm + ((k + 1 - pfirst) % NS) * L::STAGE;
+            const unsigned char *sd = STRESS ? sm + ((k - 1 - pfirst) % NS) * L::STAGE : sk;
+            staged_cell<MODE, L>(S, dst, sd, sk, su, i, j, k, tx, ty, kk, dt, G1, m0, m1, m2, rsum);
+        }
+    }
+    if (failed && t == 0) {
+        atomicOr(&S.sc->status, STATUS_STAGING);
+        // the last NS planes issued hold each stage's newest phase
+        for (int p = issued - NS + 1 > pfirst ? issued - NS + 1 : pfirst; p <= issued; ++p)
+            mbar_wait(bar_of(p), parity_of(p), kLimitNs);
+    }
+    __syncthreads();
+    if (t == 0)
+        for (int q = 0; q < NS; ++q) mbar_inval(smem_u32(&bar[q]));
+    const BIx bx = {(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y};
+    if (MODE & (P1_RMAX | P1_RSUM)) tile_store<T, NT>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+inline EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+// The tensor maps of a launch; false when the arrays do not allow the TMA form.
+template <int MODE> inline bool tma_args(TmaArgs &A, const DevState<float> &S, int src, int fcur) {
+    TmaBox B[kMaxBoxes];
+    const int n = tma_boxes<MODE>(B, S.g, bases_of<MODE>(S, src, fcur));
+    const EncodeTiledFn enc = encode_tiled();
+    if (n <= 0 || !enc) return false;
+    std::memset(&A, 0, sizeof A);
+    for (int q = 0; q < n; ++q) {
+        const TmaBox &b = B[q];
+        const cuuint64_t dim[4] = {(cuuint64_t)b.dim[0], (cuuint64_t)b.dim[1], (cuuint64_t)b.dim[2], (cuuint64_t)b.dim[3]};
+        const cuuint64_t stride[3] = {(cuuint64_t)b.stride[0], (cuuint64_t)b.stride[1], (cuuint64_t)b.stride[2]};
+        const cuuint32_t box[4] = {(cuuint32_t)b.box[0], (cuuint32_t)b.box[1], (cuuint32_t)b.box[2], (cuuint32_t)b.box[3]};
+        const cuuint32_t unit[4] = {1, 1, 1, 1};
+        if (enc(&A.map[q], b.elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 4,
+                const_cast<void *>(b.base), dim, stride, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+        A.row0[q] = b.row0;
+        A.dst[q] = b.dst;
+        A.when[q] = b.when;
+        for (unsigned kind = DOWN; kind <= TOP; kind <<= 1)
+            if (b.when & kind) A.bytes[kind] += box_bytes(b);
+    }
+    A.n = n;
+    return true;
+}
+
+template <int MODE> inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st) {
+    TmaArgs A;
+    if (!tma_args<MODE>(A, S, src, fcur)) {
+        launch_staged<MODE>(S, src, dst, fcur, st);
+        return;
+    }
+    const int kch = staged_chunk(S.g);
+    k_phase1_tma<MODE><<<staged_grid(S.g, kch), dim3(SX, SY), TLayout<MODE>::SMEM + 128, st>>>(S, A, src, dst, kch);
+}
+template <int MODE> inline void prepare_staged_tma() {
+    encode_tiled(); // looked up here, outside any stream capture
+    cudaFuncSetAttribute(k_phase1_tma<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, TLayout<MODE>::SMEM + 128);
+    cudaFuncSetAttribute(k_phase1_tma<MODE>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 #endif
 

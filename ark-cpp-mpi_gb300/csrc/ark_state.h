@@ -141,7 +141,8 @@ __host__ __device__ inline int tile_count(const Geom &g) { return tiles_x(g) * t
 constexpr int kBuckets = 256;
 
 // Sticky device status bits.
-enum : int { STATUS_NONFINITE = 1 };
+// STATUS_STAGING: a shared-memory staging wait (TMA copies on an mbarrier) gave up
+enum : int { STATUS_NONFINITE = 1, STATUS_STAGING = 2 };
 
 // Cell-flag bits: the reference tests the double `condition` three ways.
 enum : uint8_t {
@@ -193,7 +194,7 @@ struct DevScalars {
     double dt, time, ub, G;
     long long nstep;
     long long nfluid;  // fluid cells (condition == 0), set at upload
-    int status;        // sticky error bits (STATUS_NONFINITE)
+    int status;        // sticky error bits (STATUS_NONFINITE, STATUS_STAGING)
     int pad;
     long long sums[5]; // conservation sums (fixed point), see ark_sums
     long long sum_cells;
