@@ -382,7 +382,7 @@ template <class T> struct EngineT : Engine {
         if (use_step2()) {
             // Phase2 and the second Phase1 in one kernel; the new level goes to the spare, which
             // after_step swaps in as "nCon"
-            Launch<T>::phase2_phase1(S, y, fcur, S.spare, st);
+            Launch<T>::phase2_phase1(S, y, fcur, S.spare, st, ctx->p2mode == 3);
             mark(4);
             if (ctx->averaging) {
                 DevState<T> Sn = S;
@@ -418,7 +418,7 @@ template <class T> struct EngineT : Engine {
     void energy(int ncon, double *scratch, double *out) override { output_energy<T>(S, ncon, scratch, out, ctx->st); }
     DevScalars *scalars() override { return S.sc; }
     uint8_t *flags() override { return S.flags; }
-    bool use_step2() const { return ctx->p2mode == 2 && S.spare.ro; }
+    bool use_step2() const { return (ctx->p2mode == 2 || ctx->p2mode == 3) && S.spare.ro; }
     int step_launches() override { return use_step2() ? 5 : kNumStepKernels; }
     const char *step_kernel_name(int q) override {
         if (q < 0 || q >= step_launches()) return "";
@@ -596,7 +596,7 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
         if (e[0] && ok(e[1])) ctx->march[1] = e[1] - '0';
     }
     if (const char *e = std::getenv("ARK_PHASE2_FUSED"))
-        if (e[0] >= '0' && e[0] <= '2' && (e[0] != '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
+        if (e[0] >= '0' && e[0] <= '3' && (e[0] < '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
     Launch<float>::prepare();
     Launch<double>::prepare();
     cudaEventCreate(&ctx->ev0);
@@ -1274,9 +1274,9 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         // Phase2 forms: the three sweep kernels, or (FP32) one kernel for the sweeps and the
         // second Phase1.  The one-kernel Phase2 alone (mode 1) is correct but slower at every
         // size measured: left to ARK_PHASE2_FUSED=1, not tried here.
-        const int p2cand[2] = {0, 2};
+        const int p2cand[3] = {0, 2, 3};
         if (which == 2 && !fp32) continue;
-        const int ncand = which < 2 ? (fp32 ? 4 : 3) : which == 2 ? 2 : 4;
+        const int ncand = which < 2 ? (fp32 ? 4 : 3) : which == 2 ? 3 : 4;
         int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : ctx->seg_target;
         if (which == 3 && ctx->p2mode) continue; // the one-kernel forms have no segments
         for (int c = 0; c < ncand; ++c) {

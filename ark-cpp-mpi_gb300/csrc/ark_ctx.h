@@ -90,7 +90,8 @@ struct ark_ctx {
     float closure_scale = 0.f;            // u_tau / vis for the y+ feature
     int seg_target = 32;                  // x2/x3 sweep segment length (faces)
     int p2mode = 0; // Phase2: 0 three sweep kernels, 1 one kernel for the three sweeps, 2 (FP32)
-                    // one kernel for the three sweeps and the second Phase1
+                    // one kernel for the three sweeps and the second Phase1, 3 (FP32) the same
+                    // with TMA tensor copies
     // output streaming: two device and two pinned host slab buffers of io_cap doubles
     double *io_dev[2] = {nullptr, nullptr};
     double *io_host[2] = {nullptr, nullptr};

@@ -170,6 +170,48 @@ template <int MODE> struct PlanCheck {
     }
 };
 
+// The tensor-copy rules for a launch's boxes (stage bytes each): fail(what, box).
+template <class Fail> void check_boxes(const stg::TmaBox *B, int n, int stage, Fail &&fail) {
+    for (int q = 0; q < n; ++q) {
+        const stg::TmaBox &x = B[q];
+        if ((long long)x.box[0] * x.elem % 16) fail("box row not a multiple of 16 bytes", q);
+        for (int d = 0; d < 4; ++d)
+            if (x.box[d] < 1 || x.box[d] > 256) fail("box size outside 1..256", q);
+        for (int d = 0; d < 3; ++d)
+            if (x.stride[d] % 16 || x.stride[d] >= (1ll << 40)) fail("global stride", q);
+        if (x.dst % 128) fail("destination not 128-byte aligned", q);
+        if ((long long)x.dst + stg::box_bytes(x) > stage) fail("box outside its stage", q);
+    }
+}
+// The boxes of kind `kind` for plane p of the tile at column x0, row j0, byte by byte as the
+// copy engine lays them out: M[stage byte] = fake source address (-2: zero fill past the last
+// row); fail(what, value).
+template <class Fail>
+void expand_boxes(const stg::TmaBox *B, int n, unsigned kind, int x0, int j0, int p, std::vector<long long> &M, Fail &&fail) {
+    const long long stage = (long long)M.size();
+    if ((long long)x0 * 4 % 16) fail("x offset not a multiple of 16 bytes", x0);
+    for (int q = 0; q < n; ++q) {
+        const stg::TmaBox &x = B[q];
+        if (!(x.when & kind)) continue;
+        if (p < 0 || p >= x.dim[2]) fail("plane outside its array", q);
+        if (j0 + x.row0 < 0) fail("box starts at a negative row", q);
+        if (x0 + x.box[0] > x.dim[0]) fail("box leaves its row", q);
+        for (int a = 0; a < x.box[3]; ++a)
+            for (int r = 0; r < x.box[1]; ++r)
+                for (int e = 0; e < x.box[0]; ++e) {
+                    const long long y = j0 + x.row0 + r;
+                    const long long dst = x.dst + ((long long)(a * x.box[1] + r) * x.box[0] + e) * x.elem;
+                    const long long src =
+                        (long long)x.base + a * x.stride[2] + p * x.stride[1] + y * x.stride[0] + (long long)(x0 + e) * x.elem;
+                    for (int c = 0; c < x.elem; ++c) {
+                        if (dst + c >= stage) continue;
+                        if (M[dst + c] != -1) fail("two boxes into one byte", dst + c);
+                        M[dst + c] = y < x.dim[1] ? src + c : -2;
+                    }
+                }
+    }
+}
+
 // The TMA form's plan, checked the same way: the boxes of tma_boxes (from fake bases whose
 // blocks of arrays are a fixed stride apart) are expanded byte by byte as the copy engine
 // lays them out (rows past a block's last row as zero fill), with the tensor copies' rules
@@ -205,16 +247,7 @@ template <int MODE> struct TmaCheck {
             fail("no TMA plan for these arrays", 0, 0, 0, n);
             return;
         }
-        for (int q = 0; q < n; ++q) {
-            const stg::TmaBox &x = B[q];
-            if ((long long)x.box[0] * x.elem % 16) fail("box row not a multiple of 16 bytes", 0, 0, 0, q);
-            for (int d = 0; d < 4; ++d)
-                if (x.box[d] < 1 || x.box[d] > 256) fail("box size outside 1..256", 0, 0, 0, q);
-            for (int d = 0; d < 3; ++d)
-                if (x.stride[d] % 16 || x.stride[d] >= (1ll << 40)) fail("global stride", 0, 0, 0, q);
-            if (x.dst % 128) fail("destination not 128-byte aligned", 0, 0, 0, q);
-            if (x.dst + stg::box_bytes(x) > (unsigned)L::STAGE) fail("box outside its stage", 0, 0, 0, q);
-        }
+        check_boxes(B, n, L::STAGE, [&](const char *w, long long v) { fail(w, 0, 0, 0, v); });
         const dim3 grid = stg::staged_grid(g, kch);
         std::vector<std::vector<long long>> map;
         for (int bz = 0; bz < (int)grid.z; ++bz)
@@ -222,32 +255,11 @@ template <int MODE> struct TmaCheck {
                 for (int bx = 0; bx < (int)grid.x; ++bx) {
                     const int k0 = bz * kch + 1, k1 = std::min(k0 + kch - 1, g.C3);
                     const int pfirst = L::STRESS ? k0 - 1 : k0, plast = k1 + 1;
-                    const int x0 = bx * stg::SX, j0 = by * stg::SY + 1;
-                    if ((long long)x0 * 4 % 16) fail("x offset not a multiple of 16 bytes", bx, by, 0, x0);
                     map.assign(plast - pfirst + 1, std::vector<long long>(L::STAGE, -1));
                     for (int p = pfirst; p <= plast; ++p) {
                         const unsigned kind = p < k0 ? stg::DOWN : (p > k1 ? stg::TOP : stg::MID);
-                        std::vector<long long> &M = map[p - pfirst];
-                        for (int q = 0; q < n; ++q) {
-                            const stg::TmaBox &x = B[q];
-                            if (!(x.when & kind)) continue;
-                            if (p < 0 || p >= x.dim[2]) fail("plane outside its array", bx, by, p, q);
-                            if (j0 + x.row0 < 0) fail("box starts at a negative row", bx, by, p, q);
-                            if (x0 + x.box[0] > x.dim[0]) fail("box leaves its row", bx, by, p, q);
-                            for (int a = 0; a < x.box[3]; ++a)
-                                for (int r = 0; r < x.box[1]; ++r)
-                                    for (int e = 0; e < x.box[0]; ++e) {
-                                        const long long y = j0 + x.row0 + r;
-                                        const long long dst = x.dst + ((long long)(a * x.box[1] + r) * x.box[0] + e) * x.elem;
-                                        const long long src = (long long)x.base + a * x.stride[2] + p * x.stride[1] +
-                                                              y * x.stride[0] + (long long)(x0 + e) * x.elem;
-                                        for (int c = 0; c < x.elem; ++c) {
-                                            if (dst + c >= L::STAGE) continue;
-                                            if (M[dst + c] != -1) fail("two boxes into one byte", bx, by, p, dst + c);
-                                            M[dst + c] = y < x.dim[1] ? src + c : -2;
-                                        }
-                                    }
-                        }
+                        expand_boxes(B, n, kind, bx * stg::SX, by * stg::SY + 1, p, map[p - pfirst],
+                                     [&](const char *w, long long v) { fail(w, bx, by, p, v); });
                     }
                     for (int ty = 0; ty < stg::SY; ++ty)
                         for (int tx = 0; tx < stg::SX; ++tx) {
@@ -282,35 +294,54 @@ template <int MODE> struct TmaCheck {
 struct Plan2Check {
     enum { B_CELL = 0, B_FL = 8, B_FX = 9, B_FY = 13, B_N = 17 };
     const Geom g;
+    const bool tma;     // check the TMA form's boxes instead of the cp.async rows
+    const long long sp; // fake array spacing (below 2^40 for the tensor maps' strides)
     long long size[B_N];
     std::string err;
     int bad = 0;
-    explicit Plan2Check(const Geom &gg) : g(gg) {
+    explicit Plan2Check(const Geom &gg, bool t = false) : g(gg), tma(t), sp(t ? 1ll << 36 : kSpan) {
         for (int a = 0; a < B_N; ++a) size[a] = a < B_FL ? g.ncell() * 4 : (a == B_FL ? g.ncell() : g.nface() * 4);
     }
     void fail(const char *what, int bx, int by, int p, long long x) {
         if (bad++ == 0) {
             char b[256];
-            std::snprintf(b, sizeof b, "phase2+phase1 tile (%d,%d) plane %d: %s (%lld)", bx, by, p, what, x);
+            std::snprintf(b, sizeof b, "phase2+phase1%s tile (%d,%d) plane %d: %s (%lld)", tma ? " (TMA)" : "", bx, by, p,
+                          what, x);
             err = b;
         }
     }
-    static long long addr(int a, long long e, int elem) { return a * kSpan + e * elem; }
+    long long addr(int a, long long e, int elem) const { return a * sp + e * elem; }
     void run(int kch) {
         using namespace s2;
         const dim3 grd = s2::grid(g, kch);
         s2::Bases b;
-        for (int q = 0; q < 8; ++q) b.cell[q] = (const void *)((B_CELL + q) * kSpan);
-        b.fl = (const void *)(B_FL * kSpan);
+        for (int q = 0; q < 8; ++q) b.cell[q] = (const void *)((B_CELL + q) * sp);
+        b.fl = (const void *)(B_FL * sp);
         for (int a = 0; a < 4; ++a) {
-            b.fx[a] = (const void *)((B_FX + a) * kSpan);
-            b.fy[a] = (const void *)((B_FY + a) * kSpan);
+            b.fx[a] = (const void *)((B_FX + a) * sp);
+            b.fy[a] = (const void *)((B_FY + a) * sp);
         }
         stg::Group G[s2::kMaxGroups];
         std::vector<std::vector<long long>> map;
+        stg::TmaBox TB[stg::kMaxBoxes];
+        const int nb = tma ? s2::tma_boxes(TB, g, b) : 0;
+        if (tma) {
+            if (nb <= 0) fail("no TMA plan for these arrays", 0, 0, 0, nb);
+            check_boxes(TB, nb, STAGE, [&](const char *w, long long v) { fail(w, 0, 0, 0, v); });
+        }
         for (int bz = 0; bz < (int)grd.z; ++bz)
             for (int by = 0; by < (int)grd.y; ++by)
                 for (int bx = 0; bx < (int)grd.x; ++bx) {
+                    if (tma) {
+                        const int k0 = bz * kch + 1, k1 = std::min(k0 + kch - 1, g.C3);
+                        const int pfirst = k0 - 1, plast = k1 + 1;
+                        map.assign(plast - pfirst + 1, std::vector<long long>(STAGE, -1));
+                        for (int p = pfirst; p <= plast; ++p)
+                            expand_boxes(TB, nb, (p < k0 || p > k1) ? EDGE : MID, bx * SX, by * SY + 1, p, map[p - pfirst],
+                                         [&](const char *w, long long v) { fail(w, bx, by, p, v); });
+                        reads(map, pfirst, k0, k1, bx, by);
+                        continue;
+                    }
                     const int n = s2::build_groups(G, g, b, bx, by);
                     if (n > s2::kMaxGroups) {
                         fail("too many groups", bx, by, 0, n);
@@ -335,8 +366,8 @@ struct Plan2Check {
                                 for (int c = 0; c < chunks; ++c) {
                                     const long long src = (long long)w.src + (long long)p * w.plane + 16 * c;
                                     const long long dst = (w.dw & 0xFFFFFFu) + 16ll * c;
-                                    const int arr = (int)(src / kSpan);
-                                    const long long off = src % kSpan;
+                                    const int arr = (int)(src / sp);
+                                    const long long off = src % sp;
                                     total += 16;
                                     if (arr < 0 || arr >= B_N) {
                                         fail("copy from no array", bx, by, p, src);
@@ -442,10 +473,11 @@ struct Plan2Check {
 int step2_plan_check(int C1, int C2, int C3, int kch, char *msg, int cap) {
     const Geom g = device_geom(C1, C2, C3);
     if (kch <= 0) kch = s2::chunk(g);
-    Plan2Check a(g);
+    Plan2Check a(g), b(g, true);
     a.run(kch);
-    if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", a.err.c_str());
-    return a.bad;
+    b.run(kch);
+    if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", (!a.err.empty() ? a.err : b.err).c_str());
+    return a.bad + b.bad;
 }
 
 int staging_plan_check(int C1, int C2, int C3, int kch_in, char *msg, int cap) {

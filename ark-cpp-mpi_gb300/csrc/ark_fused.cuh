@@ -20,7 +20,9 @@
 // 3-stage shared-memory ring with 16-byte cp.async copies (the staged Phase1's scheme); the z
 // faces and the forces, which only the cell's own thread reads, are loaded into registers one
 // plane ahead.  The z sweep runs one plane behind the x and y sweeps' plane, and the second
-// Phase1 one plane behind the z sweep.  Two barriers per plane.
+// Phase1 one plane behind the z sweep.  Two barriers per plane.  With TMA = true the planes
+// come as five tensor-map boxes instead (both levels, the flags, the x and y face sets: the
+// staged Phase1's TMA scheme), issued by thread 0 and awaited on each stage's mbarrier.
 // Included by ark_kernels.cuh inside namespace ark.
 #pragma once
 
@@ -41,10 +43,11 @@ constexpr int O_C = 0;
 constexpr int O_FX = O_C + 8 * CR;
 constexpr int O_FY = O_FX + 4 * SY;
 constexpr int ROWS = O_FY + 4 * YR;
-constexpr int FLAG_OFF = ROWS * W * 4;
-constexpr int STAGE = FLAG_OFF + CR * WF;
+constexpr int FLAG_OFF = (ROWS * W * 4 + 127) / 128 * 128; // boxes start on 128-byte boundaries
+constexpr int STAGE = (FLAG_OFF + CR * WF + 127) / 128 * 128;
 constexpr int SMEM = NS * STAGE;
-static_assert(STAGE % 16 == 0, "stages must keep 16-byte alignment");
+static_assert(STAGE % 128 == 0 && (O_C + 4 * CR) * W * 4 % 128 == 0 && O_FX * W * 4 % 128 == 0 && O_FY * W * 4 % 128 == 0,
+              "stages and boxes on 128-byte boundaries");
 static_assert(ROWS <= stg::kMaxRows && CR <= stg::kMaxFlagRows, "row tables");
 
 // Offsets within a stage (floats; flags in bytes).  r: cell row j - (j0 - 1), x-face row
@@ -104,6 +107,23 @@ __host__ __device__ inline Bases bases_of(const DevState<float> &S, int con, int
     return b;
 }
 
+// The TMA form's boxes: the "Con" and "nCon" levels (ro, u1, u2, u3; cell rows j0-1 ..
+// j0+SY), the flags, the x faces (rows j0 .. j0+SY-1) and the y faces (rows j0-1 .. j0+SY+1),
+// p, u1, u2, u3; 0 when the arrays of a block are not a fixed stride apart.
+inline int tma_boxes(stg::TmaBox *B, const Geom &g, const Bases &b) {
+    const long long nc = g.ncell(), nf = g.nface();
+    const long long cs0 = stg::block_stride(b.cell, 4, nc * 4), cs1 = stg::block_stride(b.cell + 4, 4, nc * 4);
+    const long long xs = stg::block_stride(b.fx, 4, nf * 4), ys = stg::block_stride(b.fy, 4, nf * 4);
+    if (!cs0 || !cs1 || !xs || !ys || !stg::rows_fit(g)) return 0;
+    int n = 0;
+    B[n++] = stg::make_box(g, b.cell[0], 4, false, 4, cs0, W, CR, -1, off_cell(0, 0, 0) * 4, EDGE | MID);
+    B[n++] = stg::make_box(g, b.cell[4], 4, false, 4, cs1, W, CR, -1, off_cell(4, 0, 0) * 4, EDGE | MID);
+    B[n++] = stg::make_box(g, b.fl, 1, false, 1, nc, WF, CR, -1, FLAG_OFF, EDGE | MID);
+    B[n++] = stg::make_box(g, b.fx[0], 4, true, 4, xs, W, SY, 0, off_fx(0, 0, 0) * 4, MID);
+    B[n++] = stg::make_box(g, b.fy[0], 4, true, 4, ys, W, YR, -1, off_fy(0, 0, 0) * 4, MID);
+    return n;
+}
+
 // Planes per block: about eight waves of two blocks per SM on 152 SMs, 2 to 64 planes (small
 // grids: short chunks, so that enough blocks run; each block also sweeps the two planes at its
 // ends in z).
@@ -151,11 +171,16 @@ __device__ __forceinline__ FaceVal<float> face_val(float p, float u1, float u2, 
     return v;
 }
 
-template <class T>
+template <class T, bool TMA>
 __global__ void __launch_bounds__(NT, 2)
-    k_phase2_phase1(const __grid_constant__ DevState<T> S, int con, int fcur, const __grid_constant__ Level<T> out, int kch) {
+    k_phase2_phase1(const __grid_constant__ DevState<T> S, int con, int fcur, const __grid_constant__ Level<T> out, int kch,
+                    const __grid_constant__ stg::TmaArgs A) {
     static_assert(sizeof(T) == 4, "FP32 contexts only");
-    extern __shared__ __align__(128) unsigned char sm[];
+    constexpr unsigned long long kLimitNs = 500000000ull;
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    __shared__ __align__(8) unsigned long long bar[NS];
+    // the stages from the first 128-byte boundary (tensor copies land on 128-byte boundaries)
+    unsigned char *const sm = TMA ? sm_raw + ((128u - (stg::smem_u32(sm_raw) & 127u)) & 127u) : sm_raw;
     __shared__ stg::Row rows[stg::kMaxRows], frows[stg::kMaxFlagRows];
     __shared__ int nrow, nfrow;
     __shared__ Behind XB[SY][SX + 1]; // x: index x holds cell i0-1+x
@@ -177,7 +202,7 @@ __global__ void __launch_bounds__(NT, 2)
     const int ty_last = g.C2 - j0 < SY - 1 ? g.C2 - j0 : SY - 1;
     const bool valid = tx <= tx_last && ty <= ty_last;
     const unsigned sbase = stg::smem_u32(sm);
-    if (t == 0) {
+    if (!TMA && t == 0) {
         stg::Group G[kMaxGroups];
         const int ng = build_groups(G, g, bases_of(S, con, fcur), bxi, byi);
         int a, b;
@@ -190,9 +215,18 @@ __global__ void __launch_bounds__(NT, 2)
     // Phase1 does, costs this kernel 22 registers it does not have: spills, 11% slower)
     const int ch = t % stg::kChunks, r0 = t / stg::kChunks;
     constexpr int kRowsPerPass = NT / stg::kChunks;
+    auto bar_of = [&](int p) { return stg::smem_u32(&bar[(p - pfirst) % NS]); };
+    auto parity_of = [&](int p) { return (unsigned)(((p - pfirst) / NS) & 1); };
     auto issue = [&](int p) {
         const unsigned to = sbase + (unsigned)(((p - pfirst) % NS) * STAGE);
         const unsigned kind = (p < k0 || p > k1) ? EDGE : MID;
+        if (TMA) { // thread 0
+            const unsigned b = bar_of(p);
+            stg::mbar_expect_tx(b, A.bytes[kind]);
+            for (int q = 0; q < A.n; ++q)
+                if (A.when[q] & kind) stg::tma_load_4d(to + A.dst[q], &A.map[q], bxi * SX, j0 + A.row0[q], p, 0, b);
+            return;
+        }
         if (r0 < kRowsPerPass)
             for (int R = r0; R < nrow; R += kRowsPerPass) {
                 const stg::Row w = rows[R];
@@ -206,10 +240,22 @@ __global__ void __launch_bounds__(NT, 2)
     };
     // planes pfirst .. pfirst+NS-2 up front; at plane p (once it has landed and every thread is
     // past plane p-1) the slot of plane p-1 takes plane p+NS-1.  One commit group per plane.
-    for (int p = pfirst; p < pfirst + NS - 1; ++p) {
-        if (p <= plast) issue(p);
-        stg::cp_commit();
+    int issued = pfirst - 1; // (TMA) thread 0: the last plane issued
+    if (!TMA) {
+        for (int p = pfirst; p < pfirst + NS - 1; ++p) {
+            if (p <= plast) issue(p);
+            stg::cp_commit();
+        }
+    } else if (t == 0) {
+        for (int q = 0; q < NS; ++q) stg::mbar_init(stg::smem_u32(&bar[q]), 1);
+        stg::fence_mbar_init();
+        stg::fence_proxy_async();
+        for (int p = pfirst; p < pfirst + NS - 1 && p <= plast; ++p) {
+            issue(p);
+            issued = p;
+        }
     }
+    if (TMA) __syncthreads();
 
     const K<T> &kk = kconst<T>(S.k);
     const T dt = sc_dt<T>(S.sc);
@@ -259,13 +305,26 @@ __global__ void __launch_bounds__(NT, 2)
     long long rsum = 0;
     const int r = ty + 1, x = tx + 1; // the thread's cell in the stage
 
+    bool failed = false;
     for (int p = pfirst; p <= plast; ++p) {
-        stg::cp_wait<NS - 2>();
-        __syncthreads(); // (A)
-        {
+        if (!TMA) {
+            stg::cp_wait<NS - 2>();
+            __syncthreads(); // (A)
             const int pn = p + NS - 1;
             if (pn <= plast) issue(pn);
             stg::cp_commit();
+        } else {
+            const bool ok = stg::mbar_wait(bar_of(p), parity_of(p), kLimitNs);
+            if (__syncthreads_or(!ok)) { // (A)
+                failed = true;
+                break;
+            }
+            const int pn = p + NS - 1;
+            if (t == 0 && pn <= plast) {
+                stg::fence_proxy_async();
+                issue(pn);
+                issued = pn;
+            }
         }
         const T *st = (const T *)(sm + ((p - pfirst) % NS) * STAGE);
         const uint8_t *flg = (const uint8_t *)st;
@@ -488,18 +547,40 @@ __global__ void __launch_bounds__(NT, 2)
             }
         }
     }
-    stg::cp_wait<0>();
+    if (!TMA) stg::cp_wait<0>();
+    if (TMA) {
+        if (failed && t == 0) {
+            atomicOr(&S.sc->status, STATUS_STAGING);
+            for (int p = issued - NS + 1 > pfirst ? issued - NS + 1 : pfirst; p <= issued; ++p)
+                stg::mbar_wait(bar_of(p), parity_of(p), kLimitNs);
+        }
+        __syncthreads();
+        if (t == 0)
+            for (int q = 0; q < NS; ++q) stg::mbar_inval(stg::smem_u32(&bar[q]));
+    }
     const BIx bx = {bxi, byi, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y};
     tile_store<T, NT>(S, bx, false, true, 0, 0, 0, rsum);
 }
 
-template <class T> inline void launch(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st) {
+// tma: the TMA form (falls back to the cp.async form when the arrays do not allow it)
+template <class T> inline void launch(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st, bool tma) {
     const int kch = chunk(S.g);
-    k_phase2_phase1<T><<<grid(S.g, kch), dim3(SX, SY), SMEM, st>>>(S, con, fcur, out, kch);
+    stg::TmaArgs A;
+    std::memset(&A, 0, sizeof A);
+    if (tma) {
+        stg::TmaBox B[stg::kMaxBoxes];
+        tma = stg::encode_boxes(A, B, tma_boxes(B, S.g, bases_of(S, con, fcur)));
+    }
+    if (tma)
+        k_phase2_phase1<T, true><<<grid(S.g, kch), dim3(SX, SY), SMEM + 128, st>>>(S, con, fcur, out, kch, A);
+    else
+        k_phase2_phase1<T, false><<<grid(S.g, kch), dim3(SX, SY), SMEM, st>>>(S, con, fcur, out, kch, A);
 }
 template <class T> inline void prepare() {
-    cudaFuncSetAttribute(k_phase2_phase1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-    cudaFuncSetAttribute(k_phase2_phase1<T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_phase2_phase1<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    cudaFuncSetAttribute(k_phase2_phase1<T, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_phase2_phase1<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM + 128);
+    cudaFuncSetAttribute(k_phase2_phase1<T, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 #endif
 

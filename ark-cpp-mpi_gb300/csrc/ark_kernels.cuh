@@ -2340,8 +2340,8 @@ template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur
 }
 
 template <class T>
-void Launch<T>::phase2_phase1(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st) {
-    if constexpr (std::is_same<T, float>::value) s2::launch<float>(S, con, fcur, out, st);
+void Launch<T>::phase2_phase1(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st, bool tma) {
+    if constexpr (std::is_same<T, float>::value) s2::launch<float>(S, con, fcur, out, st, tma);
 }
 template <class T> void Launch<T>::phase2_fused(const DevState<T> &S, int con, int fcur, cudaStream_t st) {
     const int kch = stg::staged_chunk(S.g);

@@ -219,56 +219,61 @@ struct TmaBox {
 };
 constexpr int kMaxBoxes = 6;
 
+// The box of n arrays from base, `astride` bytes apart, cell (face = false) or face rows of g:
+// bw elements by br rows from row j0 + row0, into the stage at dst, loaded by planes of `when`.
+inline TmaBox make_box(const Geom &g, const void *base, int elem, bool face, int narr, long long astride, int bw, int br,
+                       int row0, int dst, unsigned when) {
+    TmaBox q;
+    q.base = base;
+    q.elem = elem;
+    q.dim[0] = face ? g.fs1 : g.cs1;
+    q.dim[1] = face ? g.C2 + 3 : g.C2 + 2;
+    q.dim[2] = face ? g.C3 + 3 : g.C3 + 2;
+    q.dim[3] = narr;
+    q.stride[0] = (face ? g.fs1 : g.cs1) * elem;
+    q.stride[1] = (face ? g.fs2 : g.cs2) * elem;
+    q.stride[2] = astride;
+    q.box[0] = bw;
+    q.box[1] = br;
+    q.box[2] = 1;
+    q.box[3] = narr;
+    q.row0 = row0;
+    q.dst = (unsigned)dst;
+    q.when = when;
+    return q;
+}
+// The stride of n arrays that must lie a fixed stride apart, each of at least min_bytes (0 if
+// they do not, or the stride is no multiple of 16 or not below 2^40, as tensor maps need).
+inline long long block_stride(const void *const *arr, int n, long long min_bytes) {
+    const long long s = (long long)((const char *)arr[1] - (const char *)arr[0]);
+    if (s < min_bytes || s % 16 || s >= (1ll << 40)) return 0;
+    for (int q = 2; q < n; ++q)
+        if ((long long)((const char *)arr[q] - (const char *)arr[0]) != q * s) return 0;
+    return s;
+}
+// The row and plane strides of g in bytes are multiples of 16 (tensor maps need it).
+inline bool rows_fit(const Geom &g) { return (g.cs1 % 16) == 0 && (g.fs1 % 16) == 0 && (g.cs2 % 16) == 0 && (g.fs2 % 16) == 0; }
+
 // The boxes of a launch of the TMA form, from the staged arrays (Bases); 0 when the arrays
 // of a block are not a fixed stride apart (then the cp.async form runs) or a stride is out of
 // the tensor maps' range.
 template <int MODE> inline int tma_boxes(TmaBox *B, const Geom &g, const Bases &b) {
     using L = TLayout<MODE>;
     const long long nc = g.ncell(), nf = g.nface();
-    auto gap = [](const void *x, const void *y) { return (long long)((const char *)x - (const char *)y); };
-    auto fits = [](long long st, long long min_bytes) { return st >= min_bytes && st % 16 == 0 && st < (1ll << 40); };
-    const long long lvs = gap(b.cu[0], b.cr);
-    if (!fits(lvs, nc * 4) || gap(b.cu[1], b.cr) != 2 * lvs || gap(b.cu[2], b.cr) != 3 * lvs) return 0;
+    const void *lv[4] = {b.cr, b.cu[0], b.cu[1], b.cu[2]};
+    const long long lvs = block_stride(lv, 4, nc * 4);
     long long fcs[3];
-    for (int d = 0; d < 3; ++d) {
-        fcs[d] = gap(b.fc[d][1], b.fc[d][0]);
-        if (!fits(fcs[d], nf * 4) || gap(b.fc[d][2], b.fc[d][0]) != 2 * fcs[d] || gap(b.fc[d][3], b.fc[d][0]) != 3 * fcs[d])
-            return 0;
-    }
-    long long ffs = 0;
-    if (L::FIN) {
-        ffs = gap(b.ff[1], b.ff[0]);
-        if (!fits(ffs, nc * 4) || gap(b.ff[2], b.ff[0]) != 2 * ffs) return 0;
-    }
-    if ((g.cs1 * 4) % 16 || (g.cs2 * 4) % 16 || (g.fs2 * 4) % 16 || g.cs1 % 16 || g.cs2 % 16) return 0;
+    for (int d = 0; d < 3; ++d) fcs[d] = block_stride(b.fc[d], 4, nf * 4);
+    const long long ffs = L::FIN ? block_stride(b.ff, 3, nc * 4) : 1;
+    if (!lvs || !fcs[0] || !fcs[1] || !fcs[2] || !ffs || !rows_fit(g)) return 0;
     const unsigned cells_when = L::STRESS ? (DOWN | MID | TOP) : MID;
     int n = 0;
-    auto add = [&](const void *base, int elem, bool face, int narr, long long astride, int bw, int br, int row0,
-                   int dst, unsigned when) {
-        TmaBox &q = B[n++];
-        q.base = base;
-        q.elem = elem;
-        q.dim[0] = face ? g.fs1 : g.cs1;
-        q.dim[1] = face ? g.C2 + 3 : g.C2 + 2;
-        q.dim[2] = face ? g.C3 + 3 : g.C3 + 2;
-        q.dim[3] = narr;
-        q.stride[0] = (face ? g.fs1 : g.cs1) * elem;
-        q.stride[1] = (face ? g.fs2 : g.cs2) * elem;
-        q.stride[2] = astride;
-        q.box[0] = bw;
-        q.box[1] = br;
-        q.box[2] = 1;
-        q.box[3] = narr;
-        q.row0 = row0;
-        q.dst = (unsigned)dst;
-        q.when = when;
-    };
-    add(b.cr, 4, false, 4, lvs, W, L::CROWS, L::CROW0, L::O_LV * 4, cells_when);
-    add(b.fl, 1, false, 1, nc, WF, L::CROWS, L::CROW0, L::FLAG_OFF, cells_when);
-    add(b.fc[0][0], 4, true, 4, fcs[0], W, SY, 0, L::O_F1 * 4, MID);
-    add(b.fc[1][0], 4, true, 4, fcs[1], W, SY + 1, 0, L::O_F2 * 4, MID);
-    add(b.fc[2][0], 4, true, 4, fcs[2], W, SY, 0, L::O_F3 * 4, MID | TOP);
-    if (L::FIN) add(b.ff[0], 4, false, 3, ffs, W, SY, 0, L::O_FF * 4, MID);
+    B[n++] = make_box(g, b.cr, 4, false, 4, lvs, W, L::CROWS, L::CROW0, L::O_LV * 4, cells_when);
+    B[n++] = make_box(g, b.fl, 1, false, 1, nc, WF, L::CROWS, L::CROW0, L::FLAG_OFF, cells_when);
+    B[n++] = make_box(g, b.fc[0][0], 4, true, 4, fcs[0], W, SY, 0, L::O_F1 * 4, MID);
+    B[n++] = make_box(g, b.fc[1][0], 4, true, 4, fcs[1], W, SY + 1, 0, L::O_F2 * 4, MID);
+    B[n++] = make_box(g, b.fc[2][0], 4, true, 4, fcs[2], W, SY, 0, L::O_F3 * 4, MID | TOP);
+    if (L::FIN) B[n++] = make_box(g, b.ff[0], 4, false, 3, ffs, W, SY, 0, L::O_FF * 4, MID);
     return n;
 }
 inline unsigned box_bytes(const TmaBox &q) { return (unsigned)(q.box[0] * q.box[1] * q.box[2] * q.box[3] * q.elem); }
@@ -668,10 +673,8 @@ inline EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// The tensor maps of a launch; false when the arrays do not allow the TMA form.
-template <int MODE> inline bool tma_args(TmaArgs &A, const DevState<float> &S, int src, int fcur) {
-    TmaBox B[kMaxBoxes];
-    const int n = tma_boxes<MODE>(B, S.g, bases_of<MODE>(S, src, fcur));
+// The tensor maps of n boxes; false when there are none or the encoder refuses one.
+inline bool encode_boxes(TmaArgs &A, const TmaBox *B, int n) {
     const EncodeTiledFn enc = encode_tiled();
     if (n <= 0 || !enc) return false;
     std::memset(&A, 0, sizeof A);
@@ -694,6 +697,12 @@ template <int MODE> inline bool tma_args(TmaArgs &A, const DevState<float> &S, i
     }
     A.n = n;
     return true;
+}
+// The tensor maps of a launch; false when the arrays do not allow the TMA form.
+template <int MODE> inline bool tma_args(TmaArgs &A, const DevState<float> &S, int src, int fcur) {
+    TmaBox B[kMaxBoxes];
+    const int n = tma_boxes<MODE>(B, S.g, bases_of<MODE>(S, src, fcur));
+    return encode_boxes(A, B, n);
 }
 
 template <int MODE> inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st) {

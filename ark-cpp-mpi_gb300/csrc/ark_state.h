@@ -306,7 +306,8 @@ template <class T> struct Launch {
     // FP32: the three sweeps and the second Phase1 (UseForces, bulk-flow partials) in one kernel,
     // the new level written to `out` (not a level the launch reads); same results as the
     // separate kernels.  No-op for FP64.
-    static void phase2_phase1(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st);
+    // tma: stage the planes with tensor-map copies (same results)
+    static void phase2_phase1(const DevState<T> &S, int con, int fcur, const Level<T> &out, cudaStream_t st, bool tma = false);
     static void boundary_fill(const DevState<T> &S, int ncon, int axis, int periodic, cudaStream_t st);
     static void sums(const DevState<T> &S, int ncon, cudaStream_t st);
     static void mean_profile(const DevState<T> &S, int ncon, long long *acc, cudaStream_t st);

@@ -329,13 +329,14 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
 
 /* Times the kernel shapes of the step on the live state (it advances) and keeps the fastest,
  * one setting at a time: the shape of the Phase1 with stress (0 one cell per thread, 1
- * marching, 2 staged in shared memory (FP32), 3 face quantities computed once (FP64)), of the
- * second Phase1, the Phase2 form (FP32: three sweep kernels, or one kernel for the three sweeps
- * and the second Phase1), and the x2/x3 sweeps' segment length (8, 16, 32, 64 faces), each
+ * marching, 2 staged in shared memory with cp.async copies (FP32), 3 face quantities computed
+ * once (FP64), 4 staged with TMA tensor copies (FP32)), of the second Phase1, the Phase2 form
+ * (FP32: three sweep kernels, or one kernel for the three sweeps and the second Phase1 with
+ * cp.async or TMA copies), and the x2/x3 sweeps' segment length (8, 16, 32, 64 faces), each
  * candidate timed three times (best kept).  The results do not depend on the shapes.  choice
  * (5 ints, may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step, Phase2
  * form: 0 sweep kernels, 1 one sweep kernel (only by ARK_PHASE2_FUSED=1), 2 sweeps and second
- * Phase1 in one kernel}. */
+ * Phase1 in one kernel, 3 the same with TMA copies}. */
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice);
 
 /* ---- ensembles: many independent channels in one launch per phase ------------------------

@@ -534,8 +534,9 @@ def test_fused_phase2_agrees(ark, port, monkeypatch, C, px, pz):
 @pytest.mark.parametrize("C,px,pz", [((40, 20, 36), True, True), ((130, 9, 70), True, True), ((70, 6, 5), False, False),
                                      ((64, 4, 1), True, False), ((65, 31, 17), True, True), ((33, 3, 9), False, True)])
 def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
-    """FP32: Phase2 and the second Phase1 in one kernel (ARK_PHASE2_FUSED=2, new level through
-    the spare buffer) give the bits of the separate kernels over several steps (both face
+    """FP32: Phase2 and the second Phase1 in one kernel (ARK_PHASE2_FUSED=2 with cp.async copies,
+    3 with TMA tensor copies; new level through the spare buffer) give the bits of the separate
+    kernels over several steps (both face
     generations, both buffer rotations), periodic and bounded axes, ragged tiles; the per-launch
     timings name its five launches.  Interior cells and computed faces are compared: ghost cells
     are each form's scratch (the separate kernels read no x ghost of the half-step level, so they
@@ -543,7 +544,7 @@ def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
     p = port.channel_params(*C, seed=29)
     st0 = port.channel_state(p)
     outs = []
-    for mode in ("0", "2"):
+    for mode in ("0", "2", "3"):
         monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
         P = params_from(ark, p, precision=ark.FP32)
         P.periodic_x, P.periodic_z = int(px), int(pz)
@@ -555,9 +556,10 @@ def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
             c.sync()
             outs.append(c.download(CELLS + FACES))
             names = [n for n, _ in kt]
-            if mode == "2":
+            if mode != "0":
                 assert names == ["finalize_dt", "wrap_con", "phase1_stress_forces", "wrap_phase2", "phase2_phase1_forces"]
             else:
                 assert len(names) == 8 and names[-1] == "phase1_forces"
-    for n in CELLS + FACES:
-        assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), n
+    for o in outs[1:]:
+        for n in CELLS + FACES:
+            assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), n
