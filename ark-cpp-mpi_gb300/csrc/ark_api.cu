@@ -588,9 +588,10 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     ctx->march[1] = params->precision == ARK_FP32 ? 4 : 3;
     if (const char *e = std::getenv("ARK_PHASE1_MARCH")) { // "ab": a for Phase1 with stress, b without
         // 0: one cell per thread, 1: marching, 2: planes staged in shared memory (FP32 only),
-        // 3: face quantities computed once (FP64 only), 4: staged with TMA copies (FP32 only)
+        // 3: face quantities computed once (FP64 only), 4: staged with TMA copies (FP32 only),
+        // 5: the same on 32 x 8 tiles
         auto ok = [&](char ch) {
-            return ch >= '0' && ch <= '1' ? true : (params->precision == ARK_FP32 ? ch == '2' || ch == '4' : ch == '3');
+            return ch >= '0' && ch <= '1' ? true : (params->precision == ARK_FP32 ? ch == '2' || ch == '4' || ch == '5' : ch == '3');
         };
         if (ok(e[0])) ctx->march[0] = e[0] - '0';
         if (e[0] && ok(e[1])) ctx->march[1] = e[1] - '0';

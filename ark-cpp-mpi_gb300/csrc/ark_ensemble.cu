@@ -130,6 +130,41 @@ __global__ void __launch_bounds__(stg::NT, 2) kb_phase1_staged(const DS *__restr
     }
 }
 
+// The tensor maps of a member for the TMA form of the staged Phase1 (64 x 4 tiles), in global
+// memory: the level boxes with the stress's rows (6) or without (4), per level; the flags
+// likewise; the face sets per generation; the forces.
+struct MemberMaps {
+    CUtensorMap lv[2][2]; // [0 with the stress, 1 without][level]
+    CUtensorMap fl[2];    // [0 with the stress, 1 without]
+    CUtensorMap fc[2][3]; // [generation][direction]
+    CUtensorMap ff;
+};
+
+// The staged Phase1 with TMA copies: work item = a member's 64 x 4 tile and chunk of planes,
+// the single-context TMA kernel's body with the member's maps (fenced for the copy engine
+// once per work item).
+template <int MODE>
+__global__ void __launch_bounds__(stg::NT, 2) kb_phase1_tma(const DS *__restrict__ inst, const MemberMaps *__restrict__ maps,
+                                                            const __grid_constant__ stg::BoxMeta meta, WorkList W, int src,
+                                                            int dst, int fcur) {
+    constexpr bool STRESS = (MODE & P1_STRESS) != 0;
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    __shared__ __align__(8) unsigned long long bar[stg::TLayout<MODE>::NS];
+    unsigned char *const sm = stg::align128(sm_raw);
+    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+        const int q = find_member(W, b);
+        const MemberMaps *M = maps + q;
+        auto map = [&](int k) -> const CUtensorMap * {
+            if (k == 0) return &M->lv[STRESS ? 0 : 1][src];
+            if (k == 1) return &M->fl[STRESS ? 0 : 1];
+            if (k <= 4) return &M->fc[fcur][k - 2];
+            return &M->ff;
+        };
+        stg::phase1_tma_body<MODE, stg::SX, stg::SY>(inst[q], map, meta, true, src, dst, W.extra[q], decode(W, q, b), sm, bar);
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(128) kb_sweep_x(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
@@ -151,7 +186,8 @@ enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, 
 // The candidate kernel shapes the autotuner chooses between.
 struct Shape {
     int march_a, march_b; // Phase1 with stress / second Phase1: 0 one cell per thread, 1 marching,
-                          // 2 planes staged in shared memory
+                          // 2 planes staged in shared memory (cp.async copies), 4 the same with
+                          // TMA tensor copies
     int seg;              // target faces per thread segment in the x2/x3 sweeps
 };
 
@@ -174,7 +210,9 @@ struct ark_ensemble {
     WrapJob *d_jobs = nullptr; // [6][n]: wrap_con for level 0/1, wrap_phase2 for (con, fcur)
     int persist = 1;           // persistent blocks per launch (all SMs x resident blocks)
     int persist_staged = 1;    // the same for the staged Phase1 (2 blocks of 256 threads per SM)
-    Shape shape = {2, 2, 32}; // staged Phase1 for both launches: what the autotuner picks on mixed ensembles
+    Shape shape = {4, 4, 32}; // staged Phase1 with TMA copies for both launches
+    MemberMaps *d_maps = nullptr;   // the members' tensor maps (null: the TMA form falls back)
+    stg::BoxMeta meta[2] = {};      // its boxes with the stress and without
     int con = 0, fcur = 0;
     bool parts_valid = false;
     bool uploaded_all = false;
@@ -198,22 +236,29 @@ template <class U> int ens_alloc(ark_ensemble *E, U **out, size_t n) {
 // rows padded as the staged Phase1 needs (its 68-value row segments stay inside a row)
 Geom geom_of(const ark_params &p) { return device_geom(p.n1_cells, p.n2_cells, p.n3_cells, true); }
 
+// n arrays of `each` floats in one allocation, a fixed stride apart (one tensor map covers them)
+int ens_block(ark_ensemble *E, float **const *out, int n, size_t each) {
+    float *base = nullptr;
+    if (int rc = ens_alloc(E, &base, each * n)) return rc;
+    for (int q = 0; q < n; ++q) *out[q] = base + each * q;
+    return ARK_OK;
+}
+
 int alloc_member(ark_ensemble *E, DS &S) {
     const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
     int rc = 0;
     for (int l = 0; l < 2; ++l) {
-        rc |= ens_alloc(E, &S.lv[l].ro, nc);
-        rc |= ens_alloc(E, &S.lv[l].u1, nc);
-        rc |= ens_alloc(E, &S.lv[l].u2, nc);
-        rc |= ens_alloc(E, &S.lv[l].u3, nc);
+        float **lv[4] = {&S.lv[l].ro, &S.lv[l].u1, &S.lv[l].u2, &S.lv[l].u3};
+        rc |= ens_block(E, lv, 4, nc);
     }
-    for (int m = 0; m < 3; ++m) rc |= ens_alloc(E, &S.f[m], nc);
+    float **ff[3] = {&S.f[0], &S.f[1], &S.f[2]};
+    rc |= ens_block(E, ff, 3, nc);
     for (int gen = 0; gen < 2; ++gen)
         for (int d = 0; d < 3; ++d) {
             FaceSet<float> &F = S.fc[gen][d];
-            rc |= ens_alloc(E, &F.p, nf);
+            float **fs[4] = {&F.p, &F.u[0], &F.u[1], &F.u[2]};
+            rc |= ens_block(E, fs, 4, nf);
             F.ro = nullptr; // FP32 derives face density from p
-            for (int m = 0; m < 3; ++m) rc |= ens_alloc(E, &F.u[m], nf);
         }
     for (int d = 0; d < 3; ++d)
         for (int m = 0; m < 3; ++m) S.sig[d][m] = nullptr;
@@ -222,6 +267,36 @@ int alloc_member(ark_ensemble *E, DS &S) {
     rc |= ens_alloc(E, &S.part_max, 3 * (size_t)kBuckets);
     rc |= ens_alloc(E, &S.part_sum, (size_t)kBuckets);
     return rc ? ARK_ERR_NOMEM : ARK_OK;
+}
+
+// The members' tensor maps for the TMA form of the staged Phase1 (left null, so that the
+// cp.async form runs, when a member's arrays do not allow it or the encoder is missing).
+int build_maps(ark_ensemble *E) {
+    constexpr int MS = P1_STRESS | P1_FORCES | P1_RMAX, MF = P1_FORCES | P1_RSUM;
+    std::vector<MemberMaps> h(E->n);
+    std::memset(h.data(), 0, sizeof(MemberMaps) * h.size());
+    for (int q = 0; q < E->n; ++q) {
+        const DS &S = E->S[q];
+        for (int l = 0; l < 2; ++l)
+            for (int gen = 0; gen < 2; ++gen) {
+                stg::TmaBox B[stg::kMaxBoxes], F[stg::kMaxBoxes];
+                const int ns = stg::tma_boxes<MS>(B, S.g, stg::bases_of<MS>(S, l, gen));
+                const int nf = stg::tma_boxes<MF>(F, S.g, stg::bases_of<MF>(S, l, gen));
+                if (ns != 5 || nf != 6) return ARK_OK;
+                bool ok = stg::encode_box(&h[q].lv[0][l], B[0]) && stg::encode_box(&h[q].lv[1][l], F[0]) &&
+                          stg::encode_box(&h[q].fl[0], B[1]) && stg::encode_box(&h[q].fl[1], F[1]) &&
+                          stg::encode_box(&h[q].ff, F[5]);
+                for (int d = 0; d < 3; ++d) ok = ok && stg::encode_box(&h[q].fc[gen][d], B[2 + d]);
+                if (!ok) return ARK_OK;
+                if (q == 0 && l == 0 && gen == 0) {
+                    stg::box_meta(E->meta[0], B, ns);
+                    stg::box_meta(E->meta[1], F, nf);
+                }
+            }
+    }
+    if (int rc = ens_alloc(E, &E->d_maps, h.size())) return rc;
+    ENS_CUDA(cudaMemcpy(E->d_maps, h.data(), sizeof(MemberMaps) * h.size(), cudaMemcpyHostToDevice));
+    return ARK_OK;
 }
 
 int segment_for(int nd, int target) {
@@ -347,7 +422,11 @@ int grid_of(const ark_ensemble *E, int kind) { return std::max(1, std::min(E->to
 
 template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst, int fcur) {
     const dim3 blk(kTileX, kTileY);
-    if (march == 2) {
+    if (march == 4 && E->d_maps) {
+        const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
+        kb_phase1_tma<MODE><<<grid, dim3(stg::SX, stg::SY), stg::TLayout<MODE>::SMEM + 128, E->st>>>(
+            E->d_inst, E->d_maps, E->meta[(MODE & P1_STRESS) ? 0 : 1], wl(E, WL_STAGED), src, dst, fcur);
+    } else if (march == 2 || march == 4) {
         const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
         kb_phase1_staged<MODE><<<grid, dim3(stg::SX, stg::SY), stg::Layout<MODE>::SMEM, E->st>>>(
             E->d_inst, wl(E, WL_STAGED), src, dst, fcur);
@@ -371,6 +450,10 @@ int prepare_staged_kernels(int sms) {
     per = std::min(per, one(kb_phase1_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
                             stg::Layout<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>::SMEM));
     per = std::min(per, one(kb_phase1_staged<P1_FORCES | P1_RSUM>, stg::Layout<P1_FORCES | P1_RSUM>::SMEM));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_RMAX>, stg::TLayout<P1_STRESS | P1_FORCES | P1_RMAX>::SMEM + 128));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
+                            stg::TLayout<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>::SMEM + 128));
+    per = std::min(per, one(kb_phase1_tma<P1_FORCES | P1_RSUM>, stg::TLayout<P1_FORCES | P1_RSUM>::SMEM + 128));
     return sms * std::max(per, 1);
 }
 
@@ -519,7 +602,9 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_phase1<P1_FORCES | P1_RSUM, false>, kTileX * kTileY, 0);
     E->persist = sms * std::max(per, 1) * 2;
     E->persist_staged = prepare_staged_kernels(sms);
-    if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get()))) return nullptr;
+    stg::encode_tiled(); // looked up here, outside any stream capture
+    if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get())) || (*status = build_maps(E.get())))
+        return nullptr;
     cudaEventCreate(&E->ev0);
     cudaEventCreate(&E->ev1);
     *status = ARK_OK;
@@ -756,8 +841,9 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
     if (steps_per_candidate < 1) return efail(ARK_ERR_PARAM, "steps_per_candidate < 1");
     for (char u : E->uploaded)
         if (!u) return efail(ARK_ERR_STATE, "every member needs a state before tuning");
-    const Shape cands[] = {{1, 0, 32}, {0, 0, 32}, {1, 1, 32}, {0, 1, 32}, {1, 0, 16}, {1, 0, 64},
-                           {0, 0, 16}, {0, 0, 64}, {2, 2, 32}, {2, 0, 32}, {0, 2, 32}, {2, 2, 64}, {2, 0, 64}};
+    const Shape cands[] = {{1, 0, 32}, {0, 0, 32}, {1, 1, 32}, {0, 1, 32}, {1, 0, 16}, {1, 0, 64}, {0, 0, 16},
+                           {0, 0, 64}, {2, 2, 32}, {2, 0, 32}, {0, 2, 32}, {2, 2, 64}, {2, 0, 64}, {4, 4, 32},
+                           {4, 4, 64}, {4, 4, 16}, {4, 2, 32}, {2, 4, 32}, {4, 0, 32}};
     Shape best = E->shape;
     double best_ms = 1e300;
     if (int rc = ensure_parts(E)) return rc;
@@ -789,7 +875,8 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
 int ark_ensemble_set_shape(ark_ensemble *E, int march_a, int march_b, int segment) {
     if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
     if (segment < 1) return efail(ARK_ERR_PARAM, "segment < 1");
-    if (march_a < 0 || march_a > 2 || march_b < 0 || march_b > 2) return efail(ARK_ERR_PARAM, "march must be 0, 1 or 2");
+    auto ok = [](int m) { return (m >= 0 && m <= 2) || m == 4; };
+    if (!ok(march_a) || !ok(march_b)) return efail(ARK_ERR_PARAM, "march must be 0, 1, 2 or 4");
     E->shape = Shape{march_a, march_b, segment};
     drop_graphs(E);
     return build_lists(E);

@@ -217,8 +217,8 @@ void expand_boxes(const stg::TmaBox *B, int n, unsigned kind, int x0, int j0, in
 // lays them out (rows past a block's last row as zero fill), with the tensor copies' rules
 // checked (16-byte global strides, x offsets and box rows; 128-byte aligned destinations; box
 // sizes at most 256), then every read of every thread as above.
-template <int MODE> struct TmaCheck {
-    using L = stg::TLayout<MODE>;
+template <int MODE, int TSX, int TSY> struct TmaCheck {
+    using L = stg::TLayout<MODE, TSX, TSY>;
     static constexpr long long kS = 1ll << 36; // fake array spacing (tensor-map strides stay below 2^40)
     enum { T_CR = 0, T_CU = 1, T_FL = 4, T_FC = 5, T_FF = 17, T_N = 20 };
     const Geom g;
@@ -242,13 +242,13 @@ template <int MODE> struct TmaCheck {
             for (int a = 0; a < 4; ++a) b.fc[d][a] = (const void *)((T_FC + 4 * d + a) * kS);
         for (int m = 0; m < 3; ++m) b.ff[m] = (const void *)((T_FF + m) * kS);
         stg::TmaBox B[stg::kMaxBoxes];
-        const int n = stg::tma_boxes<MODE>(B, g, b);
+        const int n = stg::tma_boxes<MODE, TSX, TSY>(B, g, b);
         if (n <= 0) {
             fail("no TMA plan for these arrays", 0, 0, 0, n);
             return;
         }
         check_boxes(B, n, L::STAGE, [&](const char *w, long long v) { fail(w, 0, 0, 0, v); });
-        const dim3 grid = stg::staged_grid(g, kch);
+        const dim3 grid = stg::tile_grid<TSX, TSY>(g, kch);
         std::vector<std::vector<long long>> map;
         for (int bz = 0; bz < (int)grid.z; ++bz)
             for (int by = 0; by < (int)grid.y; ++by)
@@ -258,12 +258,12 @@ template <int MODE> struct TmaCheck {
                     map.assign(plast - pfirst + 1, std::vector<long long>(L::STAGE, -1));
                     for (int p = pfirst; p <= plast; ++p) {
                         const unsigned kind = p < k0 ? stg::DOWN : (p > k1 ? stg::TOP : stg::MID);
-                        expand_boxes(B, n, kind, bx * stg::SX, by * stg::SY + 1, p, map[p - pfirst],
+                        expand_boxes(B, n, kind, bx * TSX, by * TSY + 1, p, map[p - pfirst],
                                      [&](const char *w, long long v) { fail(w, bx, by, p, v); });
                     }
-                    for (int ty = 0; ty < stg::SY; ++ty)
-                        for (int tx = 0; tx < stg::SX; ++tx) {
-                            const int i = bx * stg::SX + tx + 1, j = by * stg::SY + ty + 1;
+                    for (int ty = 0; ty < TSY; ++ty)
+                        for (int tx = 0; tx < TSX; ++tx) {
+                            const int i = bx * TSX + tx + 1, j = by * TSY + ty + 1;
                             if (i > g.C1 || j > g.C2) continue;
                             const Ids id = {T_CU, T_CR, T_FL, T_FC, T_FF};
                             for (int k = k0; k <= k1; ++k)
@@ -489,19 +489,23 @@ int staging_plan_check(int C1, int C2, int C3, int kch_in, char *msg, int cap) {
     b.run(kch);
     PlanCheck<P1_FORCES | P1_RSUM> c(g);
     c.run(kch);
-    TmaCheck<P1_STRESS | P1_FORCES | P1_RMAX> ta(g);
+    TmaCheck<P1_STRESS | P1_FORCES | P1_RMAX, 64, 4> ta(g);
     ta.run(kch);
-    TmaCheck<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX> tb(g);
+    TmaCheck<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 64, 4> tb(g);
     tb.run(kch);
-    TmaCheck<P1_FORCES | P1_RSUM> tc(g);
+    TmaCheck<P1_FORCES | P1_RSUM, 64, 4> tc(g);
     tc.run(kch);
+    TmaCheck<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 32, 8> td(g);
+    td.run(kch);
+    TmaCheck<P1_FORCES | P1_RSUM, 32, 8> te(g);
+    te.run(kch);
     char m2[256] = {0};
     const int d = step2_plan_check(C1, C2, C3, kch_in, m2, (int)sizeof m2);
     std::string e = std::string(m2);
-    for (const std::string *x : {&tc.err, &tb.err, &ta.err, &c.err, &b.err, &a.err})
+    for (const std::string *x : {&te.err, &td.err, &tc.err, &tb.err, &ta.err, &c.err, &b.err, &a.err})
         if (!x->empty()) e = *x;
     if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", e.c_str());
-    return a.bad + b.bad + c.bad + ta.bad + tb.bad + tc.bad + d;
+    return a.bad + b.bad + c.bad + ta.bad + tb.bad + tc.bad + td.bad + te.bad + d;
 }
 
 } // namespace ark

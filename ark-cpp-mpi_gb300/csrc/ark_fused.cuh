@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(NT, 2)
     extern __shared__ __align__(128) unsigned char sm_raw[];
     __shared__ __align__(8) unsigned long long bar[NS];
     // the stages from the first 128-byte boundary (tensor copies land on 128-byte boundaries)
-    unsigned char *const sm = TMA ? sm_raw + ((128u - (stg::smem_u32(sm_raw) & 127u)) & 127u) : sm_raw;
+    unsigned char *const sm = TMA ? stg::align128(sm_raw) : sm_raw;
     __shared__ stg::Row rows[stg::kMaxRows], frows[stg::kMaxFlagRows];
     __shared__ int nrow, nfrow;
     __shared__ Behind XB[SY][SX + 1]; // x: index x holds cell i0-1+x
@@ -222,9 +222,9 @@ __global__ void __launch_bounds__(NT, 2)
         const unsigned kind = (p < k0 || p > k1) ? EDGE : MID;
         if (TMA) { // thread 0
             const unsigned b = bar_of(p);
-            stg::mbar_expect_tx(b, A.bytes[kind]);
-            for (int q = 0; q < A.n; ++q)
-                if (A.when[q] & kind) stg::tma_load_4d(to + A.dst[q], &A.map[q], bxi * SX, j0 + A.row0[q], p, 0, b);
+            stg::mbar_expect_tx(b, A.m.bytes[kind]);
+            for (int q = 0; q < A.m.n; ++q)
+                if (A.m.when[q] & kind) stg::tma_load_4d(to + A.m.dst[q], &A.map[q], bxi * SX, j0 + A.m.row0[q], p, 0, b);
             return;
         }
         if (r0 < kRowsPerPass)

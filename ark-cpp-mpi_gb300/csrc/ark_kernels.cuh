@@ -2258,15 +2258,13 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
             case P1_FORCES | P1_RSUM: stg::launch_staged<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st); return;
             default: march = 0; break;
             }
-        } else if (march == 4) {
+        } else if (march == 4 || march == 5) { // TMA copies, 64 x 4 or 32 x 8 tiles
+            constexpr int A = P1_STRESS | P1_FORCES | P1_RMAX, B = A | P1_BULK, C = P1_FORCES | P1_RSUM;
+            const bool wide = march == 4;
             switch (mode) {
-            case P1_STRESS | P1_FORCES | P1_RMAX:
-                stg::launch_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX>(S, src, dst, fcur, st);
-                return;
-            case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
-                stg::launch_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(S, src, dst, fcur, st);
-                return;
-            case P1_FORCES | P1_RSUM: stg::launch_staged_tma<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st); return;
+            case A: wide ? stg::launch_staged_tma<A, 64, 4>(S, src, dst, fcur, st) : stg::launch_staged_tma<A, 32, 8>(S, src, dst, fcur, st); return;
+            case B: wide ? stg::launch_staged_tma<B, 64, 4>(S, src, dst, fcur, st) : stg::launch_staged_tma<B, 32, 8>(S, src, dst, fcur, st); return;
+            case C: wide ? stg::launch_staged_tma<C, 64, 4>(S, src, dst, fcur, st) : stg::launch_staged_tma<C, 32, 8>(S, src, dst, fcur, st); return;
             default: march = 0; break;
             }
         }
@@ -2290,9 +2288,12 @@ template <class T> void Launch<T>::prepare() {
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_RMAX>();
         stg::prepare_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>();
         stg::prepare_staged<P1_FORCES | P1_RSUM>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>();
-        stg::prepare_staged_tma<P1_FORCES | P1_RSUM>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 64, 4>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 64, 4>();
+        stg::prepare_staged_tma<P1_FORCES | P1_RSUM, 64, 4>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 32, 8>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 32, 8>();
+        stg::prepare_staged_tma<P1_FORCES | P1_RSUM, 32, 8>();
         s2::prepare<float>();
     }
 }

@@ -56,12 +56,16 @@ template <int MODE> struct Layout {
     __host__ __device__ static int ff(int m, int ty, int cx) { return (O_FF + m * SY + ty) * W + cx; }
 };
 
-// The TMA form's stage: one box per block of arrays, each at a 128-byte boundary.  The level's
-// four arrays (ro first) all take the cell rows (the stress's halo rows of ro are copied too).
+// The TMA form's stage for a TSX x TSY tile: one box per block of arrays, each at a 128-byte
+// boundary.  The level's four arrays (ro first) all take the cell rows (the stress's halo rows
+// of ro are copied too).  Rows of W = TSX + 4 values (cells i0-1 .. i0+TSX+2) and WF flag bytes
+// (TSX + 2 rounded up to 16).  Five stages when two blocks per SM hold them, else four.
 constexpr int pad32(int f) { return (f + 31) / 32 * 32; } // floats to a 128-byte boundary
-template <int MODE> struct TLayout {
+template <int MODE, int TSX = 64, int TSY = 4> struct TLayout {
     static constexpr bool STRESS = (MODE & P1_STRESS) != 0;
     static constexpr bool FIN = !STRESS && (MODE & P1_FORCES) != 0;
+    static constexpr int SX = TSX, SY = TSY, NT = TSX * TSY;
+    static constexpr int W = TSX + 4, WF = (TSX + 2 + 15) / 16 * 16;
     static constexpr int CROWS = STRESS ? SY + 2 : SY;
     static constexpr int CROW0 = STRESS ? -1 : 0;
     static constexpr int O_LV = 0;                                  // ro, u1, u2, u3: CROWS rows each
@@ -72,7 +76,12 @@ template <int MODE> struct TLayout {
     static constexpr int END = pad32(O_FF + (FIN ? 3 * SY * W : 0));
     static constexpr int FLAG_OFF = END * 4;
     static constexpr int STAGE = (FLAG_OFF + CROWS * WF + 127) / 128 * 128;
+    // two blocks per SM (228 KB of shared memory, 1 KB of it reserved per block; 128 bytes for
+    // the alignment of the stages, 512 of static shared memory)
+    static constexpr int NS = 2 * (5 * STAGE + 128 + 512 + 1024) <= 228 * 1024 ? 5 : 4;
     static constexpr int SMEM = NS * STAGE;
+    static_assert(2 * (SMEM + 128 + 512 + 1024) <= 228 * 1024, "TMA stages: two blocks per SM");
+    static_assert(W * 4 % 16 == 0 && TSX % 16 == 0, "rows of whole 16-byte units from 16-byte aligned x");
     __host__ __device__ static int cu(int m, int cr, int cx) { return O_LV + ((m + 1) * CROWS + cr) * W + cx; }
     __host__ __device__ static int ro(int ty, int cx) { return O_LV + (ty - CROW0) * W + cx; }
     __host__ __device__ static int flag(int cr, int cx) { return FLAG_OFF + cr * WF + cx; }
@@ -81,11 +90,6 @@ template <int MODE> struct TLayout {
     }
     __host__ __device__ static int ff(int m, int ty, int cx) { return O_FF + (m * SY + ty) * W + cx; }
 };
-// two blocks per SM (228 KB of shared memory, 1 KB of it reserved per block; 128 bytes for the
-// alignment of the stages, 512 of static shared memory)
-static_assert(2 * (TLayout<P1_FORCES | P1_RSUM>::SMEM + 128 + 512 + 1024) <= 228 * 1024, "TMA stages: two blocks per SM");
-static_assert(2 * (TLayout<P1_STRESS | P1_FORCES | P1_RMAX>::SMEM + 128 + 512 + 1024) <= 228 * 1024,
-              "TMA stages: two blocks per SM");
 
 // The cp.async form's offsets as free functions (the host plan check uses them).
 template <int MODE> __host__ __device__ inline int off_cu(int m, int cr, int cx) { return Layout<MODE>::cu(m, cr, cx); }
@@ -199,6 +203,16 @@ inline int staged_chunk(const Geom &g) {
     return (int)k;
 }
 inline dim3 staged_grid(const Geom &g, int kch) { return dim3(tiles_x(g), (g.C2 + SY - 1) / SY, (g.C3 + kch - 1) / kch); }
+// The same for a TSX x TSY tile of the TMA form.
+template <int TSX, int TSY> inline int tile_chunk(const Geom &g) {
+    const long long cols = (long long)((g.C1 + TSX - 1) / TSX) * ((g.C2 + TSY - 1) / TSY);
+    long long k = (long long)g.C3 * cols / (152 * 2 * 8);
+    k = k < 8 ? 8 : (k > 64 ? 64 : k);
+    return (int)k;
+}
+template <int TSX, int TSY> inline dim3 tile_grid(const Geom &g, int kch) {
+    return dim3((g.C1 + TSX - 1) / TSX, (g.C2 + TSY - 1) / TSY, (g.C3 + kch - 1) / kch);
+}
 
 
 // ---- TMA form: the boxes of a plane ----
@@ -257,8 +271,8 @@ inline bool rows_fit(const Geom &g) { return (g.cs1 % 16) == 0 && (g.fs1 % 16) =
 // The boxes of a launch of the TMA form, from the staged arrays (Bases); 0 when the arrays
 // of a block are not a fixed stride apart (then the cp.async form runs) or a stride is out of
 // the tensor maps' range.
-template <int MODE> inline int tma_boxes(TmaBox *B, const Geom &g, const Bases &b) {
-    using L = TLayout<MODE>;
+template <int MODE, int TSX = 64, int TSY = 4> inline int tma_boxes(TmaBox *B, const Geom &g, const Bases &b) {
+    using L = TLayout<MODE, TSX, TSY>;
     const long long nc = g.ncell(), nf = g.nface();
     const void *lv[4] = {b.cr, b.cu[0], b.cu[1], b.cu[2]};
     const long long lvs = block_stride(lv, 4, nc * 4);
@@ -268,12 +282,12 @@ template <int MODE> inline int tma_boxes(TmaBox *B, const Geom &g, const Bases &
     if (!lvs || !fcs[0] || !fcs[1] || !fcs[2] || !ffs || !rows_fit(g)) return 0;
     const unsigned cells_when = L::STRESS ? (DOWN | MID | TOP) : MID;
     int n = 0;
-    B[n++] = make_box(g, b.cr, 4, false, 4, lvs, W, L::CROWS, L::CROW0, L::O_LV * 4, cells_when);
-    B[n++] = make_box(g, b.fl, 1, false, 1, nc, WF, L::CROWS, L::CROW0, L::FLAG_OFF, cells_when);
-    B[n++] = make_box(g, b.fc[0][0], 4, true, 4, fcs[0], W, SY, 0, L::O_F1 * 4, MID);
-    B[n++] = make_box(g, b.fc[1][0], 4, true, 4, fcs[1], W, SY + 1, 0, L::O_F2 * 4, MID);
-    B[n++] = make_box(g, b.fc[2][0], 4, true, 4, fcs[2], W, SY, 0, L::O_F3 * 4, MID | TOP);
-    if (L::FIN) B[n++] = make_box(g, b.ff[0], 4, false, 3, ffs, W, SY, 0, L::O_FF * 4, MID);
+    B[n++] = make_box(g, b.cr, 4, false, 4, lvs, L::W, L::CROWS, L::CROW0, L::O_LV * 4, cells_when);
+    B[n++] = make_box(g, b.fl, 1, false, 1, nc, L::WF, L::CROWS, L::CROW0, L::FLAG_OFF, cells_when);
+    B[n++] = make_box(g, b.fc[0][0], 4, true, 4, fcs[0], L::W, L::SY, 0, L::O_F1 * 4, MID);
+    B[n++] = make_box(g, b.fc[1][0], 4, true, 4, fcs[1], L::W, L::SY + 1, 0, L::O_F2 * 4, MID);
+    B[n++] = make_box(g, b.fc[2][0], 4, true, 4, fcs[2], L::W, L::SY, 0, L::O_F3 * 4, MID | TOP);
+    if (L::FIN) B[n++] = make_box(g, b.ff[0], 4, false, 3, ffs, L::W, L::SY, 0, L::O_FF * 4, MID);
     return n;
 }
 inline unsigned box_bytes(const TmaBox &q) { return (unsigned)(q.box[0] * q.box[1] * q.box[2] * q.box[3] * q.elem); }
@@ -518,13 +532,17 @@ template <int MODE> inline void prepare_staged() {
 }
 
 // ---- TMA form: the kernel ----
-// The tensor maps of a launch (kernel parameters) and what each box loads.
-struct TmaArgs {
-    CUtensorMap map[kMaxBoxes];
+// What each box of a launch loads (the same for every grid of one kernel form).
+struct BoxMeta {
     int row0[kMaxBoxes];
     unsigned dst[kMaxBoxes], when[kMaxBoxes];
     unsigned bytes[5]; // the bytes a plane of kind DOWN (1), MID (2) or TOP (4) brings
     int n;
+};
+// The tensor maps of a launch (kernel parameters) and their boxes.
+struct TmaArgs {
+    CUtensorMap map[kMaxBoxes];
+    BoxMeta m;
 };
 
 __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
@@ -556,6 +574,10 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, unsigne
     return true;
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// A tensor map in global memory (written before the launch) made visible to the copy engine.
+__device__ __forceinline__ void fence_tensormap(const CUtensorMap *m) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
+}
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 // One 4-D box (x, row, plane, array) into shared memory, completing on bar.
 __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map, int x, int y, int z, int w, unsigned bar) {
@@ -564,29 +586,30 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
                  : "memory");
 }
 
-// The staged Phase1 with TMA copies: tile (blockIdx.x, blockIdx.y) of 64 x 4 columns, planes of
-// chunk blockIdx.z.  Thread 0 issues a plane's boxes into its stage (NS stages, one mbarrier
-// each); every thread waits for the planes it reads on their mbarriers.  Same plane order and
-// ring as the cp.async form: at plane k, once plane k + 1 has landed and every thread is past
-// plane k - 1, the slot of the plane no longer needed takes the next plane.  A wait that does
-// not end within half a second sets STATUS_STAGING, and the block lets its copies in flight
-// land (again with a limit) and leaves.
-template <int MODE>
-__global__ void __launch_bounds__(NT, 2)
-    k_phase1_tma(const __grid_constant__ DevState<float> S, const __grid_constant__ TmaArgs A, int src, int dst, int kch) {
-    using L = TLayout<MODE>;
+// One block's work in the staged Phase1 with TMA copies: tile (bx.x, bx.y) of TSX x TSY columns,
+// planes of chunk bx.z (kch planes).  Thread 0 issues a plane's boxes into its stage (NS
+// stages, one mbarrier each in bar); every thread waits for the planes it reads on their
+// mbarriers.  Same plane order and ring as the cp.async form: at plane k, once plane k + 1 has
+// landed and every thread is past plane k - 1, the slot of the plane no longer needed takes
+// the next plane.  map(q) is box q's tensor map (global maps are fenced for the tensor-map
+// proxy first when fence_maps is set).  A wait that does not end within half a second sets
+// STATUS_STAGING, and the block lets its copies in flight land (again with a limit) and
+// leaves.  Every thread calls it; it ends with no copy in flight and the mbarriers
+// invalidated, so a persistent kernel may run it again.
+template <int MODE, int TSX, int TSY, class Maps>
+__device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
+                                                int src, int dst, int kch, const BIx &bx, unsigned char *sm,
+                                                unsigned long long *bar) {
+    using L = TLayout<MODE, TSX, TSY>;
     using T = float;
     constexpr bool STRESS = L::STRESS;
+    constexpr int NS = L::NS, SX = TSX, SY = TSY, NT = TSX * TSY;
     constexpr unsigned long long kLimitNs = 500000000ull;
-    extern __shared__ __align__(128) unsigned char sm_raw[];
-    __shared__ __align__(8) unsigned long long bar[NS];
-    // the stages from the first 128-byte boundary (tensor copies land on 128-byte boundaries)
-    unsigned char *const sm = sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u);
     const Geom g = S.g;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * SX + tx;
-    const int i = blockIdx.x * SX + tx + 1, j = blockIdx.y * SY + ty + 1;
-    const int x0 = blockIdx.x * SX, j0 = blockIdx.y * SY + 1;
-    const int k0 = blockIdx.z * kch + 1;
+    const int i = bx.x * SX + tx + 1, j = bx.y * SY + ty + 1;
+    const int x0 = bx.x * SX, j0 = bx.y * SY + 1;
+    const int k0 = bx.z * kch + 1;
     const int k1 = k0 + kch - 1 < g.C3 ? k0 + kch - 1 : g.C3;
     const int pfirst = STRESS ? k0 - 1 : k0, plast = k1 + 1;
     const unsigned sbase = smem_u32(sm);
@@ -597,10 +620,12 @@ __global__ void __launch_bounds__(NT, 2)
         const unsigned to = sbase + (unsigned)(((p - pfirst) % NS) * L::STAGE), b = bar_of(p);
         mbar_expect_tx(b, A.bytes[kind]);
         for (int q = 0; q < A.n; ++q)
-            if (A.when[q] & kind) tma_load_4d(to + A.dst[q], &A.map[q], x0, j0 + A.row0[q], p, 0, b);
+            if (A.when[q] & kind) tma_load_4d(to + A.dst[q], map(q), x0, j0 + A.row0[q], p, 0, b);
     };
     int issued = pfirst - 1; // thread 0: the last plane issued
     if (t == 0) {
+        if (fence_maps)
+            for (int q = 0; q < A.n; ++q) fence_tensormap(map(q));
         for (int q = 0; q < NS; ++q) mbar_init(smem_u32(&bar[q]), 1);
         fence_mbar_init();
         fence_proxy_async();
@@ -653,8 +678,21 @@ __global__ void __launch_bounds__(NT, 2)
     __syncthreads();
     if (t == 0)
         for (int q = 0; q < NS; ++q) mbar_inval(smem_u32(&bar[q]));
-    const BIx bx = {(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y};
     if (MODE & (P1_RMAX | P1_RSUM)) tile_store<T, NT>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+}
+
+// The stages from the first 128-byte boundary of the dynamic shared memory (tensor copies
+// land on 128-byte boundaries; launches ask for 128 bytes more).
+__device__ __forceinline__ unsigned char *align128(unsigned char *p) { return p + ((128u - (smem_u32(p) & 127u)) & 127u); }
+
+// The single-grid kernel: maps and boxes as parameters.
+template <int MODE, int TSX, int TSY>
+__global__ void __launch_bounds__(TSX *TSY, 2)
+    k_phase1_tma(const __grid_constant__ DevState<float> S, const __grid_constant__ TmaArgs A, int src, int dst, int kch) {
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    __shared__ __align__(8) unsigned long long bar[TLayout<MODE, TSX, TSY>::NS];
+    auto map = [&](int q) { return &A.map[q]; };
+    phase1_tma_body<MODE, TSX, TSY>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
@@ -673,51 +711,63 @@ inline EncodeTiledFn encode_tiled() {
     return fn;
 }
 
+// What n boxes load.
+inline void box_meta(BoxMeta &m, const TmaBox *B, int n) {
+    std::memset(&m, 0, sizeof m);
+    for (int q = 0; q < n; ++q) {
+        m.row0[q] = B[q].row0;
+        m.dst[q] = B[q].dst;
+        m.when[q] = B[q].when;
+        for (unsigned kind = DOWN; kind <= TOP; kind <<= 1)
+            if (B[q].when & kind) m.bytes[kind] += box_bytes(B[q]);
+    }
+    m.n = n;
+}
+// The tensor map of one box.
+inline bool encode_box(CUtensorMap *map, const TmaBox &b) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dim[4] = {(cuuint64_t)b.dim[0], (cuuint64_t)b.dim[1], (cuuint64_t)b.dim[2], (cuuint64_t)b.dim[3]};
+    const cuuint64_t stride[3] = {(cuuint64_t)b.stride[0], (cuuint64_t)b.stride[1], (cuuint64_t)b.stride[2]};
+    const cuuint32_t box[4] = {(cuuint32_t)b.box[0], (cuuint32_t)b.box[1], (cuuint32_t)b.box[2], (cuuint32_t)b.box[3]};
+    const cuuint32_t unit[4] = {1, 1, 1, 1};
+    return enc(map, b.elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 4, const_cast<void *>(b.base),
+               dim, stride, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 // The tensor maps of n boxes; false when there are none or the encoder refuses one.
 inline bool encode_boxes(TmaArgs &A, const TmaBox *B, int n) {
-    const EncodeTiledFn enc = encode_tiled();
-    if (n <= 0 || !enc) return false;
+    if (n <= 0 || !encode_tiled()) return false;
     std::memset(&A, 0, sizeof A);
-    for (int q = 0; q < n; ++q) {
-        const TmaBox &b = B[q];
-        const cuuint64_t dim[4] = {(cuuint64_t)b.dim[0], (cuuint64_t)b.dim[1], (cuuint64_t)b.dim[2], (cuuint64_t)b.dim[3]};
-        const cuuint64_t stride[3] = {(cuuint64_t)b.stride[0], (cuuint64_t)b.stride[1], (cuuint64_t)b.stride[2]};
-        const cuuint32_t box[4] = {(cuuint32_t)b.box[0], (cuuint32_t)b.box[1], (cuuint32_t)b.box[2], (cuuint32_t)b.box[3]};
-        const cuuint32_t unit[4] = {1, 1, 1, 1};
-        if (enc(&A.map[q], b.elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 4,
-                const_cast<void *>(b.base), dim, stride, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return false;
-        A.row0[q] = b.row0;
-        A.dst[q] = b.dst;
-        A.when[q] = b.when;
-        for (unsigned kind = DOWN; kind <= TOP; kind <<= 1)
-            if (b.when & kind) A.bytes[kind] += box_bytes(b);
-    }
-    A.n = n;
+    for (int q = 0; q < n; ++q)
+        if (!encode_box(&A.map[q], B[q])) return false;
+    box_meta(A.m, B, n);
     return true;
 }
 // The tensor maps of a launch; false when the arrays do not allow the TMA form.
-template <int MODE> inline bool tma_args(TmaArgs &A, const DevState<float> &S, int src, int fcur) {
+template <int MODE, int TSX, int TSY> inline bool tma_args(TmaArgs &A, const DevState<float> &S, int src, int fcur) {
     TmaBox B[kMaxBoxes];
-    const int n = tma_boxes<MODE>(B, S.g, bases_of<MODE>(S, src, fcur));
+    const int n = tma_boxes<MODE, TSX, TSY>(B, S.g, bases_of<MODE>(S, src, fcur));
     return encode_boxes(A, B, n);
 }
 
-template <int MODE> inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st) {
+// TSX x TSY tiles (64 x 4 or 32 x 8)
+template <int MODE, int TSX = 64, int TSY = 4>
+inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st) {
     TmaArgs A;
-    if (!tma_args<MODE>(A, S, src, fcur)) {
+    if (!tma_args<MODE, TSX, TSY>(A, S, src, fcur)) {
         launch_staged<MODE>(S, src, dst, fcur, st);
         return;
     }
-    const int kch = staged_chunk(S.g);
-    k_phase1_tma<MODE><<<staged_grid(S.g, kch), dim3(SX, SY), TLayout<MODE>::SMEM + 128, st>>>(S, A, src, dst, kch);
+    const int kch = tile_chunk<TSX, TSY>(S.g);
+    k_phase1_tma<MODE, TSX, TSY><<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX, TSY), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(
+        S, A, src, dst, kch);
 }
-template <int MODE> inline void prepare_staged_tma() {
+template <int MODE, int TSX = 64, int TSY = 4> inline void prepare_staged_tma() {
     encode_tiled(); // looked up here, outside any stream capture
-    cudaFuncSetAttribute(k_phase1_tma<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, TLayout<MODE>::SMEM + 128);
-    cudaFuncSetAttribute(k_phase1_tma<MODE>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    constexpr int smem = TLayout<MODE, TSX, TSY>::SMEM + 128;
+    cudaFuncSetAttribute(k_phase1_tma<MODE, TSX, TSY>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_phase1_tma<MODE, TSX, TSY>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 #endif
 

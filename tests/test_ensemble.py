@@ -51,10 +51,11 @@ def test_ensemble_matches_single_contexts(ark, port):
                 assert bits_equal(port.interior(n, got[n]), port.interior(n, want[q][0][n])), (q, n)
 
 
-@pytest.mark.parametrize("shape", [(2, 2, 32), (2, 0, 16), (0, 2, 64), (1, 2, 32)])
+@pytest.mark.parametrize("shape", [(2, 2, 32), (2, 0, 16), (0, 2, 64), (1, 2, 32), (4, 4, 32), (4, 2, 16), (1, 4, 64)])
 def test_ensemble_shapes_match_single_contexts(ark, port, shape):
-    """Every Phase1 shape (one cell per thread, marching, planes staged in shared memory: a
-    persistent kernel over every member's tiles) gives each member the single-context bits."""
+    """Every Phase1 shape (one cell per thread, marching, planes staged in shared memory with
+    cp.async or TMA tensor copies: a persistent kernel over every member's tiles) gives each
+    member the single-context bits."""
     mem = members(ark)
     want = singles(ark, mem, 5)
     with ark.Ensemble([p for p, _ in mem]) as E:

@@ -376,14 +376,15 @@ def test_fp32_steps_and_pieces_interleaved_in_both_phase2_forms(ark, port, monke
 @pytest.mark.parametrize("C", [(40, 20, 36), (130, 9, 70), (64, 4, 32), (7, 3, 1)])
 def test_phase1_kernel_shapes_agree(ark, port, monkeypatch, C):
     """The marching, the one-cell-per-thread, the shared-memory-staged (FP32: cp.async copies,
-    "2", or TMA tensor copies, "4") and the face-centric (FP64) Phase1 kernels
+    "2", or TMA tensor copies on 64 x 4 or 32 x 8 tiles, "4" and "5") and the face-centric (FP64)
+    Phase1 kernels
     (ARK_PHASE1_MARCH) produce the same bits in both precisions, on grids with ragged tiles and
     fewer planes than a block marches."""
     p = port.channel_params(*C, seed=21)
     st0 = port.channel_state(p)
     for prec in (ark.FP64, ark.FP32):
         outs = []
-        for m in (("00", "11", "10", "33", "30", "03") if prec == ark.FP64 else ("00", "11", "10", "22", "20", "02", "44", "42", "24")):
+        for m in (("00", "11", "10", "33", "30", "03") if prec == ark.FP64 else ("00", "11", "10", "22", "20", "02", "44", "42", "24", "55", "54", "25")):
             monkeypatch.setenv("ARK_PHASE1_MARCH", m)
             with ark.Context(params_from(ark, p, precision=prec)) as c:
                 c.upload(st0)
