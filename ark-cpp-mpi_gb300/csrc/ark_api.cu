@@ -351,12 +351,14 @@ template <class T> struct EngineT : Engine {
     }
     // One full step of main.cpp:82-91 with "Con" = level x at entry and exit, reading the
     // dt / bulk-flow partials of the current state and leaving those of the next one.  With
-    // ev given, an event is recorded after each of the kStepKernels launches.
+    // ev given, an event is recorded after each of the step_launches() launches.
     void step(int x, int fcur, cudaEvent_t *ev) override {
         const int y = x ^ 1;
         cudaStream_t st = ctx->st;
-        auto mark = [&](int q) {
-            if (ev) cudaEventRecord(ev[q], st);
+        int nmark = 0;
+        auto mark = [&]() {
+            if (ev) cudaEventRecord(ev[nmark], st);
+            ++nmark;
         };
         int mode = P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0);
         if (ctx->closure_net) {
@@ -368,22 +370,28 @@ template <class T> struct EngineT : Engine {
             cudaEventRecord(ctx->join, ctx->side);
             mode |= P1_NUT;
         }
-        // the one-kernel Phase2 forms read x ghosts; the x1 sweep kernel does not
+        // the one-kernel Phase2 forms read x and z ghosts; the sweep kernels read the ghost
+        // positions from the cells and faces they stand for (x1: xcell; x3: zcell, unless the
+        // z ghosts are a slab's halo), so with them the Phase2 ghost fill has nothing to do and
+        // the Con level's density needs no ghosts
         const int xg = ctx->p2mode != 0 ? 1 : 0;
+        const bool nofill = skip_phase2_fill();
         Launch<T>::finalize_dt(S, 1, st);
-        mark(0);
-        Launch<T>::wrap_con(S, y, xg ? 2 : 1, st);
-        mark(1);
+        mark();
+        Launch<T>::wrap_con(S, y, xg ? 2 : nofill ? 0 : 1, st);
+        mark();
         if (ctx->closure_net) cudaStreamWaitEvent(st, ctx->join, 0);
         Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st);
-        mark(2);
-        Launch<T>::wrap_phase2(S, y, fcur, st, xg);
-        mark(3);
+        mark();
+        if (!nofill) {
+            Launch<T>::wrap_phase2(S, y, fcur, st, xg);
+            mark();
+        }
         if (use_step2()) {
             // Phase2 and the second Phase1 in one kernel; the new level goes to the spare, which
             // after_step swaps in as "nCon"
             Launch<T>::phase2_phase1(S, y, fcur, S.spare, st, ctx->p2mode == 3);
-            mark(4);
+            mark();
             if (ctx->averaging) {
                 DevState<T> Sn = S;
                 Sn.lv[y] = S.spare;
@@ -393,15 +401,15 @@ template <class T> struct EngineT : Engine {
         }
         if (ctx->p2mode == 1) { // one kernel for the three sweeps: timed in the first sweep's slot
             Launch<T>::phase2_fused(S, y, fcur, st);
-            for (int ax = 0; ax < 3; ++ax) mark(4 + ax);
+            for (int ax = 0; ax < 3; ++ax) mark();
         } else {
             for (int ax = 0; ax < 3; ++ax) {
                 Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target);
-                mark(4 + ax);
+                mark();
             }
         }
         Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
-        mark(7);
+        mark();
         // AverageValues after the step (main.cpp:93-96 when enabled), outside the timed marks
         if (ctx->averaging) output_average_add<T>(S, y, ctx->avg, st);
     }
@@ -419,9 +427,12 @@ template <class T> struct EngineT : Engine {
     DevScalars *scalars() override { return S.sc; }
     uint8_t *flags() override { return S.flags; }
     bool use_step2() const { return (ctx->p2mode == 2 || ctx->p2mode == 3) && S.spare.ro; }
-    int step_launches() override { return use_step2() ? 5 : kNumStepKernels; }
+    // the three sweep kernels of a context whose z ghosts are its own: no Phase2 ghost fill
+    bool skip_phase2_fill() const { return ctx->p2mode == 0 && !S.k.ext_z; }
+    int step_launches() override { return use_step2() ? 5 : skip_phase2_fill() ? kNumStepKernels - 1 : kNumStepKernels; }
     const char *step_kernel_name(int q) override {
         if (q < 0 || q >= step_launches()) return "";
+        if (skip_phase2_fill() && q >= 3) ++q; // no wrap_phase2
         return use_step2() && q == 4 ? "phase2_phase1_forces" : kStepKernels[q];
     }
     void after_step(int con) override {

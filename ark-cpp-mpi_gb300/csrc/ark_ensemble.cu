@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(128) kb_sweep_x(const DS *__restrict__ inst, W
 }
 
 template <int AX>
-__global__ void __launch_bounds__(128) kb_sweep_col(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
+__global__ void __launch_bounds__(128, 5) kb_sweep_col(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
         sweep_col_body<float, AX>(inst[q], con, fcur, W.extra[q], decode(W, q, b));
@@ -207,7 +207,7 @@ struct ark_ensemble {
     int4 *d_info[WL_COUNT] = {};
     int *d_extra[WL_COUNT] = {};
     int total[WL_COUNT] = {};
-    WrapJob *d_jobs = nullptr; // [6][n]: wrap_con for level 0/1, wrap_phase2 for (con, fcur)
+    WrapJob *d_jobs = nullptr; // [2][n]: wrap_con for level 0/1
     int persist = 1;           // persistent blocks per launch (all SMs x resident blocks)
     int persist_staged = 1;    // the same for the staged Phase1 (2 blocks of 256 threads per SM)
     Shape shape = {4, 4, 32}; // staged Phase1 with TMA copies for both launches
@@ -374,11 +374,12 @@ int build_lists(ark_ensemble *E) {
     return ARK_OK;
 }
 
-// Ghost-fill jobs of every member for both level roles and face generations (the same
-// arrays and modes as Launch<float>::wrap_con(with_ro = 1) / wrap_phase2(xlines = 0): the
-// ensemble's Phase2 is the three sweep kernels, whose x1 sweep reads no x ghosts).
+// Ghost-fill jobs of every member for both level roles (the same arrays and modes as
+// Launch<float>::wrap_con(with_ro = 0): the ensemble's Phase2 is the three sweep kernels, which
+// read their x and z ghost positions from the cells and faces they stand for, so only the
+// stress reads ghosts and the Phase2 ghost fill has nothing to do).
 int build_jobs(ark_ensemble *E) {
-    std::vector<WrapJob> jobs(6 * (size_t)E->n);
+    std::vector<WrapJob> jobs(2 * (size_t)E->n);
     for (int q = 0; q < E->n; ++q) {
         const DS &S = E->S[q];
         const bool px = S.k.periodic_x, pz = S.k.periodic_z;
@@ -389,23 +390,8 @@ int build_jobs(ark_ensemble *E) {
             wrap_add(J, L.u1, 0, cx, cz);
             wrap_add(J, L.u2, 0, cx, cz);
             wrap_add(J, L.u3, 0, cx, cz);
-            wrap_add(J, L.ro, 0, GH_NONE, cz);
             jobs[(size_t)lv * E->n + q] = J;
         }
-        for (int con = 0; con < 2; ++con)
-            for (int fc = 0; fc < 2; ++fc) {
-                WrapJob J = {};
-                const Level<float> Ln = S.lv[con ^ 1], Lc = S.lv[con];
-                wrap_add(J, Ln.u1, 0, GH_NONE, cz);
-                wrap_add(J, Ln.u2, 0, GH_NONE, cz);
-                wrap_add(J, Ln.u3, 0, GH_NONE, cz);
-                wrap_add(J, Ln.ro, 0, GH_NONE, cz);
-                wrap_add(J, Lc.ro, 0, GH_NONE, cz);
-                const FaceSet<float> &Z = S.fc[fc][2];
-                float *fz[4] = {Z.p, Z.u[0], Z.u[1], Z.u[2]};
-                for (int a = 0; a < 4; ++a) wrap_add(J, fz[a], 1, GH_NONE, cz);
-                jobs[(size_t)(2 + 2 * con + fc) * E->n + q] = J;
-            }
     }
     if (!E->d_jobs)
         if (int rc = ens_alloc(E, &E->d_jobs, jobs.size())) return rc;
@@ -458,6 +444,11 @@ int prepare_staged_kernels(int sms) {
 }
 
 // One step of every member (the order of main.cpp:82-91, as the single-context fused step).
+// The launches of an ensemble step, in order (ark_ensemble_kernel_times reports them so).
+const char *const kEnsKernels[] = {"finalize_dt", "wrap_con", "phase1_stress_forces", "sweep_x1",
+                                   "sweep_x2",    "sweep_x3", "phase1_forces"};
+constexpr int kEnsPhases = 7;
+
 void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     const int y = x ^ 1;
     auto mark = [&](int q) {
@@ -473,17 +464,14 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     else
         launch_p1<P1_STRESS | P1_FORCES | P1_RMAX>(E, E->shape.march_a, y, x, fc);
     mark(2);
-    kb_wrap<<<grid_of(E, WL_WRAP), 128, 0, E->st>>>(E->d_inst, E->d_jobs + (size_t)(2 + 2 * y + fc) * E->n,
-                                                     wl(E, WL_WRAP));
-    mark(3);
     kb_sweep_x<<<grid_of(E, WL_SWEEPX), 128, 0, E->st>>>(E->d_inst, wl(E, WL_SWEEPX), y, fc);
-    mark(4);
+    mark(3);
     kb_sweep_col<1><<<grid_of(E, WL_COL1), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL1), y, fc);
-    mark(5);
+    mark(4);
     kb_sweep_col<2><<<grid_of(E, WL_COL2), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL2), y, fc);
-    mark(6);
+    mark(5);
     launch_p1<P1_FORCES | P1_RSUM>(E, E->shape.march_b, x, y, fc ^ 1);
-    mark(7);
+    mark(6);
 }
 
 void drop_graphs(ark_ensemble *E) {
@@ -767,8 +755,12 @@ int ark_ensemble_time_steps(ark_ensemble *E, int nsteps, double *ms) {
 
 // The launches of a step in the order ark_kernel_name lists them (the same eight phases as
 // the single-context step), each timed with events around it, averaged over nsteps.
+const char *ark_ensemble_kernel_name(int index) {
+    return index >= 0 && index < kEnsPhases ? kEnsKernels[index] : nullptr;
+}
+
 int ark_ensemble_kernel_times(ark_ensemble *E, int nsteps, double *ms, int cap, int *count) {
-    constexpr int kPhases = 8;
+    constexpr int kPhases = kEnsPhases;
     if (!E || !ms || !count || nsteps < 1) return efail(ARK_ERR_PARAM, "bad arguments");
     for (char u : E->uploaded)
         if (!u) return efail(ARK_ERR_STATE, "every member needs a state before stepping");

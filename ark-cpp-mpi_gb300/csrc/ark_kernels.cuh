@@ -1664,6 +1664,13 @@ __device__ __forceinline__ int xcell(int s, int C1, bool periodic) {
 __device__ __forceinline__ int xface(int s, int C1, bool periodic) {
     return !periodic ? s : s == 0 ? C1 : s == C1 + 2 ? 2 : s;
 }
+// The x3 sweep does the same along z (unless the z ghosts are a slab's halo): cell 0 is cell C3
+// (periodic) or 1 (bounded), cell C3+1 cell 1 or C3; face 0 is face C3 or 1, face C3+2 face 2 or
+// C3+1 (the ghost fill copies the adjacent face on a bounded z).
+__device__ __forceinline__ int zcell(int s, int C3, bool periodic) { return xcell(s, C3, periodic); }
+__device__ __forceinline__ int zface(int s, int C3, bool periodic) {
+    return s == 0 ? (periodic ? C3 : 1) : s == C3 + 2 ? (periodic ? 2 : C3 + 1) : s;
+}
 
 // x1 sweep: one warp per (j,k) line, lanes on consecutive cells (coalesced), marching along
 // i in chunks of 32 with the next chunk's loads issued before the current chunk is
@@ -1843,22 +1850,31 @@ __device__ __forceinline__ void sweep_col_body(const DevState<T> &S, int con, in
     const NCell<T> N = {R.nN, R.nA, R.nB, R.nR, R.nc};
     const SweepK<T> q = sweep_consts(S, AX);
     const int cst = AX == 1 ? (int)g.cs1 : (int)g.cs2, fst = AX == 1 ? (int)g.fs1 : (int)g.fs2;
+    // z: the ghost positions read from the cells and faces they stand for (zcell, zface), the
+    // flags from the ghost cells themselves: c0 / f0 shift cell 0 / face 0, c1 / f1 cell nd =
+    // C3+1 / face nd+1 (zero along y, or when the z ghosts are a slab's halo)
+    const bool fold = AX == 2 && !S.k.ext_z, pz = S.k.periodic_z;
+    const int c0 = fold ? zcell(0, g.C3, pz) * cst : 0, f0 = fold ? zface(0, g.C3, pz) * fst : 0;
+    const int c1 = fold ? (zcell(nd, g.C3, pz) - nd) * cst : 0, f1 = fold ? (zface(nd + 1, g.C3, pz) - nd - 1) * fst : 0;
     int c = (AX == 1 ? g.ci(i, 0, o) : g.ci(i, o, 0)) + s0 * cst;
     int fb = (AX == 1 ? g.fi(i, 0, o) : g.fi(i, o, 0)) + s0 * fst;
-    T uA_b = R.FA[ARK_CK(fb, R.nf)], uB_b = R.FB[ARK_CK(fb, R.nf)];
-    RQ<T> rqb = face_rq(R.FN[ARK_CK(fb, R.nf)], R.FP[ARK_CK(fb, R.nf)], q); // then the forward face's, carried
+    const int fb0 = fb + (s0 == 0 ? f0 : 0);
+    T uA_b = R.FA[ARK_CK(fb0, R.nf)], uB_b = R.FB[ARK_CK(fb0, R.nf)];
+    RQ<T> rqb = face_rq(R.FN[ARK_CK(fb0, R.nf)], R.FP[ARK_CK(fb0, R.nf)], q); // then the forward face's, carried
     SweepIn<T> cur, nxt = {};
-    sweep_load(R, c, fb + fst, cur);
+    sweep_load(R, c + (s0 == 0 ? c0 : 0), fb + fst, cur, c); // (s0 < nd: its forward face is inside)
     Ext<T> prev = {};
     T uprev = 0;
     uint8_t flprev = 0;
     for (int s = s0; s <= s1; ++s, c += cst, fb += fst) {
-        if (s < s1) sweep_load(R, c + cst, fb + 2 * fst, nxt);
+        const bool last = s + 1 == nd; // the next position is the ghost C3+1, its forward face C3+2
+        if (s < s1) sweep_load(R, c + cst + (last ? c1 : 0), fb + 2 * fst + (last ? f1 : 0), nxt, c + cst);
         const RQ<T> rqf = face_rq(cur.uN_f, cur.p_f, q);
         const Ext<T> e = extrapolate_rq<T, AX == 2>(rqf, rqb, cur.nN, cur.cN, cur.uA_f, uA_b, cur.nA, cur.cA, cur.uB_f,
                                                     uB_b, cur.nB, cur.cB, cur.nR, cur.cR, q);
         if (s > s0)
-            face_update<T, AX == 1>(N, W, c - cst, c, fb, flprev, cur.fl, uprev, cur.nN, prev, e, uA_b, uB_b, q);
+            face_update<T, AX == 1>(N, W, c - cst + (s == 1 ? c0 : 0), c + (s == nd ? c1 : 0), fb, flprev, cur.fl, uprev,
+                                    cur.nN, prev, e, uA_b, uB_b, q);
         prev = e;
         uprev = cur.nN;
         flprev = cur.fl;

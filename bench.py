@@ -348,7 +348,7 @@ def ensemble_leg(arkgpu, members, steps, warmup, device, seed=4242):
     counts = {f"{a}x{b}x{c}": sum(1 for C, _ in states if C == (a, b, c)) for a, b, c in ENSEMBLE_GRIDS}
     return {"value": round(cells * steps / (ms * 1e-3) / 1e6, 3), "unit": UNIT, "members": members,
             "cells": cells, "grids": counts, "steps": steps, "ms_per_step": round(ms / steps, 4),
-            "dtype": "f32 (f64 reductions)", "launches_per_step": 8, "autotuned_shape": shape,
+            "dtype": "f32 (f64 reductions)", "launches_per_step": len(ktimes), "autotuned_shape": shape,
             "autotune_s": round(tune_s, 3), "finite": finite,
             "kernels_ms": {k: round(v, 4) for k, v in ktimes}, "ktimes": ktimes,
             "step_roofline": {"bytes_per_cell": STEP_VALUES * 4,

@@ -357,8 +357,10 @@ int ark_ensemble_download(ark_ensemble *ens, int member, ark_host_state *host);
 int ark_ensemble_step(ark_ensemble *ens, int nsteps);
 int ark_ensemble_sync(ark_ensemble *ens);
 int ark_ensemble_time_steps(ark_ensemble *ens, int nsteps, double *ms);
-/* Per-launch times of a step (ms, averaged over nsteps; names from ark_kernel_name). */
+/* Per-launch times of a step (ms, averaged over nsteps; names from ark_ensemble_kernel_name). */
 int ark_ensemble_kernel_times(ark_ensemble *ens, int nsteps, double *ms, int cap, int *count);
+/* The name of launch `index` of an ensemble step (NULL past the last). */
+const char *ark_ensemble_kernel_name(int index);
 int ark_ensemble_get_scalars(ark_ensemble *ens, int member, ark_scalars *out);
 int ark_ensemble_mean_profile(ark_ensemble *ens, int member, double *mean_u1, double *wall_shear);
 /* Times each candidate kernel shape (for each Phase1: 0 one cell per thread, 1 marching, 2 planes

@@ -81,7 +81,8 @@ def test_ensemble_autotune_keeps_results(ark, port):
         choice = E.autotune(1)
         assert choice["segment"] in (16, 32, 64)
         kt = E.kernel_times(2)
-        assert [n for n, _ in kt][2] == "phase1_stress_forces" and len(kt) == 8
+        assert [n for n, _ in kt] == ["finalize_dt", "wrap_con", "phase1_stress_forces", "sweep_x1", "sweep_x2", "sweep_x3",
+                                      "phase1_forces"]
         assert all(ms > 0 for _, ms in kt)
         done = E.scalars(0).nstep
         E.sync()
