@@ -316,10 +316,11 @@ def fp32_error_report():
 ENSEMBLE_GRIDS = ((32, 32, 32), (64, 32, 32), (64, 48, 48), (96, 64, 64), (128, 64, 64))
 
 
-def ensemble_leg(arkgpu, members, steps, warmup, device, seed=4242):
+def ensemble_leg(arkgpu, members, steps, warmup, device, seed=4242, shape=None):
     """A batched ensemble of independent FP32 channels: grids drawn from ENSEMBLE_GRIDS, Re_b
     uniform in [2000, 6000], perturbation amplitude uniform in [0.05, 0.15], bulk forcing;
-    one persistent launch per phase under a CUDA graph, kernel shapes autotuned first."""
+    one persistent launch per phase under a CUDA graph, kernel shapes autotuned first (or set
+    to `shape`: Phase1 + stress shape, second Phase1 shape, segment)."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
@@ -335,7 +336,11 @@ def ensemble_leg(arkgpu, members, steps, warmup, device, seed=4242):
         for q, (p, (C, amp)) in enumerate(zip(params, states)):
             E.upload(q, arkgpu.channel_init(p, seed=seed + q, amp=amp))
         t0 = time.perf_counter()
-        shape = E.autotune(3)
+        if shape:
+            E.set_shape(*shape)
+            shape = {"march_phase1_stress": shape[0], "march_phase1": shape[1], "segment": shape[2], "us_per_step": None}
+        else:
+            shape = E.autotune(3)
         tune_s = time.perf_counter() - t0
         E.step(warmup)
         E.sync()
@@ -435,6 +440,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--ensemble", type=int, default=64, help="ensemble members (0: no ensemble leg)")
     ap.add_argument("--ensemble-steps", type=int, default=500)
+    ap.add_argument("--ensemble-shape", type=int, nargs=3, default=None,
+                    help="fixed ensemble kernel shape (Phase1 + stress, second Phase1, segment) instead of autotuning")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -492,12 +499,12 @@ def main():
                                           "frac": round(f["cells"] * STEP_VALUES * 4 / f_step_s / 1e9 / peak, 4)},
                         "kernels_ms": {k: round(v, 4) for k, v in f["ktimes"]}, "clocks": f["clocks"],
                         "kernel_shapes": f["shapes"], "error": fp32_error_report()}
-        line["gpu_launches"] += launches_per_step * f_steps
+        line["gpu_launches"] += len(f["ktimes"]) * f_steps
 
     if rank == 0 and args.ensemble > 0:
-        e = ensemble_leg(arkgpu, args.ensemble, args.ensemble_steps, args.warmup, device)
+        e = ensemble_leg(arkgpu, args.ensemble, args.ensemble_steps, args.warmup, device, shape=args.ensemble_shape)
         e["step_roofline"].update(peak=peak, frac=round(e["step_roofline"]["achieved"] / peak, 4))
-        e["roofline"] = roofline(e.pop("ktimes"), e["cells"], 4, peak, peak_kind, traffic, "fp32")
+        e["roofline"] = roofline(e.pop("ktimes"), e["cells"], 4, peak, peak_kind, traffic, "ensemble")
         line["ensemble"] = e
         line["gpu_launches"] += e["launches_per_step"] * args.ensemble_steps
 
