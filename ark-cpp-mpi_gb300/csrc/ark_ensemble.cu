@@ -140,27 +140,41 @@ struct MemberMaps {
     CUtensorMap ff;
 };
 
-// The staged Phase1 with TMA copies: work item = a member's 64 x 4 tile and chunk of planes,
-// the single-context TMA kernel's body with the member's maps (fenced for the copy engine
-// once per work item).
+// The staged Phase1 with TMA copies: work item = a member's tile (64 x 4, or 32 x 8 when the
+// work list marks the member narrow: extra = planes per chunk | narrow << 16) and chunk of
+// planes, the single-context TMA kernel's body with the member's maps for that tile shape
+// (maps[2 q + narrow], fenced for the copy engine once per work item); meta[narrow] the boxes.
+template <int MODE> struct TmaMetas {
+    stg::BoxMeta m[2];
+};
+template <int MODE> constexpr int tma_ens_smem() {
+    return (stg::TLayout<MODE, 64, 4>::SMEM > stg::TLayout<MODE, 32, 8>::SMEM ? stg::TLayout<MODE, 64, 4>::SMEM
+                                                                               : stg::TLayout<MODE, 32, 8>::SMEM) +
+           128;
+}
 template <int MODE>
 __global__ void __launch_bounds__(stg::NT, 2) kb_phase1_tma(const DS *__restrict__ inst, const MemberMaps *__restrict__ maps,
-                                                            const __grid_constant__ stg::BoxMeta meta, WorkList W, int src,
+                                                            const __grid_constant__ TmaMetas<MODE> meta, WorkList W, int src,
                                                             int dst, int fcur) {
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
+    static_assert(stg::TLayout<MODE, 64, 4>::NS == stg::TLayout<MODE, 32, 8>::NS, "one ring depth for both tiles");
     extern __shared__ __align__(128) unsigned char sm_raw[];
     __shared__ __align__(8) unsigned long long bar[stg::TLayout<MODE>::NS];
     unsigned char *const sm = stg::align128(sm_raw);
     for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
         const int q = find_member(W, b);
-        const MemberMaps *M = maps + q;
+        const int extra = W.extra[q], narrow = extra >> 16, kch = extra & 0xFFFF;
+        const MemberMaps *M = maps + 2 * q + narrow;
         auto map = [&](int k) -> const CUtensorMap * {
             if (k == 0) return &M->lv[STRESS ? 0 : 1][src];
             if (k == 1) return &M->fl[STRESS ? 0 : 1];
             if (k <= 4) return &M->fc[fcur][k - 2];
             return &M->ff;
         };
-        stg::phase1_tma_body<MODE, stg::SX, stg::SY>(inst[q], map, meta, true, src, dst, W.extra[q], decode(W, q, b), sm, bar);
+        if (narrow)
+            stg::phase1_tma_body<MODE, 32, 8>(inst[q], map, meta.m[1], true, src, dst, kch, decode(W, q, b), sm, bar);
+        else
+            stg::phase1_tma_body<MODE, 64, 4>(inst[q], map, meta.m[0], true, src, dst, kch, decode(W, q, b), sm, bar);
         __syncthreads();
     }
 }
@@ -181,13 +195,20 @@ __global__ void __launch_bounds__(128, 5) kb_sweep_col(const DS *__restrict__ in
 }
 
 // Kinds of work list.
-enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, WL_COUNT };
+// WL_STAGED: 64 x 4 tiles of the staged Phase1 for every member; WL_STAGED_T: 32 x 8 tiles for
+// the members whose width is an odd multiple of 32 (a 64-wide tile would be half empty at
+// their end), 64 x 4 for the others.
+enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, WL_STAGED_T, WL_COUNT };
+
+// the staged Phase1 of a member of width C1 in 32 x 8 tiles (WL_STAGED_T)
+inline bool narrow_tiles(int C1) { return ((C1 + 31) / 32) % 2 == 1; }
 
 // The candidate kernel shapes the autotuner chooses between.
 struct Shape {
     int march_a, march_b; // Phase1 with stress / second Phase1: 0 one cell per thread, 1 marching,
                           // 2 planes staged in shared memory (cp.async copies), 4 the same with
-                          // TMA tensor copies
+                          // TMA tensor copies, 5 TMA with 32 x 8 tiles for the members whose
+                          // width is an odd multiple of 32
     int seg;              // target faces per thread segment in the x2/x3 sweeps
 };
 
@@ -210,9 +231,9 @@ struct ark_ensemble {
     WrapJob *d_jobs = nullptr; // [2][n]: wrap_con for level 0/1
     int persist = 1;           // persistent blocks per launch (all SMs x resident blocks)
     int persist_staged = 1;    // the same for the staged Phase1 (2 blocks of 256 threads per SM)
-    Shape shape = {4, 4, 32}; // staged Phase1 with TMA copies for both launches
-    MemberMaps *d_maps = nullptr;   // the members' tensor maps (null: the TMA form falls back)
-    stg::BoxMeta meta[2] = {};      // its boxes with the stress and without
+    Shape shape = {5, 5, 32}; // staged Phase1 with TMA copies for both launches, 32 x 8 tiles on odd-32 widths
+    MemberMaps *d_maps = nullptr;   // the members' tensor maps, [2 q + narrow] (null: the TMA form falls back)
+    stg::BoxMeta meta[2][2] = {};   // its boxes: [narrow][0 with the stress, 1 without]
     int con = 0, fcur = 0;
     bool parts_valid = false;
     bool uploaded_all = false;
@@ -273,28 +294,31 @@ int alloc_member(ark_ensemble *E, DS &S) {
 // cp.async form runs, when a member's arrays do not allow it or the encoder is missing).
 int build_maps(ark_ensemble *E) {
     constexpr int MS = P1_STRESS | P1_FORCES | P1_RMAX, MF = P1_FORCES | P1_RSUM;
-    std::vector<MemberMaps> h(E->n);
+    std::vector<MemberMaps> h(2 * (size_t)E->n);
     std::memset(h.data(), 0, sizeof(MemberMaps) * h.size());
     for (int q = 0; q < E->n; ++q) {
         const DS &S = E->S[q];
-        for (int l = 0; l < 2; ++l)
-            for (int gen = 0; gen < 2; ++gen) {
-                stg::TmaBox B[stg::kMaxBoxes], F[stg::kMaxBoxes];
-                const int ns = stg::tma_boxes<MS>(B, S.g, stg::bases_of<MS>(S, l, gen));
-                const int nf = stg::tma_boxes<MF>(F, S.g, stg::bases_of<MF>(S, l, gen));
-                if (ns != 5 || nf != 6) return ARK_OK;
-                bool ok = stg::encode_box(&h[q].lv[0][l], B[0]) && stg::encode_box(&h[q].lv[1][l], F[0]) &&
-                          stg::encode_box(&h[q].fl[0], B[1]) && stg::encode_box(&h[q].fl[1], F[1]) &&
-                          stg::encode_box(&h[q].ff, F[5]);
-                for (int d = 0; d < 3; ++d) ok = ok && stg::encode_box(&h[q].fc[gen][d], B[2 + d]);
-                if (!ok) return ARK_OK;
-                if (q == 0 && l == 0 && gen == 0) {
-                    stg::box_meta(E->meta[0], B, ns);
-                    stg::box_meta(E->meta[1], F, nf);
+        for (int narrow = 0; narrow < 2; ++narrow)
+            for (int l = 0; l < 2; ++l)
+                for (int gen = 0; gen < 2; ++gen) {
+                    stg::TmaBox B[stg::kMaxBoxes], F[stg::kMaxBoxes];
+                    const stg::Bases bs = stg::bases_of<MS>(S, l, gen), bf = stg::bases_of<MF>(S, l, gen);
+                    const int ns = narrow ? stg::tma_boxes<MS, 32, 8>(B, S.g, bs) : stg::tma_boxes<MS, 64, 4>(B, S.g, bs);
+                    const int nf = narrow ? stg::tma_boxes<MF, 32, 8>(F, S.g, bf) : stg::tma_boxes<MF, 64, 4>(F, S.g, bf);
+                    if (ns != 5 || nf != 6) return ARK_OK;
+                    MemberMaps &m = h[2 * q + narrow];
+                    bool ok = stg::encode_box(&m.lv[0][l], B[0]) && stg::encode_box(&m.lv[1][l], F[0]) &&
+                              stg::encode_box(&m.fl[0], B[1]) && stg::encode_box(&m.fl[1], F[1]) &&
+                              stg::encode_box(&m.ff, F[5]);
+                    for (int d = 0; d < 3; ++d) ok = ok && stg::encode_box(&m.fc[gen][d], B[2 + d]);
+                    if (!ok) return ARK_OK;
+                    if (q == 0 && l == 0 && gen == 0) {
+                        stg::box_meta(E->meta[narrow][0], B, ns);
+                        stg::box_meta(E->meta[narrow][1], F, nf);
+                    }
                 }
-            }
     }
-    if (int rc = ens_alloc(E, &E->d_maps, h.size())) return rc;
+    if (int rc = ens_alloc(E, &E->d_maps, h.size())) return rc;  // [2 q + narrow]
     ENS_CUDA(cudaMemcpy(E->d_maps, h.data(), sizeof(MemberMaps) * h.size(), cudaMemcpyHostToDevice));
     return ARK_OK;
 }
@@ -351,11 +375,13 @@ int build_lists(ark_ensemble *E) {
                 gx = (int)((tot + 127) / 128);
                 break;
             }
-            case WL_STAGED: { // 64 x 4 tiles and chunks of planes of the staged Phase1
+            case WL_STAGED: // tiles and chunks of planes of the staged Phase1
+            case WL_STAGED_T: {
                 const int nch = (g.C3 + kens - 1) / kens;     // chunks of the column, of
                 const int kch = (g.C3 + nch - 1) / nch;       // balanced lengths
-                extra[q] = kch;
-                const dim3 gr = stg::staged_grid(g, kch);
+                const bool narrow = kind == WL_STAGED_T && narrow_tiles(g.C1);
+                extra[q] = kch | (narrow ? 1 << 16 : 0);
+                const dim3 gr = narrow ? stg::tile_grid<32, 8>(g, kch) : stg::staged_grid(g, kch);
                 gx = (int)gr.x, gy = (int)gr.y, gz = (int)gr.z;
                 break;
             }
@@ -408,11 +434,14 @@ int grid_of(const ark_ensemble *E, int kind) { return std::max(1, std::min(E->to
 
 template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst, int fcur) {
     const dim3 blk(kTileX, kTileY);
-    if (march == 4 && E->d_maps) {
-        const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
-        kb_phase1_tma<MODE><<<grid, dim3(stg::SX, stg::SY), stg::TLayout<MODE>::SMEM + 128, E->st>>>(
-            E->d_inst, E->d_maps, E->meta[(MODE & P1_STRESS) ? 0 : 1], wl(E, WL_STAGED), src, dst, fcur);
-    } else if (march == 2 || march == 4) {
+    if ((march == 4 || march == 5) && E->d_maps) {
+        const int kind = march == 5 ? WL_STAGED_T : WL_STAGED;
+        const int grid = std::max(1, std::min(E->total[kind], E->persist_staged));
+        const int m = (MODE & P1_STRESS) ? 0 : 1;
+        const TmaMetas<MODE> metas = {{E->meta[0][m], E->meta[1][m]}};
+        kb_phase1_tma<MODE><<<grid, dim3(stg::SX, stg::SY), tma_ens_smem<MODE>(), E->st>>>(E->d_inst, E->d_maps, metas,
+                                                                                           wl(E, kind), src, dst, fcur);
+    } else if (march == 2 || march == 4 || march == 5) {
         const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
         kb_phase1_staged<MODE><<<grid, dim3(stg::SX, stg::SY), stg::Layout<MODE>::SMEM, E->st>>>(
             E->d_inst, wl(E, WL_STAGED), src, dst, fcur);
@@ -436,10 +465,10 @@ int prepare_staged_kernels(int sms) {
     per = std::min(per, one(kb_phase1_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
                             stg::Layout<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>::SMEM));
     per = std::min(per, one(kb_phase1_staged<P1_FORCES | P1_RSUM>, stg::Layout<P1_FORCES | P1_RSUM>::SMEM));
-    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_RMAX>, stg::TLayout<P1_STRESS | P1_FORCES | P1_RMAX>::SMEM + 128));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_RMAX>, tma_ens_smem<P1_STRESS | P1_FORCES | P1_RMAX>()));
     per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
-                            stg::TLayout<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>::SMEM + 128));
-    per = std::min(per, one(kb_phase1_tma<P1_FORCES | P1_RSUM>, stg::TLayout<P1_FORCES | P1_RSUM>::SMEM + 128));
+                            tma_ens_smem<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>()));
+    per = std::min(per, one(kb_phase1_tma<P1_FORCES | P1_RSUM>, tma_ens_smem<P1_FORCES | P1_RSUM>()));
     return sms * std::max(per, 1);
 }
 
@@ -835,7 +864,8 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
         if (!u) return efail(ARK_ERR_STATE, "every member needs a state before tuning");
     const Shape cands[] = {{1, 0, 32}, {0, 0, 32}, {1, 1, 32}, {0, 1, 32}, {1, 0, 16}, {1, 0, 64}, {0, 0, 16},
                            {0, 0, 64}, {2, 2, 32}, {2, 0, 32}, {0, 2, 32}, {2, 2, 64}, {2, 0, 64}, {4, 4, 32},
-                           {4, 4, 64}, {4, 4, 16}, {4, 2, 32}, {2, 4, 32}, {4, 0, 32}};
+                           {4, 4, 64}, {4, 4, 16}, {4, 2, 32}, {2, 4, 32}, {4, 0, 32}, {5, 5, 32}, {5, 4, 32},
+                           {4, 5, 32}, {5, 5, 64}};
     Shape best = E->shape;
     double best_ms = 1e300;
     if (int rc = ensure_parts(E)) return rc;
@@ -867,8 +897,8 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
 int ark_ensemble_set_shape(ark_ensemble *E, int march_a, int march_b, int segment) {
     if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
     if (segment < 1) return efail(ARK_ERR_PARAM, "segment < 1");
-    auto ok = [](int m) { return (m >= 0 && m <= 2) || m == 4; };
-    if (!ok(march_a) || !ok(march_b)) return efail(ARK_ERR_PARAM, "march must be 0, 1, 2 or 4");
+    auto ok = [](int m) { return (m >= 0 && m <= 2) || m == 4 || m == 5; };
+    if (!ok(march_a) || !ok(march_b)) return efail(ARK_ERR_PARAM, "march must be 0, 1, 2, 4 or 5");
     E->shape = Shape{march_a, march_b, segment};
     drop_graphs(E);
     return build_lists(E);

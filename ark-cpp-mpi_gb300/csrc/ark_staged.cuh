@@ -606,7 +606,9 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
     constexpr int NS = L::NS, SX = TSX, SY = TSY, NT = TSX * TSY;
     constexpr unsigned long long kLimitNs = 500000000ull;
     const Geom g = S.g;
-    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * SX + tx;
+    // the thread's tile column from its linear index (the ensemble launches 64 x 4 blocks for
+    // both tile shapes)
+    const int t = threadIdx.y * blockDim.x + threadIdx.x, tx = t % SX, ty = t / SX;
     const int i = bx.x * SX + tx + 1, j = bx.y * SY + ty + 1;
     const int x0 = bx.x * SX, j0 = bx.y * SY + 1;
     const int k0 = bx.z * kch + 1;

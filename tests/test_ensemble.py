@@ -16,7 +16,7 @@ def bits_equal(a, b):
 
 def members(ark):
     spec = [((32, 16, 16), 2000.0, 0.05, 1, 1), ((40, 24, 20), 3500.0, 0.10, 1, 1),
-            ((24, 12, 30), 6000.0, 0.15, 0, 1), ((17, 9, 11), 2800.0, 0.08, 1, 0)]
+            ((24, 12, 30), 6000.0, 0.15, 0, 1), ((17, 9, 11), 2800.0, 0.08, 1, 0), ((70, 6, 5), 4000.0, 0.1, 0, 0)]
     out = []
     for q, (C, re, amp, px, pz) in enumerate(spec):
         p = ark.make_params(*C, re_b=re, precision=ark.FP32)
@@ -51,11 +51,13 @@ def test_ensemble_matches_single_contexts(ark, port):
                 assert bits_equal(port.interior(n, got[n]), port.interior(n, want[q][0][n])), (q, n)
 
 
-@pytest.mark.parametrize("shape", [(2, 2, 32), (2, 0, 16), (0, 2, 64), (1, 2, 32), (4, 4, 32), (4, 2, 16), (1, 4, 64)])
+@pytest.mark.parametrize("shape", [(2, 2, 32), (2, 0, 16), (0, 2, 64), (1, 2, 32), (4, 4, 32), (4, 2, 16), (1, 4, 64),
+                                   (5, 5, 32), (5, 4, 16)])
 def test_ensemble_shapes_match_single_contexts(ark, port, shape):
     """Every Phase1 shape (one cell per thread, marching, planes staged in shared memory with
-    cp.async or TMA tensor copies: a persistent kernel over every member's tiles) gives each
-    member the single-context bits."""
+    cp.async or TMA tensor copies, 64 x 4 tiles or 32 x 8 for the members whose width is an odd
+    multiple of 32: a persistent kernel over every member's tiles) gives each member the
+    single-context bits."""
     mem = members(ark)
     want = singles(ark, mem, 5)
     with ark.Ensemble([p for p, _ in mem]) as E:
