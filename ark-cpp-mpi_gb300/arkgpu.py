@@ -31,7 +31,7 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_boundary_fill", "ark_boundary_conditions", "ark_set_dt", "ark_step", "ark_sync", "ark_time_steps",
            "ark_get_scalars", "ark_set_scalars", "ark_conservation_sums", "ark_channel_init",
            "ark_kernel_times", "ark_kernel_name", "ark_step_kernel_name", "ark_alloc_host_state", "ark_free_host_state",
-           "ark_conservation_sums_noalloc", "ark_mean_profile", "ark_selftest_division",
+           "ark_conservation_sums_noalloc", "ark_mean_profile", "ark_selftest_division", "ark_selftest_staging_timeout",
            "ark_ensemble_create", "ark_ensemble_destroy", "ark_ensemble_last_error", "ark_ensemble_size",
            "ark_ensemble_upload", "ark_ensemble_download", "ark_ensemble_step", "ark_ensemble_sync",
            "ark_ensemble_time_steps", "ark_ensemble_get_scalars", "ark_ensemble_mean_profile",
@@ -116,7 +116,7 @@ def lib():
         L.ark_get_array.argtypes = [vp, ctypes.c_char_p, _DP]
         L.ark_put_array.argtypes = [vp, ctypes.c_char_p, _DP]
         for fn in ("ark_time_step_size", "ark_phase1", "ark_stress_tensor", "ark_use_forces", "ark_phase2",
-                   "ark_sync"):
+                   "ark_sync", "ark_selftest_staging_timeout"):
             getattr(L, fn).argtypes = [vp]
         L.ark_boundary_fill.argtypes = [vp, ctypes.c_int]
         L.ark_boundary_conditions.argtypes = [vp] + [ctypes.c_int] * 4

@@ -413,6 +413,7 @@ template <class T> struct EngineT : Engine {
         // AverageValues after the step (main.cpp:93-96 when enabled), outside the timed marks
         if (ctx->averaging) output_average_add<T>(S, y, ctx->avg, st);
     }
+    int staging_unmet(int x, int fcur) override { return Launch<T>::staging_unmet(S, x ^ 1, x, fcur, ctx->st); }
     void boundary_fill(int ncon, int axis, int periodic) override {
         Launch<T>::boundary_fill(S, ncon, axis, periodic, ctx->st);
     }
@@ -1034,6 +1035,14 @@ int ark_conservation_sums(ark_ctx *ctx, ark_sums *out) {
     out->momentum3 = (double)v[3] * q;
     out->kinetic = (double)v[4] * q;
     out->cells = v[5];
+    return ARK_OK;
+}
+
+int ark_selftest_staging_timeout(ark_ctx *ctx) {
+    if (int rc = check_ctx(ctx, true)) return rc;
+    if (ctx->P.precision != ARK_FP32) return fail(ARK_ERR_UNSUPPORTED, "the TMA staging runs in FP32 contexts");
+    if (!ctx->eng->staging_unmet(ctx->con, ctx->fcur)) return fail(ARK_ERR_UNSUPPORTED, "no TMA staging for this grid");
+    ARK_CUDA(cudaGetLastError());
     return ARK_OK;
 }
 

@@ -61,6 +61,8 @@ struct Engine {
     // Returns the count.
     virtual int halo_arrays(int exchange, int x, int fcur, void **ptrs, int *face) = 0;
     virtual void halo_exchange(const HaloJob *jobs, int njobs) = 0;
+    // the TMA staging's bounded-wait check (Launch<T>::staging_unmet): 1 launched, 0 unavailable
+    virtual int staging_unmet(int x, int fcur) = 0;
 };
 
 

@@ -2314,6 +2314,12 @@ template <class T> void Launch<T>::prepare() {
     }
 }
 
+template <class T> int Launch<T>::staging_unmet(const DevState<T> &S, int src, int dst, int fcur, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value)
+        return stg::launch_staged_tma_unmet<P1_STRESS | P1_FORCES | P1_RMAX>(S, src, dst, fcur, 16, st) ? 1 : 0;
+    return 0;
+}
+
 template <class T> void Launch<T>::stress(const DevState<T> &S, int con, int bulk, cudaStream_t st) {
     const dim3 block(kCellBX, kCellBY);
     k_stress_force<T><<<cell_grid(S.g), block, 0, st>>>(S, con, bulk);

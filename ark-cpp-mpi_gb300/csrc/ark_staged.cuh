@@ -765,6 +765,19 @@ inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fc
     k_phase1_tma<MODE, TSX, TSY><<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX, TSY), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(
         S, A, src, dst, kch);
 }
+// The bounded-wait check: the same launch with every plane expecting `extra` bytes more than its
+// boxes bring, so no stage's mbarrier completes and every block gives up (STATUS_STAGING) after
+// its bounded waits; no copy is left in flight.  False when the TMA form is not available.
+template <int MODE>
+inline bool launch_staged_tma_unmet(const DevState<float> &S, int src, int dst, int fcur, unsigned extra, cudaStream_t st) {
+    TmaArgs A;
+    if (!tma_args<MODE, 64, 4>(A, S, src, fcur)) return false;
+    for (unsigned kind = DOWN; kind <= TOP; kind <<= 1) A.m.bytes[kind] += extra;
+    const int kch = tile_chunk<64, 4>(S.g);
+    k_phase1_tma<MODE, 64, 4><<<tile_grid<64, 4>(S.g, kch), dim3(64, 4), TLayout<MODE, 64, 4>::SMEM + 128, st>>>(S, A, src,
+                                                                                                           dst, kch);
+    return true;
+}
 template <int MODE, int TSX = 64, int TSY = 4> inline void prepare_staged_tma() {
     encode_tiled(); // looked up here, outside any stream capture
     constexpr int smem = TLayout<MODE, TSX, TSY>::SMEM + 128;

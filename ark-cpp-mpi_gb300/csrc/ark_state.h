@@ -316,6 +316,10 @@ template <class T> struct Launch {
     static void halo_exchange(const Geom &g, const HaloJob *jobs, int njobs, cudaStream_t st);
     // one-time launch attributes (the staged Phase1's shared memory); host only
     static void prepare();
+    // FP32: a TMA-staged Phase1 + stress whose planes expect 16 bytes more than they bring, so
+    // its bounded waits give up and set STATUS_STAGING (the error path, without a fault); 1 if
+    // launched, 0 if the TMA form is unavailable (FP64: 0)
+    static int staging_unmet(const DevState<T> &S, int src, int dst, int fcur, cudaStream_t st);
 };
 
 // Checks the staged Phase1's copy plan of a C1 x C2 x C3 grid with kch planes per block (0:

@@ -258,6 +258,14 @@ int ark_vorticity(ark_ctx *ctx, double *out);
  * Runs on the current device. */
 int ark_selftest_division(long long n, unsigned long long seed, long long *mismatches);
 
+/* Check of the error path of the TMA-staged Phase1's bounded waits (FP32 contexts with a
+ * state): launches one Phase1 + stress on ctx's state whose planes expect 16 bytes more than
+ * their copies bring, so no stage's mbarrier completes; every block gives up after its bounded
+ * waits (half a second each), lets its copies land and leaves, and the next ark_sync reports
+ * ARK_ERR_CUDA.  No fault: the context stays usable, but its state is no longer a step's result
+ * and its error bit stays set (re-create the context).  Returns ARK_OK once launched. */
+int ark_selftest_staging_timeout(ark_ctx *ctx);
+
 /* Bounds-checked builds (compiled with -DARK_CHECK, the library's lib_check/ variant): the
  * kernels compare the indices of their global-memory accesses (sweeps, ghost fills, halo
  * exchange, boundary conditions, the closure's inference) and the cell coordinates their blocks

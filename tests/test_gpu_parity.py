@@ -565,3 +565,27 @@ def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
     for o in outs[1:]:
         for n in CELLS + FACES:
             assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), n
+
+
+def test_staging_wait_gives_up_with_status(ark, port):
+    """The TMA-staged Phase1's waits are bounded: a launch whose planes expect more bytes than
+    their copies bring makes every block give up after half a second, report STATUS_STAGING
+    through ark_sync (ARK_ERR_CUDA) and leave the device usable (no fault, no hang)."""
+    import time
+
+    p = port.channel_params(64, 4, 2, seed=3)
+    with ark.Context(params_from(ark, p, precision=ark.FP32)) as c:
+        c.upload(port.channel_state(p))
+        c.sync()
+        t0 = time.time()
+        assert ark.lib().ark_selftest_staging_timeout(c.h) == 0
+        with pytest.raises(ark.ArkError) as err:
+            c.sync()
+        assert "TMA" in str(err.value)
+        assert time.time() - t0 < 30.0
+    # the device still runs a fresh context bit for bit
+    with ark.Context(params_from(ark, p, precision=ark.FP32)) as c:
+        c.upload(port.channel_state(p))
+        c.step(3)
+        c.sync()
+        assert np.isfinite(c.download(["u1nCon"])["u1nCon"]).all()
