@@ -174,6 +174,40 @@ template <class T> struct U_ptrs {
     T **&operator[](int q) { return p[q]; }
 };
 
+// The device address of a page-locked (cudaHostAlloc / cudaHostRegister) host array, which
+// kernels may read and write in place; null for pageable memory.
+static const void *mapped_host(const void *host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError(); // pageable memory on older drivers: not an error of the caller's
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// The flag bits of every cell from the condition array (host layout hg, device memory) into the
+// padded device rows (dg), and the count of interior fluid cells (condition == 0) into *nfluid
+// (atomic integer adds: the count does not depend on their order).
+__global__ void k_condition_flags(const double *__restrict__ cond, uint8_t *__restrict__ flags, Geom hg, Geom dg,
+                                  unsigned long long *nfluid) {
+    __shared__ unsigned int cnt;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    const int64_t n = hg.ncell(), plane = hg.cs2;
+    unsigned int mine = 0;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(c / plane), rem = (int)(c - (int64_t)k * plane);
+        const int j = rem / (int)hg.cs1, i = rem - j * (int)hg.cs1;
+        const double v = cond[c];
+        const uint8_t f = (uint8_t)((v < 0.5 ? FL_LT : 0) | (v > 0.5 ? FL_GT : 0) | (v == 0 ? FL_EQ0 : 0));
+        flags[dg.cell(i, j, k)] = f;
+        if ((f & FL_EQ0) && i >= 1 && i <= hg.C1 && j >= 1 && j <= hg.C2 && k >= 1 && k <= hg.C3) ++mine;
+    }
+    if (mine) atomicAdd(&cnt, mine);
+    __syncthreads();
+    if (threadIdx.x == 0 && cnt) atomicAdd(nfluid, (unsigned long long)cnt);
+}
+
 template <class T> struct EngineT : Engine {
     ark_ctx *ctx;
     DevState<T> S;
@@ -258,18 +292,28 @@ template <class T> struct EngineT : Engine {
     // Host arrays in the Arr3d layout <-> device arrays with padded rows, through the contiguous
     // double staging buffer: one plain copy across the bus, then a kernel moves the rows (and
     // converts for FP32 contexts, whose density fields hold rho - ro0).
+    // A page-locked host array is read or written in place by the row kernels over the host
+    // link (one pass); pageable memory goes through the device staging buffer.
     int copy_in(T *dev, const double *host, int face, double offset) {
         const RowShape r = row_shape(S.g, face);
-        ARK_CUDA(cudaMemcpyAsync(ctx->stage, host, sizeof(double) * r.w * r.rows, cudaMemcpyHostToDevice, ctx->st));
-        rows_from_double<T>(dev, ctx->stage, r.w, r.rows, r.pitch, offset, ctx->st);
+        if (const double *m = (const double *)mapped_host(host)) {
+            rows_from_double<T>(dev, m, r.w, r.rows, r.pitch, offset, ctx->st);
+        } else {
+            ARK_CUDA(cudaMemcpyAsync(ctx->stage, host, sizeof(double) * r.w * r.rows, cudaMemcpyHostToDevice, ctx->st));
+            rows_from_double<T>(dev, ctx->stage, r.w, r.rows, r.pitch, offset, ctx->st);
+        }
         ARK_CUDA(cudaStreamSynchronize(ctx->st));
         return ARK_OK;
     }
 
     int copy_out(double *host, const T *dev, int face, double offset) {
         const RowShape r = row_shape(S.g, face);
-        rows_to_double<T>(ctx->stage, dev, r.w, r.rows, r.pitch, offset, ctx->st);
-        ARK_CUDA(cudaMemcpyAsync(host, ctx->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, ctx->st));
+        if (double *m = (double *)mapped_host(host)) {
+            rows_to_double<T>(m, dev, r.w, r.rows, r.pitch, offset, ctx->st);
+        } else {
+            rows_to_double<T>(ctx->stage, dev, r.w, r.rows, r.pitch, offset, ctx->st);
+            ARK_CUDA(cudaMemcpyAsync(host, ctx->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, ctx->st));
+        }
         ARK_CUDA(cudaStreamSynchronize(ctx->st));
         return ARK_OK;
     }
@@ -286,8 +330,11 @@ template <class T> struct EngineT : Engine {
         if (Storage<T>::deviation && is_face_density(which)) {
             const int d = (which - 9) / 5;
             const RowShape r = row_shape(S.g, 1);
-            rows_face_density<T>(ctx->stage, S.fc[ctx->fcur][d].p, r.w, r.rows, r.pitch, ctx->k.ro0, ctx->k.rc2, ctx->st);
-            ARK_CUDA(cudaMemcpyAsync(host, ctx->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, ctx->st));
+            double *m = (double *)mapped_host(host);
+            rows_face_density<T>(m ? m : ctx->stage, S.fc[ctx->fcur][d].p, r.w, r.rows, r.pitch, ctx->k.ro0, ctx->k.rc2,
+                                 ctx->st);
+            if (!m)
+                ARK_CUDA(cudaMemcpyAsync(host, ctx->stage, sizeof(double) * r.w * r.rows, cudaMemcpyDeviceToHost, ctx->st));
             ARK_CUDA(cudaStreamSynchronize(ctx->st));
             return ARK_OK;
         }
@@ -626,6 +673,7 @@ int ark_destroy(ark_ctx *ctx) {
             if (ctx->graph[a][b]) cudaGraphExecDestroy(ctx->graph[a][b]);
     ctx->eng.reset();
     if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->cond_dev) cudaFree(ctx->cond_dev);
     for (double *a : ctx->avg.a)
         if (a) cudaFree(a);
     if (ctx->closure_net) cudaFree(ctx->closure_net);
@@ -661,26 +709,22 @@ int ark_upload(ark_ctx *ctx, const ark_host_state *h) {
         if (int rc = ctx->eng->upload_field(w, kFields[w].face, h->*kFields[w].member)) return rc;
     }
     if (!h->condition) return ARK_OK; // keep the condition (and the scalars) of the last upload
-    // condition: kept on the host for download, turned into flag bits on the device
+    // condition: a device copy in the host layout (for download), turned into flag bits and the
+    // fluid-cell count on the device; the scalars start from zero
     const Geom hg = host_geom(ctx->g.C1, ctx->g.C2, ctx->g.C3);
     const size_t nc = (size_t)hg.ncell();
-    ctx->cond_host.assign(h->condition, h->condition + nc);
-    std::vector<uint8_t> fl(nc);
-    long long nfluid = 0;
-    for (size_t c = 0; c < nc; ++c) {
-        const double v = h->condition[c];
-        fl[c] = (uint8_t)((v < 0.5 ? FL_LT : 0) | (v > 0.5 ? FL_GT : 0) | (v == 0 ? FL_EQ0 : 0));
+    if (!ctx->cond_dev && cudaMalloc(&ctx->cond_dev, sizeof(double) * nc) != cudaSuccess) {
+        ctx->cond_dev = nullptr;
+        return fail(ARK_ERR_NOMEM, "condition array allocation failed");
     }
-    for (int k = 1; k <= hg.C3; ++k)
-        for (int j = 1; j <= hg.C2; ++j)
-            for (int i = 1; i <= hg.C1; ++i)
-                if (fl[(size_t)hg.cell(i, j, k)] & FL_EQ0) ++nfluid;
-    ARK_CUDA(copy_rows(ctx->eng->flags(), fl.data(), ctx->g, 0, 1, cudaMemcpyHostToDevice, ctx->st));
+    ARK_CUDA(cudaMemcpyAsync(ctx->cond_dev, h->condition, sizeof(double) * nc, cudaMemcpyHostToDevice, ctx->st));
+    DevScalars *sc = ctx->eng->scalars();
+    ARK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), ctx->st));
+    const int blocks = (int)std::min<size_t>((nc + 255) / 256, 152 * 16);
+    k_condition_flags<<<blocks, 256, 0, ctx->st>>>(ctx->cond_dev, ctx->eng->flags(), hg, ctx->g,
+                                                    (unsigned long long *)&sc->nfluid);
+    ARK_CUDA(cudaGetLastError());
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
-    DevScalars sc;
-    std::memset(&sc, 0, sizeof(sc));
-    sc.nfluid = nfluid;
-    ARK_CUDA(cudaMemcpy(ctx->eng->scalars(), &sc, sizeof(sc), cudaMemcpyHostToDevice));
     ctx->uploaded = true;
     return ARK_OK;
 }
@@ -693,11 +737,13 @@ int ark_download(ark_ctx *ctx, ark_host_state *h) {
         double *dst = h->*kFields[w].member;
         if (!dst) continue;
         if (w == 8) {
-            std::memcpy(dst, ctx->cond_host.data(), sizeof(double) * ctx->cond_host.size());
+            ARK_CUDA(cudaMemcpyAsync(dst, ctx->cond_dev, sizeof(double) * (size_t)host_geom(ctx->g.C1, ctx->g.C2, ctx->g.C3).ncell(),
+                                     cudaMemcpyDeviceToHost, ctx->st));
             continue;
         }
         if (int rc = ctx->eng->download_field(w, kFields[w].face, dst)) return rc;
     }
+    ARK_CUDA(cudaStreamSynchronize(ctx->st));
     return ARK_OK;
 }
 
@@ -730,7 +776,8 @@ int ark_get_array(ark_ctx *ctx, const char *name, double *host) {
     if (!name || !host) return fail(ARK_ERR_PARAM, "NULL name or buffer");
     ARK_CUDA(cudaStreamSynchronize(ctx->st));
     if (std::strcmp(name, "condition") == 0) {
-        std::memcpy(host, ctx->cond_host.data(), sizeof(double) * ctx->cond_host.size());
+        ARK_CUDA(cudaMemcpy(host, ctx->cond_dev, sizeof(double) * (size_t)host_geom(ctx->g.C1, ctx->g.C2, ctx->g.C3).ncell(),
+                            cudaMemcpyDeviceToHost));
         return ARK_OK;
     }
     for (int w = 0; w < 24; ++w)

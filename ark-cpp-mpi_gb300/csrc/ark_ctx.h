@@ -74,7 +74,7 @@ struct ark_ctx {
     ark::Consts k;
     cudaStream_t st = nullptr;
     std::unique_ptr<ark::Engine> eng;
-    std::vector<double> cond_host;
+    double *cond_dev = nullptr; // the last uploaded condition array (host layout), on the device
     int con = 0;  // the cell level holding "Con"
     int fcur = 0; // the current face generation
     bool uploaded = false;
