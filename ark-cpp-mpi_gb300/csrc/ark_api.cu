@@ -296,7 +296,10 @@ template <class T> struct EngineT : Engine {
     // link (one pass); pageable memory goes through the device staging buffer.
     int copy_in(T *dev, const double *host, int face, double offset) {
         const RowShape r = row_shape(S.g, face);
-        if (const double *m = (const double *)mapped_host(host)) {
+        const double *m = (const double *)mapped_host(host);
+        if (m && ((uintptr_t)m & 15) == 0) {
+            flat_from_host<T>(dev, m, r.w, r.rows, r.pitch, offset, ctx->st);
+        } else if (m) {
             rows_from_double<T>(dev, m, r.w, r.rows, r.pitch, offset, ctx->st);
         } else {
             ARK_CUDA(cudaMemcpyAsync(ctx->stage, host, sizeof(double) * r.w * r.rows, cudaMemcpyHostToDevice, ctx->st));
@@ -308,7 +311,10 @@ template <class T> struct EngineT : Engine {
 
     int copy_out(double *host, const T *dev, int face, double offset) {
         const RowShape r = row_shape(S.g, face);
-        if (double *m = (double *)mapped_host(host)) {
+        double *m = (double *)mapped_host(host);
+        if (m && ((uintptr_t)m & 15) == 0) {
+            flat_to_host<T>(m, dev, r.w, r.rows, r.pitch, offset, ctx->st);
+        } else if (m) {
             rows_to_double<T>(m, dev, r.w, r.rows, r.pitch, offset, ctx->st);
         } else {
             rows_to_double<T>(ctx->stage, dev, r.w, r.rows, r.pitch, offset, ctx->st);

@@ -6,6 +6,8 @@ namespace ark {
 template struct Launch<float>;
 template void rows_from_double<float>(float *, const double *, int, int64_t, int, double, cudaStream_t);
 template void rows_to_double<float>(double *, const float *, int, int64_t, int, double, cudaStream_t);
+template void flat_from_host<float>(float *, const double *, int, int64_t, int, double, cudaStream_t);
+template void flat_to_host<float>(double *, const float *, int, int64_t, int, double, cudaStream_t);
 template void rows_face_density<float>(double *, const float *, int, int64_t, int, double, double, cudaStream_t);
 
 } // namespace ark

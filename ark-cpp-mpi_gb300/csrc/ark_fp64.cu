@@ -9,6 +9,8 @@ namespace ark {
 template struct Launch<double>;
 template void rows_from_double<double>(double *, const double *, int, int64_t, int, double, cudaStream_t);
 template void rows_to_double<double>(double *, const double *, int, int64_t, int, double, cudaStream_t);
+template void flat_from_host<double>(double *, const double *, int, int64_t, int, double, cudaStream_t);
+template void flat_to_host<double>(double *, const double *, int, int64_t, int, double, cudaStream_t);
 template void rows_face_density<double>(double *, const double *, int, int64_t, int, double, double, cudaStream_t);
 
 // Self-check of div_rn against the hardware IEEE division: n operand pairs from splitmix64

@@ -2415,6 +2415,42 @@ __global__ void k_rows_face_density(double *dst, const T *p, int w, int64_t rows
     if (c >= w) return;
     for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) dst[r * w + c] = ro0 + (double)p[r * pitch + c] * rc2;
 }
+// The same conversions with the host array read or written in place (page-locked host memory
+// over the host link): the host side walked flat, two doubles per 16-byte access, four accesses
+// in flight per thread; the device side scattered into its padded rows.  The host array must
+// start on a 16-byte boundary.
+template <class T> __global__ void k_flat_in(T *dst, const double2 *src, int w, int64_t n, int pitch, double offset) {
+    const int64_t n2 = n >> 1, step = (int64_t)gridDim.x * blockDim.x;
+    auto put = [&](int64_t e, double v) {
+        const int64_t r = e / w;
+        dst[r * pitch + (e - r * w)] = (T)(offset == 0.0 ? v : v - offset);
+    };
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += 4 * step) {
+        double2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (q + u * step < n2) v[u] = src[q + u * step];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (q + u * step < n2) {
+                put(2 * (q + u * step), v[u].x);
+                put(2 * (q + u * step) + 1, v[u].y);
+            }
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) put(n - 1, ((const double *)src)[n - 1]);
+}
+template <class T> __global__ void k_flat_out(double2 *dst, const T *src, int w, int64_t n, int pitch, double offset) {
+    const int64_t n2 = n >> 1, step = (int64_t)gridDim.x * blockDim.x;
+    auto get = [&](int64_t e) {
+        const int64_t r = e / w;
+        const double v = (double)src[r * pitch + (e - r * w)];
+        return offset == 0.0 ? v : v + offset;
+    };
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += step)
+        dst[q] = make_double2(get(2 * q), get(2 * q + 1));
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) ((double *)dst)[n - 1] = get(n - 1);
+}
+
 inline dim3 rows_grid(int w, int64_t rows) {
     return dim3((w + 127) / 128, (unsigned)(rows < 16384 ? (rows < 1 ? 1 : rows) : 16384));
 }
@@ -2426,6 +2462,14 @@ void rows_from_double(T *dst, const double *src, int w, int64_t rows, int pitch,
 template <class T>
 void rows_to_double(double *dst, const T *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st) {
     k_rows_out<T><<<rows_grid(w, rows), 128, 0, st>>>(dst, src, w, rows, pitch, offset);
+}
+template <class T>
+void flat_from_host(T *dst, const double *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st) {
+    k_flat_in<T><<<152 * 8, 256, 0, st>>>(dst, (const double2 *)src, w, (int64_t)w * rows, pitch, offset);
+}
+template <class T>
+void flat_to_host(double *dst, const T *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st) {
+    k_flat_out<T><<<152 * 8, 256, 0, st>>>((double2 *)dst, src, w, (int64_t)w * rows, pitch, offset);
 }
 template <class T>
 void rows_face_density(double *dst, const T *p, int w, int64_t rows, int pitch, double ro0, double rc2, cudaStream_t st) {

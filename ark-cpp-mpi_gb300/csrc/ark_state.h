@@ -388,6 +388,11 @@ template <class T>
 void rows_from_double(T *dst, const double *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st);
 template <class T>
 void rows_to_double(double *dst, const T *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st);
+// the same with dst / src page-locked host memory (16-byte aligned) read or written in place
+template <class T>
+void flat_from_host(T *dst, const double *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st);
+template <class T>
+void flat_to_host(double *dst, const T *src, int w, int64_t rows, int pitch, double offset, cudaStream_t st);
 template <class T>
 void rows_face_density(double *dst, const T *p, int w, int64_t rows, int pitch, double ro0, double rc2, cudaStream_t st);
 // the row shape of a cell (face = 0) or face (1) array: w values per row, rows, pitch
