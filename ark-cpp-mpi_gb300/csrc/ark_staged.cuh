@@ -549,6 +549,9 @@ __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
 __device__ __forceinline__ void mbar_inval(unsigned bar) { asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory"); }
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
@@ -595,7 +598,8 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
 // proxy first when fence_maps is set).  A wait that does not end within half a second sets
 // STATUS_STAGING, and the block lets its copies in flight land (again with a limit) and
 // leaves.  Every thread calls it; it ends with no copy in flight and the mbarriers
-// invalidated, so a persistent kernel may run it again.
+// invalidated, so a persistent kernel may run it again.  (The ensemble's persistent kernel runs
+// this form: its work items are short, and the producer-warp form below measured slower there.)
 template <int MODE, int TSX, int TSY, class Maps>
 __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
                                                 int src, int dst, int kch, const BIx &bx, unsigned char *sm,
@@ -683,18 +687,128 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
     if (MODE & (P1_RMAX | P1_RSUM)) tile_store<T, NT>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
 }
 
+// The same with a producer warp (the single-grid kernel): TSX * TSY consumer threads (one cell
+// column each) and one producer warp (threads TSX * TSY ..; its lane 0 works).  The producer issues a plane's
+// boxes into its stage (NS stages) once every consumer warp has released the plane the slot
+// held; every consumer waits for the planes it reads on the stage's "full" mbarrier and each
+// consumer warp, done with a plane, arrives on the stage's "empty" mbarrier.  No block-wide
+// barrier runs per plane.  A consumer at plane k reads k - 1 (with the stress), k and k + 1
+// and then releases k - 1 (with the stress) or k.  bar: NS full, NS empty mbarriers and an
+// abort flag.  map(q) is box q's tensor map (global maps are fenced for the tensor-map proxy
+// first when fence_maps is set).  A wait that does not end within half a second sets
+// STATUS_STAGING and the abort flag; every thread then leaves its loop (at most one more
+// bounded wait each), and the block lets its copies in flight land (again with a limit) and
+// leaves.  Every thread calls it; it ends with no copy in flight and the mbarriers
+// invalidated, so a persistent kernel may run it again.
+template <int MODE, int TSX, int TSY, class Maps>
+__device__ __forceinline__ void phase1_tma_body_pw(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
+                                                int src, int dst, int kch, const BIx &bx, unsigned char *sm,
+                                                unsigned long long *bar) {
+    using L = TLayout<MODE, TSX, TSY>;
+    using T = float;
+    constexpr bool STRESS = L::STRESS;
+    constexpr int NS = L::NS, SX = TSX, SY = TSY, NT = TSX * TSY;
+    constexpr unsigned long long kLimitNs = 500000000ull;
+    const Geom g = S.g;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x, tx = t % SX, ty = t / SX;
+    const bool consumer = t < NT;
+    const int i = bx.x * SX + tx + 1, j = bx.y * SY + ty + 1;
+    const int x0 = bx.x * SX, j0 = bx.y * SY + 1;
+    const int k0 = bx.z * kch + 1;
+    const int k1 = k0 + kch - 1 < g.C3 ? k0 + kch - 1 : g.C3;
+    const int pfirst = STRESS ? k0 - 1 : k0, plast = k1 + 1;
+    const unsigned sbase = smem_u32(sm);
+    auto bar_of = [&](int p) { return smem_u32(&bar[(p - pfirst) % NS]); };       // full
+    auto empty_of = [&](int p) { return smem_u32(&bar[NS + (p - pfirst) % NS]); }; // empty
+    auto parity_of = [&](int p) { return (unsigned)(((p - pfirst) / NS) & 1); };
+    volatile unsigned long long *const abort_flag = bar + 2 * NS;
+    if (t == NT) {
+        if (fence_maps)
+            for (int q = 0; q < A.n; ++q) fence_tensormap(map(q));
+        for (int q = 0; q < NS; ++q) {
+            mbar_init(smem_u32(&bar[q]), 1);
+            mbar_init(smem_u32(&bar[NS + q]), NT / 32);
+        }
+        *abort_flag = 0;
+        fence_mbar_init();
+        fence_proxy_async();
+    }
+    __syncthreads();
+
+    bool failed = false;
+    int issued = pfirst - 1; // the producer: the last plane issued
+    unsigned long long m0 = 0, m1 = 0, m2 = 0;
+    long long rsum = 0;
+    if (t == NT) { // the producer
+        for (int p = pfirst; p <= plast; ++p) {
+            // the slot's previous plane, p - NS, released by every consumer warp
+            if (p - NS >= pfirst && !mbar_wait(empty_of(p - NS), parity_of(p - NS), kLimitNs)) {
+                *abort_flag = 1;
+                failed = true;
+                break;
+            }
+            if (*abort_flag) break;
+            const unsigned kind = p < k0 ? DOWN : (p > k1 ? TOP : MID);
+            const unsigned to = sbase + (unsigned)(((p - pfirst) % NS) * L::STAGE), b = bar_of(p);
+            fence_proxy_async();
+            mbar_expect_tx(b, A.bytes[kind]);
+            for (int q = 0; q < A.n; ++q)
+                if (A.when[q] & kind) tma_load_4d(to + A.dst[q], map(q), x0, j0 + A.row0[q], p, 0, b);
+            issued = p;
+        }
+    } else if (consumer) {
+        const K<T> &kk = kconst<T>(S.k);
+        const T dt = sc_dt<T>(S.sc);
+        const T G1 = (MODE & P1_BULK) ? sc_G<T>(S.sc) : (T)0;
+        const bool valid = i <= g.C1 && j <= g.C2;
+        for (int k = k0; k <= k1; ++k) {
+            bool ok = true;
+            if (k == k0) {
+                if (STRESS) ok = mbar_wait(bar_of(k - 1), parity_of(k - 1), kLimitNs);
+                ok = ok && mbar_wait(bar_of(k), parity_of(k), kLimitNs);
+            }
+            ok = ok && mbar_wait(bar_of(k + 1), parity_of(k + 1), kLimitNs);
+            if (!ok) *abort_flag = 1;
+            // warp-uniform (the warp's lanes meet at __syncwarp below)
+            if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) {
+                failed = true;
+                break;
+            }
+            if (valid) {
+                const unsigned char *sk = sm + ((k - pfirst) % NS) * L::STAGE;
+                const unsigned char *su = sm + ((k + 1 - pfirst) % NS) * L::STAGE;
+                const unsigned char *sd = STRESS ? sm + ((k - 1 - pfirst) % NS) * L::STAGE : sk;
+                staged_cell<MODE, L>(S, dst, sd, sk, su, i, j, k, tx, ty, kk, dt, G1, m0, m1, m2, rsum);
+            }
+            // the warp is done with plane k - 1 (with the stress) or k
+            __syncwarp();
+            if ((t & 31) == 0) mbar_arrive(empty_of(STRESS ? k - 1 : k));
+        }
+    }
+    if (failed) atomicOr(&S.sc->status, STATUS_STAGING);
+    __syncthreads();
+    if (t == NT && *abort_flag) // the last NS planes issued hold each stage's newest phase
+        for (int p = issued - NS + 1 > pfirst ? issued - NS + 1 : pfirst; p <= issued; ++p)
+            mbar_wait(bar_of(p), parity_of(p), kLimitNs);
+    __syncthreads();
+    if (t == NT)
+        for (int q = 0; q < 2 * NS; ++q) mbar_inval(smem_u32(&bar[q]));
+    if (MODE & (P1_RMAX | P1_RSUM))
+        tile_store<T, NT + 32>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
+}
+
 // The stages from the first 128-byte boundary of the dynamic shared memory (tensor copies
 // land on 128-byte boundaries; launches ask for 128 bytes more).
 __device__ __forceinline__ unsigned char *align128(unsigned char *p) { return p + ((128u - (smem_u32(p) & 127u)) & 127u); }
 
 // The single-grid kernel: maps and boxes as parameters.
 template <int MODE, int TSX, int TSY>
-__global__ void __launch_bounds__(TSX *TSY, 2)
+__global__ void __launch_bounds__(TSX *TSY + 32, 2)
     k_phase1_tma(const __grid_constant__ DevState<float> S, const __grid_constant__ TmaArgs A, int src, int dst, int kch) {
     extern __shared__ __align__(128) unsigned char sm_raw[];
-    __shared__ __align__(8) unsigned long long bar[TLayout<MODE, TSX, TSY>::NS];
+    __shared__ __align__(8) unsigned long long bar[2 * TLayout<MODE, TSX, TSY>::NS + 1];
     auto map = [&](int q) { return &A.map[q]; };
-    phase1_tma_body<MODE, TSX, TSY>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar);
+    phase1_tma_body_pw<MODE, TSX, TSY>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
@@ -762,7 +876,7 @@ inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fc
         return;
     }
     const int kch = tile_chunk<TSX, TSY>(S.g);
-    k_phase1_tma<MODE, TSX, TSY><<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX, TSY), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(
+    k_phase1_tma<MODE, TSX, TSY><<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX * TSY + 32), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(
         S, A, src, dst, kch);
 }
 // The bounded-wait check: the same launch with every plane expecting `extra` bytes more than its
@@ -774,7 +888,7 @@ inline bool launch_staged_tma_unmet(const DevState<float> &S, int src, int dst, 
     if (!tma_args<MODE, 64, 4>(A, S, src, fcur)) return false;
     for (unsigned kind = DOWN; kind <= TOP; kind <<= 1) A.m.bytes[kind] += extra;
     const int kch = tile_chunk<64, 4>(S.g);
-    k_phase1_tma<MODE, 64, 4><<<tile_grid<64, 4>(S.g, kch), dim3(64, 4), TLayout<MODE, 64, 4>::SMEM + 128, st>>>(S, A, src,
+    k_phase1_tma<MODE, 64, 4><<<tile_grid<64, 4>(S.g, kch), dim3(64 * 4 + 32), TLayout<MODE, 64, 4>::SMEM + 128, st>>>(S, A, src,
                                                                                                            dst, kch);
     return true;
 }
