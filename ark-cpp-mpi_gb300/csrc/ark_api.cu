@@ -429,10 +429,21 @@ template <class T> struct EngineT : Engine {
         // the Con level's density needs no ghosts
         const int xg = ctx->p2mode != 0 ? 1 : 0;
         const bool nofill = skip_phase2_fill();
-        Launch<T>::finalize_dt(S, 1, st);
-        mark();
-        Launch<T>::wrap_con(S, y, xg ? 2 : nofill ? 0 : 1, st);
-        mark();
+        if (!ev) {
+            // captured: the ghost fill (the "Con" level's ghosts) beside dt (the partial slots
+            // and the scalars): independent work, both done before Phase1
+            cudaEventRecord(ctx->fill_fork, st);
+            cudaStreamWaitEvent(ctx->fill, ctx->fill_fork, 0);
+            Launch<T>::wrap_con(S, y, xg ? 2 : nofill ? 0 : 1, ctx->fill);
+            cudaEventRecord(ctx->fill_join, ctx->fill);
+            Launch<T>::finalize_dt(S, 1, st);
+            cudaStreamWaitEvent(st, ctx->fill_join, 0);
+        } else { // timed one launch after the other
+            Launch<T>::finalize_dt(S, 1, st);
+            mark();
+            Launch<T>::wrap_con(S, y, xg ? 2 : nofill ? 0 : 1, st);
+            mark();
+        }
         if (ctx->closure_net) cudaStreamWaitEvent(st, ctx->join, 0);
         Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st);
         mark();
@@ -631,7 +642,10 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     // learned closure's inference) only takes SMs the step's kernels leave idle
     int prio_low = 0, prio_high = 0;
     cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
-    if (cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, prio_high) != cudaSuccess) {
+    if (cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->fill, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fill_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fill_join, cudaEventDisableTiming) != cudaSuccess) {
         *status = fail(ARK_ERR_CUDA, "cudaStreamCreate failed");
         return nullptr;
     }
@@ -689,6 +703,12 @@ int ark_destroy(ark_ctx *ctx) {
     }
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->join) cudaEventDestroy(ctx->join);
+    if (ctx->fill) {
+        cudaStreamSynchronize(ctx->fill);
+        cudaStreamDestroy(ctx->fill);
+    }
+    if (ctx->fill_fork) cudaEventDestroy(ctx->fill_fork);
+    if (ctx->fill_join) cudaEventDestroy(ctx->fill_join);
     for (int b = 0; b < 2; ++b) {
         if (ctx->io_dev[b]) cudaFree(ctx->io_dev[b]);
         if (ctx->io_host[b]) cudaFreeHost(ctx->io_host[b]);

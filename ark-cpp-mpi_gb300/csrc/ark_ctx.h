@@ -89,6 +89,8 @@ struct ark_ctx {
     void *closure_net = nullptr;          // learned closure: the network's constants (device copy)
     cudaStream_t side = nullptr;          // the closure's branch of the step
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t fill = nullptr;          // the captured step's ghost fill, beside dt
+    cudaEvent_t fill_fork = nullptr, fill_join = nullptr;
     float closure_scale = 0.f;            // u_tau / vis for the y+ feature
     int seg_target = 32;                  // x2/x3 sweep segment length (faces)
     int p2mode = 0; // Phase2: 0 three sweep kernels, 1 one kernel for the three sweeps, 2 (FP32)
