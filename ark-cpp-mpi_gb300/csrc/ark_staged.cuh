@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(TSX *TSY + 32, 2)
     phase1_tma_body_pw<MODE, TSX, TSY>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar);
 }
 
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
+// cuTensorMapEncodeTiled through the runtime's entry-point lookup (no link to libcuda)
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
