@@ -400,7 +400,7 @@ template <class T> struct EngineT : Engine {
     void use_forces(int ncon) override { Launch<T>::use_forces(S, ncon, ctx->st); }
     void phase2(int con, int fcur) override {
         Launch<T>::wrap_phase2(S, con, fcur, ctx->st);
-        for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, con, fcur, ax, ctx->st, ctx->seg_target);
+        for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, con, fcur, ax, ctx->st, ctx->seg_target, ctx->x1_lines);
     }
     // One full step of main.cpp:82-91 with "Con" = level x at entry and exit, reading the
     // dt / bulk-flow partials of the current state and leaving those of the next one.  With
@@ -468,7 +468,7 @@ template <class T> struct EngineT : Engine {
             for (int ax = 0; ax < 3; ++ax) mark();
         } else {
             for (int ax = 0; ax < 3; ++ax) {
-                Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target);
+                Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
                 mark();
             }
         }
@@ -525,7 +525,7 @@ template <class T> struct EngineT : Engine {
             break;
         case 3: Launch<T>::wrap_phase2(S, y, fcur, st); break;
         default:
-            for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target);
+            for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
             Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
             break;
         }
@@ -1335,7 +1335,8 @@ extern "C" {
 // Times the candidate kernel shapes on the live state (results do not depend on the shape)
 // one setting at a time: the shape of the Phase1 with stress, then of the second Phase1, then
 // the three sweeps separate or fused, then (separate) the x2/x3 sweep segment (8, 16, 32, 64
-// faces).  choice (may be NULL): {shape 1, shape 2, segment, microseconds per step, fused}.
+// faces) and the x1 sweep's lines per warp (1 to 4).  choice (may be NULL): {shape 1, shape 2,
+// segment, microseconds per step, fused}.
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (steps_per_candidate < 1) return fail(ARK_ERR_PARAM, "steps_per_candidate < 1");
@@ -1361,20 +1362,23 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     auto set = [&](int which, int v) {
         if (which < 2) ctx->march[which] = v;
         else if (which == 2) ctx->p2mode = v;
-        else ctx->seg_target = v;
+        else if (which == 3) ctx->seg_target = v;
+        else ctx->x1_lines = v;
     };
-    for (int which = 0; which < 4; ++which) {
+    if (ctx->x1_lines <= 0) ctx->x1_lines = x_lines_per_warp(ctx->g, !fp32);
+    for (int which = 0; which < 5; ++which) {
         const int segs[4] = {8, 16, 32, 64};
+        const int lines[4] = {1, 2, 3, 4}; // x1 sweep lines per warp
         // Phase2 forms: the three sweep kernels, or (FP32) one kernel for the sweeps and the
         // second Phase1.  The one-kernel Phase2 alone (mode 1) is correct but slower at every
         // size measured: left to ARK_PHASE2_FUSED=1, not tried here.
         const int p2cand[3] = {0, 2, 3};
         if (which == 2 && !fp32) continue;
         const int ncand = which < 2 ? (fp32 ? 4 : 3) : which == 2 ? 3 : 4;
-        int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : ctx->seg_target;
-        if (which == 3 && ctx->p2mode) continue; // the one-kernel forms have no segments
+        int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : which == 3 ? ctx->seg_target : ctx->x1_lines;
+        if (which >= 3 && ctx->p2mode) continue; // the one-kernel forms have no segments, no x1 sweep
         for (int c = 0; c < ncand; ++c) {
-            const int v = which < 2 ? shapes[c] : which == 2 ? p2cand[c] : segs[c];
+            const int v = which < 2 ? shapes[c] : which == 2 ? p2cand[c] : which == 3 ? segs[c] : lines[c];
             if (v == keep) continue;
             set(which, v);
             double us = 0.0;

@@ -1677,16 +1677,6 @@ __device__ __forceinline__ int zface(int s, int C3, bool periodic) {
 // computed.  A face needs the forward values of the cell behind it: a shuffle from the
 // neighbouring lane, or the carry from the previous chunk's last lane.  Old faces come from
 // generation fcur, new faces go to fcur^1.
-// Lines per warp in the x1 sweep: a warp walks the cells 0..C1+1 of that many consecutive lines as
-// one stream of positions, 32 at a time, so a chunk that ends one line carries on with the next
-// instead of leaving lanes idle (a 32-cell line alone fills 34 of 64 lanes).  Short lines: 4.
-// Long lines waste less and keep more warps for the waves to come out even: FP64 takes 2 (a
-// 256-cell line alone leaves 30 of 288 lanes idle; 2 lines per warp 28 of 544: 0.496 -> 0.484
-// ms at 256x128x128, where 4 lines made it 20% slower), FP32 1 (2 lines: 0.422 -> 0.431 ms at
-// 512x256x256).
-__host__ __device__ inline int x_lines_per_warp(const Geom &g, bool fp64 = false) {
-    return g.C1 < 200 ? 4 : fp64 ? 2 : 1;
-}
 
 template <class T>
 __device__ __forceinline__ void sweep_x_body(const DevState<T> &S, int con, int fcur, int glines, const BIx &bx) {
@@ -2348,9 +2338,10 @@ inline int sweep_segment(int nd, int target, int *nseg) {
     return (nd + n - 1) / n;
 }
 
-template <class T> void Launch<T>::sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target) {
+template <class T>
+void Launch<T>::sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target, int xlines) {
     if (axis == 0) {
-        const int lines_x = S.g.C2 * S.g.C3, gl = x_lines_per_warp(S.g, sizeof(T) == 8);
+        const int lines_x = S.g.C2 * S.g.C3, gl = xlines > 0 ? xlines : x_lines_per_warp(S.g, sizeof(T) == 8);
         const dim3 grid((lines_x + 4 * gl - 1) / (4 * gl)); // 4 warps of gl lines
         k_sweep_x<T><<<grid, 128, 0, st>>>(S, con, fcur, gl);
     } else if (axis == 1) {

@@ -93,6 +93,17 @@ inline Geom host_geom(int C1, int C2, int C3) {
     return g;
 }
 
+// Lines per warp in the x1 sweep: a warp walks the cells 0..C1+1 of that many consecutive lines as
+// one stream of positions, 32 at a time, so a chunk that ends one line carries on with the next
+// instead of leaving lanes idle (a 32-cell line alone fills 34 of 64 lanes).  Short lines: 4.
+// Long lines waste less, and the count also sets how evenly the blocks fill the GPU's waves:
+// FP64 takes 3 (at 256x128x128: 1 line 0.495 ms, 2 lines 0.484, 3 lines 0.457, where the
+// blocks make 3.0 waves; 4 lines 20% slower), FP32 1 (2 lines: 0.422 -> 0.431 ms at
+// 512x256x256).  ark_autotune tries 1 to 4 per context.
+__host__ __device__ inline int x_lines_per_warp(const Geom &g, bool fp64 = false) {
+    return g.C1 < 200 ? 4 : fp64 ? 3 : 1;
+}
+
 // Device arrays keep the same (i, j, k) indexing with every row padded to one pitch for cells
 // and faces: a multiple of 32 elements (rows start on 128-byte boundaries, as bulk copies need),
 // and long enough that the row segment a 64-cell tile stages (68 elements from x = 64*tile, or
@@ -300,7 +311,8 @@ template <class T> struct Launch {
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
     // x2/x3 sweeps: lines cut into balanced segments of at most `target` faces
-    static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target = 32);
+    // x1 sweep: xlines lines per warp (0: x_lines_per_warp's choice)
+    static void sweep(const DevState<T> &S, int con, int fcur, int axis, cudaStream_t st, int target = 32, int xlines = 0);
     // the three sweeps in one kernel (same results)
     static void phase2_fused(const DevState<T> &S, int con, int fcur, cudaStream_t st);
     // FP32: the three sweeps and the second Phase1 (UseForces, bulk-flow partials) in one kernel,
