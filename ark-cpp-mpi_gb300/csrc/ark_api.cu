@@ -386,7 +386,7 @@ template <class T> struct EngineT : Engine {
         Launch<T>::reduce_start(S, con, ctx->st);
     }
     void phase1(int src, int dst, int fcur, int mode) override {
-        Launch<T>::phase1(S, src, dst, fcur, mode, ctx->march[0], ctx->st);
+        Launch<T>::phase1(S, src, dst, fcur, mode, ctx->march[0], ctx->st, ctx->p1_chunk);
     }
     void stress(int con, int bulk) override {
         Launch<T>::wrap_con(S, con, 0, ctx->st);
@@ -445,7 +445,7 @@ template <class T> struct EngineT : Engine {
             mark();
         }
         if (ctx->closure_net) cudaStreamWaitEvent(st, ctx->join, 0);
-        Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st);
+        Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st, ctx->p1_chunk);
         mark();
         if (!nofill) {
             Launch<T>::wrap_phase2(S, y, fcur, st, xg);
@@ -472,7 +472,7 @@ template <class T> struct EngineT : Engine {
                 mark();
             }
         }
-        Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
+        Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st, ctx->p1_chunk);
         mark();
         // AverageValues after the step (main.cpp:93-96 when enabled), outside the timed marks
         if (ctx->averaging) output_average_add<T>(S, y, ctx->avg, st);
@@ -521,12 +521,12 @@ template <class T> struct EngineT : Engine {
         case 1: Launch<T>::wrap_con(S, y, 1, st); break;
         case 2:
             Launch<T>::phase1(S, y, x, fcur, P1_STRESS | P1_FORCES | P1_RMAX | (ctx->k.forcing ? P1_BULK : 0),
-                              ctx->march[0], st);
+                              ctx->march[0], st, ctx->p1_chunk);
             break;
         case 3: Launch<T>::wrap_phase2(S, y, fcur, st); break;
         default:
             for (int ax = 0; ax < 3; ++ax) Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
-            Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st);
+            Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st, ctx->p1_chunk);
             break;
         }
     }
@@ -1335,8 +1335,8 @@ extern "C" {
 // Times the candidate kernel shapes on the live state (results do not depend on the shape)
 // one setting at a time: the shape of the Phase1 with stress, then of the second Phase1, then
 // the three sweeps separate or fused, then (separate) the x2/x3 sweep segment (8, 16, 32, 64
-// faces) and the x1 sweep's lines per warp (1 to 4).  choice (may be NULL): {shape 1, shape 2,
-// segment, microseconds per step, fused}.
+// faces), the x1 sweep's lines per warp (1 to 4) and the staged Phase1's planes per block.
+// choice (may be NULL): {shape 1, shape 2, segment, microseconds per step, fused}.
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     if (int rc = check_ctx(ctx, true)) return rc;
     if (steps_per_candidate < 1) return fail(ARK_ERR_PARAM, "steps_per_candidate < 1");
@@ -1363,12 +1363,33 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         if (which < 2) ctx->march[which] = v;
         else if (which == 2) ctx->p2mode = v;
         else if (which == 3) ctx->seg_target = v;
-        else ctx->x1_lines = v;
+        else if (which == 4) ctx->x1_lines = v;
+        else ctx->p1_chunk = v;
     };
     if (ctx->x1_lines <= 0) ctx->x1_lines = x_lines_per_warp(ctx->g, !fp32);
-    for (int which = 0; which < 5; ++which) {
+    for (int which = 0; which < 6; ++which) {
         const int segs[4] = {8, 16, 32, 64};
         const int lines[4] = {1, 2, 3, 4}; // x1 sweep lines per warp
+        // planes per block of the staged / face-centric Phase1 (0: the default rule); the count
+        // sets how evenly the blocks fill the GPU's waves against the halo planes per block
+        const int chunks[8] = {0, 2, 4, 6, 8, 16, 32, 48};
+        if (which == 5) {
+            const bool staged = (ctx->march[0] >= 2 || ctx->march[1] >= 2);
+            if (!staged) continue;
+            int keep = ctx->p1_chunk;
+            for (int v : chunks) {
+                if (v == keep || v > ctx->g.C3) continue;
+                set(which, v);
+                double us = 0.0;
+                if (int rc = measure(&us)) return rc;
+                if (us < best) {
+                    best = us;
+                    keep = v;
+                }
+            }
+            set(which, keep);
+            continue;
+        }
         // Phase2 forms: the three sweep kernels, or (FP32) one kernel for the sweeps and the
         // second Phase1.  The one-kernel Phase2 alone (mode 1) is correct but slower at every
         // size measured: left to ARK_PHASE2_FUSED=1, not tried here.

@@ -94,6 +94,7 @@ struct ark_ctx {
     float closure_scale = 0.f;            // u_tau / vis for the y+ feature
     int seg_target = 32;                  // x2/x3 sweep segment length (faces)
     int x1_lines = 0;                     // x1 sweep lines per warp (0: x_lines_per_warp's choice)
+    int p1_chunk = 0;                     // planes per block of the staged / face-centric Phase1 (0: default)
     int p2mode = 0; // Phase2: 0 three sweep kernels, 1 one kernel for the three sweeps, 2 (FP32)
                     // one kernel for the three sweeps and the second Phase1, 3 (FP32) the same
                     // with TMA tensor copies

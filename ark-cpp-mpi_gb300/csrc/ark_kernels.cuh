@@ -2231,14 +2231,19 @@ template <class T, int MODE> struct CellK {
 // (FP32); both for the two Phase1 modes of a step, other modes fall back to the one-cell
 // kernel; 1: k_phase1 (a block marches kTileK planes); 0: k_phase1_cell
 template <class T>
-void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st) {
+void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st, int kch_in) {
     if (mode & P1_NUT) {
         launch_phase1_nut<T>(S, src, dst, fcur, mode, dim3(tiles_x(S.g), tiles_y(S.g), S.g.C3), st);
         return;
     }
     if constexpr (std::is_same<T, double>::value) {
         if (march == 3) {
-            const int kch = stg::staged_chunk(S.g);
+            // default planes per block: about nine waves of three blocks per SM (at 256x128x128:
+            // 4 planes, Phase1 + stress 1.208 -> 1.178 ms and second Phase1 0.758 -> 0.739 ms
+            // against 8; 2, 3, 6 and 12 planes measured between)
+            const long long cols = (long long)((S.g.C1 + fcs::SX - 1) / fcs::SX) * ((S.g.C2 + fcs::SY - 1) / fcs::SY);
+            const int kdef = (int)std::max(2LL, std::min(64LL, (long long)S.g.C3 * cols / (152 * 3 * 9)));
+            const int kch = kch_in > 0 ? std::min(kch_in, S.g.C3) : kdef;
             const dim3 grid((S.g.C1 + fcs::SX - 1) / fcs::SX, (S.g.C2 + fcs::SY - 1) / fcs::SY, (S.g.C3 + kch - 1) / kch);
             const dim3 block(fcs::SX, fcs::SY);
             switch (mode) {
@@ -2260,21 +2265,21 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
         if (march == 2) {
             switch (mode) {
             case P1_STRESS | P1_FORCES | P1_RMAX:
-                stg::launch_staged<P1_STRESS | P1_FORCES | P1_RMAX>(S, src, dst, fcur, st);
+                stg::launch_staged<P1_STRESS | P1_FORCES | P1_RMAX>(S, src, dst, fcur, st, kch_in);
                 return;
             case P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX:
-                stg::launch_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(S, src, dst, fcur, st);
+                stg::launch_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(S, src, dst, fcur, st, kch_in);
                 return;
-            case P1_FORCES | P1_RSUM: stg::launch_staged<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st); return;
+            case P1_FORCES | P1_RSUM: stg::launch_staged<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st, kch_in); return;
             default: march = 0; break;
             }
         } else if (march == 4 || march == 5) { // TMA copies, 64 x 4 or 32 x 8 tiles
             constexpr int A = P1_STRESS | P1_FORCES | P1_RMAX, B = A | P1_BULK, C = P1_FORCES | P1_RSUM;
             const bool wide = march == 4;
             switch (mode) {
-            case A: wide ? stg::launch_staged_tma<A, 64, 4>(S, src, dst, fcur, st) : stg::launch_staged_tma<A, 32, 8>(S, src, dst, fcur, st); return;
-            case B: wide ? stg::launch_staged_tma<B, 64, 4>(S, src, dst, fcur, st) : stg::launch_staged_tma<B, 32, 8>(S, src, dst, fcur, st); return;
-            case C: wide ? stg::launch_staged_tma<C, 64, 4>(S, src, dst, fcur, st) : stg::launch_staged_tma<C, 32, 8>(S, src, dst, fcur, st); return;
+            case A: wide ? stg::launch_staged_tma<A, 64, 4>(S, src, dst, fcur, st, kch_in) : stg::launch_staged_tma<A, 32, 8>(S, src, dst, fcur, st, kch_in); return;
+            case B: wide ? stg::launch_staged_tma<B, 64, 4>(S, src, dst, fcur, st, kch_in) : stg::launch_staged_tma<B, 32, 8>(S, src, dst, fcur, st, kch_in); return;
+            case C: wide ? stg::launch_staged_tma<C, 64, 4>(S, src, dst, fcur, st, kch_in) : stg::launch_staged_tma<C, 32, 8>(S, src, dst, fcur, st, kch_in); return;
             default: march = 0; break;
             }
         }

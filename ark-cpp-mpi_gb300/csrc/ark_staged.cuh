@@ -522,8 +522,9 @@ __global__ void __launch_bounds__(NT, 2)
     phase1_staged_body<MODE>(S, src, dst, fcur, kch, bix_here(), sm, rt);
 }
 
-template <int MODE> inline void launch_staged(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st) {
-    const int kch = staged_chunk(S.g);
+// kch: planes per block (0: staged_chunk's choice)
+template <int MODE> inline void launch_staged(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st, int kch_in = 0) {
+    const int kch = kch_in > 0 ? (kch_in < S.g.C3 ? kch_in : S.g.C3) : staged_chunk(S.g);
     k_phase1_staged<MODE><<<staged_grid(S.g, kch), dim3(SX, SY), Layout<MODE>::SMEM, st>>>(S, src, dst, fcur, kch);
 }
 template <int MODE> inline void prepare_staged() {
@@ -867,15 +868,15 @@ template <int MODE, int TSX, int TSY> inline bool tma_args(TmaArgs &A, const Dev
     return encode_boxes(A, B, n);
 }
 
-// TSX x TSY tiles (64 x 4 or 32 x 8)
+// TSX x TSY tiles (64 x 4 or 32 x 8); kch: planes per block (0: tile_chunk's choice)
 template <int MODE, int TSX = 64, int TSY = 4>
-inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st) {
+inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fcur, cudaStream_t st, int kch_in = 0) {
     TmaArgs A;
     if (!tma_args<MODE, TSX, TSY>(A, S, src, fcur)) {
-        launch_staged<MODE>(S, src, dst, fcur, st);
+        launch_staged<MODE>(S, src, dst, fcur, st, kch_in);
         return;
     }
-    const int kch = tile_chunk<TSX, TSY>(S.g);
+    const int kch = kch_in > 0 ? (kch_in < S.g.C3 ? kch_in : S.g.C3) : tile_chunk<TSX, TSY>(S.g);
     k_phase1_tma<MODE, TSX, TSY><<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX * TSY + 32), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(
         S, A, src, dst, kch);
 }

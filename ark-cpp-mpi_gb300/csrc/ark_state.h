@@ -307,7 +307,9 @@ template <class T> struct Launch {
     static void wrap_con(const DevState<T> &S, int con, int with_ro, cudaStream_t st);
     // xlines: also the x ghosts (the one-kernel Phase2 forms read them; the x1 sweep does not)
     static void wrap_phase2(const DevState<T> &S, int con, int fcur, cudaStream_t st, int xlines = 0);
-    static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st);
+    // kch: planes per block of the staged and face-centric forms (0: their default)
+    static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st,
+                       int kch = 0);
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
     // x2/x3 sweeps: lines cut into balanced segments of at most `target` faces
