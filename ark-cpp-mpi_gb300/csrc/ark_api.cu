@@ -1335,7 +1335,8 @@ extern "C" {
 // Times the candidate kernel shapes on the live state (results do not depend on the shape)
 // one setting at a time: the shape of the Phase1 with stress, then of the second Phase1, then
 // the three sweeps separate or fused, then (separate) the x2/x3 sweep segment (8, 16, 32, 64
-// faces), the x1 sweep's lines per warp (1 to 4) and the staged Phase1's planes per block.
+// faces, and 12, 20, 24, 48), the x1 sweep's lines per warp (1 to 4) and the staged Phase1's
+// planes per block.
 // choice (may be NULL): {shape 1, shape 2, segment, microseconds per step, fused}.
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     if (int rc = check_ctx(ctx, true)) return rc;
@@ -1368,7 +1369,8 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     };
     if (ctx->x1_lines <= 0) ctx->x1_lines = x_lines_per_warp(ctx->g, !fp32);
     for (int which = 0; which < 6; ++which) {
-        const int segs[4] = {8, 16, 32, 64};
+        // segment lengths: the steps between also move the blocks' last wave
+        const int segs[8] = {8, 12, 16, 20, 24, 32, 48, 64};
         const int lines[4] = {1, 2, 3, 4}; // x1 sweep lines per warp
         // planes per block of the staged / face-centric Phase1 (0: the default rule); the count
         // sets how evenly the blocks fill the GPU's waves against the halo planes per block
@@ -1395,7 +1397,7 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         // size measured: left to ARK_PHASE2_FUSED=1, not tried here.
         const int p2cand[3] = {0, 2, 3};
         if (which == 2 && !fp32) continue;
-        const int ncand = which < 2 ? (fp32 ? 4 : 3) : which == 2 ? 3 : 4;
+        const int ncand = which < 2 ? (fp32 ? 4 : 3) : which == 2 ? 3 : which == 3 ? 8 : 4;
         int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : which == 3 ? ctx->seg_target : ctx->x1_lines;
         if (which >= 3 && ctx->p2mode) continue; // the one-kernel forms have no segments, no x1 sweep
         for (int c = 0; c < ncand; ++c) {

@@ -340,7 +340,7 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
  * marching, 2 staged in shared memory with cp.async copies (FP32), 3 face quantities computed
  * once (FP64), 4 staged with TMA tensor copies (FP32)), of the second Phase1, the Phase2 form
  * (FP32: three sweep kernels, or one kernel for the three sweeps and the second Phase1 with
- * cp.async or TMA copies), the x2/x3 sweeps' segment length (8, 16, 32, 64 faces), the x1
+ * cp.async or TMA copies), the x2/x3 sweeps' segment length (8 to 64 faces), the x1
  * sweep's lines per warp (1 to 4) and the staged / face-centric Phase1's planes per block, each
  * candidate timed three times (best kept).  The results do not depend on the shapes.  choice
  * (5 ints, may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step, Phase2
