@@ -664,6 +664,9 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     // Phase1 0.507 against 0.540); FP64 computes each face's quantities once (1.94 vs 2.37 ms
     // and 1.10 vs 1.18 ms one cell per thread at 256x128x128).  ark_autotune picks per grid.
     ctx->march[0] = params->precision == ARK_FP32 ? 4 : 3;
+    // x2/x3 segments: 20 faces for FP64 (0.531 / 0.508 -> 0.513 / 0.492 ms at 256x128x128 against
+    // 32), 16 for FP32 (what the autotuner picks at 512x256x256)
+    ctx->seg_target = params->precision == ARK_FP32 ? 16 : 20;
     ctx->march[1] = params->precision == ARK_FP32 ? 4 : 3;
     if (const char *e = std::getenv("ARK_PHASE1_MARCH")) { // "ab": a for Phase1 with stress, b without
         // 0: one cell per thread, 1: marching, 2: planes staged in shared memory (FP32 only),
