@@ -152,16 +152,23 @@ template <int MODE> constexpr int tma_ens_smem() {
                                                                                : stg::TLayout<MODE, 32, 8>::SMEM) +
            128;
 }
+// Work items are taken from a counter (*next, zeroed before the launch) rather than in a fixed
+// stride: the items differ in cost (chunk lengths, partial tiles), so the blocks finish together.
 template <int MODE>
 __global__ void __launch_bounds__(stg::NT, 2) kb_phase1_tma(const DS *__restrict__ inst, const MemberMaps *__restrict__ maps,
                                                             const __grid_constant__ TmaMetas<MODE> meta, WorkList W, int src,
-                                                            int dst, int fcur) {
+                                                            int dst, int fcur, int *next) {
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
     static_assert(stg::TLayout<MODE, 64, 4>::NS == stg::TLayout<MODE, 32, 8>::NS, "one ring depth for both tiles");
     extern __shared__ __align__(128) unsigned char sm_raw[];
     __shared__ __align__(8) unsigned long long bar[stg::TLayout<MODE>::NS];
+    __shared__ int item;
     unsigned char *const sm = stg::align128(sm_raw);
-    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+    for (;;) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) item = atomicAdd(next, 1);
+        __syncthreads();
+        const int b = item;
+        if (b >= W.total) break; // (block-uniform)
         const int q = find_member(W, b);
         const int extra = W.extra[q], narrow = extra >> 16, kch = extra & 0xFFFF;
         const MemberMaps *M = maps + 2 * q + narrow;
@@ -179,16 +186,27 @@ __global__ void __launch_bounds__(stg::NT, 2) kb_phase1_tma(const DS *__restrict
     }
 }
 
-__global__ void __launch_bounds__(128) kb_sweep_x(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
-    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+// The next work item of a block from the counter *next (zeroed before the launch); every thread
+// of the block calls it.
+__device__ __forceinline__ int next_item(int *next, int &slot) {
+    __syncthreads(); // every thread has read the previous item
+    if (threadIdx.x == 0 && threadIdx.y == 0) slot = atomicAdd(next, 1);
+    __syncthreads();
+    return slot;
+}
+
+__global__ void __launch_bounds__(128) kb_sweep_x(const DS *__restrict__ inst, WorkList W, int con, int fcur, int *next) {
+    __shared__ int slot;
+    for (int b = next_item(next, slot); b < W.total; b = next_item(next, slot)) {
         const int q = find_member(W, b);
         sweep_x_body<float>(inst[q], con, fcur, W.extra[q], decode(W, q, b));
     }
 }
 
 template <int AX>
-__global__ void __launch_bounds__(128, 5) kb_sweep_col(const DS *__restrict__ inst, WorkList W, int con, int fcur) {
-    for (int b = blockIdx.x; b < W.total; b += gridDim.x) {
+__global__ void __launch_bounds__(128, 5) kb_sweep_col(const DS *__restrict__ inst, WorkList W, int con, int fcur, int *next) {
+    __shared__ int slot;
+    for (int b = next_item(next, slot); b < W.total; b = next_item(next, slot)) {
         const int q = find_member(W, b);
         sweep_col_body<float, AX>(inst[q], con, fcur, W.extra[q], decode(W, q, b));
     }
@@ -233,6 +251,7 @@ struct ark_ensemble {
     int persist_staged = 1;    // the same for the staged Phase1 (2 blocks of 256 threads per SM)
     Shape shape = {5, 5, 32}; // staged Phase1 with TMA copies for both launches, 32 x 8 tiles on odd-32 widths
     MemberMaps *d_maps = nullptr;   // the members' tensor maps, [2 q + narrow] (null: the TMA form falls back)
+    int *d_next = nullptr;          // work counters: the two TMA Phase1 launches, the three sweeps (zeroed per step)
     stg::BoxMeta meta[2][2] = {};   // its boxes: [narrow][0 with the stress, 1 without]
     int con = 0, fcur = 0;
     bool parts_valid = false;
@@ -439,8 +458,8 @@ template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst,
         const int grid = std::max(1, std::min(E->total[kind], E->persist_staged));
         const int m = (MODE & P1_STRESS) ? 0 : 1;
         const TmaMetas<MODE> metas = {{E->meta[0][m], E->meta[1][m]}};
-        kb_phase1_tma<MODE><<<grid, dim3(stg::SX, stg::SY), tma_ens_smem<MODE>(), E->st>>>(E->d_inst, E->d_maps, metas,
-                                                                                           wl(E, kind), src, dst, fcur);
+        kb_phase1_tma<MODE><<<grid, dim3(stg::SX, stg::SY), tma_ens_smem<MODE>(), E->st>>>(
+            E->d_inst, E->d_maps, metas, wl(E, kind), src, dst, fcur, E->d_next + ((MODE & P1_STRESS) ? 0 : 1));
     } else if (march == 2 || march == 4 || march == 5) {
         const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
         kb_phase1_staged<MODE><<<grid, dim3(stg::SX, stg::SY), stg::Layout<MODE>::SMEM, E->st>>>(
@@ -483,6 +502,7 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     auto mark = [&](int q) {
         if (ev) cudaEventRecord(ev[q], E->st);
     };
+    cudaMemsetAsync(E->d_next, 0, 5 * sizeof(int), E->st);
     kb_finalize<<<E->n, 1024, 0, E->st>>>(E->d_inst, 1);
     mark(0);
     kb_wrap<<<grid_of(E, WL_WRAP), 128, 0, E->st>>>(E->d_inst, E->d_jobs + (size_t)y * E->n, wl(E, WL_WRAP));
@@ -493,11 +513,11 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     else
         launch_p1<P1_STRESS | P1_FORCES | P1_RMAX>(E, E->shape.march_a, y, x, fc);
     mark(2);
-    kb_sweep_x<<<grid_of(E, WL_SWEEPX), 128, 0, E->st>>>(E->d_inst, wl(E, WL_SWEEPX), y, fc);
+    kb_sweep_x<<<grid_of(E, WL_SWEEPX), 128, 0, E->st>>>(E->d_inst, wl(E, WL_SWEEPX), y, fc, E->d_next + 2);
     mark(3);
-    kb_sweep_col<1><<<grid_of(E, WL_COL1), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL1), y, fc);
+    kb_sweep_col<1><<<grid_of(E, WL_COL1), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL1), y, fc, E->d_next + 3);
     mark(4);
-    kb_sweep_col<2><<<grid_of(E, WL_COL2), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL2), y, fc);
+    kb_sweep_col<2><<<grid_of(E, WL_COL2), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL2), y, fc, E->d_next + 4);
     mark(5);
     launch_p1<P1_FORCES | P1_RSUM>(E, E->shape.march_b, x, y, fc ^ 1);
     mark(6);
@@ -620,7 +640,8 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
     E->persist = sms * std::max(per, 1) * 2;
     E->persist_staged = prepare_staged_kernels(sms);
     stg::encode_tiled(); // looked up here, outside any stream capture
-    if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get())) || (*status = build_maps(E.get())))
+    if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get())) || (*status = build_maps(E.get())) ||
+        (*status = ens_alloc(E.get(), &E->d_next, 5)))
         return nullptr;
     cudaEventCreate(&E->ev0);
     cudaEventCreate(&E->ev1);
