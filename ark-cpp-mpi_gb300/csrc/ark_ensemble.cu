@@ -155,13 +155,13 @@ template <int MODE> constexpr int tma_ens_smem() {
 // Work items are taken from a counter (*next, zeroed before the launch) rather than in a fixed
 // stride: the items differ in cost (chunk lengths, partial tiles), so the blocks finish together.
 template <int MODE>
-__global__ void __launch_bounds__(stg::NT, 2) kb_phase1_tma(const DS *__restrict__ inst, const MemberMaps *__restrict__ maps,
+__global__ void __launch_bounds__(stg::NT + 32, 2) kb_phase1_tma(const DS *__restrict__ inst, const MemberMaps *__restrict__ maps,
                                                             const __grid_constant__ TmaMetas<MODE> meta, WorkList W, int src,
                                                             int dst, int fcur, int *next) {
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
     static_assert(stg::TLayout<MODE, 64, 4>::NS == stg::TLayout<MODE, 32, 8>::NS, "one ring depth for both tiles");
     extern __shared__ __align__(128) unsigned char sm_raw[];
-    __shared__ __align__(8) unsigned long long bar[stg::TLayout<MODE>::NS];
+    __shared__ __align__(8) unsigned long long bar[2 * stg::TLayout<MODE>::NS + 1];
     __shared__ int item;
     unsigned char *const sm = stg::align128(sm_raw);
     for (;;) {
@@ -458,7 +458,7 @@ template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst,
         const int grid = std::max(1, std::min(E->total[kind], E->persist_staged));
         const int m = (MODE & P1_STRESS) ? 0 : 1;
         const TmaMetas<MODE> metas = {{E->meta[0][m], E->meta[1][m]}};
-        kb_phase1_tma<MODE><<<grid, dim3(stg::SX, stg::SY), tma_ens_smem<MODE>(), E->st>>>(
+        kb_phase1_tma<MODE><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(
             E->d_inst, E->d_maps, metas, wl(E, kind), src, dst, fcur, E->d_next + ((MODE & P1_STRESS) ? 0 : 1));
     } else if (march == 2 || march == 4 || march == 5) {
         const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
@@ -473,21 +473,21 @@ template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst,
 
 // The staged kernels' shared-memory limits (once per process) and their resident blocks per SM.
 int prepare_staged_kernels(int sms) {
-    auto one = [](auto kern, int smem) {
+    auto one = [](auto kern, int smem, int threads = stg::NT) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         int per = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, stg::NT, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem);
         return per;
     };
     int per = one(kb_phase1_staged<P1_STRESS | P1_FORCES | P1_RMAX>, stg::Layout<P1_STRESS | P1_FORCES | P1_RMAX>::SMEM);
     per = std::min(per, one(kb_phase1_staged<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
                             stg::Layout<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>::SMEM));
     per = std::min(per, one(kb_phase1_staged<P1_FORCES | P1_RSUM>, stg::Layout<P1_FORCES | P1_RSUM>::SMEM));
-    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_RMAX>, tma_ens_smem<P1_STRESS | P1_FORCES | P1_RMAX>()));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_RMAX>, tma_ens_smem<P1_STRESS | P1_FORCES | P1_RMAX>(), stg::NT + 32));
     per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
-                            tma_ens_smem<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>()));
-    per = std::min(per, one(kb_phase1_tma<P1_FORCES | P1_RSUM>, tma_ens_smem<P1_FORCES | P1_RSUM>()));
+                            tma_ens_smem<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(), stg::NT + 32));
+    per = std::min(per, one(kb_phase1_tma<P1_FORCES | P1_RSUM>, tma_ens_smem<P1_FORCES | P1_RSUM>(), stg::NT + 32));
     return sms * std::max(per, 1);
 }
 

@@ -591,105 +591,8 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
 }
 
 // One block's work in the staged Phase1 with TMA copies: tile (bx.x, bx.y) of TSX x TSY columns,
-// planes of chunk bx.z (kch planes).  Thread 0 issues a plane's boxes into its stage (NS
-// stages, one mbarrier each in bar); every thread waits for the planes it reads on their
-// mbarriers.  Same plane order and ring as the cp.async form: at plane k, once plane k + 1 has
-// landed and every thread is past plane k - 1, the slot of the plane no longer needed takes
-// the next plane.  map(q) is box q's tensor map (global maps are fenced for the tensor-map
-// proxy first when fence_maps is set).  A wait that does not end within half a second sets
-// STATUS_STAGING, and the block lets its copies in flight land (again with a limit) and
-// leaves.  Every thread calls it; it ends with no copy in flight and the mbarriers
-// invalidated, so a persistent kernel may run it again.  (The ensemble's persistent kernel runs
-// this form: its work items are short, and the producer-warp form below measured slower there.)
-template <int MODE, int TSX, int TSY, class Maps>
-__device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
-                                                int src, int dst, int kch, const BIx &bx, unsigned char *sm,
-                                                unsigned long long *bar) {
-    using L = TLayout<MODE, TSX, TSY>;
-    using T = float;
-    constexpr bool STRESS = L::STRESS;
-    constexpr int NS = L::NS, SX = TSX, SY = TSY, NT = TSX * TSY;
-    constexpr unsigned long long kLimitNs = 500000000ull;
-    const Geom g = S.g;
-    // the thread's tile column from its linear index (the ensemble launches 64 x 4 blocks for
-    // both tile shapes)
-    const int t = threadIdx.y * blockDim.x + threadIdx.x, tx = t % SX, ty = t / SX;
-    const int i = bx.x * SX + tx + 1, j = bx.y * SY + ty + 1;
-    const int x0 = bx.x * SX, j0 = bx.y * SY + 1;
-    const int k0 = bx.z * kch + 1;
-    const int k1 = k0 + kch - 1 < g.C3 ? k0 + kch - 1 : g.C3;
-    const int pfirst = STRESS ? k0 - 1 : k0, plast = k1 + 1;
-    const unsigned sbase = smem_u32(sm);
-    auto bar_of = [&](int p) { return smem_u32(&bar[(p - pfirst) % NS]); };
-    auto parity_of = [&](int p) { return (unsigned)(((p - pfirst) / NS) & 1); };
-    auto issue = [&](int p) { // thread 0
-        const unsigned kind = p < k0 ? DOWN : (p > k1 ? TOP : MID);
-        const unsigned to = sbase + (unsigned)(((p - pfirst) % NS) * L::STAGE), b = bar_of(p);
-        mbar_expect_tx(b, A.bytes[kind]);
-        for (int q = 0; q < A.n; ++q)
-            if (A.when[q] & kind) tma_load_4d(to + A.dst[q], map(q), x0, j0 + A.row0[q], p, 0, b);
-    };
-    int issued = pfirst - 1; // thread 0: the last plane issued
-    if (t == 0) {
-        if (fence_maps)
-            for (int q = 0; q < A.n; ++q) fence_tensormap(map(q));
-        for (int q = 0; q < NS; ++q) mbar_init(smem_u32(&bar[q]), 1);
-        fence_mbar_init();
-        fence_proxy_async();
-        for (int p = pfirst; p < pfirst + NS - 1 && p <= plast; ++p) {
-            issue(p);
-            issued = p;
-        }
-    }
-    __syncthreads();
-
-    const K<T> &kk = kconst<T>(S.k);
-    const T dt = sc_dt<T>(S.sc);
-    const T G1 = (MODE & P1_BULK) ? sc_G<T>(S.sc) : (T)0;
-    const bool valid = i <= g.C1 && j <= g.C2;
-    unsigned long long m0 = 0, m1 = 0, m2 = 0;
-    long long rsum = 0;
-    bool failed = false;
-    for (int k = k0; k <= k1; ++k) {
-        bool ok = true;
-        if (k == k0) {
-            if (STRESS) ok = mbar_wait(bar_of(k - 1), parity_of(k - 1), kLimitNs);
-            ok = ok && mbar_wait(bar_of(k), parity_of(k), kLimitNs);
-        }
-        ok = ok && mbar_wait(bar_of(k + 1), parity_of(k + 1), kLimitNs);
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        if (t == 0) {
-            const int pn = k + NS - (STRESS ? 2 : 1);
-            if (pn <= plast) {
-                fence_proxy_async();
-                issue(pn);
-                issued = pn;
-            }
-        }
-        if (valid) {
-            const unsigned char *sk = sm + ((k - pfirst) % NS) * L::STAGE;
-            const unsigned char *su = sm + ((k + 1 - pfirst) % NS) * L::STAGE;
-            const unsigned char *sd = STRESS ? sm + ((k - 1 - pfirst) % NS) * L::STAGE : sk;
-            staged_cell<MODE, L>(S, dst, sd, sk, su, i, j, k, tx, ty, kk, dt, G1, m0, m1, m2, rsum);
-        }
-    }
-    if (failed && t == 0) {
-        atomicOr(&S.sc->status, STATUS_STAGING);
-        // the last NS planes issued hold each stage's newest phase
-        for (int p = issued - NS + 1 > pfirst ? issued - NS + 1 : pfirst; p <= issued; ++p)
-            mbar_wait(bar_of(p), parity_of(p), kLimitNs);
-    }
-    __syncthreads();
-    if (t == 0)
-        for (int q = 0; q < NS; ++q) mbar_inval(smem_u32(&bar[q]));
-    if (MODE & (P1_RMAX | P1_RSUM)) tile_store<T, NT>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
-}
-
-// The same with a producer warp (the single-grid kernel): TSX * TSY consumer threads (one cell
-// column each) and one producer warp (threads TSX * TSY ..; its lane 0 works).  The producer issues a plane's
+// planes of chunk bx.z (kch planes), by TSX * TSY consumer threads (one cell column each) and
+// one producer warp (threads TSX * TSY ..; its lane 0 works).  The producer issues a plane's
 // boxes into its stage (NS stages) once every consumer warp has released the plane the slot
 // held; every consumer waits for the planes it reads on the stage's "full" mbarrier and each
 // consumer warp, done with a plane, arrives on the stage's "empty" mbarrier.  No block-wide
@@ -702,7 +605,7 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
 // leaves.  Every thread calls it; it ends with no copy in flight and the mbarriers
 // invalidated, so a persistent kernel may run it again.
 template <int MODE, int TSX, int TSY, class Maps>
-__device__ __forceinline__ void phase1_tma_body_pw(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
+__device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
                                                 int src, int dst, int kch, const BIx &bx, unsigned char *sm,
                                                 unsigned long long *bar) {
     using L = TLayout<MODE, TSX, TSY>;
@@ -809,7 +712,7 @@ __global__ void __launch_bounds__(TSX *TSY + 32, 2)
     extern __shared__ __align__(128) unsigned char sm_raw[];
     __shared__ __align__(8) unsigned long long bar[2 * TLayout<MODE, TSX, TSY>::NS + 1];
     auto map = [&](int q) { return &A.map[q]; };
-    phase1_tma_body_pw<MODE, TSX, TSY>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar);
+    phase1_tma_body<MODE, TSX, TSY>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar);
 }
 
 // cuTensorMapEncodeTiled through the runtime's entry-point lookup (no link to libcuda)
