@@ -1377,7 +1377,7 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         const int lines[4] = {1, 2, 3, 4}; // x1 sweep lines per warp
         // planes per block of the staged / face-centric Phase1 (0: the default rule); the count
         // sets how evenly the blocks fill the GPU's waves against the halo planes per block
-        const int chunks[8] = {0, 2, 4, 6, 8, 16, 32, 48};
+        const int chunks[16] = {0, 2, 3, 4, 6, 8, 12, 16, 22, 24, 29, 32, 37, 43, 48, 64};
         if (which == 5) {
             const bool staged = (ctx->march[0] >= 2 || ctx->march[1] >= 2);
             if (!staged) continue;
