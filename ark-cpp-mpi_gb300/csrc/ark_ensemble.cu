@@ -241,6 +241,8 @@ struct ark_ensemble {
     std::vector<std::vector<double>> cond_host;
     DS *d_inst = nullptr;
     cudaStream_t st = nullptr;
+    cudaStream_t fill = nullptr; // the captured step's ghost fill, beside dt
+    cudaEvent_t fill_fork = nullptr, fill_join = nullptr;
     double *stage = nullptr; // double staging buffer (largest member)
     // work lists: device arrays, rebuilt when the shape changes
     int4 *d_info[WL_COUNT] = {};
@@ -503,10 +505,19 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
         if (ev) cudaEventRecord(ev[q], E->st);
     };
     cudaMemsetAsync(E->d_next, 0, 5 * sizeof(int), E->st);
-    kb_finalize<<<E->n, 1024, 0, E->st>>>(E->d_inst, 1);
-    mark(0);
-    kb_wrap<<<grid_of(E, WL_WRAP), 128, 0, E->st>>>(E->d_inst, E->d_jobs + (size_t)y * E->n, wl(E, WL_WRAP));
-    mark(1);
+    if (!ev) { // captured: the ghost fill beside dt (independent; Phase1 waits for both)
+        cudaEventRecord(E->fill_fork, E->st);
+        cudaStreamWaitEvent(E->fill, E->fill_fork, 0);
+        kb_wrap<<<grid_of(E, WL_WRAP), 128, 0, E->fill>>>(E->d_inst, E->d_jobs + (size_t)y * E->n, wl(E, WL_WRAP));
+        cudaEventRecord(E->fill_join, E->fill);
+        kb_finalize<<<E->n, 1024, 0, E->st>>>(E->d_inst, 1);
+        cudaStreamWaitEvent(E->st, E->fill_join, 0);
+    } else { // timed one launch after the other
+        kb_finalize<<<E->n, 1024, 0, E->st>>>(E->d_inst, 1);
+        mark(0);
+        kb_wrap<<<grid_of(E, WL_WRAP), 128, 0, E->st>>>(E->d_inst, E->d_jobs + (size_t)y * E->n, wl(E, WL_WRAP));
+        mark(1);
+    }
     // every member of an ensemble runs the bulk forcing or none does (checked at creation)
     if (E->K[0].forcing)
         launch_p1<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(E, E->shape.march_a, y, x, fc);
@@ -630,7 +641,10 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
         return nullptr;
     }
     if ((*status = ens_alloc(E.get(), &E->stage, maxf))) return nullptr;
-    if (cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&E->fill, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->fill_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->fill_join, cudaEventDisableTiming) != cudaSuccess) {
         *status = efail(ARK_ERR_CUDA, "stream creation failed");
         return nullptr;
     }
@@ -657,6 +671,12 @@ int ark_ensemble_destroy(ark_ensemble *E) {
     if (E->ev0) cudaEventDestroy(E->ev0);
     if (E->ev1) cudaEventDestroy(E->ev1);
     if (E->st) cudaStreamDestroy(E->st);
+    if (E->fill) {
+        cudaStreamSynchronize(E->fill);
+        cudaStreamDestroy(E->fill);
+    }
+    if (E->fill_fork) cudaEventDestroy(E->fill_fork);
+    if (E->fill_join) cudaEventDestroy(E->fill_join);
     delete E;
     return ARK_OK;
 }
