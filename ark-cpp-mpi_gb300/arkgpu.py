@@ -443,6 +443,7 @@ class Context:
         c = (ctypes.c_int * 5)()
         self._call("ark_autotune", int(steps_per_candidate), c)
         # phase2_form: 0 three sweep kernels, 1 one sweep kernel, 2 sweeps + second Phase1 in one kernel
+        # (3: the same with TMA copies), 4 the x1 sweep folded into Phase1 + stress
         return {"phase1_stress": c[0], "phase1": c[1], "segment": c[2], "us_per_step": c[3], "phase2_form": c[4]}
 
     def set_closure(self, mlp, u_tau=0.0):

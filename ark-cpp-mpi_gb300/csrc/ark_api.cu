@@ -211,6 +211,7 @@ __global__ void k_condition_flags(const double *__restrict__ cond, uint8_t *__re
 template <class T> struct EngineT : Engine {
     ark_ctx *ctx;
     DevState<T> S;
+    XSeams seams = {};   // FP32: the folded x1 sweep's tile seams (Phase2 form 4)
     std::vector<void *> allocs;
 
     explicit EngineT(ark_ctx *c) : ctx(c) { std::memset(&S, 0, sizeof(S)); }
@@ -244,8 +245,18 @@ template <class T> struct EngineT : Engine {
         const size_t nc = (size_t)S.g.ncell(), nf = (size_t)S.g.nface();
         int rc = 0;
         for (int l = 0; l < 2; ++l) rc |= get_block({&S.lv[l].ro, &S.lv[l].u1, &S.lv[l].u2, &S.lv[l].u3}, 4, nc);
-        if (Storage<T>::deviation) // FP32: the level the one-kernel Phase2 + second Phase1 writes
+        if (Storage<T>::deviation) { // FP32: the level the one-kernel Phase2 + second Phase1 writes
             rc |= get_block({&S.spare.ro, &S.spare.u1, &S.spare.u2, &S.spare.u3}, 4, nc);
+            // the seam arrays of Phase1 + stress with the x1 sweep folded in (any tile width)
+            const size_t ns = (size_t)seam_slots(S.g, 32);
+            float *sb = nullptr;
+            rc |= get(&sb, 18 * ns);
+            if (sb) {
+                for (int q = 0; q < 8; ++q) seams.b[q] = sb + q * ns;
+                for (int q = 0; q < 10; ++q) seams.a[q] = sb + (8 + q) * ns;
+                seams.n = (int)ns;
+            }
+        }
         rc |= get_block({&S.f[0], &S.f[1], &S.f[2], nullptr}, 3, nc);
         for (int gen = 0; gen < 2; ++gen)
             for (int d = 0; d < 3; ++d) {
@@ -427,7 +438,7 @@ template <class T> struct EngineT : Engine {
         // positions from the cells and faces they stand for (x1: xcell; x3: zcell, unless the
         // z ghosts are a slab's halo), so with them the Phase2 ghost fill has nothing to do and
         // the Con level's density needs no ghosts
-        const int xg = ctx->p2mode != 0 ? 1 : 0;
+        const int xg = ctx->p2mode >= 1 && ctx->p2mode <= 3 ? 1 : 0;
         const bool nofill = skip_phase2_fill();
         if (!ev) {
             // captured: the ghost fill (the "Con" level's ghosts) beside dt (the partial slots
@@ -445,7 +456,13 @@ template <class T> struct EngineT : Engine {
             mark();
         }
         if (ctx->closure_net) cudaStreamWaitEvent(st, ctx->join, 0);
-        Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st, ctx->p1_chunk);
+        // Phase2 form 4: the x1 sweep folded into Phase1 + stress (TMA-staged FP32 shapes; the
+        // seam kernel takes the x1 sweep's launch), else Phase1 + stress alone (should the folded
+        // form be unavailable, the x1 sweep follows in the same timed slot)
+        const bool fold = folds_x1();
+        const bool xs = fold && Launch<T>::phase1_sweep_x(S, y, x, fcur, mode, ctx->march[0], st, ctx->p1_chunk, seams);
+        if (!xs) Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st, ctx->p1_chunk);
+        if (fold && !xs) Launch<T>::sweep(S, y, fcur, 0, st, ctx->seg_target, ctx->x1_lines);
         mark();
         if (!nofill) {
             Launch<T>::wrap_phase2(S, y, fcur, st, xg);
@@ -468,7 +485,8 @@ template <class T> struct EngineT : Engine {
             for (int ax = 0; ax < 3; ++ax) mark();
         } else {
             for (int ax = 0; ax < 3; ++ax) {
-                Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
+                if (ax == 0 && xs) Launch<T>::sweep_x_seams(S, y, fcur, seams, st);
+                else if (ax > 0 || !fold) Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
                 mark();
             }
         }
@@ -492,13 +510,20 @@ template <class T> struct EngineT : Engine {
     DevScalars *scalars() override { return S.sc; }
     uint8_t *flags() override { return S.flags; }
     bool use_step2() const { return (ctx->p2mode == 2 || ctx->p2mode == 3) && S.spare.ro; }
-    // the three sweep kernels of a context whose z ghosts are its own: no Phase2 ghost fill
-    bool skip_phase2_fill() const { return ctx->p2mode == 0 && !S.k.ext_z; }
+    // the three sweep kernels (or the x1 sweep folded into Phase1) of a context whose z ghosts
+    // are its own: no Phase2 ghost fill
+    bool skip_phase2_fill() const { return (ctx->p2mode == 0 || ctx->p2mode == 4) && !S.k.ext_z; }
+    // Phase2 form 4 where the Phase1 shape allows it (FP32, TMA-staged Phase1 + stress)
+    bool folds_x1() const {
+        return ctx->p2mode == 4 && seams.b[0] && ctx->march[0] >= 4 && ctx->march[0] <= 6 && !ctx->closure_net;
+    }
     int step_launches() override { return use_step2() ? 5 : skip_phase2_fill() ? kNumStepKernels - 1 : kNumStepKernels; }
     const char *step_kernel_name(int q) override {
         if (q < 0 || q >= step_launches()) return "";
         if (skip_phase2_fill() && q >= 3) ++q; // no wrap_phase2
-        return use_step2() && q == 4 ? "phase2_phase1_forces" : kStepKernels[q];
+        if (use_step2() && q == 4) return "phase2_phase1_forces";
+        if (folds_x1() && (q == 2 || q == 4)) return q == 2 ? "phase1_stress_sweep_x1" : "sweep_x1_seams";
+        return kStepKernels[q];
     }
     void after_step(int con) override {
         if (use_step2()) std::swap(S.lv[con ^ 1], S.spare);
@@ -664,6 +689,14 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     // Phase1 0.507 against 0.540); FP64 computes each face's quantities once (1.94 vs 2.37 ms
     // and 1.10 vs 1.18 ms one cell per thread at 256x128x128).  ark_autotune picks per grid.
     ctx->march[0] = params->precision == ARK_FP32 ? 4 : 3;
+    if (params->precision == ARK_FP32) {
+        // FP32: the x1 sweep folded into Phase1 + stress (Phase2 form 4), on 128 x 2 tiles where
+        // lines are long enough to fill them (a tile seam every 128 cells): at 512x256x256 the
+        // step takes 2.140 ms against 2.209 with the separate x1 sweep (Phase1 + stress and x1
+        // sweep 0.835 + seams 0.053 ms against 0.538 + 0.421; on 64 x 4 tiles 0.818 + 0.082)
+        ctx->p2mode = 4;
+        if (params->n1_cells >= 256) ctx->march[0] = 6;
+    }
     // x2/x3 segments: 20 faces for FP64 (0.531 / 0.508 -> 0.513 / 0.492 ms at 256x128x128 against
     // 32), 16 for FP32 (what the autotuner picks at 512x256x256)
     ctx->seg_target = params->precision == ARK_FP32 ? 16 : 20;
@@ -671,15 +704,15 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     if (const char *e = std::getenv("ARK_PHASE1_MARCH")) { // "ab": a for Phase1 with stress, b without
         // 0: one cell per thread, 1: marching, 2: planes staged in shared memory (FP32 only),
         // 3: face quantities computed once (FP64 only), 4: staged with TMA copies (FP32 only),
-        // 5: the same on 32 x 8 tiles
+        // 5: the same on 32 x 8 tiles, 6: on 128 x 2 tiles
         auto ok = [&](char ch) {
-            return ch >= '0' && ch <= '1' ? true : (params->precision == ARK_FP32 ? ch == '2' || ch == '4' || ch == '5' : ch == '3');
+            return ch >= '0' && ch <= '1' ? true : (params->precision == ARK_FP32 ? ch == '2' || (ch >= '4' && ch <= '6') : ch == '3');
         };
         if (ok(e[0])) ctx->march[0] = e[0] - '0';
         if (e[0] && ok(e[1])) ctx->march[1] = e[1] - '0';
     }
     if (const char *e = std::getenv("ARK_PHASE2_FUSED"))
-        if (e[0] >= '0' && e[0] <= '3' && (e[0] < '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
+        if (e[0] >= '0' && e[0] <= '4' && (e[0] < '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
     Launch<float>::prepare();
     Launch<double>::prepare();
     cudaEventCreate(&ctx->ev0);
@@ -1347,7 +1380,7 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
     // Phase1 shapes: one cell per thread, marching, and the precision's own (staged with
     // cp.async or TMA copies for FP32, face-centric for FP64)
     const bool fp32 = ctx->P.precision == ARK_FP32;
-    const int shapes[4] = {0, 1, fp32 ? 2 : 3, 4};
+    const int shapes[5] = {0, 1, fp32 ? 2 : 3, 4, 6};
     // best of three timings of steps_per_candidate steps each
     auto measure = [&](double *us) -> int {
         ARK_CUDA(cudaStreamSynchronize(ctx->st));
@@ -1396,13 +1429,15 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
             continue;
         }
         // Phase2 forms: the three sweep kernels, or (FP32) one kernel for the sweeps and the
-        // second Phase1.  The one-kernel Phase2 alone (mode 1) is correct but slower at every
-        // size measured: left to ARK_PHASE2_FUSED=1, not tried here.
-        const int p2cand[3] = {0, 2, 3};
+        // second Phase1, or (FP32) the x1 sweep folded into Phase1 + stress.  The one-kernel
+        // Phase2 alone (mode 1) is correct but slower at every size measured: left to
+        // ARK_PHASE2_FUSED=1, not tried here.
+        const int p2cand[4] = {0, 2, 3, 4};
         if (which == 2 && !fp32) continue;
-        const int ncand = which < 2 ? (fp32 ? 4 : 3) : which == 2 ? 3 : which == 3 ? 8 : 4;
+        const int ncand = which < 2 ? (fp32 ? 5 : 3) : which == 2 ? 4 : which == 3 ? 8 : 4;
         int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : which == 3 ? ctx->seg_target : ctx->x1_lines;
-        if (which >= 3 && ctx->p2mode) continue; // the one-kernel forms have no segments, no x1 sweep
+        // the one-kernel forms have no segments and no x1 sweep; the folded x1 sweep no x1 sweep
+        if (which >= 3 && ctx->p2mode != 0 && !(which == 3 && ctx->p2mode == 4)) continue;
         for (int c = 0; c < ncand; ++c) {
             const int v = which < 2 ? shapes[c] : which == 2 ? p2cand[c] : which == 3 ? segs[c] : lines[c];
             if (v == keep) continue;

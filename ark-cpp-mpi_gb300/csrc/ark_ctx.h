@@ -97,7 +97,9 @@ struct ark_ctx {
     int p1_chunk = 0;                     // planes per block of the staged / face-centric Phase1 (0: default)
     int p2mode = 0; // Phase2: 0 three sweep kernels, 1 one kernel for the three sweeps, 2 (FP32)
                     // one kernel for the three sweeps and the second Phase1, 3 (FP32) the same
-                    // with TMA tensor copies
+                    // with TMA tensor copies, 4 (FP32, TMA-staged Phase1 + stress) the x1 sweep
+                    // folded into Phase1 + stress (a seam kernel finishes it), then the x2 and
+                    // x3 sweeps
     // output streaming: two device and two pinned host slab buffers of io_cap doubles
     double *io_dev[2] = {nullptr, nullptr};
     double *io_host[2] = {nullptr, nullptr};

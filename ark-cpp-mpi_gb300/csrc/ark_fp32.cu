@@ -186,8 +186,9 @@ template <class Fail> void check_boxes(const stg::TmaBox *B, int n, int stage, F
     }
 }
 // The boxes of kind `kind` for plane p of the tile at column x0, row j0, byte by byte as the
-// copy engine lays them out: M[stage byte] = fake source address (-2: zero fill past the last
-// row); fail(what, value).
+// copy engine lays them out: M[stage byte] = fake source address (-2: zero fill past the end of
+// a row or past the last row: a 128-wide tile's box may reach past a narrow grid's rows, and
+// the reads below then show that no thread uses those bytes); fail(what, value).
 template <class Fail>
 void expand_boxes(const stg::TmaBox *B, int n, unsigned kind, int x0, int j0, int p, std::vector<long long> &M, Fail &&fail) {
     const long long stage = (long long)M.size();
@@ -197,7 +198,7 @@ void expand_boxes(const stg::TmaBox *B, int n, unsigned kind, int x0, int j0, in
         if (!(x.when & kind)) continue;
         if (p < 0 || p >= x.dim[2]) fail("plane outside its array", q);
         if (j0 + x.row0 < 0) fail("box starts at a negative row", q);
-        if (x0 + x.box[0] > x.dim[0]) fail("box leaves its row", q);
+        if (x0 >= x.dim[0]) fail("box starts past the end of its row", q);
         for (int a = 0; a < x.box[3]; ++a)
             for (int r = 0; r < x.box[1]; ++r)
                 for (int e = 0; e < x.box[0]; ++e) {
@@ -208,7 +209,7 @@ void expand_boxes(const stg::TmaBox *B, int n, unsigned kind, int x0, int j0, in
                     for (int c = 0; c < x.elem; ++c) {
                         if (dst + c >= stage) continue;
                         if (M[dst + c] != -1) fail("two boxes into one byte", dst + c);
-                        M[dst + c] = y < x.dim[1] ? src + c : -2;
+                        M[dst + c] = y < x.dim[1] && x0 + e < x.dim[0] ? src + c : -2;
                     }
                 }
     }
@@ -501,13 +502,17 @@ int staging_plan_check(int C1, int C2, int C3, int kch_in, char *msg, int cap) {
     td.run(kch);
     TmaCheck<P1_FORCES | P1_RSUM, 32, 8> te(g);
     te.run(kch);
+    TmaCheck<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 128, 2> tf(g);
+    tf.run(kch);
+    TmaCheck<P1_FORCES | P1_RSUM, 128, 2> th(g);
+    th.run(kch);
     char m2[256] = {0};
     const int d = step2_plan_check(C1, C2, C3, kch_in, m2, (int)sizeof m2);
     std::string e = std::string(m2);
-    for (const std::string *x : {&te.err, &td.err, &tc.err, &tb.err, &ta.err, &c.err, &b.err, &a.err})
+    for (const std::string *x : {&th.err, &tf.err, &te.err, &td.err, &tc.err, &tb.err, &ta.err, &c.err, &b.err, &a.err})
         if (!x->empty()) e = *x;
     if (msg && cap > 0) std::snprintf(msg, (size_t)cap, "%s", e.c_str());
-    return a.bad + b.bad + c.bad + ta.bad + tb.bad + tc.bad + td.bad + te.bad + d;
+    return a.bad + b.bad + c.bad + ta.bad + tb.bad + tc.bad + td.bad + te.bad + tf.bad + th.bad + d;
 }
 
 } // namespace ark

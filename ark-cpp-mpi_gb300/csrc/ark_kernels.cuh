@@ -1469,15 +1469,31 @@ template <class T> struct FaceOut {
 // The new values of one face: pressure, density, normal and tangential velocities.
 template <class T> struct FaceNew { T p, ro, n, a, b; };
 
+// The half-step values (tangential velocities nA / nB, density ro) of the cell behind (0) and
+// ahead (1) of a face that the rarer branches of a face update read: from the level in memory
+// (the sweeps, loaded only in those branches) or from registers (NVals).
+template <class T> struct NAt {
+    const NCell<T> &N;
+    int cb, cf;
+    __device__ __forceinline__ T nA(int ahead) const { return N.nA[ahead ? cf : cb]; }
+    __device__ __forceinline__ T nB(int ahead) const { return N.nB[ahead ? cf : cb]; }
+    __device__ __forceinline__ T ro(int ahead) const { return N.ro[ahead ? cf : cb]; }
+};
+template <class T> struct NVals {
+    T a[2], b[2], r[2];
+    __device__ __forceinline__ T nA(int ahead) const { return a[ahead]; }
+    __device__ __forceinline__ T nB(int ahead) const { return b[ahead]; }
+    __device__ __forceinline__ T ro(int ahead) const { return r[ahead]; }
+};
+
 // Face update (main.cpp:1920-2008).  prev = the cell behind the face (index f-1), cur = the
-// cell ahead (index f); cb/cf index those cells; flb/flf their flags and ucb/ucf their
-// half-step normal velocities.  uA_old/uB_old: the face's previous tangential velocities.
-// WALL_A_FROM_N: the x2 sweep takes the tangential u1 from u2nCon in its wall branches
-// (main.cpp:2219, 2238).
-template <class T, bool WALL_A_FROM_N>
-__device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int cf, uint8_t flb, uint8_t flf, T ucb,
-                                                  T ucf, const Ext<T> &prev, const Ext<T> &cur, T uA_old, T uB_old,
-                                                  const SweepK<T> &q) {
+// cell ahead (index f); V gives those cells' half-step values for the rarer branches; flb/flf
+// their flags and ucb/ucf their half-step normal velocities.  uA_old/uB_old: the face's
+// previous tangential velocities.  WALL_A_FROM_N: the x2 sweep takes the tangential u1 from
+// u2nCon in its wall branches (main.cpp:2219, 2238).
+template <class T, bool WALL_A_FROM_N, class NV>
+__device__ __forceinline__ FaceNew<T> face_values_v(const NV &V, uint8_t flb, uint8_t flf, T ucb, T ucf, const Ext<T> &prev,
+                                                    const Ext<T> &cur, T uA_old, T uB_old, const SweepK<T> &q) {
     constexpr bool DEV = Storage<T>::deviation;
     T un, pn, ro_n, ua, ub;
     if ((flb & FL_LT) && (flf & FL_LT)) {
@@ -1500,8 +1516,8 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
                 ub = cur.bb;
             }
         } else {
-            ua = N.nA[cf] + N.nA[cb] - uA_old;
-            ub = N.nB[cf] + N.nB[cb] - uB_old;
+            ua = V.nA(1) + V.nA(0) - uA_old;
+            ub = V.nB(1) + V.nB(0) - uB_old;
         }
     } else {
         un = (T)0;
@@ -1513,10 +1529,10 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
                 ua = cur.ab;
                 ub = cur.bb;
             } else {
-                ro_n = N.ro[cf];
+                ro_n = V.ro(1);
                 pn = DEV ? ro_n * q.c2 : (ro_n - q.ro0) * q.c2;
-                ua = WALL_A_FROM_N ? ucf : N.nA[cf];
-                ub = N.nB[cf];
+                ua = WALL_A_FROM_N ? ucf : V.nA(1);
+                ub = V.nB(1);
             }
         } else if ((flb & FL_LT) && (flf & FL_GT)) {
             if (ge0(ucb)) {
@@ -1526,10 +1542,10 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
                 ua = prev.af;
                 ub = prev.bf;
             } else {
-                ro_n = N.ro[cb];
+                ro_n = V.ro(0);
                 pn = DEV ? ro_n * q.c2 : (ro_n - q.ro0) * q.c2;
-                ua = WALL_A_FROM_N ? ucb : N.nA[cb];
-                ub = N.nB[cb];
+                ua = WALL_A_FROM_N ? ucb : V.nA(0);
+                ub = V.nB(0);
             }
         } else {
             pn = (T)0;
@@ -1545,6 +1561,13 @@ __device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int
     v.a = ua;
     v.b = ub;
     return v;
+}
+// cb / cf index the cells behind and ahead in the half-step level N
+template <class T, bool WALL_A_FROM_N>
+__device__ __forceinline__ FaceNew<T> face_values(const NCell<T> &N, int cb, int cf, uint8_t flb, uint8_t flf, T ucb,
+                                                  T ucf, const Ext<T> &prev, const Ext<T> &cur, T uA_old, T uB_old,
+                                                  const SweepK<T> &q) {
+    return face_values_v<T, WALL_A_FROM_N>(NAt<T>{N, cb, cf}, flb, flf, ucb, ucf, prev, cur, uA_old, uB_old, q);
 }
 
 template <class T> __device__ __forceinline__ void face_store(const FaceOut<T> &W, int fc, const FaceNew<T> &v) {
@@ -1815,6 +1838,73 @@ template <class T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3)
     k_sweep_x(const __grid_constant__ DevState<T> S, int con, int fcur, int glines) {
     sweep_x_body<T>(S, con, fcur, glines, bix_here());
+}
+
+// The x faces that Phase1 + stress with the x1 sweep folded in leaves (stg::phase1_tma_body
+// with XS): per line (j, k), face b * tw + 1 of every tile seam b < nb = ceil(C1 / tw), between
+// the last cell of tile b - 1 and the first of tile b, and face C1 + 1.  Everything comes from
+// the seam arrays the tiles wrote.  On a periodic x axis the ghost positions stand for cells C1
+// (behind face 1) and 1 (ahead of face C1 + 1): their values are those cells' (slots nb and 0),
+// and so are their extrapolations when the old faces 1 and C1 + 1 agree bit for bit (as every
+// step leaves them: the two faces are one, updated from the same values); otherwise the ghost
+// position's extrapolation is computed here as k_sweep_x computes it, from the cell and the
+// faces it stands for (xcell, xface).  One thread per face, the seams of a line side by side.
+template <class T>
+__global__ void __launch_bounds__(256) k_sweep_x_seams(const __grid_constant__ DevState<T> S, int con, int fcur,
+                                                       const __grid_constant__ XSeams X) {
+    const Geom g = S.g;
+    const int rows = g.C2 * g.C3, nb = (g.C1 + X.tw - 1) / X.tw;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= rows * (nb + 1)) return;
+    const int row = id / (nb + 1), b = id - row * (nb + 1);
+    const int j = row % g.C2 + 1, k = row / g.C2 + 1;
+    const int s = b == nb ? g.C1 + 1 : b * X.tw + 1; // the face, between positions s - 1 and s
+    const bool px = S.k.periodic_x;
+    const int w = ARK_CK(seam_slot(g, X.tw, b, j, k), X.n);
+    // the slots of the cells behind and ahead (the cells the periodic ghost positions stand for)
+    const int wb = ARK_CK(px && b == 0 ? w + nb : w, X.n), wa = ARK_CK(px && b == nb ? w - nb : w, X.n);
+    Ext<T> prev = {}, cur = {};
+    prev.rf = X.b[0][wb];
+    prev.af = X.b[1][wb];
+    prev.bf = X.b[2][wb];
+    cur.qb = X.a[0][wa];
+    cur.ab = X.a[1][wa];
+    cur.bb = X.a[2][wa];
+    const SweepK<T> q = sweep_consts(S, 0);
+    if (px && (b == 0 || b == nb)) {
+        const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
+        const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k), f1 = ARK_CK(f0 + 1, R.nf), fe = ARK_CK(f0 + g.C1 + 1, R.nf);
+        auto same = [](T u, T v) { return __float_as_int(u) == __float_as_int(v); };
+        if (!(same(R.FN[f1], R.FN[fe]) && same(R.FA[f1], R.FA[fe]) && same(R.FB[f1], R.FB[fe]) && same(R.FP[f1], R.FP[fe]))) {
+            const bool lo = b == 0; // ghost position 0 (cell C1; faces 1 ahead, C1 behind) or C1 + 1
+            const int c = ARK_CK(c0 + (lo ? g.C1 : 1), R.nc);
+            const int ff = ARK_CK(f0 + (lo ? 1 : 2), R.nf), fb = ARK_CK(f0 + (lo ? g.C1 : g.C1 + 1), R.nf);
+            const Ext<T> e = extrapolate_rq<T, true>(face_rq(R.FN[ff], R.FP[ff], q), face_rq(R.FN[fb], R.FP[fb], q), R.nN[c],
+                                                     R.cN[c], R.FA[ff], R.FA[fb], R.nA[c], R.cA[c], R.FB[ff], R.FB[fb], R.nB[c],
+                                                     R.cB[c], R.nR[c], R.cR[c], q);
+            if (lo) {
+                prev.rf = e.rf;
+                prev.af = e.af;
+                prev.bf = e.bf;
+            } else {
+                cur.qb = e.qb;
+                cur.ab = e.ab;
+                cur.bb = e.bb;
+            }
+        }
+    }
+    NVals<T> V;
+    V.a[0] = X.b[4][wb];
+    V.b[0] = X.b[5][wb];
+    V.r[0] = X.b[6][wb];
+    V.a[1] = X.a[4][wa];
+    V.b[1] = X.a[5][wa];
+    V.r[1] = X.a[6][wa];
+    // the positions' own flags and the face's old tangential velocities: slot w's
+    const uint8_t flb = (uint8_t)__float_as_int(X.b[7][w]), flf = (uint8_t)__float_as_int(X.a[7][w]);
+    const FaceOut<T> W = sweep_out(S, fcur, 0);
+    face_store(W, ARK_CK(g.fi(s, j, k), W.nf),
+               face_values_v<T, false>(V, flb, flf, X.b[3][wb], X.a[3][wa], prev, cur, X.a[8][w], X.a[9][w], q));
 }
 
 // x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,
@@ -2273,13 +2363,18 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
             case P1_FORCES | P1_RSUM: stg::launch_staged<P1_FORCES | P1_RSUM>(S, src, dst, fcur, st, kch_in); return;
             default: march = 0; break;
             }
-        } else if (march == 4 || march == 5) { // TMA copies, 64 x 4 or 32 x 8 tiles
+        } else if (march >= 4 && march <= 6) { // TMA copies, 64 x 4, 32 x 8 or 128 x 2 tiles
             constexpr int A = P1_STRESS | P1_FORCES | P1_RMAX, B = A | P1_BULK, C = P1_FORCES | P1_RSUM;
-            const bool wide = march == 4;
+            auto shape = [&](auto m) {
+                constexpr int M = decltype(m)::value;
+                if (march == 4) stg::launch_staged_tma<M, 64, 4>(S, src, dst, fcur, st, kch_in);
+                else if (march == 5) stg::launch_staged_tma<M, 32, 8>(S, src, dst, fcur, st, kch_in);
+                else stg::launch_staged_tma<M, 128, 2>(S, src, dst, fcur, st, kch_in);
+            };
             switch (mode) {
-            case A: wide ? stg::launch_staged_tma<A, 64, 4>(S, src, dst, fcur, st, kch_in) : stg::launch_staged_tma<A, 32, 8>(S, src, dst, fcur, st, kch_in); return;
-            case B: wide ? stg::launch_staged_tma<B, 64, 4>(S, src, dst, fcur, st, kch_in) : stg::launch_staged_tma<B, 32, 8>(S, src, dst, fcur, st, kch_in); return;
-            case C: wide ? stg::launch_staged_tma<C, 64, 4>(S, src, dst, fcur, st, kch_in) : stg::launch_staged_tma<C, 32, 8>(S, src, dst, fcur, st, kch_in); return;
+            case A: shape(std::integral_constant<int, A>()); return;
+            case B: shape(std::integral_constant<int, B>()); return;
+            case C: shape(std::integral_constant<int, C>()); return;
             default: march = 0; break;
             }
         }
@@ -2289,6 +2384,33 @@ void Launch<T>::phase1(const DevState<T> &S, int src, int dst, int fcur, int mod
     else
         launch_phase1<T, CellK>(S, src, dst, fcur, mode, dim3(tiles_x(S.g), tiles_y(S.g), S.g.C3), st);
 }
+
+template <class T> void Launch<T>::sweep_x_seams(const DevState<T> &S, int con, int fcur, const XSeams &X, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        const long long n = seam_slots(S.g, X.tw);
+        k_sweep_x_seams<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(S, con, fcur, X);
+    }
+}
+
+template <class T>
+bool Launch<T>::phase1_sweep_x(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st, int kch,
+                               XSeams &X) {
+    if constexpr (std::is_same<T, float>::value) {
+        constexpr int A = P1_STRESS | P1_FORCES | P1_RMAX, B = A | P1_BULK;
+        if (march == 4) {
+            if (mode == A) return stg::launch_staged_tma_xs<A, 64, 4>(S, src, dst, fcur, X, st, kch);
+            if (mode == B) return stg::launch_staged_tma_xs<B, 64, 4>(S, src, dst, fcur, X, st, kch);
+        } else if (march == 5) {
+            if (mode == A) return stg::launch_staged_tma_xs<A, 32, 8>(S, src, dst, fcur, X, st, kch);
+            if (mode == B) return stg::launch_staged_tma_xs<B, 32, 8>(S, src, dst, fcur, X, st, kch);
+        } else if (march == 6) {
+            if (mode == A) return stg::launch_staged_tma_xs<A, 128, 2>(S, src, dst, fcur, X, st, kch);
+            if (mode == B) return stg::launch_staged_tma_xs<B, 128, 2>(S, src, dst, fcur, X, st, kch);
+        }
+    }
+    return false;
+}
+
 
 template <class T> void Launch<T>::prepare() {
     if constexpr (std::is_same<T, double>::value) {
@@ -2309,6 +2431,15 @@ template <class T> void Launch<T>::prepare() {
         stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 32, 8>();
         stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 32, 8>();
         stg::prepare_staged_tma<P1_FORCES | P1_RSUM, 32, 8>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 128, 2>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 128, 2>();
+        stg::prepare_staged_tma<P1_FORCES | P1_RSUM, 128, 2>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 128, 2, true>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 128, 2, true>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 64, 4, true>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 64, 4, true>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 32, 8, true>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 32, 8, true>();
         s2::prepare<float>();
     }
 }

@@ -258,6 +258,7 @@ ark_slabs *ark_slabs_create(const ark_params *params, int nslabs, int *status) {
         c->k = K;
         c->eng->set_consts(K);
         c->p2mode = 0; // the three sweep kernels (the one-kernel forms rotate levels per launch)
+        if (c->march[0] == 6) c->march[0] = 4; // 128 x 2 tiles pay off only with the x1 sweep folded in
         cudaStreamDestroy(c->st);
         c->st = G->st;
         c->eng->share_scalars(G->sc, G->part_max, G->part_sum);

@@ -300,14 +300,22 @@ __device__ __forceinline__ void cp16(unsigned dst, const void *src) {
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// A cell's values after Phase1: the half-step level written (ro_n, un), the level read (ro_c,
+// uc) and the flags (what the folded x1 sweep extrapolates from).
+struct XCell {
+    float ro_n, un[3], ro_c, uc[3];
+    uint8_t fl;
+};
+
 // One cell (i, j, k) of a staged Phase1 from the stages of planes k - 1 (sd, read with the
 // stress), k (sk) and k + 1 (su), offsets by the stage layout L; the thread's tile column (tx, ty).
-// The arithmetic of k_phase1_cell, in the same order.
+// The arithmetic of k_phase1_cell, in the same order.  xo (when given): the cell's values.
 template <int MODE, class L>
 __device__ __forceinline__ void staged_cell(const DevState<float> &S, int dst, const unsigned char *sd,
                                             const unsigned char *sk, const unsigned char *su, int i, int j, int k,
                                             int tx, int ty, const K<float> &kk, float dt, float G1, unsigned long long &m0,
-                                            unsigned long long &m1, unsigned long long &m2, long long &rsum) {
+                                            unsigned long long &m1, unsigned long long &m2, long long &rsum,
+                                            XCell *xo = nullptr) {
     using T = float;
     constexpr bool STRESS = L::STRESS;
     const Geom &g = S.g;
@@ -380,6 +388,16 @@ __device__ __forceinline__ void staged_cell(const DevState<float> &S, int dst, c
     S.lv[dst].u1[c] = ucn[0];
     S.lv[dst].u2[c] = ucn[1];
     S.lv[dst].u3[c] = ucn[2];
+    if (xo) {
+        xo->ro_n = ro_cn;
+        xo->ro_c = ro_c;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            xo->un[m] = ucn[m];
+            xo->uc[m] = uc[m];
+        }
+        xo->fl = fl;
+    }
     if (MODE & P1_RMAX) {
         const unsigned long long b0 = abs_key(ucn[0]), b1 = abs_key(ucn[1]), b2 = abs_key(ucn[2]);
         m0 = b0 > m0 ? b0 : m0;
@@ -604,14 +622,46 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
 // bounded wait each), and the block lets its copies in flight land (again with a limit) and
 // leaves.  Every thread calls it; it ends with no copy in flight and the mbarriers
 // invalidated, so a persistent kernel may run it again.
-template <int MODE, int TSX, int TSY, class Maps>
+//
+// XS (Phase1 + stress only): the x1 sweep folded in.  The x extrapolation of a cell needs its
+// half-step values (just computed), its old values and its two old x faces (staged), so per
+// plane every cell also extrapolates along x (main.cpp:1756-1873) and updates the x face below
+// it from the cell behind (main.cpp:1920-2008): the lane before, or for the first lane of a
+// tile row's second warp the last lane of the first, handed over through shared memory (xh: a
+// slot per plane of a ring of NS, completed on its own mbarrier with a bounded wait; the first
+// warp can run at most NS - 2 planes ahead of the second, since the stages it needs are only
+// refilled once the second has released them, so a slot is never rewritten before it was
+// read).  The faces at the tiles' seams (below a tile's first column, and face C1 + 1) are
+// left to k_sweep_x_seams: the tile's first and last cells write all that their side of such a
+// face needs into X (see XSeams).  Same arithmetic, same inputs, same bits as k_sweep_x.
+// One side of a seam face in X (q: X.b or X.a): the three extrapolated values, the cell's
+// half-step values and (fl) its flags.
+__device__ __forceinline__ void seam_put(float *const *q, int s, float e0, float e1, float e2, const XCell &c, bool fl) {
+    q[0][s] = e0;
+    q[1][s] = e1;
+    q[2][s] = e2;
+    q[3][s] = c.un[0];
+    q[4][s] = c.un[1];
+    q[5][s] = c.un[2];
+    q[6][s] = c.ro_n;
+    if (fl) q[7][s] = __int_as_float((int)c.fl);
+}
+template <int TSX, int TSY, int NS> struct XHand {
+    static constexpr int NH = TSX / 32 > 1 ? TSX / 32 - 1 : 1; // hand-overs per row
+    unsigned long long bar[TSY][NH][NS];
+    float v[TSY][NH][NS][8]; // rf, af, bf, u1, u2, u3, ro of the half-step level, flags
+};
+template <int MODE, int TSX, int TSY, bool XS = false, class Maps>
 __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
                                                 int src, int dst, int kch, const BIx &bx, unsigned char *sm,
-                                                unsigned long long *bar) {
+                                                unsigned long long *bar, int fcur = 0, const XSeams *X = nullptr,
+                                                XHand<TSX, TSY, TLayout<MODE, TSX, TSY>::NS> *xh = nullptr) {
     using L = TLayout<MODE, TSX, TSY>;
     using T = float;
     constexpr bool STRESS = L::STRESS;
     constexpr int NS = L::NS, SX = TSX, SY = TSY, NT = TSX * TSY;
+    constexpr int NW = TSX / 32; // warps per tile row
+    static_assert(!XS || (STRESS && TSX % 32 == 0), "the x1 sweep folds into Phase1 + stress, whole warps per row");
     constexpr unsigned long long kLimitNs = 500000000ull;
     const Geom g = S.g;
     const int t = threadIdx.y * blockDim.x + threadIdx.x, tx = t % SX, ty = t / SX;
@@ -633,6 +683,10 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
             mbar_init(smem_u32(&bar[q]), 1);
             mbar_init(smem_u32(&bar[NS + q]), NT / 32);
         }
+        if (XS && NW > 1)
+            for (int r = 0; r < SY; ++r)
+                for (int h = 0; h < NW - 1; ++h)
+                    for (int q = 0; q < NS; ++q) mbar_init(smem_u32(&xh->bar[r][h][q]), 1);
         *abort_flag = 0;
         fence_mbar_init();
         fence_proxy_async();
@@ -665,6 +719,12 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
         const T dt = sc_dt<T>(S.sc);
         const T G1 = (MODE & P1_BULK) ? sc_G<T>(S.sc) : (T)0;
         const bool valid = i <= g.C1 && j <= g.C2;
+        // the folded x1 sweep: its constants and output faces; the warp's place in the tile row
+        // and whether its first lane's face takes a hand-over (warp-uniform)
+        const SweepK<T> qx = sweep_consts(S, 0);
+        const FaceOut<T> WX = sweep_out(S, fcur, 0);
+        const int lane = t & 31, w = tx >> 5;
+        const bool takes = XS && NW > 1 && w > 0 && x0 + 32 * w + 1 <= g.C1 && j <= g.C2;
         for (int k = k0; k <= k1; ++k) {
             bool ok = true;
             if (k == k0) {
@@ -678,11 +738,103 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
                 failed = true;
                 break;
             }
+            const unsigned char *sk = sm + ((k - pfirst) % NS) * L::STAGE;
+            XCell xc = {};
             if (valid) {
-                const unsigned char *sk = sm + ((k - pfirst) % NS) * L::STAGE;
                 const unsigned char *su = sm + ((k + 1 - pfirst) % NS) * L::STAGE;
                 const unsigned char *sd = STRESS ? sm + ((k - 1 - pfirst) % NS) * L::STAGE : sk;
-                staged_cell<MODE, L>(S, dst, sd, sk, su, i, j, k, tx, ty, kk, dt, G1, m0, m1, m2, rsum);
+                staged_cell<MODE, L>(S, dst, sd, sk, su, i, j, k, tx, ty, kk, dt, G1, m0, m1, m2, rsum, XS ? &xc : nullptr);
+            }
+            if constexpr (XS) {
+                // the cell's x extrapolation (the x1 sweep's extrapolate, from the same values)
+                const T *fm = (const T *)sk;
+                const int cx = tx + 1;
+                auto F = [&](int a, int x) { return fm[L::face(0, a, ty, x)]; };
+                Ext<T> e = {};
+                T uAo = (T)0, uBo = (T)0;
+                if (valid) {
+                    e = extrapolate<T, true>(F(1, cx + 1), F(1, cx), xc.un[0], xc.uc[0], F(2, cx + 1), F(2, cx), xc.un[1],
+                                             xc.uc[1], F(3, cx + 1), F(3, cx), xc.un[2], xc.uc[2], xc.ro_n, xc.ro_c,
+                                             F(0, cx + 1), F(0, cx), qx);
+                    uAo = F(2, cx);
+                    uBo = F(3, cx);
+                }
+                // the cell behind the face below: the lane before
+                Ext<T> pv = {};
+                NVals<T> nv;
+                pv.rf = __shfl_up_sync(0xffffffffu, e.rf, 1);
+                pv.af = __shfl_up_sync(0xffffffffu, e.af, 1);
+                pv.bf = __shfl_up_sync(0xffffffffu, e.bf, 1);
+                T ucb = __shfl_up_sync(0xffffffffu, xc.un[0], 1);
+                nv.a[0] = __shfl_up_sync(0xffffffffu, xc.un[1], 1);
+                nv.b[0] = __shfl_up_sync(0xffffffffu, xc.un[2], 1);
+                nv.r[0] = __shfl_up_sync(0xffffffffu, xc.ro_n, 1);
+                int flb = __shfl_up_sync(0xffffffffu, (int)xc.fl, 1);
+                nv.a[1] = xc.un[1];
+                nv.b[1] = xc.un[2];
+                nv.r[1] = xc.ro_n;
+                if constexpr (NW > 1) {
+                    // hand-over within the tile row: warp w's last lane to warp w + 1's first
+                    const int u = k - k0, slot = u % NS;
+                    const unsigned par = (unsigned)((u / NS) & 1);
+                    if (w < NW - 1 && lane == 31) {
+                        float *hv = xh->v[ty][w][slot];
+                        hv[0] = e.rf;
+                        hv[1] = e.af;
+                        hv[2] = e.bf;
+                        hv[3] = xc.un[0];
+                        hv[4] = xc.un[1];
+                        hv[5] = xc.un[2];
+                        hv[6] = xc.ro_n;
+                        hv[7] = __int_as_float((int)xc.fl);
+                        mbar_arrive(smem_u32(&xh->bar[ty][w][slot])); // releases the writes above
+                    }
+                    bool got = true;
+                    if (takes) got = mbar_wait(smem_u32(&xh->bar[ty][w - 1][slot]), par, kLimitNs);
+                    if (!got) *abort_flag = 1;
+                    if (__any_sync(0xffffffffu, !got)) {
+                        failed = true;
+                        break;
+                    }
+                    if (takes && lane == 0) {
+                        const float *hv = xh->v[ty][w - 1][slot];
+                        pv.rf = hv[0];
+                        pv.af = hv[1];
+                        pv.bf = hv[2];
+                        ucb = hv[3];
+                        nv.a[0] = hv[4];
+                        nv.b[0] = hv[5];
+                        nv.r[0] = hv[6];
+                        flb = __float_as_int(hv[7]);
+                    }
+                }
+                if (valid && tx != 0) // the face below the cell (main.cpp:1920-2008)
+                    face_store(WX, ARK_CK(g.fi(i, j, k), WX.nf),
+                               face_values_v<T, false>(nv, (uint8_t)flb, xc.fl, ucb, xc.un[0], pv, e, uAo, uBo, qx));
+                const bool px = S.k.periodic_x;
+                const uint8_t *flm = sk;
+                if (valid && tx == 0) { // the tile's seam b = bx.x: the cell ahead of its face
+                    const int s = ARK_CK(seam_slot(g, SX, bx.x, j, k), X->n);
+                    seam_put(X->a, s, e.qb, e.ab, e.bb, xc, true);
+                    X->a[8][s] = uAo;
+                    X->a[9][s] = uBo;
+                    if (i == 1) { // face 1: the ghost position 0 behind it (its own flags)
+                        X->b[7][s] = __int_as_float((int)flm[L::flag(ty - L::CROW0, cx - 1)]);
+                        if (!px) // bounded: the inflow invariant, the values of cell 1 (xcell)
+                            seam_put(X->b, s, (xc.fl & FL_LT) ? (T)1 : (T)0, (T)0, (T)0, xc, false);
+                    }
+                }
+                if (valid && (tx == SX - 1 || i == g.C1)) { // seam bx.x + 1: the cell behind its face
+                    const int s = ARK_CK(seam_slot(g, SX, bx.x + 1, j, k), X->n);
+                    seam_put(X->b, s, e.rf, e.af, e.bf, xc, true);
+                    if (i == g.C1) { // face C1 + 1: the ghost position C1 + 1 ahead of it, the old face
+                        X->a[7][s] = __int_as_float((int)flm[L::flag(ty - L::CROW0, cx + 1)]);
+                        X->a[8][s] = F(2, cx + 1);
+                        X->a[9][s] = F(3, cx + 1);
+                        if (!px) // bounded: the outflow invariant, the values of cell C1 (xcell)
+                            seam_put(X->a, s, (T)(5. / 6.), (T)0, (T)0, xc, false);
+                    }
+                }
             }
             // the warp is done with plane k - 1 (with the stress) or k
             __syncwarp();
@@ -695,8 +847,13 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
         for (int p = issued - NS + 1 > pfirst ? issued - NS + 1 : pfirst; p <= issued; ++p)
             mbar_wait(bar_of(p), parity_of(p), kLimitNs);
     __syncthreads();
-    if (t == NT)
+    if (t == NT) {
         for (int q = 0; q < 2 * NS; ++q) mbar_inval(smem_u32(&bar[q]));
+        if (XS && NW > 1)
+            for (int r = 0; r < SY; ++r)
+                for (int h = 0; h < NW - 1; ++h)
+                    for (int q = 0; q < NS; ++q) mbar_inval(smem_u32(&xh->bar[r][h][q]));
+    }
     if (MODE & (P1_RMAX | P1_RSUM))
         tile_store<T, NT + 32>(S, bx, (MODE & P1_RMAX) != 0, (MODE & P1_RSUM) != 0, m0, m1, m2, rsum);
 }
@@ -705,14 +862,22 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
 // land on 128-byte boundaries; launches ask for 128 bytes more).
 __device__ __forceinline__ unsigned char *align128(unsigned char *p) { return p + ((128u - (smem_u32(p) & 127u)) & 127u); }
 
-// The single-grid kernel: maps and boxes as parameters.
-template <int MODE, int TSX, int TSY>
+// The single-grid kernel: maps and boxes as parameters.  XS: the x1 sweep folded in (fcur: the
+// face generation read; X: the seam arrays).
+template <int MODE, int TSX, int TSY, bool XS = false>
 __global__ void __launch_bounds__(TSX *TSY + 32, 2)
-    k_phase1_tma(const __grid_constant__ DevState<float> S, const __grid_constant__ TmaArgs A, int src, int dst, int kch) {
+    k_phase1_tma(const __grid_constant__ DevState<float> S, const __grid_constant__ TmaArgs A, int src, int dst, int kch,
+                 int fcur, const __grid_constant__ XSeams X) {
+    using L = TLayout<MODE, TSX, TSY>;
+    using H = XHand<TSX, TSY, L::NS>;
+    // two blocks per SM with the hand-over slots too
+    static_assert(!XS || 2 * (L::SMEM + 128 + 512 + (int)sizeof(H) + 1024) <= 228 * 1024, "shared memory: two blocks per SM");
     extern __shared__ __align__(128) unsigned char sm_raw[];
-    __shared__ __align__(8) unsigned long long bar[2 * TLayout<MODE, TSX, TSY>::NS + 1];
+    __shared__ __align__(8) unsigned long long bar[2 * L::NS + 1];
+    __shared__ __align__(8) unsigned char xh_raw[XS ? sizeof(H) : 8];
     auto map = [&](int q) { return &A.map[q]; };
-    phase1_tma_body<MODE, TSX, TSY>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar);
+    phase1_tma_body<MODE, TSX, TSY, XS>(S, map, A.m, false, src, dst, kch, bix_here(), align128(sm_raw), bar, fcur, &X,
+                                        reinterpret_cast<H *>(xh_raw));
 }
 
 // cuTensorMapEncodeTiled through the runtime's entry-point lookup (no link to libcuda)
@@ -781,7 +946,20 @@ inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fc
     }
     const int kch = kch_in > 0 ? (kch_in < S.g.C3 ? kch_in : S.g.C3) : tile_chunk<TSX, TSY>(S.g);
     k_phase1_tma<MODE, TSX, TSY><<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX * TSY + 32), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(
-        S, A, src, dst, kch);
+        S, A, src, dst, kch, fcur, XSeams{});
+}
+// Phase1 + stress with the x1 sweep folded in (X.tw set to TSX); false, launching nothing, when
+// the arrays do not allow the TMA form
+template <int MODE, int TSX, int TSY>
+inline bool launch_staged_tma_xs(const DevState<float> &S, int src, int dst, int fcur, XSeams &X, cudaStream_t st, int kch_in) {
+    TmaArgs A;
+    if (!tma_args<MODE, TSX, TSY>(A, S, src, fcur)) return false;
+    X.tw = TSX;
+    const int kch = kch_in > 0 ? (kch_in < S.g.C3 ? kch_in : S.g.C3) : tile_chunk<TSX, TSY>(S.g);
+    k_phase1_tma<MODE, TSX, TSY, true>
+        <<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX * TSY + 32), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(S, A, src, dst, kch,
+                                                                                                      fcur, X);
+    return true;
 }
 // The bounded-wait check: the same launch with every plane expecting `extra` bytes more than its
 // boxes bring, so no stage's mbarrier completes and every block gives up (STATUS_STAGING) after
@@ -793,14 +971,15 @@ inline bool launch_staged_tma_unmet(const DevState<float> &S, int src, int dst, 
     for (unsigned kind = DOWN; kind <= TOP; kind <<= 1) A.m.bytes[kind] += extra;
     const int kch = tile_chunk<64, 4>(S.g);
     k_phase1_tma<MODE, 64, 4><<<tile_grid<64, 4>(S.g, kch), dim3(64 * 4 + 32), TLayout<MODE, 64, 4>::SMEM + 128, st>>>(S, A, src,
-                                                                                                           dst, kch);
+                                                                                                           dst, kch, fcur,
+                                                                                                           XSeams{});
     return true;
 }
-template <int MODE, int TSX = 64, int TSY = 4> inline void prepare_staged_tma() {
+template <int MODE, int TSX = 64, int TSY = 4, bool XS = false> inline void prepare_staged_tma() {
     encode_tiled(); // looked up here, outside any stream capture
     constexpr int smem = TLayout<MODE, TSX, TSY>::SMEM + 128;
-    cudaFuncSetAttribute(k_phase1_tma<MODE, TSX, TSY>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_phase1_tma<MODE, TSX, TSY>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_phase1_tma<MODE, TSX, TSY, XS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_phase1_tma<MODE, TSX, TSY, XS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 #endif
 

@@ -294,6 +294,28 @@ struct HaloJob {
     int dst_plane, src_plane, face, dst_planes, src_planes, pad;
 };
 
+// The x1 sweep folded into the first Phase1 (FP32, TMA-staged): a tile of tw cells of a line
+// sweeps the x faces between its own cells and leaves the face at each of its seams (below its
+// first column; C1 + 1 after the last tile) to the seam kernel, writing what its side of such a
+// face needs.  Per slot, b: the cell behind the face (its forward extrapolation rf, af, bf, its
+// half-step u1, u2, u3, ro and its flags), a: the cell ahead (qb, ab, bb, half-step u1, u2, u3,
+// ro, flags, and the face's old u2, u3).  The ghost positions' flags (and, on a bounded x axis,
+// their edge invariants and the values of the cells they stand for) are written by the tiles
+// holding cells 1 and C1.  Slot (b, j, k) is element ((k - 1) * C2 + j - 1) * (nb + 1) + b of
+// each array, b = 0 .. nb = ceil(C1 / tw): the seams of a line side by side, as the seam kernel's
+// threads take them; seam_slots(g, 32) elements per array cover every tw.  Flags are stored as
+// the bits of a float.
+struct XSeams {
+    float *b[8], *a[10];
+    int tw, n; // tile width; elements per array (bounds-checked builds)
+};
+__host__ __device__ inline long long seam_slots(const Geom &g, int tw) {
+    return (long long)((g.C1 + tw - 1) / tw + 1) * g.C2 * g.C3;
+}
+__host__ __device__ inline int seam_slot(const Geom &g, int tw, int b, int j, int k) {
+    return ((k - 1) * g.C2 + j - 1) * ((g.C1 + tw - 1) / tw + 1) + b;
+}
+
 // Launch entry points (defined per precision in ark_fp64.cu / ark_fp32.cu).
 // P1_RMAX / P1_RSUM: also take the dt partials (max |u| of the level written) or the bulk-flow
 // partials (sum of u1 of the level written) for the next step.
@@ -310,6 +332,14 @@ template <class T> struct Launch {
     // kch: planes per block of the staged and face-centric forms (0: their default)
     static void phase1(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st,
                        int kch = 0);
+    // FP32, TMA-staged shapes (march 4 / 5): Phase1 + stress with the x1 sweep folded in (the x
+    // faces between the cells of each tile; X.tw is set to the tile width).  Returns false,
+    // launching nothing, where that form is not available (the caller runs phase1 and the x1
+    // sweep instead).
+    static bool phase1_sweep_x(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st,
+                               int kch, XSeams &X);
+    // the x faces phase1_sweep_x leaves: the tile seams and the faces beside the ghost positions
+    static void sweep_x_seams(const DevState<T> &S, int con, int fcur, const XSeams &X, cudaStream_t st);
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
     // x2/x3 sweeps: lines cut into balanced segments of at most `target` faces

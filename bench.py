@@ -56,7 +56,10 @@ ALGO_VALUES_FP32 = dict(ALGO_VALUES, phase1_stress_forces=(23, 1), phase1_forces
                         sweep_x2=(16, 1), sweep_x3=(16, 1),
                         # Phase2 and the second Phase1 in one kernel: Con 4 + nCon 4 + faces 12 + f 3
                         # -> faces 12 + new level 4
-                        phase2_phase1_forces=(39, 1))
+                        phase2_phase1_forces=(39, 1),
+                        # Phase1 + stress with the x1 sweep folded in: its 23 values plus the 4 new
+                        # x faces
+                        phase1_stress_sweep_x1=(27, 1))
 # Persistent state per cell: cell rho,u1,u2,u3 + 3 face sets x {p,u1,u2,u3}; read and
 # written once per step (the step's algorithmic bytes).
 STEP_VALUES = 2 * 16

@@ -340,12 +340,13 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
  * marching, 2 staged in shared memory with cp.async copies (FP32), 3 face quantities computed
  * once (FP64), 4 staged with TMA tensor copies (FP32)), of the second Phase1, the Phase2 form
  * (FP32: three sweep kernels, or one kernel for the three sweeps and the second Phase1 with
- * cp.async or TMA copies), the x2/x3 sweeps' segment length (8 to 64 faces), the x1
+ * cp.async or TMA copies, or the x1 sweep folded into a TMA-staged Phase1 + stress with a seam
+ * kernel in its place), the x2/x3 sweeps' segment length (8 to 64 faces), the x1
  * sweep's lines per warp (1 to 4) and the staged / face-centric Phase1's planes per block, each
  * candidate timed three times (best kept).  The results do not depend on the shapes.  choice
  * (5 ints, may be NULL): the chosen {shape 1, shape 2, segment, microseconds per step, Phase2
  * form: 0 sweep kernels, 1 one sweep kernel (only by ARK_PHASE2_FUSED=1), 2 sweeps and second
- * Phase1 in one kernel, 3 the same with TMA copies}. */
+ * Phase1 in one kernel, 3 the same with TMA copies, 4 the x1 sweep folded into Phase1 + stress}. */
 int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice);
 
 /* ---- ensembles: many independent channels in one launch per phase ------------------------

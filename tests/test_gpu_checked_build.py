@@ -69,6 +69,8 @@ SMALL_GRID_TESTS = [
     "tests/test_gpu_parity.py::test_bounded_axes_match_oracle",
     "tests/test_gpu_parity.py::test_fused_phase2_agrees",
     "tests/test_gpu_parity.py::test_phase2_phase1_kernel_agrees",
+    "tests/test_gpu_parity.py::test_x1_sweep_folded_into_phase1_agrees",
+    "tests/test_gpu_parity.py::test_x1_sweep_folded_with_solids",
     "tests/test_gpu_slabs.py",
     "tests/test_ensemble.py",
     "tests/test_gpu_closure.py",

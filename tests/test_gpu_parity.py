@@ -376,7 +376,8 @@ def test_fp32_steps_and_pieces_interleaved_in_both_phase2_forms(ark, port, monke
 @pytest.mark.parametrize("C", [(40, 20, 36), (130, 9, 70), (64, 4, 32), (7, 3, 1)])
 def test_phase1_kernel_shapes_agree(ark, port, monkeypatch, C):
     """The marching, the one-cell-per-thread, the shared-memory-staged (FP32: cp.async copies,
-    "2", or TMA tensor copies on 64 x 4 or 32 x 8 tiles, "4" and "5") and the face-centric (FP64)
+    "2", or TMA tensor copies on 64 x 4, 32 x 8 or 128 x 2 tiles, "4", "5" and "6") and the
+    face-centric (FP64)
     Phase1 kernels
     (ARK_PHASE1_MARCH) produce the same bits in both precisions, on grids with ragged tiles and
     fewer planes than a block marches."""
@@ -384,7 +385,7 @@ def test_phase1_kernel_shapes_agree(ark, port, monkeypatch, C):
     st0 = port.channel_state(p)
     for prec in (ark.FP64, ark.FP32):
         outs = []
-        for m in (("00", "11", "10", "33", "30", "03") if prec == ark.FP64 else ("00", "11", "10", "22", "20", "02", "44", "42", "24", "55", "54", "25")):
+        for m in (("00", "11", "10", "33", "30", "03") if prec == ark.FP64 else ("00", "11", "10", "22", "20", "02", "44", "42", "24", "55", "54", "25", "66", "64", "46")):
             monkeypatch.setenv("ARK_PHASE1_MARCH", m)
             with ark.Context(params_from(ark, p, precision=prec)) as c:
                 c.upload(st0)
@@ -500,7 +501,9 @@ def test_autotune_keeps_results(ark, port, prec):
         a.upload(st0)
         b.upload(st0)
         choice = a.autotune(1)
-        assert choice["segment"] in (8, 16, 32, 64) and choice["phase1"] in (0, 1, 2)
+        assert choice["segment"] in (8, 12, 16, 20, 24, 32, 48, 64)
+        assert choice["phase1_stress"] in range(7) and choice["phase1"] in range(7)
+        assert choice["phase2_form"] in ((0, 2, 3, 4) if prec == "fp32" else (0,))
         n = a.scalars().nstep
         b.step(n)
         a.sync()
@@ -565,6 +568,66 @@ def test_phase2_phase1_kernel_agrees(ark, port, monkeypatch, C, px, pz):
     for o in outs[1:]:
         for n in CELLS + FACES:
             assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), n
+
+
+@pytest.mark.parametrize("C,px,pz", [((40, 20, 36), True, True), ((130, 9, 70), True, True), ((70, 6, 5), False, False),
+                                     ((64, 4, 1), True, False), ((65, 31, 17), True, True), ((33, 3, 9), False, True),
+                                     ((20, 7, 5), True, True), ((97, 5, 4), False, True)])
+def test_x1_sweep_folded_into_phase1_agrees(ark, port, monkeypatch, C, px, pz):
+    """FP32 Phase2 form 4: the x1 sweep folded into the TMA-staged Phase1 + stress (x faces
+    between a tile's cells, handed between the two warps of a 64-wide tile row; the seam kernel
+    finishing the faces at the tiles' seams and beside the ghost positions from what the tiles
+    left) gives the bits of the separate x1 sweep, on 64 x 4, 32 x 8 and 128 x 2 tiles (two,
+    one and four warps per tile row), ragged and one-warp rows, one tile per line, periodic and
+    bounded x; with a Phase1 shape that cannot
+    fold ("22") form 4 runs the separate sweep."""
+    p = port.channel_params(*C, seed=31)
+    st0 = port.channel_state(p)
+    for march in ("44", "55", "66", "64", "22"):
+        outs = []
+        for mode in ("0", "4"):
+            monkeypatch.setenv("ARK_PHASE1_MARCH", march)
+            monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
+            P = params_from(ark, p, precision=ark.FP32)
+            P.periodic_x, P.periodic_z = int(px), int(pz)
+            with ark.Context(P) as c:
+                c.upload(st0)
+                c.step(3)
+                kt = c.kernel_times(2)
+                c.step(2)
+                c.sync()
+                outs.append(c.download(CELLS + FACES))
+                names = [n for n, _ in kt]
+                folded = mode == "4" and march[0] in "456"
+                assert names == ["finalize_dt", "wrap_con", "phase1_stress_sweep_x1" if folded else "phase1_stress_forces",
+                                 "sweep_x1_seams" if folded else "sweep_x1", "sweep_x2", "sweep_x3", "phase1_forces"]
+        for n in CELLS + FACES:
+            assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), (march, n)
+
+
+def test_x1_sweep_folded_with_solids(ark, port, monkeypatch):
+    """The folded x1 sweep through the face update's wall branches: the reference's stock
+    backward-facing step (solid block inside the domain, bounded axes) in FP32, form 4 against
+    form 0, on both tile shapes."""
+    g = np.load(os.path.join(GOLD, "stock_case.npz"))
+    p = json.loads(str(g["params"]))
+    st = {n[5:]: np.ascontiguousarray(g[n]) for n in g.files if n.startswith("init/")}
+    for march in ("44", "55", "66"):
+        outs = []
+        for mode in ("0", "4"):
+            monkeypatch.setenv("ARK_PHASE1_MARCH", march)
+            monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
+            gp = ark.make_params(p["C1"], p["C2"], p["C3"], vis=p["nu"], sound=p["sound"], rho0=p["rho0"], cfl=p["cfl"],
+                                 lx=p["lx"], ly=p["ly"], lz=p["lz"], forcing=False)
+            gp.periodic_x = gp.periodic_z = 0
+            gp.precision = ark.FP32
+            with ark.Context(gp) as ctx:
+                ctx.upload(st)
+                ctx.step(int(g["steps"]))
+                ctx.sync()
+                outs.append(ctx.download(CELLS + FACES))
+        for n in CELLS + FACES:
+            assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), (march, n)
 
 
 def test_staging_wait_gives_up_with_status(ark, port):
