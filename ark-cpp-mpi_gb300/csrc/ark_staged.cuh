@@ -721,8 +721,8 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
         const bool valid = i <= g.C1 && j <= g.C2;
         // the folded x1 sweep: its constants and output faces; the warp's place in the tile row
         // and whether its first lane's face takes a hand-over (warp-uniform)
-        const SweepK<T> qx = sweep_consts(S, 0);
-        const FaceOut<T> WX = sweep_out(S, fcur, 0);
+        const SweepK<T> qx = XS ? sweep_consts(S, 0) : SweepK<T>{};
+        const FaceOut<T> WX = XS ? sweep_out(S, fcur, 0) : FaceOut<T>{};
         const int lane = t & 31, w = tx >> 5;
         const bool takes = XS && NW > 1 && w > 0 && x0 + 32 * w + 1 <= g.C1 && j <= g.C2;
         for (int k = k0; k <= k1; ++k) {

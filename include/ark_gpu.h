@@ -338,7 +338,8 @@ int ark_set_closure(ark_ctx *ctx, const ark_mlp *mlp, double u_tau);
 /* Times the kernel shapes of the step on the live state (it advances) and keeps the fastest,
  * one setting at a time: the shape of the Phase1 with stress (0 one cell per thread, 1
  * marching, 2 staged in shared memory with cp.async copies (FP32), 3 face quantities computed
- * once (FP64), 4 staged with TMA tensor copies (FP32)), of the second Phase1, the Phase2 form
+ * once (FP64), 4 staged with TMA tensor copies (FP32) on 64 x 4 tiles, 6 the same on 128 x 2
+ * tiles), of the second Phase1, the Phase2 form
  * (FP32: three sweep kernels, or one kernel for the three sweeps and the second Phase1 with
  * cp.async or TMA copies, or the x1 sweep folded into a TMA-staged Phase1 + stress with a seam
  * kernel in its place), the x2/x3 sweeps' segment length (8 to 64 faces), the x1
