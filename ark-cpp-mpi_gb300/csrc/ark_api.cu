@@ -484,11 +484,24 @@ template <class T> struct EngineT : Engine {
             Launch<T>::phase2_fused(S, y, fcur, st);
             for (int ax = 0; ax < 3; ++ax) mark();
         } else {
+            // the seam faces of the folded x1 sweep: only the second Phase1 reads x faces, so
+            // (captured) they are written beside the x2 and x3 sweeps, on the second stream
+            const bool beside = xs && !ev;
+            if (beside) {
+                cudaEventRecord(ctx->seam_fork, st);
+                cudaStreamWaitEvent(ctx->fill, ctx->seam_fork, 0);
+                Launch<T>::sweep_x_seams(S, y, fcur, seams, ctx->fill);
+                cudaEventRecord(ctx->seam_join, ctx->fill);
+            }
             for (int ax = 0; ax < 3; ++ax) {
-                if (ax == 0 && xs) Launch<T>::sweep_x_seams(S, y, fcur, seams, st);
-                else if (ax > 0 || !fold) Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
+                if (ax == 0 && xs) {
+                    if (!beside) Launch<T>::sweep_x_seams(S, y, fcur, seams, st);
+                } else if (ax > 0 || !fold) {
+                    Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
+                }
                 mark();
             }
+            if (beside) cudaStreamWaitEvent(st, ctx->seam_join, 0);
         }
         Launch<T>::phase1(S, x, y, fcur ^ 1, P1_FORCES | P1_RSUM, ctx->march[1], st, ctx->p1_chunk);
         mark();
@@ -670,7 +683,9 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     if (cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
         cudaStreamCreateWithPriority(&ctx->fill, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->fill_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->fill_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->fill_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->seam_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->seam_join, cudaEventDisableTiming) != cudaSuccess) {
         *status = fail(ARK_ERR_CUDA, "cudaStreamCreate failed");
         return nullptr;
     }
@@ -745,6 +760,8 @@ int ark_destroy(ark_ctx *ctx) {
     }
     if (ctx->fill_fork) cudaEventDestroy(ctx->fill_fork);
     if (ctx->fill_join) cudaEventDestroy(ctx->fill_join);
+    if (ctx->seam_fork) cudaEventDestroy(ctx->seam_fork);
+    if (ctx->seam_join) cudaEventDestroy(ctx->seam_join);
     for (int b = 0; b < 2; ++b) {
         if (ctx->io_dev[b]) cudaFree(ctx->io_dev[b]);
         if (ctx->io_host[b]) cudaFreeHost(ctx->io_host[b]);

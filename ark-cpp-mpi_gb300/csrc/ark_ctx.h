@@ -91,6 +91,7 @@ struct ark_ctx {
     cudaEvent_t fork = nullptr, join = nullptr;
     cudaStream_t fill = nullptr;          // the captured step's ghost fill, beside dt
     cudaEvent_t fill_fork = nullptr, fill_join = nullptr;
+    cudaEvent_t seam_fork = nullptr, seam_join = nullptr; // the seam kernel on `fill`, beside the x2 and x3 sweeps
     float closure_scale = 0.f;            // u_tau / vis for the y+ feature
     int seg_target = 32;                  // x2/x3 sweep segment length (faces)
     int x1_lines = 0;                     // x1 sweep lines per warp (0: x_lines_per_warp's choice)
