@@ -459,8 +459,10 @@ template <class T> struct EngineT : Engine {
         // Phase2 form 4: the x1 sweep folded into Phase1 + stress (TMA-staged FP32 shapes; the
         // seam kernel takes the x1 sweep's launch), else Phase1 + stress alone (should the folded
         // form be unavailable, the x1 sweep follows in the same timed slot)
-        const bool fold = folds_x1();
-        const bool xs = fold && Launch<T>::phase1_sweep_x(S, y, x, fcur, mode, ctx->march[0], st, ctx->p1_chunk, seams);
+        const bool fold = folds_x1(), fold3 = fold && ctx->p2mode == 5;
+        const bool xs =
+            fold && Launch<T>::phase1_sweep_x(S, y, x, fcur, mode, ctx->march[0], st, ctx->p1_chunk, seams, fold3 ? 3 : 1);
+        const bool zs = xs && fold3; // form 5: the x3 sweep folded in too
         if (!xs) Launch<T>::phase1(S, y, x, fcur, mode, ctx->march[0], st, ctx->p1_chunk);
         if (fold && !xs) Launch<T>::sweep(S, y, fcur, 0, st, ctx->seg_target, ctx->x1_lines);
         mark();
@@ -484,18 +486,22 @@ template <class T> struct EngineT : Engine {
             Launch<T>::phase2_fused(S, y, fcur, st);
             for (int ax = 0; ax < 3; ++ax) mark();
         } else {
-            // the seam faces of the folded x1 sweep: only the second Phase1 reads x faces, so
-            // (captured) they are written beside the x2 and x3 sweeps, on the second stream
+            // the seam faces of the folded sweeps: only the second Phase1 reads the x and z faces,
+            // so (captured) they are written beside the x2 sweep (and the x3 sweep), on the second
+            // stream
             const bool beside = xs && !ev;
             if (beside) {
                 cudaEventRecord(ctx->seam_fork, st);
                 cudaStreamWaitEvent(ctx->fill, ctx->seam_fork, 0);
                 Launch<T>::sweep_x_seams(S, y, fcur, seams, ctx->fill);
+                if (zs) Launch<T>::sweep_z_seams(S, y, fcur, seams.kch, ctx->fill);
                 cudaEventRecord(ctx->seam_join, ctx->fill);
             }
             for (int ax = 0; ax < 3; ++ax) {
                 if (ax == 0 && xs) {
                     if (!beside) Launch<T>::sweep_x_seams(S, y, fcur, seams, st);
+                } else if (ax == 2 && zs) {
+                    if (!beside) Launch<T>::sweep_z_seams(S, y, fcur, seams.kch, st);
                 } else if (ax > 0 || !fold) {
                     Launch<T>::sweep(S, y, fcur, ax, st, ctx->seg_target, ctx->x1_lines);
                 }
@@ -525,16 +531,19 @@ template <class T> struct EngineT : Engine {
     bool use_step2() const { return (ctx->p2mode == 2 || ctx->p2mode == 3) && S.spare.ro; }
     // the three sweep kernels (or the x1 sweep folded into Phase1) of a context whose z ghosts
     // are its own: no Phase2 ghost fill
-    bool skip_phase2_fill() const { return (ctx->p2mode == 0 || ctx->p2mode == 4) && !S.k.ext_z; }
-    // Phase2 form 4 where the Phase1 shape allows it (FP32, TMA-staged Phase1 + stress)
+    bool skip_phase2_fill() const { return (ctx->p2mode == 0 || ctx->p2mode >= 4) && !S.k.ext_z; }
+    // Phase2 forms 4 and 5 where the Phase1 shape allows them (FP32, TMA-staged Phase1 + stress)
     bool folds_x1() const {
-        return ctx->p2mode == 4 && seams.b[0] && ctx->march[0] >= 4 && ctx->march[0] <= 6 && !ctx->closure_net;
+        return (ctx->p2mode == 4 || ctx->p2mode == 5) && seams.b[0] && ctx->march[0] >= 4 && ctx->march[0] <= 6 &&
+               !ctx->closure_net && !S.k.ext_z;
     }
     int step_launches() override { return use_step2() ? 5 : skip_phase2_fill() ? kNumStepKernels - 1 : kNumStepKernels; }
     const char *step_kernel_name(int q) override {
         if (q < 0 || q >= step_launches()) return "";
         if (skip_phase2_fill() && q >= 3) ++q; // no wrap_phase2
         if (use_step2() && q == 4) return "phase2_phase1_forces";
+        if (folds_x1() && ctx->p2mode == 5 && (q == 2 || q == 6))
+            return q == 2 ? "phase1_stress_sweep_x1_x3" : "sweep_x3_seams";
         if (folds_x1() && (q == 2 || q == 4)) return q == 2 ? "phase1_stress_sweep_x1" : "sweep_x1_seams";
         return kStepKernels[q];
     }
@@ -705,11 +714,13 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
     // and 1.10 vs 1.18 ms one cell per thread at 256x128x128).  ark_autotune picks per grid.
     ctx->march[0] = params->precision == ARK_FP32 ? 4 : 3;
     if (params->precision == ARK_FP32) {
-        // FP32: the x1 sweep folded into Phase1 + stress (Phase2 form 4), on 128 x 2 tiles where
-        // lines are long enough to fill them (a tile seam every 128 cells): at 512x256x256 the
-        // step takes 2.140 ms against 2.209 with the separate x1 sweep (Phase1 + stress and x1
-        // sweep 0.835 + seams 0.053 ms against 0.538 + 0.421; on 64 x 4 tiles 0.818 + 0.082)
-        ctx->p2mode = 4;
+        // FP32: the x1 and x3 sweeps folded into Phase1 + stress (Phase2 form 5), on 128 x 2
+        // tiles where lines are long enough to fill them (a tile seam every 128 cells): at
+        // 512x256x256 the step takes 1.980 ms against 2.130 with the x1 sweep alone folded in
+        // (form 4) and 2.210 with the separate sweeps (form 0); Phase1 + stress with both sweeps
+        // 1.032 ms and the seams 0.055 + 0.029 ms, against 0.538 + 0.421 + 0.374 for the three
+        // kernels.  On 64 x 4 tiles: 2.012 ms
+        ctx->p2mode = 5;
         if (params->n1_cells >= 256) ctx->march[0] = 6;
     }
     // x2/x3 segments: 20 faces for FP64 (0.531 / 0.508 -> 0.513 / 0.492 ms at 256x128x128 against
@@ -727,7 +738,7 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
         if (e[0] && ok(e[1])) ctx->march[1] = e[1] - '0';
     }
     if (const char *e = std::getenv("ARK_PHASE2_FUSED"))
-        if (e[0] >= '0' && e[0] <= '4' && (e[0] < '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
+        if (e[0] >= '0' && e[0] <= '5' && (e[0] < '2' || params->precision == ARK_FP32)) ctx->p2mode = e[0] - '0';
     Launch<float>::prepare();
     Launch<double>::prepare();
     cudaEventCreate(&ctx->ev0);
@@ -1449,12 +1460,12 @@ int ark_autotune(ark_ctx *ctx, int steps_per_candidate, int *choice) {
         // second Phase1, or (FP32) the x1 sweep folded into Phase1 + stress.  The one-kernel
         // Phase2 alone (mode 1) is correct but slower at every size measured: left to
         // ARK_PHASE2_FUSED=1, not tried here.
-        const int p2cand[4] = {0, 2, 3, 4};
+        const int p2cand[5] = {0, 2, 3, 4, 5};
         if (which == 2 && !fp32) continue;
-        const int ncand = which < 2 ? (fp32 ? 5 : 3) : which == 2 ? 4 : which == 3 ? 8 : 4;
+        const int ncand = which < 2 ? (fp32 ? 5 : 3) : which == 2 ? 5 : which == 3 ? 8 : 4;
         int keep = which < 2 ? ctx->march[which] : which == 2 ? ctx->p2mode : which == 3 ? ctx->seg_target : ctx->x1_lines;
-        // the one-kernel forms have no segments and no x1 sweep; the folded x1 sweep no x1 sweep
-        if (which >= 3 && ctx->p2mode != 0 && !(which == 3 && ctx->p2mode == 4)) continue;
+        // the one-kernel forms have no segments and no x1 sweep; the folded forms no x1 sweep
+        if (which >= 3 && ctx->p2mode != 0 && !(which == 3 && ctx->p2mode >= 4)) continue;
         for (int c = 0; c < ncand; ++c) {
             const int v = which < 2 ? shapes[c] : which == 2 ? p2cand[c] : which == 3 ? segs[c] : lines[c];
             if (v == keep) continue;

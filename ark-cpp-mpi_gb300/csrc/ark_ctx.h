@@ -100,7 +100,8 @@ struct ark_ctx {
                     // one kernel for the three sweeps and the second Phase1, 3 (FP32) the same
                     // with TMA tensor copies, 4 (FP32, TMA-staged Phase1 + stress) the x1 sweep
                     // folded into Phase1 + stress (a seam kernel finishes it), then the x2 and
-                    // x3 sweeps
+                    // x3 sweeps, 5 the x1 and x3 sweeps folded in (two seam kernels), then the
+                    // x2 sweep
     // output streaming: two device and two pinned host slab buffers of io_cap doubles
     double *io_dev[2] = {nullptr, nullptr};
     double *io_host[2] = {nullptr, nullptr};

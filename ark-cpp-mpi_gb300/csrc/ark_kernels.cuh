@@ -1974,6 +1974,18 @@ __global__ void __launch_bounds__(128) k_sweep_col(const __grid_constant__ DevSt
     sweep_col_body<T, AX>(S, con, fcur, seg, bix_here());
 }
 
+// The z faces that Phase1 + stress with the x3 sweep folded in leaves (stg::phase1_tma_body with
+// XS & 2): per column, the face below the first plane of each chunk of kch planes (c * kch + 1,
+// blockIdx.z = c < nch) and face C3 + 1 (blockIdx.z = nch), each the x3 sweep's own segment of
+// one face (positions s0 and s0 + 1, ghost positions read where they stand for).
+template <class T>
+__global__ void __launch_bounds__(128) k_sweep_z_seams(const __grid_constant__ DevState<T> S, int con, int fcur, int kch) {
+    BIx bx = bix_here();
+    const int nch = (S.g.C3 + kch - 1) / kch;
+    bx.z = (int)blockIdx.z < nch ? (int)blockIdx.z * kch : S.g.C3;
+    sweep_col_body<T, 2>(S, con, fcur, 1, bx);
+}
+
 // ---------------------------------------------------------------------------------------
 // Phase2 with the three sweeps fused.  The sweeps are independent (each reads its own face
 // set and the two cell levels, and writes its own new face generation), so one kernel can do
@@ -2394,21 +2406,28 @@ template <class T> void Launch<T>::sweep_x_seams(const DevState<T> &S, int con, 
 
 template <class T>
 bool Launch<T>::phase1_sweep_x(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st, int kch,
-                               XSeams &X) {
+                               XSeams &X, int fold) {
     if constexpr (std::is_same<T, float>::value) {
         constexpr int A = P1_STRESS | P1_FORCES | P1_RMAX, B = A | P1_BULK;
-        if (march == 4) {
-            if (mode == A) return stg::launch_staged_tma_xs<A, 64, 4>(S, src, dst, fcur, X, st, kch);
-            if (mode == B) return stg::launch_staged_tma_xs<B, 64, 4>(S, src, dst, fcur, X, st, kch);
-        } else if (march == 5) {
-            if (mode == A) return stg::launch_staged_tma_xs<A, 32, 8>(S, src, dst, fcur, X, st, kch);
-            if (mode == B) return stg::launch_staged_tma_xs<B, 32, 8>(S, src, dst, fcur, X, st, kch);
-        } else if (march == 6) {
-            if (mode == A) return stg::launch_staged_tma_xs<A, 128, 2>(S, src, dst, fcur, X, st, kch);
-            if (mode == B) return stg::launch_staged_tma_xs<B, 128, 2>(S, src, dst, fcur, X, st, kch);
-        }
+        if (mode != A && mode != B) return false;
+        auto go = [&](auto m, auto xs) {
+            constexpr int M = decltype(m)::value, XS = decltype(xs)::value;
+            if (march == 4) return stg::launch_staged_tma_xs<M, 64, 4, XS>(S, src, dst, fcur, X, st, kch);
+            if (march == 5) return stg::launch_staged_tma_xs<M, 32, 8, XS>(S, src, dst, fcur, X, st, kch);
+            if (march == 6) return stg::launch_staged_tma_xs<M, 128, 2, XS>(S, src, dst, fcur, X, st, kch);
+            return false;
+        };
+        using I1 = std::integral_constant<int, 1>;
+        using I3 = std::integral_constant<int, 3>;
+        if (mode == A) return fold == 3 ? go(std::integral_constant<int, A>(), I3()) : go(std::integral_constant<int, A>(), I1());
+        return fold == 3 ? go(std::integral_constant<int, B>(), I3()) : go(std::integral_constant<int, B>(), I1());
     }
     return false;
+}
+
+template <class T> void Launch<T>::sweep_z_seams(const DevState<T> &S, int con, int fcur, int kch, cudaStream_t st) {
+    const int nch = (S.g.C3 + kch - 1) / kch;
+    k_sweep_z_seams<T><<<dim3(col_sweep_blocks(S.g, 2), 1, nch + 1), 128, 0, st>>>(S, con, fcur, kch);
 }
 
 
@@ -2434,12 +2453,18 @@ template <class T> void Launch<T>::prepare() {
         stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 128, 2>();
         stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 128, 2>();
         stg::prepare_staged_tma<P1_FORCES | P1_RSUM, 128, 2>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 128, 2, true>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 128, 2, true>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 64, 4, true>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 64, 4, true>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 32, 8, true>();
-        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 32, 8, true>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 128, 2, 1>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 128, 2, 1>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 64, 4, 1>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 64, 4, 1>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 32, 8, 1>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 32, 8, 1>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 128, 2, 3>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 128, 2, 3>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 64, 4, 3>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 64, 4, 3>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_RMAX, 32, 8, 3>();
+        stg::prepare_staged_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 32, 8, 3>();
         s2::prepare<float>();
     }
 }

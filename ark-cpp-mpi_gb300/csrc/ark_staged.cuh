@@ -608,6 +608,18 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
                  : "memory");
 }
 
+// One side of a seam face in X (q: X.b or X.a): the three extrapolated values, the cell's
+// half-step values and (fl) its flags.
+__device__ __forceinline__ void seam_put(float *const *q, int s, float e0, float e1, float e2, const XCell &c, bool fl) {
+    q[0][s] = e0;
+    q[1][s] = e1;
+    q[2][s] = e2;
+    q[3][s] = c.un[0];
+    q[4][s] = c.un[1];
+    q[5][s] = c.un[2];
+    q[6][s] = c.ro_n;
+    if (fl) q[7][s] = __int_as_float((int)c.fl);
+}
 // One block's work in the staged Phase1 with TMA copies: tile (bx.x, bx.y) of TSX x TSY columns,
 // planes of chunk bx.z (kch planes), by TSX * TSY consumer threads (one cell column each) and
 // one producer warp (threads TSX * TSY ..; its lane 0 works).  The producer issues a plane's
@@ -623,7 +635,7 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
 // leaves.  Every thread calls it; it ends with no copy in flight and the mbarriers
 // invalidated, so a persistent kernel may run it again.
 //
-// XS (Phase1 + stress only): the x1 sweep folded in.  The x extrapolation of a cell needs its
+// XS & 1 (Phase1 + stress only): the x1 sweep folded in.  The x extrapolation of a cell needs its
 // half-step values (just computed), its old values and its two old x faces (staged), so per
 // plane every cell also extrapolates along x (main.cpp:1756-1873) and updates the x face below
 // it from the cell behind (main.cpp:1920-2008): the lane before, or for the first lane of a
@@ -634,24 +646,19 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
 // read).  The faces at the tiles' seams (below a tile's first column, and face C1 + 1) are
 // left to k_sweep_x_seams: the tile's first and last cells write all that their side of such a
 // face needs into X (see XSeams).  Same arithmetic, same inputs, same bits as k_sweep_x.
-// One side of a seam face in X (q: X.b or X.a): the three extrapolated values, the cell's
-// half-step values and (fl) its flags.
-__device__ __forceinline__ void seam_put(float *const *q, int s, float e0, float e1, float e2, const XCell &c, bool fl) {
-    q[0][s] = e0;
-    q[1][s] = e1;
-    q[2][s] = e2;
-    q[3][s] = c.un[0];
-    q[4][s] = c.un[1];
-    q[5][s] = c.un[2];
-    q[6][s] = c.ro_n;
-    if (fl) q[7][s] = __int_as_float((int)c.fl);
-}
+//
+// XS & 2: the x3 sweep folded in too.  A cell's z extrapolation needs its two old z faces, both
+// staged (its plane's and the plane above's), and the z face below a cell needs the cell one
+// plane down: this thread's previous plane, carried in registers.  So every plane but the
+// chunk's first also updates the z face below its cells (main.cpp:2261-2494, the x3 sweep's
+// extrapolate and face_values with the same inputs).  The face below a chunk's first plane and
+// face C3 + 1 are left to k_sweep_z_seams: contiguous rows of faces, coalesced.
 template <int TSX, int TSY, int NS> struct XHand {
     static constexpr int NH = TSX / 32 > 1 ? TSX / 32 - 1 : 1; // hand-overs per row
     unsigned long long bar[TSY][NH][NS];
     float v[TSY][NH][NS][8]; // rf, af, bf, u1, u2, u3, ro of the half-step level, flags
 };
-template <int MODE, int TSX, int TSY, bool XS = false, class Maps>
+template <int MODE, int TSX, int TSY, int XS = 0, class Maps>
 __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const Maps &map, const BoxMeta &A, bool fence_maps,
                                                 int src, int dst, int kch, const BIx &bx, unsigned char *sm,
                                                 unsigned long long *bar, int fcur = 0, const XSeams *X = nullptr,
@@ -683,7 +690,7 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
             mbar_init(smem_u32(&bar[q]), 1);
             mbar_init(smem_u32(&bar[NS + q]), NT / 32);
         }
-        if (XS && NW > 1)
+        if ((XS & 1) && NW > 1)
             for (int r = 0; r < SY; ++r)
                 for (int h = 0; h < NW - 1; ++h)
                     for (int q = 0; q < NS; ++q) mbar_init(smem_u32(&xh->bar[r][h][q]), 1);
@@ -721,10 +728,17 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
         const bool valid = i <= g.C1 && j <= g.C2;
         // the folded x1 sweep: its constants and output faces; the warp's place in the tile row
         // and whether its first lane's face takes a hand-over (warp-uniform)
-        const SweepK<T> qx = XS ? sweep_consts(S, 0) : SweepK<T>{};
-        const FaceOut<T> WX = XS ? sweep_out(S, fcur, 0) : FaceOut<T>{};
+        const SweepK<T> qx = (XS & 1) ? sweep_consts(S, 0) : SweepK<T>{};
+        const FaceOut<T> WX = (XS & 1) ? sweep_out(S, fcur, 0) : FaceOut<T>{};
         const int lane = t & 31, w = tx >> 5;
-        const bool takes = XS && NW > 1 && w > 0 && x0 + 32 * w + 1 <= g.C1 && j <= g.C2;
+        const bool takes = (XS & 1) && NW > 1 && w > 0 && x0 + 32 * w + 1 <= g.C1 && j <= g.C2;
+        // the folded x3 sweep: its constants and output faces; the cell one plane down (its
+        // forward extrapolation, half-step u3, u1, u2, density, flags)
+        const SweepK<T> qz = (XS & 2) ? sweep_consts(S, 2) : SweepK<T>{};
+        const FaceOut<T> WZ = (XS & 2) ? sweep_out(S, fcur, 2) : FaceOut<T>{};
+        Ext<T> zprev = {};
+        T zun = (T)0, zua = (T)0, zub = (T)0, zro = (T)0;
+        uint8_t zfl = 0;
         for (int k = k0; k <= k1; ++k) {
             bool ok = true;
             if (k == k0) {
@@ -739,13 +753,41 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
                 break;
             }
             const unsigned char *sk = sm + ((k - pfirst) % NS) * L::STAGE;
+            const unsigned char *su = sm + ((k + 1 - pfirst) % NS) * L::STAGE;
             XCell xc = {};
             if (valid) {
-                const unsigned char *su = sm + ((k + 1 - pfirst) % NS) * L::STAGE;
                 const unsigned char *sd = STRESS ? sm + ((k - 1 - pfirst) % NS) * L::STAGE : sk;
                 staged_cell<MODE, L>(S, dst, sd, sk, su, i, j, k, tx, ty, kk, dt, G1, m0, m1, m2, rsum, XS ? &xc : nullptr);
             }
-            if constexpr (XS) {
+            if constexpr ((XS & 2) != 0) {
+                // the cell's z extrapolation (the x3 sweep's: normal u3, tangential u1 and u2)
+                const T *fm = (const T *)sk, *fu = (const T *)su;
+                const int cx = tx + 1;
+                auto Z = [&](const T *f, int a) { return f[L::face(2, a, ty, cx)]; };
+                if (valid) {
+                    const Ext<T> ez =
+                        extrapolate<T, true>(Z(fu, 3), Z(fm, 3), xc.un[2], xc.uc[2], Z(fu, 1), Z(fm, 1), xc.un[0], xc.uc[0],
+                                             Z(fu, 2), Z(fm, 2), xc.un[1], xc.uc[1], xc.ro_n, xc.ro_c, Z(fu, 0), Z(fm, 0), qz);
+                    if (k > k0) { // the face below the cell (main.cpp:1920-2008 as the x3 sweep applies it)
+                        NVals<T> nv;
+                        nv.a[0] = zua;
+                        nv.b[0] = zub;
+                        nv.r[0] = zro;
+                        nv.a[1] = xc.un[0];
+                        nv.b[1] = xc.un[1];
+                        nv.r[1] = xc.ro_n;
+                        face_store(WZ, ARK_CK(g.fi(i, j, k), WZ.nf),
+                                   face_values_v<T, false>(nv, zfl, xc.fl, zun, xc.un[2], zprev, ez, Z(fm, 1), Z(fm, 2), qz));
+                    }
+                    zprev = ez;
+                    zun = xc.un[2];
+                    zua = xc.un[0];
+                    zub = xc.un[1];
+                    zro = xc.ro_n;
+                    zfl = xc.fl;
+                }
+            }
+            if constexpr ((XS & 1) != 0) {
                 // the cell's x extrapolation (the x1 sweep's extrapolate, from the same values)
                 const T *fm = (const T *)sk;
                 const int cx = tx + 1;
@@ -849,7 +891,7 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
     __syncthreads();
     if (t == NT) {
         for (int q = 0; q < 2 * NS; ++q) mbar_inval(smem_u32(&bar[q]));
-        if (XS && NW > 1)
+        if ((XS & 1) && NW > 1)
             for (int r = 0; r < SY; ++r)
                 for (int h = 0; h < NW - 1; ++h)
                     for (int q = 0; q < NS; ++q) mbar_inval(smem_u32(&xh->bar[r][h][q]));
@@ -862,9 +904,9 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
 // land on 128-byte boundaries; launches ask for 128 bytes more).
 __device__ __forceinline__ unsigned char *align128(unsigned char *p) { return p + ((128u - (smem_u32(p) & 127u)) & 127u); }
 
-// The single-grid kernel: maps and boxes as parameters.  XS: the x1 sweep folded in (fcur: the
-// face generation read; X: the seam arrays).
-template <int MODE, int TSX, int TSY, bool XS = false>
+// The single-grid kernel: maps and boxes as parameters.  XS: the sweeps folded in (1: x1, 3: x1
+// and x3; fcur: the face generation read; X: the seam arrays).
+template <int MODE, int TSX, int TSY, int XS = 0>
 __global__ void __launch_bounds__(TSX *TSY + 32, 2)
     k_phase1_tma(const __grid_constant__ DevState<float> S, const __grid_constant__ TmaArgs A, int src, int dst, int kch,
                  int fcur, const __grid_constant__ XSeams X) {
@@ -948,15 +990,17 @@ inline void launch_staged_tma(const DevState<float> &S, int src, int dst, int fc
     k_phase1_tma<MODE, TSX, TSY><<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX * TSY + 32), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(
         S, A, src, dst, kch, fcur, XSeams{});
 }
-// Phase1 + stress with the x1 sweep folded in (X.tw set to TSX); false, launching nothing, when
-// the arrays do not allow the TMA form
-template <int MODE, int TSX, int TSY>
+// Phase1 + stress with the x1 sweep (XS = 1) or the x1 and x3 sweeps (XS = 3) folded in (X.tw
+// and X.kch set to the tile width and the planes per block); false, launching nothing, when the
+// arrays do not allow the TMA form
+template <int MODE, int TSX, int TSY, int XS>
 inline bool launch_staged_tma_xs(const DevState<float> &S, int src, int dst, int fcur, XSeams &X, cudaStream_t st, int kch_in) {
     TmaArgs A;
     if (!tma_args<MODE, TSX, TSY>(A, S, src, fcur)) return false;
-    X.tw = TSX;
     const int kch = kch_in > 0 ? (kch_in < S.g.C3 ? kch_in : S.g.C3) : tile_chunk<TSX, TSY>(S.g);
-    k_phase1_tma<MODE, TSX, TSY, true>
+    X.tw = TSX;
+    X.kch = kch;
+    k_phase1_tma<MODE, TSX, TSY, XS>
         <<<tile_grid<TSX, TSY>(S.g, kch), dim3(TSX * TSY + 32), TLayout<MODE, TSX, TSY>::SMEM + 128, st>>>(S, A, src, dst, kch,
                                                                                                       fcur, X);
     return true;
@@ -975,7 +1019,7 @@ inline bool launch_staged_tma_unmet(const DevState<float> &S, int src, int dst, 
                                                                                                            XSeams{});
     return true;
 }
-template <int MODE, int TSX = 64, int TSY = 4, bool XS = false> inline void prepare_staged_tma() {
+template <int MODE, int TSX = 64, int TSY = 4, int XS = 0> inline void prepare_staged_tma() {
     encode_tiled(); // looked up here, outside any stream capture
     constexpr int smem = TLayout<MODE, TSX, TSY>::SMEM + 128;
     cudaFuncSetAttribute(k_phase1_tma<MODE, TSX, TSY, XS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -308,6 +308,7 @@ struct HaloJob {
 struct XSeams {
     float *b[8], *a[10];
     int tw, n; // tile width; elements per array (bounds-checked builds)
+    int kch;   // planes per block of the launch (the chunks whose first planes' z faces are left)
 };
 __host__ __device__ inline long long seam_slots(const Geom &g, int tw) {
     return (long long)((g.C1 + tw - 1) / tw + 1) * g.C2 * g.C3;
@@ -336,10 +337,13 @@ template <class T> struct Launch {
     // faces between the cells of each tile; X.tw is set to the tile width).  Returns false,
     // launching nothing, where that form is not available (the caller runs phase1 and the x1
     // sweep instead).
+    // fold: 1 the x1 sweep, 3 the x1 and x3 sweeps (X.kch set to the planes per block)
     static bool phase1_sweep_x(const DevState<T> &S, int src, int dst, int fcur, int mode, int march, cudaStream_t st,
-                               int kch, XSeams &X);
+                               int kch, XSeams &X, int fold = 1);
     // the x faces phase1_sweep_x leaves: the tile seams and the faces beside the ghost positions
     static void sweep_x_seams(const DevState<T> &S, int con, int fcur, const XSeams &X, cudaStream_t st);
+    // the z faces it leaves with the x3 sweep folded in: below each chunk's first plane, and C3 + 1
+    static void sweep_z_seams(const DevState<T> &S, int con, int fcur, int kch, cudaStream_t st);
     static void stress(const DevState<T> &S, int con, int bulk, cudaStream_t st);
     static void use_forces(const DevState<T> &S, int ncon, cudaStream_t st);
     // x2/x3 sweeps: lines cut into balanced segments of at most `target` faces

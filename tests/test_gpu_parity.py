@@ -579,13 +579,15 @@ def test_x1_sweep_folded_into_phase1_agrees(ark, port, monkeypatch, C, px, pz):
     finishing the faces at the tiles' seams and beside the ghost positions from what the tiles
     left) gives the bits of the separate x1 sweep, on 64 x 4, 32 x 8 and 128 x 2 tiles (two,
     one and four warps per tile row), ragged and one-warp rows, one tile per line, periodic and
-    bounded x; with a Phase1 shape that cannot
-    fold ("22") form 4 runs the separate sweep."""
+    bounded x.  Form 5 folds the x3 sweep in as well (the z face below each plane but a chunk's
+    first from the thread's previous plane; the chunks' first faces and the z ends from the
+    x3 sweep's code, periodic and bounded z, single-plane grids).  With a Phase1 shape that
+    cannot fold ("22") forms 4 and 5 run the separate sweeps."""
     p = port.channel_params(*C, seed=31)
     st0 = port.channel_state(p)
     for march in ("44", "55", "66", "64", "22"):
         outs = []
-        for mode in ("0", "4"):
+        for mode in ("0", "4", "5"):
             monkeypatch.setenv("ARK_PHASE1_MARCH", march)
             monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
             P = params_from(ark, p, precision=ark.FP32)
@@ -598,23 +600,28 @@ def test_x1_sweep_folded_into_phase1_agrees(ark, port, monkeypatch, C, px, pz):
                 c.sync()
                 outs.append(c.download(CELLS + FACES))
                 names = [n for n, _ in kt]
-                folded = mode == "4" and march[0] in "456"
-                assert names == ["finalize_dt", "wrap_con", "phase1_stress_sweep_x1" if folded else "phase1_stress_forces",
-                                 "sweep_x1_seams" if folded else "sweep_x1", "sweep_x2", "sweep_x3", "phase1_forces"]
-        for n in CELLS + FACES:
-            assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), (march, n)
+                folded = mode != "0" and march[0] in "456"
+                if folded and mode == "5":
+                    assert names == ["finalize_dt", "wrap_con", "phase1_stress_sweep_x1_x3", "sweep_x1_seams", "sweep_x2",
+                                     "sweep_x3_seams", "phase1_forces"]
+                else:
+                    assert names == ["finalize_dt", "wrap_con", "phase1_stress_sweep_x1" if folded else "phase1_stress_forces",
+                                     "sweep_x1_seams" if folded else "sweep_x1", "sweep_x2", "sweep_x3", "phase1_forces"]
+        for o in outs[1:]:
+            for n in CELLS + FACES:
+                assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), (march, n)
 
 
 def test_x1_sweep_folded_with_solids(ark, port, monkeypatch):
-    """The folded x1 sweep through the face update's wall branches: the reference's stock
-    backward-facing step (solid block inside the domain, bounded axes) in FP32, form 4 against
-    form 0, on both tile shapes."""
+    """The folded x1 (and x3) sweeps through the face update's wall branches: the reference's
+    stock backward-facing step (solid block inside the domain, bounded axes) in FP32, forms 4
+    and 5 against form 0, on the three TMA tile shapes."""
     g = np.load(os.path.join(GOLD, "stock_case.npz"))
     p = json.loads(str(g["params"]))
     st = {n[5:]: np.ascontiguousarray(g[n]) for n in g.files if n.startswith("init/")}
     for march in ("44", "55", "66"):
         outs = []
-        for mode in ("0", "4"):
+        for mode in ("0", "4", "5"):
             monkeypatch.setenv("ARK_PHASE1_MARCH", march)
             monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
             gp = ark.make_params(p["C1"], p["C2"], p["C3"], vis=p["nu"], sound=p["sound"], rho0=p["rho0"], cfl=p["cfl"],
@@ -626,8 +633,34 @@ def test_x1_sweep_folded_with_solids(ark, port, monkeypatch):
                 ctx.step(int(g["steps"]))
                 ctx.sync()
                 outs.append(ctx.download(CELLS + FACES))
+        for o in outs[1:]:
+            for n in CELLS + FACES:
+                assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), (march, n)
+
+
+@pytest.mark.parametrize("march", ["44", "66"])
+def test_folded_sweeps_around_a_solid_block(ark, port, monkeypatch, march):
+    """FP32 forms 4 and 5 against form 0 in a 3-D channel with a solid block inside: fluid-solid
+    faces in x, y and z, the block's z faces inside a Phase1 chunk (the folded x3 sweep's wall
+    branches) and at nothing special, periodic x and z."""
+    p = port.channel_params(72, 16, 40, seed=37)
+    st0 = port.channel_state(p)
+    blk = (slice(10, 22), slice(5, 10), slice(20, 33)) # planes k, rows j, columns i
+    st0["condition"][blk] = 1.0
+    for n in ("u1Con", "u2Con", "u3Con", "u1nCon", "u2nCon", "u3nCon"):
+        st0[n][blk] = 0.0
+    outs = []
+    for mode in ("0", "4", "5"):
+        monkeypatch.setenv("ARK_PHASE1_MARCH", march)
+        monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
+        with ark.Context(params_from(ark, p, precision=ark.FP32)) as c:
+            c.upload(st0)
+            c.step(6)
+            c.sync()
+            outs.append(c.download(CELLS + FACES))
+    for o in outs[1:]:
         for n in CELLS + FACES:
-            assert bits_equal(port.interior(n, outs[1][n]), port.interior(n, outs[0][n])), (march, n)
+            assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), n
 
 
 def test_staging_wait_gives_up_with_status(ark, port):
