@@ -36,6 +36,7 @@ EXPORTS = ("ark_create", "ark_destroy", "ark_last_error", "ark_status_string", "
            "ark_ensemble_upload", "ark_ensemble_download", "ark_ensemble_step", "ark_ensemble_sync",
            "ark_ensemble_time_steps", "ark_ensemble_get_scalars", "ark_ensemble_mean_profile",
            "ark_ensemble_autotune", "ark_ensemble_set_shape", "ark_ensemble_kernel_times", "ark_ensemble_kernel_name",
+           "ark_ensemble_step_kernel_name",
            "ark_write_vtk", "ark_average_values", "ark_set_averaging", "ark_write_average_vtk",
            "ark_kinetic_energy", "ark_write_energy", "ark_vorticity", "ark_selftest_staging",
            "ark_closure_last_error", "ark_closure_data_create", "ark_closure_data_destroy", "ark_closure_data_size",
@@ -195,6 +196,8 @@ def lib():
         L.ark_ensemble_kernel_times.argtypes = [vp, ctypes.c_int, _DP, ctypes.c_int, ip]
         L.ark_ensemble_kernel_name.restype = ctypes.c_char_p
         L.ark_ensemble_kernel_name.argtypes = [ctypes.c_int]
+        L.ark_ensemble_step_kernel_name.restype = ctypes.c_char_p
+        L.ark_ensemble_step_kernel_name.argtypes = [vp, ctypes.c_int]
         L.ark_ensemble_get_scalars.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Scalars)]
         L.ark_ensemble_mean_profile.argtypes = [vp, ctypes.c_int, _DP, _DP]
         L.ark_ensemble_autotune.argtypes = [vp, ctypes.c_int, ip]
@@ -614,7 +617,7 @@ class Ensemble:
         ms = (ctypes.c_double * 32)()
         cnt = ctypes.c_int(0)
         self._call("ark_ensemble_kernel_times", int(nsteps), ms, 32, ctypes.byref(cnt))
-        return [(lib().ark_ensemble_kernel_name(q).decode(), ms[q]) for q in range(cnt.value)]
+        return [(lib().ark_ensemble_step_kernel_name(self.h, q).decode(), ms[q]) for q in range(cnt.value)]
 
     def scalars(self, member) -> Scalars:
         s = Scalars()

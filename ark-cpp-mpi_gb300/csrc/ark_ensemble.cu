@@ -154,7 +154,8 @@ template <int MODE> constexpr int tma_ens_smem() {
 }
 // Work items are taken from a counter (*next, zeroed before the launch) rather than in a fixed
 // stride: the items differ in cost (chunk lengths, partial tiles), so the blocks finish together.
-template <int MODE>
+// XS = 2: the x3 sweep folded in (the z faces inside each chunk; kb_sweep_z_seams does the rest).
+template <int MODE, int XS = 0>
 __global__ void __launch_bounds__(stg::NT + 32, 2) kb_phase1_tma(const DS *__restrict__ inst, const MemberMaps *__restrict__ maps,
                                                             const __grid_constant__ TmaMetas<MODE> meta, WorkList W, int src,
                                                             int dst, int fcur, int *next) {
@@ -179,9 +180,9 @@ __global__ void __launch_bounds__(stg::NT + 32, 2) kb_phase1_tma(const DS *__res
             return &M->ff;
         };
         if (narrow)
-            stg::phase1_tma_body<MODE, 32, 8>(inst[q], map, meta.m[1], true, src, dst, kch, decode(W, q, b), sm, bar);
+            stg::phase1_tma_body<MODE, 32, 8, XS>(inst[q], map, meta.m[1], true, src, dst, kch, decode(W, q, b), sm, bar, fcur);
         else
-            stg::phase1_tma_body<MODE, 64, 4>(inst[q], map, meta.m[0], true, src, dst, kch, decode(W, q, b), sm, bar);
+            stg::phase1_tma_body<MODE, 64, 4, XS>(inst[q], map, meta.m[0], true, src, dst, kch, decode(W, q, b), sm, bar, fcur);
         __syncthreads();
     }
 }
@@ -212,11 +213,27 @@ __global__ void __launch_bounds__(128, 5) kb_sweep_col(const DS *__restrict__ in
     }
 }
 
+// The z faces the x3 sweep folded into Phase1 + stress leaves (WL_ZSEAMS: per member the column
+// blocks of the x3 sweep times its chunks + 1, extra = its planes per chunk): the face below each
+// chunk's first plane and face C3 + 1, each the x3 sweep's own one-face segment (as
+// k_sweep_z_seams for one grid).
+__global__ void __launch_bounds__(128, 5) kb_sweep_z_seams(const DS *__restrict__ inst, WorkList W, int con, int fcur, int *next) {
+    __shared__ int slot;
+    for (int b = next_item(next, slot); b < W.total; b = next_item(next, slot)) {
+        const int q = find_member(W, b);
+        const int kch = W.extra[q], C3 = inst[q].g.C3, nch = (C3 + kch - 1) / kch;
+        BIx bx = decode(W, q, b);
+        bx.z = bx.z < nch ? bx.z * kch : C3;
+        sweep_col_body<float, 2>(inst[q], con, fcur, 1, bx);
+    }
+}
+
 // Kinds of work list.
 // WL_STAGED: 64 x 4 tiles of the staged Phase1 for every member; WL_STAGED_T: 32 x 8 tiles for
 // the members whose width is an odd multiple of 32 (a 64-wide tile would be half empty at
 // their end), 64 x 4 for the others.
-enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, WL_STAGED_T, WL_COUNT };
+// WL_ZSEAMS: the z faces at the staged Phase1's chunk boundaries (the x3 sweep folded in).
+enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, WL_STAGED_T, WL_ZSEAMS, WL_COUNT };
 
 // the staged Phase1 of a member of width C1 in 32 x 8 tiles (WL_STAGED_T)
 inline bool narrow_tiles(int C1) { return ((C1 + 31) / 32) % 2 == 1; }
@@ -226,7 +243,8 @@ struct Shape {
     int march_a, march_b; // Phase1 with stress / second Phase1: 0 one cell per thread, 1 marching,
                           // 2 planes staged in shared memory (cp.async copies), 4 the same with
                           // TMA tensor copies, 5 TMA with 32 x 8 tiles for the members whose
-                          // width is an odd multiple of 32
+                          // width is an odd multiple of 32; Phase1 with stress also 6 and 7:
+                          // 4 and 5 with the x3 sweep folded in
     int seg;              // target faces per thread segment in the x2/x3 sweeps
 };
 
@@ -243,6 +261,7 @@ struct ark_ensemble {
     cudaStream_t st = nullptr;
     cudaStream_t fill = nullptr; // the captured step's ghost fill, beside dt
     cudaEvent_t fill_fork = nullptr, fill_join = nullptr;
+    cudaEvent_t seam_fork = nullptr, seam_join = nullptr; // the folded x3 sweep's seams on `fill`
     double *stage = nullptr; // double staging buffer (largest member)
     // work lists: device arrays, rebuilt when the shape changes
     int4 *d_info[WL_COUNT] = {};
@@ -251,9 +270,11 @@ struct ark_ensemble {
     WrapJob *d_jobs = nullptr; // [2][n]: wrap_con for level 0/1
     int persist = 1;           // persistent blocks per launch (all SMs x resident blocks)
     int persist_staged = 1;    // the same for the staged Phase1 (2 blocks of 256 threads per SM)
-    Shape shape = {5, 5, 32}; // staged Phase1 with TMA copies for both launches, 32 x 8 tiles on odd-32 widths
+    // staged Phase1 with TMA copies for both launches, 32 x 8 tiles on odd-32 widths, the x3 sweep
+    // folded into Phase1 + stress (64 members of mixed grids: 1.341 ms per step against 1.439)
+    Shape shape = {7, 5, 32};
     MemberMaps *d_maps = nullptr;   // the members' tensor maps, [2 q + narrow] (null: the TMA form falls back)
-    int *d_next = nullptr;          // work counters: the two TMA Phase1 launches, the three sweeps (zeroed per step)
+    int *d_next = nullptr;          // work counters: the two TMA Phase1 launches, the three sweeps, the z seams (zeroed per step)
     stg::BoxMeta meta[2][2] = {};   // its boxes: [narrow][0 with the stress, 1 without]
     int con = 0, fcur = 0;
     bool parts_valid = false;
@@ -406,6 +427,12 @@ int build_lists(ark_ensemble *E) {
                 gx = (int)gr.x, gy = (int)gr.y, gz = (int)gr.z;
                 break;
             }
+            case WL_ZSEAMS: { // the staged lists' chunks (both tile kinds chunk alike)
+                const int nch = (g.C3 + kens - 1) / kens, kch = (g.C3 + nch - 1) / nch;
+                extra[q] = kch;
+                gx = col_sweep_blocks(g, 2), gz = (g.C3 + kch - 1) / kch + 1;
+                break;
+            }
             }
             info[q] = make_int4(start, gx, gy, gz);
             start += gx * gy * gz;
@@ -453,15 +480,29 @@ WorkList wl(const ark_ensemble *E, int kind) {
 
 int grid_of(const ark_ensemble *E, int kind) { return std::max(1, std::min(E->total[kind], E->persist)); }
 
+// whether a shape folds the x3 sweep into Phase1 + stress (shapes 6 and 7: 4 and 5 folded)
+inline bool folds_x3(const Shape &s) { return s.march_a == 6 || s.march_a == 7; }
+
 template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst, int fcur) {
     const dim3 blk(kTileX, kTileY);
+    const bool fold = (MODE & P1_STRESS) && (march == 6 || march == 7);
+    if (fold) march -= 2;
     if ((march == 4 || march == 5) && E->d_maps) {
         const int kind = march == 5 ? WL_STAGED_T : WL_STAGED;
         const int grid = std::max(1, std::min(E->total[kind], E->persist_staged));
         const int m = (MODE & P1_STRESS) ? 0 : 1;
         const TmaMetas<MODE> metas = {{E->meta[0][m], E->meta[1][m]}};
-        kb_phase1_tma<MODE><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(
-            E->d_inst, E->d_maps, metas, wl(E, kind), src, dst, fcur, E->d_next + ((MODE & P1_STRESS) ? 0 : 1));
+        int *next = E->d_next + ((MODE & P1_STRESS) ? 0 : 1);
+        bool done = false;
+        if constexpr ((MODE & P1_STRESS) != 0)
+            if (fold) {
+                kb_phase1_tma<MODE, 2><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(E->d_inst, E->d_maps, metas,
+                                                                                                wl(E, kind), src, dst, fcur, next);
+                done = true;
+            }
+        if (!done)
+            kb_phase1_tma<MODE><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(E->d_inst, E->d_maps, metas,
+                                                                                         wl(E, kind), src, dst, fcur, next);
     } else if (march == 2 || march == 4 || march == 5) {
         const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
         kb_phase1_staged<MODE><<<grid, dim3(stg::SX, stg::SY), stg::Layout<MODE>::SMEM, E->st>>>(
@@ -490,6 +531,10 @@ int prepare_staged_kernels(int sms) {
     per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>,
                             tma_ens_smem<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(), stg::NT + 32));
     per = std::min(per, one(kb_phase1_tma<P1_FORCES | P1_RSUM>, tma_ens_smem<P1_FORCES | P1_RSUM>(), stg::NT + 32));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_RMAX, 2>, tma_ens_smem<P1_STRESS | P1_FORCES | P1_RMAX>(),
+                            stg::NT + 32));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 2>,
+                            tma_ens_smem<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(), stg::NT + 32));
     return sms * std::max(per, 1);
 }
 
@@ -504,7 +549,7 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     auto mark = [&](int q) {
         if (ev) cudaEventRecord(ev[q], E->st);
     };
-    cudaMemsetAsync(E->d_next, 0, 5 * sizeof(int), E->st);
+    cudaMemsetAsync(E->d_next, 0, 6 * sizeof(int), E->st);
     if (!ev) { // captured: the ghost fill beside dt (independent; Phase1 waits for both)
         cudaEventRecord(E->fill_fork, E->st);
         cudaStreamWaitEvent(E->fill, E->fill_fork, 0);
@@ -524,11 +569,25 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     else
         launch_p1<P1_STRESS | P1_FORCES | P1_RMAX>(E, E->shape.march_a, y, x, fc);
     mark(2);
+    // the x3 sweep folded in: its seam faces (read by the second Phase1 only) beside the x1 and
+    // x2 sweeps when captured, in the x3 sweep's timed slot otherwise
+    const bool fold = folds_x3(E->shape) && E->d_maps, beside = fold && !ev;
+    auto zseams = [&](cudaStream_t s) {
+        kb_sweep_z_seams<<<grid_of(E, WL_ZSEAMS), 128, 0, s>>>(E->d_inst, wl(E, WL_ZSEAMS), y, fc, E->d_next + 5);
+    };
+    if (beside) {
+        cudaEventRecord(E->seam_fork, E->st);
+        cudaStreamWaitEvent(E->fill, E->seam_fork, 0);
+        zseams(E->fill);
+        cudaEventRecord(E->seam_join, E->fill);
+    }
     kb_sweep_x<<<grid_of(E, WL_SWEEPX), 128, 0, E->st>>>(E->d_inst, wl(E, WL_SWEEPX), y, fc, E->d_next + 2);
     mark(3);
     kb_sweep_col<1><<<grid_of(E, WL_COL1), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL1), y, fc, E->d_next + 3);
     mark(4);
-    kb_sweep_col<2><<<grid_of(E, WL_COL2), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL2), y, fc, E->d_next + 4);
+    if (!fold) kb_sweep_col<2><<<grid_of(E, WL_COL2), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL2), y, fc, E->d_next + 4);
+    else if (!beside) zseams(E->st);
+    if (beside) cudaStreamWaitEvent(E->st, E->seam_join, 0);
     mark(5);
     launch_p1<P1_FORCES | P1_RSUM>(E, E->shape.march_b, x, y, fc ^ 1);
     mark(6);
@@ -644,7 +703,9 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
     if (cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&E->fill, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&E->fill_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&E->fill_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&E->fill_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->seam_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->seam_join, cudaEventDisableTiming) != cudaSuccess) {
         *status = efail(ARK_ERR_CUDA, "stream creation failed");
         return nullptr;
     }
@@ -655,7 +716,7 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
     E->persist_staged = prepare_staged_kernels(sms);
     stg::encode_tiled(); // looked up here, outside any stream capture
     if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get())) || (*status = build_maps(E.get())) ||
-        (*status = ens_alloc(E.get(), &E->d_next, 5)))
+        (*status = ens_alloc(E.get(), &E->d_next, 6)))
         return nullptr;
     cudaEventCreate(&E->ev0);
     cudaEventCreate(&E->ev1);
@@ -677,6 +738,8 @@ int ark_ensemble_destroy(ark_ensemble *E) {
     }
     if (E->fill_fork) cudaEventDestroy(E->fill_fork);
     if (E->fill_join) cudaEventDestroy(E->fill_join);
+    if (E->seam_fork) cudaEventDestroy(E->seam_fork);
+    if (E->seam_join) cudaEventDestroy(E->seam_join);
     delete E;
     return ARK_OK;
 }
@@ -828,6 +891,13 @@ int ark_ensemble_time_steps(ark_ensemble *E, int nsteps, double *ms) {
 const char *ark_ensemble_kernel_name(int index) {
     return index >= 0 && index < kEnsPhases ? kEnsKernels[index] : nullptr;
 }
+// The same for the ensemble's current shape (with the x3 sweep folded in, its seam kernel in the
+// x3 sweep's place).
+const char *ark_ensemble_step_kernel_name(const ark_ensemble *E, int index) {
+    if (!E || index < 0 || index >= kEnsPhases) return nullptr;
+    if (folds_x3(E->shape) && (index == 2 || index == 5)) return index == 2 ? "phase1_stress_sweep_x3" : "sweep_x3_seams";
+    return kEnsKernels[index];
+}
 
 int ark_ensemble_kernel_times(ark_ensemble *E, int nsteps, double *ms, int cap, int *count) {
     constexpr int kPhases = kEnsPhases;
@@ -906,7 +976,8 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
     const Shape cands[] = {{1, 0, 32}, {0, 0, 32}, {1, 1, 32}, {0, 1, 32}, {1, 0, 16}, {1, 0, 64}, {0, 0, 16},
                            {0, 0, 64}, {2, 2, 32}, {2, 0, 32}, {0, 2, 32}, {2, 2, 64}, {2, 0, 64}, {4, 4, 32},
                            {4, 4, 64}, {4, 4, 16}, {4, 2, 32}, {2, 4, 32}, {4, 0, 32}, {5, 5, 32}, {5, 4, 32},
-                           {4, 5, 32}, {5, 5, 64}};
+                           {4, 5, 32}, {5, 5, 64}, {7, 5, 32}, {6, 4, 32}, {7, 4, 32}, {6, 5, 32}, {7, 5, 16},
+                           {7, 5, 64}};
     Shape best = E->shape;
     double best_ms = 1e300;
     if (int rc = ensure_parts(E)) return rc;
@@ -939,7 +1010,8 @@ int ark_ensemble_set_shape(ark_ensemble *E, int march_a, int march_b, int segmen
     if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
     if (segment < 1) return efail(ARK_ERR_PARAM, "segment < 1");
     auto ok = [](int m) { return (m >= 0 && m <= 2) || m == 4 || m == 5; };
-    if (!ok(march_a) || !ok(march_b)) return efail(ARK_ERR_PARAM, "march must be 0, 1, 2, 4 or 5");
+    if (!(ok(march_a) || march_a == 6 || march_a == 7) || !ok(march_b))
+        return efail(ARK_ERR_PARAM, "march must be 0, 1, 2, 4 or 5 (and 6 or 7 for the Phase1 with stress)");
     E->shape = Shape{march_a, march_b, segment};
     drop_graphs(E);
     return build_lists(E);

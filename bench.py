@@ -59,7 +59,8 @@ ALGO_VALUES_FP32 = dict(ALGO_VALUES, phase1_stress_forces=(23, 1), phase1_forces
                         phase2_phase1_forces=(39, 1),
                         # Phase1 + stress with the x1 sweep folded in: its 23 values plus the 4 new
                         # x faces (and the 4 new z faces with the x3 sweep too)
-                        phase1_stress_sweep_x1=(27, 1), phase1_stress_sweep_x1_x3=(31, 1))
+                        phase1_stress_sweep_x1=(27, 1), phase1_stress_sweep_x1_x3=(31, 1),
+                        phase1_stress_sweep_x3=(27, 1))
 # Persistent state per cell: cell rho,u1,u2,u3 + 3 face sets x {p,u1,u2,u3}; read and
 # written once per step (the step's algorithmic bytes).
 STEP_VALUES = 2 * 16
