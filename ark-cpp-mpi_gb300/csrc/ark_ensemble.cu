@@ -154,15 +154,19 @@ template <int MODE> constexpr int tma_ens_smem() {
 }
 // Work items are taken from a counter (*next, zeroed before the launch) rather than in a fixed
 // stride: the items differ in cost (chunk lengths, partial tiles), so the blocks finish together.
-// XS = 2: the x3 sweep folded in (the z faces inside each chunk; kb_sweep_z_seams does the rest).
+// XS: the sweeps folded in (2: the x3 sweep, the z faces inside each chunk, kb_sweep_z_seams doing
+// the rest; 3: the x1 sweep too, with the member's seam arrays seams[q] for kb_sweep_x_seams).
 template <int MODE, int XS = 0>
 __global__ void __launch_bounds__(stg::NT + 32, 2) kb_phase1_tma(const DS *__restrict__ inst, const MemberMaps *__restrict__ maps,
                                                             const __grid_constant__ TmaMetas<MODE> meta, WorkList W, int src,
-                                                            int dst, int fcur, int *next) {
+                                                            int dst, int fcur, int *next, const XSeams *__restrict__ seams) {
     constexpr bool STRESS = (MODE & P1_STRESS) != 0;
-    static_assert(stg::TLayout<MODE, 64, 4>::NS == stg::TLayout<MODE, 32, 8>::NS, "one ring depth for both tiles");
+    constexpr int NS = stg::TLayout<MODE, 64, 4>::NS;
+    static_assert(NS == stg::TLayout<MODE, 32, 8>::NS, "one ring depth for both tiles");
     extern __shared__ __align__(128) unsigned char sm_raw[];
     __shared__ __align__(8) unsigned long long bar[2 * stg::TLayout<MODE>::NS + 1];
+    // the x1 sweep's hand-over slots between the two warps of a 64-wide tile row
+    __shared__ __align__(8) unsigned char xh_raw[(XS & 1) ? sizeof(stg::XHand<64, 4, NS>) : 8];
     __shared__ int item;
     unsigned char *const sm = stg::align128(sm_raw);
     for (;;) {
@@ -179,10 +183,13 @@ __global__ void __launch_bounds__(stg::NT + 32, 2) kb_phase1_tma(const DS *__res
             if (k <= 4) return &M->fc[fcur][k - 2];
             return &M->ff;
         };
+        const XSeams *X = (XS & 1) ? &seams[q] : nullptr;
         if (narrow)
-            stg::phase1_tma_body<MODE, 32, 8, XS>(inst[q], map, meta.m[1], true, src, dst, kch, decode(W, q, b), sm, bar, fcur);
+            stg::phase1_tma_body<MODE, 32, 8, XS>(inst[q], map, meta.m[1], true, src, dst, kch, decode(W, q, b), sm, bar, fcur, X,
+                                                  reinterpret_cast<stg::XHand<32, 8, NS> *>(xh_raw));
         else
-            stg::phase1_tma_body<MODE, 64, 4, XS>(inst[q], map, meta.m[0], true, src, dst, kch, decode(W, q, b), sm, bar, fcur);
+            stg::phase1_tma_body<MODE, 64, 4, XS>(inst[q], map, meta.m[0], true, src, dst, kch, decode(W, q, b), sm, bar, fcur, X,
+                                                  reinterpret_cast<stg::XHand<64, 4, NS> *>(xh_raw));
         __syncthreads();
     }
 }
@@ -213,6 +220,17 @@ __global__ void __launch_bounds__(128, 5) kb_sweep_col(const DS *__restrict__ in
     }
 }
 
+// The x faces the x1 sweep folded into Phase1 + stress leaves (WL_XSEAMS: per member its seam
+// slots in blocks of 128, seams[q] its seam arrays), as k_sweep_x_seams for one grid.
+__global__ void __launch_bounds__(128) kb_sweep_x_seams(const DS *__restrict__ inst, const XSeams *__restrict__ seams, WorkList W,
+                                                        int con, int fcur, int *next) {
+    __shared__ int slot;
+    for (int b = next_item(next, slot); b < W.total; b = next_item(next, slot)) {
+        const int q = find_member(W, b);
+        sweep_x_seams_body<float>(inst[q], con, fcur, seams[q], (b - W.info[q].x) * 128 + (int)threadIdx.x);
+    }
+}
+
 // The z faces the x3 sweep folded into Phase1 + stress leaves (WL_ZSEAMS: per member the column
 // blocks of the x3 sweep times its chunks + 1, extra = its planes per chunk): the face below each
 // chunk's first plane and face C3 + 1, each the x3 sweep's own one-face segment (as
@@ -232,8 +250,9 @@ __global__ void __launch_bounds__(128, 5) kb_sweep_z_seams(const DS *__restrict_
 // WL_STAGED: 64 x 4 tiles of the staged Phase1 for every member; WL_STAGED_T: 32 x 8 tiles for
 // the members whose width is an odd multiple of 32 (a 64-wide tile would be half empty at
 // their end), 64 x 4 for the others.
-// WL_ZSEAMS: the z faces at the staged Phase1's chunk boundaries (the x3 sweep folded in).
-enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, WL_STAGED_T, WL_ZSEAMS, WL_COUNT };
+// WL_ZSEAMS: the z faces at the staged Phase1's chunk boundaries (the x3 sweep folded in);
+// WL_XSEAMS: the x faces at its tile seams (the x1 sweep folded in).
+enum { WL_TILES = 0, WL_CELLS, WL_SWEEPX, WL_COL1, WL_COL2, WL_WRAP, WL_STAGED, WL_STAGED_T, WL_ZSEAMS, WL_XSEAMS, WL_COUNT };
 
 // the staged Phase1 of a member of width C1 in 32 x 8 tiles (WL_STAGED_T)
 inline bool narrow_tiles(int C1) { return ((C1 + 31) / 32) % 2 == 1; }
@@ -244,7 +263,8 @@ struct Shape {
                           // 2 planes staged in shared memory (cp.async copies), 4 the same with
                           // TMA tensor copies, 5 TMA with 32 x 8 tiles for the members whose
                           // width is an odd multiple of 32; Phase1 with stress also 6 and 7:
-                          // 4 and 5 with the x3 sweep folded in
+                          // 4 and 5 with the x3 sweep folded in, 8 and 9: with the x1 and x3
+                          // sweeps folded in
     int seg;              // target faces per thread segment in the x2/x3 sweeps
 };
 
@@ -261,7 +281,9 @@ struct ark_ensemble {
     cudaStream_t st = nullptr;
     cudaStream_t fill = nullptr; // the captured step's ghost fill, beside dt
     cudaEvent_t fill_fork = nullptr, fill_join = nullptr;
-    cudaEvent_t seam_fork = nullptr, seam_join = nullptr; // the folded x3 sweep's seams on `fill`
+    cudaEvent_t seam_fork = nullptr, seam_join = nullptr; // the folded sweeps' seams on `fill`
+    std::vector<XSeams> seams; // the members' seam arrays for the folded x1 sweep (tw per shape)
+    XSeams *d_seams = nullptr;
     double *stage = nullptr; // double staging buffer (largest member)
     // work lists: device arrays, rebuilt when the shape changes
     int4 *d_info[WL_COUNT] = {};
@@ -274,7 +296,7 @@ struct ark_ensemble {
     // folded into Phase1 + stress (64 members of mixed grids: 1.341 ms per step against 1.439)
     Shape shape = {7, 5, 32};
     MemberMaps *d_maps = nullptr;   // the members' tensor maps, [2 q + narrow] (null: the TMA form falls back)
-    int *d_next = nullptr;          // work counters: the two TMA Phase1 launches, the three sweeps, the z seams (zeroed per step)
+    int *d_next = nullptr;          // work counters: the two TMA Phase1 launches, the three sweeps, the z and x seams (zeroed per step)
     stg::BoxMeta meta[2][2] = {};   // its boxes: [narrow][0 with the stress, 1 without]
     int con = 0, fcur = 0;
     bool parts_valid = false;
@@ -370,6 +392,13 @@ int segment_for(int nd, int target) {
     return (nd + ns - 1) / ns;
 }
 
+// The x1 sweep's tile width for a member under a shape: 32 where the shape stages the member's
+// planes in 32 x 8 tiles (shapes 5, 7, 9 on odd-32 widths), else 64.
+int seam_width(const Shape &s, const Geom &g) {
+    const bool t = s.march_a == 5 || s.march_a == 7 || s.march_a == 9;
+    return t && narrow_tiles(g.C1) ? 32 : 64;
+}
+
 // Builds the work lists for the current shape.
 int build_lists(ark_ensemble *E) {
     // Planes per staged Phase1 block, sized over the whole ensemble (about four waves of two
@@ -433,6 +462,9 @@ int build_lists(ark_ensemble *E) {
                 gx = col_sweep_blocks(g, 2), gz = (g.C3 + kch - 1) / kch + 1;
                 break;
             }
+            case WL_XSEAMS: // the seam slots of the member's tile width, 128 per block
+                gx = (int)((seam_slots(g, seam_width(E->shape, g)) + 127) / 128);
+                break;
             }
             info[q] = make_int4(start, gx, gy, gz);
             start += gx * gy * gz;
@@ -444,6 +476,10 @@ int build_lists(ark_ensemble *E) {
         }
         ENS_CUDA(cudaMemcpy(E->d_info[kind], info.data(), sizeof(int4) * E->n, cudaMemcpyHostToDevice));
         ENS_CUDA(cudaMemcpy(E->d_extra[kind], extra.data(), sizeof(int) * E->n, cudaMemcpyHostToDevice));
+    }
+    if (E->d_seams) { // the tile width of each member's seams under this shape
+        for (int q = 0; q < E->n; ++q) E->seams[q].tw = seam_width(E->shape, E->S[q].g);
+        ENS_CUDA(cudaMemcpy(E->d_seams, E->seams.data(), sizeof(XSeams) * E->n, cudaMemcpyHostToDevice));
     }
     return ARK_OK;
 }
@@ -480,13 +516,14 @@ WorkList wl(const ark_ensemble *E, int kind) {
 
 int grid_of(const ark_ensemble *E, int kind) { return std::max(1, std::min(E->total[kind], E->persist)); }
 
-// whether a shape folds the x3 sweep into Phase1 + stress (shapes 6 and 7: 4 and 5 folded)
-inline bool folds_x3(const Shape &s) { return s.march_a == 6 || s.march_a == 7; }
+// whether a shape folds the x3 sweep (shapes 6 to 9) or the x1 sweep too (8, 9) into Phase1 + stress
+inline bool folds_x3(const Shape &s) { return s.march_a >= 6 && s.march_a <= 9; }
+inline bool folds_x1(const Shape &s) { return s.march_a == 8 || s.march_a == 9; }
 
 template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst, int fcur) {
     const dim3 blk(kTileX, kTileY);
-    const bool fold = (MODE & P1_STRESS) && (march == 6 || march == 7);
-    if (fold) march -= 2;
+    const bool fold = (MODE & P1_STRESS) && march >= 6 && march <= 9, fold1 = fold && march >= 8 && E->d_seams;
+    if (fold) march -= march >= 8 ? 4 : 2;
     if ((march == 4 || march == 5) && E->d_maps) {
         const int kind = march == 5 ? WL_STAGED_T : WL_STAGED;
         const int grid = std::max(1, std::min(E->total[kind], E->persist_staged));
@@ -496,13 +533,17 @@ template <int MODE> void launch_p1(ark_ensemble *E, int march, int src, int dst,
         bool done = false;
         if constexpr ((MODE & P1_STRESS) != 0)
             if (fold) {
-                kb_phase1_tma<MODE, 2><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(E->d_inst, E->d_maps, metas,
-                                                                                                wl(E, kind), src, dst, fcur, next);
+                if (fold1)
+                    kb_phase1_tma<MODE, 3><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(
+                        E->d_inst, E->d_maps, metas, wl(E, kind), src, dst, fcur, next, E->d_seams);
+                else
+                    kb_phase1_tma<MODE, 2><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(
+                        E->d_inst, E->d_maps, metas, wl(E, kind), src, dst, fcur, next, nullptr);
                 done = true;
             }
         if (!done)
             kb_phase1_tma<MODE><<<grid, dim3(stg::NT + 32), tma_ens_smem<MODE>(), E->st>>>(E->d_inst, E->d_maps, metas,
-                                                                                         wl(E, kind), src, dst, fcur, next);
+                                                                                         wl(E, kind), src, dst, fcur, next, nullptr);
     } else if (march == 2 || march == 4 || march == 5) {
         const int grid = std::max(1, std::min(E->total[WL_STAGED], E->persist_staged));
         kb_phase1_staged<MODE><<<grid, dim3(stg::SX, stg::SY), stg::Layout<MODE>::SMEM, E->st>>>(
@@ -535,6 +576,10 @@ int prepare_staged_kernels(int sms) {
                             stg::NT + 32));
     per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 2>,
                             tma_ens_smem<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(), stg::NT + 32));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_RMAX, 3>, tma_ens_smem<P1_STRESS | P1_FORCES | P1_RMAX>(),
+                            stg::NT + 32));
+    per = std::min(per, one(kb_phase1_tma<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX, 3>,
+                            tma_ens_smem<P1_STRESS | P1_FORCES | P1_BULK | P1_RMAX>(), stg::NT + 32));
     return sms * std::max(per, 1);
 }
 
@@ -549,7 +594,7 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     auto mark = [&](int q) {
         if (ev) cudaEventRecord(ev[q], E->st);
     };
-    cudaMemsetAsync(E->d_next, 0, 6 * sizeof(int), E->st);
+    cudaMemsetAsync(E->d_next, 0, 7 * sizeof(int), E->st);
     if (!ev) { // captured: the ghost fill beside dt (independent; Phase1 waits for both)
         cudaEventRecord(E->fill_fork, E->st);
         cudaStreamWaitEvent(E->fill, E->fill_fork, 0);
@@ -569,19 +614,25 @@ void ens_step(ark_ensemble *E, int x, int fc, cudaEvent_t *ev) {
     else
         launch_p1<P1_STRESS | P1_FORCES | P1_RMAX>(E, E->shape.march_a, y, x, fc);
     mark(2);
-    // the x3 sweep folded in: its seam faces (read by the second Phase1 only) beside the x1 and
-    // x2 sweeps when captured, in the x3 sweep's timed slot otherwise
-    const bool fold = folds_x3(E->shape) && E->d_maps, beside = fold && !ev;
+    // the x3 (and x1) sweeps folded in: their seam faces (read by the second Phase1 only) beside
+    // the remaining sweeps when captured, in the folded sweeps' timed slots otherwise
+    const bool fold = folds_x3(E->shape) && E->d_maps, fold1 = fold && folds_x1(E->shape) && E->d_seams;
+    const bool beside = fold && !ev;
     auto zseams = [&](cudaStream_t s) {
         kb_sweep_z_seams<<<grid_of(E, WL_ZSEAMS), 128, 0, s>>>(E->d_inst, wl(E, WL_ZSEAMS), y, fc, E->d_next + 5);
+    };
+    auto xseams = [&](cudaStream_t s) {
+        kb_sweep_x_seams<<<grid_of(E, WL_XSEAMS), 128, 0, s>>>(E->d_inst, E->d_seams, wl(E, WL_XSEAMS), y, fc, E->d_next + 6);
     };
     if (beside) {
         cudaEventRecord(E->seam_fork, E->st);
         cudaStreamWaitEvent(E->fill, E->seam_fork, 0);
+        if (fold1) xseams(E->fill);
         zseams(E->fill);
         cudaEventRecord(E->seam_join, E->fill);
     }
-    kb_sweep_x<<<grid_of(E, WL_SWEEPX), 128, 0, E->st>>>(E->d_inst, wl(E, WL_SWEEPX), y, fc, E->d_next + 2);
+    if (!fold1) kb_sweep_x<<<grid_of(E, WL_SWEEPX), 128, 0, E->st>>>(E->d_inst, wl(E, WL_SWEEPX), y, fc, E->d_next + 2);
+    else if (!beside) xseams(E->st);
     mark(3);
     kb_sweep_col<1><<<grid_of(E, WL_COL1), 128, 0, E->st>>>(E->d_inst, wl(E, WL_COL1), y, fc, E->d_next + 3);
     mark(4);
@@ -700,6 +751,24 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
         return nullptr;
     }
     if ((*status = ens_alloc(E.get(), &E->stage, maxf))) return nullptr;
+    { // the members' seam arrays for the folded x1 sweep (slots for any tile width; build_lists sets tw)
+        size_t tot = 0;
+        for (int q = 0; q < n; ++q) tot += 18 * (size_t)seam_slots(E->S[q].g, 32);
+        float *pool = nullptr;
+        if ((*status = ens_alloc(E.get(), &pool, tot))) return nullptr;
+        E->seams.assign(n, XSeams{});
+        size_t off = 0;
+        for (int q = 0; q < n; ++q) {
+            const size_t ns = (size_t)seam_slots(E->S[q].g, 32);
+            XSeams &X = E->seams[q];
+            for (int a = 0; a < 8; ++a) X.b[a] = pool + off + a * ns;
+            for (int a = 0; a < 10; ++a) X.a[a] = pool + off + (8 + a) * ns;
+            X.n = (int)ns;
+            X.tw = 64;
+            off += 18 * ns;
+        }
+        if ((*status = ens_alloc(E.get(), &E->d_seams, (size_t)n))) return nullptr;
+    }
     if (cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&E->fill, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&E->fill_fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -716,7 +785,7 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
     E->persist_staged = prepare_staged_kernels(sms);
     stg::encode_tiled(); // looked up here, outside any stream capture
     if ((*status = build_lists(E.get())) || (*status = build_jobs(E.get())) || (*status = build_maps(E.get())) ||
-        (*status = ens_alloc(E.get(), &E->d_next, 6)))
+        (*status = ens_alloc(E.get(), &E->d_next, 7)))
         return nullptr;
     cudaEventCreate(&E->ev0);
     cudaEventCreate(&E->ev1);
@@ -895,6 +964,7 @@ const char *ark_ensemble_kernel_name(int index) {
 // x3 sweep's place).
 const char *ark_ensemble_step_kernel_name(const ark_ensemble *E, int index) {
     if (!E || index < 0 || index >= kEnsPhases) return nullptr;
+    if (folds_x1(E->shape) && (index == 2 || index == 3)) return index == 2 ? "phase1_stress_sweep_x1_x3" : "sweep_x1_seams";
     if (folds_x3(E->shape) && (index == 2 || index == 5)) return index == 2 ? "phase1_stress_sweep_x3" : "sweep_x3_seams";
     return kEnsKernels[index];
 }
@@ -977,7 +1047,7 @@ int ark_ensemble_autotune(ark_ensemble *E, int steps_per_candidate, int *choice)
                            {0, 0, 64}, {2, 2, 32}, {2, 0, 32}, {0, 2, 32}, {2, 2, 64}, {2, 0, 64}, {4, 4, 32},
                            {4, 4, 64}, {4, 4, 16}, {4, 2, 32}, {2, 4, 32}, {4, 0, 32}, {5, 5, 32}, {5, 4, 32},
                            {4, 5, 32}, {5, 5, 64}, {7, 5, 32}, {6, 4, 32}, {7, 4, 32}, {6, 5, 32}, {7, 5, 16},
-                           {7, 5, 64}};
+                           {7, 5, 64}, {9, 5, 32}, {8, 4, 32}, {9, 4, 32}, {9, 5, 64}};
     Shape best = E->shape;
     double best_ms = 1e300;
     if (int rc = ensure_parts(E)) return rc;
@@ -1010,8 +1080,8 @@ int ark_ensemble_set_shape(ark_ensemble *E, int march_a, int march_b, int segmen
     if (!E) return efail(ARK_ERR_PARAM, "ensemble is NULL");
     if (segment < 1) return efail(ARK_ERR_PARAM, "segment < 1");
     auto ok = [](int m) { return (m >= 0 && m <= 2) || m == 4 || m == 5; };
-    if (!(ok(march_a) || march_a == 6 || march_a == 7) || !ok(march_b))
-        return efail(ARK_ERR_PARAM, "march must be 0, 1, 2, 4 or 5 (and 6 or 7 for the Phase1 with stress)");
+    if (!(ok(march_a) || (march_a >= 6 && march_a <= 9)) || !ok(march_b))
+        return efail(ARK_ERR_PARAM, "march must be 0, 1, 2, 4 or 5 (and 6 to 9 for the Phase1 with stress)");
     E->shape = Shape{march_a, march_b, segment};
     drop_graphs(E);
     return build_lists(E);

@@ -1848,13 +1848,12 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 3)
 // and so are their extrapolations when the old faces 1 and C1 + 1 agree bit for bit (as every
 // step leaves them: the two faces are one, updated from the same values); otherwise the ghost
 // position's extrapolation is computed here as k_sweep_x computes it, from the cell and the
-// faces it stands for (xcell, xface).  One thread per face, the seams of a line side by side.
+// faces it stands for (xcell, xface).  One thread per face (id < seam_slots(g, tw)), the seams of
+// a line side by side.
 template <class T>
-__global__ void __launch_bounds__(256) k_sweep_x_seams(const __grid_constant__ DevState<T> S, int con, int fcur,
-                                                       const __grid_constant__ XSeams X) {
+__device__ __forceinline__ void sweep_x_seams_body(const DevState<T> &S, int con, int fcur, const XSeams &X, int id) {
     const Geom g = S.g;
     const int rows = g.C2 * g.C3, nb = (g.C1 + X.tw - 1) / X.tw;
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= rows * (nb + 1)) return;
     const int row = id / (nb + 1), b = id - row * (nb + 1);
     const int j = row % g.C2 + 1, k = row / g.C2 + 1;
@@ -1905,6 +1904,11 @@ __global__ void __launch_bounds__(256) k_sweep_x_seams(const __grid_constant__ D
     const FaceOut<T> W = sweep_out(S, fcur, 0);
     face_store(W, ARK_CK(g.fi(s, j, k), W.nf),
                face_values_v<T, false>(V, flb, flf, X.b[3][wb], X.a[3][wa], prev, cur, X.a[8][w], X.a[9][w], q));
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_sweep_x_seams(const __grid_constant__ DevState<T> S, int con, int fcur,
+                                                       const __grid_constant__ XSeams X) {
+    sweep_x_seams_body<T>(S, con, fcur, X, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // x2 (AX = 1) and x3 (AX = 2) sweeps: one thread per segment of `seg` faces of a line,

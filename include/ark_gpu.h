@@ -373,20 +373,22 @@ int ark_ensemble_kernel_times(ark_ensemble *ens, int nsteps, double *ms, int cap
 /* The name of launch `index` of an ensemble step (NULL past the last). */
 const char *ark_ensemble_kernel_name(int index);
 /* The same for the ensemble's current shape: with the x3 sweep folded into Phase1 + stress
- * (shapes 6 and 7), "phase1_stress_sweep_x3" and "sweep_x3_seams" in launches 2 and 5. */
+ * (shapes 6 and 7), "phase1_stress_sweep_x3" and "sweep_x3_seams" in launches 2 and 5; with the
+ * x1 sweep too (8 and 9), "phase1_stress_sweep_x1_x3" and "sweep_x1_seams" in launches 2 and 3. */
 const char *ark_ensemble_step_kernel_name(const ark_ensemble *ens, int index);
 int ark_ensemble_get_scalars(ark_ensemble *ens, int member, ark_scalars *out);
 int ark_ensemble_mean_profile(ark_ensemble *ens, int member, double *mean_u1, double *wall_shear);
 /* Times each candidate kernel shape (for each Phase1: 0 one cell per thread, 1 marching, 2 planes
  * staged in shared memory with cp.async copies, 4 the same with TMA tensor copies, 5 TMA with
  * 32 x 8 tiles for the members whose width is an odd multiple of 32; for the Phase1 with stress
- * also 6 and 7, shapes 4 and 5 with the x3 sweep folded in; the x2/x3 sweep segment
+ * also 6 and 7, shapes 4 and 5 with the x3 sweep folded in, and 8 and 9, with the x1 and x3
+ * sweeps folded in; the x2/x3 sweep segment
  * length) for steps_per_candidate steps on the
  * live state -- the results do not depend on the shape -- and keeps the fastest.  choice (4
  * ints, or NULL): {Phase1+stress shape, second Phase1 shape, segment target, microseconds per
  * step}. */
 int ark_ensemble_autotune(ark_ensemble *ens, int steps_per_candidate, int *choice);
-/* Sets the kernel shape directly (march_a: 0, 1, 2, 4, 5, 6 or 7, march_b: 0, 1, 2, 4 or 5 as
+/* Sets the kernel shape directly (march_a: 0, 1, 2 or 4 to 9, march_b: 0, 1, 2, 4 or 5 as
  * above).  Until this or ark_ensemble_autotune is called, an ensemble uses 7, 5 and 32-face
  * segments. */
 int ark_ensemble_set_shape(ark_ensemble *ens, int march_a, int march_b, int segment);

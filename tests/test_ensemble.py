@@ -52,13 +52,14 @@ def test_ensemble_matches_single_contexts(ark, port):
 
 
 @pytest.mark.parametrize("shape", [(2, 2, 32), (2, 0, 16), (0, 2, 64), (1, 2, 32), (4, 4, 32), (4, 2, 16), (1, 4, 64),
-                                   (5, 5, 32), (5, 4, 16), (7, 5, 32), (6, 4, 16), (7, 0, 64)])
+                                   (5, 5, 32), (5, 4, 16), (7, 5, 32), (6, 4, 16), (7, 0, 64), (9, 5, 32), (8, 4, 16),
+                                   (9, 2, 64)])
 def test_ensemble_shapes_match_single_contexts(ark, port, shape):
     """Every Phase1 shape (one cell per thread, marching, planes staged in shared memory with
     cp.async or TMA tensor copies, 64 x 4 tiles or 32 x 8 for the members whose width is an odd
     multiple of 32: a persistent kernel over every member's tiles; with the x3 sweep folded into
-    Phase1 + stress, shapes 6 and 7, and its seam faces by their own persistent kernel) gives each
-    member the single-context bits."""
+    Phase1 + stress, shapes 6 and 7, or the x1 and x3 sweeps, 8 and 9, and their seam faces by
+    their own persistent kernels) gives each member the single-context bits."""
     mem = members(ark)
     want = singles(ark, mem, 5)
     with ark.Ensemble([p for p, _ in mem]) as E:
@@ -84,9 +85,10 @@ def test_ensemble_autotune_keeps_results(ark, port):
         choice = E.autotune(1)
         assert choice["segment"] in (16, 32, 64)
         kt = E.kernel_times(2)
-        folded = choice["march_phase1_stress"] in (6, 7)
-        assert [n for n, _ in kt] == ["finalize_dt", "wrap_con", "phase1_stress_sweep_x3" if folded else "phase1_stress_forces",
-                                      "sweep_x1", "sweep_x2", "sweep_x3_seams" if folded else "sweep_x3", "phase1_forces"]
+        a = choice["march_phase1_stress"]
+        p1 = "phase1_stress_sweep_x1_x3" if a in (8, 9) else "phase1_stress_sweep_x3" if a in (6, 7) else "phase1_stress_forces"
+        assert [n for n, _ in kt] == ["finalize_dt", "wrap_con", p1, "sweep_x1_seams" if a in (8, 9) else "sweep_x1", "sweep_x2",
+                                      "sweep_x3_seams" if a in (6, 7, 8, 9) else "sweep_x3", "phase1_forces"]
         assert all(ms > 0 for _, ms in kt)
         done = E.scalars(0).nstep
         E.sync()
