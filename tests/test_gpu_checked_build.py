@@ -72,6 +72,7 @@ SMALL_GRID_TESTS = [
     "tests/test_gpu_parity.py::test_x1_sweep_folded_into_phase1_agrees",
     "tests/test_gpu_parity.py::test_x1_sweep_folded_with_solids",
     "tests/test_gpu_parity.py::test_folded_sweeps_around_a_solid_block",
+    "tests/test_gpu_parity.py::test_folded_x1_sweep_with_distinct_periodic_end_faces",
     "tests/test_gpu_slabs.py",
     "tests/test_ensemble.py",
     "tests/test_gpu_closure.py",

@@ -663,6 +663,31 @@ def test_folded_sweeps_around_a_solid_block(ark, port, monkeypatch, march):
             assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), n
 
 
+@pytest.mark.parametrize("march", ["44", "66"])
+def test_folded_x1_sweep_with_distinct_periodic_end_faces(ark, port, monkeypatch, march):
+    """A periodic-x state whose x faces 1 and C1 + 1 differ: the two stored images of one face,
+    which every step leaves equal but an uploaded state need not.  The seam kernel then computes
+    the ghost positions' extrapolations from the cells and faces they stand for (its path when
+    the images differ); forms 4 and 5 against form 0."""
+    p = port.channel_params(70, 12, 20, seed=41)
+    st0 = port.channel_state(p)
+    rng = np.random.default_rng(5)
+    for n in ("p1", "u11", "u21", "u31"):
+        st0[n][1:-2, 1:-2, 1] += 0.01 * rng.standard_normal(st0[n][1:-2, 1:-2, 1].shape)
+    outs = []
+    for mode in ("0", "4", "5"):
+        monkeypatch.setenv("ARK_PHASE1_MARCH", march)
+        monkeypatch.setenv("ARK_PHASE2_FUSED", mode)
+        with ark.Context(params_from(ark, p, precision=ark.FP32)) as c:
+            c.upload(st0)
+            c.step(4)
+            c.sync()
+            outs.append(c.download(CELLS + FACES))
+    for o in outs[1:]:
+        for n in CELLS + FACES:
+            assert bits_equal(port.interior(n, o[n]), port.interior(n, outs[0][n])), n
+
+
 def test_staging_wait_gives_up_with_status(ark, port):
     """The TMA-staged Phase1's waits are bounded: a launch whose planes expect more bytes than
     their copies bring makes every block give up after half a second, report STATUS_STAGING
