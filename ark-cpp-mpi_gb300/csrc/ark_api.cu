@@ -719,9 +719,11 @@ ark_ctx *ark_create(const ark_params *params, int *status) {
         // 512x256x256 the step takes 1.980 ms against 2.130 with the x1 sweep alone folded in
         // (form 4) and 2.210 with the separate sweeps (form 0); Phase1 + stress with both sweeps
         // 1.032 ms and the seams 0.055 + 0.029 ms, against 0.538 + 0.421 + 0.374 for the three
-        // kernels.  On 64 x 4 tiles: 2.012 ms
+        // kernels.  On 64 x 4 tiles: 2.012 ms.  Smaller grids (form 5 on 64 x 4 / 128 x 2 tiles
+        // against form 0, ms per step): 256x128x128 0.329 / 0.324 against 0.353, 128x64x64
+        // 0.0606 / 0.0595 against 0.0734, 64x48x48 0.0451 / 0.0461 against 0.0522
         ctx->p2mode = 5;
-        if (params->n1_cells >= 256) ctx->march[0] = 6;
+        if (params->n1_cells >= 128) ctx->march[0] = 6;
     }
     // x2/x3 segments: 20 faces for FP64 (0.531 / 0.508 -> 0.513 / 0.492 ms at 256x128x128 against
     // 32), 16 for FP32 (what the autotuner picks at 512x256x256)
