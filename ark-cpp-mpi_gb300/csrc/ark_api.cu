@@ -250,10 +250,10 @@ template <class T> struct EngineT : Engine {
             // the seam arrays of Phase1 + stress with the x1 sweep folded in (any tile width)
             const size_t ns = (size_t)seam_slots(S.g, 32);
             float *sb = nullptr;
-            rc |= get(&sb, 18 * ns);
+            rc |= get(&sb, 20 * ns);
             if (sb) {
                 for (int q = 0; q < 8; ++q) seams.b[q] = sb + q * ns;
-                for (int q = 0; q < 10; ++q) seams.a[q] = sb + (8 + q) * ns;
+                for (int q = 0; q < 12; ++q) seams.a[q] = sb + (8 + q) * ns;
                 seams.n = (int)ns;
             }
         }

@@ -753,7 +753,7 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
     if ((*status = ens_alloc(E.get(), &E->stage, maxf))) return nullptr;
     { // the members' seam arrays for the folded x1 sweep (slots for any tile width; build_lists sets tw)
         size_t tot = 0;
-        for (int q = 0; q < n; ++q) tot += 18 * (size_t)seam_slots(E->S[q].g, 32);
+        for (int q = 0; q < n; ++q) tot += 20 * (size_t)seam_slots(E->S[q].g, 32);
         float *pool = nullptr;
         if ((*status = ens_alloc(E.get(), &pool, tot))) return nullptr;
         E->seams.assign(n, XSeams{});
@@ -762,10 +762,10 @@ ark_ensemble *ark_ensemble_create(const ark_params *params, int n, int *status) 
             const size_t ns = (size_t)seam_slots(E->S[q].g, 32);
             XSeams &X = E->seams[q];
             for (int a = 0; a < 8; ++a) X.b[a] = pool + off + a * ns;
-            for (int a = 0; a < 10; ++a) X.a[a] = pool + off + (8 + a) * ns;
+            for (int a = 0; a < 12; ++a) X.a[a] = pool + off + (8 + a) * ns;
             X.n = (int)ns;
             X.tw = 64;
-            off += 18 * ns;
+            off += 20 * ns;
         }
         if ((*status = ens_alloc(E.get(), &E->d_seams, (size_t)n))) return nullptr;
     }

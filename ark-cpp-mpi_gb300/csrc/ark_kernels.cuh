@@ -1871,10 +1871,13 @@ __device__ __forceinline__ void sweep_x_seams_body(const DevState<T> &S, int con
     cur.bb = X.a[2][wa];
     const SweepK<T> q = sweep_consts(S, 0);
     if (px && (b == 0 || b == nb)) {
-        const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
-        const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k), f1 = ARK_CK(f0 + 1, R.nf), fe = ARK_CK(f0 + g.C1 + 1, R.nf);
-        auto same = [](T u, T v) { return __float_as_int(u) == __float_as_int(v); };
-        if (!(same(R.FN[f1], R.FN[fe]) && same(R.FA[f1], R.FA[fe]) && same(R.FB[f1], R.FB[fe]) && same(R.FP[f1], R.FP[fe]))) {
+        // faces 1 and C1 + 1 (u2, u3, u1, p) as the tiles holding cells 1 and C1 left them in
+        // slots 0 and nb
+        const int w0 = ARK_CK(w - b, X.n), we = ARK_CK(w - b + nb, X.n);
+        auto same = [&](int a) { return __float_as_int(X.a[a][w0]) == __float_as_int(X.a[a][we]); };
+        if (!(same(8) && same(9) && same(10) && same(11))) {
+            const SweepSrc<T> R = sweep_src(S, con, fcur, 0);
+            const int c0 = g.ci(0, j, k), f0 = g.fi(0, j, k);
             const bool lo = b == 0; // ghost position 0 (cell C1; faces 1 ahead, C1 behind) or C1 + 1
             const int c = ARK_CK(c0 + (lo ? g.C1 : 1), R.nc);
             const int ff = ARK_CK(f0 + (lo ? 1 : 2), R.nf), fb = ARK_CK(f0 + (lo ? g.C1 : g.C1 + 1), R.nf);

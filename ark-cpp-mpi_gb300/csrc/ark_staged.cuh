@@ -860,8 +860,10 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
                     seam_put(X->a, s, e.qb, e.ab, e.bb, xc, true);
                     X->a[8][s] = uAo;
                     X->a[9][s] = uBo;
-                    if (i == 1) { // face 1: the ghost position 0 behind it (its own flags)
+                    if (i == 1) { // face 1: the ghost position 0 behind it (its own flags), the face's u1, p
                         X->b[7][s] = __int_as_float((int)flm[L::flag(ty - L::CROW0, cx - 1)]);
+                        X->a[10][s] = F(1, cx);
+                        X->a[11][s] = F(0, cx);
                         if (!px) // bounded: the inflow invariant, the values of cell 1 (xcell)
                             seam_put(X->b, s, (xc.fl & FL_LT) ? (T)1 : (T)0, (T)0, (T)0, xc, false);
                     }
@@ -873,6 +875,8 @@ __device__ __forceinline__ void phase1_tma_body(const DevState<float> &S, const 
                         X->a[7][s] = __int_as_float((int)flm[L::flag(ty - L::CROW0, cx + 1)]);
                         X->a[8][s] = F(2, cx + 1);
                         X->a[9][s] = F(3, cx + 1);
+                        X->a[10][s] = F(1, cx + 1);
+                        X->a[11][s] = F(0, cx + 1);
                         if (!px) // bounded: the outflow invariant, the values of cell C1 (xcell)
                             seam_put(X->a, s, (T)(5. / 6.), (T)0, (T)0, xc, false);
                     }

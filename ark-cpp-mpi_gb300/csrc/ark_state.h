@@ -299,14 +299,15 @@ struct HaloJob {
 // first column; C1 + 1 after the last tile) to the seam kernel, writing what its side of such a
 // face needs.  Per slot, b: the cell behind the face (its forward extrapolation rf, af, bf, its
 // half-step u1, u2, u3, ro and its flags), a: the cell ahead (qb, ab, bb, half-step u1, u2, u3,
-// ro, flags, and the face's old u2, u3).  The ghost positions' flags (and, on a bounded x axis,
+// ro, flags, and the face's old u2, u3; slots 0 and nb also its old u1 and p, so that the seam
+// kernel compares faces 1 and C1 + 1 from the seam arrays).  The ghost positions' flags (and, on a bounded x axis,
 // their edge invariants and the values of the cells they stand for) are written by the tiles
 // holding cells 1 and C1.  Slot (b, j, k) is element ((k - 1) * C2 + j - 1) * (nb + 1) + b of
 // each array, b = 0 .. nb = ceil(C1 / tw): the seams of a line side by side, as the seam kernel's
 // threads take them; seam_slots(g, 32) elements per array cover every tw.  Flags are stored as
 // the bits of a float.
 struct XSeams {
-    float *b[8], *a[10];
+    float *b[8], *a[12];
     int tw, n; // tile width; elements per array (bounds-checked builds)
     int kch;   // planes per block of the launch (the chunks whose first planes' z faces are left)
 };
